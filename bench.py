@@ -1,0 +1,336 @@
+#!/usr/bin/env python3
+"""Benchmark: adaptive SPH particle relaxation on one GB300.
+
+Workload (default): the inside of a torus (R = 1, r = 0.35) on three nested
+level-set grids, spacing 0.005..0.02 by the tanh law, ~1.0M particles,
+Wendland C2, h = 1.3 dx, FP32-split positions; synthetic and seeded (Philox,
+seed 0).  A step is one relaxation step (SPH_run_mesh_generation).
+
+Prints one JSON line.  `value` = relaxed particle-steps/s of the FP32-split
+path with the state resident in HBM (device-timed with CUDA events on the
+engine's stream); `e2e` = the same metric through the C ABI with host buffers
+(positions uploaded from pinned memory and downloaded every step); the FP64
+plain path, pair-interactions/s, a per-phase roofline and the CPU oracle
+(all host cores) are reported beside it.
+
+--impl reference times the CPU implementation of the path (the FP64 oracle,
+a restatement of the reference code; the reference itself does not build
+here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sph-mesh-generation_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "relaxed particle-steps/s & pair-interactions/s, batched FP32 vs FP64 plain"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mrsph", choices=["mrsph", "reference"])
+    ap.add_argument("--workload", default="torus_3d")
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name: str, precision: str):
+    from mrsph import cases
+    if name == "torus_3d":
+        return cases.torus_3d(precision=precision)
+    if name == "disc_hole_2d":
+        return cases.disc_hole_2d(precision=precision)
+    if name == "torus_3d_small":
+        return cases.torus_3d(dx_min=0.01, dx_max=0.04, precision=precision)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def config_of(case, name):
+    p = case.params
+    return {"workload": f"{name}: {case.name}, N={case.n_particles}", "n_particles": case.n_particles,
+            "dim": p["dim"], "kernel": "wendland_c2" if p["kernel"] == 2 else p["kernel"],
+            "h_over_dx": p["cell_ratio"] / p["cutoff"], "dx_range": [p["min_dl"], p["max_dl"]],
+            "levelset_levels": len(case.levels),
+            "levelset_cells": [int(lv.phi.size) for lv in case.levels],
+            "precision": "fp32_split", "l2": "working set (state + neighbour lists) larger than the 129 MB L2",
+            "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev: int):
+        self.lines = []
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={dev}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for ln in self.p.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+                pw.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, precision: str, dim: int):
+    """DRAM bytes per particle of a kernel from a committed ncu summary, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            d = json.load(f)
+        return d[f"{precision}_{dim}d"][kernel]["dram_bytes_per_particle"]
+    except Exception:
+        return None
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def max_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_oracle_run(case, steps: int):
+    """Time the FP64 oracle (OpenMP, all host threads) on the workload."""
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle(case)
+    t0 = time.perf_counter()
+    orc.seed(case.n_particles)
+    orc.pre_run()
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pairs = orc.steps(steps)
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "steps": steps, "pairs": pairs, "setup_s": setup, "threads": oracle.num_threads()}
+
+
+def run_reference(args, ws, rank, dist):
+    if rank != 0:
+        return
+    case = workload(args.workload, "fp32")
+    cfg = config_of(case, args.workload)
+    cfg["precision"] = "fp64 (CPU oracle)"
+    warm = min(args.warmup, 1)
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle(case)
+    orc.seed(case.n_particles)
+    orc.pre_run()
+    if warm:
+        orc.steps(warm)
+    # bounded sample: stop adding steps once ~120 s of CPU time is spent
+    t0 = time.perf_counter()
+    done, pairs = 0, 0
+    while done < args.steps:
+        pairs += orc.steps(1)
+        done += 1
+        if time.perf_counter() - t0 > 120.0:
+            break
+    dt = time.perf_counter() - t0
+    v = case.n_particles * done / dt
+    threads = oracle.num_threads()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg,
+            "pair_interactions_per_s": 3.0 * pairs / dt,
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{done} of {args.steps} relaxation steps of the full workload "
+                                       f"(N={case.n_particles}), FP64 oracle restating the reference, "
+                                       f"OpenMP on {threads} threads"},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_mrsph(args, ws, rank, local, dist):
+    import numpy as np
+    from mrsph import SPHMeshGeneration
+    from mrsph import build as mbuild
+    from mrsph import roofline
+    mbuild.build()
+    dev = local
+    case = workload(args.workload, "fp32")
+    n = case.n_particles
+    dim = case.params["dim"]
+    gpu = SPHMeshGeneration(case, precision="fp32", device=dev)
+    gpu.Initialize_case(n)
+    gpu.SPH_run_mesh_generation(max(args.warmup, 3))
+    gpu.sync()
+    prof = gpu.profile_steps(3)
+    st0 = gpu.stats()
+    gpu.sync()
+    barrier(dist)
+    clk = ClockSampler(dev)
+    ms = gpu.step_timed(args.steps)
+    clocks = clk.stop()
+    barrier(dist)
+    ms = max_over_ranks(ms, dist)
+    st1 = gpu.stats()
+    pairs = st1["pairs_total"] - st0["pairs_total"]
+    value = ws * n * args.steps / (ms / 1000.0)
+    pair_rate = ws * 3.0 * pairs / (ms / 1000.0)
+    ms_step = ms / args.steps
+
+    # roofline of the dominant phase (device-timed per phase, eager launches)
+    bytes_ = roofline.step_bytes(dim, "fp32", n, st1["num_cells"])
+    top = max(prof, key=prof.get)
+    peak, peak_kind = peaks()
+    ach = bytes_[top] / (prof[top] / 1000.0) / 1e9
+    step_ach = sum(bytes_.values()) / (ms_step / 1000.0) / 1e9
+    tr = ncu_traffic(top, "fp32", dim)
+    roof = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_kind": peak_kind,
+            "traffic": (tr * n if tr is not None else None),
+            "algorithmic_bytes_per_launch": bytes_[top],
+            "step_achieved": step_ach, "step_frac": step_ach / peak,
+            "step_bytes_per_particle": roofline.total_bytes_per_particle(dim, "fp32")}
+
+    # e2e through the C ABI with host buffers (pinned when torch is available)
+    try:
+        import torch
+        host_in = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        host_out = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        pinned = True
+    except Exception:
+        host_in = np.empty((n, 3))
+        host_out = np.empty((n, 3))
+        pinned = False
+    gpu.download_positions(host_in)
+    gpu.sync()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        gpu.upload_positions(host_in)
+        gpu.SPH_run_mesh_generation(1)
+        gpu.download_positions(host_out)
+        s = gpu.stats()
+        host_in, host_out = host_out, host_in
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = {"value": ws * n * args.e2e_steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out.nbytes) + 96,
+           "steps": args.e2e_steps, "pinned": pinned, "timer": "host wall clock, synchronised"}
+    flags = s["flags"]
+    gpu.close()
+
+    # FP64-plain path on the same workload
+    fp64 = None
+    if not args.no_fp64:
+        g64 = SPHMeshGeneration(case, precision="fp64", device=dev)
+        g64.Initialize_case(n)
+        g64.SPH_run_mesh_generation(1)
+        g64.sync()
+        ms64 = max_over_ranks(g64.step_timed(args.fp64_steps), dist)
+        v64 = ws * n * args.fp64_steps / (ms64 / 1000.0)
+        fp64 = {"value": v64, "unit": "particle-steps/s", "steps": args.fp64_steps, "ms_per_step": ms64 / args.fp64_steps}
+        g64.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        r = cpu_oracle_run(case, args.cpu_steps)
+        cpu = {"value": n * r["steps"] / r["seconds"], "unit": "particle-steps/s", "cores": r["threads"],
+               "kind": "port",
+               "sample": f"{r['steps']} relaxation step(s) of the full workload (N={n}) after seeding, FP64 "
+                         f"oracle (restatement of the reference, OpenMP {r['threads']} threads)"}
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(case, args.workload),
+            "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
+            "fp64_plain": fp64, "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
+            "phase_ms": prof, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": 12 * args.steps, "clocks": clocks, "device_flags": flags}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local, dist = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, dist)
+    else:
+        run_mrsph(args, ws, rank, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,220 @@
+/*
+ * mrsph_relax.h — C ABI of the GB300 relaxation engine (adaptive SPH particle
+ * relaxation driven by a level set, the data-parallel core of the SPH mesh
+ * generator Xiangyu-Hu/SPH-mesh-generation).
+ *
+ * The reference has no plugin or FFI layer: its hot path sits behind the C++
+ * class SPH_mesh_generation (src/sph_mesh_generation/sph_mesh_generation.h:10-154)
+ * and the per-particle methods of Particle_mesh_generation
+ * (src/sph_mesh_generation/particle_mesh_generation.h:78-120), called from
+ * Solver (src/solver.cpp:35-321).  Each entry point below names the reference
+ * member it replaces.
+ *
+ * Conventions: every function returns 0 on success or a negative MRSPH_ERR_*
+ * code; mrsph_last_error() gives the message.  No exception crosses the ABI.
+ * The library owns all device memory; results are copied into caller buffers
+ * (host memory, particle-id order).  One host thread per handle; handles are
+ * independent.  All pointers are plain host pointers.
+ */
+#ifndef MRSPH_RELAX_H
+#define MRSPH_RELAX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MRSPH_API_VERSION 1
+
+/* status codes */
+#define MRSPH_OK 0
+#define MRSPH_ERR_ARG (-1)     /* invalid argument */
+#define MRSPH_ERR_CUDA (-2)    /* CUDA runtime error */
+#define MRSPH_ERR_STATE (-3)   /* call out of order (e.g. no level set yet) */
+#define MRSPH_ERR_OOM (-4)     /* device allocation failed */
+#define MRSPH_ERR_RANGE (-5)   /* size beyond a documented limit */
+#define MRSPH_ERR_DEVICE (-6)  /* a device-side check failed (see stats.flags) */
+
+/* kernels (Makefile.in:36-40) */
+#define MRSPH_KERNEL_HYPERBOLIC 0
+#define MRSPH_KERNEL_CUBIC 1
+#define MRSPH_KERNEL_WENDLAND 2 /* the reference's _WINDLAND_C4_ (Wendland C2 form) */
+#define MRSPH_KERNEL_GAUSSIAN 3
+#define MRSPH_KERNEL_QUINTIC 4
+
+/* precision modes */
+#define MRSPH_FP64_PLAIN 0 /* absolute FP64 positions, FP64 arithmetic */
+#define MRSPH_FP32_SPLIT 1 /* int cell key + FP32 offset, FP32 arithmetic, FP64 reductions */
+
+/* particle types (glbparam.h:53-60) */
+#define MRSPH_REAL 0
+#define MRSPH_SURFACE 1
+#define MRSPH_SINGULARITY 2
+#define MRSPH_SEGMENT 3
+
+/* device-side flags reported in mrsph_stats.flags */
+#define MRSPH_FLAG_REMAP_EXHAUSTED 1 /* a re-seed loop hit its attempt limit */
+#define MRSPH_FLAG_SEED_EXHAUSTED 2  /* a seeding loop hit its attempt limit */
+#define MRSPH_FLAG_LEVEL_CLAMPED 4   /* a particle scale left the planned cell-list levels */
+#define MRSPH_FLAG_NEIGHBOR_SPILL 8  /* a neighbour list exceeded its capacity (handled by re-scan) */
+
+/* run_phase selectors (a step is MAP -> BIN -> DENSITY -> FORCE1 -> FORCE2) */
+#define MRSPH_PHASE_MAP 1
+#define MRSPH_PHASE_BIN 2
+#define MRSPH_PHASE_DENSITY 3
+#define MRSPH_PHASE_FORCE1 4
+#define MRSPH_PHASE_FORCE2 5
+
+typedef struct mrsph_handle mrsph_handle;
+
+/* Run parameters.  Replaces the compile-time flags of Makefile.in:14-195 and
+ * the constants hard-coded in SPH_mesh_generation::SPH_mesh_generation /
+ * Initialize_case (sph_mesh_generation.cpp:8-152, 680-712). */
+typedef struct {
+  int dim;              /* 2 or 3 */
+  int kernel;           /* MRSPH_KERNEL_* */
+  int precision;        /* MRSPH_FP64_PLAIN or MRSPH_FP32_SPLIT */
+  double cell_ratio;    /* CELL_RATIO: h = scale*cell_ratio/cutoff (glbparam.h:171-183) */
+  double cutoff;        /* CUT_OFF (2.0) */
+  double angle_thres;   /* surface-neighbour angle threshold, rad (reference 0.4*PI) */
+  double nu_coeff;      /* artificial viscosity coefficient (reference 0.1) */
+  double damp_coeff;    /* velocity damping (reference 0) */
+  double min_dl;        /* minimum target spacing (Levelset::minimum_dl) */
+  double max_dl;        /* maximum target spacing (Levelset::maximum_dl) */
+  double box_l[3];      /* domain (SPH::box_l, box_r) = level-set level-0 interior box */
+  double box_r[3];
+  unsigned long long seed; /* Philox4x32-10 key for seeding and re-seeding */
+  int neighbor_cap;     /* neighbour-list capacity per particle; 0 = automatic */
+  int device;           /* CUDA device ordinal */
+} mrsph_params;
+
+/* One level of a (possibly nested) level set: packages of 4^D cells covering
+ * [box_l, box_l + num_pkg*dpkg) plus `margin` packages on every side
+ * (Levelset_levelinfo::Initialize, lset_level_infor.cpp:17-117).  phi holds
+ * cell-centred values incl. margins, x fastest, positive inside the body.
+ * active (optional, one byte per package incl. margins, x fastest) marks the
+ * packages a finer nested level covers; NULL = all packages active. */
+typedef struct {
+  double box_l[3];
+  double dpkg[3];
+  int num_pkg[3];
+  int margin;
+  const double* phi;
+  const unsigned char* active;
+} mrsph_levelset_level;
+
+typedef struct {
+  double dt;          /* glbl_timestep after the last step (stage 2) */
+  double dt_stage1;   /* glbl_timestep of stage 1 of the last step */
+  double max_v;       /* glbl_max_v of the last step (stage 2) */
+  long long step;     /* completed relaxation steps */
+  long long n;        /* particles */
+  long long n_surface;/* SURFACE particles after the last map phase */
+  long long pairs;    /* ordered neighbour pairs i != j of the last step */
+  long long remapped; /* REAL particles re-seeded into phi > h by the last map phase */
+  long long pairs_total; /* ordered neighbour pairs summed over all steps since seeding */
+  int flags;          /* MRSPH_FLAG_* accumulated since the last mrsph_get_stats */
+  int num_cell_levels;/* cell-list levels in use */
+  long long num_cells;/* cell-list cells over all levels */
+  double max_phi;     /* maximum phi of the level set (Levelset::maximum_phi) */
+} mrsph_stats;
+
+/* Host views for particle taps, particle-id order; any pointer may be NULL.
+ * Vectors are n x 3 (z = 0 in 2D). */
+typedef struct {
+  double* xyz;
+  double* v;
+  int* type;
+  double* h;
+  int* level;   /* cell-list level (0 = coarsest) */
+  double* phi;
+  double* curv;
+  double* norm;
+  double* sum;  /* inverse kernel sum of the last density phase */
+  double* rho;
+  double* nu;
+  double* a1;   /* stage-1 acceleration of the last step */
+  double* a2;   /* stage-2 acceleration of the last step */
+} mrsph_particle_view;
+
+/* State injection for parity runs (particle-id order).  v, nu, h may be NULL
+ * (zero); level NULL = coarsest level (Particle_mesh_generation::Initialize). */
+typedef struct {
+  const double* xyz;
+  const double* v;
+  const int* type;
+  const double* h;
+  const int* level;
+  const double* nu;
+  double dt;          /* glbl_timestep used by the next advection */
+  long long step;     /* completed steps (drives the re-seed random stream) */
+} mrsph_state_in;
+
+int mrsph_version(void);
+
+/* SPH_mesh_generation constructor + Define_level_infor_tight (sph.cpp:144-180). */
+int mrsph_create(const mrsph_params* params, mrsph_handle** out);
+int mrsph_destroy(mrsph_handle* h);
+/* Last error message of the handle (or of the last failed mrsph_create when h is NULL). */
+int mrsph_last_error(mrsph_handle* h, char* buf, size_t len);
+
+/* Levelset::Initialize + Calculate_level_set (level_set.cpp:51-88, 238-307):
+ * copies phi to the device and builds normals, cut-cell tags, curvature and
+ * maximum phi there.  nlevels <= 4, finest last. */
+int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level* levels);
+/* Tap: the device-built fields of one level (arrays sized like phi; NULL skips). */
+int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, double* nz, double* curv,
+                       unsigned char* tag, double* max_phi);
+/* Levelset::Get_phi_at_position / Calculate_particle_infor (level_set.cpp:372-436,
+ * particle_mesh_generation.cpp:175-265) at n host points (xyz n x 3). */
+int mrsph_sample_levelset(mrsph_handle* h, long long n, const double* xyz, double* phi, double* norm,
+                          double* curv, int* tag);
+
+/* Random_particle_distribution (sph_mesh_generation.cpp:1302-1367) + Pre_run
+ * (:1010-1050): n particles seeded where phi > h. */
+int mrsph_seed(mrsph_handle* h, long long n);
+/* Parity entry: particles from given positions (e.g. a reference .pst file),
+ * optionally with full state; runs Pre_run when pre_run != 0. */
+int mrsph_set_state(mrsph_handle* h, long long n, const mrsph_state_in* st, int pre_run);
+
+/* SPH_run_mesh_generation x nsteps (sph_mesh_generation.cpp:1371-1463),
+ * asynchronous on the handle's stream, CUDA-graph replayed. */
+int mrsph_step(mrsph_handle* h, int nsteps);
+/* One step up to and including `phase` (MRSPH_PHASE_*), for phase-by-phase parity. */
+int mrsph_run_phase(mrsph_handle* h, int phase);
+int mrsph_sync(mrsph_handle* h);
+/* mrsph_step timed on the device: CUDA events recorded on the handle's stream
+ * around the graph launches; *ms = elapsed device milliseconds (synchronises). */
+int mrsph_step_timed(mrsph_handle* h, int nsteps, double* ms);
+/* Per-phase device time of nsteps eagerly launched steps (the reference's
+ * time_for_* timers, sph_mesh_generation.cpp:1373-1454).  phase_ms[k] receives
+ * the mean milliseconds per step of phase k (MRSPH_TIMER_*), nphase <= 8. */
+#define MRSPH_TIMER_MAP 0     /* begin + advect/sample/map/spacing/key */
+#define MRSPH_TIMER_SCAN 1    /* cell histogram scan */
+#define MRSPH_TIMER_SORT 2    /* scatter + in-cell rank */
+#define MRSPH_TIMER_REORDER 3
+#define MRSPH_TIMER_DENSITY 4 /* neighbour search + kernel sum */
+#define MRSPH_TIMER_FORCE1 5
+#define MRSPH_TIMER_FORCE2 6
+#define MRSPH_NUM_TIMERS 7
+int mrsph_profile_steps(mrsph_handle* h, int nsteps, double* phase_ms, int nphase);
+
+int mrsph_get_stats(mrsph_handle* h, mrsph_stats* out);
+int mrsph_get_particles(mrsph_handle* h, const mrsph_particle_view* view);
+/* Cell binning tap: per particle (id order) level, cx, cy, cz (n x 4 ints);
+ * sorted_ids (n ints) = particle ids in device storage order (cells grouped,
+ * ascending id inside a cell).  Either pointer may be NULL. */
+int mrsph_get_cells(mrsph_handle* h, int* level_cell, int* sorted_ids);
+/* Neighbour lists of the last density phase in CSR form, particle-id order,
+ * neighbour ids ascending.  Call with nb == NULL to get *total only. */
+int mrsph_get_neighbors(mrsph_handle* h, long long* offsets, int* nb, long long cap, long long* total);
+
+/* e2e helpers: positions in id order (n x 3), host memory (pinned or not). */
+int mrsph_upload_positions(mrsph_handle* h, const double* xyz);
+int mrsph_download_positions(mrsph_handle* h, double* xyz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MRSPH_RELAX_H */

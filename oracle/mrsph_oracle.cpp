@@ -1,0 +1,1156 @@
+// mrsph_oracle.cpp — CPU FP64 restatement of the reference relaxation path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the parity checker and the timed CPU
+// baseline.  Only tests/, __graft_entry__.smoke() and bench.py (its CPU
+// baseline and reference arms) may load it.  The product library
+// (sph-mesh-generation_gb300/csrc) never links or calls it.
+//
+// Parity status: UNPINNED against the reference binary.  The reference
+// (Xiangyu-Hu/SPH-mesh-generation) needs TBB, Boost.MPI/Graph/Serialization
+// and voro++ to build, none of which exist here, and it ships no tests, golden
+// vectors or fixtures.  This restatement is pinned instead by analytic
+// known-answer tests (kernel normalisation, zero gradient sum on a lattice,
+// exact bilinear interpolation of linear phi, projection onto phi = 0,
+// spacing-law endpoints) in tests/test_oracle_kat.py.
+//
+// Every function cites the reference file:line it restates (paths relative to
+// the reference's src/).  Arithmetic is FP64 and follows the reference's
+// expression order; build with -ffp-contract=off so no multiply-add is fused.
+// Deterministic order: each neighbour list is sorted by particle id before any
+// summation.  Reference build flags restated: _MESH_GENERATION_, _DOUBLE_,
+// _NON_PERI_, _NON_SYM_ (symmetric-mirror ghosts off), one rank.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const double PI_REF = 3.1415926;  // glbparam.h:186 (#define PI 3.1415926)
+
+enum { REAL_PARTICLE = 0, SURFACE_PARTICLE = 1, SINGULARITY_PARTICLE = 2, SEGMENT_PARTICLE = 3 };
+enum { NORMAL_CELL = 0, CUT_CELL = 1 };
+enum { K_HYPERBOLIC = 0, K_CUBIC = 1, K_WENDLAND = 2, K_GAUSSIAN = 3, K_QUINTIC = 4 };
+
+// glbfunc.h:42-53
+inline double powern(double a, int n) {
+  double res = 1;
+  for (int i = 0; i < n; i++) res *= a;
+  return res;
+}
+inline double AMAX1(double a, double b) { return a >= b ? a : b; }  // glbfunc.h:56
+inline double AMIN1(double a, double b) { return a <= b ? a : b; }  // glbfunc.h:61
+inline int IMAX1(int a, int b) { return a >= b ? a : b; }
+inline int IMIN1(int a, int b) { return a <= b ? a : b; }
+inline int signum(double x) { return (0.0 < x) - (x < 0.0); }  // glbfunc.h:35-39
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), written from the paper.
+// Replaces the reference's srand(time)/rand() seeding (reference quirk Q5).
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t v[4]; };
+inline U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t seed) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; r++) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  U4 o; o.v[0] = c0; o.v[1] = c1; o.v[2] = c2; o.v[3] = c3; return o;
+}
+inline double u53(uint32_t a, uint32_t b) {
+  return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+enum { RNG_SEED = 1, RNG_REMAP = 2 };
+
+// ---------------------------------------------------------------------------
+// SPH kernels: particle.cpp:31-807.  D is the kernel dimension (1, 2, 3).
+// W  = Kernel_function{,_1D,_2D,_3D}
+// dW = Derivative_kernel_function{,_1D,_2D,_3D} (already divided by dist)
+// ---------------------------------------------------------------------------
+double kernel_W(int kind, int D, double dist, double h) {
+  double s = dist / h, C = 0.0, val = 0.0;
+  switch (kind) {
+    case K_HYPERBOLIC:  // particle.cpp:33-46, 112-125, 201-214, 290-306
+      if (D == 1) C = 1.0 / 7.0 / powern(h, 1);
+      else if (D == 2) C = 1.0 / (3.0 * PI_REF) / powern(h, 2);
+      else C = 15.0 / (62.0 * PI_REF) / powern(h, 3);
+      if (s < 1) val = C * (6.0 - 6.0 * s + s * s * s);
+      else if (s < 2) val = C * (2 - s) * (2 - s) * (2 - s);
+      return val;
+    case K_CUBIC:  // particle.cpp:48-63, 127-142, 216-231, 308-330
+      if (D == 1) C = 0.666666667 / powern(h, 1);
+      else if (D == 2) C = 0.454728408 / powern(h, 2);
+      else C = 0.318309886 / powern(h, 3);
+      if (s < 1) val = C * (1 - 1.5 * s * s + 0.75 * s * s * s);
+      else if (s < 2) val = C / 4.0 * (2 - s) * (2 - s) * (2 - s);
+      return val;
+    case K_WENDLAND:  // particle.cpp:65-69 (1D unsupported, Q2), 144-157, 233-246, 332-348
+      if (D == 1) return 0.0;
+      if (D == 2) C = 1.0 / PI_REF / powern(h, 2) * 7. / 4.;
+      else C = 1.0 / PI_REF / powern(h, 3) * 21. / 16.;
+      if (s < 2) val = C * powern((1. - 0.5 * s), 4) * (1. + 2. * s);
+      return val;
+    case K_GAUSSIAN: {  // particle.cpp:71-87, 159-176, 248-265, 350-376
+      double fac = 0.5 * 2 / std::sqrt(PI_REF);
+      if (D > 1) fac *= 0.5 * 2 / std::sqrt(PI_REF);
+      if (D > 2) fac *= 0.5 * 2 / std::sqrt(PI_REF);
+      if (D == 1) C = fac / h;
+      else C = fac / powern(h, D);
+      if (s < 3) val = std::exp(-1. * s * s) * C;
+      return val;
+    }
+    case K_QUINTIC:  // particle.cpp:89-106, 178-195, 267-284, 378-400
+      if (D == 1) C = 1.0 / 120. / powern(h, 1);
+      else if (D == 2) C = 1.0 / PI_REF * 7. / 478. / powern(h, 2);
+      else C = 1.0 / PI_REF * 3. / 359. / powern(h, 3);
+      if (s < 1) val = C * (powern((3. - s), 5) - 6. * powern((2. - s), 5) + 15. * powern((1. - s), 5));
+      else if (s < 2) val = C * (powern((3. - s), 5) - 6. * powern((2. - s), 5));
+      else if (s < 3) val = C * (powern((3. - s), 5));
+      return val;
+  }
+  return 0.0;
+}
+
+double kernel_dW(int kind, int D, double dist, double h) {
+  double s = dist / h, C = 0.0, val = 0.0;
+  switch (kind) {
+    case K_HYPERBOLIC:  // particle.cpp:405-420, 491-506, 588-603, 686-706
+      if (D == 1) C = 1.0 / 7.0 / powern(h, 2);
+      else if (D == 2) C = 1.0 / (3.0 * PI_REF) / powern(h, 3);
+      else C = 15.0 / (62.0 * PI_REF) / powern(h, 4);
+      if (s < 1) val = C * (-6.0 + 3. * s * s);
+      else if (s < 2) val = C * (-3.0) * (2 - s) * (2 - s);
+      val /= (dist + 1.e-20);
+      return val;
+    case K_CUBIC:  // particle.cpp:422-439, 508-525, 605-622, 708-730
+      if (D == 1) C = 0.666666667 / powern(h, 2);
+      else if (D == 2) C = 0.454728408 / powern(h, 3);
+      else C = 0.318309886 / powern(h, 4);
+      if (s < 1) val = 3 * C * (-s + 3 * (s * s) / 4);
+      else if (s < 2) val = -3 / 4.0 * C * (2 - s) * (2 - s);
+      val /= (dist + 1.e-20);
+      return val;
+    case K_WENDLAND:  // particle.cpp:441-444 (1D: 0, Q2), 527-540, 624-637, 732-748
+      if (D == 1) return 0.0;
+      if (D == 2) C = 1.0 / PI_REF / powern(h, 2) * 7. / 4.;
+      else C = 1.0 / PI_REF / powern(h, 3) * 21. / 16.;
+      if (s < 2) val = -5. * C * powern((1. - 0.5 * s), 3) * s / h / (dist + 1.e-15);
+      return val;
+    case K_GAUSSIAN: {  // particle.cpp:446-463, 542-560, 639-658, 750-776
+      double fac = 0.5 * 2 / std::sqrt(PI_REF);
+      if (D > 1) fac *= 0.5 * 2 / std::sqrt(PI_REF);
+      if (D > 2) fac *= 0.5 * 2 / std::sqrt(PI_REF);
+      if (D == 1) C = fac / h;
+      else C = fac / powern(h, D);
+      if (s < 3) val = -2. * s * std::exp(-1. * s * s) * C / h / (dist + 1.e-15);
+      return val;
+    }
+    case K_QUINTIC:  // particle.cpp:465-488, 562-585, 660-683, 778-807
+      if (D == 1) C = 1.0 / 120. / powern(h, 1);
+      else if (D == 2) C = 1.0 / PI_REF * 7. / 478. / powern(h, 2);
+      else C = 1.0 / PI_REF * 3. / 359. / powern(h, 3);
+      if (s < 1) {
+        val = C * (-5. * powern((3. - s), 4) + 30. * powern((2. - s), 4) - 75. * powern((1. - s), 4));
+        val = val / h / (dist + 1.e-15);
+      } else if (s < 2) {
+        val = C * (-5. * powern((3. - s), 4) + 30. * powern((2. - s), 4));
+        val = val / h / (dist + 1.e-15);
+      } else if (s < 3) {
+        val = C * (-5. * powern((3. - s), 4));
+        val = val / h / (dist + 1.e-15);
+      }
+      return val;
+  }
+  return 0.0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C interface (ctypes).  Structures mirrored in oracle/oracle.py.
+// ===========================================================================
+extern "C" {
+
+struct orc_level {
+  // One level-set level: a dense cell-centred grid of packages of 4^D cells
+  // with `margin` packages on every side (lset_level_infor.cpp:17-85).
+  double box_l[3];  // corner of interior package (0,0,0)
+  double dpkg[3];   // package size (cell size = dpkg/4)
+  int num_pkg[3];   // interior packages per axis
+  int margin;       // margin packages per side
+  double* phi;      // [ntot] input
+  double* nx;       // [ntot] output of orc_ls_build
+  double* ny;
+  double* nz;
+  double* curv;
+  int* tag;         // tag_interface: NORMAL_CELL / CUT_CELL
+  const uint8_t* active;  // per package incl. margins (NULL = all active)
+};
+
+struct orc_ctx {
+  int dim, kernel;
+  double cell_ratio;   // glbparam.h:171-183 CELL_RATIO (h = scale*cell_ratio/cutoff)
+  double cutoff;       // CUT_OFF
+  double angle_thres;  // sph_mesh_generation.cpp:689 (PI*0.4)
+  double nu_coeff;     // sph_mesh_generation.cpp:691-694
+  double damp_coeff;   // sph_mesh_generation.cpp:696-699
+  double min_dl, max_dl, max_phi;
+  double box_l[3], box_r[3];
+  unsigned long long seed;
+  int nls;
+  orc_level* ls;
+  // cell-list levels, filled by orc_define_levels (sph.cpp:144-180, level_infor.cpp:35-110)
+  int ncl;
+  double max_scale, min_scale;
+  int ini_num_cell[3];
+  double cl_dcell[16][3];
+  int cl_ncell[16][3];
+  double cl_scale[16];
+};
+
+struct orc_state {
+  long long n;
+  double *x, *y, *z, *vx, *vy, *vz;
+  int *type, *id, *level;
+  double *h, *scale, *phi, *curv, *nx, *ny, *nz, *sum, *rho, *vol, *nu;
+  double *ax, *ay, *az;  // acceleration of the last force stage
+  double dt;             // glbl_timestep
+  double max_v;          // glbl_max_v
+  long long step;        // run_time counter (RNG stream)
+  long long remapped;    // particles re-seeded by the last map phase
+};
+
+}  // extern "C"
+
+namespace {
+
+inline int ls_ncell(const orc_level& L, int d) { return (L.num_pkg[d] + 2 * L.margin) * 4; }
+inline long long ls_index(const orc_level& L, int D, int gi, int gj, int gk) {
+  // global cell index g in [-4*margin, 4*(num_pkg+margin)) -> array index
+  long long a0 = gi + 4 * L.margin, a1 = gj + 4 * L.margin, a2 = (D == 3) ? gk + 4 * L.margin : 0;
+  long long n0 = ls_ncell(L, 0), n1 = ls_ncell(L, 1);
+  return (a2 * n1 + a1) * n0 + a0;
+}
+
+// level-set cell size along d
+inline double ls_dcell(const orc_level& L, int d) { return L.dpkg[d] / 4.0; }
+inline double ls_dl(const orc_level& L, int D) {  // lset_level_infor.cpp:48-51
+  double dl = 1.e20;
+  for (int d = 0; d < D; d++) dl = AMIN1(ls_dcell(L, d), dl);
+  return dl;
+}
+
+// ---------------------------------------------------------------------------
+// A15 level-set grid build: lset_package.cpp:332-356 (Get_normal),
+// :359-390 (Get_BC_normal), :450-470 (Get_interface_tag),
+// :664-762 (Is_cut_cell / Get_phi_at_corners), :393-434 (Get_curvature),
+// :765-786 (Get_global_scale -> maximum_phi).
+// Interior packages get central-difference normals, tags and curvature;
+// margin packages get one-sided in-package normals, NORMAL_CELL, curv 0.
+// ---------------------------------------------------------------------------
+template <int D>
+void ls_build(orc_level& L, double* max_phi) {
+  const int n0 = ls_ncell(L, 0), n1 = ls_ncell(L, 1), n2 = (D == 3) ? ls_ncell(L, 2) : 1;
+  const int m4 = 4 * L.margin;
+  double dc[3] = {ls_dcell(L, 0), ls_dcell(L, 1), (D == 3) ? ls_dcell(L, 2) : 1.0};
+  auto P = [&](int gi, int gj, int gk) { return L.phi[ls_index(L, D, gi, gj, gk)]; };
+  auto interior = [&](int gi, int gj, int gk) {
+    bool in = gi >= 0 && gi < 4 * L.num_pkg[0] && gj >= 0 && gj < 4 * L.num_pkg[1];
+    if (D == 3) in = in && gk >= 0 && gk < 4 * L.num_pkg[2];
+    return in;
+  };
+  long long ntot = (long long)n0 * n1 * n2;
+  for (long long a = 0; a < ntot; a++) { L.tag[a] = NORMAL_CELL; L.curv[a] = 0.0; }
+  // normals
+#pragma omp parallel for schedule(static)
+  for (int ak = 0; ak < n2; ak++)
+    for (int aj = 0; aj < n1; aj++)
+      for (int ai = 0; ai < n0; ai++) {
+        int gi = ai - m4, gj = aj - m4, gk = (D == 3) ? ak - m4 : 0;
+        double g[3] = {0, 0, 0};
+        if (interior(gi, gj, gk)) {
+          g[0] = 0.5 * (P(gi + 1, gj, gk) - P(gi - 1, gj, gk)) / dc[0];
+          g[1] = 0.5 * (P(gi, gj + 1, gk) - P(gi, gj - 1, gk)) / dc[1];
+          if (D == 3) g[2] = 0.5 * (P(gi, gj, gk + 1) - P(gi, gj, gk - 1)) / dc[2];
+        } else {
+          int gg[3] = {gi, gj, gk};
+          for (int d = 0; d < D; d++) {
+            int loc = ((gg[d] % 4) + 4) % 4;  // cell index inside its package
+            int e[3] = {0, 0, 0};
+            e[d] = 1;
+            if (loc == 0)
+              g[d] = (P(gi + e[0], gj + e[1], gk + e[2]) - P(gi, gj, gk)) / dc[d];
+            else if (loc == 3)
+              g[d] = (P(gi, gj, gk) - P(gi - e[0], gj - e[1], gk - e[2])) / dc[d];
+            else
+              g[d] = 0.5 * (P(gi + e[0], gj + e[1], gk + e[2]) - P(gi - e[0], gj - e[1], gk - e[2])) / dc[d];
+          }
+        }
+        double dist = 0.0;
+        dist += g[0] * g[0];
+        dist += g[1] * g[1];
+        if (D == 3) dist += g[2] * g[2];
+        dist = std::sqrt(dist) + 1.e-12;
+        double inv = 1. / dist;
+        long long a = ls_index(L, D, gi, gj, gk);
+        L.nx[a] = g[0] * inv;
+        L.ny[a] = g[1] * inv;
+        L.nz[a] = (D == 3) ? g[2] * inv : 0.0;
+      }
+  // cut-cell tags (interior only)
+#pragma omp parallel for schedule(static)
+  for (int gk = 0; gk < ((D == 3) ? 4 * L.num_pkg[2] : 1); gk++)
+    for (int gj = 0; gj < 4 * L.num_pkg[1]; gj++)
+      for (int gi = 0; gi < 4 * L.num_pkg[0]; gi++) {
+        int ip = gi + 1, im = gi - 1, jp = gj + 1, jm = gj - 1;
+        int kp = (D == 3) ? gk + 1 : 0, km = (D == 3) ? gk - 1 : 0;
+        double v[3][3][3];
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++)
+            for (int c = 0; c < 3; c++) {
+              int ii = (a == 0) ? im : (a == 1 ? gi : ip);
+              int jj = (b == 0) ? jm : (b == 1 ? gj : jp);
+              int kk = (c == 0) ? km : (c == 1 ? gk : kp);
+              v[a][b][c] = P(ii, jj, kk);
+            }
+        // corner vectors in the order of lset_package.cpp:726-733; index 0=m,1=centre,2=p
+        const int cv[8][8][3] = {
+            {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}},
+            {{0, 0, 2}, {1, 0, 2}, {0, 1, 2}, {1, 1, 2}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}},
+            {{1, 0, 2}, {2, 0, 2}, {1, 1, 2}, {2, 1, 2}, {1, 0, 1}, {2, 0, 1}, {1, 1, 1}, {2, 1, 1}},
+            {{1, 0, 0}, {2, 0, 0}, {1, 1, 0}, {2, 1, 0}, {1, 0, 1}, {2, 0, 1}, {1, 1, 1}, {2, 1, 1}},
+            {{0, 2, 0}, {1, 2, 0}, {0, 1, 0}, {1, 1, 0}, {0, 2, 1}, {1, 2, 1}, {0, 1, 1}, {1, 1, 1}},
+            {{0, 2, 2}, {1, 2, 2}, {0, 1, 2}, {1, 1, 2}, {0, 2, 1}, {1, 2, 1}, {0, 1, 1}, {1, 1, 1}},
+            {{1, 2, 2}, {2, 2, 2}, {1, 1, 2}, {2, 1, 2}, {1, 2, 1}, {2, 2, 1}, {1, 1, 1}, {2, 1, 1}},
+            {{1, 2, 0}, {2, 2, 0}, {1, 1, 0}, {2, 1, 0}, {1, 2, 1}, {2, 2, 1}, {1, 1, 1}, {2, 1, 1}}};
+        double corner[8];
+        for (int u = 0; u < 8; u++) {
+          double w[8];
+          for (int q = 0; q < 8; q++) {
+            int a = cv[u][q][0], b = cv[u][q][1], c = cv[u][q][2];
+            if (D == 2) c = 1;  // kp = km = k in 2D (lset_package.cpp:673-676)
+            w[q] = v[a][b][c];
+          }
+          std::sort(w, w + 8);
+          double s = 0.0;
+          for (int q = 0; q < 8; q++) s += w[q];
+          corner[u] = s * 0.125;
+        }
+        bool cut = false;
+        for (int c = 0; c < 8; c++)
+          if (signum(corner[c]) != signum(corner[0])) cut = true;
+        if (signum(v[1][1][1]) != signum(corner[0])) cut = true;
+        L.tag[ls_index(L, D, gi, gj, gk)] = cut ? CUT_CELL : NORMAL_CELL;
+      }
+  // curvature for cut cells (interior only)
+  double cdist = 0.0;
+  for (int d = 0; d < D; d++) cdist += dc[d] * dc[d];
+  cdist = std::sqrt(cdist);
+  double mphi = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : mphi)
+  for (int gk = 0; gk < ((D == 3) ? 4 * L.num_pkg[2] : 1); gk++)
+    for (int gj = 0; gj < 4 * L.num_pkg[1]; gj++)
+      for (int gi = 0; gi < 4 * L.num_pkg[0]; gi++) {
+        long long a = ls_index(L, D, gi, gj, gk);
+        double p0 = L.phi[a];
+        if (p0 > 0.) mphi = AMAX1(mphi, std::fabs(p0));
+        if (L.tag[a] != CUT_CELL) continue;
+        double px = 0, py = 0, pz = 0, pxx = 0, pyy = 0, pzz = 0, pxy = 0, pyz = 0, pxz = 0;
+        int i = gi, j = gj, k = gk;
+        px = (8.0 * (P(i + 1, j, k) - P(i - 1, j, k)) - (P(i + 2, j, k) - P(i - 2, j, k))) / dc[0] / 12.0;
+        pxx = (P(i + 1, j, k) - 2 * P(i, j, k) + P(i - 1, j, k)) / dc[0] / dc[0];
+        py = (8.0 * (P(i, j + 1, k) - P(i, j - 1, k)) - (P(i, j + 2, k) - P(i, j - 2, k))) / dc[1] / 12.0;
+        pyy = (P(i, j + 1, k) - 2 * P(i, j, k) + P(i, j - 1, k)) / dc[1] / dc[1];
+        if (D == 3) {
+          pz = (8.0 * (P(i, j, k + 1) - P(i, j, k - 1)) - (P(i, j, k + 2) - P(i, j, k - 2))) / dc[2] / 12.0;
+          pzz = (P(i, j, k + 1) - 2 * P(i, j, k) + P(i, j, k - 1)) / dc[2] / dc[2];
+        }
+        pxy = 0.25 * (P(i + 1, j + 1, k) - P(i - 1, j + 1, k) - P(i + 1, j - 1, k) + P(i - 1, j - 1, k)) / dc[0] / dc[1];
+        if (D == 3) {
+          pxz = 0.25 * (P(i + 1, j, k + 1) - P(i - 1, j, k + 1) - P(i + 1, j, k - 1) + P(i - 1, j, k - 1)) / dc[0] / dc[2];
+          pyz = 0.25 * (P(i, j + 1, k + 1) - P(i, j + 1, k - 1) - P(i, j - 1, k + 1) + P(i, j - 1, k - 1)) / dc[1] / dc[2];
+        }
+        double c = (px * px * pyy - 2 * px * py * pxy + py * py * pxx + px * px * pzz - 2 * px * pz * pxz +
+                    pz * pz * pxx + py * py * pzz - 2 * py * pz * pyz + pz * pz * pyy) /
+                   std::pow(px * px + py * py + pz * pz, (double)1.5);
+        L.curv[a] = std::fabs(AMIN1(AMAX1(c, -2. / cdist), 2. / cdist));
+      }
+  *max_phi = mphi;
+}
+
+// ---------------------------------------------------------------------------
+// Nested level choice (build extension for reference quirk Q9: the reference
+// has one level-set level).  The finest level whose interior box contains the
+// point and whose package there is active is used; level 0 otherwise.
+// ---------------------------------------------------------------------------
+template <int D>
+int ls_pick(const orc_ctx& c, const double* x) {
+  for (int l = c.nls - 1; l >= 1; l--) {
+    const orc_level& L = c.ls[l];
+    int pk[3] = {0, 0, 0};
+    bool inside = true;
+    for (int d = 0; d < D; d++) {
+      double cs = x[d] - L.box_l[d];
+      double dom = L.dpkg[d] * L.num_pkg[d];
+      if (!(cs >= 0.0 && cs < dom)) { inside = false; break; }
+      pk[d] = (int)std::floor(cs / L.dpkg[d]);
+      if (pk[d] < 0 || pk[d] >= L.num_pkg[d]) { inside = false; break; }
+    }
+    if (!inside) continue;
+    if (L.active) {
+      long long np0 = L.num_pkg[0] + 2 * L.margin, np1 = L.num_pkg[1] + 2 * L.margin;
+      long long pidx = ((long long)((D == 3) ? pk[2] + L.margin : 0) * np1 + (pk[1] + L.margin)) * np0 + (pk[0] + L.margin);
+      if (!L.active[pidx]) continue;
+    }
+    return l;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// A2: Calculate_particle_infor, particle_mesh_generation.cpp:175-265.
+// Bilinear/trilinear interpolation of phi, n, curv.  The final normal
+// "renormalisation" discards its result in the reference (Q1), so n stays the
+// raw interpolated normal.
+// ---------------------------------------------------------------------------
+template <int D>
+void sample(const orc_ctx& c, const double* x, double* phi, double* n, double* curv) {
+  const orc_level& L = c.ls[ls_pick<D>(c, x)];
+  double cs[3] = {0, 0, 0};
+  int pos[3] = {0, 0, 0};
+  double rr[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+  int im[3] = {0, 0, 0};
+  const double ICP = 4.0;
+  for (int d = 0; d < D; d++) {
+    double dom = L.dpkg[d] * L.num_pkg[d];
+    cs[d] = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
+    // get_cell_id, glbfunc.h:196-208 (clamped to the package range incl. margins)
+    int p = (int)std::floor(cs[d] / L.dpkg[d]);
+    pos[d] = IMAX1(-L.margin, IMIN1(p, L.num_pkg[d] + L.margin - 1));
+    double csp = cs[d] - L.dpkg[d] * pos[d];
+    rr[d] = csp / ls_dcell(L, d) - 0.5;
+    rr[d] = AMAX1(-0.5, AMIN1(rr[d], ICP - 0.5));
+    im[d] = (int)std::floor(rr[d]);
+    w[d] = rr[d] - (double)im[d];
+  }
+  double ph = 0., n0 = 0., n1 = 0., n2 = 0., cv = 0.;
+  for (int r = 0; r <= 1; r++)
+    for (int s = 0; s <= 1; s++)
+      for (int t = 0; t <= (D == 3 ? 1 : 0); t++) {
+        int gi = pos[0] * 4 + im[0] + r, gj = pos[1] * 4 + im[1] + s;
+        int gk = (D == 3) ? pos[2] * 4 + im[2] + t : 0;
+        long long a = ls_index(L, D, gi, gj, gk);
+        double coef = std::fabs(w[0] - (1.0 - r)) * std::fabs(w[1] - (1.0 - s)) *
+                      ((D == 3) ? std::fabs(w[2] - (1.0 - t)) : 1.0);
+        ph += L.phi[a] * coef;
+        n0 += L.nx[a] * coef;
+        n1 += L.ny[a] * coef;
+        n2 += L.nz[a] * coef;
+        cv += L.curv[a] * coef;
+      }
+  *phi = ph;
+  n[0] = n0; n[1] = n1; n[2] = (D == 3) ? n2 : 0.0;
+  *curv = cv;
+}
+
+// Get_level_set_char_cell_tag_and_idx, particle_mesh_generation.cpp:552-573,
+// via Levelset_levelinfo::Get_id_pkg_cell, lset_level_infor.cpp:350-366.
+template <int D>
+int cell_tag(const orc_ctx& c, const double* x) {
+  const orc_level& L = c.ls[ls_pick<D>(c, x)];
+  int g[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    double dom = L.dpkg[d] * L.num_pkg[d];
+    double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
+    int p = (int)std::floor(cs / L.dpkg[d]);
+    p = IMAX1(-L.margin, IMIN1(p, L.num_pkg[d] + L.margin - 1));
+    double csp = cs - L.dpkg[d] * p;
+    int ci = (int)std::floor(csp / ls_dcell(L, d));
+    ci = IMAX1(0, IMIN1(ci, 3));
+    g[d] = p * 4 + ci;
+  }
+  return L.tag[ls_index(L, D, g[0], g[1], g[2])];
+}
+
+// Levelset::Get_scale, level_set.cpp:311-351 (active tanh law)
+inline double get_scale(const orc_ctx& c, int D, double phi) {
+  double dl0 = ls_dl(c.ls[0], D);
+  if (phi > 0. || std::fabs(phi) < dl0) {
+    double factor = 2.5;
+    return c.min_dl + std::tanh(factor * std::fabs(phi) / c.max_phi) / std::tanh(factor) * (c.max_dl - c.min_dl);
+  }
+  return c.min_dl;
+}
+
+// Particle_mesh_generation::Set_particle_info, particle_mesh_generation.cpp:361-381
+template <int D>
+inline void set_info(const orc_ctx& c, orc_state& s, long long i) {
+  double h_tmp = get_scale(c, D, s.phi[i]);
+  s.h[i] = h_tmp * c.cell_ratio / c.cutoff;
+  // pow(h_tmp, DIM): for DIM = 2 the correctly rounded square, h_tmp*h_tmp
+  s.vol[i] = (D == 2) ? h_tmp * h_tmp : std::pow(h_tmp, 3.0);
+  s.rho[i] = 1.0 / s.vol[i];  // mass = 1 (Particle_mesh_generation::Initialize :53-63)
+}
+
+template <int D>
+inline void get_xyz(const orc_state& s, long long i, double* x) {
+  x[0] = s.x[i]; x[1] = s.y[i]; x[2] = (D == 3) ? s.z[i] : 0.0;
+}
+template <int D>
+inline void put_xyz(orc_state& s, long long i, const double* x) {
+  s.x[i] = x[0]; s.y[i] = x[1]; if (D == 3) s.z[i] = x[2];
+}
+
+template <int D>
+inline void sample_particle(const orc_ctx& c, orc_state& s, long long i) {
+  double x[3], n[3];
+  get_xyz<D>(s, i, x);
+  sample<D>(c, x, &s.phi[i], n, &s.curv[i]);
+  s.nx[i] = n[0]; s.ny[i] = n[1]; s.nz[i] = n[2];
+}
+
+// SPH_mesh_generation::Remap_this_particle_to_positive_phase,
+// sph_mesh_generation.cpp:1885-1928 (non-MPI box).  Random draws: Philox.
+template <int D>
+bool remap(const orc_ctx& c, orc_state& s, long long i) {
+  double box[3], bl[3], br[3];
+  for (int d = 0; d < 3; d++) { bl[d] = c.box_l[d]; br[d] = c.box_r[d]; box[d] = br[d] - bl[d]; }
+  for (uint32_t att = 0; att < 10000000u; att++) {
+    double x[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      U4 r = philox((uint32_t)s.id[i], (uint32_t)s.step, att, (RNG_REMAP << 8) | d, c.seed);
+      double u1 = u53(r.v[0], r.v[1]), u2 = u53(r.v[2], r.v[3]);
+      x[d] = u1 * box[d] + u2 * 1.e-3 + bl[d];
+      x[d] = AMAX1(bl[d] + 1.e-10, AMIN1(x[d], br[d] - 1.e-10));
+    }
+    put_xyz<D>(s, i, x);
+    sample_particle<D>(c, s, i);
+    if (s.phi[i] > s.h[i]) {
+      s.type[i] = REAL_PARTICLE;
+      set_info<D>(c, s, i);
+      return true;
+    }
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// A3: Particle_mesh_generation::Find_and_map_particle :408-467 plus the
+// driver loop sph_mesh_generation.cpp:1506-1545 (dispersal, re-sample,
+// re-seed of REAL particles with phi < 0).  No characteristic
+// (segment/singularity) cells exist in any configured level set, so
+// tag_characteristic is always NORMAL_CELL.
+// ---------------------------------------------------------------------------
+template <int D>
+void map_particle(const orc_ctx& c, orc_state& s, long long i, long long* nremap) {
+  double x[3];
+  get_xyz<D>(s, i, x);
+  int tag = cell_tag<D>(c, x);
+  int t = s.type[i];
+  double nrm[3] = {s.nx[i], s.ny[i], s.nz[i]};
+  double phi = s.phi[i];
+  auto nlen = [&]() {
+    double d = 0.0;
+    d += nrm[0] * nrm[0];
+    d += nrm[1] * nrm[1];
+    if (D == 3) d += nrm[2] * nrm[2];
+    return std::sqrt(d);
+  };
+  if (tag == CUT_CELL && (t == REAL_PARTICLE || t == SURFACE_PARTICLE)) {
+    t = SURFACE_PARTICLE;
+    double dist = std::fabs(phi);
+    double div = 1.0 / (nlen() + 1.0e-15);
+    for (int d = 0; d < D; d++) {
+      double nn = nrm[d] * div;
+      double n_d = phi < 0.0 ? nn : -nn;
+      x[d] = x[d] + n_d * dist;
+    }
+  } else {
+    t = REAL_PARTICLE;
+  }
+  s.type[i] = t;
+  if (t == SURFACE_PARTICLE) {
+    // Get_dispersed_position(0.00001*h), particle_mesh_generation.cpp:385-404
+    double dx = 0.00001 * s.h[i];
+    double div = 1.0 / (nlen() + 1.0e-15);
+    for (int d = 0; d < D; d++) {
+      double nn = nrm[d] * div;
+      double n_d = phi < 0.0 ? nn : -nn;
+      x[d] = x[d] + n_d * dx;
+    }
+  }
+  put_xyz<D>(s, i, x);
+  sample_particle<D>(c, s, i);
+  if (s.phi[i] < 0. && s.type[i] == REAL_PARTICLE) {
+    remap<D>(c, s, i);
+    (*nremap)++;
+  }
+}
+
+// Particle_base::Set_particle_scale, particle.cpp:957-975 (the coarse/finer
+// level flags are reported; levels are planned so they never fire).
+inline int set_particle_scale(const orc_ctx& c, double h, double* scale) {
+  int flag = 0;
+  for (;;) {
+    if (h * c.cutoff > *scale + 1.e-15) {
+      *scale *= 2;
+      if (*scale > c.max_scale + 1.e-15) flag = -1;
+    } else if (h * c.cutoff < *scale / 2 - 1.e-15) {
+      *scale /= 2;
+      if (*scale < c.min_scale - 1.e-15) flag = 1;
+    } else
+      break;
+  }
+  return flag;
+}
+
+// SPH::Map_the_particle_to_tree, sph.cpp:247-276 (level from scale)
+inline int level_of_scale(const orc_ctx& c, double scale) {
+  int current = 0;
+  for (int j = c.ncl - 1; j >= 0; j--) {
+    if (std::fabs(scale - c.cl_scale[j]) <= 1.e-10) return j;
+    if (j >= 1 && scale > c.cl_scale[j] && scale < c.cl_scale[j - 1]) return j - 1;
+  }
+  return current;
+}
+
+// get_cell_id, glbfunc.h:196-208 with _NON_SYM_ (cell range [0, num_cell))
+template <int D>
+inline void cell_of(const orc_ctx& c, int lev, const double* x, int* cell) {
+  for (int d = 0; d < 3; d++) cell[d] = 0;
+  for (int d = 0; d < D; d++) {
+    int p = (int)std::floor((x[d] - c.box_l[d]) / c.cl_dcell[lev][d]);
+    cell[d] = IMAX1(0, IMIN1(p, c.cl_ncell[lev][d] - 1));
+  }
+}
+
+// Neighbour set + geometry for one ordered pair, level_infor.cpp:469-506
+template <int D>
+inline bool is_neighbor(const orc_state& s, long long i, long long j, double cutoff) {
+  double dr[3] = {s.x[i] - s.x[j], s.y[i] - s.y[j], (D == 3) ? s.z[i] - s.z[j] : 0.0};
+  double dist = 0.0;
+  dist += dr[0] * dr[0];
+  dist += dr[1] * dr[1];
+  if (D == 3) dist += dr[2] * dr[2];
+  dist = std::sqrt(dist);
+  return (dist <= (s.h[i] * cutoff + 1.e-10)) || (dist <= (s.h[j] * cutoff + 1.e-10));
+}
+
+struct Neighbors {
+  std::vector<long long> off;  // CSR offsets
+  std::vector<int> nb;         // neighbour indices, sorted by particle id
+};
+
+// ---------------------------------------------------------------------------
+// A5 + A6: cell binning into the multi-resolution tree and neighbour search.
+//   Level_info::Update_cell_list level_infor.cpp:325-344 (own level),
+//   Level_info::Update_every_level_info :407-464 (parents get all child-cell
+//   particles), Level_info::Refresh_neighbor_info :469-506 (3^D own-level
+//   cells; cross-level pairs back-inserted into the finer particle's list).
+// ---------------------------------------------------------------------------
+template <int D>
+void build_neighbors(const orc_ctx& c, const orc_state& s, Neighbors& out) {
+  const long long n = s.n;
+  const int nl = c.ncl;
+  std::vector<std::vector<std::vector<int>>> cells(nl);
+  auto cid = [&](int l, const int* cc) -> long long {
+    return ((long long)cc[2] * c.cl_ncell[l][1] + cc[1]) * c.cl_ncell[l][0] + cc[0];
+  };
+  for (int l = 0; l < nl; l++) {
+    long long nc = (long long)c.cl_ncell[l][0] * c.cl_ncell[l][1] * (D == 3 ? c.cl_ncell[l][2] : 1);
+    cells[l].assign(nc, std::vector<int>());
+  }
+  // own-level binning in index order
+  for (long long i = 0; i < n; i++) {
+    double x[3]; get_xyz<D>(s, i, x);
+    int cc[3]; cell_of<D>(c, s.level[i], x, cc);
+    cells[s.level[i]][cid(s.level[i], cc)].push_back((int)i);
+  }
+  // parents collect all child-cell particles, finest to coarsest
+  for (int l = nl - 2; l >= 0; l--) {
+    int nc0 = c.cl_ncell[l][0], nc1 = c.cl_ncell[l][1], nc2 = (D == 3) ? c.cl_ncell[l][2] : 1;
+    for (int k = 0; k < nc2; k++)
+      for (int j = 0; j < nc1; j++)
+        for (int i = 0; i < nc0; i++) {
+          int pc[3] = {i, j, k};
+          auto& dst = cells[l][cid(l, pc)];
+          for (int t = 0; t < 2; t++)
+            for (int u = 0; u < 2; u++)
+              for (int m = 0; m < (D == 3 ? 2 : 1); m++) {
+                int ch[3] = {2 * i + t, 2 * j + u, (D == 3) ? 2 * k + m : 0};
+                if (ch[0] >= c.cl_ncell[l + 1][0] || ch[1] >= c.cl_ncell[l + 1][1]) continue;
+                if (D == 3 && ch[2] >= c.cl_ncell[l + 1][2]) continue;
+                auto& src = cells[l + 1][cid(l + 1, ch)];
+                dst.insert(dst.end(), src.begin(), src.end());
+              }
+        }
+  }
+  std::vector<std::vector<int>> lists(n);
+  std::vector<std::vector<std::pair<int, int>>> back(
+#ifdef _OPENMP
+      omp_get_max_threads()
+#else
+      1
+#endif
+  );
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long i = 0; i < n; i++) {
+#ifdef _OPENMP
+    int tid = omp_get_thread_num();
+#else
+    int tid = 0;
+#endif
+    int l = s.level[i];
+    double x[3]; get_xyz<D>(s, i, x);
+    int cc[3]; cell_of<D>(c, l, x, cc);
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+      int span = (d < D) ? 1 : 0;
+      lo[d] = IMAX1(cc[d] - span, 0);
+      hi[d] = IMIN1(cc[d] + span, (d < D ? c.cl_ncell[l][d] : 1) - 1);
+    }
+    for (int t = lo[0]; t <= hi[0]; t++)
+      for (int u = lo[1]; u <= hi[1]; u++)
+        for (int m = lo[2]; m <= hi[2]; m++) {
+          int q[3] = {t, u, m};
+          for (int j : cells[l][cid(l, q)]) {
+            if (is_neighbor<D>(s, i, j, c.cutoff)) {
+              lists[i].push_back(j);
+              if (s.level[j] != l) back[tid].push_back(std::make_pair(j, (int)i));
+            }
+          }
+        }
+  }
+  for (auto& b : back)
+    for (auto& p : b) lists[p.first].push_back(p.second);
+  out.off.assign(n + 1, 0);
+  for (long long i = 0; i < n; i++) {
+    std::sort(lists[i].begin(), lists[i].end(), [&](int a, int b) { return s.id[a] < s.id[b]; });
+    out.off[i + 1] = out.off[i] + (long long)lists[i].size();
+  }
+  out.nb.resize(out.off[n]);
+  for (long long i = 0; i < n; i++) std::copy(lists[i].begin(), lists[i].end(), out.nb.begin() + out.off[i]);
+}
+
+// ---------------------------------------------------------------------------
+// A7: Particle_mesh_generation::Get_kernel_summation, :690-765
+// ---------------------------------------------------------------------------
+template <int D>
+void density(const orc_ctx& c, orc_state& s, const Neighbors& nb) {
+  const double cos_t = std::cos(c.angle_thres);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < s.n; i++) {
+    double sum = 0.;
+    int ncount = 0;
+    int ti = s.type[i];
+    double ni[3] = {s.nx[i], s.ny[i], s.nz[i]};
+    for (long long q = nb.off[i]; q < nb.off[i + 1]; q++) {
+      int j = nb.nb[q];
+      double vec[3] = {s.x[i] - s.x[j], s.y[i] - s.y[j], (D == 3) ? s.z[i] - s.z[j] : 0.0};
+      if (ti == REAL_PARTICLE) {
+        double dist = 0.0;
+        dist += vec[0] * vec[0]; dist += vec[1] * vec[1]; if (D == 3) dist += vec[2] * vec[2];
+        dist = std::sqrt(dist);
+        sum += kernel_W(c.kernel, D, dist, s.h[i]);
+        ncount++;
+      } else if (ti == SURFACE_PARTICLE) {
+        double dn = 0.0;
+        dn += vec[0] * ni[0]; dn += vec[1] * ni[1]; if (D == 3) dn += vec[2] * ni[2];
+        double dr[3];
+        for (int d = 0; d < 3; d++) dr[d] = vec[d] - ni[d] * dn;
+        double dist = 0.0;
+        dist += dr[0] * dr[0]; dist += dr[1] * dr[1]; if (D == 3) dist += dr[2] * dr[2];
+        dist = std::sqrt(dist);
+        int tj = s.type[j];
+        if (tj == SURFACE_PARTICLE) {
+          double nj[3] = {s.nx[j], s.ny[j], s.nz[j]};
+          double ca = 0.0;
+          ca += ni[0] * nj[0]; ca += ni[1] * nj[1]; if (D == 3) ca += ni[2] * nj[2];
+          if (std::fabs(ca) > cos_t) {
+            sum += kernel_W(c.kernel, D - 1, dist, s.h[i]);
+            ncount++;
+          }
+        } else if (tj == SEGMENT_PARTICLE || tj == SINGULARITY_PARTICLE) {
+          sum += kernel_W(c.kernel, D - 1, dist, s.h[i]);
+          ncount++;
+        }
+      }
+    }
+    if (ncount > 1) sum = 1. / (sum + 1.e-15);
+    s.sum[i] = sum;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// A8: Accumulate_particle_force_real :995-1118, _surf :883-991,
+// Map_surface_particle_force :1122-1126.  A9: Set_timestep(stage) :127-145
+// and ParallelGetTimestep parallelfunc.cpp:50-58.  A10: Update_velocity_half_step
+// :1130-1135.  One rank, so the MPI colour ramp sigma is 1.
+// ---------------------------------------------------------------------------
+template <int D>
+void force_stage(const orc_ctx& c, orc_state& s, const Neighbors& nb, int stage) {
+  const double cos_t = std::cos(c.angle_thres);
+  const long long n = s.n;
+  std::vector<double> axv(n), ayv(n), azv(n);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    int ti = s.type[i];
+    double F1[3] = {0, 0, 0}, F2[3] = {0, 0, 0};
+    double ni[3] = {s.nx[i], s.ny[i], s.nz[i]};
+    double v[3] = {s.vx[i], s.vy[i], (D == 3) ? s.vz[i] : 0.0};
+    double rho = s.rho[i], h = s.h[i], sum = s.sum[i], nu = s.nu[i];
+    double P = 1.0, mass_j = 1.0, P_j = 1.0, sigma = 1.;
+    if (ti == REAL_PARTICLE || ti == SURFACE_PARTICLE) {
+      for (long long q = nb.off[i]; q < nb.off[i + 1]; q++) {
+        int j = nb.nb[q];
+        int tj = s.type[j];
+        if (ti == SURFACE_PARTICLE && tj == REAL_PARTICLE) continue;
+        if (s.id[i] == s.id[j]) continue;
+        double h_j = s.h[j], rho_j = s.rho[j], nu_j = s.nu[j];
+        double vj[3] = {s.vx[j], s.vy[j], (D == 3) ? s.vz[j] : 0.0};
+        double vec[3] = {s.x[i] - s.x[j], s.y[i] - s.y[j], (D == 3) ? s.z[i] - s.z[j] : 0.0};
+        double dr[3], dist = 0.0, aw;
+        double vol_i = P / powern(rho, 2), vol_j = P_j / powern(rho_j, 2);
+        if (ti == REAL_PARTICLE) {
+          if (tj != REAL_PARTICLE) for (int d = 0; d < 3; d++) vj[d] = v[d] * -1.0;
+          for (int d = 0; d < 3; d++) dr[d] = vec[d];
+          dist += dr[0] * dr[0]; dist += dr[1] * dr[1]; if (D == 3) dist += dr[2] * dr[2];
+          dist = std::sqrt(dist);
+          aw = kernel_dW(c.kernel, D, dist, 0.5 * (h + h_j));
+        } else {
+          double dn = 0.0;
+          dn += vec[0] * ni[0]; dn += vec[1] * ni[1]; if (D == 3) dn += vec[2] * ni[2];
+          for (int d = 0; d < 3; d++) dr[d] = vec[d] - ni[d] * dn;
+          dist += dr[0] * dr[0]; dist += dr[1] * dr[1]; if (D == 3) dist += dr[2] * dr[2];
+          dist = std::sqrt(dist);
+          if (tj == SURFACE_PARTICLE) {
+            double nj[3] = {s.nx[j], s.ny[j], s.nz[j]};
+            double ca = 0.0;
+            ca += ni[0] * nj[0]; ca += ni[1] * nj[1]; if (D == 3) ca += ni[2] * nj[2];
+            if (std::fabs(ca) <= cos_t) continue;
+          }
+          aw = kernel_dW(c.kernel, D - 1, dist, 0.5 * (h + h_j));
+        }
+        double awax[3] = {dr[0] * aw, dr[1] * aw, dr[2] * aw};
+        if (stage == 1) {
+          double P_ij = sigma * mass_j * sum * (vol_i + vol_j);
+          for (int d = 0; d < D; d++) F1[d] = F1[d] + awax[d] * -P_ij;
+        } else {
+          double eta_i = nu * rho, eta_j = nu_j * rho_j;
+          double eta_ij = 2. * eta_j * eta_i / (eta_i + eta_j + 1.e-15);
+          double temp0 = aw * eta_ij * mass_j * (1. / rho / rho + 1. / rho_j / rho_j);
+          for (int d = 0; d < D; d++) F2[d] = F2[d] + (v[d] - vj[d]) * temp0;
+        }
+      }
+    }
+    double a[3] = {0, 0, 0};
+    if (ti == REAL_PARTICLE || ti == SURFACE_PARTICLE) {
+      for (int d = 0; d < D; d++) a[d] = F1[d] + F2[d];
+      if (stage == 2)
+        for (int d = 0; d < D; d++) a[d] = a[d] + v[d] * c.damp_coeff;
+      if (ti == SURFACE_PARTICLE) {
+        double nf = 0.0;
+        nf += a[0] * ni[0]; nf += a[1] * ni[1]; if (D == 3) nf += a[2] * ni[2];
+        for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
+      }
+    }
+    axv[i] = a[0]; ayv[i] = a[1]; azv[i] = a[2];
+  }
+  // Set_timestep(stage) + global min/max
+  double dtmin = 1.e300, vmax = 0.0;
+  std::vector<double> nu_new(n);
+#pragma omp parallel for schedule(static) reduction(min : dtmin) reduction(max : vmax)
+  for (long long i = 0; i < n; i++) {
+    double v[3] = {s.vx[i], s.vy[i], (D == 3) ? s.vz[i] : 0.0};
+    double U = 0.0; U += v[0] * v[0]; U += v[1] * v[1]; if (D == 3) U += v[2] * v[2]; U = std::sqrt(U);
+    double A = 0.0; A += axv[i] * axv[i]; A += ayv[i] * ayv[i]; if (D == 3) A += azv[i] * azv[i]; A = std::sqrt(A);
+    double h = s.h[i];
+    double ts = 0.25 * std::sqrt(h / (A + 1.e-15));
+    ts = AMIN1(ts, h / 40. / (U + 1.e-15));
+    double nu = s.nu[i];
+    if (stage == 2) {
+      nu = c.nu_coeff * h * U;
+      ts = AMIN1(ts, 0.125 * h * h / (nu + 1.e-15));
+    }
+    nu_new[i] = nu;
+    dtmin = AMIN1(dtmin, ts);
+    vmax = AMAX1(vmax, U);
+  }
+  s.dt = dtmin;
+  s.max_v = vmax;
+  // Update_velocity_half_step
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    s.nu[i] = nu_new[i];
+    s.ax[i] = axv[i]; s.ay[i] = ayv[i]; if (D == 3) s.az[i] = azv[i];
+    double hdt = 0.5 * s.dt;
+    s.vx[i] = s.vx[i] + axv[i] * hdt;
+    s.vy[i] = s.vy[i] + ayv[i] * hdt;
+    if (D == 3) s.vz[i] = s.vz[i] + azv[i] * hdt;
+  }
+}
+
+// Reset_particle_force(1): v := 0 every step (Q4), particle_mesh_generation.cpp:149-171
+template <int D>
+void reset_stage1(orc_state& s) {
+  for (long long i = 0; i < s.n; i++) {
+    s.sum[i] = 0.;
+    s.vx[i] = 0.; s.vy[i] = 0.; if (D == 3) s.vz[i] = 0.;
+  }
+}
+
+// Update_coord_full_step, particle_mesh_generation.cpp:1139-1179 (no periodic wrap)
+template <int D>
+void advect(orc_state& s) {
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < s.n; i++) {
+    if (s.type[i] == SINGULARITY_PARTICLE) continue;
+    s.x[i] = s.x[i] + s.vx[i] * s.dt;
+    s.y[i] = s.y[i] + s.vy[i] * s.dt;
+    if (D == 3) s.z[i] = s.z[i] + s.vz[i] * s.dt;
+  }
+}
+
+// Phase "map": Update_coord_full_step, Get_particle_info, Find_and_map_particle,
+// Set_particle_scale and the scale/level refresh of Prepare_for_the_current_step
+// (sph_mesh_generation.cpp:1371-1393, 1984-2022; sph.cpp:456-486).
+template <int D>
+void phase_map(const orc_ctx& c, orc_state& s, int do_advect) {
+  if (do_advect) advect<D>(s);
+  long long nremap = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : nremap)
+  for (long long i = 0; i < s.n; i++) {
+    sample_particle<D>(c, s, i);
+    map_particle<D>(c, s, i, &nremap);
+  }
+  s.remapped = nremap;
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < s.n; i++) {
+    set_info<D>(c, s, i);
+    set_particle_scale(c, s.h[i], &s.scale[i]);
+    s.level[i] = level_of_scale(c, s.scale[i]);
+  }
+}
+
+// Pre_run, sph_mesh_generation.cpp:1010-1050: sample, Set_particle_info,
+// Find_and_map; forces of Pre_run vanish (sum = 0, v = 0), leaving v = 0, nu = 0.
+template <int D>
+void pre_run(const orc_ctx& c, orc_state& s) {
+  long long nremap = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : nremap)
+  for (long long i = 0; i < s.n; i++) {
+    sample_particle<D>(c, s, i);
+    set_info<D>(c, s, i);
+    map_particle<D>(c, s, i, &nremap);
+  }
+  s.remapped = nremap;
+  for (long long i = 0; i < s.n; i++) {
+    set_particle_scale(c, s.h[i], &s.scale[i]);
+    s.level[i] = level_of_scale(c, s.scale[i]);
+    s.vx[i] = 0; s.vy[i] = 0; if (D == 3) s.vz[i] = 0;
+    s.nu[i] = 0;
+  }
+  s.dt = 0.0;
+}
+
+// Random_particle_distribution, sph_mesh_generation.cpp:1302-1367 (non-MPI)
+template <int D>
+int seed_particles(const orc_ctx& c, orc_state& s) {
+  const orc_level& L0 = c.ls[0];
+  double padding = L0.dpkg[0];  // lset_level_info[0]->scale (lset_level_infor.cpp:47)
+  double lbl[3], lbr[3];
+  for (int d = 0; d < 3; d++) { lbl[d] = L0.box_l[d]; lbr[d] = L0.box_l[d] + L0.dpkg[d] * L0.num_pkg[d]; }
+  int fail = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : fail)
+  for (long long i = 0; i < s.n; i++) {
+    s.type[i] = REAL_PARTICLE;
+    s.scale[i] = c.max_scale;  // Particle_mesh_generation::Initialize :53-63
+    bool ok = false;
+    for (uint32_t att = 0; att < 10000000u && !ok; att++) {
+      double x[3] = {0, 0, 0};
+      for (int d = 0; d < D; d++) {
+        U4 r = philox((uint32_t)s.id[i], 0u, att, (RNG_SEED << 8) | d, c.seed);
+        double u1 = u53(r.v[0], r.v[1]), u2 = u53(r.v[2], r.v[3]);
+        double box = c.box_r[d] - c.box_l[d];
+        x[d] = u1 * box + u2 * 1.e-3 + c.box_l[d];
+        x[d] = AMAX1(c.box_l[d] + 1.e-10, AMIN1(x[d], c.box_r[d] - 1.e-10));
+        x[d] = AMAX1(lbl[d] + padding, AMIN1(lbr[d] - padding, x[d]));
+      }
+      put_xyz<D>(s, i, x);
+      sample_particle<D>(c, s, i);
+      set_info<D>(c, s, i);
+      if (s.phi[i] > s.h[i]) ok = true;
+    }
+    if (!ok) fail++;
+  }
+  return fail ? -1 : 0;
+}
+
+template <int D>
+void one_step(const orc_ctx& c, orc_state& s, Neighbors& nb) {
+  s.step += 1;
+  phase_map<D>(c, s, 1);
+  build_neighbors<D>(c, s, nb);
+  reset_stage1<D>(s);
+  density<D>(c, s, nb);
+  force_stage<D>(c, s, nb, 1);
+  force_stage<D>(c, s, nb, 2);
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+// SPH::Define_level_infor_tight sph.cpp:144-180 + Level_info::Initialize
+// level_infor.cpp:35-110 (cell sizes per level), with max/min_scale from
+// Initialize_case sph_mesh_generation.cpp:781-787.
+int orc_define_levels(orc_ctx* c) {
+  const int D = c->dim;
+  double domain[3];
+  for (int d = 0; d < 3; d++) domain[d] = c->box_r[d] - c->box_l[d];
+  c->max_scale = c->max_dl * c->cell_ratio;
+  c->min_scale = c->min_dl * c->cell_ratio;
+  double ini_scale = c->max_scale;
+  double scale_temp = domain[0];
+  if (D >= 2) scale_temp = AMIN1(domain[1], scale_temp);
+  if (D == 3) scale_temp = AMIN1(domain[2], scale_temp);
+  int temp = (int)std::floor(scale_temp / ini_scale);
+  if (temp < 1) return -1;
+  ini_scale = scale_temp / (double)temp;
+  c->max_scale = ini_scale;
+  scale_temp = ini_scale;
+  int num_level = 1;
+  while ((scale_temp + 1.e-6) > c->min_scale) {
+    scale_temp /= 2;
+    num_level++;
+  }
+  c->min_scale = scale_temp * 2;
+  num_level -= 1;
+  if (num_level < 1 || num_level > 16) return -2;
+  c->ncl = num_level;
+  for (int d = 0; d < 3; d++) c->ini_num_cell[d] = (d < D) ? (int)(domain[d] / c->max_scale) : 1;
+  for (int l = 0; l < num_level; l++) {
+    double multi = powern(2.0, l);
+    double sc = 1.e300;
+    for (int d = 0; d < 3; d++) {
+      c->cl_ncell[l][d] = (d < D) ? (int)(c->ini_num_cell[d] * multi) : 1;
+      c->cl_dcell[l][d] = (d < D) ? domain[d] / c->cl_ncell[l][d] : 1.0;
+      if (d < D) sc = AMIN1(sc, c->cl_dcell[l][d]);
+    }
+    c->cl_scale[l] = sc;
+  }
+  return 0;
+}
+
+int orc_ls_build(orc_ctx* c, int level, double* max_phi) {
+  if (c->dim == 2) ls_build<2>(c->ls[level], max_phi);
+  else ls_build<3>(c->ls[level], max_phi);
+  return 0;
+}
+
+void orc_kernel_W(int kind, int D, long long n, const double* dist, double h, double* out) {
+  for (long long i = 0; i < n; i++) out[i] = kernel_W(kind, D, dist[i], h);
+}
+void orc_kernel_dW(int kind, int D, long long n, const double* dist, double h, double* out) {
+  for (long long i = 0; i < n; i++) out[i] = kernel_dW(kind, D, dist[i], h);
+}
+double orc_get_scale(const orc_ctx* c, double phi) { return get_scale(*c, c->dim, phi); }
+
+void orc_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed, uint32_t* out) {
+  U4 r = philox(c0, c1, c2, c3, seed);
+  for (int i = 0; i < 4; i++) out[i] = r.v[i];
+}
+
+void orc_sample(const orc_ctx* c, long long n, const double* xyz, double* phi, double* nrm, double* curv, int* tag) {
+  for (long long i = 0; i < n; i++) {
+    double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    if (c->dim == 2) {
+      sample<2>(*c, x, &phi[i], &nrm[3 * i], &curv[i]);
+      if (tag) tag[i] = cell_tag<2>(*c, x);
+    } else {
+      sample<3>(*c, x, &phi[i], &nrm[3 * i], &curv[i]);
+      if (tag) tag[i] = cell_tag<3>(*c, x);
+    }
+  }
+}
+
+int orc_seed(const orc_ctx* c, orc_state* s) {
+  return c->dim == 2 ? seed_particles<2>(*c, *s) : seed_particles<3>(*c, *s);
+}
+void orc_pre_run(const orc_ctx* c, orc_state* s) {
+  if (c->dim == 2) pre_run<2>(*c, *s); else pre_run<3>(*c, *s);
+}
+void orc_phase_map(const orc_ctx* c, orc_state* s, int do_advect) {
+  if (c->dim == 2) phase_map<2>(*c, *s, do_advect); else phase_map<3>(*c, *s, do_advect);
+}
+
+// per-particle cell key at its own level: (level, cx, cy, cz)
+void orc_cells(const orc_ctx* c, const orc_state* s, int* out4) {
+  for (long long i = 0; i < s->n; i++) {
+    double x[3] = {s->x[i], s->y[i], c->dim == 3 ? s->z[i] : 0.0};
+    int cc[3];
+    if (c->dim == 2) cell_of<2>(*c, s->level[i], x, cc); else cell_of<3>(*c, s->level[i], x, cc);
+    out4[4 * i] = s->level[i];
+    out4[4 * i + 1] = cc[0]; out4[4 * i + 2] = cc[1]; out4[4 * i + 3] = cc[2];
+  }
+}
+
+// Neighbour lists in CSR form (sorted by particle id).  Two-call protocol:
+// with nb == NULL only *total is returned.
+static Neighbors g_nb_cache;
+long long orc_neighbors(const orc_ctx* c, const orc_state* s, long long* off, int* nb, long long cap) {
+  if (c->dim == 2) build_neighbors<2>(*c, *s, g_nb_cache); else build_neighbors<3>(*c, *s, g_nb_cache);
+  long long tot = g_nb_cache.off[s->n];
+  if (off) for (long long i = 0; i <= s->n; i++) off[i] = g_nb_cache.off[i];
+  if (nb && cap >= tot) std::copy(g_nb_cache.nb.begin(), g_nb_cache.nb.end(), nb);
+  return tot;
+}
+
+// Density and force stages on given CSR neighbour lists.
+void orc_density(const orc_ctx* c, orc_state* s, const long long* off, const int* nbr) {
+  Neighbors nb;
+  nb.off.assign(off, off + s->n + 1);
+  nb.nb.assign(nbr, nbr + off[s->n]);
+  if (c->dim == 2) density<2>(*c, *s, nb); else density<3>(*c, *s, nb);
+}
+void orc_force(const orc_ctx* c, orc_state* s, const long long* off, const int* nbr, int stage) {
+  Neighbors nb;
+  nb.off.assign(off, off + s->n + 1);
+  nb.nb.assign(nbr, nbr + off[s->n]);
+  if (c->dim == 2) force_stage<2>(*c, *s, nb, stage); else force_stage<3>(*c, *s, nb, stage);
+}
+void orc_reset_stage1(const orc_ctx* c, orc_state* s) {
+  if (c->dim == 2) reset_stage1<2>(*s); else reset_stage1<3>(*s);
+}
+
+// Full relaxation steps (SPH_run_mesh_generation x nsteps).
+long long orc_steps(const orc_ctx* c, orc_state* s, int nsteps) {
+  Neighbors nb;
+  long long pairs = 0;
+  for (int k = 0; k < nsteps; k++) {
+    if (c->dim == 2) one_step<2>(*c, *s, nb); else one_step<3>(*c, *s, nb);
+    pairs += nb.off[s->n] - s->n;
+  }
+  return pairs;
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,284 @@
+"""ctypes front end of the CPU FP64 oracle (oracle/mrsph_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py (CPU
+baseline and reference arms) use this module as the checker.  The product
+library never imports it.
+
+Parity status: unpinned against the reference binary (the reference needs TBB,
+Boost.MPI and voro++ and ships no tests or golden vectors); pinned to analytic
+known-answer tests instead.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "mrsph_oracle.cpp")
+LIB = os.path.join(HERE, "_build", "libmrsph_oracle.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (OpenMP, no fused multiply-add)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           SRC, "-o", LIB + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class OrcLevel(C.Structure):
+    _fields_ = [("box_l", C.c_double * 3), ("dpkg", C.c_double * 3), ("num_pkg", C.c_int * 3),
+                ("margin", C.c_int), ("phi", C.c_void_p), ("nx", C.c_void_p), ("ny", C.c_void_p),
+                ("nz", C.c_void_p), ("curv", C.c_void_p), ("tag", C.c_void_p), ("active", C.c_void_p)]
+
+
+class OrcCtx(C.Structure):
+    _fields_ = [("dim", C.c_int), ("kernel", C.c_int), ("cell_ratio", C.c_double), ("cutoff", C.c_double),
+                ("angle_thres", C.c_double), ("nu_coeff", C.c_double), ("damp_coeff", C.c_double),
+                ("min_dl", C.c_double), ("max_dl", C.c_double), ("max_phi", C.c_double),
+                ("box_l", C.c_double * 3), ("box_r", C.c_double * 3), ("seed", C.c_ulonglong),
+                ("nls", C.c_int), ("ls", C.POINTER(OrcLevel)), ("ncl", C.c_int),
+                ("max_scale", C.c_double), ("min_scale", C.c_double), ("ini_num_cell", C.c_int * 3),
+                ("cl_dcell", (C.c_double * 3) * 16), ("cl_ncell", (C.c_int * 3) * 16),
+                ("cl_scale", C.c_double * 16)]
+
+
+_DBL_FIELDS = ["x", "y", "z", "vx", "vy", "vz"]
+_INT_FIELDS = ["type", "id", "level"]
+_DBL2_FIELDS = ["h", "scale", "phi", "curv", "nx", "ny", "nz", "sum", "rho", "vol", "nu"]
+_ACC_FIELDS = ["ax", "ay", "az"]
+
+
+class OrcState(C.Structure):
+    _fields_ = ([("n", C.c_longlong)] + [(f, C.c_void_p) for f in _DBL_FIELDS]
+                + [(f, C.c_void_p) for f in _INT_FIELDS] + [(f, C.c_void_p) for f in _DBL2_FIELDS]
+                + [(f, C.c_void_p) for f in _ACC_FIELDS]
+                + [("dt", C.c_double), ("max_v", C.c_double), ("step", C.c_longlong),
+                   ("remapped", C.c_longlong)])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.orc_define_levels.argtypes = [C.POINTER(OrcCtx)]
+        L.orc_ls_build.argtypes = [C.POINTER(OrcCtx), C.c_int, C.POINTER(C.c_double)]
+        L.orc_kernel_W.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_void_p, C.c_double, C.c_void_p]
+        L.orc_kernel_dW.argtypes = L.orc_kernel_W.argtypes
+        L.orc_get_scale.argtypes = [C.POINTER(OrcCtx), C.c_double]
+        L.orc_get_scale.restype = C.c_double
+        L.orc_philox.argtypes = [C.c_uint32] * 4 + [C.c_ulonglong, C.c_void_p]
+        L.orc_sample.argtypes = [C.POINTER(OrcCtx), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p]
+        L.orc_seed.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState)]
+        L.orc_pre_run.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState)]
+        L.orc_phase_map.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_int]
+        L.orc_cells.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_void_p]
+        L.orc_neighbors.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_void_p, C.c_void_p,
+                                    C.c_longlong]
+        L.orc_neighbors.restype = C.c_longlong
+        L.orc_density.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_void_p, C.c_void_p]
+        L.orc_force.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_reset_stage1.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState)]
+        L.orc_steps.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_int]
+        L.orc_steps.restype = C.c_longlong
+        L.orc_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """FP64 oracle for one geometry (mirrors the C-ABI handle of the product)."""
+
+    def __init__(self, case):
+        self.case = case
+        p = case.params
+        self.ctx = OrcCtx()
+        c = self.ctx
+        c.dim = p["dim"]
+        c.kernel = p["kernel"]
+        c.cell_ratio = p["cell_ratio"]
+        c.cutoff = p["cutoff"]
+        c.angle_thres = p["angle_thres"]
+        c.nu_coeff = p["nu_coeff"]
+        c.damp_coeff = p["damp_coeff"]
+        c.min_dl = p["min_dl"]
+        c.max_dl = p["max_dl"]
+        for d in range(3):
+            c.box_l[d] = p["box_l"][d]
+            c.box_r[d] = p["box_r"][d]
+        c.seed = p["seed"]
+        # level-set levels
+        self._keep = []
+        levels = case.levels
+        arr = (OrcLevel * len(levels))()
+        self.fields = []
+        for i, lv in enumerate(levels):
+            L = arr[i]
+            for d in range(3):
+                L.box_l[d] = lv.box_l[d]
+                L.dpkg[d] = lv.dpkg[d]
+                L.num_pkg[d] = lv.num_pkg[d]
+            L.margin = lv.margin
+            phi = np.ascontiguousarray(lv.phi, dtype=np.float64).ravel()
+            f = {"phi": phi}
+            for k in ("nx", "ny", "nz", "curv"):
+                f[k] = np.zeros_like(phi)
+            f["tag"] = np.zeros(phi.shape, dtype=np.int32)
+            for k in ("phi", "nx", "ny", "nz", "curv", "tag"):
+                setattr(L, k, _p(f[k]))
+            if lv.active is not None:
+                act = np.ascontiguousarray(lv.active, dtype=np.uint8).ravel()
+                f["active"] = act
+                L.active = _p(act)
+            else:
+                L.active = None
+            self.fields.append(f)
+        self.levels_arr = arr
+        c.nls = len(levels)
+        c.ls = C.cast(arr, C.POINTER(OrcLevel))
+        rc = lib().orc_define_levels(C.byref(c))
+        if rc != 0:
+            raise RuntimeError(f"orc_define_levels failed ({rc})")
+        mp = 0.0
+        for i in range(len(levels)):
+            m = C.c_double(0.0)
+            lib().orc_ls_build(C.byref(c), i, C.byref(m))
+            mp = max(mp, m.value)
+        c.max_phi = mp
+        self.state = None
+        self.arrays = {}
+
+    # ----------------------------------------------------------------- state
+    def alloc(self, n: int):
+        a = {}
+        for f in _DBL_FIELDS + _DBL2_FIELDS + _ACC_FIELDS:
+            a[f] = np.zeros(n, dtype=np.float64)
+        for f in _INT_FIELDS:
+            a[f] = np.zeros(n, dtype=np.int32)
+        a["id"][:] = np.arange(n, dtype=np.int32)
+        a["scale"][:] = self.ctx.max_scale
+        s = OrcState()
+        s.n = n
+        for f, v in a.items():
+            setattr(s, f, _p(v))
+        s.dt = 0.0
+        s.step = 0
+        self.state = s
+        self.arrays = a
+        return a
+
+    def set_state(self, st: dict):
+        """Load a state dictionary (FP64 arrays in particle-id order)."""
+        n = len(st["x"])
+        a = self.alloc(n)
+        for k, v in st.items():
+            if k in a:
+                a[k][:] = v
+        if "dt" in st:
+            self.state.dt = float(st["dt"])
+        if "step" in st:
+            self.state.step = int(st["step"])
+
+    def get_state(self) -> dict:
+        out = {k: v.copy() for k, v in self.arrays.items()}
+        out["dt"] = self.state.dt
+        out["max_v"] = self.state.max_v
+        out["step"] = self.state.step
+        return out
+
+    # ----------------------------------------------------------------- phases
+    def seed(self, n: int):
+        self.alloc(n)
+        rc = lib().orc_seed(C.byref(self.ctx), C.byref(self.state))
+        if rc != 0:
+            raise RuntimeError("oracle seeding did not converge")
+
+    def pre_run(self):
+        lib().orc_pre_run(C.byref(self.ctx), C.byref(self.state))
+
+    def phase_map(self, advect: bool = True):
+        self.state.step += 1
+        lib().orc_phase_map(C.byref(self.ctx), C.byref(self.state), 1 if advect else 0)
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros((self.state.n, 4), dtype=np.int32)
+        lib().orc_cells(C.byref(self.ctx), C.byref(self.state), _p(out))
+        return out
+
+    def neighbors(self):
+        n = self.state.n
+        off = np.zeros(n + 1, dtype=np.int64)
+        tot = lib().orc_neighbors(C.byref(self.ctx), C.byref(self.state), _p(off), None, 0)
+        nb = np.zeros(max(tot, 1), dtype=np.int32)
+        lib().orc_neighbors(C.byref(self.ctx), C.byref(self.state), _p(off), _p(nb), tot)
+        return off, nb[:tot]
+
+    def density(self, off, nb):
+        lib().orc_reset_stage1(C.byref(self.ctx), C.byref(self.state))
+        lib().orc_density(C.byref(self.ctx), C.byref(self.state), _p(off), _p(nb))
+
+    def force(self, off, nb, stage: int):
+        lib().orc_force(C.byref(self.ctx), C.byref(self.state), _p(off), _p(nb), stage)
+
+    def steps(self, k: int) -> int:
+        return lib().orc_steps(C.byref(self.ctx), C.byref(self.state), k)
+
+    def sample(self, xyz: np.ndarray):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = len(xyz)
+        phi = np.zeros(n)
+        nrm = np.zeros((n, 3))
+        curv = np.zeros(n)
+        tag = np.zeros(n, dtype=np.int32)
+        lib().orc_sample(C.byref(self.ctx), n, _p(xyz), _p(phi), _p(nrm), _p(curv), _p(tag))
+        return phi, nrm, curv, tag
+
+    def get_scale(self, phi: float) -> float:
+        return lib().orc_get_scale(C.byref(self.ctx), phi)
+
+    def levels(self):
+        c = self.ctx
+        return {"ncl": c.ncl, "max_scale": c.max_scale, "min_scale": c.min_scale,
+                "ncell": [list(c.cl_ncell[l]) for l in range(c.ncl)],
+                "dcell": [list(c.cl_dcell[l]) for l in range(c.ncl)],
+                "scale": [c.cl_scale[l] for l in range(c.ncl)]}
+
+
+def kernel_W(kind: int, dim: int, dist: np.ndarray, h: float) -> np.ndarray:
+    dist = np.ascontiguousarray(dist, dtype=np.float64)
+    out = np.zeros_like(dist)
+    lib().orc_kernel_W(kind, dim, len(dist), _p(dist), h, _p(out))
+    return out
+
+
+def kernel_dW(kind: int, dim: int, dist: np.ndarray, h: float) -> np.ndarray:
+    dist = np.ascontiguousarray(dist, dtype=np.float64)
+    out = np.zeros_like(dist)
+    lib().orc_kernel_dW(kind, dim, len(dist), _p(dist), h, _p(out))
+    return out
+
+
+def philox(c0, c1, c2, c3, seed):
+    out = (C.c_uint32 * 4)()
+    lib().orc_philox(c0, c1, c2, c3, seed, out)
+    return list(out)
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()

@@ -1,0 +1,1210 @@
+// engine.cuh — the relaxation step as CUDA kernels, templated on dimension D
+// and arithmetic type R (double: FP64-plain, float: FP32-split).  Included by
+// mrsph_fp64.cu (compiled without FMA contraction so FP64 results follow the
+// reference's operation order) and mrsph_fp32.cu.
+//
+// One step (SPH_mesh_generation::SPH_run_mesh_generation,
+// sph_mesh_generation.cpp:1371-1463) is 11 launches on one stream, replayed as
+// a CUDA graph:
+//   k_begin_step   scalars of the step
+//   k_map          A1 advect + A2 sample + A3 surface map/re-seed + A4 spacing
+//                  + scale/level refresh + cell key + cell histogram
+//   scan x3, scatter, rank      A5 counting sort into (level, cell) order
+//   k_reorder      gather persistent state into the sorted order
+//   k_density      A6 neighbour search over the cell table + A7 kernel sum,
+//                  writes the neighbour list (ELL, column-major)
+//   k_force<1>     A8 stage 1 + A9 dt/max|v| grid reduction (FP64 bit atomics)
+//   k_force<2>     A8 stage 2 + A9 + A10 (stage-1 kick folded in; the stage-2
+//                  kick is folded into the next k_map)
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "engine_iface.h"
+
+namespace mrsph {
+
+using std::max;
+using std::min;
+
+// ---------------------------------------------------------------------------
+// device data
+// ---------------------------------------------------------------------------
+template <class R>
+struct Buf {  // persistent per-particle state, one ping-pong half
+  typename V4<R>::T* posh;  // FP64: (x, y, z, h); FP32: (offset in anchor cell, h)
+  typename V4<R>::T* nr;    // (nx, ny, nz, rho)
+  typename V4<R>::T* v1;    // velocity after the stage-1 kick
+  typename V4<R>::T* a2;    // stage-2 acceleration
+  int* key;                 // FP32 anchor cell, packed (FP64: unused)
+  int* meta;                // type | level << 8
+  int* id;
+  R* nu;                    // viscosity read by stage 2
+  R* nu_next;               // viscosity written by stage 2
+  R* phi;
+  R* curv;
+  int* cellkey;             // (level, cell) table index
+};
+
+template <class R>
+struct Work {  // per-step arrays in sorted order
+  R* sum;
+  typename V4<R>::T* a1;
+  int* cnt;
+  int* nbl;  // neighbour list, column-major: nbl[q * n + i]
+  int cap;
+  int* counts;
+  int* cstart;
+  int* perm;
+  int* perm2;
+  int* blocksums;
+  int* slot_of_id;
+};
+
+struct KCtx {
+  Params prm;
+  CellGeo geo;
+  LsSet ls;
+  long long n;
+  DevScalars* sc;
+};
+
+enum { MAP_STEP = 0, MAP_PRE = 1 };
+
+// ---------------------------------------------------------------------------
+// position representations
+// ---------------------------------------------------------------------------
+template <int D, class R> struct PosOps;
+
+template <int D>
+struct PosOps<D, double> {
+  using T4 = double4;
+  __device__ static void world(const KCtx&, const T4& p, int, double* x) { x[0] = p.x; x[1] = p.y; x[2] = (D == 3) ? p.z : 0.0; }
+  __device__ static void set_world(const KCtx&, T4& p, int&, const double* x) { p.x = x[0]; p.y = x[1]; p.z = (D == 3) ? x[2] : 0.0; }
+  // x = x + d  (the reference's coord + delta, component-wise)
+  __device__ static void add(const KCtx&, T4& p, int&, const double* d) {
+    p.x = p.x + d[0];
+    p.y = p.y + d[1];
+    if (D == 3) p.z = p.z + d[2];
+  }
+  // get_cell_id, glbfunc.h:196-208 (_NON_SYM_: [0, num_cell))
+  __device__ static void cell(const KCtx& c, int L, const T4& p, int, int* cc) {
+    double x[3] = {p.x, p.y, p.z};
+    cc[2] = 0;
+    for (int d = 0; d < D; d++) {
+      int q = (int)floor((x[d] - c.geo.box_l[d]) / c.geo.dcell[L][d]);
+      cc[d] = max(0, min(q, c.geo.n[L][d] - 1));
+    }
+  }
+  __device__ static void rel(const KCtx&, const T4& pi, int, const T4& pj, int, double* dr) {
+    dr[0] = pi.x - pj.x;
+    dr[1] = pi.y - pj.y;
+    dr[2] = (D == 3) ? pi.z - pj.z : 0.0;
+  }
+};
+
+// FP32-split: position = anchor cell (finest cell-list cell) + FP32 offset.
+template <int D>
+struct PosOps<D, float> {
+  using T4 = float4;
+  __device__ static void unpack(int key, int* k) {
+    unsigned u = (unsigned)key;
+    if (D == 2) { k[0] = u & 0xFFFF; k[1] = (u >> 16) & 0xFFFF; k[2] = 0; }
+    else { k[0] = u & 0x7FF; k[1] = (u >> 11) & 0x7FF; k[2] = (u >> 22) & 0x3FF; }
+  }
+  __device__ static int pack(const int* k) {
+    if (D == 2) return (int)((unsigned)k[0] | ((unsigned)k[1] << 16));
+    return (int)((unsigned)k[0] | ((unsigned)k[1] << 11) | ((unsigned)k[2] << 22));
+  }
+  __device__ static void world(const KCtx& c, const T4& p, int key, double* x) {
+    int k[3];
+    unpack(key, k);
+    float o[3] = {p.x, p.y, p.z};
+    x[2] = 0.0;
+    for (int d = 0; d < D; d++) x[d] = c.geo.box_l[d] + ((double)k[d] * c.geo.A[d] + (double)o[d]);
+  }
+  __device__ static void set_world(const KCtx& c, T4& p, int& key, const double* x) {
+    int k[3] = {0, 0, 0};
+    float o[3] = {0.f, 0.f, 0.f};
+    const int lm = c.geo.ncl - 1;
+    for (int d = 0; d < D; d++) {
+      double rel = x[d] - c.geo.box_l[d];
+      int q = (int)floor(rel / c.geo.A[d]);
+      q = max(0, min(q, c.geo.n[lm][d] - 1));
+      k[d] = q;
+      o[d] = (float)(rel - (double)q * c.geo.A[d]);
+    }
+    p.x = o[0]; p.y = o[1]; p.z = o[2];
+    key = pack(k);
+  }
+  __device__ static void add(const KCtx& c, T4& p, int& key, const float* dlt) {
+    int k[3];
+    unpack(key, k);
+    float o[3] = {p.x, p.y, p.z};
+    const int lm = c.geo.ncl - 1;
+    for (int d = 0; d < D; d++) {
+      o[d] = o[d] + dlt[d];
+      float q = floorf(o[d] / c.geo.Af[d]);
+      if (q != 0.f) {
+        int kn = max(0, min(k[d] + (int)q, c.geo.n[lm][d] - 1));
+        o[d] -= (float)(kn - k[d]) * c.geo.Af[d];
+        k[d] = kn;
+      }
+    }
+    p.x = o[0]; p.y = o[1]; p.z = o[2];
+    key = pack(k);
+  }
+  __device__ static void cell(const KCtx& c, int L, const T4&, int key, int* cc) {
+    int k[3];
+    unpack(key, k);
+    int sh = c.geo.ncl - 1 - L;
+    cc[2] = 0;
+    for (int d = 0; d < D; d++) cc[d] = k[d] >> sh;
+  }
+  __device__ static void rel(const KCtx& c, const T4& pi, int ki, const T4& pj, int kj, float* dr) {
+    int a[3], b[3];
+    unpack(ki, a);
+    unpack(kj, b);
+    dr[0] = (float)(a[0] - b[0]) * c.geo.Af[0] + (pi.x - pj.x);
+    dr[1] = (float)(a[1] - b[1]) * c.geo.Af[1] + (pi.y - pj.y);
+    dr[2] = (D == 3) ? (float)(a[2] - b[2]) * c.geo.Af[2] + (pi.z - pj.z) : 0.f;
+  }
+};
+
+template <class R> __device__ inline typename V4<R>::T mk4(R a, R b, R c, R d);
+template <> __device__ inline double4 mk4<double>(double a, double b, double c, double d) { return make_double4(a, b, c, d); }
+template <> __device__ inline float4 mk4<float>(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+template <int D, class R>
+__device__ inline R dot3(const R* a, const R* b) {
+  R s = 0;
+  s += a[0] * b[0];
+  s += a[1] * b[1];
+  if (D == 3) s += a[2] * b[2];
+  return s;
+}
+
+// Set_particle_info, particle_mesh_generation.cpp:361-381 (mass = 1)
+template <int D, class R>
+__device__ inline void set_info(const KCtx& c, R phi, R& h, R& rho) {
+  R h_tmp = get_scale<R>(c.ls, phi);
+  h = h_tmp * (R)c.prm.cell_ratio / (R)c.prm.cutoff;
+  R vol = (D == 2) ? h_tmp * h_tmp : (R)pow((double)h_tmp, 3.0);
+  rho = (R)1.0 / vol;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+static __global__ void k_begin_step(DevScalars* sc, int inc) {
+  sc->dt_adv = sc->dt2;
+  sc->dt1 = 0x7FF0000000000000ull;  // +inf
+  sc->dt2 = 0x7FF0000000000000ull;
+  sc->vmax1 = 0;
+  sc->vmax2 = 0;
+  sc->pairs = 0;
+  sc->remap = 0;
+  sc->nsurf = 0;
+  sc->maxcnt = 0;
+  sc->step += inc;
+}
+
+// Random_particle_distribution, sph_mesh_generation.cpp:1302-1367 (one rank)
+template <int D, class R>
+__global__ void k_seed(KCtx c, Buf<R> b, unsigned max_att) {
+  using P = PosOps<D, R>;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  const LsLevel& L0 = c.ls.lv[0];
+  double padding = L0.dpkg[0];
+  R phi = 0, n[3] = {0, 0, 0}, curv = 0, h = 0, rho = 0;
+  double x[3] = {0, 0, 0};
+  bool ok = false;
+  for (unsigned att = 0; att < max_att && !ok; att++) {
+    for (int d = 0; d < D; d++) {
+      U4 r = philox((uint32_t)i, 0u, att, (RNG_SEED << 8) | d, c.prm.seed);
+      double u1 = u53(r.v[0], r.v[1]), u2 = u53(r.v[2], r.v[3]);
+      double box = c.prm.box_r[d] - c.prm.box_l[d];
+      double lbl = L0.box_l[d], lbr = L0.box_l[d] + L0.dpkg[d] * L0.num_pkg[d];
+      double xd = u1 * box + u2 * 1.e-3 + c.prm.box_l[d];
+      xd = AMAX1(c.prm.box_l[d] + 1.e-10, AMIN1(xd, c.prm.box_r[d] - 1.e-10));
+      xd = AMAX1(lbl + padding, AMIN1(lbr - padding, xd));
+      x[d] = xd;
+    }
+    ls_sample<D, R>(c.ls, x, phi, n, curv);
+    set_info<D, R>(c, phi, h, rho);
+    if (phi > h) ok = true;
+  }
+  if (!ok) atomicOr(&c.sc->flags, (unsigned)FLAG_SEED);
+  typename V4<R>::T p = mk4<R>(0, 0, 0, h);
+  int key = 0;
+  P::set_world(c, p, key, x);
+  b.posh[i] = p;
+  if (b.key) b.key[i] = key;
+  b.nr[i] = mk4<R>(n[0], n[1], n[2], rho);
+  b.meta[i] = REAL_P;  // level 0: scale = max_scale (Particle_mesh_generation::Initialize)
+  b.id[i] = (int)i;
+  b.nu[i] = 0;
+  b.nu_next[i] = 0;
+  b.phi[i] = phi;
+  b.curv[i] = curv;
+  b.v1[i] = mk4<R>(0, 0, 0, 0);
+  b.a2[i] = mk4<R>(0, 0, 0, 0);
+}
+
+// A1-A4 + scale refresh + cell key (see file header).  mode MAP_PRE is the
+// map part of Pre_run (sph_mesh_generation.cpp:1010-1050): no advection,
+// Set_particle_info before Find_and_map.
+template <int D, class R>
+__global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int mode, unsigned max_att) {
+  using P = PosOps<D, R>;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned surf = 0;
+  if (i < c.n) {
+    int meta = b.meta[i];
+    int type = meta & 0xFF;
+    int e = (int)(signed char)((meta >> 8) & 0xFF);
+    typename V4<R>::T p = b.posh[i];
+    int key = b.key ? b.key[i] : 0;
+    const int id = b.id[i];
+    R h = p.w;
+    // A1 Update_coord_full_step (particle_mesh_generation.cpp:1139-1179), with
+    // the stage-2 half kick of the previous step folded in (:1130-1135)
+    if (mode == MAP_STEP && type != SINGULARITY_P) {
+      double dt2 = bitsd(c.sc->dt_adv);
+      typename V4<R>::T v1 = b.v1[i], a2 = b.a2[i];
+      R hdt = (R)(0.5 * dt2), dtr = (R)dt2;
+      R v[3] = {v1.x + a2.x * hdt, v1.y + a2.y * hdt, v1.z + a2.z * hdt};
+      R dl[3] = {v[0] * dtr, v[1] * dtr, (D == 3) ? v[2] * dtr : (R)0};
+      P::add(c, p, key, dl);
+    }
+    double x[3];
+    P::world(c, p, key, x);
+    R phi, n[3], curv, rho = 0;
+    ls_sample<D, R>(c.ls, x, phi, n, curv);  // A2 Get_particle_info
+    if (mode == MAP_PRE) set_info<D, R>(c, phi, h, rho);
+    // A3 Find_and_map_particle (:408-467) + driver loop (sph_mesh_generation.cpp:1506-1545)
+    int tag = ls_tag<D>(c.ls, x);
+    R nl = r_sqrt(dot3<D, R>(n, n));
+    if (tag == CUT_CELL && (type == REAL_P || type == SURFACE_P)) {
+      type = SURFACE_P;
+      R dist = r_fabs(phi);
+      R div = (R)1.0 / (nl + (R)1.0e-15);
+      R dl[3] = {0, 0, 0};
+      for (int d = 0; d < D; d++) {
+        R nn = n[d] * div;
+        R nd = phi < (R)0 ? nn : -nn;
+        dl[d] = nd * dist;
+      }
+      P::add(c, p, key, dl);
+    } else {
+      type = REAL_P;
+    }
+    if (type == SURFACE_P) {  // Get_dispersed_position(0.00001*h), :385-404
+      R dx = (R)0.00001 * h;
+      R div = (R)1.0 / (nl + (R)1.0e-15);
+      R dl[3] = {0, 0, 0};
+      for (int d = 0; d < D; d++) {
+        R nn = n[d] * div;
+        R nd = phi < (R)0 ? nn : -nn;
+        dl[d] = nd * dx;
+      }
+      P::add(c, p, key, dl);
+    }
+    P::world(c, p, key, x);
+    ls_sample<D, R>(c.ls, x, phi, n, curv);
+    if (phi < (R)0 && type == REAL_P) {
+      // Remap_this_particle_to_positive_phase, sph_mesh_generation.cpp:1885-1928
+      atomicAdd(&c.sc->remap, 1u);
+      bool ok = false;
+      for (unsigned att = 0; att < max_att && !ok; att++) {
+        for (int d = 0; d < D; d++) {
+          U4 r = philox((uint32_t)id, c.sc->step, att, (RNG_REMAP << 8) | d, c.prm.seed);
+          double u1 = u53(r.v[0], r.v[1]), u2 = u53(r.v[2], r.v[3]);
+          double bl = c.prm.box_l[d], br = c.prm.box_r[d], box = br - bl;
+          double xd = u1 * box + u2 * 1.e-3 + bl;
+          x[d] = AMAX1(bl + 1.e-10, AMIN1(xd, br - 1.e-10));
+        }
+        ls_sample<D, R>(c.ls, x, phi, n, curv);
+        if (phi > h) ok = true;
+      }
+      if (!ok) atomicOr(&c.sc->flags, (unsigned)FLAG_REMAP);
+      P::set_world(c, p, key, x);
+      type = REAL_P;
+      set_info<D, R>(c, phi, h, rho);
+    }
+    // A4 Set_particle_scale (:361-381)
+    if (mode == MAP_STEP) set_info<D, R>(c, phi, h, rho);
+    // Particle_base::Set_particle_scale, particle.cpp:957-975 (scale = max_scale*2^-e)
+    {
+      R sc = (R)ldexp(c.geo.max_scale, -e);
+      R hc = h * (R)c.prm.cutoff;
+      for (int it = 0; it < 64; it++) {
+        if (hc > sc + (R)1.e-15) { sc *= 2; e--; }
+        else if (hc < sc / 2 - (R)1.e-15) { sc /= 2; e++; }
+        else break;
+      }
+    }
+    int L = e;
+    if (L < 0 || L >= c.geo.ncl) {
+      atomicOr(&c.sc->flags, (unsigned)FLAG_LEVEL);
+      L = max(0, min(L, c.geo.ncl - 1));
+      e = L;
+    }
+    int cc[3];
+    P::cell(c, L, p, key, cc);
+    int ck = (int)(c.geo.off[L] + ((long long)cc[2] * c.geo.n[L][1] + cc[1]) * c.geo.n[L][0] + cc[0]);
+    atomicAdd(&counts[ck], 1);
+    p.w = h;
+    b.posh[i] = p;
+    if (b.key) b.key[i] = key;
+    b.nr[i] = mk4<R>(n[0], n[1], n[2], rho);
+    b.meta[i] = type | ((e & 0xFF) << 8);
+    b.phi[i] = phi;
+    b.curv[i] = curv;
+    b.cellkey[i] = ck;
+    surf = (type == SURFACE_P) ? 1u : 0u;
+  }
+  unsigned ws = __popc(__ballot_sync(0xffffffffu, surf != 0));
+  if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&c.sc->nsurf, ws);
+}
+
+template <int D, class R>
+__global__ void k_reorder(Buf<R> src, Buf<R> dst, const int* __restrict__ perm2, int* __restrict__ slot_of_id,
+                          long long n, int partial) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int o = perm2[s];
+  dst.posh[s] = src.posh[o];
+  if (src.key) dst.key[s] = src.key[o];
+  dst.nr[s] = src.nr[o];
+  dst.meta[s] = src.meta[o];
+  int id = src.id[o];
+  dst.id[s] = id;
+  dst.nu[s] = src.nu_next[o];
+  dst.phi[s] = src.phi[o];
+  dst.curv[s] = src.curv[o];
+  dst.cellkey[s] = src.cellkey[o];
+  if (partial) {  // a step that stops before stage 2 keeps these consistent
+    dst.nu_next[s] = src.nu_next[o];
+    dst.v1[s] = src.v1[o];
+    dst.a2[s] = src.a2[o];
+  }
+  slot_of_id[id] = (int)s;
+}
+
+// Candidate cells of particle i (level Li, own cell ci) over all cell-list
+// levels, equivalent to the reference's tree walk (level_infor.cpp:407-506):
+//   L <= Li: 3^D cells around ci >> (Li-L) at level L (particles of level L;
+//            for L < Li these are the coarse particles whose walk finds i),
+//   L >  Li: the level-L cells under the 3^D level-Li cells around ci.
+// Each (z, y) row of cells is one contiguous range of the sorted arrays.
+template <int D, class F>
+__device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart, int Li, const int* ci, F&& f) {
+  for (int L = 0; L < c.geo.ncl; L++) {
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      int nL = c.geo.n[L][d];
+      if (L <= Li) {
+        int cc = ci[d] >> (Li - L);
+        lo[d] = max(cc - 1, 0);
+        hi[d] = min(cc + 1, nL - 1);
+      } else {
+        int k = L - Li;
+        lo[d] = max((ci[d] - 1) * (1 << k), 0);
+        hi[d] = min((ci[d] + 2) * (1 << k) - 1, nL - 1);
+      }
+    }
+    const long long off = c.geo.off[L];
+    for (int z = lo[2]; z <= hi[2]; z++)
+      for (int y = lo[1]; y <= hi[1]; y++) {
+        long long rb = off + ((long long)z * c.geo.n[L][1] + y) * c.geo.n[L][0];
+        int s = __ldg(&cstart[rb + lo[0]]), e = __ldg(&cstart[rb + hi[0] + 1]);
+        for (int j = s; j < e; j++) f(j);
+      }
+  }
+}
+
+// Neighbour criterion, level_infor.cpp:491-500.
+__device__ inline bool nb_test(double d2, double hi, double hj, double cutoff, double& dist) {
+  double R = fmax(hi, hj) * cutoff + 1.e-10;
+  if (d2 > R * R * (1.0 + 1.e-9)) return false;  // conservative pre-reject
+  dist = sqrt(d2);
+  return (dist <= (hi * cutoff + 1.e-10)) || (dist <= (hj * cutoff + 1.e-10));
+}
+__device__ inline bool nb_test(float d2, float hi, float hj, double cutoff, float& dist) {
+  float R = fmaxf(hi, hj) * (float)cutoff;
+  if (d2 > R * R) return false;
+  dist = sqrtf(d2);
+  return true;
+}
+
+// A6 + A7: Refresh_neighbor_info (level_infor.cpp:469-506) and
+// Get_kernel_summation (particle_mesh_generation.cpp:690-765).
+template <int D, class R>
+__global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
+  using P = PosOps<D, R>;
+  using T4 = typename V4<R>::T;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long pairs = 0;
+  if (i < c.n) {
+    const T4 pi = b.posh[i];
+    const int ki = b.key ? b.key[i] : 0;
+    const int mi = b.meta[i];
+    const int ti = mi & 0xFF;
+    const int Li = (int)(signed char)((mi >> 8) & 0xFF);
+    const T4 nri = b.nr[i];
+    const R ni[3] = {nri.x, nri.y, nri.z};
+    const R hi = pi.w;
+    const R cos_t = (R)c.prm.cos_thres;
+    int ci[3];
+    P::cell(c, Li, pi, ki, ci);
+    R sum = 0;
+    int ncount = 0, cnt = 0;
+    const long long n = c.n;
+    scan_candidates<D>(c, w.cstart, Li, ci, [&](int j) {
+      const T4 pj = b.posh[j];
+      const int kj = b.key ? b.key[j] : 0;
+      R dr[3];
+      P::rel(c, pi, ki, pj, kj, dr);
+      R d2 = 0;
+      d2 += dr[0] * dr[0];
+      d2 += dr[1] * dr[1];
+      if (D == 3) d2 += dr[2] * dr[2];
+      R dist;
+      if (!nb_test(d2, hi, pj.w, c.prm.cutoff, dist)) return;
+      if (cnt < w.cap) w.nbl[(long long)cnt * n + i] = j;
+      cnt++;
+      if (ti == REAL_P) {
+        sum += kernel_W<R>(c.prm.kernel, D, dist, hi);
+        ncount++;
+      } else if (ti == SURFACE_P) {
+        const int tj = b.meta[j] & 0xFF;
+        R dn = dot3<D, R>(dr, ni);
+        R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
+        R pd = r_sqrt(dot3<D, R>(pr, pr));
+        if (tj == SURFACE_P) {
+          const T4 nrj = b.nr[j];
+          const R nj[3] = {nrj.x, nrj.y, nrj.z};
+          if (r_fabs(dot3<D, R>(ni, nj)) > cos_t) {
+            sum += kernel_W<R>(c.prm.kernel, D - 1, pd, hi);
+            ncount++;
+          }
+        } else if (tj == SEGMENT_P || tj == SINGULARITY_P) {
+          sum += kernel_W<R>(c.prm.kernel, D - 1, pd, hi);
+          ncount++;
+        }
+      }
+    });
+    if (ncount > 1) sum = (R)1. / (sum + (R)1.e-15);
+    w.sum[i] = sum;
+    w.cnt[i] = cnt;
+    if (cnt > w.cap) atomicOr(&c.sc->flags, (unsigned)FLAG_SPILL);
+    pairs = (unsigned long long)(cnt - 1);
+  }
+  unsigned mc = (unsigned)(pairs + 1);
+  for (int o = 16; o > 0; o >>= 1) mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+  if ((threadIdx.x & 31) == 0 && mc > 1) atomicMax(&c.sc->maxcnt, mc);
+  block_sum_u64_to_global(pairs, &c.sc->pairs);
+}
+
+static __global__ void k_accum_pairs(DevScalars* sc) { sc->pairs_total += sc->pairs; }
+
+// A8 force stages + A9 timestep (Set_timestep(stage), particle_mesh_generation.cpp:127-145)
+template <int D, class R, int STAGE>
+__global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
+  using P = PosOps<D, R>;
+  using T4 = typename V4<R>::T;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double my_dt = 1.e300, my_v = 0.0;
+  if (i < c.n) {
+    const long long n = c.n;
+    const T4 pi = b.posh[i];
+    const int ki = b.key ? b.key[i] : 0;
+    const int mi = b.meta[i];
+    const int ti = mi & 0xFF;
+    const T4 nri = b.nr[i];
+    const R ni[3] = {nri.x, nri.y, nri.z};
+    const R rho = nri.w, h = pi.w;
+    const R cos_t = (R)c.prm.cos_thres;
+    const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
+    const R nu = (STAGE == 2) ? b.nu[i] : (R)0;
+    R hdt1 = 0;
+    R vi[3] = {0, 0, 0};
+    if (STAGE == 2) {
+      hdt1 = (R)(0.5 * bitsd(c.sc->dt1));
+      T4 a1 = w.a1[i];
+      vi[0] = a1.x * hdt1; vi[1] = a1.y * hdt1; vi[2] = a1.z * hdt1;
+    }
+    R F[3] = {0, 0, 0};
+    const R vol_i = (R)1.0 / (rho * rho);
+    auto pair = [&](int j) {
+      if (j == (int)i) return;
+      const int tj = b.meta[j] & 0xFF;
+      if (ti == SURFACE_P && tj == REAL_P) return;
+      const T4 pj = b.posh[j];
+      const int kj = b.key ? b.key[j] : 0;
+      const T4 nrj = b.nr[j];
+      R vec[3];
+      P::rel(c, pi, ki, pj, kj, vec);
+      R dr[3], aw;
+      const R hij = (R)0.5 * (h + pj.w);
+      if (ti == REAL_P) {
+        dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
+        R dist = r_sqrt(dot3<D, R>(dr, dr));
+        aw = kernel_dW<R>(c.prm.kernel, D, dist, hij);
+      } else {
+        R dn = dot3<D, R>(vec, ni);
+        dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
+        R dist = r_sqrt(dot3<D, R>(dr, dr));
+        if (tj == SURFACE_P) {
+          const R nj[3] = {nrj.x, nrj.y, nrj.z};
+          if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return;
+        }
+        aw = kernel_dW<R>(c.prm.kernel, D - 1, dist, hij);
+      }
+      const R rho_j = nrj.w;
+      if (STAGE == 1) {
+        const R vol_j = (R)1.0 / (rho_j * rho_j);
+        const R P_ij = sum * (vol_i + vol_j);
+        for (int d = 0; d < D; d++) F[d] = F[d] + (dr[d] * aw) * -P_ij;
+      } else {
+        R vj[3];
+        if (ti == REAL_P && tj != REAL_P) {
+          vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
+        } else {
+          T4 a1j = w.a1[j];
+          vj[0] = a1j.x * hdt1; vj[1] = a1j.y * hdt1; vj[2] = a1j.z * hdt1;
+        }
+        const R nu_j = b.nu[j];
+        const R eta_i = nu * rho, eta_j = nu_j * rho_j;
+        const R eta_ij = (R)2. * eta_j * eta_i / (eta_i + eta_j + (R)1.e-15);
+        const R temp0 = aw * eta_ij * ((R)1. / rho / rho + (R)1. / rho_j / rho_j);
+        for (int d = 0; d < D; d++) F[d] = F[d] + (vi[d] - vj[d]) * temp0;
+      }
+    };
+    if (ti == REAL_P || ti == SURFACE_P) {
+      const int cnt = w.cnt[i];
+      if (cnt <= w.cap) {
+        for (int q = 0; q < cnt; q++) pair(__ldg(&w.nbl[(long long)q * n + i]));
+      } else {
+        const int Li = (int)(signed char)((mi >> 8) & 0xFF);
+        int ci[3];
+        P::cell(c, Li, pi, ki, ci);
+        scan_candidates<D>(c, w.cstart, Li, ci, [&](int j) {
+          const T4 pj = b.posh[j];
+          const int kj = b.key ? b.key[j] : 0;
+          R dr[3];
+          P::rel(c, pi, ki, pj, kj, dr);
+          R d2 = 0;
+          d2 += dr[0] * dr[0];
+          d2 += dr[1] * dr[1];
+          if (D == 3) d2 += dr[2] * dr[2];
+          R dist;
+          if (nb_test(d2, h, pj.w, c.prm.cutoff, dist)) pair(j);
+        });
+      }
+    }
+    R a[3] = {0, 0, 0};
+    if (ti == REAL_P || ti == SURFACE_P) {
+      for (int d = 0; d < D; d++) a[d] = F[d];
+      if (STAGE == 2)
+        for (int d = 0; d < D; d++) a[d] = a[d] + vi[d] * (R)c.prm.damp_coeff;
+      if (ti == SURFACE_P) {  // Map_surface_particle_force, :1122-1126
+        R nf = dot3<D, R>(a, ni);
+        for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
+      }
+    }
+    R U = r_sqrt(dot3<D, R>(vi, vi));
+    R A = r_sqrt(dot3<D, R>(a, a));
+    R ts = (R)0.25 * r_sqrt(h / (A + (R)1.e-15));
+    ts = AMIN1(ts, h / (R)40. / (U + (R)1.e-15));
+    if (STAGE == 2) {
+      R nu_new = (R)c.prm.nu_coeff * h * U;
+      ts = AMIN1(ts, (R)0.125 * h * h / (nu_new + (R)1.e-15));
+      b.nu_next[i] = nu_new;
+      b.v1[i] = mk4<R>(vi[0], vi[1], vi[2], U);
+      b.a2[i] = mk4<R>(a[0], a[1], a[2], 0);
+    } else {
+      w.a1[i] = mk4<R>(a[0], a[1], a[2], 0);
+    }
+    my_dt = (double)ts;
+    my_v = (double)U;
+  }
+  if (STAGE == 1) block_minmax_to_global(my_dt, my_v, &c.sc->dt1, &c.sc->vmax1);
+  else block_minmax_to_global(my_dt, my_v, &c.sc->dt2, &c.sc->vmax2);
+}
+
+// ----------------------------------------------------------------- taps
+template <int D, class R>
+__global__ void k_tap(KCtx c, Buf<R> b, Work<R> w, const int* __restrict__ slot_of_id, double* out, int field,
+                      int have_work) {
+  using P = PosOps<D, R>;
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  int s = slot_of_id[k];
+  double* o3 = out + 3 * k;
+  switch (field) {
+    case 0: { double x[3]; P::world(c, b.posh[s], b.key ? b.key[s] : 0, x); o3[0] = x[0]; o3[1] = x[1]; o3[2] = x[2]; break; }
+    case 1: {  // velocity after the last complete step
+      double dt2 = bitsd(c.sc->dt2);
+      auto v1 = b.v1[s]; auto a2 = b.a2[s];
+      R hdt = (R)(0.5 * dt2);
+      o3[0] = (double)(v1.x + a2.x * hdt); o3[1] = (double)(v1.y + a2.y * hdt);
+      o3[2] = (D == 3) ? (double)(v1.z + a2.z * hdt) : 0.0;
+      break;
+    }
+    case 2: { auto q = b.nr[s]; o3[0] = q.x; o3[1] = q.y; o3[2] = q.z; break; }
+    case 3: { auto q = have_work ? w.a1[s] : mk4<R>(0, 0, 0, 0); o3[0] = q.x; o3[1] = q.y; o3[2] = q.z; break; }
+    case 4: { auto q = b.a2[s]; o3[0] = q.x; o3[1] = q.y; o3[2] = q.z; break; }
+    case 5: out[k] = (double)b.posh[s].w; break;
+    case 6: out[k] = (double)b.phi[s]; break;
+    case 7: out[k] = (double)b.curv[s]; break;
+    case 8: out[k] = have_work ? (double)w.sum[s] : 0.0; break;
+    case 9: out[k] = (double)b.nr[s].w; break;
+    case 10: out[k] = (double)b.nu_next[s]; break;
+    case 11: out[k] = (double)(b.meta[s] & 0xFF); break;
+    case 12: out[k] = (double)(signed char)((b.meta[s] >> 8) & 0xFF); break;
+  }
+}
+
+template <int D, class R>
+__global__ void k_upload(KCtx c, Buf<R> b, const double* __restrict__ xyz) {
+  using P = PosOps<D, R>;
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= c.n) return;
+  int id = b.id[s];
+  double x[3] = {xyz[3 * (long long)id], xyz[3 * (long long)id + 1], xyz[3 * (long long)id + 2]};
+  auto p = b.posh[s];
+  int key = b.key ? b.key[s] : 0;
+  P::set_world(c, p, key, x);
+  b.posh[s] = p;
+  if (b.key) b.key[s] = key;
+}
+
+template <int D, class R>
+__global__ void k_set_state(KCtx c, Buf<R> b, const double* __restrict__ in, int has_v, int has_h, int has_nu,
+                            int has_level, const int* __restrict__ type, const int* __restrict__ level) {
+  using P = PosOps<D, R>;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  const long long n = c.n;
+  double x[3] = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+  typename V4<R>::T p = mk4<R>(0, 0, 0, has_h ? (R)in[9 * n + i] : (R)0);
+  int key = 0;
+  P::set_world(c, p, key, x);
+  b.posh[i] = p;
+  if (b.key) b.key[i] = key;
+  R v[3] = {0, 0, 0};
+  if (has_v) for (int d = 0; d < 3; d++) v[d] = (R)in[3 * n + 3 * i + d];
+  b.v1[i] = mk4<R>(v[0], v[1], v[2], 0);
+  b.a2[i] = mk4<R>(0, 0, 0, 0);
+  R nu = has_nu ? (R)in[6 * n + i] : (R)0;
+  b.nu[i] = nu;
+  b.nu_next[i] = nu;
+  int t = type ? type[i] : REAL_P;
+  int e = has_level ? level[i] : 0;
+  b.meta[i] = t | ((e & 0xFF) << 8);
+  b.id[i] = (int)i;
+  b.nr[i] = mk4<R>(0, 0, 0, 0);
+  b.phi[i] = 0;
+  b.curv[i] = 0;
+}
+
+static __global__ void k_iota(int* a, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = (int)i;
+}
+
+template <int D, class R>
+__global__ void k_sample_points(KCtx c, long long n, const double* __restrict__ xyz, double* out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  R phi, nn[3], curv;
+  ls_sample<D, R>(c.ls, x, phi, nn, curv);
+  out[6 * i + 0] = phi;
+  out[6 * i + 1] = nn[0];
+  out[6 * i + 2] = nn[1];
+  out[6 * i + 3] = nn[2];
+  out[6 * i + 4] = curv;
+  out[6 * i + 5] = (double)ls_tag<D>(c.ls, x);
+}
+
+// ---------------------------------------------------------------------------
+// host engine
+// ---------------------------------------------------------------------------
+#define MR_CK(call)                                                                     \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);                         \
+      return MRSPH_ERR_CUDA;                                                            \
+    }                                                                                   \
+  } while (0)
+
+template <int D, class R>
+class Engine : public EngineBase {
+  using T4 = typename V4<R>::T;
+
+ public:
+  explicit Engine(const EngineConfig& cfg) : cfg_(cfg) {
+    kc_.prm = cfg.prm;
+    kc_.geo = cfg.geo;
+    kc_.ls = cfg.ls;
+    kc_.n = 0;
+    kc_.sc = nullptr;
+    st_ = cfg.stream;
+  }
+  ~Engine() override { release(); }
+
+  int seed(long long n) override {
+    int rc = alloc(n);
+    if (rc) return rc;
+    MR_CK(cudaMemsetAsync(kc_.sc, 0, sizeof(DevScalars), st_));
+    k_seed<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], 1000000u);
+    MR_CK(cudaGetLastError());
+    return pre_run();
+  }
+
+  int set_state(long long n, const mrsph_state_in* s, int pre) override {
+    int rc = alloc(n);
+    if (rc) return rc;
+    std::vector<double> host((size_t)10 * n, 0.0);
+    for (long long i = 0; i < 3 * n; i++) host[i] = s->xyz[i];
+    if (s->v) for (long long i = 0; i < 3 * n; i++) host[3 * n + i] = s->v[i];
+    if (s->nu) for (long long i = 0; i < n; i++) host[6 * n + i] = s->nu[i];
+    if (s->h) for (long long i = 0; i < n; i++) host[9 * n + i] = s->h[i];
+    double* dbuf = nullptr;
+    int* dint = nullptr;
+    MR_CK(cudaMalloc(&dbuf, sizeof(double) * 10 * n));
+    MR_CK(cudaMalloc(&dint, sizeof(int) * 2 * n));
+    MR_CK(cudaMemcpyAsync(dbuf, host.data(), sizeof(double) * 10 * n, cudaMemcpyHostToDevice, st_));
+    if (s->type) MR_CK(cudaMemcpyAsync(dint, s->type, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
+    if (s->level) MR_CK(cudaMemcpyAsync(dint + n, s->level, sizeof(int) * n, cudaMemcpyHostToDevice, st_));
+    MR_CK(cudaMemsetAsync(kc_.sc, 0, sizeof(DevScalars), st_));
+    k_set_state<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], dbuf, s->v != nullptr, s->h != nullptr,
+                                                 s->nu != nullptr, s->level != nullptr,
+                                                 s->type ? dint : nullptr, dint + n);
+    MR_CK(cudaGetLastError());
+    DevScalars h{};
+    h.dt2 = dbits_host(s->dt);
+    h.step = (unsigned)s->step;
+    MR_CK(cudaMemcpyAsync(kc_.sc, &h, sizeof(h), cudaMemcpyHostToDevice, st_));
+    k_iota<<<grid(n), 256, 0, st_>>>(w_.slot_of_id, n);
+    MR_CK(cudaStreamSynchronize(st_));
+    cudaFree(dbuf);
+    cudaFree(dint);
+    have_work_ = false;
+    if (pre) return pre_run();
+    return 0;  // state stays in id order (slot_of_id = identity) until the next step
+  }
+
+  int run_phase(int phase) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    int rc = launch_step(phase);
+    if (rc) return rc;
+    MR_CK(cudaStreamSynchronize(st_));
+    MR_CK(cudaGetLastError());
+    return 0;
+  }
+
+  // Graph replay.  The neighbour-list capacity follows the largest list
+  // seen: every 32 steps (and on the first call) the device max count is read
+  // and the list grown, within a memory budget; particles whose list does not
+  // fit are handled by re-scanning their cells in the force kernels.
+  int step(int nsteps) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    if (nsteps <= 0) return 0;
+    for (int k = 0; k < nsteps; k++) {
+      int rc = build_graphs();
+      if (rc) return rc;
+      MR_CK(cudaGraphLaunch(graph_[cur_], st_));
+      cur_ ^= 1;
+      have_work_ = true;
+      if (--countdown_ <= 0) {
+        rc = maybe_grow_cap();
+        if (rc) return rc;
+        countdown_ = 32;
+      }
+    }
+    return 0;
+  }
+
+  // Reads the largest neighbour count of the last step and grows the list
+  // capacity (graphs are rebuilt).  Stays with the re-scan fallback when the
+  // allocation fails or exceeds the budget, or when the caller fixed the cap.
+  int maybe_grow_cap() {
+    unsigned mc = 0;
+    MR_CK(cudaMemcpyAsync(&mc, &kc_.sc->maxcnt, sizeof(unsigned), cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaStreamSynchronize(st_));
+    if ((int)mc <= w_.cap || cfg_.neighbor_cap > 0) return 0;
+    long long want = ((long long)mc * 5 / 4 + 31) / 32 * 32;
+    const long long budget = 24ll << 30;  // bytes for the list
+    long long maxcap = budget / (4 * n_);
+    if (want > maxcap) want = maxcap;
+    if (want <= w_.cap) return 0;
+    int* nb = nullptr;
+    cudaError_t e = cudaMalloc(&nb, sizeof(int) * (size_t)want * n_);
+    if (e != cudaSuccess) { cudaGetLastError(); return 0; }
+    for (auto& p : allocs_)
+      if (p == w_.nbl) { cudaFree(p); p = nb; }
+    w_.nbl = nb;
+    w_.cap = (int)want;
+    for (int p = 0; p < 2; p++)
+      if (graph_[p]) { cudaGraphExecDestroy(graph_[p]); graph_[p] = nullptr; }
+    return 0;
+  }
+
+  int build_graphs() {
+    for (int p = 0; p < 2; p++) {
+      if (!graph_[p]) {
+        int saved = cur_;
+        cur_ = p;
+        MR_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_step(MRSPH_PHASE_FORCE2);
+        cudaGraph_t g;
+        cudaError_t ee = cudaStreamEndCapture(st_, &g);
+        cur_ = saved;
+        if (rc) return rc;
+        if (ee != cudaSuccess) { err = cudaGetErrorString(ee); return MRSPH_ERR_CUDA; }
+        MR_CK(cudaGraphInstantiate(&graph_[p], g, 0));
+        cudaGraphDestroy(g);
+      }
+    }
+    return 0;
+  }
+
+  int stats(mrsph_stats* o) override {
+    DevScalars h;
+    MR_CK(cudaMemcpyAsync(&h, kc_.sc, sizeof(h), cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaStreamSynchronize(st_));
+    unsigned zero = 0;
+    MR_CK(cudaMemcpy(&kc_.sc->flags, &zero, sizeof(unsigned), cudaMemcpyHostToDevice));
+    o->dt = bitsd_host(h.dt2);
+    o->dt_stage1 = bitsd_host(h.dt1);
+    o->max_v = bitsd_host(h.vmax2);
+    o->step = h.step;
+    o->n = n_;
+    o->n_surface = h.nsurf;
+    o->pairs = (long long)h.pairs;
+    o->pairs_total = (long long)h.pairs_total;
+    o->remapped = h.remap;
+    o->flags = (int)h.flags;
+    o->num_cell_levels = kc_.geo.ncl;
+    o->num_cells = kc_.geo.off[kc_.geo.ncl];
+    o->max_phi = kc_.ls.max_phi;
+    return 0;
+  }
+
+  int get_particles(const mrsph_particle_view* v) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    struct F { void* p; int field; int vec; bool isint; };
+    F fs[] = {{v->xyz, 0, 1, false}, {v->v, 1, 1, false}, {v->norm, 2, 1, false}, {v->a1, 3, 1, false},
+              {v->a2, 4, 1, false}, {v->h, 5, 0, false}, {v->phi, 6, 0, false}, {v->curv, 7, 0, false},
+              {v->sum, 8, 0, false}, {v->rho, 9, 0, false}, {v->nu, 10, 0, false}, {v->type, 11, 0, true},
+              {v->level, 12, 0, true}};
+    std::vector<double> host((size_t)3 * n_);
+    for (auto& f : fs) {
+      if (!f.p) continue;
+      k_tap<D, R><<<grid(n_), 256, 0, st_>>>(kc_, buf_[cur_], w_, w_.slot_of_id, stage_, f.field, have_work_);
+      MR_CK(cudaGetLastError());
+      size_t cnt = (size_t)(f.vec ? 3 : 1) * n_;
+      MR_CK(cudaMemcpyAsync(host.data(), stage_, sizeof(double) * cnt, cudaMemcpyDeviceToHost, st_));
+      MR_CK(cudaStreamSynchronize(st_));
+      if (f.isint) {
+        int* o = (int*)f.p;
+        for (size_t k = 0; k < cnt; k++) o[k] = (int)host[k];
+      } else {
+        std::memcpy(f.p, host.data(), sizeof(double) * cnt);
+      }
+    }
+    return 0;
+  }
+
+  int get_cells(int* level_cell, int* sorted_ids) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    std::vector<int> ck(n_), ids(n_);
+    MR_CK(cudaMemcpyAsync(ck.data(), buf_[cur_].cellkey, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaMemcpyAsync(ids.data(), buf_[cur_].id, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaStreamSynchronize(st_));
+    if (sorted_ids) std::memcpy(sorted_ids, ids.data(), sizeof(int) * n_);
+    if (level_cell) {
+      for (long long s = 0; s < n_; s++) {
+        long long key = ck[s];
+        int L = 0;
+        while (L + 1 < kc_.geo.ncl && key >= kc_.geo.off[L + 1]) L++;
+        long long r = key - kc_.geo.off[L];
+        int cx = (int)(r % kc_.geo.n[L][0]);
+        r /= kc_.geo.n[L][0];
+        int cy = (int)(r % kc_.geo.n[L][1]);
+        int cz = (int)(r / kc_.geo.n[L][1]);
+        int* o = level_cell + 4 * (long long)ids[s];
+        o[0] = L; o[1] = cx; o[2] = cy; o[3] = cz;
+      }
+    }
+    return 0;
+  }
+
+  int get_neighbors(long long* off, int* nb, long long cap, long long* total) override {
+    if (!have_work_) { err = "no density phase has run"; return MRSPH_ERR_STATE; }
+    std::vector<int> cnt(n_), ids(n_);
+    MR_CK(cudaMemcpyAsync(cnt.data(), w_.cnt, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaMemcpyAsync(ids.data(), buf_[cur_].id, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaStreamSynchronize(st_));
+    long long tot = 0;
+    std::vector<long long> byid_cnt(n_);
+    for (long long s = 0; s < n_; s++) {
+      if (cnt[s] > w_.cap) { err = "neighbour list spilled; raise neighbor_cap"; return MRSPH_ERR_RANGE; }
+      byid_cnt[ids[s]] = cnt[s];
+      tot += cnt[s];
+    }
+    if (total) *total = tot;
+    if (!nb) return 0;
+    if (cap < tot || !off) { err = "neighbour buffer too small"; return MRSPH_ERR_ARG; }
+    std::vector<int> nbl((size_t)w_.cap * n_);
+    MR_CK(cudaMemcpy(nbl.data(), w_.nbl, sizeof(int) * (size_t)w_.cap * n_, cudaMemcpyDeviceToHost));
+    off[0] = 0;
+    for (long long k = 0; k < n_; k++) off[k + 1] = off[k] + byid_cnt[k];
+    for (long long s = 0; s < n_; s++) {
+      long long base = off[ids[s]];
+      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nbl[(size_t)q * n_ + s]];
+      std::sort(nb + base, nb + base + cnt[s]);
+    }
+    return 0;
+  }
+
+  int upload_positions(const double* xyz) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    MR_CK(cudaMemcpyAsync(stage_, xyz, sizeof(double) * 3 * n_, cudaMemcpyHostToDevice, st_));
+    k_upload<D, R><<<grid(n_), 256, 0, st_>>>(kc_, buf_[cur_], stage_);
+    MR_CK(cudaGetLastError());
+    return 0;
+  }
+
+  int download_positions(double* xyz) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    k_tap<D, R><<<grid(n_), 256, 0, st_>>>(kc_, buf_[cur_], w_, w_.slot_of_id, stage_, 0, have_work_);
+    MR_CK(cudaGetLastError());
+    MR_CK(cudaMemcpyAsync(xyz, stage_, sizeof(double) * 3 * n_, cudaMemcpyDeviceToHost, st_));
+    MR_CK(cudaStreamSynchronize(st_));
+    return 0;
+  }
+
+  int sample(long long n, const double* xyz, double* phi, double* norm, double* curv, int* tag) override {
+    double *din = nullptr, *dout = nullptr;
+    MR_CK(cudaMalloc(&din, sizeof(double) * 3 * n));
+    MR_CK(cudaMalloc(&dout, sizeof(double) * 6 * n));
+    MR_CK(cudaMemcpyAsync(din, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st_));
+    k_sample_points<D, R><<<grid(n), 256, 0, st_>>>(kc_, n, din, dout);
+    std::vector<double> h((size_t)6 * n);
+    cudaError_t e = cudaMemcpyAsync(h.data(), dout, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    cudaFree(din);
+    cudaFree(dout);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return MRSPH_ERR_CUDA; }
+    for (long long i = 0; i < n; i++) {
+      if (phi) phi[i] = h[6 * i];
+      if (norm) for (int d = 0; d < 3; d++) norm[3 * i + d] = h[6 * i + 1 + d];
+      if (curv) curv[i] = h[6 * i + 4];
+      if (tag) tag[i] = (int)h[6 * i + 5];
+    }
+    return 0;
+  }
+
+ private:
+  static unsigned long long dbits_host(double x) { unsigned long long u; std::memcpy(&u, &x, 8); return u; }
+  static double bitsd_host(unsigned long long u) { double x; std::memcpy(&x, &u, 8); return x; }
+  static int grid(long long n) { return (int)((n + 255) / 256); }
+
+  int pre_run() {
+    k_begin_step<<<1, 1, 0, st_>>>(kc_.sc, 0);
+    int rc = run_map_and_bin(MAP_PRE);
+    if (rc) return rc;
+    MR_CK(cudaStreamSynchronize(st_));
+    have_work_ = false;
+    return 0;
+  }
+
+  // map (mode) + counting sort + reorder; swaps cur_.
+  int run_map_and_bin(int mode) {
+    const long long n = n_;
+    k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, mode, 1000000u);
+    MR_CK(cudaGetLastError());
+    return bin(1);
+  }
+
+  int bin(int partial) {
+    const long long n = n_;
+    cell_scan(w_.counts, w_.cstart, w_.blocksums, ncells_, (int)n, st_);
+    cell_scatter(buf_[cur_].cellkey, w_.counts, w_.cstart, w_.perm, n, st_);
+    cell_rank(buf_[cur_].cellkey, w_.cstart, w_.perm, buf_[cur_].id, w_.perm2, n, st_);
+    k_reorder<D, R><<<grid(n), 256, 0, st_>>>(buf_[cur_], buf_[cur_ ^ 1], w_.perm2, w_.slot_of_id, n, partial);
+    MR_CK(cudaGetLastError());
+    cur_ ^= 1;
+    return 0;
+  }
+
+  // ev (optional, 8 events) brackets the timer phases MRSPH_TIMER_*.
+  int launch_step(int phase, cudaEvent_t* ev = nullptr) {
+    const long long n = n_;
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st_); };
+    mark(0);
+    k_begin_step<<<1, 1, 0, st_>>>(kc_.sc, 1);
+    k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, MAP_STEP, 1000000u);
+    MR_CK(cudaGetLastError());
+    mark(1);
+    if (phase < MRSPH_PHASE_BIN) return 0;
+    cell_scan(w_.counts, w_.cstart, w_.blocksums, ncells_, (int)n, st_);
+    mark(2);
+    cell_scatter(buf_[cur_].cellkey, w_.counts, w_.cstart, w_.perm, n, st_);
+    cell_rank(buf_[cur_].cellkey, w_.cstart, w_.perm, buf_[cur_].id, w_.perm2, n, st_);
+    mark(3);
+    k_reorder<D, R><<<grid(n), 256, 0, st_>>>(buf_[cur_], buf_[cur_ ^ 1], w_.perm2, w_.slot_of_id, n,
+                                              phase < MRSPH_PHASE_FORCE2 ? 1 : 0);
+    MR_CK(cudaGetLastError());
+    cur_ ^= 1;
+    mark(4);
+    if (phase < MRSPH_PHASE_DENSITY) return 0;
+    k_density<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    k_accum_pairs<<<1, 1, 0, st_>>>(kc_.sc);
+    have_work_ = true;
+    mark(5);
+    if (phase < MRSPH_PHASE_FORCE1) return 0;
+    k_force<D, R, 1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    mark(6);
+    if (phase < MRSPH_PHASE_FORCE2) return 0;
+    k_force<D, R, 2><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    mark(7);
+    MR_CK(cudaGetLastError());
+    return 0;
+  }
+
+ public:
+  int step_timed(int nsteps, double* ms) override {
+    cudaEvent_t a, b;
+    MR_CK(cudaEventCreate(&a));
+    MR_CK(cudaEventCreate(&b));
+    int rc = 0;
+    if (have_work_) rc = maybe_grow_cap();  // settle the list capacity first
+    if (!rc) rc = build_graphs();            // instantiate outside the timed region
+    if (rc) return rc;
+    const int saved = countdown_;
+    countdown_ = 1 << 30;                    // no capacity checks while timing
+    MR_CK(cudaEventRecord(a, st_));
+    rc = step(nsteps);
+    MR_CK(cudaEventRecord(b, st_));
+    countdown_ = saved;
+    MR_CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    MR_CK(cudaEventElapsedTime(&f, a, b));
+    *ms = f;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+  }
+
+  int profile_steps(int nsteps, double* phase_ms, int nphase) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    cudaEvent_t ev[8];
+    for (int k = 0; k < 8; k++) MR_CK(cudaEventCreate(&ev[k]));
+    double acc[8] = {0};
+    for (int s = 0; s < nsteps; s++) {
+      int rc = launch_step(MRSPH_PHASE_FORCE2, ev);
+      if (rc) return rc;
+      MR_CK(cudaEventSynchronize(ev[7]));
+      for (int k = 0; k < 7; k++) {
+        float f = 0.f;
+        MR_CK(cudaEventElapsedTime(&f, ev[k], ev[k + 1]));
+        acc[k] += f;
+      }
+    }
+    for (int k = 0; k < nphase && k < 7; k++) phase_ms[k] = acc[k] / (nsteps > 0 ? nsteps : 1);
+    for (int k = 0; k < 8; k++) cudaEventDestroy(ev[k]);
+    return 0;
+  }
+
+ private:
+
+  int alloc(long long n) {
+    if (n <= 0 || n > (1ll << 30)) { err = "particle count out of range"; return MRSPH_ERR_RANGE; }
+    release();
+    n_ = n;
+    kc_.n = n;
+    ncells_ = kc_.geo.off[kc_.geo.ncl];
+    int cap = cfg_.neighbor_cap > 0 ? cfg_.neighbor_cap : (D == 2 ? 64 : 192);
+    w_.cap = cap;
+    auto A = [&](void** p, size_t bytes) -> int {
+      cudaError_t e = cudaMalloc(p, bytes);
+      if (e != cudaSuccess) { err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return MRSPH_ERR_OOM; }
+      allocs_.push_back(*p);
+      return 0;
+    };
+    int rc = 0;
+    for (int k = 0; k < 2 && !rc; k++) {
+      Buf<R>& b = buf_[k];
+      rc |= A((void**)&b.posh, sizeof(T4) * n);
+      rc |= A((void**)&b.nr, sizeof(T4) * n);
+      rc |= A((void**)&b.v1, sizeof(T4) * n);
+      rc |= A((void**)&b.a2, sizeof(T4) * n);
+      if (sizeof(R) == 4) rc |= A((void**)&b.key, sizeof(int) * n); else b.key = nullptr;
+      rc |= A((void**)&b.meta, sizeof(int) * n);
+      rc |= A((void**)&b.id, sizeof(int) * n);
+      rc |= A((void**)&b.nu, sizeof(R) * n);
+      rc |= A((void**)&b.nu_next, sizeof(R) * n);
+      rc |= A((void**)&b.phi, sizeof(R) * n);
+      rc |= A((void**)&b.curv, sizeof(R) * n);
+      rc |= A((void**)&b.cellkey, sizeof(int) * n);
+    }
+    if (!rc) {
+      rc |= A((void**)&w_.sum, sizeof(R) * n);
+      rc |= A((void**)&w_.a1, sizeof(T4) * n);
+      rc |= A((void**)&w_.cnt, sizeof(int) * n);
+      rc |= A((void**)&w_.nbl, sizeof(int) * (size_t)cap * n);
+      rc |= A((void**)&w_.counts, sizeof(int) * ncells_);
+      rc |= A((void**)&w_.cstart, sizeof(int) * (ncells_ + 1));
+      rc |= A((void**)&w_.perm, sizeof(int) * n);
+      rc |= A((void**)&w_.perm2, sizeof(int) * n);
+      rc |= A((void**)&w_.blocksums, sizeof(int) * scan_blocksums_size(ncells_));
+      rc |= A((void**)&w_.slot_of_id, sizeof(int) * n);
+      rc |= A((void**)&stage_, sizeof(double) * 3 * n);
+      rc |= A((void**)&kc_.sc, sizeof(DevScalars));
+    }
+    if (rc) { release(); return rc; }
+    MR_CK(cudaMemsetAsync(w_.counts, 0, sizeof(int) * ncells_, st_));
+    MR_CK(cudaMemsetAsync(w_.cnt, 0, sizeof(int) * n, st_));
+    MR_CK(cudaMemsetAsync(kc_.sc, 0, sizeof(DevScalars), st_));
+    cur_ = 0;
+    countdown_ = 0;
+    return 0;
+  }
+
+  void release() {
+    for (int p = 0; p < 2; p++)
+      if (graph_[p]) { cudaGraphExecDestroy(graph_[p]); graph_[p] = nullptr; }
+    for (void* p : allocs_) cudaFree(p);
+    allocs_.clear();
+    n_ = 0;
+    kc_.n = 0;
+    kc_.sc = nullptr;
+    stage_ = nullptr;
+  }
+
+  EngineConfig cfg_;
+  KCtx kc_;
+  cudaStream_t st_;
+  Buf<R> buf_[2]{};
+  Work<R> w_{};
+  double* stage_ = nullptr;
+  long long n_ = 0, ncells_ = 0;
+  int cur_ = 0;
+  bool have_work_ = false;
+  int countdown_ = 0;
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  std::vector<void*> allocs_;
+};
+
+}  // namespace mrsph

@@ -1,0 +1,57 @@
+// engine_iface.h — host-side interface between the C ABI (mrsph_api.cu) and
+// the precision-specific engines (mrsph_fp64.cu, mrsph_fp32.cu).
+#pragma once
+#include <string>
+
+#include "../../include/mrsph_relax.h"
+#include "mrsph_common.cuh"
+
+namespace mrsph {
+
+struct EngineConfig {
+  Params prm;
+  CellGeo geo;
+  LsSet ls;            // device pointers of the built level set
+  int neighbor_cap;
+  cudaStream_t stream;
+};
+
+class EngineBase {
+ public:
+  virtual ~EngineBase() {}
+  virtual int seed(long long n) = 0;
+  virtual int set_state(long long n, const mrsph_state_in* st, int pre_run) = 0;
+  virtual int run_phase(int phase) = 0;
+  virtual int step(int nsteps) = 0;
+  virtual int step_timed(int nsteps, double* ms) = 0;
+  virtual int profile_steps(int nsteps, double* phase_ms, int nphase) = 0;
+  virtual int stats(mrsph_stats* out) = 0;
+  virtual int get_particles(const mrsph_particle_view* v) = 0;
+  virtual int get_cells(int* level_cell, int* sorted_ids) = 0;
+  virtual int get_neighbors(long long* off, int* nb, long long cap, long long* total) = 0;
+  virtual int upload_positions(const double* xyz) = 0;
+  virtual int download_positions(double* xyz) = 0;
+  virtual int sample(long long n, const double* xyz, double* phi, double* norm, double* curv, int* tag) = 0;
+  std::string err;
+};
+
+EngineBase* make_engine_fp64(const EngineConfig& cfg);
+EngineBase* make_engine_fp32(const EngineConfig& cfg);
+
+// level-set grid build (mrsph_levelset.cu)
+struct LsBuildDesc {
+  int D;
+  int num_pkg[3], margin, n[3];
+  double dcell[3];
+};
+cudaError_t ls_build_level(const LsBuildDesc& L, const double* d_phi, double4* g64, double* c64, float4* g32,
+                           float* c32, uint8_t* tag, unsigned long long* max_phi_bits, cudaStream_t s);
+
+// sort / scan primitives (mrsph_sort.cu)
+void cell_scan(int* counts, int* cstart, int* blocksums, long long ncells, int ntotal, cudaStream_t s);
+void cell_scatter(const int* cellkey, int* cursor, const int* cstart, int* perm, long long n, cudaStream_t s);
+void cell_rank(const int* cellkey, const int* cstart, const int* perm, const int* id, int* perm2, long long n,
+               cudaStream_t s);
+long long scan_blocksums_size(long long ncells);
+
+}  // namespace mrsph

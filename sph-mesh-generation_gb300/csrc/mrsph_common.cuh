@@ -1,0 +1,391 @@
+// mrsph_common.cuh — device-side building blocks shared by the FP64-plain and
+// FP32-split engines: geometry descriptors, Philox4x32-10, the SPH kernel
+// functions and level-set sampling.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mrsph {
+
+constexpr double PI_REF = 3.1415926;  // glbparam.h:186
+constexpr int MAX_LS = 4;             // nested level-set levels
+constexpr int MAX_CL = 8;             // cell-list levels
+
+enum { REAL_P = 0, SURFACE_P = 1, SINGULARITY_P = 2, SEGMENT_P = 3 };
+enum { K_HYP = 0, K_CUB = 1, K_WEN = 2, K_GAU = 3, K_QUI = 4 };
+enum { CUT_CELL = 1 };
+enum { FLAG_REMAP = 1, FLAG_SEED = 2, FLAG_LEVEL = 4, FLAG_SPILL = 8 };
+enum { RNG_SEED = 1, RNG_REMAP = 2 };
+
+// One nested level-set level on the device (dense, margins included).
+struct LsLevel {
+  double box_l[3], dpkg[3], dcell[3];
+  int num_pkg[3], margin, n[3];
+  const double4* g64;  // (phi, nx, ny, nz)
+  const double* c64;   // curvature
+  const float4* g32;
+  const float* c32;
+  const uint8_t* tag;
+  const uint8_t* active;  // per package incl. margins, or nullptr
+};
+
+struct LsSet {
+  int nls;
+  double max_phi, dl0, min_dl, max_dl;
+  LsLevel lv[MAX_LS];
+};
+
+// Cell-list levels (Level_info, level_infor.cpp:35-110): level 0 is the
+// coarsest (scale = max_scale), level ncl-1 the finest.  Cells of level l are
+// concatenated in one table at offset off[l], row-major (x fastest).
+struct CellGeo {
+  int ncl;
+  double box_l[3];
+  double max_scale, min_scale;
+  int n[MAX_CL][3];
+  double dcell[MAX_CL][3];
+  long long off[MAX_CL + 1];
+  double A[3];  // anchor cell of the FP32-split position = finest cell
+  float Af[3];
+};
+
+struct Params {
+  int dim, kernel;
+  double cell_ratio, cutoff, angle_thres, cos_thres, nu_coeff, damp_coeff;
+  double box_l[3], box_r[3];
+  unsigned long long seed;
+};
+
+// Device scalars of a step.  Doubles are kept as their bit patterns so that
+// min/max of non-negative values reduce exactly with integer atomics.
+struct DevScalars {
+  unsigned long long dt1, vmax1, dt2, vmax2, dt_adv;
+  unsigned long long pairs;
+  unsigned long long pairs_total;
+  unsigned int remap, nsurf, flags, spill;
+  unsigned int step;
+  unsigned int maxcnt;  // largest neighbour count of the last density phase
+};
+
+// ---------------------------------------------------------------- Philox
+struct U4 { uint32_t v[4]; };
+__host__ __device__ inline U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  U4 o; o.v[0] = c0; o.v[1] = c1; o.v[2] = c2; o.v[3] = c3;
+  return o;
+}
+__host__ __device__ inline double u53(uint32_t a, uint32_t b) {
+  return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------- helpers
+template <class R> struct V4;
+template <> struct V4<double> { using T = double4; };
+template <> struct V4<float> { using T = float4; };
+
+__device__ inline double r_sqrt(double x) { return sqrt(x); }
+__device__ inline float r_sqrt(float x) { return sqrtf(x); }
+__device__ inline double r_exp(double x) { return exp(x); }
+__device__ inline float r_exp(float x) { return __expf(x); }
+__device__ inline double r_tanh(double x) { return tanh(x); }
+__device__ inline float r_tanh(float x) { return tanhf(x); }
+__device__ inline double r_fabs(double x) { return fabs(x); }
+__device__ inline float r_fabs(float x) { return fabsf(x); }
+
+template <class R> __device__ inline R powern(R a, int n) {
+  R res = 1;
+  for (int i = 0; i < n; i++) res *= a;
+  return res;
+}
+template <class R> __device__ inline R AMIN1(R a, R b) { return a <= b ? a : b; }
+template <class R> __device__ inline R AMAX1(R a, R b) { return a >= b ? a : b; }
+
+__device__ inline unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ inline double bitsd(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// ---------------------------------------------------------------- SPH kernels
+// particle.cpp:31-807 restated.  D = kernel dimension.  dW returns
+// dW/dr / dist (Derivative_kernel_function convention).
+template <class R>
+__device__ inline R kernel_W(int kind, int D, R dist, R h) {
+  const R PI = (R)PI_REF;
+  R s = dist / h, C = 0, val = 0;
+  if (kind == K_WEN) {
+    if (D == 1) return 0;
+    if (D == 2) C = (R)1.0 / PI / powern(h, 2) * (R)7. / (R)4.;
+    else C = (R)1.0 / PI / powern(h, 3) * (R)21. / (R)16.;
+    if (s < 2) val = C * powern(((R)1. - (R)0.5 * s), 4) * ((R)1. + (R)2. * s);
+    return val;
+  }
+  if (kind == K_HYP) {
+    if (D == 1) C = (R)1.0 / (R)7.0 / powern(h, 1);
+    else if (D == 2) C = (R)1.0 / ((R)3.0 * PI) / powern(h, 2);
+    else C = (R)15.0 / ((R)62.0 * PI) / powern(h, 3);
+    if (s < 1) val = C * ((R)6.0 - (R)6.0 * s + s * s * s);
+    else if (s < 2) val = C * (2 - s) * (2 - s) * (2 - s);
+    return val;
+  }
+  if (kind == K_CUB) {
+    if (D == 1) C = (R)0.666666667 / powern(h, 1);
+    else if (D == 2) C = (R)0.454728408 / powern(h, 2);
+    else C = (R)0.318309886 / powern(h, 3);
+    if (s < 1) val = C * (1 - (R)1.5 * s * s + (R)0.75 * s * s * s);
+    else if (s < 2) val = C / (R)4.0 * (2 - s) * (2 - s) * (2 - s);
+    return val;
+  }
+  if (kind == K_GAU) {
+    R fac = (R)0.5 * 2 / r_sqrt(PI);
+    if (D > 1) fac *= (R)0.5 * 2 / r_sqrt(PI);
+    if (D > 2) fac *= (R)0.5 * 2 / r_sqrt(PI);
+    if (D == 1) C = fac / h;
+    else C = fac / powern(h, D);
+    if (s < 3) val = r_exp((R)-1. * s * s) * C;
+    return val;
+  }
+  // quintic
+  if (D == 1) C = (R)1.0 / (R)120. / powern(h, 1);
+  else if (D == 2) C = (R)1.0 / PI * (R)7. / (R)478. / powern(h, 2);
+  else C = (R)1.0 / PI * (R)3. / (R)359. / powern(h, 3);
+  if (s < 1) val = C * (powern(((R)3. - s), 5) - (R)6. * powern(((R)2. - s), 5) + (R)15. * powern(((R)1. - s), 5));
+  else if (s < 2) val = C * (powern(((R)3. - s), 5) - (R)6. * powern(((R)2. - s), 5));
+  else if (s < 3) val = C * (powern(((R)3. - s), 5));
+  return val;
+}
+
+template <class R>
+__device__ inline R kernel_dW(int kind, int D, R dist, R h) {
+  const R PI = (R)PI_REF;
+  R s = dist / h, C = 0, val = 0;
+  if (kind == K_WEN) {
+    if (D == 1) return 0;
+    if (D == 2) C = (R)1.0 / PI / powern(h, 2) * (R)7. / (R)4.;
+    else C = (R)1.0 / PI / powern(h, 3) * (R)21. / (R)16.;
+    if (s < 2) val = (R)-5. * C * powern(((R)1. - (R)0.5 * s), 3) * s / h / (dist + (R)1.e-15);
+    return val;
+  }
+  if (kind == K_HYP) {
+    if (D == 1) C = (R)1.0 / (R)7.0 / powern(h, 2);
+    else if (D == 2) C = (R)1.0 / ((R)3.0 * PI) / powern(h, 3);
+    else C = (R)15.0 / ((R)62.0 * PI) / powern(h, 4);
+    if (s < 1) val = C * ((R)-6.0 + (R)3. * s * s);
+    else if (s < 2) val = C * (R)(-3.0) * (2 - s) * (2 - s);
+    val /= (dist + (R)1.e-20);
+    return val;
+  }
+  if (kind == K_CUB) {
+    if (D == 1) C = (R)0.666666667 / powern(h, 2);
+    else if (D == 2) C = (R)0.454728408 / powern(h, 3);
+    else C = (R)0.318309886 / powern(h, 4);
+    if (s < 1) val = 3 * C * (-s + 3 * (s * s) / 4);
+    else if (s < 2) val = (R)(-3 / 4.0) * C * (2 - s) * (2 - s);
+    val /= (dist + (R)1.e-20);
+    return val;
+  }
+  if (kind == K_GAU) {
+    R fac = (R)0.5 * 2 / r_sqrt(PI);
+    if (D > 1) fac *= (R)0.5 * 2 / r_sqrt(PI);
+    if (D > 2) fac *= (R)0.5 * 2 / r_sqrt(PI);
+    if (D == 1) C = fac / h;
+    else C = fac / powern(h, D);
+    if (s < 3) val = (R)-2. * s * r_exp((R)-1. * s * s) * C / h / (dist + (R)1.e-15);
+    return val;
+  }
+  if (D == 1) C = (R)1.0 / (R)120. / powern(h, 1);
+  else if (D == 2) C = (R)1.0 / PI * (R)7. / (R)478. / powern(h, 2);
+  else C = (R)1.0 / PI * (R)3. / (R)359. / powern(h, 3);
+  if (s < 1) {
+    val = C * ((R)-5. * powern(((R)3. - s), 4) + (R)30. * powern(((R)2. - s), 4) - (R)75. * powern(((R)1. - s), 4));
+    val = val / h / (dist + (R)1.e-15);
+  } else if (s < 2) {
+    val = C * ((R)-5. * powern(((R)3. - s), 4) + (R)30. * powern(((R)2. - s), 4));
+    val = val / h / (dist + (R)1.e-15);
+  } else if (s < 3) {
+    val = C * ((R)-5. * powern(((R)3. - s), 4));
+    val = val / h / (dist + (R)1.e-15);
+  }
+  return val;
+}
+
+// ---------------------------------------------------------------- level set
+__device__ inline long long ls_index(const LsLevel& L, int D, int gi, int gj, int gk) {
+  long long a0 = gi + 4 * L.margin, a1 = gj + 4 * L.margin, a2 = (D == 3) ? gk + 4 * L.margin : 0;
+  return (a2 * L.n[1] + a1) * L.n[0] + a0;
+}
+
+// Finest nested level whose interior contains x and whose package is active
+// (build extension for a multi-level level set; the reference has one level).
+template <int D>
+__device__ inline int ls_pick(const LsSet& ls, const double* x) {
+  for (int l = ls.nls - 1; l >= 1; l--) {
+    const LsLevel& L = ls.lv[l];
+    int pk[3] = {0, 0, 0};
+    bool inside = true;
+    for (int d = 0; d < D; d++) {
+      double cs = x[d] - L.box_l[d];
+      double dom = L.dpkg[d] * L.num_pkg[d];
+      if (!(cs >= 0.0 && cs < dom)) { inside = false; break; }
+      pk[d] = (int)floor(cs / L.dpkg[d]);
+      if (pk[d] < 0 || pk[d] >= L.num_pkg[d]) { inside = false; break; }
+    }
+    if (!inside) continue;
+    if (L.active) {
+      long long np0 = L.num_pkg[0] + 2 * L.margin, np1 = L.num_pkg[1] + 2 * L.margin;
+      long long pidx = ((long long)((D == 3) ? pk[2] + L.margin : 0) * np1 + (pk[1] + L.margin)) * np0 + (pk[0] + L.margin);
+      if (!L.active[pidx]) continue;
+    }
+    return l;
+  }
+  return 0;
+}
+
+template <class R> __device__ inline void ls_fetch(const LsLevel& L, long long a, R& phi, R& nx, R& ny, R& nz, R& c);
+template <> __device__ inline void ls_fetch<double>(const LsLevel& L, long long a, double& phi, double& nx, double& ny,
+                                                    double& nz, double& c) {
+  double4 g = L.g64[a];
+  phi = g.x; nx = g.y; ny = g.z; nz = g.w; c = L.c64[a];
+}
+template <> __device__ inline void ls_fetch<float>(const LsLevel& L, long long a, float& phi, float& nx, float& ny,
+                                                   float& nz, float& c) {
+  float4 g = __ldg(&L.g32[a]);
+  phi = g.x; nx = g.y; ny = g.z; nz = g.w; c = __ldg(&L.c32[a]);
+}
+
+// Calculate_particle_infor, particle_mesh_generation.cpp:175-265.  Cell
+// location and weights in FP64 (as the reference); accumulation in R.  The
+// interpolated normal is not renormalised (reference quirk Q1).
+template <int D, class R>
+__device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n, R& curv) {
+  const LsLevel& L = ls.lv[ls_pick<D>(ls, x)];
+  int pos[3] = {0, 0, 0}, im[3] = {0, 0, 0};
+  double w[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    double dom = L.dpkg[d] * L.num_pkg[d];
+    double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
+    int p = (int)floor(cs / L.dpkg[d]);
+    p = max(-L.margin, min(p, L.num_pkg[d] + L.margin - 1));
+    pos[d] = p;
+    double csp = cs - L.dpkg[d] * p;
+    double rr = csp / L.dcell[d] - 0.5;
+    rr = AMAX1(-0.5, AMIN1(rr, 4.0 - 0.5));
+    im[d] = (int)floor(rr);
+    w[d] = rr - (double)im[d];
+  }
+  R ph = 0, n0 = 0, n1 = 0, n2 = 0, cv = 0;
+#pragma unroll
+  for (int r = 0; r <= 1; r++)
+#pragma unroll
+    for (int s = 0; s <= 1; s++)
+#pragma unroll
+      for (int t = 0; t <= (D == 3 ? 1 : 0); t++) {
+        int gi = pos[0] * 4 + im[0] + r, gj = pos[1] * 4 + im[1] + s;
+        int gk = (D == 3) ? pos[2] * 4 + im[2] + t : 0;
+        long long a = ls_index(L, D, gi, gj, gk);
+        double cf = fabs(w[0] - (1.0 - r)) * fabs(w[1] - (1.0 - s)) * ((D == 3) ? fabs(w[2] - (1.0 - t)) : 1.0);
+        R coef = (R)cf;
+        R p_, x_, y_, z_, c_;
+        ls_fetch<R>(L, a, p_, x_, y_, z_, c_);
+        ph += p_ * coef;
+        n0 += x_ * coef;
+        n1 += y_ * coef;
+        n2 += z_ * coef;
+        cv += c_ * coef;
+      }
+  phi = ph;
+  n[0] = n0; n[1] = n1; n[2] = (D == 3) ? n2 : (R)0;
+  curv = cv;
+}
+
+// Get_level_set_char_cell_tag_and_idx (particle_mesh_generation.cpp:552-573)
+// via Get_id_pkg_cell (lset_level_infor.cpp:350-366).
+template <int D>
+__device__ inline int ls_tag(const LsSet& ls, const double* x) {
+  const LsLevel& L = ls.lv[ls_pick<D>(ls, x)];
+  int g[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    double dom = L.dpkg[d] * L.num_pkg[d];
+    double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
+    int p = (int)floor(cs / L.dpkg[d]);
+    p = max(-L.margin, min(p, L.num_pkg[d] + L.margin - 1));
+    double csp = cs - L.dpkg[d] * p;
+    int ci = (int)floor(csp / L.dcell[d]);
+    ci = max(0, min(ci, 3));
+    g[d] = p * 4 + ci;
+  }
+  return L.tag[ls_index(L, D, g[0], g[1], g[2])];
+}
+
+// Levelset::Get_scale, level_set.cpp:311-351 (active tanh law)
+template <class R>
+__device__ inline R get_scale(const LsSet& ls, R phi) {
+  if (phi > 0 || r_fabs(phi) < (R)ls.dl0) {
+    R factor = (R)2.5;
+    return (R)ls.min_dl + r_tanh(factor * r_fabs(phi) / (R)ls.max_phi) / r_tanh(factor) * ((R)ls.max_dl - (R)ls.min_dl);
+  }
+  return (R)ls.min_dl;
+}
+
+// ---------------------------------------------------------------- reductions
+__device__ inline double warp_min(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ inline double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ inline unsigned long long warp_sum_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide min/max of non-negative doubles folded into global bit-pattern
+// atomics (exact and order-independent).  All threads of the block must call.
+__device__ inline void block_minmax_to_global(double vmin, double vmax, unsigned long long* gmin,
+                                              unsigned long long* gmax) {
+  __shared__ double smin[32], smax[32];
+  vmin = warp_min(vmin);
+  vmax = warp_max(vmax);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { smin[wid] = vmin; smax[wid] = vmax; }
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    vmin = lane < nw ? smin[lane] : 1.e300;
+    vmax = lane < nw ? smax[lane] : 0.0;
+    vmin = warp_min(vmin);
+    vmax = warp_max(vmax);
+    if (lane == 0) {
+      if (gmin) atomicMin(gmin, dbits(vmin));
+      if (gmax) atomicMax(gmax, dbits(vmax));
+    }
+  }
+}
+
+__device__ inline void block_sum_u64_to_global(unsigned long long v, unsigned long long* g) {
+  __shared__ unsigned long long ss[32];
+  v = warp_sum_u64(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) ss[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? ss[lane] : 0ull;
+    v = warp_sum_u64(v);
+    if (lane == 0 && v) atomicAdd(g, v);
+  }
+}
+
+}  // namespace mrsph

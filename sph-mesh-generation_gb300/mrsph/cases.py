@@ -1,0 +1,211 @@
+"""Case definitions: analytic level sets and relaxation parameters.
+
+This is the user-defined part of a run, the counterpart of the reference's
+``SPH_mesh_generation::Load_case`` (sph_mesh_generation/sph_mesh_generation.cpp:156-319)
+and ``Levelset::F_phi`` (level_set_solver/level_set.cpp:92-173): it chooses the
+domain, the level-set grid(s) and the target spacing range, and evaluates phi
+(positive inside the body) at level-set cell centres.  Normals, cut-cell tags,
+curvature and the maximum phi are computed on the GPU by the library
+(``mrsph_set_levelset``).
+
+Grid layout (one nested level): interior packages of 4^D cells cover
+``[box_l, box_l + num_pkg*dpkg)`` and ``margin`` packages pad every side
+(lset_level_infor.cpp:17-85).  Cell centres are
+``pkg*dpkg + (cell + 0.5)*dcell + box_l`` (lset_package.cpp:70-79), evaluated
+in that order so phi matches what the reference would sample.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional
+
+import numpy as np
+
+PI_REF = 3.1415926  # glbparam.h:186
+
+KERNELS = {"hyperbolic": 0, "cubic": 1, "wendland": 2, "gaussian": 3, "quintic": 4}
+PRECISIONS = {"fp64": 0, "fp32": 1}
+
+
+@dataclass
+class LevelGrid:
+    box_l: List[float]
+    dpkg: List[float]
+    num_pkg: List[int]
+    margin: int
+    phi: np.ndarray                    # float64, shape (nz, ny, nx) incl. margins (nz = 1 in 2D)
+    active: Optional[np.ndarray] = None  # uint8 per package incl. margins, or None
+
+
+@dataclass
+class Case:
+    name: str
+    params: dict
+    levels: List[LevelGrid]
+    n_particles: int
+    steps: int = 200
+    notes: str = ""
+    extra: dict = field(default_factory=dict)
+
+
+def default_params(dim: int) -> dict:
+    """Reference defaults: Wendland C2 off, hyperbolic kernel (Makefile.in:36),
+    CELL_RATIO 2.0 (2D) / 1.45 (3D) (glbparam.h:171-183), CUT_OFF 2,
+    angle_thres 0.4*PI, nu 0.1, damping 0 (sph_mesh_generation.cpp:688-703)."""
+    return {
+        "dim": dim,
+        "kernel": KERNELS["hyperbolic"],
+        "precision": PRECISIONS["fp64"],
+        "cell_ratio": 2.0 if dim == 2 else 1.45,
+        "cutoff": 2.0,
+        "angle_thres": PI_REF * 0.4,
+        "nu_coeff": 0.1,
+        "damp_coeff": 0.0,
+        "min_dl": 0.01,
+        "max_dl": 0.01,
+        "box_l": [0.0, 0.0, 0.0],
+        "box_r": [1.0, 1.0, 1.0],
+        "seed": 0,
+        "neighbor_cap": 0,
+    }
+
+
+def cell_centres(box_l, dpkg, num_pkg, margin, dim):
+    """Axis coordinates of the cell centres incl. margin packages."""
+    axes = []
+    for d in range(3):
+        if d >= dim:
+            axes.append(np.zeros(1))
+            continue
+        pk = np.repeat(np.arange(-margin, num_pkg[d] + margin), 4).astype(np.float64)
+        cl = np.tile(np.arange(4), num_pkg[d] + 2 * margin).astype(np.float64)
+        dcell = dpkg[d] / 4.0
+        axes.append(pk * dpkg[d] + (cl + 0.5) * dcell + box_l[d])
+    return axes
+
+
+def make_level(sdf: Callable, dim: int, box_l, dpkg, num_pkg, margin: int = 1) -> LevelGrid:
+    ax = cell_centres(box_l, dpkg, num_pkg, margin, dim)
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    phi = np.ascontiguousarray(sdf(X, Y, Z), dtype=np.float64)
+    return LevelGrid(list(box_l), list(dpkg), list(num_pkg), margin, phi, None)
+
+
+def nested_active(level: LevelGrid, band: float, dim: int) -> np.ndarray:
+    """Package mask of a finer nested level: active where any cell has |phi| < band."""
+    m = level.margin
+    nz = (level.num_pkg[2] + 2 * m) if dim == 3 else 1
+    ny = level.num_pkg[1] + 2 * m
+    nx = level.num_pkg[0] + 2 * m
+    a = np.abs(level.phi)
+    if dim == 3:
+        blk = a.reshape(nz, 4, ny, 4, nx, 4).min(axis=(1, 3, 5))
+    else:
+        blk = a.reshape(1, ny, 4, nx, 4).min(axis=(2, 4))
+    return (blk < band).astype(np.uint8)
+
+
+def scale_law(phi, min_dl, max_dl, max_phi, dl0):
+    """Levelset::Get_scale, level_set_solver/level_set.cpp:311-351 (tanh law)."""
+    phi = np.asarray(phi, dtype=np.float64)
+    s = min_dl + np.tanh(2.5 * np.abs(phi) / max_phi) / np.tanh(2.5) * (max_dl - min_dl)
+    return np.where((phi > 0) | (np.abs(phi) < dl0), s, min_dl)
+
+
+def particle_count(levels: List[LevelGrid], params: dict) -> int:
+    """Target count from the spacing integral over phi > 0 (the reference's
+    total_mass = sum vol/scale^D, lset_package.cpp:1283-1397, without the
+    cut-cell geometry refinement), evaluated on the finest level."""
+    dim = params["dim"]
+    mp = max_phi(levels, dim)
+    fine = levels[-1]
+    m = fine.margin * 4
+    sl = [slice(m, -m) for _ in range(dim)]
+    if dim == 2:
+        inner = fine.phi[0][sl[1], sl[0]]
+    else:
+        inner = fine.phi[sl[2], sl[1], sl[0]]
+    dV = 1.0
+    for d in range(dim):
+        dV *= fine.dpkg[d] / 4.0
+    dl0 = min(levels[0].dpkg[d] / 4.0 for d in range(dim))
+    sc = scale_law(inner, params["min_dl"], params["max_dl"], mp, dl0)
+    return int(np.sum(np.where(inner > 0, dV / sc ** dim, 0.0)))
+
+
+def max_phi(levels: List[LevelGrid], dim: int) -> float:
+    mp = 0.0
+    for lv in levels:
+        m = lv.margin * 4
+        if dim == 2:
+            inner = lv.phi[0][m:-m, m:-m]
+        else:
+            inner = lv.phi[m:-m, m:-m, m:-m]
+        pos = inner[inner > 0]
+        if pos.size:
+            mp = max(mp, float(pos.max()))
+    return mp
+
+
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+def disc_hole_2d(spacing: float = 0.01, grid: int = 256, kernel: str = "wendland",
+                 h_over_dx: float = 1.3, precision: str = "fp64", seed: int = 0,
+                 steps: int = 200) -> Case:
+    """Unit square minus a disc (r = 0.2 at (0.5, 0.5)), analytic SDF on a
+    grid^2 cell-centred level set, constant spacing."""
+    p = default_params(2)
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=spacing, max_dl=spacing,
+             cell_ratio=2.0 * h_over_dx, box_l=[0.0, 0.0, 0.0], box_r=[1.0, 1.0, 0.0], seed=seed)
+
+    def sdf(X, Y, Z):
+        disc = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2) - 0.2
+        return np.minimum(np.minimum(np.minimum(X, 1.0 - X), np.minimum(Y, 1.0 - Y)), disc)
+
+    npkg = grid // 4
+    lv = make_level(sdf, 2, [0.0, 0.0, 0.0], [1.0 / npkg, 1.0 / npkg, 1.0], [npkg, npkg, 1])
+    n = particle_count([lv], p)
+    return Case("disc_hole_2d", p, [lv], n, steps=steps)
+
+
+def torus_3d(dx_min: float = 0.005, dx_max: float = 0.02, kernel: str = "wendland",
+             h_over_dx: float = 1.3, precision: str = "fp32", seed: int = 0, steps: int = 500,
+             fine_pkg: int = 64, nlevels: int = 3) -> Case:
+    """Inside of a torus (R = 1, r = 0.35), nested level-set grids of
+    16/32/64 packages along x (64^3/128^3/256^3 cells nominal; z extent
+    trimmed to whole packages), finer levels active where |phi| < 4 cells of
+    the next-coarser level.  Spacing from dx_min to dx_max by the tanh law."""
+    p = default_params(3)
+    zhalf = 0.0
+    npx0 = fine_pkg >> (nlevels - 1)
+    dpkg0 = 2.9 / npx0
+    npz0 = int(round(0.9 / dpkg0))
+    zhalf = 0.5 * npz0 * dpkg0
+    box_l = [-1.45, -1.45, -zhalf]
+    box_r = [1.45, 1.45, zhalf]
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=dx_min, max_dl=dx_max,
+             cell_ratio=2.0 * h_over_dx, box_l=box_l, box_r=box_r, seed=seed)
+
+    def sdf(X, Y, Z):
+        return 0.35 - np.sqrt((np.sqrt(X * X + Y * Y) - 1.0) ** 2 + Z * Z)
+
+    levels = []
+    for l in range(nlevels):
+        f = 1 << l
+        dp = dpkg0 / f
+        lv = make_level(sdf, 3, box_l, [dp, dp, dp], [npx0 * f, npx0 * f, npz0 * f])
+        if l > 0:
+            lv.active = nested_active(lv, 4.0 * (dp * 2 / 4.0), 3)
+        levels.append(lv)
+    n = particle_count(levels, p)
+    return Case("torus_3d", p, levels, n, steps=steps)
+
+
+def case_by_name(name: str, **kw) -> Case:
+    if name == "disc_hole_2d":
+        return disc_hole_2d(**kw)
+    if name == "torus_3d":
+        return torus_3d(**kw)
+    raise KeyError(name)

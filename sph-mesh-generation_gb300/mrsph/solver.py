@@ -1,0 +1,214 @@
+"""Host-side mirror of the reference's relaxation driver.
+
+``SPHMeshGeneration`` keeps the entry-point names of the reference's
+``SPH_mesh_generation`` class (src/sph_mesh_generation/sph_mesh_generation.h:10-154,
+driven by Solver, src/solver.cpp:35-321) and forwards every call through the C
+ABI of include/mrsph_relax.h to the CUDA engine.  Arrays in and out are numpy,
+in particle-id order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+from .cases import Case
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class SPHMeshGeneration:
+    """One geometry on one GPU (the reference's SPH_mesh_generation + Levelset)."""
+
+    def __init__(self, case: Case, precision: Optional[str] = None, device: int = 0,
+                 neighbor_cap: int = 0):
+        self.lib = L.load()
+        self.case = case
+        p = dict(case.params)
+        if precision is not None:
+            p["precision"] = {"fp64": L.FP64_PLAIN, "fp32": L.FP32_SPLIT}[precision]
+        self.params = p
+        prm = L.Params()
+        prm.dim = p["dim"]
+        prm.kernel = p["kernel"]
+        prm.precision = p["precision"]
+        prm.cell_ratio = p["cell_ratio"]
+        prm.cutoff = p["cutoff"]
+        prm.angle_thres = p["angle_thres"]
+        prm.nu_coeff = p["nu_coeff"]
+        prm.damp_coeff = p["damp_coeff"]
+        prm.min_dl = p["min_dl"]
+        prm.max_dl = p["max_dl"]
+        for d in range(3):
+            prm.box_l[d] = p["box_l"][d]
+            prm.box_r[d] = p["box_r"][d]
+        prm.seed = p["seed"]
+        prm.neighbor_cap = neighbor_cap or p.get("neighbor_cap", 0)
+        prm.device = device
+        h = C.c_void_p()
+        L.check(self.lib.mrsph_create(C.byref(prm), C.byref(h)), None, "mrsph_create")
+        self.h = h
+        self.n = 0
+        self._set_levelset()
+
+    # ------------------------------------------------------------------ setup
+    def _set_levelset(self):
+        levels = self.case.levels
+        arr = (L.LevelsetLevel * len(levels))()
+        self._ls_keep = []
+        for i, lv in enumerate(levels):
+            a = arr[i]
+            for d in range(3):
+                a.box_l[d] = lv.box_l[d]
+                a.dpkg[d] = lv.dpkg[d]
+                a.num_pkg[d] = lv.num_pkg[d]
+            a.margin = lv.margin
+            phi = np.ascontiguousarray(lv.phi, dtype=np.float64)
+            self._ls_keep.append(phi)
+            a.phi = phi.ctypes.data_as(C.c_void_p)
+            if lv.active is not None:
+                act = np.ascontiguousarray(lv.active, dtype=np.uint8)
+                self._ls_keep.append(act)
+                a.active = act.ctypes.data_as(C.c_void_p)
+            else:
+                a.active = None
+        L.check(self.lib.mrsph_set_levelset(self.h, len(levels), arr), self.h, "mrsph_set_levelset")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mrsph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --------------------------------------------------- reference entry points
+    def Initialize_case(self, n: Optional[int] = None):
+        """Random_particle_distribution + Pre_run (sph_mesh_generation.cpp:594-1050)."""
+        n = int(n if n is not None else self.case.n_particles)
+        L.check(self.lib.mrsph_seed(self.h, n), self.h, "mrsph_seed")
+        self.n = n
+
+    def SPH_run_mesh_generation(self, nsteps: int = 1):
+        """SPH_mesh_generation::SPH_run_mesh_generation x nsteps (asynchronous)."""
+        L.check(self.lib.mrsph_step(self.h, int(nsteps)), self.h, "mrsph_step")
+
+    def step_timed(self, nsteps: int) -> float:
+        """nsteps relaxation steps; returns device milliseconds (CUDA events on the engine stream)."""
+        ms = C.c_double(0)
+        L.check(self.lib.mrsph_step_timed(self.h, int(nsteps), C.byref(ms)), self.h, "mrsph_step_timed")
+        return ms.value
+
+    def profile_steps(self, nsteps: int) -> dict:
+        """Mean device milliseconds per step of each phase (eager launches)."""
+        out = np.zeros(len(L.TIMERS))
+        L.check(self.lib.mrsph_profile_steps(self.h, int(nsteps), _ptr(out), len(L.TIMERS)), self.h,
+                "mrsph_profile_steps")
+        return dict(zip(L.TIMERS, out.tolist()))
+
+    def Get_timestep(self) -> float:
+        return self.stats()["dt"]
+
+    # ------------------------------------------------------------- parity API
+    def set_state(self, st: dict, pre_run: bool = False):
+        xyz = np.ascontiguousarray(st["xyz"], dtype=np.float64).reshape(-1, 3)
+        n = len(xyz)
+        keep = [xyz]
+        s = L.StateIn()
+        s.xyz = _ptr(xyz)
+
+        def opt(key, dtype, shape):
+            if key not in st or st[key] is None:
+                return None
+            a = np.ascontiguousarray(st[key], dtype=dtype).reshape(shape)
+            keep.append(a)
+            return _ptr(a)
+
+        s.v = opt("v", np.float64, (-1, 3))
+        s.type = opt("type", np.int32, (-1,))
+        s.h = opt("h", np.float64, (-1,))
+        s.level = opt("level", np.int32, (-1,))
+        s.nu = opt("nu", np.float64, (-1,))
+        s.dt = float(st.get("dt", 0.0))
+        s.step = int(st.get("step", 0))
+        L.check(self.lib.mrsph_set_state(self.h, n, C.byref(s), 1 if pre_run else 0), self.h, "mrsph_set_state")
+        self.n = n
+
+    def run_phase(self, phase: int):
+        L.check(self.lib.mrsph_run_phase(self.h, phase), self.h, "mrsph_run_phase")
+
+    def sync(self):
+        L.check(self.lib.mrsph_sync(self.h), self.h, "mrsph_sync")
+
+    def stats(self) -> dict:
+        s = L.Stats()
+        L.check(self.lib.mrsph_get_stats(self.h, C.byref(s)), self.h, "mrsph_get_stats")
+        return {f: getattr(s, f) for f, _ in L.Stats._fields_}
+
+    def particles(self, fields=("xyz", "v", "type", "h", "level", "phi", "curv", "norm", "sum", "rho", "nu",
+                                "a1", "a2")) -> dict:
+        n = self.n
+        out = {}
+        v = L.ParticleView()
+        for f in fields:
+            if f in ("xyz", "v", "norm", "a1", "a2"):
+                out[f] = np.zeros((n, 3), dtype=np.float64)
+            elif f in ("type", "level"):
+                out[f] = np.zeros(n, dtype=np.int32)
+            else:
+                out[f] = np.zeros(n, dtype=np.float64)
+            setattr(v, f, _ptr(out[f]))
+        L.check(self.lib.mrsph_get_particles(self.h, C.byref(v)), self.h, "mrsph_get_particles")
+        return out
+
+    def cells(self):
+        lc = np.zeros((self.n, 4), dtype=np.int32)
+        ids = np.zeros(self.n, dtype=np.int32)
+        L.check(self.lib.mrsph_get_cells(self.h, _ptr(lc), _ptr(ids)), self.h, "mrsph_get_cells")
+        return lc, ids
+
+    def neighbors(self):
+        tot = C.c_longlong(0)
+        L.check(self.lib.mrsph_get_neighbors(self.h, None, None, 0, C.byref(tot)), self.h, "mrsph_get_neighbors")
+        off = np.zeros(self.n + 1, dtype=np.int64)
+        nb = np.zeros(max(tot.value, 1), dtype=np.int32)
+        L.check(self.lib.mrsph_get_neighbors(self.h, _ptr(off), _ptr(nb), tot.value, C.byref(tot)), self.h,
+                "mrsph_get_neighbors")
+        return off, nb[: tot.value]
+
+    def levelset_fields(self, level: int):
+        lv = self.case.levels[level]
+        shp = lv.phi.shape
+        out = {k: np.zeros(shp, dtype=np.float64) for k in ("nx", "ny", "nz", "curv")}
+        out["tag"] = np.zeros(shp, dtype=np.uint8)
+        mp = C.c_double(0)
+        L.check(self.lib.mrsph_get_levelset(self.h, level, _ptr(out["nx"]), _ptr(out["ny"]), _ptr(out["nz"]),
+                                            _ptr(out["curv"]), _ptr(out["tag"]), C.byref(mp)), self.h,
+                "mrsph_get_levelset")
+        out["max_phi"] = mp.value
+        return out
+
+    def sample_levelset(self, xyz: np.ndarray):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = len(xyz)
+        phi = np.zeros(n)
+        nrm = np.zeros((n, 3))
+        curv = np.zeros(n)
+        tag = np.zeros(n, dtype=np.int32)
+        L.check(self.lib.mrsph_sample_levelset(self.h, n, _ptr(xyz), _ptr(phi), _ptr(nrm), _ptr(curv), _ptr(tag)),
+                self.h, "mrsph_sample_levelset")
+        return phi, nrm, curv, tag
+
+    def upload_positions(self, xyz: np.ndarray):
+        L.check(self.lib.mrsph_upload_positions(self.h, _ptr(xyz)), self.h, "mrsph_upload_positions")
+
+    def download_positions(self, out: np.ndarray):
+        L.check(self.lib.mrsph_download_positions(self.h, _ptr(out)), self.h, "mrsph_download_positions")
+        return out

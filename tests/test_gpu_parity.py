@@ -1,0 +1,206 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the FP64 oracle.
+
+Bars (from the project's correctness contract):
+  * FP64-plain: cell binning and neighbour sets bit-exact given identical
+    positions; level-set fields bit-exact; single-step densities, forces and
+    time steps within 1e-12 relative.
+  * FP32-split: single-step forces within 1e-4 of the largest force (FP32
+    accumulation over ~20-80 neighbours), positions within 1e-5 of the local
+    spacing, neighbour sets equal except pairs within FP32 rounding of the
+    cut-off.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mrsph import _lib as L
+from paritylib import (gpu_post_map_to_oracle, make_gpu, neighbor_sets, oracle_state_to_gpu, rel_err,
+                       small_cases, warm_oracle)
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def warmed(request):
+    case = CASES[request.param]()
+    orc = warm_oracle(case)
+    return request.param, case, orc.get_state()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_levelset_build_matches_oracle(name):
+    case = CASES[name]()
+    orc = oracle.Oracle(case)
+    gpu = make_gpu(case, "fp64")
+    for l in range(len(case.levels)):
+        g = gpu.levelset_fields(l)
+        f = orc.fields[l]
+        shp = g["nx"].shape
+        for k in ("nx", "ny", "nz"):
+            assert np.array_equal(g[k].ravel(), f[k]), f"{k} level {l}"
+        assert np.array_equal(g["tag"].ravel().astype(np.int32), f["tag"]), f"tag level {l}"
+        assert rel_err(g["curv"].ravel(), f["curv"]) < 1e-12
+        assert shp == case.levels[l].phi.shape
+    assert g["max_phi"] == orc.ctx.max_phi
+    gpu.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_levelset_sampling(name, prec):
+    case = CASES[name]()
+    orc = oracle.Oracle(case)
+    gpu = make_gpu(case, prec)
+    rng = np.random.default_rng(5)
+    p = case.params
+    lo = np.array(p["box_l"])
+    hi = np.array(p["box_r"])
+    pts = lo + rng.random((4000, 3)) * (hi - lo)
+    if p["dim"] == 2:
+        pts[:, 2] = 0.0
+    phi, nrm, curv, tag = gpu.sample_levelset(pts)
+    rphi, rnrm, rcurv, rtag = orc.sample(pts)
+    tol = 1e-13 if prec == "fp64" else 1e-5 * orc.ctx.max_phi
+    assert np.max(np.abs(phi - rphi)) <= tol
+    assert np.max(np.abs(nrm - rnrm)) <= (1e-13 if prec == "fp64" else 1e-5)
+    assert np.array_equal(tag, rtag)
+    gpu.close()
+
+
+def _gpu_step_taps(case, prec, st):
+    gpu = make_gpu(case, prec)
+    gpu.set_state(oracle_state_to_gpu(st))
+    gpu.run_phase(L.PHASE_FORCE2)
+    gp = gpu.particles()
+    lc, ids = gpu.cells()
+    off, nb = gpu.neighbors()
+    stats = gpu.stats()
+    gpu.close()
+    return gp, lc, ids, off, nb, stats
+
+
+def test_fp64_step_phase_parity(warmed):
+    name, case, st = warmed
+    gp, lc, ids, off, nb, stats = _gpu_step_taps(case, "fp64", st)
+    # map phase from the same injected state
+    orc = oracle.Oracle(case)
+    orc.set_state(st)
+    orc.phase_map(advect=True)
+    ost = orc.get_state()
+    oxyz = np.stack([ost["x"], ost["y"], ost["z"]], axis=1)
+    assert np.array_equal(gp["type"], ost["type"])
+    assert np.array_equal(gp["level"], ost["level"])
+    assert np.max(np.abs(gp["xyz"] - oxyz)) < 1e-12
+    assert rel_err(gp["h"], ost["h"]) < 1e-12
+    assert rel_err(gp["phi"], ost["phi"]) < 1e-12
+    assert np.max(np.abs(gp["norm"] - np.stack([ost["nx"], ost["ny"], ost["nz"]], 1))) < 1e-12
+    # binning + neighbours bit-exact from the GPU's own post-map state
+    o2 = oracle.Oracle(case)
+    gpu_post_map_to_oracle(o2, gp, st)
+    oc = o2.cells()
+    assert np.array_equal(lc, oc), "cell binning differs"
+    # storage order: cells contiguous, ids ascending inside a cell
+    key = [tuple(lc[i]) for i in ids]
+    for a in range(1, len(ids)):
+        if key[a] == key[a - 1]:
+            assert ids[a] > ids[a - 1]
+    ooff, onb = o2.neighbors()
+    assert np.array_equal(off, ooff), "neighbour counts differ"
+    assert np.array_equal(nb, onb), "neighbour sets differ"
+    assert stats["pairs"] == len(onb) - len(off) + 1
+    # density and the two force stages on identical inputs
+    o2.density(ooff, onb)
+    s = o2.get_state()
+    assert rel_err(gp["sum"], s["sum"]) < 1e-12
+    o2.force(ooff, onb, 1)
+    s1 = o2.get_state()
+    a1 = np.stack([s1["ax"], s1["ay"], s1["az"]], 1)
+    assert rel_err(gp["a1"], a1) < 1e-12
+    assert abs(stats["dt_stage1"] - s1["dt"]) <= 1e-12 * s1["dt"]
+    o2.force(ooff, onb, 2)
+    s2 = o2.get_state()
+    a2 = np.stack([s2["ax"], s2["ay"], s2["az"]], 1)
+    assert rel_err(gp["a2"], a2, floor=1e-300) < 1e-12
+    assert abs(stats["dt"] - s2["dt"]) <= 1e-12 * s2["dt"]
+    assert abs(stats["max_v"] - s2["max_v"]) <= 1e-12 * max(s2["max_v"], 1e-300)
+    assert rel_err(gp["nu"], s2["nu"]) < 1e-12
+    v = np.stack([s2["vx"], s2["vy"], s2["vz"]], 1)
+    assert rel_err(gp["v"], v) < 1e-12
+
+
+def test_fp32_step_phase_parity(warmed):
+    name, case, st = warmed
+    gp, lc, ids, off, nb, stats = _gpu_step_taps(case, "fp32", st)
+    dx = case.params["min_dl"]
+    orc = oracle.Oracle(case)
+    orc.set_state(st)
+    orc.phase_map(advect=True)
+    ost = orc.get_state()
+    oxyz = np.stack([ost["x"], ost["y"], ost["z"]], axis=1)
+    same = gp["type"] == ost["type"]
+    assert same.mean() > 0.999
+    assert np.max(np.abs(gp["xyz"][same] - oxyz[same])) < 1e-5 * dx
+    o2 = oracle.Oracle(case)
+    gpu_post_map_to_oracle(o2, gp, st)
+    ooff, onb = o2.neighbors()
+    gs, os_ = neighbor_sets(off, nb), neighbor_sets(ooff, onb)
+    diff = sum(len(a ^ b) for a, b in zip(gs, os_))
+    assert diff <= max(2, 1e-4 * len(onb))
+    o2.density(ooff, onb)
+    s = o2.get_state()
+    real = gp["type"] == 0
+    assert rel_err(gp["sum"][real], s["sum"][real]) < 1e-5
+    o2.force(ooff, onb, 1)
+    s1 = o2.get_state()
+    a1 = np.stack([s1["ax"], s1["ay"], s1["az"]], 1)
+    assert rel_err(gp["a1"], a1) < 1e-4
+    assert abs(stats["dt_stage1"] - s1["dt"]) <= 1e-4 * s1["dt"]
+    o2.force(ooff, onb, 2)
+    s2 = o2.get_state()
+    assert abs(stats["dt"] - s2["dt"]) <= 1e-3 * s2["dt"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_multistep_statistics(prec):
+    """20 relaxation steps from identical seeds: spacing statistics within 1%."""
+    case = CASES["disc2d_wendland"]()
+    orc = warm_oracle(case, max_steps=0, need_surface=False)
+    st = orc.get_state()
+    gpu = make_gpu(case, prec)
+    gpu.set_state(oracle_state_to_gpu(st))
+    gpu.SPH_run_mesh_generation(20)
+    gpu.sync()
+    orc.steps(20)
+    gp = gpu.particles(("xyz", "type", "h"))
+    os_ = orc.get_state()
+    oxyz = np.stack([os_["x"], os_["y"], os_["z"]], 1)
+    from scipy.spatial import cKDTree
+    def stats(x):
+        d, _ = cKDTree(x[:, :2]).query(x[:, :2], k=2)
+        return d[:, 1].min(), np.median(d[:, 1])
+    gmin, gmed = stats(gp["xyz"])
+    omin, omed = stats(oxyz)
+    assert abs(gmed - omed) <= 0.01 * omed
+    assert abs(gmin - omin) <= 0.05 * omin + 1e-3 * omed
+    assert abs((gp["type"] == 1).sum() - (os_["type"] == 1).sum()) <= 0.01 * len(gp["type"]) + 2
+    s = gpu.stats()
+    assert s["step"] == 20
+    assert s["flags"] & ~L.FLAG_NEIGHBOR_SPILL == 0
+    gpu.close()
+
+
+def test_seed_matches_oracle_fp64():
+    case = CASES["disc2d_hyperbolic"]()
+    orc = oracle.Oracle(case)
+    orc.seed(case.n_particles)
+    orc.pre_run()
+    o = orc.get_state()
+    gpu = make_gpu(case, "fp64")
+    gpu.Initialize_case(case.n_particles)
+    gp = gpu.particles(("xyz", "type", "h"))
+    oxyz = np.stack([o["x"], o["y"], o["z"]], 1)
+    assert np.max(np.abs(gp["xyz"] - oxyz)) < 1e-12
+    assert np.array_equal(gp["type"], o["type"])
+    gpu.close()

@@ -1,0 +1,153 @@
+"""Known-answer tests of the FP64 oracle (CPU).  The reference ships no tests
+or golden vectors, so the oracle is pinned to analytic identities of the
+equations it restates."""
+import numpy as np
+import pytest
+from scipy import integrate
+
+import oracle
+from mrsph import cases
+
+PI_REF = 3.1415926
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_kernel_normalisation(kind, dim):
+    """Integral of W over its support is 1 up to the reference's truncated PI
+    and its rounded coefficients (cubic 0.4547..., quintic 7/478)."""
+    h = 0.7
+    r = np.linspace(0.0, 3.0 * h, 200001)
+    w = oracle.kernel_W(kind, dim, r, h)
+    shell = 2 * np.pi * r if dim == 2 else 4 * np.pi * r * r
+    total = integrate.simpson(w * shell, x=r)
+    tol = {0: 1e-6, 1: 1e-3, 2: 1e-6, 3: 1e-3, 4: 4e-3}[kind]  # Gaussian truncated at 3h; quintic 3/359 rounded
+    assert abs(total - np.pi / PI_REF) < tol
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2, 4])
+def test_kernel_gradient_matches_derivative(kind):
+    h = 0.5
+    r = np.linspace(0.05, 1.9 * h, 400)
+    eps = 1e-6
+    for dim in (2, 3):
+        w1 = oracle.kernel_W(kind, dim, r + eps, h)
+        w0 = oracle.kernel_W(kind, dim, r - eps, h)
+        fd = (w1 - w0) / (2 * eps)
+        dw = oracle.kernel_dW(kind, dim, r, h) * r  # dW returns (dW/dr)/r
+        assert np.max(np.abs(fd - dw)) < 1e-4 * np.max(np.abs(dw))
+
+
+def test_wendland_1d_is_zero():
+    """Reference quirk Q2: the Wendland kernel has no 1D form (returns 0)."""
+    r = np.linspace(0, 1, 10)
+    assert np.all(oracle.kernel_W(2, 1, r, 0.3) == 0)
+    assert np.all(oracle.kernel_dW(2, 1, r, 0.3) == 0)
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 test vectors published with the algorithm (Random123)."""
+    assert oracle.philox(0, 0, 0, 0, 0) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert oracle.philox(0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFFFFFFFFFF) == \
+        [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+
+
+def _linear_case():
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    lv = case.levels[0]
+    ax = cases.cell_centres(lv.box_l, lv.dpkg, lv.num_pkg, lv.margin, 2)
+    Y, X = np.meshgrid(ax[1], ax[0], indexing="ij")
+    lv.phi = (0.3 * X - 0.2 * Y + 0.1)[None, :, :].copy()
+    return case
+
+
+def test_bilinear_interpolation_exact_for_linear_phi():
+    case = _linear_case()
+    orc = oracle.Oracle(case)
+    rng = np.random.default_rng(1)
+    pts = np.zeros((500, 3))
+    pts[:, :2] = 0.05 + 0.9 * rng.random((500, 2))
+    phi, nrm, curv, tag = orc.sample(pts)
+    assert np.max(np.abs(phi - (0.3 * pts[:, 0] - 0.2 * pts[:, 1] + 0.1))) < 1e-14
+    n = np.array([0.3, -0.2]) / np.hypot(0.3, 0.2)
+    assert np.max(np.abs(nrm[:, :2] - n)) < 1e-10
+
+
+def test_projection_lands_on_zero_level():
+    """A REAL particle in a cut cell of a circle is projected onto phi = 0
+    (Find_and_map_particle) to within the interpolation error."""
+    case = cases.disc_hole_2d(spacing=0.005, grid=256)
+    orc = oracle.Oracle(case)
+    rng = np.random.default_rng(2)
+    ang = rng.random(200) * 2 * np.pi
+    rad = 0.2 + (rng.random(200) - 0.5) * 0.002
+    x = np.zeros(200)
+    st = {"x": 0.5 + rad * np.cos(ang), "y": 0.5 + rad * np.sin(ang), "z": x, "h": np.full(200, 0.0065),
+          "type": np.zeros(200, dtype=np.int32), "step": 0, "dt": 0.0}
+    orc.set_state(st)
+    orc.phase_map(advect=False)
+    s = orc.get_state()
+    surf = s["type"] == 1
+    assert surf.sum() > 150
+    r = np.hypot(s["x"][surf] - 0.5, s["y"][surf] - 0.5)
+    assert np.max(np.abs(r - 0.2)) < 2e-4
+
+
+def test_scale_law_endpoints():
+    case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    orc = oracle.Oracle(case)
+    mp = orc.ctx.max_phi
+    assert abs(orc.get_scale(0.0) - 0.03) < 1e-15
+    assert abs(orc.get_scale(mp) - 0.09) < 1e-12
+    assert orc.get_scale(-1.0) == 0.03
+
+
+def test_lattice_gradient_sum_vanishes():
+    """On a perfect lattice with uniform h the stage-1 force of an interior
+    particle is zero (antisymmetric gradient sum)."""
+    case = cases.disc_hole_2d(spacing=0.01, grid=256, kernel="wendland")
+    orc = oracle.Oracle(case)
+    g = np.arange(0.1, 0.3, 0.01)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    n = X.size
+    st = {"x": X.ravel(), "y": Y.ravel(), "z": np.zeros(n), "h": np.full(n, 0.013),
+          "rho": np.full(n, 1e4), "type": np.zeros(n, dtype=np.int32), "step": 0, "dt": 0.0,
+          "level": np.zeros(n, dtype=np.int32)}
+    orc.set_state(st)
+    off, nb = orc.neighbors()
+    orc.density(off, nb)
+    orc.force(off, nb, 1)
+    s = orc.get_state()
+    inner = (np.abs(X.ravel() - 0.195) < 0.05) & (np.abs(Y.ravel() - 0.195) < 0.05)
+    a = np.hypot(s["ax"], s["ay"])
+    assert np.max(a[inner]) < 1e-9 * np.max(np.abs(s["sum"])) * 1e3
+
+
+def test_level_plan_restates_define_level_infor_tight():
+    case = cases.torus_3d(dx_min=0.005, dx_max=0.02)
+    orc = oracle.Oracle(case)
+    lv = orc.levels()
+    assert lv["ncl"] == 3
+    for l in range(3):
+        assert abs(lv["scale"][l] - lv["max_scale"] / 2 ** l) < 1e-10
+    assert lv["ncell"][2] == [216, 216, 68]
+
+
+def test_neighbor_relation_symmetric_and_includes_self():
+    case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    orc = oracle.Oracle(case)
+    orc.seed(case.n_particles)
+    orc.pre_run()
+    for _ in range(40):  # relax until surface particles (finest spacing) appear
+        orc.steps(1)
+        if (orc.arrays["type"] == 1).sum() > 100:
+            break
+    off, nb = orc.neighbors()
+    n = len(off) - 1
+    sets = [set(nb[off[i]:off[i + 1]].tolist()) for i in range(n)]
+    assert all(i in sets[i] for i in range(n))
+    for i in range(0, n, 7):
+        for j in sets[i]:
+            assert i in sets[j]
+    lev = orc.arrays["level"]
+    assert len(set(lev.tolist())) >= 2  # adaptive: more than one cell-list level
