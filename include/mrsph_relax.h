@@ -171,6 +171,18 @@ int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, doubl
 int mrsph_sample_levelset(mrsph_handle* h, long long n, const double* xyz, double* phi, double* norm,
                           double* curv, int* tag);
 
+/* No counterpart in the reference.  Same results as mrsph_sample_levelset for
+ * callers that cannot allocate device memory (cudaMalloc synchronises the
+ * device and may be forbidden where another allocator owns the memory or on a
+ * latency-critical path): points and results are staged through a fixed
+ * scratch array that is part of the library image (held on every GPU that
+ * loads the library until exit).  At most 65536 points per call, else
+ * MRSPH_ERR_RANGE.  The first call on a device looks up the scratch address;
+ * make that first call before any stream capture.  All calls on a device
+ * share the scratch: calls that overlap on the GPU race. */
+int mrsph_sample_levelset_noalloc(mrsph_handle* h, long long n, const double* xyz, double* phi, double* norm,
+                                  double* curv, int* tag);
+
 /* Random_particle_distribution (sph_mesh_generation.cpp:1302-1367) + Pre_run
  * (:1010-1050): n particles seeded where phi > h. */
 int mrsph_seed(mrsph_handle* h, long long n);

@@ -1015,6 +1015,14 @@ class Engine : public EngineBase {
     return 0;
   }
 
+  int sample_device(long long n, const double* d_xyz, double* d_out) override {
+    k_sample_points<D, R><<<grid(n), 256, 0, st_>>>(kc_, n, d_xyz, d_out);
+    MR_CK(cudaGetLastError());
+    return 0;
+  }
+
+  cudaStream_t stream() const override { return st_; }
+
  private:
   static unsigned long long dbits_host(double x) { unsigned long long u; std::memcpy(&u, &x, 8); return u; }
   static double bitsd_host(unsigned long long u) { double x; std::memcpy(&x, &u, 8); return x; }

@@ -32,6 +32,10 @@ class EngineBase {
   virtual int upload_positions(const double* xyz) = 0;
   virtual int download_positions(double* xyz) = 0;
   virtual int sample(long long n, const double* xyz, double* phi, double* norm, double* curv, int* tag) = 0;
+  // Level-set sampling between caller-owned device buffers (xyz n x 3 in,
+  // out n x 6: phi, nx, ny, nz, curv, tag); enqueued on the engine stream.
+  virtual int sample_device(long long n, const double* d_xyz, double* d_out) = 0;
+  virtual cudaStream_t stream() const = 0;
   std::string err;
 };
 

@@ -1,0 +1,18 @@
+// handle.h — the opaque mrsph_handle of the C ABI (internal).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "engine_iface.h"
+
+struct mrsph_handle {
+  mrsph_params prm{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  mrsph::CellGeo geo{};
+  mrsph::LsSet ls{};
+  int nls = 0;
+  long long ls_ntot[mrsph::MAX_LS] = {0, 0, 0, 0};
+  std::vector<void*> ls_allocs;
+  mrsph::EngineBase* eng = nullptr;
+};

@@ -10,19 +10,9 @@
 
 #include "engine_iface.h"
 
-using namespace mrsph;
+#include "handle.h"
 
-struct mrsph_handle {
-  mrsph_params prm{};
-  std::string err;
-  cudaStream_t stream = nullptr;
-  CellGeo geo{};
-  LsSet ls{};
-  int nls = 0;
-  long long ls_ntot[MAX_LS] = {0, 0, 0, 0};
-  std::vector<void*> ls_allocs;
-  EngineBase* eng = nullptr;
-};
+using namespace mrsph;
 
 static thread_local std::string g_create_error;
 

@@ -58,6 +58,7 @@ EXPORTS = {
     "mrsph_set_levelset": ([C.c_void_p, C.c_int, C.POINTER(LevelsetLevel)], C.c_int),
     "mrsph_get_levelset": ([C.c_void_p, C.c_int] + [C.c_void_p] * 5 + [C.POINTER(C.c_double)], C.c_int),
     "mrsph_sample_levelset": ([C.c_void_p, C.c_longlong] + [C.c_void_p] * 5, C.c_int),
+    "mrsph_sample_levelset_noalloc": ([C.c_void_p, C.c_longlong] + [C.c_void_p] * 5, C.c_int),
     "mrsph_seed": ([C.c_void_p, C.c_longlong], C.c_int),
     "mrsph_set_state": ([C.c_void_p, C.c_longlong, C.POINTER(StateIn), C.c_int], C.c_int),
     "mrsph_step": ([C.c_void_p, C.c_int], C.c_int),

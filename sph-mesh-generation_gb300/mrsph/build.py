@@ -24,6 +24,7 @@ SOURCES = {
     "mrsph_levelset.cu": ["-fmad=false"],
     "mrsph_fp64.cu": ["-fmad=false"],
     "mrsph_fp32.cu": [],
+    "mrsph_noalloc.cu": [],
 }
 
 

@@ -206,6 +206,18 @@ class SPHMeshGeneration:
                 self.h, "mrsph_sample_levelset")
         return phi, nrm, curv, tag
 
+    def sample_levelset_noalloc(self, xyz: np.ndarray):
+        """Same as sample_levelset without any device allocation (<= 65536 points)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = len(xyz)
+        phi = np.zeros(n)
+        nrm = np.zeros((n, 3))
+        curv = np.zeros(n)
+        tag = np.zeros(n, dtype=np.int32)
+        L.check(self.lib.mrsph_sample_levelset_noalloc(self.h, n, _ptr(xyz), _ptr(phi), _ptr(nrm), _ptr(curv),
+                                                       _ptr(tag)), self.h, "mrsph_sample_levelset_noalloc")
+        return phi, nrm, curv, tag
+
     def upload_positions(self, xyz: np.ndarray):
         L.check(self.lib.mrsph_upload_positions(self.h, _ptr(xyz)), self.h, "mrsph_upload_positions")
 
