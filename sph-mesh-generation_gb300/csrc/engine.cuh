@@ -12,7 +12,7 @@
 //   scan x3, scatter, rank      A5 counting sort into (level, cell) order
 //   k_reorder      gather persistent state into the sorted order
 //   k_density      A6 neighbour search over the cell table + A7 kernel sum,
-//                  writes the neighbour list (ELL, column-major)
+//                  writes the neighbour list (one row per particle)
 //   k_force<1>     A8 stage 1 + A9 dt/max|v| grid reduction (FP64 bit atomics)
 //   k_force<2>     A8 stage 2 + A9 + A10 (stage-1 kick folded in; the stage-2
 //                  kick is folded into the next k_map)
@@ -47,6 +47,7 @@ struct Buf {  // persistent per-particle state, one ping-pong half
   R* phi;
   R* curv;
   int* cellkey;             // (level, cell) table index
+  typename V4<R>::T* rec;   // packed neighbour-pass record, 2 words per particle
 };
 
 template <class R>
@@ -54,7 +55,7 @@ struct Work {  // per-step arrays in sorted order
   R* sum;
   typename V4<R>::T* a1;
   int* cnt;
-  int* nbl;  // neighbour list, column-major: nbl[q * n + i]
+  int* nbl;  // neighbour lists, one row of `cap` entries per particle
   int cap;
   int* counts;
   int* cstart;
@@ -372,16 +373,59 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
   if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&c.sc->nsurf, ws);
 }
 
+// Packed record read by the neighbour passes, two V4 words per particle so
+// that one candidate costs one 32-byte sector (FP32):
+//   FP32: w0 = (offset x, y, z, h), w1 = (anchor x, y, z as exact floats, +-rho)
+//   FP64: w0 = (x, y, z, h),        w1 = (0, 0, 0, +-rho)
+// The sign of rho carries the type: negative for a SURFACE particle.
+template <int D, class R> struct RecOps;
+template <int D>
+struct RecOps<D, double> {
+  __device__ static void pack(const KCtx&, const double4& p, int, int type, double rho, double4& w0, double4& w1) {
+    w0 = p;
+    w1 = make_double4(0.0, 0.0, 0.0, type == SURFACE_P ? -rho : rho);
+  }
+  __device__ static void rel(const KCtx&, const double4& a0, const double4&, const double4& b0, const double4&,
+                             double* dr) {
+    dr[0] = a0.x - b0.x;
+    dr[1] = a0.y - b0.y;
+    dr[2] = (D == 3) ? a0.z - b0.z : 0.0;
+  }
+};
+template <int D>
+struct RecOps<D, float> {
+  __device__ static void pack(const KCtx&, const float4& p, int key, int type, float rho, float4& w0, float4& w1) {
+    int k[3];
+    PosOps<D, float>::unpack(key, k);
+    w0 = p;
+    w1 = make_float4((float)k[0], (float)k[1], (float)k[2], type == SURFACE_P ? -rho : rho);
+  }
+  __device__ static void rel(const KCtx& c, const float4& a0, const float4& a1, const float4& b0, const float4& b1,
+                             float* dr) {
+    dr[0] = (a1.x - b1.x) * c.geo.Af[0] + (a0.x - b0.x);
+    dr[1] = (a1.y - b1.y) * c.geo.Af[1] + (a0.y - b0.y);
+    dr[2] = (D == 3) ? (a1.z - b1.z) * c.geo.Af[2] + (a0.z - b0.z) : 0.f;
+  }
+};
+
 template <int D, class R>
-__global__ void k_reorder(Buf<R> src, Buf<R> dst, const int* __restrict__ perm2, int* __restrict__ slot_of_id,
-                          long long n, int partial) {
+__global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict__ perm2,
+                          int* __restrict__ slot_of_id, long long n, int partial) {
   long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   int o = perm2[s];
-  dst.posh[s] = src.posh[o];
-  if (src.key) dst.key[s] = src.key[o];
-  dst.nr[s] = src.nr[o];
-  dst.meta[s] = src.meta[o];
+  const auto p = src.posh[o];
+  const int key = src.key ? src.key[o] : 0;
+  const auto nr = src.nr[o];
+  const int meta = src.meta[o];
+  dst.posh[s] = p;
+  if (src.key) dst.key[s] = key;
+  dst.nr[s] = nr;
+  dst.meta[s] = meta;
+  typename V4<R>::T w0, w1;
+  RecOps<D, R>::pack(c, p, key, meta & 0xFF, nr.w, w0, w1);
+  dst.rec[2 * s] = w0;
+  dst.rec[2 * s + 1] = w1;
   int id = src.id[o];
   dst.id[s] = id;
   dst.nu[s] = src.nu_next[o];
@@ -442,58 +486,60 @@ __device__ inline bool nb_test(float d2, float hi, float hj, double cutoff, floa
   return true;
 }
 
+template <class R> __device__ inline R d2_of(const R* dr, int D) {
+  R d2 = 0;
+  d2 += dr[0] * dr[0];
+  d2 += dr[1] * dr[1];
+  if (D == 3) d2 += dr[2] * dr[2];
+  return d2;
+}
+
 // A6 + A7: Refresh_neighbor_info (level_infor.cpp:469-506) and
-// Get_kernel_summation (particle_mesh_generation.cpp:690-765).
+// Get_kernel_summation (particle_mesh_generation.cpp:690-765).  The
+// neighbour list is written row-major (one row of `cap` entries per
+// particle), in the fixed scan order.
 template <int D, class R>
 __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
+  using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long pairs = 0;
   if (i < c.n) {
-    const T4 pi = b.posh[i];
-    const int ki = b.key ? b.key[i] : 0;
+    const T4 a0 = b.rec[2 * i], a1 = b.rec[2 * i + 1];
     const int mi = b.meta[i];
     const int ti = mi & 0xFF;
     const int Li = (int)(signed char)((mi >> 8) & 0xFF);
-    const T4 nri = b.nr[i];
-    const R ni[3] = {nri.x, nri.y, nri.z};
-    const R hi = pi.w;
+    R ni[3] = {0, 0, 0};
+    if (ti == SURFACE_P) {
+      const T4 nri = b.nr[i];
+      ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
+    }
+    const R hi = a0.w;
     const R cos_t = (R)c.prm.cos_thres;
     int ci[3];
-    P::cell(c, Li, pi, ki, ci);
+    P::cell(c, Li, b.posh[i], b.key ? b.key[i] : 0, ci);
     R sum = 0;
     int ncount = 0, cnt = 0;
-    const long long n = c.n;
+    int* row = w.nbl + i * (long long)w.cap;
     scan_candidates<D>(c, w.cstart, Li, ci, [&](int j) {
-      const T4 pj = b.posh[j];
-      const int kj = b.key ? b.key[j] : 0;
+      const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
       R dr[3];
-      P::rel(c, pi, ki, pj, kj, dr);
-      R d2 = 0;
-      d2 += dr[0] * dr[0];
-      d2 += dr[1] * dr[1];
-      if (D == 3) d2 += dr[2] * dr[2];
+      Q::rel(c, a0, a1, b0, b1, dr);
       R dist;
-      if (!nb_test(d2, hi, pj.w, c.prm.cutoff, dist)) return;
-      if (cnt < w.cap) w.nbl[(long long)cnt * n + i] = j;
+      if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
+      if (cnt < w.cap) row[cnt] = j;
       cnt++;
       if (ti == REAL_P) {
         sum += kernel_W<R>(c.prm.kernel, D, dist, hi);
         ncount++;
-      } else if (ti == SURFACE_P) {
-        const int tj = b.meta[j] & 0xFF;
+      } else if (ti == SURFACE_P && b1.w < (R)0) {  // surface neighbour of a surface particle
         R dn = dot3<D, R>(dr, ni);
         R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
         R pd = r_sqrt(dot3<D, R>(pr, pr));
-        if (tj == SURFACE_P) {
-          const T4 nrj = b.nr[j];
-          const R nj[3] = {nrj.x, nrj.y, nrj.z};
-          if (r_fabs(dot3<D, R>(ni, nj)) > cos_t) {
-            sum += kernel_W<R>(c.prm.kernel, D - 1, pd, hi);
-            ncount++;
-          }
-        } else if (tj == SEGMENT_P || tj == SINGULARITY_P) {
+        const T4 nrj = b.nr[j];
+        const R nj[3] = {nrj.x, nrj.y, nrj.z};
+        if (r_fabs(dot3<D, R>(ni, nj)) > cos_t) {
           sum += kernel_W<R>(c.prm.kernel, D - 1, pd, hi);
           ncount++;
         }
@@ -513,45 +559,46 @@ __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
 
 static __global__ void k_accum_pairs(DevScalars* sc) { sc->pairs_total += sc->pairs; }
 
-// A8 force stages + A9 timestep (Set_timestep(stage), particle_mesh_generation.cpp:127-145)
+// A8 force stages + A9 timestep (Set_timestep(stage), particle_mesh_generation.cpp:127-145).
+// Stage 1 stores (a1, nu) so that stage 2 reads one vector per neighbour.
 template <int D, class R, int STAGE>
 __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
+  using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double my_dt = 1.e300, my_v = 0.0;
   if (i < c.n) {
-    const long long n = c.n;
-    const T4 pi = b.posh[i];
-    const int ki = b.key ? b.key[i] : 0;
+    const T4 a0 = b.rec[2 * i], a1r = b.rec[2 * i + 1];
     const int mi = b.meta[i];
     const int ti = mi & 0xFF;
-    const T4 nri = b.nr[i];
-    const R ni[3] = {nri.x, nri.y, nri.z};
-    const R rho = nri.w, h = pi.w;
+    R ni[3] = {0, 0, 0};
+    if (ti == SURFACE_P) {
+      const T4 nri = b.nr[i];
+      ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
+    }
+    const R rho = r_fabs(a1r.w), h = a0.w;
     const R cos_t = (R)c.prm.cos_thres;
     const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
-    const R nu = (STAGE == 2) ? b.nu[i] : (R)0;
+    R nu = 0;
     R hdt1 = 0;
     R vi[3] = {0, 0, 0};
     if (STAGE == 2) {
       hdt1 = (R)(0.5 * bitsd(c.sc->dt1));
-      T4 a1 = w.a1[i];
-      vi[0] = a1.x * hdt1; vi[1] = a1.y * hdt1; vi[2] = a1.z * hdt1;
+      T4 an = w.a1[i];
+      vi[0] = an.x * hdt1; vi[1] = an.y * hdt1; vi[2] = an.z * hdt1;
+      nu = an.w;
+    } else {
+      nu = b.nu[i];
     }
     R F[3] = {0, 0, 0};
     const R vol_i = (R)1.0 / (rho * rho);
-    auto pair = [&](int j) {
+    auto pair = [&](int j, const T4& b0, const T4& b1, const R* vec) {
       if (j == (int)i) return;
-      const int tj = b.meta[j] & 0xFF;
-      if (ti == SURFACE_P && tj == REAL_P) return;
-      const T4 pj = b.posh[j];
-      const int kj = b.key ? b.key[j] : 0;
-      const T4 nrj = b.nr[j];
-      R vec[3];
-      P::rel(c, pi, ki, pj, kj, vec);
+      const bool surf_j = b1.w < (R)0;
+      if (ti == SURFACE_P && !surf_j) return;
       R dr[3], aw;
-      const R hij = (R)0.5 * (h + pj.w);
+      const R hij = (R)0.5 * (h + b0.w);
       if (ti == REAL_P) {
         dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
         R dist = r_sqrt(dot3<D, R>(dr, dr));
@@ -560,26 +607,25 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
         R dn = dot3<D, R>(vec, ni);
         dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
         R dist = r_sqrt(dot3<D, R>(dr, dr));
-        if (tj == SURFACE_P) {
-          const R nj[3] = {nrj.x, nrj.y, nrj.z};
-          if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return;
-        }
+        const T4 nrj = b.nr[j];
+        const R nj[3] = {nrj.x, nrj.y, nrj.z};
+        if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return;
         aw = kernel_dW<R>(c.prm.kernel, D - 1, dist, hij);
       }
-      const R rho_j = nrj.w;
+      const R rho_j = r_fabs(b1.w);
       if (STAGE == 1) {
         const R vol_j = (R)1.0 / (rho_j * rho_j);
         const R P_ij = sum * (vol_i + vol_j);
         for (int d = 0; d < D; d++) F[d] = F[d] + (dr[d] * aw) * -P_ij;
       } else {
+        const T4 anj = w.a1[j];
         R vj[3];
-        if (ti == REAL_P && tj != REAL_P) {
+        if (ti == REAL_P && surf_j) {
           vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
         } else {
-          T4 a1j = w.a1[j];
-          vj[0] = a1j.x * hdt1; vj[1] = a1j.y * hdt1; vj[2] = a1j.z * hdt1;
+          vj[0] = anj.x * hdt1; vj[1] = anj.y * hdt1; vj[2] = anj.z * hdt1;
         }
-        const R nu_j = b.nu[j];
+        const R nu_j = anj.w;
         const R eta_i = nu * rho, eta_j = nu_j * rho_j;
         const R eta_ij = (R)2. * eta_j * eta_i / (eta_i + eta_j + (R)1.e-15);
         const R temp0 = aw * eta_ij * ((R)1. / rho / rho + (R)1. / rho_j / rho_j);
@@ -589,22 +635,24 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
     if (ti == REAL_P || ti == SURFACE_P) {
       const int cnt = w.cnt[i];
       if (cnt <= w.cap) {
-        for (int q = 0; q < cnt; q++) pair(__ldg(&w.nbl[(long long)q * n + i]));
+        const int* row = w.nbl + i * (long long)w.cap;
+        for (int q = 0; q < cnt; q++) {
+          const int j = __ldg(&row[q]);
+          const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
+          R vec[3];
+          Q::rel(c, a0, a1r, b0, b1, vec);
+          pair(j, b0, b1, vec);
+        }
       } else {
         const int Li = (int)(signed char)((mi >> 8) & 0xFF);
         int ci[3];
-        P::cell(c, Li, pi, ki, ci);
+        P::cell(c, Li, b.posh[i], b.key ? b.key[i] : 0, ci);
         scan_candidates<D>(c, w.cstart, Li, ci, [&](int j) {
-          const T4 pj = b.posh[j];
-          const int kj = b.key ? b.key[j] : 0;
-          R dr[3];
-          P::rel(c, pi, ki, pj, kj, dr);
-          R d2 = 0;
-          d2 += dr[0] * dr[0];
-          d2 += dr[1] * dr[1];
-          if (D == 3) d2 += dr[2] * dr[2];
+          const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
+          R vec[3];
+          Q::rel(c, a0, a1r, b0, b1, vec);
           R dist;
-          if (nb_test(d2, h, pj.w, c.prm.cutoff, dist)) pair(j);
+          if (nb_test(d2_of(vec, D), h, b0.w, c.prm.cutoff, dist)) pair(j, b0, b1, vec);
         });
       }
     }
@@ -629,7 +677,7 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
       b.v1[i] = mk4<R>(vi[0], vi[1], vi[2], U);
       b.a2[i] = mk4<R>(a[0], a[1], a[2], 0);
     } else {
-      w.a1[i] = mk4<R>(a[0], a[1], a[2], 0);
+      w.a1[i] = mk4<R>(a[0], a[1], a[2], nu);
     }
     my_dt = (double)ts;
     my_v = (double)U;
@@ -971,7 +1019,7 @@ class Engine : public EngineBase {
     for (long long k = 0; k < n_; k++) off[k + 1] = off[k] + byid_cnt[k];
     for (long long s = 0; s < n_; s++) {
       long long base = off[ids[s]];
-      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nbl[(size_t)q * n_ + s]];
+      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nbl[(size_t)s * w_.cap + q]];
       std::sort(nb + base, nb + base + cnt[s]);
     }
     return 0;
@@ -1050,7 +1098,7 @@ class Engine : public EngineBase {
     cell_scan(w_.counts, w_.cstart, w_.blocksums, ncells_, (int)n, st_);
     cell_scatter(buf_[cur_].cellkey, w_.counts, w_.cstart, w_.perm, n, st_);
     cell_rank(buf_[cur_].cellkey, w_.cstart, w_.perm, buf_[cur_].id, w_.perm2, n, st_);
-    k_reorder<D, R><<<grid(n), 256, 0, st_>>>(buf_[cur_], buf_[cur_ ^ 1], w_.perm2, w_.slot_of_id, n, partial);
+    k_reorder<D, R><<<grid(n), 256, 0, st_>>>(buf_[cur_], buf_[cur_ ^ 1], kc_, w_.perm2, w_.slot_of_id, n, partial);
     MR_CK(cudaGetLastError());
     cur_ ^= 1;
     return 0;
@@ -1071,7 +1119,7 @@ class Engine : public EngineBase {
     cell_scatter(buf_[cur_].cellkey, w_.counts, w_.cstart, w_.perm, n, st_);
     cell_rank(buf_[cur_].cellkey, w_.cstart, w_.perm, buf_[cur_].id, w_.perm2, n, st_);
     mark(3);
-    k_reorder<D, R><<<grid(n), 256, 0, st_>>>(buf_[cur_], buf_[cur_ ^ 1], w_.perm2, w_.slot_of_id, n,
+    k_reorder<D, R><<<grid(n), 256, 0, st_>>>(buf_[cur_], buf_[cur_ ^ 1], kc_, w_.perm2, w_.slot_of_id, n,
                                               phase < MRSPH_PHASE_FORCE2 ? 1 : 0);
     MR_CK(cudaGetLastError());
     cur_ ^= 1;
@@ -1166,6 +1214,7 @@ class Engine : public EngineBase {
       rc |= A((void**)&b.phi, sizeof(R) * n);
       rc |= A((void**)&b.curv, sizeof(R) * n);
       rc |= A((void**)&b.cellkey, sizeof(int) * n);
+      rc |= A((void**)&b.rec, sizeof(T4) * 2 * n);
     }
     if (!rc) {
       rc |= A((void**)&w_.sum, sizeof(R) * n);
