@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cvp-vps", type=int, default=256)
+    ap.add_argument("--cvp-iters", type=int, default=50)
     return ap.parse_args()
 
 
@@ -288,6 +290,19 @@ def run_mrsph(args, ws, rank, local, dist):
            "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out.nbytes) + 96,
            "steps": args.e2e_steps, "pinned": pinned, "timer": "host wall clock, synchronised"}
     flags = s["flags"]
+    # CVP partition of the relaxed particles (256 cells, 50 Lloyd iterations)
+    cvp = None
+    if args.cvp_vps > 0:
+        xyz_now = gpu.particles(("xyz",))["xyz"]
+        rng = np.random.default_rng(0)
+        vp0 = xyz_now[rng.choice(n, args.cvp_vps, replace=False)].copy()
+        gpu.sync()
+        t0 = time.perf_counter()
+        _, labels, vmass, cres = gpu.Partitioning(vp0, max_iter=args.cvp_iters - 1)
+        cvp_s = time.perf_counter() - t0
+        cvp = {"num_vp": args.cvp_vps, "iterations": cres["iterations"], "seconds": cvp_s,
+               "ms_per_iteration": 1000.0 * cvp_s / max(cres["iterations"], 1), "error_max": cres["error_max"],
+               "points": n, "timer": "host wall clock around mrsph_cvp (FP64, bit-exact vs the oracle)"}
     gpu.close()
 
     # FP64-plain path on the same workload
@@ -316,7 +331,7 @@ def run_mrsph(args, ws, rank, local, dist):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(case, args.workload),
             "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
             "fp64_plain": fp64, "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
-            "phase_ms": prof, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "phase_ms": prof, "cvp": cvp, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": 12 * args.steps, "clocks": clocks, "device_flags": flags}
     print(json.dumps(line), flush=True)
 

@@ -222,6 +222,38 @@ int mrsph_get_cells(mrsph_handle* h, int* level_cell, int* sorted_ids);
  * neighbour ids ascending.  Call with nb == NULL to get *total only. */
 int mrsph_get_neighbors(mrsph_handle* h, long long* offsets, int* nb, long long cap, long long* total);
 
+/* Centroidal Voronoi partitioning (row A13): Voronoi::Partitioning
+ * (src/CVP/voronoi.cpp:1376-1446) with Get_CPU_id assignment (:480-493),
+ * mass / mass-centre / energy sums (:617-631), face-pressure step
+ * Update_position (:830-897), Lloyd step Update_position_CVT (:901-992) and
+ * the convergence test Check_partition_error (:1228-1262).  voro++ faces are
+ * replaced by exact in-box Voronoi faces computed on the GPU. */
+typedef struct {
+  int num_vp;             /* K partitions, 1..1024 */
+  int max_iter;           /* Max_iterate_number (reference 4000; 800 for level-set packages) */
+  int pressure_step;      /* 1: face-pressure move before the Lloyd step (reference); 0: Lloyd only */
+  double error_tolerance; /* reference 0.05 */
+  double relax_ratio;     /* initial relax ratio (reference 0.8) */
+} mrsph_cvp_params;
+
+typedef struct {
+  int iterations;
+  int converged;
+  double error_max;     /* max |mass - target| / target of the last iteration */
+  double total_energy;  /* sum of mass x distance to the VP */
+} mrsph_cvp_result;
+
+/* Partition the handle's particles (mass 1).  vp_xyz (K x 3) holds the
+ * initial VP positions and receives the final ones; labels (n, id order) and
+ * vp_mass (K) may be NULL. */
+int mrsph_cvp(mrsph_handle* h, const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass,
+              mrsph_cvp_result* res);
+/* Same on given host points with masses (e.g. level-set package centres with
+ * their total mass, Voronoi_lset); mass NULL = 1.  The box is the handle's domain. */
+int mrsph_cvp_points(mrsph_handle* h, long long n, const double* xyz, const double* mass,
+                     const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass,
+                     mrsph_cvp_result* res);
+
 /* e2e helpers: positions in id order (n x 3), host memory (pinned or not). */
 int mrsph_upload_positions(mrsph_handle* h, const double* xyz);
 int mrsph_download_positions(mrsph_handle* h, double* xyz);

@@ -1145,6 +1145,305 @@ long long orc_steps(const orc_ctx* c, orc_state* s, int nsteps) {
   return pairs;
 }
 
+// ===========================================================================
+// A13 CVP: Voronoi::Partitioning (CVP/voronoi.cpp:1376-1446) on a weighted
+// point set.  voro++ is replaced by exact in-box Voronoi faces: the face of
+// VP k on plane p (a bisector with VP m, or a box wall) is the plane's
+// polygon inside the box clipped by every other bisector half-space.
+// Per-VP sums run in particle order split into CVP_CHUNK-particle chunks
+// (chunk partials, then partials in chunk order); faces are summed in plane
+// order (VPs by index, then walls x-, x+, y-, y+, z-, z+).
+// ===========================================================================
+struct orc_cvp_params {
+  int dim, num_vp, max_iter, pressure_step;
+  double error_tolerance, relax_ratio;
+  double box_l[3], box_r[3];
+};
+struct orc_cvp_result { int iterations, converged; double error_max, total_energy; };
+
+static const int CVP_CHUNK = 2048;
+static const int CVP_MAXV = 64;
+
+static inline double cvp_dot(const double* a, const double* b) {
+  double s = 0.0;
+  s += a[0] * b[0];
+  s += a[1] * b[1];
+  s += a[2] * b[2];
+  return s;
+}
+
+// keep the part of polygon v (nv vertices) with n.x - d <= 0
+static int cvp_clip(double (*v)[3], int nv, const double* n, double d, double (*o)[3]) {
+  int no = 0;
+  for (int a = 0; a < nv; a++) {
+    int b = (a + 1) % nv;
+    double sa = cvp_dot(n, v[a]) - d, sb = cvp_dot(n, v[b]) - d;
+    if (sa <= 0.0) {
+      if (no < CVP_MAXV) { o[no][0] = v[a][0]; o[no][1] = v[a][1]; o[no][2] = v[a][2]; }
+      no++;
+    }
+    if ((sa <= 0.0) != (sb <= 0.0)) {
+      double t = sa / (sa - sb);
+      if (no < CVP_MAXV)
+        for (int q = 0; q < 3; q++) o[no][q] = v[a][q] + (v[b][q] - v[a][q]) * t;
+      no++;
+    }
+  }
+  return no < CVP_MAXV ? no : CVP_MAXV;
+}
+
+// plane p of VP k: unit normal n (outward of k) and offset d (n.x <= d inside)
+static void cvp_plane(const orc_cvp_params& P, const double* vp, int k, int p, double* n, double* d) {
+  const int K = P.num_vp;
+  if (p < K) {
+    const double* ck = vp + 3 * k;
+    const double* cm = vp + 3 * p;
+    double e[3] = {cm[0] - ck[0], cm[1] - ck[1], cm[2] - ck[2]};
+    double len = std::sqrt(cvp_dot(e, e));
+    double mid[3] = {0.5 * (ck[0] + cm[0]), 0.5 * (ck[1] + cm[1]), 0.5 * (ck[2] + cm[2])};
+    for (int q = 0; q < 3; q++) n[q] = e[q] / len;
+    *d = cvp_dot(n, mid);
+  } else {
+    int w = p - K, ax = w / 2, hi = w % 2;
+    n[0] = n[1] = n[2] = 0.0;
+    n[ax] = hi ? 1.0 : -1.0;
+    *d = hi ? P.box_r[ax] : -P.box_l[ax];
+  }
+}
+
+// face of VP k on plane p: returns 1 and area, normal, dist if non-empty
+static int cvp_face(const orc_cvp_params& P, const double* vp, int k, int p, double* area, double* nrm, double* dist) {
+  const int K = P.num_vp;
+  double n[3], d;
+  cvp_plane(P, vp, k, p, n, &d);
+  double lo[3], hi[3];
+  for (int q = 0; q < 3; q++) {
+    lo[q] = q < P.dim ? P.box_l[q] : -0.5;
+    hi[q] = q < P.dim ? P.box_r[q] : 0.5;
+  }
+  double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+  double S = 0.0;
+  for (int q = 0; q < 3; q++) S += (hi[q] - lo[q]) * (hi[q] - lo[q]);
+  S = 2.0 * std::sqrt(S);
+  // in-plane frame
+  int ax = 0;
+  if (std::fabs(n[1]) < std::fabs(n[ax])) ax = 1;
+  if (std::fabs(n[2]) < std::fabs(n[ax])) ax = 2;
+  double e[3] = {0, 0, 0};
+  e[ax] = 1.0;
+  double u[3] = {n[1] * e[2] - n[2] * e[1], n[2] * e[0] - n[0] * e[2], n[0] * e[1] - n[1] * e[0]};
+  double ul = std::sqrt(cvp_dot(u, u));
+  for (int q = 0; q < 3; q++) u[q] = u[q] / ul;
+  double w[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2], n[0] * u[1] - n[1] * u[0]};
+  double off = d - cvp_dot(n, c);
+  double p0[3] = {c[0] + n[0] * off, c[1] + n[1] * off, c[2] + n[2] * off};
+  double A[CVP_MAXV][3], B[CVP_MAXV][3];
+  const double sg[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+  for (int a = 0; a < 4; a++)
+    for (int q = 0; q < 3; q++) A[a][q] = p0[q] + u[q] * (sg[a][0] * S) + w[q] * (sg[a][1] * S);
+  int nv = 4;
+  // box walls (the plane's own wall excluded)
+  for (int wq = 0; wq < 6 && nv > 0; wq++) {
+    if (p >= K && wq == p - K) continue;
+    int axw = wq / 2, hw = wq % 2;
+    double wn[3] = {0, 0, 0};
+    wn[axw] = hw ? 1.0 : -1.0;
+    double wd = hw ? hi[axw] : -lo[axw];
+    nv = cvp_clip(A, nv, wn, wd, B);
+    for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
+  }
+  // other bisectors
+  for (int m = 0; m < K && nv > 0; m++) {
+    if (m == k || m == p) continue;
+    double bn[3], bd;
+    cvp_plane(P, vp, k, m, bn, &bd);
+    nv = cvp_clip(A, nv, bn, bd, B);
+    for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
+  }
+  if (nv < 3) return 0;
+  double ar = 0.0;
+  for (int a = 1; a + 1 < nv; a++) {
+    double x[3] = {A[a][0] - A[0][0], A[a][1] - A[0][1], A[a][2] - A[0][2]};
+    double y[3] = {A[a + 1][0] - A[0][0], A[a + 1][1] - A[0][1], A[a + 1][2] - A[0][2]};
+    double cr[3] = {x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0]};
+    ar += cvp_dot(cr, n);
+  }
+  ar = 0.5 * std::fabs(ar);
+  double ext = S * S;
+  if (!(ar > 1.e-13 * ext)) return 0;
+  *area = ar;
+  nrm[0] = n[0]; nrm[1] = n[1]; nrm[2] = n[2];
+  const double* ck = vp + 3 * k;
+  double dx[3] = {A[0][0] - ck[0], A[0][1] - ck[1], A[0][2] - ck[2]};
+  *dist = std::fabs(cvp_dot(dx, n)) * 2.;
+  return 1;
+}
+
+static inline double cvp_dist(int D, const double* a, const double* b) {  // get_distance_2p, glbfunc.h:253-261
+  double s = 0.0;
+  s += (a[0] - b[0]) * (a[0] - b[0]);
+  s += (a[1] - b[1]) * (a[1] - b[1]);
+  if (D == 3) s += (a[2] - b[2]) * (a[2] - b[2]);
+  return std::sqrt(s);
+}
+
+int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const double* pmass, double* vp, int* label,
+            double* vp_mass, orc_cvp_result* res) {
+  const orc_cvp_params& P = *Pp;
+  const int K = P.num_vp, D = P.dim, NP = K + 2 * D;
+  const long long nchunk = (n + CVP_CHUNK - 1) / CVP_CHUNK;
+  std::vector<double> part((size_t)nchunk * K * 5), tmass(nchunk);
+  // Set_target_mass (voronoi.cpp:495-510), chunked order
+  for (long long c = 0; c < nchunk; c++) {
+    double s = 0.0;
+    for (long long i = c * CVP_CHUNK; i < std::min(n, (c + 1) * CVP_CHUNK); i++) s += pmass[i];
+    tmass[c] = s;
+  }
+  double total = 0.0;
+  for (long long c = 0; c < nchunk; c++) total += tmass[c];
+  const double target = total / K;
+  std::vector<double> mass(K), mc(3 * K), energy(K), Pk(K), err(K), f(3 * K), hk(K), shift(3 * K), tcvt(K);
+  std::vector<double> farea((size_t)K * NP), fnrm((size_t)K * NP * 3), fdist((size_t)K * NP);
+  std::vector<int> fex((size_t)K * NP);
+  double relax = P.relax_ratio, error_record = 0.0;
+  int converged = 0, iter = 0;
+  double error_max = 0.0, total_energy = 0.0;
+  for (iter = 0; iter <= P.max_iter && converged == 0; iter++) {
+    double scale_coeff = 0.25 + 1.75 * (1. - AMIN1((iter - 1) / 500., 1.));
+    // assignment: Get_CPU_id (voronoi.cpp:480-493), strict <
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; i++) {
+      double best = 1.e20;
+      int idx = 0;
+      for (int k = 0; k < K; k++) {
+        double dd = cvp_dist(D, xyz + 3 * i, vp + 3 * k);
+        if (dd < best) { best = dd; idx = k; }
+      }
+      label[i] = idx;
+    }
+    // mass, mass centre, energy (voronoi.cpp:617-631)
+#pragma omp parallel for schedule(static)
+    for (long long c = 0; c < nchunk; c++)
+      for (int k = 0; k < K; k++) {
+        double m = 0.0, x = 0.0, y = 0.0, z = 0.0, e = 0.0;
+        for (long long i = c * CVP_CHUNK; i < std::min(n, (c + 1) * CVP_CHUNK); i++) {
+          if (label[i] != k) continue;
+          double pm = pmass[i];
+          m += pm;
+          x = x + xyz[3 * i] * pm;
+          y = y + xyz[3 * i + 1] * pm;
+          z = z + xyz[3 * i + 2] * pm;
+          e += pm * cvp_dist(D, vp + 3 * k, xyz + 3 * i);
+        }
+        double* q = &part[((size_t)c * K + k) * 5];
+        q[0] = m; q[1] = x; q[2] = y; q[3] = z; q[4] = e;
+      }
+    error_max = 0.0;
+    total_energy = 0.0;
+    for (int k = 0; k < K; k++) {
+      double m = 0.0, x = 0.0, y = 0.0, z = 0.0, e = 0.0;
+      for (long long c = 0; c < nchunk; c++) {
+        const double* q = &part[((size_t)c * K + k) * 5];
+        m += q[0]; x = x + q[1]; y = y + q[2]; z = z + q[3]; e += q[4];
+      }
+      mass[k] = m;
+      energy[k] = e;
+      double inv = 1. / m;  // voronoi.cpp:672-687
+      mc[3 * k] = x * inv;
+      mc[3 * k + 1] = y * inv;
+      mc[3 * k + 2] = (D == 3) ? z * inv : 0.0;
+      Pk[k] = target / m;
+      err[k] = std::fabs(m - target) / target;
+    }
+    for (int k = 0; k < K; k++) {
+      error_max = AMAX1(error_max, err[k]);
+      total_energy += energy[k];
+    }
+    // faces (replacing the voro++ loop, voronoi.cpp:724-790)
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long t = 0; t < (long long)K * NP; t++) {
+      int k = (int)(t / NP), p = (int)(t % NP);
+      int pp = (p < K) ? p : K + (p - K);  // walls: x-, x+, y-, y+, (z-, z+)
+      fex[t] = 0;
+      if (p < K && p == k) continue;
+      double ar, nn[3], ds;
+      if (cvp_face(P, vp, k, pp, &ar, nn, &ds)) {
+        fex[t] = 1;
+        farea[t] = ar;
+        fnrm[3 * t] = nn[0]; fnrm[3 * t + 1] = nn[1]; fnrm[3 * t + 2] = nn[2];
+        fdist[t] = ds;
+      }
+    }
+    for (int k = 0; k < K; k++) {
+      double fx = 0.0, fy = 0.0, fz = 0.0, sr = 0.0;
+      int nnb = 0;
+      for (int p = 0; p < NP; p++) {
+        size_t t = (size_t)k * NP + p;
+        if (!fex[t]) continue;
+        nnb++;
+        double nP = (p < K) ? Pk[p] : Pk[k];
+        sr += fdist[t];
+        double pmid = 0.5 * (Pk[k] + nP);
+        double coef = -1 * pmid * farea[t];
+        fx = fx + fnrm[3 * t] * coef;
+        fy = fy + fnrm[3 * t + 1] * coef;
+        fz = fz + fnrm[3 * t + 2] * coef;
+      }
+      f[3 * k] = fx; f[3 * k + 1] = fy; f[3 * k + 2] = fz;
+      hk[k] = scale_coeff * sr / (double)nnb;
+    }
+    // Check_partition_error (voronoi.cpp:1228-1262)
+    error_record = error_record + error_max;
+    if (iter % 40 == 0) {
+      error_record /= 40.;
+      if (error_max <= P.error_tolerance && error_record <= P.error_tolerance) converged = 1;
+      error_record = 0.;
+    }
+    if (converged == 0) {
+      // Update_position (voronoi.cpp:830-897)
+      double gdt = 1.e20;
+      std::vector<double> a(3 * K);
+      for (int k = 0; k < K; k++) {
+        double inv = 1. / mass[k];
+        for (int q = 0; q < 3; q++) a[3 * k + q] = f[3 * k + q] * inv;
+        double acc = 0.0;
+        for (int q = 0; q < D; q++) acc += a[3 * k + q] * a[3 * k + q];
+        acc = std::sqrt(acc);
+        double ts = 0.25 * std::sqrt(hk[k] / (acc + 1.e-20));
+        gdt = AMIN1(ts, gdt);
+      }
+      double gcvt = 1.e20;
+      for (int k = 0; k < K; k++) {
+        double fac = gdt * gdt * 0.5 * relax;
+        for (int q = 0; q < D; q++) {
+          double v = P.pressure_step ? vp[3 * k + q] + a[3 * k + q] * fac : vp[3 * k + q];
+          vp[3 * k + q] = AMAX1(P.box_l[q] + 1.e-20, AMIN1(v, P.box_r[q] - 1.e-20));
+        }
+        double sh = 0.0;
+        for (int q = 0; q < D; q++) {
+          shift[3 * k + q] = mc[3 * k + q] - vp[3 * k + q];
+          sh += shift[3 * k + q] * shift[3 * k + q];
+        }
+        sh = std::sqrt(sh);
+        double sc = AMIN1(sh, 1. / 32. * hk[k]);
+        tcvt[k] = sc / (sh + 1.e-20);
+        gcvt = AMIN1(tcvt[k], gcvt);
+      }
+      // Update_position_CVT (voronoi.cpp:901-992)
+      for (int k = 0; k < K; k++)
+        for (int q = 0; q < D; q++) {
+          double v = vp[3 * k + q] + shift[3 * k + q] * (gcvt * (1 - relax));
+          vp[3 * k + q] = AMAX1(P.box_l[q] + 1.e-20, AMIN1(v, P.box_r[q] - 1.e-20));
+        }
+    }
+    if (iter % 600 == 0) relax = 1.02 * relax;
+    relax = AMIN1(relax, 0.90);
+  }
+  if (vp_mass) for (int k = 0; k < K; k++) vp_mass[k] = mass[k];
+  if (res) { res->iterations = iter; res->converged = converged; res->error_max = error_max; res->total_energy = total_energy; }
+  return 0;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -64,6 +64,17 @@ class OrcState(C.Structure):
                    ("remapped", C.c_longlong)])
 
 
+class OrcCvpParams(C.Structure):
+    _fields_ = [("dim", C.c_int), ("num_vp", C.c_int), ("max_iter", C.c_int), ("pressure_step", C.c_int),
+                ("error_tolerance", C.c_double), ("relax_ratio", C.c_double), ("box_l", C.c_double * 3),
+                ("box_r", C.c_double * 3)]
+
+
+class OrcCvpResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("error_max", C.c_double),
+                ("total_energy", C.c_double)]
+
+
 _lib = None
 
 
@@ -94,6 +105,8 @@ def lib():
         L.orc_steps.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_int]
         L.orc_steps.restype = C.c_longlong
         L.orc_num_threads.restype = C.c_int
+        L.orc_cvp.argtypes = [C.POINTER(OrcCvpParams), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p, C.c_void_p, C.POINTER(OrcCvpResult)]
         _lib = L
     return _lib
 
@@ -278,6 +291,26 @@ def philox(c0, c1, c2, c3, seed):
     out = (C.c_uint32 * 4)()
     lib().orc_philox(c0, c1, c2, c3, seed, out)
     return list(out)
+
+
+def cvp(dim, box_l, box_r, xyz, vp_xyz, mass=None, max_iter=4000, error_tolerance=0.05, relax_ratio=0.8,
+        pressure_step=True):
+    """Voronoi::Partitioning restated (CVP/voronoi.cpp:1376-1446) on weighted points."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    vp = np.ascontiguousarray(vp_xyz, dtype=np.float64).reshape(-1, 3).copy()
+    n, K = len(xyz), len(vp)
+    pm = np.ones(n) if mass is None else np.ascontiguousarray(mass, dtype=np.float64)
+    p = OrcCvpParams()
+    p.dim, p.num_vp, p.max_iter, p.pressure_step = dim, K, max_iter, 1 if pressure_step else 0
+    p.error_tolerance, p.relax_ratio = error_tolerance, relax_ratio
+    for d in range(3):
+        p.box_l[d] = box_l[d]
+        p.box_r[d] = box_r[d]
+    labels = np.zeros(n, dtype=np.int32)
+    vmass = np.zeros(K)
+    res = OrcCvpResult()
+    lib().orc_cvp(C.byref(p), n, _p(xyz), _p(pm), _p(vp), _p(labels), _p(vmass), C.byref(res))
+    return vp, labels, vmass, {f: getattr(res, f) for f, _ in OrcCvpResult._fields_}
 
 
 def num_threads() -> int:

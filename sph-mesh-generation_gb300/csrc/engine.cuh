@@ -1070,6 +1070,14 @@ class Engine : public EngineBase {
   }
 
   cudaStream_t stream() const override { return st_; }
+  long long num_particles() const override { return n_; }
+
+  int world_positions(double* d_out) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    k_tap<D, R><<<grid(n_), 256, 0, st_>>>(kc_, buf_[cur_], w_, w_.slot_of_id, d_out, 0, have_work_);
+    MR_CK(cudaGetLastError());
+    return 0;
+  }
 
  private:
   static unsigned long long dbits_host(double x) { unsigned long long u; std::memcpy(&u, &x, 8); return u; }

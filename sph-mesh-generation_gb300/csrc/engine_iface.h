@@ -36,6 +36,9 @@ class EngineBase {
   // out n x 6: phi, nx, ny, nz, curv, tag); enqueued on the engine stream.
   virtual int sample_device(long long n, const double* d_xyz, double* d_out) = 0;
   virtual cudaStream_t stream() const = 0;
+  virtual long long num_particles() const = 0;
+  // FP64 world positions in particle-id order into a device buffer (n x 3)
+  virtual int world_positions(double* d_out) = 0;
   std::string err;
 };
 

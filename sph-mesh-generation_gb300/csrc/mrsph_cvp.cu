@@ -1,0 +1,474 @@
+// mrsph_cvp.cu — centroidal Voronoi partitioning of the particles (row A13),
+// Voronoi::Partitioning (CVP/voronoi.cpp:1376-1446) on the GPU.
+//
+// One iteration = five kernels:
+//   k_cvp_assign    nearest VP per point, strict '<' (Get_CPU_id, voronoi.cpp:480-493)
+//   k_cvp_partials  per (VP, 2048-point chunk) mass, mass centre and energy,
+//                   points in order (voronoi.cpp:617-631)
+//   k_cvp_reduce    per VP: chunk partials in order, centroid, pressure, error
+//   k_cvp_faces     per (VP, plane) the exact Voronoi face inside the box: the
+//                   plane's polygon clipped by every other bisector half-space
+//                   (replaces voro++, voronoi.cpp:724-790)
+//   k_cvp_update    face pressure force, h, Update_position (voronoi.cpp:830-897),
+//                   Update_position_CVT (:901-992), Check_partition_error (:1228-1262)
+// Compiled with -fmad=false: every operation rounds as written, in the same
+// order as the oracle, so labels and VP positions match it bit for bit.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "handle.h"
+
+namespace mrsph {
+namespace {
+
+constexpr int CVP_CHUNK = 2048;
+constexpr int CVP_MAXV = 64;
+constexpr int CVP_MAX_K = 1024;
+
+struct CvpGeo {
+  int dim, K, NP;
+  double box_l[3], box_r[3];
+};
+
+struct CvpState {  // device-resident iteration state
+  double relax, error_record, error_max, total_energy, target;
+  int converged, iter;
+};
+
+__device__ inline double cdot(const double* a, const double* b) {
+  double s = 0.0;
+  s += a[0] * b[0];
+  s += a[1] * b[1];
+  s += a[2] * b[2];
+  return s;
+}
+
+__device__ inline double cdist(int D, const double* a, const double* b) {
+  double s = 0.0;
+  s += (a[0] - b[0]) * (a[0] - b[0]);
+  s += (a[1] - b[1]) * (a[1] - b[1]);
+  if (D == 3) s += (a[2] - b[2]) * (a[2] - b[2]);
+  return sqrt(s);
+}
+
+__device__ inline double cmin(double a, double b) { return a <= b ? a : b; }
+__device__ inline double cmax(double a, double b) { return a >= b ? a : b; }
+
+__device__ int cclip(double (*v)[3], int nv, const double* n, double d, double (*o)[3]) {
+  int no = 0;
+  for (int a = 0; a < nv; a++) {
+    int b = (a + 1) % nv;
+    double sa = cdot(n, v[a]) - d, sb = cdot(n, v[b]) - d;
+    if (sa <= 0.0) {
+      if (no < CVP_MAXV) { o[no][0] = v[a][0]; o[no][1] = v[a][1]; o[no][2] = v[a][2]; }
+      no++;
+    }
+    if ((sa <= 0.0) != (sb <= 0.0)) {
+      double t = sa / (sa - sb);
+      if (no < CVP_MAXV)
+        for (int q = 0; q < 3; q++) o[no][q] = v[a][q] + (v[b][q] - v[a][q]) * t;
+      no++;
+    }
+  }
+  return no < CVP_MAXV ? no : CVP_MAXV;
+}
+
+__device__ void cplane(const CvpGeo& G, const double* vp, int k, int p, double* n, double* d) {
+  if (p < G.K) {
+    const double* ck = vp + 3 * k;
+    const double* cm = vp + 3 * p;
+    double e[3] = {cm[0] - ck[0], cm[1] - ck[1], cm[2] - ck[2]};
+    double len = sqrt(cdot(e, e));
+    double mid[3] = {0.5 * (ck[0] + cm[0]), 0.5 * (ck[1] + cm[1]), 0.5 * (ck[2] + cm[2])};
+    for (int q = 0; q < 3; q++) n[q] = e[q] / len;
+    *d = cdot(n, mid);
+  } else {
+    int w = p - G.K, ax = w / 2, hi = w % 2;
+    n[0] = n[1] = n[2] = 0.0;
+    n[ax] = hi ? 1.0 : -1.0;
+    *d = hi ? G.box_r[ax] : -G.box_l[ax];
+  }
+}
+
+__global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int K, const double* __restrict__ vp,
+                             int D, int* __restrict__ label) {
+  __shared__ double s_vp[3 * CVP_MAX_K];
+  for (int t = threadIdx.x; t < 3 * K; t += blockDim.x) s_vp[t] = vp[t];
+  __syncthreads();
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  double best = 1.e20;
+  int idx = 0;
+  for (int k = 0; k < K; k++) {
+    double dd = cdist(D, x, s_vp + 3 * k);
+    if (dd < best) { best = dd; idx = k; }
+  }
+  label[i] = idx;
+}
+
+// total point mass in chunked order (Set_target_mass, voronoi.cpp:495-510)
+__global__ void k_cvp_chunk_mass(long long n, const double* __restrict__ pm, long long nchunk, double* out) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchunk) return;
+  double s = 0.0;
+  long long e = min(n, (c + 1) * (long long)CVP_CHUNK);
+  for (long long i = c * CVP_CHUNK; i < e; i++) s += pm[i];
+  out[c] = s;
+}
+
+__global__ void k_cvp_target(long long nchunk, const double* tm, int K, CvpState* st) {
+  double t = 0.0;
+  for (long long c = 0; c < nchunk; c++) t += tm[c];
+  st->target = t / K;
+}
+
+// thread (k, chunk c): points of the chunk in order
+__global__ void k_cvp_partials(long long n, const double* __restrict__ xyz, const double* __restrict__ pm,
+                               const int* __restrict__ label, int K, const double* __restrict__ vp, int D,
+                               double* __restrict__ part) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  long long c = blockIdx.y;
+  if (k >= K) return;
+  const double ck[3] = {vp[3 * k], vp[3 * k + 1], vp[3 * k + 2]};
+  double m = 0.0, x = 0.0, y = 0.0, z = 0.0, e = 0.0;
+  long long end = min(n, (c + 1) * (long long)CVP_CHUNK);
+  for (long long i = c * CVP_CHUNK; i < end; i++) {
+    if (__ldg(&label[i]) != k) continue;
+    double w = pm[i];
+    const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    m += w;
+    x = x + p[0] * w;
+    y = y + p[1] * w;
+    z = z + p[2] * w;
+    e += w * cdist(D, ck, p);
+  }
+  double* q = part + ((size_t)c * K + k) * 5;
+  q[0] = m; q[1] = x; q[2] = y; q[3] = z; q[4] = e;
+}
+
+__global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __restrict__ part,
+                             const CvpState* st, double* mass, double* mc, double* energy, double* P,
+                             double* err) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  double m = 0.0, x = 0.0, y = 0.0, z = 0.0, e = 0.0;
+  for (long long c = 0; c < nchunk; c++) {
+    const double* q = part + ((size_t)c * K + k) * 5;
+    m += q[0]; x = x + q[1]; y = y + q[2]; z = z + q[3]; e += q[4];
+  }
+  mass[k] = m;
+  energy[k] = e;
+  double inv = 1. / m;
+  mc[3 * k] = x * inv;
+  mc[3 * k + 1] = y * inv;
+  mc[3 * k + 2] = (D == 3) ? z * inv : 0.0;
+  double target = st->target;
+  P[k] = target / m;
+  err[k] = fabs(m - target) / target;
+}
+
+// face of VP k on plane p; out: exists, area, n (3), dist
+__global__ void k_cvp_faces(CvpGeo G, const double* __restrict__ vp, double* __restrict__ face) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)G.K * G.NP) return;
+  int k = (int)(t / G.NP), p = (int)(t % G.NP);
+  double* out = face + 6 * t;
+  out[0] = 0.0;
+  if (p < G.K && p == k) return;
+  double n[3], d;
+  cplane(G, vp, k, p, n, &d);
+  double lo[3], hi[3];
+  for (int q = 0; q < 3; q++) {
+    lo[q] = q < G.dim ? G.box_l[q] : -0.5;
+    hi[q] = q < G.dim ? G.box_r[q] : 0.5;
+  }
+  double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+  double S = 0.0;
+  for (int q = 0; q < 3; q++) S += (hi[q] - lo[q]) * (hi[q] - lo[q]);
+  S = 2.0 * sqrt(S);
+  int ax = 0;
+  if (fabs(n[1]) < fabs(n[ax])) ax = 1;
+  if (fabs(n[2]) < fabs(n[ax])) ax = 2;
+  double e[3] = {0, 0, 0};
+  e[ax] = 1.0;
+  double u[3] = {n[1] * e[2] - n[2] * e[1], n[2] * e[0] - n[0] * e[2], n[0] * e[1] - n[1] * e[0]};
+  double ul = sqrt(cdot(u, u));
+  for (int q = 0; q < 3; q++) u[q] = u[q] / ul;
+  double w[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2], n[0] * u[1] - n[1] * u[0]};
+  double off = d - cdot(n, c);
+  double p0[3] = {c[0] + n[0] * off, c[1] + n[1] * off, c[2] + n[2] * off};
+  double A[CVP_MAXV][3], B[CVP_MAXV][3];
+  const double sg[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+  for (int a = 0; a < 4; a++)
+    for (int q = 0; q < 3; q++) A[a][q] = p0[q] + u[q] * (sg[a][0] * S) + w[q] * (sg[a][1] * S);
+  int nv = 4;
+  for (int wq = 0; wq < 6 && nv > 0; wq++) {
+    if (p >= G.K && wq == p - G.K) continue;
+    int axw = wq / 2, hw = wq % 2;
+    double wn[3] = {0, 0, 0};
+    wn[axw] = hw ? 1.0 : -1.0;
+    double wd = hw ? hi[axw] : -lo[axw];
+    nv = cclip(A, nv, wn, wd, B);
+    for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
+  }
+  for (int m = 0; m < G.K && nv > 0; m++) {
+    if (m == k || m == p) continue;
+    double bn[3], bd;
+    cplane(G, vp, k, m, bn, &bd);
+    nv = cclip(A, nv, bn, bd, B);
+    for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
+  }
+  if (nv < 3) return;
+  double ar = 0.0;
+  for (int a = 1; a + 1 < nv; a++) {
+    double x[3] = {A[a][0] - A[0][0], A[a][1] - A[0][1], A[a][2] - A[0][2]};
+    double y[3] = {A[a + 1][0] - A[0][0], A[a + 1][1] - A[0][1], A[a + 1][2] - A[0][2]};
+    double cr[3] = {x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0]};
+    ar += cdot(cr, n);
+  }
+  ar = 0.5 * fabs(ar);
+  double ext = S * S;
+  if (!(ar > 1.e-13 * ext)) return;
+  const double* ck = vp + 3 * k;
+  double dx[3] = {A[0][0] - ck[0], A[0][1] - ck[1], A[0][2] - ck[2]};
+  out[0] = 1.0;
+  out[1] = ar;
+  out[2] = n[0];
+  out[3] = n[1];
+  out[4] = n[2];
+  out[5] = fabs(cdot(dx, n)) * 2.;
+}
+
+// Sequential VP update, one thread (K is at most 1024).
+__global__ void k_cvp_update(CvpGeo G, double* vp, const double* __restrict__ face, const double* mass,
+                             const double* mc, const double* energy, const double* P, const double* err,
+                             double* f, double* hk, double* shift, CvpState* st, double error_tolerance,
+                             int pressure_step) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int K = G.K, D = G.dim, NP = G.NP;
+  const int iter = st->iter;
+  double scale_coeff = 0.25 + 1.75 * (1. - cmin((iter - 1) / 500., 1.));
+  double error_max = 0.0, total_energy = 0.0;
+  for (int k = 0; k < K; k++) {
+    error_max = cmax(error_max, err[k]);
+    total_energy += energy[k];
+  }
+  for (int k = 0; k < K; k++) {
+    double fx = 0.0, fy = 0.0, fz = 0.0, sr = 0.0;
+    int nnb = 0;
+    for (int p = 0; p < NP; p++) {
+      const double* fc = face + 6 * ((size_t)k * NP + p);
+      if (fc[0] == 0.0) continue;
+      nnb++;
+      double nP = (p < K) ? P[p] : P[k];
+      sr += fc[5];
+      double pmid = 0.5 * (P[k] + nP);
+      double coef = -1 * pmid * fc[1];
+      fx = fx + fc[2] * coef;
+      fy = fy + fc[3] * coef;
+      fz = fz + fc[4] * coef;
+    }
+    f[3 * k] = fx; f[3 * k + 1] = fy; f[3 * k + 2] = fz;
+    hk[k] = scale_coeff * sr / (double)nnb;
+  }
+  st->error_record = st->error_record + error_max;
+  if (iter % 40 == 0) {
+    st->error_record /= 40.;
+    if (error_max <= error_tolerance && st->error_record <= error_tolerance) st->converged = 1;
+    st->error_record = 0.;
+  }
+  st->error_max = error_max;
+  st->total_energy = total_energy;
+  const double relax = st->relax;
+  if (st->converged == 0) {
+    double gdt = 1.e20;
+    for (int k = 0; k < K; k++) {
+      double inv = 1. / mass[k];
+      double acc = 0.0;
+      for (int q = 0; q < D; q++) {
+        double a = f[3 * k + q] * inv;
+        acc += a * a;
+      }
+      acc = sqrt(acc);
+      double ts = 0.25 * sqrt(hk[k] / (acc + 1.e-20));
+      gdt = cmin(ts, gdt);
+    }
+    double gcvt = 1.e20;
+    for (int k = 0; k < K; k++) {
+      double inv = 1. / mass[k];
+      double fac = gdt * gdt * 0.5 * relax;
+      for (int q = 0; q < D; q++) {
+        double a = f[3 * k + q] * inv;
+        double v = pressure_step ? vp[3 * k + q] + a * fac : vp[3 * k + q];
+        vp[3 * k + q] = cmax(G.box_l[q] + 1.e-20, cmin(v, G.box_r[q] - 1.e-20));
+      }
+      double sh = 0.0;
+      for (int q = 0; q < D; q++) {
+        shift[3 * k + q] = mc[3 * k + q] - vp[3 * k + q];
+        sh += shift[3 * k + q] * shift[3 * k + q];
+      }
+      sh = sqrt(sh);
+      double sc = cmin(sh, 1. / 32. * hk[k]);
+      gcvt = cmin(sc / (sh + 1.e-20), gcvt);
+    }
+    for (int k = 0; k < K; k++)
+      for (int q = 0; q < D; q++) {
+        double v = vp[3 * k + q] + shift[3 * k + q] * (gcvt * (1 - relax));
+        vp[3 * k + q] = cmax(G.box_l[q] + 1.e-20, cmin(v, G.box_r[q] - 1.e-20));
+      }
+  }
+  double r = relax;
+  if (iter % 600 == 0) r = 1.02 * r;
+  st->relax = cmin(r, 0.90);
+  st->iter = iter + 1;
+}
+
+int cfail(mrsph_handle* h, int code, const std::string& msg) {
+  h->err = msg;
+  return code;
+}
+
+#define CV_CK(call)                                                                     \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) { rc = cfail(h, MRSPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); goto done; } \
+  } while (0)
+
+// Core loop on device points (xyz n x 3, pm n), id order.
+int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrsph_cvp_params* p, double* vp_xyz,
+            int* labels, double* vp_mass, mrsph_cvp_result* res) {
+  const int K = p->num_vp, D = h->prm.dim;
+  CvpGeo G;
+  G.dim = D;
+  G.K = K;
+  G.NP = K + 2 * D;
+  for (int q = 0; q < 3; q++) {
+    G.box_l[q] = h->prm.box_l[q];
+    G.box_r[q] = h->prm.box_r[q];
+  }
+  const long long nchunk = (n + CVP_CHUNK - 1) / CVP_CHUNK;
+  cudaStream_t s = h->stream;
+  int rc = 0;
+  std::vector<void*> mem;
+  double *d_vp = nullptr, *d_part = nullptr, *d_face = nullptr, *d_k = nullptr, *d_tm = nullptr;
+  int* d_label = nullptr;
+  CvpState* d_st = nullptr;
+  CvpState hs;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.relax = p->relax_ratio;
+  auto A = [&](void** ptr, size_t bytes) -> cudaError_t {
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e == cudaSuccess) mem.push_back(*ptr);
+    return e;
+  };
+  CV_CK(A((void**)&d_vp, sizeof(double) * 3 * K));
+  CV_CK(A((void**)&d_part, sizeof(double) * 5 * K * nchunk));
+  CV_CK(A((void**)&d_face, sizeof(double) * 6 * (size_t)K * G.NP));
+  CV_CK(A((void**)&d_k, sizeof(double) * 12 * K));  // mass, mc(3), energy, P, err, f(3), hk, pad
+  CV_CK(A((void**)&d_tm, sizeof(double) * nchunk));
+  CV_CK(A((void**)&d_label, sizeof(int) * n));
+  CV_CK(A((void**)&d_st, sizeof(CvpState)));
+  {
+    double* vp3 = nullptr;
+    CV_CK(A((void**)&vp3, sizeof(double) * 3 * K));  // shift
+    CV_CK(cudaMemcpyAsync(d_vp, vp_xyz, sizeof(double) * 3 * K, cudaMemcpyHostToDevice, s));
+    CV_CK(cudaMemcpyAsync(d_st, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    double *mass = d_k, *mc = d_k + K, *energy = d_k + 4 * K, *P = d_k + 5 * K, *err = d_k + 6 * K,
+           *f = d_k + 7 * K, *hk = d_k + 10 * K;
+    k_cvp_chunk_mass<<<(int)((nchunk + 127) / 128), 128, 0, s>>>(n, d_pm, nchunk, d_tm);
+    k_cvp_target<<<1, 1, 0, s>>>(nchunk, d_tm, K, d_st);
+    const int nb = (int)((n + 255) / 256);
+    const int ftot = K * G.NP;
+    int it = 0;
+    for (; it <= p->max_iter; it++) {
+      k_cvp_assign<<<nb, 256, 0, s>>>(n, d_xyz, K, d_vp, D, d_label);
+      dim3 g((K + 63) / 64, (unsigned)nchunk);
+      k_cvp_partials<<<g, 64, 0, s>>>(n, d_xyz, d_pm, d_label, K, d_vp, D, d_part);
+      k_cvp_reduce<<<(K + 127) / 128, 128, 0, s>>>(nchunk, K, D, d_part, d_st, mass, mc, energy, P, err);
+      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_face);
+      k_cvp_update<<<1, 32, 0, s>>>(G, d_vp, d_face, mass, mc, energy, P, err, f, hk, vp3, d_st,
+                                    p->error_tolerance, p->pressure_step);
+      CV_CK(cudaGetLastError());
+      CV_CK(cudaMemcpyAsync(&hs, d_st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+      CV_CK(cudaStreamSynchronize(s));
+      if (hs.converged) { it++; break; }
+    }
+    CV_CK(cudaMemcpyAsync(vp_xyz, d_vp, sizeof(double) * 3 * K, cudaMemcpyDeviceToHost, s));
+    if (labels) CV_CK(cudaMemcpyAsync(labels, d_label, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    if (vp_mass) CV_CK(cudaMemcpyAsync(vp_mass, mass, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+    CV_CK(cudaStreamSynchronize(s));
+    if (res) {
+      res->iterations = it;
+      res->converged = hs.converged;
+      res->error_max = hs.error_max;
+      res->total_energy = hs.total_energy;
+    }
+  }
+done:
+  for (void* q : mem) cudaFree(q);
+  return rc;
+}
+
+}  // namespace
+}  // namespace mrsph
+
+using namespace mrsph;
+
+static int cvp_check(mrsph_handle* h, const mrsph_cvp_params* p, double* vp_xyz) {
+  if (!h) return MRSPH_ERR_ARG;
+  if (!p || !vp_xyz) return cfail(h, MRSPH_ERR_ARG, "null argument");
+  if (p->num_vp < 1 || p->num_vp > CVP_MAX_K) return cfail(h, MRSPH_ERR_RANGE, "num_vp must be 1..1024");
+  if (p->max_iter < 0) return cfail(h, MRSPH_ERR_ARG, "max_iter must be >= 0");
+  return 0;
+}
+
+extern "C" int mrsph_cvp_points(mrsph_handle* h, long long n, const double* xyz, const double* mass,
+                                const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass,
+                                mrsph_cvp_result* res) {
+  int rc = cvp_check(h, p, vp_xyz);
+  if (rc) return rc;
+  if (n <= 0 || !xyz) return cfail(h, MRSPH_ERR_ARG, "no points");
+  if (cudaSetDevice(h->prm.device) != cudaSuccess) return cfail(h, MRSPH_ERR_CUDA, "cudaSetDevice failed");
+  double *d_xyz = nullptr, *d_pm = nullptr;
+  if (cudaMalloc(&d_xyz, sizeof(double) * 3 * n) != cudaSuccess ||
+      cudaMalloc(&d_pm, sizeof(double) * n) != cudaSuccess) {
+    cudaFree(d_xyz);
+    return cfail(h, MRSPH_ERR_OOM, "cudaMalloc failed");
+  }
+  std::vector<double> ones;
+  const double* pm = mass;
+  if (!pm) { ones.assign(n, 1.0); pm = ones.data(); }
+  cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(d_pm, pm, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream);
+  rc = cvp_run(h, n, d_xyz, d_pm, p, vp_xyz, labels, vp_mass, res);
+  cudaFree(d_xyz);
+  cudaFree(d_pm);
+  return rc;
+}
+
+extern "C" int mrsph_cvp(mrsph_handle* h, const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass,
+                         mrsph_cvp_result* res) {
+  int rc = cvp_check(h, p, vp_xyz);
+  if (rc) return rc;
+  if (!h->eng) return cfail(h, MRSPH_ERR_STATE, "no particles");
+  if (cudaSetDevice(h->prm.device) != cudaSuccess) return cfail(h, MRSPH_ERR_CUDA, "cudaSetDevice failed");
+  long long n = h->eng->num_particles();
+  if (n <= 0) return cfail(h, MRSPH_ERR_STATE, "no particles");
+  double *d_xyz = nullptr, *d_pm = nullptr;
+  if (cudaMalloc(&d_xyz, sizeof(double) * 3 * n) != cudaSuccess ||
+      cudaMalloc(&d_pm, sizeof(double) * n) != cudaSuccess) {
+    cudaFree(d_xyz);
+    return cfail(h, MRSPH_ERR_OOM, "cudaMalloc failed");
+  }
+  rc = h->eng->world_positions(d_xyz);  // particle mass 1 (Particle_mesh_generation::Initialize)
+  if (rc) { h->err = h->eng->err; cudaFree(d_xyz); cudaFree(d_pm); return rc; }
+  std::vector<double> ones(n, 1.0);
+  cudaMemcpyAsync(d_pm, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream);
+  rc = cvp_run(h, n, d_xyz, d_pm, p, vp_xyz, labels, vp_mass, res);
+  cudaFree(d_xyz);
+  cudaFree(d_pm);
+  return rc;
+}

@@ -45,6 +45,16 @@ class ParticleView(C.Structure):
                                           "nu", "a1", "a2")]
 
 
+class CvpParams(C.Structure):
+    _fields_ = [("num_vp", C.c_int), ("max_iter", C.c_int), ("pressure_step", C.c_int),
+                ("error_tolerance", C.c_double), ("relax_ratio", C.c_double)]
+
+
+class CvpResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("error_max", C.c_double),
+                ("total_energy", C.c_double)]
+
+
 class StateIn(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("v", C.c_void_p), ("type", C.c_void_p), ("h", C.c_void_p),
                 ("level", C.c_void_p), ("nu", C.c_void_p), ("dt", C.c_double), ("step", C.c_longlong)]
@@ -70,6 +80,10 @@ EXPORTS = {
     "mrsph_get_particles": ([C.c_void_p, C.POINTER(ParticleView)], C.c_int),
     "mrsph_get_cells": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_get_neighbors": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)], C.c_int),
+    "mrsph_cvp": ([C.c_void_p, C.POINTER(CvpParams), C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(CvpResult)],
+                  C.c_int),
+    "mrsph_cvp_points": ([C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p, C.POINTER(CvpParams), C.c_void_p,
+                          C.c_void_p, C.c_void_p, C.POINTER(CvpResult)], C.c_int),
     "mrsph_upload_positions": ([C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_download_positions": ([C.c_void_p, C.c_void_p], C.c_int),
 }

@@ -25,6 +25,7 @@ SOURCES = {
     "mrsph_fp64.cu": ["-fmad=false"],
     "mrsph_fp32.cu": [],
     "mrsph_noalloc.cu": [],
+    "mrsph_cvp.cu": ["-fmad=false"],
 }
 
 

@@ -218,6 +218,46 @@ class SPHMeshGeneration:
                                                        _ptr(tag)), self.h, "mrsph_sample_levelset_noalloc")
         return phi, nrm, curv, tag
 
+    # ------------------------------------------------------------------ CVP
+    @staticmethod
+    def _cvp_params(num_vp, max_iter, tol, relax, pressure_step):
+        p = L.CvpParams()
+        p.num_vp = int(num_vp)
+        p.max_iter = int(max_iter)
+        p.pressure_step = 1 if pressure_step else 0
+        p.error_tolerance = float(tol)
+        p.relax_ratio = float(relax)
+        return p
+
+    def Partitioning(self, vp_xyz: np.ndarray, max_iter: int = 4000, error_tolerance: float = 0.05,
+                     relax_ratio: float = 0.8, pressure_step: bool = True):
+        """Voronoi::Partitioning of the current particles (CVP/voronoi.cpp:1376-1446)."""
+        vp = np.ascontiguousarray(vp_xyz, dtype=np.float64).reshape(-1, 3).copy()
+        K = len(vp)
+        labels = np.zeros(self.n, dtype=np.int32)
+        mass = np.zeros(K)
+        res = L.CvpResult()
+        prm = self._cvp_params(K, max_iter, error_tolerance, relax_ratio, pressure_step)
+        L.check(self.lib.mrsph_cvp(self.h, C.byref(prm), _ptr(vp), _ptr(labels), _ptr(mass), C.byref(res)),
+                self.h, "mrsph_cvp")
+        return vp, labels, mass, {f: getattr(res, f) for f, _ in L.CvpResult._fields_}
+
+    def partition_points(self, xyz: np.ndarray, vp_xyz: np.ndarray, mass: Optional[np.ndarray] = None,
+                         max_iter: int = 4000, error_tolerance: float = 0.05, relax_ratio: float = 0.8,
+                         pressure_step: bool = True):
+        """CVP of given weighted points (e.g. level-set packages, Voronoi_lset)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        vp = np.ascontiguousarray(vp_xyz, dtype=np.float64).reshape(-1, 3).copy()
+        m = None if mass is None else np.ascontiguousarray(mass, dtype=np.float64)
+        K = len(vp)
+        labels = np.zeros(len(xyz), dtype=np.int32)
+        vmass = np.zeros(K)
+        res = L.CvpResult()
+        prm = self._cvp_params(K, max_iter, error_tolerance, relax_ratio, pressure_step)
+        L.check(self.lib.mrsph_cvp_points(self.h, len(xyz), _ptr(xyz), _ptr(m), C.byref(prm), _ptr(vp),
+                                          _ptr(labels), _ptr(vmass), C.byref(res)), self.h, "mrsph_cvp_points")
+        return vp, labels, vmass, {f: getattr(res, f) for f, _ in L.CvpResult._fields_}
+
     def upload_positions(self, xyz: np.ndarray):
         L.check(self.lib.mrsph_upload_positions(self.h, _ptr(xyz)), self.h, "mrsph_upload_positions")
 

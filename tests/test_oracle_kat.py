@@ -151,3 +151,19 @@ def test_neighbor_relation_symmetric_and_includes_self():
             assert i in sets[j]
     lev = orc.arrays["level"]
     assert len(set(lev.tolist())) >= 2  # adaptive: more than one cell-list level
+
+
+def test_cvp_converges_to_quadrant_centroids():
+    """Four VPs on a uniform grid of the unit square converge to the quadrant
+    centroids with mass error below the tolerance (Voronoi::Partitioning)."""
+    g = (np.arange(100) + 0.5) / 100
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    xyz = np.stack([X.ravel(), Y.ravel(), 0 * X.ravel()], 1)
+    rng = np.random.default_rng(0)
+    vp = np.zeros((4, 3))
+    vp[:, :2] = 0.3 + 0.4 * rng.random((4, 2))
+    v, lab, m, r = oracle.cvp(2, [0, 0, 0], [1, 1, 0], xyz, vp, max_iter=400)
+    assert r["converged"] == 1 and r["error_max"] <= 0.05
+    for c in ([0.25, 0.25], [0.25, 0.75], [0.75, 0.25], [0.75, 0.75]):
+        assert np.min(np.hypot(v[:, 0] - c[0], v[:, 1] - c[1])) < 0.03
+    assert np.bincount(lab, minlength=4).min() > 2300
