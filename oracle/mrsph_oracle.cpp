@@ -24,6 +24,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <array>
+#include <set>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1442,6 +1444,343 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
   if (vp_mass) for (int k = 0; k < K; k++) vp_mass[k] = mass[k];
   if (res) { res->iterations = iter; res->converged = converged; res->error_max = error_max; res->total_energy = total_energy; }
   return 0;
+}
+
+// ===========================================================================
+// A14 triangulation (2D): Local_voronoi_diagram / Voronoi_construction::
+// Local_VD_generation (voronoi_construction.cpp:6-127) + Graphmeshcls::
+// Reconstruct_tris (graph_mesh.cpp:37-409) + Tri_quality_statistics (:411-670).
+// voro++ is replaced by exact local Delaunay predicates: j is a Voronoi
+// neighbour of i among i's neighbour set S iff some circle through i and j
+// has no point of S strictly inside or on it.  Signs are exact (FP64 filter,
+// then expansion arithmetic after Priest / Shewchuk 1997), so any correct
+// implementation returns the same edges.
+// ===========================================================================
+namespace xp {
+inline void two_sum(double a, double b, double& x, double& y) {
+  x = a + b;
+  double bv = x - a, av = x - bv, br = b - bv, ar = a - av;
+  y = ar + br;
+}
+inline void two_diff(double a, double b, double& x, double& y) {
+  x = a - b;
+  double bv = a - x, av = x + bv, br = bv - b, ar = a - av;
+  y = ar + br;
+}
+inline void two_prod(double a, double b, double& x, double& y) {
+  x = a * b;
+  y = std::fma(a, b, -x);
+}
+// h = e + b (e nonoverlapping, increasing magnitude); returns length
+inline int grow(const double* e, int m, double b, double* h) {
+  double Q = b;
+  int k = 0;
+  for (int i = 0; i < m; i++) {
+    double Qn, hh;
+    two_sum(Q, e[i], Qn, hh);
+    Q = Qn;
+    if (hh != 0.0) h[k++] = hh;
+  }
+  if (Q != 0.0 || k == 0) h[k++] = Q;
+  return k;
+}
+// h = e * b
+inline int scale(const double* e, int m, double b, double* h) {
+  double Q, hh;
+  int k = 0;
+  two_prod(e[0], b, Q, hh);
+  if (hh != 0.0) h[k++] = hh;
+  for (int i = 1; i < m; i++) {
+    double T, t, Q2, s;
+    two_prod(e[i], b, T, t);
+    two_sum(Q, t, Q2, s);
+    if (s != 0.0) h[k++] = s;
+    double x = T + Q2, bv = x - T;
+    s = Q2 - bv;
+    Q = x;
+    if (s != 0.0) h[k++] = s;
+  }
+  if (Q != 0.0 || k == 0) h[k++] = Q;
+  return k;
+}
+// running sum acc (length *n) += product of four doubles
+inline void acc4(double* acc, int* n, double* tmp, double p, double q, double r, double s, double sign) {
+  double e[8], f[8];
+  int m;
+  two_prod(p, q, e[1], e[0]);
+  m = 2;
+  m = scale(e, m, r, f);
+  m = scale(f, m, s * sign, e);
+  for (int i = 0; i < m; i++) {
+    int l = grow(acc, *n, e[i], tmp);
+    for (int t = 0; t < l; t++) acc[t] = tmp[t];
+    *n = l;
+  }
+}
+inline int sign_of(const double* e, int n) {
+  for (int i = n - 1; i >= 0; i--)
+    if (e[i] != 0.0) return e[i] > 0 ? 1 : -1;
+  return 0;
+}
+}  // namespace xp
+
+// sign of (a-c) x (b-c)
+static int orient2d(const double* a, const double* b, const double* c) {
+  double acx = a[0] - c[0], bcx = b[0] - c[0], acy = a[1] - c[1], bcy = b[1] - c[1];
+  double l = acx * bcy, r = acy * bcx;
+  double det = l - r;
+  double bound = 1.0e-15 * (std::fabs(l) + std::fabs(r));
+  if (det > bound) return 1;
+  if (-det > bound) return -1;
+  double ax[2], ay[2], bx[2], by[2];
+  xp::two_diff(a[0], c[0], ax[1], ax[0]);
+  xp::two_diff(a[1], c[1], ay[1], ay[0]);
+  xp::two_diff(b[0], c[0], bx[1], bx[0]);
+  xp::two_diff(b[1], c[1], by[1], by[0]);
+  double acc[80], tmp[80];
+  int n = 0;
+  for (int u = 0; u < 2; u++)
+    for (int v = 0; v < 2; v++) {
+      xp::acc4(acc, &n, tmp, ax[u], by[v], 1.0, 1.0, 1.0);
+      xp::acc4(acc, &n, tmp, ay[u], bx[v], 1.0, 1.0, -1.0);
+    }
+  return xp::sign_of(acc, n);
+}
+
+// > 0 when d lies inside the circle through a, b, c (a, b, c counter-clockwise)
+static int incircle(const double* a, const double* b, const double* c, const double* d) {
+  double adx = a[0] - d[0], ady = a[1] - d[1], bdx = b[0] - d[0], bdy = b[1] - d[1];
+  double cdx = c[0] - d[0], cdy = c[1] - d[1];
+  double al = adx * adx + ady * ady, bl = bdx * bdx + bdy * bdy, cl = cdx * cdx + cdy * cdy;
+  double t1 = bdx * cdy, t2 = cdx * bdy, t3 = cdx * ady, t4 = adx * cdy, t5 = adx * bdy, t6 = bdx * ady;
+  double det = al * (t1 - t2) + bl * (t3 - t4) + cl * (t5 - t6);
+  double perm = (std::fabs(t1) + std::fabs(t2)) * al + (std::fabs(t3) + std::fabs(t4)) * bl +
+                (std::fabs(t5) + std::fabs(t6)) * cl;
+  double bound = 2.0e-14 * perm;
+  if (det > bound) return 1;
+  if (-det > bound) return -1;
+  double X[3][2], Y[3][2];
+  const double* P[3] = {a, b, c};
+  for (int q = 0; q < 3; q++) {
+    xp::two_diff(P[q][0], d[0], X[q][1], X[q][0]);
+    xp::two_diff(P[q][1], d[1], Y[q][1], Y[q][0]);
+  }
+  static thread_local double acc[4096], tmp[4096];
+  int n = 0;
+  // det = sum over cyclic (a,b,c): (ax^2 + ay^2) * (bx*cy - cx*by)
+  for (int q = 0; q < 3; q++) {
+    int r = (q + 1) % 3, s = (q + 2) % 3;
+    for (int u = 0; u < 2; u++)
+      for (int v = 0; v < 2; v++)
+        for (int w = 0; w < 2; w++)
+          for (int z = 0; z < 2; z++) {
+            xp::acc4(acc, &n, tmp, X[q][u], X[q][v], X[r][w], Y[s][z], 1.0);
+            xp::acc4(acc, &n, tmp, Y[q][u], Y[q][v], X[r][w], Y[s][z], 1.0);
+            xp::acc4(acc, &n, tmp, X[q][u], X[q][v], X[s][w], Y[r][z], -1.0);
+            xp::acc4(acc, &n, tmp, Y[q][u], Y[q][v], X[s][w], Y[r][z], -1.0);
+          }
+  }
+  return xp::sign_of(acc, n);
+}
+
+// j is a Voronoi neighbour of i among points S (ids), positions xyz
+static bool local_delaunay(const double* xyz, int i, int j, const int* S, int ns) {
+  const double* pi = xyz + 3 * (long long)i;
+  const double* pj = xyz + 3 * (long long)j;
+  int lstar = -1, rstar = -1;
+  for (int q = 0; q < ns; q++) {
+    int k = S[q];
+    if (k == i || k == j) continue;
+    const double* pk = xyz + 3 * (long long)k;
+    int o = orient2d(pi, pj, pk);
+    if (o == 0) {
+      // collinear: blocks the edge when strictly between i and j
+      double t = (pk[0] - pi[0]) * (pj[0] - pi[0]) + (pk[1] - pi[1]) * (pj[1] - pi[1]);
+      double L = (pj[0] - pi[0]) * (pj[0] - pi[0]) + (pj[1] - pi[1]) * (pj[1] - pi[1]);
+      if (t > 0 && t < L) return false;
+      continue;
+    }
+    if (o > 0) {
+      if (lstar < 0 || incircle(pi, pj, xyz + 3 * (long long)lstar, pk) > 0) lstar = k;
+    } else {
+      if (rstar < 0 || incircle(pj, pi, xyz + 3 * (long long)rstar, pk) > 0) rstar = k;
+    }
+  }
+  if (lstar < 0 || rstar < 0) return true;
+  return incircle(pi, pj, xyz + 3 * (long long)lstar, xyz + 3 * (long long)rstar) < 0;
+}
+
+struct orc_tri_quality {
+  long long ntri, nedge, nedge_first, ndeleted, nerror;
+  double max_angle, min_angle, max_aspect, max_edge, min_edge, max_area, min_area, G_min, G_avg, min_angle_avg;
+  double theta_30, total_area;
+  long long hist[45];
+};
+
+// neighbour CSR (id space, rows sorted, self included or not), positions in id order
+long long orc_triangulate(const orc_ctx* c, long long n, const double* xyz, const int* type, const double* phi,
+                          const long long* off, const int* nbr, int* tris, long long cap, orc_tri_quality* Q) {
+  // 1. local Delaunay edges, symmetrised
+  std::vector<std::vector<int>> adj(n);
+  std::vector<std::vector<char>> mark(n);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long long i = 0; i < n; i++) {
+    const int* S = nbr + off[i];
+    int ns = (int)(off[i + 1] - off[i]);
+    mark[i].assign(ns, 0);
+    for (int q = 0; q < ns; q++) {
+      int j = S[q];
+      if (j == i) continue;
+      mark[i][q] = local_delaunay(xyz, (int)i, j, S, ns) ? 1 : 0;
+    }
+  }
+  auto find = [&](long long a, int b) -> int {
+    const int* S = nbr + off[a];
+    int ns = (int)(off[a + 1] - off[a]);
+    int lo = 0, hi = ns - 1;
+    while (lo <= hi) {
+      int m = (lo + hi) / 2;
+      if (S[m] == b) return m;
+      if (S[m] < b) lo = m + 1; else hi = m - 1;
+    }
+    return -1;
+  };
+  long long nedge1 = 0;
+  for (long long i = 0; i < n; i++) {
+    const int* S = nbr + off[i];
+    int ns = (int)(off[i + 1] - off[i]);
+    for (int q = 0; q < ns; q++) {
+      int j = S[q];
+      if (j == i) continue;
+      int p = find(j, (int)i);
+      bool e = mark[i][q] || (p >= 0 && mark[j][p]);
+      if (e) { adj[i].push_back(j); if (j > i) nedge1++; }
+    }
+  }
+  auto has = [&](const std::vector<std::vector<int>>& A, int a, int b) {
+    return std::binary_search(A[a].begin(), A[a].end(), b);
+  };
+  // 2. pass 1: triangles i > j > k, centroid rule for all-boundary triangles
+  std::set<std::pair<int, int>> del;
+  std::vector<std::array<int, 3>> kept;
+  for (long long i = 0; i < n; i++) {
+    for (int j : adj[i]) {
+      if (j >= i) break;
+      for (int k : adj[i]) {
+        if (k >= j) break;
+        if (!has(adj, j, k)) continue;
+        int I = (int)i;
+        bool keep = true;
+        if (type[I] != REAL_PARTICLE && type[j] != REAL_PARTICLE && type[k] != REAL_PARTICLE) {
+          const double* p1 = xyz + 3 * (long long)I;
+          const double* p2 = xyz + 3 * (long long)j;
+          const double* p3 = xyz + 3 * (long long)k;
+          double cen[3] = {1. / 3. * (p1[0] + p2[0] + p3[0]), 1. / 3. * (p1[1] + p2[1] + p3[1]),
+                           1. / 3. * (p1[2] + p2[2] + p3[2])};
+          double pc, nn[3], cv;
+          sample<2>(*c, cen, &pc, nn, &cv);
+          double phi_size = 1. / 3. * (phi[I] + phi[j] + phi[k]);
+          if (!(pc > 0.0001 * phi_size)) {
+            keep = false;
+            double v1[2] = {p2[0] - p1[0], p2[1] - p1[1]};
+            double v2[2] = {p3[0] - p2[0], p3[1] - p2[1]};
+            double v3[2] = {p1[0] - p3[0], p1[1] - p3[1]};
+            double d = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1]);
+            std::pair<int, int> e(I, j);
+            double d2 = std::sqrt(v2[0] * v2[0] + v2[1] * v2[1]);
+            if (d2 > d) { d = d2; e = std::make_pair(j, k); }
+            double d3 = std::sqrt(v3[0] * v3[0] + v3[1] * v3[1]);
+            if (d3 > d) { d = d3; e = std::make_pair(I, k); }
+            del.insert(e);
+          }
+        }
+        if (keep) kept.push_back({I, j, k});
+      }
+    }
+  }
+  // 3. rebuild from kept triangles without a deleted edge
+  std::vector<std::vector<int>> adj2(n);
+  for (auto& t : kept) {
+    if (del.count({t[0], t[1]}) || del.count({t[0], t[2]}) || del.count({t[1], t[2]})) continue;
+    int e[3][2] = {{t[0], t[1]}, {t[1], t[2]}, {t[0], t[2]}};
+    for (auto& q : e) { adj2[q[0]].push_back(q[1]); adj2[q[1]].push_back(q[0]); }
+  }
+  long long nedge2 = 0;
+  for (long long i = 0; i < n; i++) {
+    std::sort(adj2[i].begin(), adj2[i].end());
+    adj2[i].erase(std::unique(adj2[i].begin(), adj2[i].end()), adj2[i].end());
+    for (int j : adj2[i]) if (j > i) nedge2++;
+  }
+  // 4. pass 2: final triangles = 3-cycles; error checks (graph_mesh.cpp:300-365)
+  long long ntri = 0, nerr = 0;
+  for (long long i = 0; i < n; i++) {
+    for (int j : adj2[i]) {
+      if (j >= i) break;
+      int common = 0, c0 = -1, c1 = -1;
+      for (int k : adj2[i]) {
+        if (k == j) continue;
+        if (!has(adj2, j, k)) continue;
+        if (common == 0) c0 = k; else if (common == 1) c1 = k;
+        common++;
+        if (k < j) {
+          if (tris && ntri < cap) { tris[3 * ntri] = (int)i; tris[3 * ntri + 1] = j; tris[3 * ntri + 2] = k; }
+          ntri++;
+        }
+      }
+      if (common > 2 || (common == 2 && has(adj2, c0, c1))) nerr++;
+    }
+  }
+  if (!Q) return ntri;
+  // 5. quality statistics (Tri_quality_statistics, graph_mesh.cpp:411-670)
+  std::memset(Q, 0, sizeof(*Q));
+  Q->ntri = ntri; Q->nedge = nedge2; Q->nedge_first = nedge1; Q->ndeleted = (long long)del.size(); Q->nerror = nerr;
+  double maxa = 0., mina = 1.e15, maxasp = 0., maxe = 0., mine = 1.e15, maxar = 0., minar = 1.e15, Gmin = 1.e20;
+  double Gsum = 0., minavg = 0., tot = 0.;
+  long long th30 = 0;
+  const double rad = 180. / std::acos(-1.);
+  for (long long t = 0; t < std::min(ntri, cap); t++) {
+    const double* v0 = xyz + 3 * (long long)tris[3 * t];
+    const double* v1 = xyz + 3 * (long long)tris[3 * t + 1];
+    const double* v2 = xyz + 3 * (long long)tris[3 * t + 2];
+    double a1[2] = {v1[0] - v0[0], v1[1] - v0[1]}, a2[2] = {v2[0] - v1[0], v2[1] - v1[1]},
+           a3[2] = {v0[0] - v2[0], v0[1] - v2[1]};
+    double d1 = std::sqrt(a1[0] * a1[0] + a1[1] * a1[1]);
+    double d2 = std::sqrt(a2[0] * a2[0] + a2[1] * a2[1]);
+    double d3 = std::sqrt(a3[0] * a3[0] + a3[1] * a3[1]);
+    double dmax = AMAX1(d1, AMAX1(d2, d3)), dmin = AMIN1(d1, AMIN1(d2, d3));
+    maxe = AMAX1(maxe, dmax);
+    mine = AMIN1(mine, dmin);
+    maxasp = AMAX1(maxasp, dmax / (dmin + 1.e-20));
+    double c13 = -(a1[0] * a3[0] + a1[1] * a3[1]) / (d3 * d1 + 1.e-20);
+    double al1 = rad * std::acos(c13);
+    double al2 = rad * std::acos(-(a1[0] * a2[0] + a1[1] * a2[1]) / (d2 * d1 + 1.e-20));
+    double al3 = rad * std::acos(-(a2[0] * a3[0] + a2[1] * a3[1]) / (d3 * d2 + 1.e-20));
+    al1 = AMAX1(0., AMIN1(al1, 180.));
+    al2 = AMAX1(0., AMIN1(al2, 180.));
+    al3 = AMAX1(0., AMIN1(al3, 180.));
+    maxa = AMAX1(maxa, AMAX1(al1, AMAX1(al2, al3)));
+    double mm = AMIN1(al1, AMIN1(al2, al3));
+    mina = AMIN1(mina, mm);
+    Q->hist[std::min(44, (int)(al1 / 4.0))]++;
+    Q->hist[std::min(44, (int)(al2 / 4.0))]++;
+    Q->hist[std::min(44, (int)(al3 / 4.0))]++;
+    if (mm < 30.) th30++;
+    minavg += mm;
+    double area = 0.5 * (d3 * d1) * std::sin(std::acos(c13));
+    tot += area;
+    maxar = AMAX1(maxar, area);
+    minar = AMIN1(minar, area);
+    double G = 2. * std::sqrt(3.) * area / (dmax * (d1 + d2 + d3) / 2.);
+    Gmin = AMIN1(G, Gmin);
+    Gsum = Gsum + G;
+  }
+  Q->max_angle = maxa; Q->min_angle = mina; Q->max_aspect = maxasp; Q->max_edge = maxe; Q->min_edge = mine;
+  Q->max_area = maxar; Q->min_area = minar; Q->G_min = Gmin;
+  Q->G_avg = ntri ? Gsum / ntri : 0.0;
+  Q->min_angle_avg = ntri ? minavg / ntri : 0.0;
+  Q->theta_30 = ntri ? (double)th30 / (double)ntri : 0.0;
+  Q->total_area = tot;
+  return ntri;
 }
 
 int orc_num_threads(void) {

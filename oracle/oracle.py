@@ -75,6 +75,14 @@ class OrcCvpResult(C.Structure):
                 ("total_energy", C.c_double)]
 
 
+class OrcTriQuality(C.Structure):
+    _fields_ = ([(f, C.c_longlong) for f in ("ntri", "nedge", "nedge_first", "ndeleted", "nerror")]
+                + [(f, C.c_double) for f in ("max_angle", "min_angle", "max_aspect", "max_edge", "min_edge",
+                                             "max_area", "min_area", "G_min", "G_avg", "min_angle_avg",
+                                             "theta_30", "total_area")]
+                + [("hist", C.c_longlong * 45)])
+
+
 _lib = None
 
 
@@ -105,6 +113,9 @@ def lib():
         L.orc_steps.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcState), C.c_int]
         L.orc_steps.restype = C.c_longlong
         L.orc_num_threads.restype = C.c_int
+        L.orc_triangulate.argtypes = [C.POINTER(OrcCtx), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(OrcTriQuality)]
+        L.orc_triangulate.restype = C.c_longlong
         L.orc_cvp.argtypes = [C.POINTER(OrcCvpParams), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_void_p, C.c_void_p, C.POINTER(OrcCvpResult)]
         _lib = L
@@ -261,6 +272,23 @@ class Oracle:
         tag = np.zeros(n, dtype=np.int32)
         lib().orc_sample(C.byref(self.ctx), n, _p(xyz), _p(phi), _p(nrm), _p(curv), _p(tag))
         return phi, nrm, curv, tag
+
+    def triangulate(self, xyz, type_, phi, off, nbr):
+        """2D neighbour-graph triangulation + quality (graph_mesh.cpp:37-670), id space."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(type_, dtype=np.int32)
+        ph = np.ascontiguousarray(phi, dtype=np.float64)
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        q = OrcTriQuality()
+        n = len(xyz)
+        ntri = lib().orc_triangulate(C.byref(self.ctx), n, _p(xyz), _p(t), _p(ph), _p(off), _p(nbr), None, 0, None)
+        tris = np.zeros((max(ntri, 1), 3), dtype=np.int32)
+        lib().orc_triangulate(C.byref(self.ctx), n, _p(xyz), _p(t), _p(ph), _p(off), _p(nbr), _p(tris), ntri,
+                              C.byref(q))
+        qd = {f: getattr(q, f) for f, _ in OrcTriQuality._fields_ if f != "hist"}
+        qd["hist"] = list(q.hist)
+        return tris[:ntri], qd
 
     def get_scale(self, phi: float) -> float:
         return lib().orc_get_scale(C.byref(self.ctx), phi)

@@ -154,18 +154,26 @@ def max_phi(levels: List[LevelGrid], dim: int) -> float:
 def disc_hole_2d(spacing: float = 0.01, grid: int = 256, kernel: str = "wendland",
                  h_over_dx: float = 1.3, precision: str = "fp64", seed: int = 0,
                  steps: int = 200) -> Case:
-    """Unit square minus a disc (r = 0.2 at (0.5, 0.5)), analytic SDF on a
-    grid^2 cell-centred level set, constant spacing."""
+    """Unit square minus a disc (r = 0.2 at (0.5, 0.5)), analytic SDF sampled
+    at grid cells per unit length (grid^2 cells over the unit square), constant
+    spacing.  The domain adds grid/16 cells of margin on every side so that the
+    seeding clamp (one package inside the box, Random_particle_distribution,
+    sph_mesh_generation.cpp:1331-1345) falls outside the body."""
     p = default_params(2)
+    npkg_unit = grid // 4
+    margin_pkg = max(npkg_unit // 16, 1)
+    dpkg = 1.0 / npkg_unit
+    lo = -margin_pkg * dpkg
+    hi = 1.0 + margin_pkg * dpkg
+    npkg = npkg_unit + 2 * margin_pkg
     p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=spacing, max_dl=spacing,
-             cell_ratio=2.0 * h_over_dx, box_l=[0.0, 0.0, 0.0], box_r=[1.0, 1.0, 0.0], seed=seed)
+             cell_ratio=2.0 * h_over_dx, box_l=[lo, lo, 0.0], box_r=[hi, hi, 0.0], seed=seed)
 
     def sdf(X, Y, Z):
         disc = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2) - 0.2
         return np.minimum(np.minimum(np.minimum(X, 1.0 - X), np.minimum(Y, 1.0 - Y)), disc)
 
-    npkg = grid // 4
-    lv = make_level(sdf, 2, [0.0, 0.0, 0.0], [1.0 / npkg, 1.0 / npkg, 1.0], [npkg, npkg, 1])
+    lv = make_level(sdf, 2, [lo, lo, 0.0], [dpkg, dpkg, 1.0], [npkg, npkg, 1])
     n = particle_count([lv], p)
     return Case("disc_hole_2d", p, [lv], n, steps=steps)
 
@@ -173,18 +181,19 @@ def disc_hole_2d(spacing: float = 0.01, grid: int = 256, kernel: str = "wendland
 def torus_3d(dx_min: float = 0.005, dx_max: float = 0.02, kernel: str = "wendland",
              h_over_dx: float = 1.3, precision: str = "fp32", seed: int = 0, steps: int = 500,
              fine_pkg: int = 64, nlevels: int = 3) -> Case:
-    """Inside of a torus (R = 1, r = 0.35), nested level-set grids of
-    16/32/64 packages along x (64^3/128^3/256^3 cells nominal; z extent
-    trimmed to whole packages), finer levels active where |phi| < 4 cells of
-    the next-coarser level.  Spacing from dx_min to dx_max by the tanh law."""
+    """Inside of a torus (R = 1, r = 0.35) in the box [-1.6, 1.6]^2 x [-0.6, 0.6]
+    on nested level-set grids of fine_pkg/4, fine_pkg/2, fine_pkg packages along
+    x (64/128/256 cells for fine_pkg = 64), finer levels active where |phi| is
+    below 4 cells of the next-coarser level.  The box leaves one coarse package
+    between the body and the seeding clamp.  Spacing dx_min..dx_max by the
+    reference's tanh law."""
     p = default_params(3)
-    zhalf = 0.0
     npx0 = fine_pkg >> (nlevels - 1)
-    dpkg0 = 2.9 / npx0
-    npz0 = int(round(0.9 / dpkg0))
+    dpkg0 = 3.2 / npx0
+    npz0 = int(round(1.2 / dpkg0))
     zhalf = 0.5 * npz0 * dpkg0
-    box_l = [-1.45, -1.45, -zhalf]
-    box_r = [1.45, 1.45, zhalf]
+    box_l = [-1.6, -1.6, -zhalf]
+    box_r = [1.6, 1.6, zhalf]
     p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=dx_min, max_dl=dx_max,
              cell_ratio=2.0 * h_over_dx, box_l=box_l, box_r=box_r, seed=seed)
 

@@ -130,7 +130,7 @@ def test_level_plan_restates_define_level_infor_tight():
     assert lv["ncl"] == 3
     for l in range(3):
         assert abs(lv["scale"][l] - lv["max_scale"] / 2 ** l) < 1e-10
-    assert lv["ncell"][2] == [216, 216, 68]
+    assert lv["ncell"][2] == [244, 244, 92]
 
 
 def test_neighbor_relation_symmetric_and_includes_self():
