@@ -254,6 +254,35 @@ int mrsph_cvp_points(mrsph_handle* h, long long n, const double* xyz, const doub
                      const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass,
                      mrsph_cvp_result* res);
 
+/* 2D triangulation of the relaxed particles (row A14): the neighbour-graph
+ * mesh of Voronoi_construction::Local_VD_generation
+ * (src/geometry_tools/voronoi_construction.cpp:6-127: an edge i-j when j is a
+ * Voronoi neighbour of i among i's neighbours; voro++ replaced by exact
+ * orient2d / incircle signs), Graphmeshcls::Reconstruct_tris
+ * (src/geometry_tools/graph_mesh.cpp:37-409: 3-cycles i > j > k; a triangle of
+ * three non-REAL particles whose centroid phi <= 1e-4 x the vertex mean loses
+ * its longest edge; the graph is rebuilt from the kept triangles; final
+ * 3-cycles plus non-manifold / crossing checks) and Tri_quality_statistics
+ * (graph_mesh.cpp:411-670).  Uses the neighbour lists of the last density
+ * phase and the current positions. */
+typedef struct {
+  long long ntri;        /* final triangles */
+  long long nedge;       /* edges after the rebuild */
+  long long nedge_first; /* local-Voronoi edges before pass 1 */
+  long long ndeleted;    /* edges removed by the centroid rule */
+  long long nerror;      /* edges with > 2 triangles or crossing opposite vertices */
+  double max_angle, min_angle, max_aspect, max_edge, min_edge, max_area, min_area;
+  double G_min, G_avg;   /* shape factor 2 sqrt(3) A / (l_max s) */
+  double min_angle_avg, theta_30; /* mean minimum angle; share of triangles with min angle < 30 deg */
+  double total_area;
+  long long hist[45];    /* all angles, 4-degree bins (the last bin takes 176..180) */
+} mrsph_tri_quality;
+
+/* tris (cap x 3 ints, vertex ids, rows ordered i > j > k, ascending (i, j, k))
+ * may be NULL or too small: *ntri is always set and tris is filled only when
+ * cap >= *ntri.  quality may be NULL.  2D handles only. */
+int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri, mrsph_tri_quality* quality);
+
 /* e2e helpers: positions in id order (n x 3), host memory (pinned or not). */
 int mrsph_upload_positions(mrsph_handle* h, const double* xyz);
 int mrsph_download_positions(mrsph_handle* h, double* xyz);

@@ -719,6 +719,33 @@ __global__ void k_tap(KCtx c, Buf<R> b, Work<R> w, const int* __restrict__ slot_
   }
 }
 
+// triangulation inputs by particle id; rows translated to ids and sorted
+template <int D, class R>
+__global__ void k_export_tri(KCtx c, Buf<R> b, Work<R> w, double* __restrict__ xyz, int* __restrict__ type,
+                             double* __restrict__ phi, int* __restrict__ rows, int* __restrict__ cnt, int rowcap,
+                             unsigned* flags) {
+  using P = PosOps<D, R>;
+  long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  int s = w.slot_of_id[k];
+  double x[3];
+  P::world(c, b.posh[s], b.key ? b.key[s] : 0, x);
+  xyz[3 * k] = x[0]; xyz[3 * k + 1] = x[1]; xyz[3 * k + 2] = x[2];
+  type[k] = b.meta[s] & 0xFF;
+  phi[k] = (double)b.phi[s];
+  int m = w.cnt[s];
+  if (m > w.cap || m > rowcap) { atomicOr(flags, 4u); m = min(w.cap, rowcap); }
+  cnt[k] = m;
+  const int* src = w.nbl + (long long)s * w.cap;
+  int* dst = rows + k * rowcap;
+  for (int q = 0; q < m; q++) {  // insertion sort by id
+    int v = b.id[src[q]];
+    int p = q;
+    while (p > 0 && dst[p - 1] > v) { dst[p] = dst[p - 1]; p--; }
+    dst[p] = v;
+  }
+}
+
 template <int D, class R>
 __global__ void k_upload(KCtx c, Buf<R> b, const double* __restrict__ xyz) {
   using P = PosOps<D, R>;
@@ -1078,6 +1105,18 @@ class Engine : public EngineBase {
     MR_CK(cudaGetLastError());
     return 0;
   }
+
+  int export_tri(double* d_xyz, int* d_type, double* d_phi, int* d_rows, int* d_cnt, int rowcap,
+                 unsigned* d_flags) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    if (!have_work_) { err = "no density phase has run"; return MRSPH_ERR_STATE; }
+    k_export_tri<D, R><<<grid(n_), 256, 0, st_>>>(kc_, buf_[cur_], w_, d_xyz, d_type, d_phi, d_rows, d_cnt, rowcap,
+                                                   d_flags);
+    MR_CK(cudaGetLastError());
+    return 0;
+  }
+
+  int neighbor_capacity() const override { return w_.cap; }
 
  private:
   static unsigned long long dbits_host(double x) { unsigned long long u; std::memcpy(&u, &x, 8); return u; }

@@ -39,6 +39,12 @@ class EngineBase {
   virtual long long num_particles() const = 0;
   // FP64 world positions in particle-id order into a device buffer (n x 3)
   virtual int world_positions(double* d_out) = 0;
+  // Triangulation inputs in particle-id order: FP64 positions (n x 3), type,
+  // phi, neighbour rows of the last density phase (n x rowcap ids, ascending,
+  // spilled rows clamped with bit 4 set in *d_flags) and their counts.
+  virtual int export_tri(double* d_xyz, int* d_type, double* d_phi, int* d_rows, int* d_cnt, int rowcap,
+                         unsigned* d_flags) = 0;
+  virtual int neighbor_capacity() const = 0;
   std::string err;
 };
 

@@ -55,6 +55,14 @@ class CvpResult(C.Structure):
                 ("total_energy", C.c_double)]
 
 
+class TriQuality(C.Structure):
+    _fields_ = ([(k, C.c_longlong) for k in ("ntri", "nedge", "nedge_first", "ndeleted", "nerror")] +
+                [(k, C.c_double) for k in ("max_angle", "min_angle", "max_aspect", "max_edge", "min_edge",
+                                           "max_area", "min_area", "G_min", "G_avg", "min_angle_avg", "theta_30",
+                                           "total_area")] +
+                [("hist", C.c_longlong * 45)])
+
+
 class StateIn(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("v", C.c_void_p), ("type", C.c_void_p), ("h", C.c_void_p),
                 ("level", C.c_void_p), ("nu", C.c_void_p), ("dt", C.c_double), ("step", C.c_longlong)]
@@ -84,6 +92,8 @@ EXPORTS = {
                   C.c_int),
     "mrsph_cvp_points": ([C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p, C.POINTER(CvpParams), C.c_void_p,
                           C.c_void_p, C.c_void_p, C.POINTER(CvpResult)], C.c_int),
+    "mrsph_triangulate": ([C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(TriQuality)],
+                          C.c_int),
     "mrsph_upload_positions": ([C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_download_positions": ([C.c_void_p, C.c_void_p], C.c_int),
 }

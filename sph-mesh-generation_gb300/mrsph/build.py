@@ -26,6 +26,7 @@ SOURCES = {
     "mrsph_fp32.cu": [],
     "mrsph_noalloc.cu": [],
     "mrsph_cvp.cu": ["-fmad=false"],
+    "mrsph_tri.cu": ["-fmad=false"],
 }
 
 

@@ -148,6 +148,31 @@ def max_phi(levels: List[LevelGrid], dim: int) -> float:
     return mp
 
 
+def cell_levels_consistent(box_l, box_r, dim: int, max_scale: float, min_scale: float) -> bool:
+    """True when the reference's tight level plan (sph.cpp:144-180) gives every
+    cell-list level a cell size of max_scale' / 2^l, max_scale' = domain /
+    floor(domain / max_scale).  The plan truncates domain / max_scale' per axis,
+    which for some domains loses a cell to rounding (1.125 / (1.125 / 28) < 28);
+    the library rejects such domains."""
+    dom = [box_r[d] - box_l[d] for d in range(dim)]
+    st = min(dom)
+    temp = math.floor(st / max_scale)
+    if temp < 1:
+        return False
+    ini = st / temp
+    sc, nl = ini, 1
+    while sc + 1.e-6 > min_scale:
+        sc /= 2
+        nl += 1
+    nl -= 1
+    n0 = [int(dom[d] / ini) for d in range(dim)]
+    for l in range(nl):
+        s = min(dom[d] / (n0[d] * 2.0 ** l) for d in range(dim))
+        if abs(s - math.ldexp(ini, -l)) > 1.e-10:
+            return False
+    return True
+
+
 # ---------------------------------------------------------------------------
 # Workloads
 # ---------------------------------------------------------------------------
@@ -161,13 +186,17 @@ def disc_hole_2d(spacing: float = 0.01, grid: int = 256, kernel: str = "wendland
     sph_mesh_generation.cpp:1331-1345) falls outside the body."""
     p = default_params(2)
     npkg_unit = grid // 4
-    margin_pkg = max(npkg_unit // 16, 1)
     dpkg = 1.0 / npkg_unit
+    cell_ratio = 2.0 * h_over_dx
+    margin_pkg = max(npkg_unit // 16, 1)
+    while not cell_levels_consistent([-margin_pkg * dpkg] * 2, [1.0 + margin_pkg * dpkg] * 2, 2,
+                                     spacing * cell_ratio, spacing * cell_ratio):
+        margin_pkg += 1
     lo = -margin_pkg * dpkg
     hi = 1.0 + margin_pkg * dpkg
     npkg = npkg_unit + 2 * margin_pkg
     p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=spacing, max_dl=spacing,
-             cell_ratio=2.0 * h_over_dx, box_l=[lo, lo, 0.0], box_r=[hi, hi, 0.0], seed=seed)
+             cell_ratio=cell_ratio, box_l=[lo, lo, 0.0], box_r=[hi, hi, 0.0], seed=seed)
 
     def sdf(X, Y, Z):
         disc = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2) - 0.2
@@ -196,6 +225,8 @@ def torus_3d(dx_min: float = 0.005, dx_max: float = 0.02, kernel: str = "wendlan
     box_r = [1.6, 1.6, zhalf]
     p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=dx_min, max_dl=dx_max,
              cell_ratio=2.0 * h_over_dx, box_l=box_l, box_r=box_r, seed=seed)
+    if not cell_levels_consistent(box_l, box_r, 3, dx_max * p["cell_ratio"], dx_min * p["cell_ratio"]):
+        raise ValueError("torus box gives an inconsistent cell-list level plan")
 
     def sdf(X, Y, Z):
         return 0.35 - np.sqrt((np.sqrt(X * X + Y * Y) - 1.0) ** 2 + Z * Z)

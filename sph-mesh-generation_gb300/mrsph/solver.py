@@ -258,6 +258,23 @@ class SPHMeshGeneration:
                                           _ptr(labels), _ptr(vmass), C.byref(res)), self.h, "mrsph_cvp_points")
         return vp, labels, vmass, {f: getattr(res, f) for f, _ in L.CvpResult._fields_}
 
+    # -------------------------------------------------------- triangulation
+    def Reconstruct_tris(self):
+        """2D triangle mesh of the current particles and its quality statistics
+        (Graphmeshcls::Reconstruct_tris, geometry_tools/graph_mesh.cpp:37-409, on the
+        local-Voronoi graph of Voronoi_construction::Local_VD_generation,
+        geometry_tools/voronoi_construction.cpp:6-127; Tri_quality_statistics,
+        graph_mesh.cpp:411-670).  Returns (tris (ntri x 3 ids), quality dict)."""
+        q = L.TriQuality()
+        nt = C.c_longlong(0)
+        L.check(self.lib.mrsph_triangulate(self.h, None, 0, C.byref(nt), None), self.h, "mrsph_triangulate")
+        tris = np.zeros((max(nt.value, 1), 3), dtype=np.int32)
+        L.check(self.lib.mrsph_triangulate(self.h, _ptr(tris), nt.value, C.byref(nt), C.byref(q)), self.h,
+                "mrsph_triangulate")
+        out = {f: getattr(q, f) for f, _ in L.TriQuality._fields_ if f != "hist"}
+        out["hist"] = np.array(q.hist[:], dtype=np.int64)
+        return tris[: nt.value], out
+
     def upload_positions(self, xyz: np.ndarray):
         L.check(self.lib.mrsph_upload_positions(self.h, _ptr(xyz)), self.h, "mrsph_upload_positions")
 

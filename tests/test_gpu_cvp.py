@@ -31,7 +31,8 @@ def test_cvp_square_quadrants():
     rng = np.random.default_rng(0)
     vp = np.zeros((4, 3))
     vp[:, :2] = 0.3 + 0.4 * rng.random((4, 2))
-    gv, gl, gm, gr = _compare(gpu, 2, [0, 0, 0], [1, 1, 0], xyz, vp, 400)
+    p = case.params  # mrsph_cvp_points partitions inside the handle's domain
+    gv, gl, gm, gr = _compare(gpu, 2, p["box_l"], p["box_r"], xyz, vp, 400)
     assert gr["converged"] == 1
     assert gm.min() > 0.9 * 2500
     gpu.close()

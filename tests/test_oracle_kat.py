@@ -167,3 +167,35 @@ def test_cvp_converges_to_quadrant_centroids():
     for c in ([0.25, 0.25], [0.25, 0.75], [0.75, 0.25], [0.75, 0.75]):
         assert np.min(np.hypot(v[:, 0] - c[0], v[:, 1] - c[1])) < 0.03
     assert np.bincount(lab, minlength=4).min() > 2300
+
+
+def test_triangulation_with_full_rows_is_delaunay():
+    """With every point in every neighbour row, the local-Voronoi edges of the
+    oracle are the Delaunay edges of the point set (checked against qhull),
+    and every Delaunay triangle is a final triangle."""
+    spatial = pytest.importorskip("scipy.spatial")
+    rng = np.random.default_rng(5)
+    n = 160
+    xyz = np.zeros((n, 3))
+    xyz[:, :2] = 0.1 + 0.8 * rng.random((n, 2))
+    off = np.arange(n + 1, dtype=np.int64) * n
+    nbr = np.tile(np.arange(n, dtype=np.int32), n)
+    orc = oracle.Oracle(cases.disc_hole_2d(spacing=0.02, grid=64))
+    tris, q = orc.triangulate(xyz, np.zeros(n, dtype=np.int32), np.ones(n), off, nbr)
+    d = spatial.Delaunay(xyz[:, :2])
+    edges = set()
+    for s in d.simplices:
+        for a in range(3):
+            for b in range(a + 1, 3):
+                edges.add((min(s[a], s[b]), max(s[a], s[b])))
+    assert q["nedge_first"] == len(edges)
+    assert q["ndeleted"] == 0
+    got = {tuple(sorted(t)) for t in tris.tolist()}
+    want = {tuple(sorted(s)) for s in d.simplices.tolist()}
+    assert want <= got
+    assert q["ntri"] == len(got)
+    assert sum(q["hist"]) == 3 * q["ntri"]
+    hull_area = spatial.ConvexHull(xyz[:, :2]).volume
+    sep = len(got) - len(want)  # separating 3-cycles add area
+    if sep == 0:
+        assert abs(q["total_area"] - hull_area) < 1e-12
