@@ -116,7 +116,7 @@ typedef struct {
   long long pairs_total; /* ordered neighbour pairs summed over all steps since seeding */
   int flags;          /* MRSPH_FLAG_* accumulated since the last mrsph_get_stats */
   int num_cell_levels;/* cell-list levels in use */
-  long long num_cells;/* cell-list cells over all levels */
+  long long num_cells;/* entries of the sort table (half-size cell-list cells, all levels) */
   double max_phi;     /* maximum phi of the level set (Levelset::maximum_phi) */
 } mrsph_stats;
 
@@ -215,8 +215,9 @@ int mrsph_profile_steps(mrsph_handle* h, int nsteps, double* phase_ms, int nphas
 int mrsph_get_stats(mrsph_handle* h, mrsph_stats* out);
 int mrsph_get_particles(mrsph_handle* h, const mrsph_particle_view* view);
 /* Cell binning tap: per particle (id order) level, cx, cy, cz (n x 4 ints);
- * sorted_ids (n ints) = particle ids in device storage order (cells grouped,
- * ascending id inside a cell).  Either pointer may be NULL. */
+ * sorted_ids (n ints) = particle ids in device storage order: levels in
+ * turn, half cells (dcell/2) row-major within a level, ascending id inside a
+ * half cell.  Either pointer may be NULL. */
 int mrsph_get_cells(mrsph_handle* h, int* level_cell, int* sorted_ids);
 /* Neighbour lists of the last density phase in CSR form, particle-id order,
  * neighbour ids ascending.  Call with nb == NULL to get *total only. */

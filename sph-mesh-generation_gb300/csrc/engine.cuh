@@ -100,6 +100,12 @@ struct PosOps<D, double> {
       cc[d] = max(0, min(q, c.geo.n[L][d] - 1));
     }
   }
+  // box-relative position (the operand of get_cell_id)
+  __device__ static void xrel(const KCtx& c, const T4& p, int, double* xr) {
+    xr[0] = p.x - c.geo.box_l[0];
+    xr[1] = p.y - c.geo.box_l[1];
+    xr[2] = (D == 3) ? p.z - c.geo.box_l[2] : 0.0;
+  }
   __device__ static void rel(const KCtx&, const T4& pi, int, const T4& pj, int, double* dr) {
     dr[0] = pi.x - pj.x;
     dr[1] = pi.y - pj.y;
@@ -165,6 +171,13 @@ struct PosOps<D, float> {
     cc[2] = 0;
     for (int d = 0; d < D; d++) cc[d] = k[d] >> sh;
   }
+  __device__ static void xrel(const KCtx& c, const T4& p, int key, double* xr) {
+    int k[3];
+    unpack(key, k);
+    const float o[3] = {p.x, p.y, p.z};
+    xr[2] = 0.0;
+    for (int d = 0; d < D; d++) xr[d] = (double)k[d] * c.geo.A[d] + (double)o[d];
+  }
   __device__ static void rel(const KCtx& c, const T4& pi, int ki, const T4& pj, int kj, float* dr) {
     int a[3], b[3];
     unpack(ki, a);
@@ -210,6 +223,10 @@ static __global__ void k_begin_step(DevScalars* sc, int inc) {
   sc->remap = 0;
   sc->nsurf = 0;
   sc->maxcnt = 0;
+  for (int l = 0; l < MAX_CL; l++) {
+    sc->hmax[l] = 0;
+    sc->lcount[l] = 0;
+  }
   sc->step += inc;
 }
 
@@ -262,6 +279,13 @@ __global__ void k_seed(KCtx c, Buf<R> b, unsigned max_att) {
 template <int D, class R>
 __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int mode, unsigned max_att) {
   using P = PosOps<D, R>;
+  __shared__ unsigned long long s_hmax[MAX_CL];
+  __shared__ unsigned s_lcount[MAX_CL];
+  if (threadIdx.x < MAX_CL) {
+    s_hmax[threadIdx.x] = 0;
+    s_lcount[threadIdx.x] = 0;
+  }
+  __syncthreads();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned surf = 0;
   if (i < c.n) {
@@ -355,10 +379,19 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
       L = max(0, min(L, c.geo.ncl - 1));
       e = L;
     }
-    int cc[3];
-    P::cell(c, L, p, key, cc);
-    int ck = (int)(c.geo.off[L] + ((long long)cc[2] * c.geo.n[L][1] + cc[1]) * c.geo.n[L][0] + cc[0]);
+    // sort key: level-L half cell (get_cell_id, glbfunc.h:196-208, at dcell/2)
+    double xr[3];
+    P::xrel(c, p, key, xr);
+    int hq[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      double u = floor(xr[d] / c.geo.hs[L][d]);
+      u = fmax(0.0, fmin(u, (double)(c.geo.hn[L][d] - 1)));
+      hq[d] = (int)u;
+    }
+    int ck = (int)(c.geo.hoff[L] + ((long long)hq[2] * c.geo.hn[L][1] + hq[1]) * c.geo.hn[L][0] + hq[0]);
     atomicAdd(&counts[ck], 1);
+    atomicMax(&s_hmax[L], dbits((double)h));
+    atomicAdd(&s_lcount[L], 1u);
     p.w = h;
     b.posh[i] = p;
     if (b.key) b.key[i] = key;
@@ -371,6 +404,11 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
   }
   unsigned ws = __popc(__ballot_sync(0xffffffffu, surf != 0));
   if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&c.sc->nsurf, ws);
+  __syncthreads();
+  if (threadIdx.x < MAX_CL && s_lcount[threadIdx.x]) {
+    atomicMax(&c.sc->hmax[threadIdx.x], s_hmax[threadIdx.x]);
+    atomicAdd(&c.sc->lcount[threadIdx.x], s_lcount[threadIdx.x]);
+  }
 }
 
 // Packed record read by the neighbour passes, two V4 words per particle so
@@ -440,35 +478,67 @@ __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict_
   slot_of_id[id] = (int)s;
 }
 
-// Candidate cells of particle i (level Li, own cell ci) over all cell-list
-// levels, equivalent to the reference's tree walk (level_infor.cpp:407-506):
-//   L <= Li: 3^D cells around ci >> (Li-L) at level L (particles of level L;
-//            for L < Li these are the coarse particles whose walk finds i),
-//   L >  Li: the level-L cells under the 3^D level-Li cells around ci.
-// Each (z, y) row of cells is one contiguous range of the sorted arrays.
+// Candidates of particle i over all cell-list levels.  The reference walks
+// the 3^D cells of i's level, whose lists hold the particles of that level and
+// of every finer one, and links i and j when r <= 2 h_i or r <= 2 h_j
+// (level_infor.cpp:407-506).  The same relation is found here per level L
+// among the level-L particles within R_L = cutoff * max(h_i, hmax_L) + 1e-10
+// of x_i, hmax_L being the largest h on level L this step: only the half cells
+// of the sort table that the sphere of radius R_L reaches are read.  Each
+// (z, y) row of half cells is one contiguous range of the sorted arrays; rows
+// farther than R_L are skipped and the x range of each row is cut to the
+// sphere.  Edge rows extend to infinity (keys are clamped into the table).
+// R_L carries a 1e-5 relative pad for the rounding of the keys and of the
+// FP32 row arithmetic; the candidate test itself decides membership.
 template <int D, class F>
-__device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart, int Li, const int* ci, F&& f) {
+__device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart, const double* xr,
+                                       double hi, F&& f) {
+  const double hic = hi * c.prm.cutoff;
   for (int L = 0; L < c.geo.ncl; L++) {
-    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (c.sc->lcount[L] == 0) continue;
+    const double Rw = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
+    const float R = (float)(Rw * (1.0 + 1.e-5));
+    int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {0, 0, 0}, hn[3];
+    float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
+    for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
     for (int d = 0; d < D; d++) {
-      int nL = c.geo.n[L][d];
-      if (L <= Li) {
-        int cc = ci[d] >> (Li - L);
-        lo[d] = max(cc - 1, 0);
-        hi[d] = min(cc + 1, nL - 1);
-      } else {
-        int k = L - Li;
-        lo[d] = max((ci[d] - 1) * (1 << k), 0);
-        hi[d] = min((ci[d] + 2) * (1 << k) - 1, nL - 1);
+      double u = xr[d] / c.geo.hs[L][d];
+      u = fmax(-1.0e6, fmin(u, 1.0e9));
+      const double fl = floor(u);
+      q[d] = (int)fl;
+      fr[d] = (float)(u - fl);
+      hs[d] = (float)c.geo.hs[L][d];
+      const float rr = R / hs[d];
+      lo[d] = max(q[d] + (int)floorf(fr[d] - rr), 0);
+      up[d] = min(q[d] + (int)floorf(fr[d] + rr), hn[d] - 1);
+    }
+    const long long base = c.geo.hoff[L];
+    const float R2 = R * R;
+    for (int z = lo[2]; z <= up[2]; z++) {
+      float gz = 0.f;
+      if (D == 3) {
+        const int m = z - q[2];
+        if (z > 0) gz = fmaxf(gz, (float)m - fr[2]);
+        if (z < hn[2] - 1) gz = fmaxf(gz, fr[2] - (float)(m + 1));
+        gz *= hs[2];
+      }
+      for (int y = lo[1]; y <= up[1]; y++) {
+        const int m = y - q[1];
+        float gy = 0.f;
+        if (y > 0) gy = fmaxf(gy, (float)m - fr[1]);
+        if (y < hn[1] - 1) gy = fmaxf(gy, fr[1] - (float)(m + 1));
+        gy *= hs[1];
+        const float rem = R2 - gy * gy - gz * gz;
+        if (rem < 0.f) continue;
+        const float w = sqrtf(rem) / hs[0];
+        const int xl = max(q[0] + (int)floorf(fr[0] - w), 0);
+        const int xh = min(q[0] + (int)floorf(fr[0] + w), hn[0] - 1);
+        if (xl > xh) continue;
+        const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
+        const int s0 = __ldg(&cstart[rb + xl]), e0 = __ldg(&cstart[rb + xh + 1]);
+        for (int j = s0; j < e0; j++) f(j);
       }
     }
-    const long long off = c.geo.off[L];
-    for (int z = lo[2]; z <= hi[2]; z++)
-      for (int y = lo[1]; y <= hi[1]; y++) {
-        long long rb = off + ((long long)z * c.geo.n[L][1] + y) * c.geo.n[L][0];
-        int s = __ldg(&cstart[rb + lo[0]]), e = __ldg(&cstart[rb + hi[0] + 1]);
-        for (int j = s; j < e; j++) f(j);
-      }
   }
 }
 
@@ -509,7 +579,6 @@ __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
     const T4 a0 = b.rec[2 * i], a1 = b.rec[2 * i + 1];
     const int mi = b.meta[i];
     const int ti = mi & 0xFF;
-    const int Li = (int)(signed char)((mi >> 8) & 0xFF);
     R ni[3] = {0, 0, 0};
     if (ti == SURFACE_P) {
       const T4 nri = b.nr[i];
@@ -517,12 +586,12 @@ __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
     }
     const R hi = a0.w;
     const R cos_t = (R)c.prm.cos_thres;
-    int ci[3];
-    P::cell(c, Li, b.posh[i], b.key ? b.key[i] : 0, ci);
+    double xr[3];
+    P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
     R sum = 0;
     int ncount = 0, cnt = 0;
     int* row = w.nbl + i * (long long)w.cap;
-    scan_candidates<D>(c, w.cstart, Li, ci, [&](int j) {
+    scan_candidates<D>(c, w.cstart, xr, (double)hi, [&](int j) {
       const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
       R dr[3];
       Q::rel(c, a0, a1, b0, b1, dr);
@@ -644,10 +713,9 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
           pair(j, b0, b1, vec);
         }
       } else {
-        const int Li = (int)(signed char)((mi >> 8) & 0xFF);
-        int ci[3];
-        P::cell(c, Li, b.posh[i], b.key ? b.key[i] : 0, ci);
-        scan_candidates<D>(c, w.cstart, Li, ci, [&](int j) {
+        double xr[3];
+        P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
+        scan_candidates<D>(c, w.cstart, xr, (double)h, [&](int j) {
           const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
           R vec[3];
           Q::rel(c, a0, a1r, b0, b1, vec);
@@ -970,7 +1038,7 @@ class Engine : public EngineBase {
     o->remapped = h.remap;
     o->flags = (int)h.flags;
     o->num_cell_levels = kc_.geo.ncl;
-    o->num_cells = kc_.geo.off[kc_.geo.ncl];
+    o->num_cells = kc_.geo.hoff[kc_.geo.ncl];
     o->max_phi = kc_.ls.max_phi;
     return 0;
   }
@@ -1011,12 +1079,12 @@ class Engine : public EngineBase {
       for (long long s = 0; s < n_; s++) {
         long long key = ck[s];
         int L = 0;
-        while (L + 1 < kc_.geo.ncl && key >= kc_.geo.off[L + 1]) L++;
-        long long r = key - kc_.geo.off[L];
-        int cx = (int)(r % kc_.geo.n[L][0]);
-        r /= kc_.geo.n[L][0];
-        int cy = (int)(r % kc_.geo.n[L][1]);
-        int cz = (int)(r / kc_.geo.n[L][1]);
+        while (L + 1 < kc_.geo.ncl && key >= kc_.geo.hoff[L + 1]) L++;
+        long long r = key - kc_.geo.hoff[L];  // half cell -> reference cell
+        int cx = (int)(r % kc_.geo.hn[L][0]) >> 1;
+        r /= kc_.geo.hn[L][0];
+        int cy = (int)(r % kc_.geo.hn[L][1]) >> 1;
+        int cz = (int)(r / kc_.geo.hn[L][1]) >> 1;
         int* o = level_cell + 4 * (long long)ids[s];
         o[0] = L; o[1] = cx; o[2] = cy; o[3] = cz;
       }
@@ -1237,7 +1305,7 @@ class Engine : public EngineBase {
     release();
     n_ = n;
     kc_.n = n;
-    ncells_ = kc_.geo.off[kc_.geo.ncl];
+    ncells_ = kc_.geo.hoff[kc_.geo.ncl];
     int cap = cfg_.neighbor_cap > 0 ? cfg_.neighbor_cap : (D == 2 ? 64 : 192);
     w_.cap = cap;
     auto A = [&](void** p, size_t bytes) -> int {

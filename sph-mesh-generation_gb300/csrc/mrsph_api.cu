@@ -70,25 +70,33 @@ static int plan_levels(mrsph_handle* h) {
     ini[d] = (d < D) ? (int)(domain[d] / max_scale) : 1;
     g.box_l[d] = (d < D) ? p.box_l[d] : 0.0;
   }
-  long long off = 0;
+  long long off = 0, hoff = 0;
   for (int l = 0; l < num_level; l++) {
     double multi = powern_d(2.0, l);
     double sc = 1.e300;
-    long long nc = 1;
+    long long nc = 1, hc = 1;
     for (int d = 0; d < 3; d++) {
       g.n[l][d] = (d < D) ? (int)(ini[d] * multi) : 1;
       g.dcell[l][d] = (d < D) ? domain[d] / g.n[l][d] : 1.0;
       if (d < D) sc = std::min(sc, g.dcell[l][d]);
       nc *= g.n[l][d];
+      // sort table of half cells: floor(x / (dcell/2)) >> 1 == floor(x / dcell)
+      // exactly, since halving commutes with rounding
+      g.hn[l][d] = (d < D) ? 2 * g.n[l][d] : 1;
+      g.hs[l][d] = (d < D) ? 0.5 * g.dcell[l][d] : 1.0;
+      hc *= g.hn[l][d];
     }
     // the engine keys levels by exponent: scale = max_scale * 2^-l (sph.cpp:247-276)
     if (std::fabs(sc - std::ldexp(max_scale, -l)) > 1.e-10)
       return fail(h, MRSPH_ERR_ARG, "cell-list level scale does not match max_scale/2^l; adjust the domain");
     g.off[l] = off;
     off += nc;
+    g.hoff[l] = hoff;
+    hoff += hc;
   }
   g.off[num_level] = off;
-  if (off > (1ll << 26)) return fail(h, MRSPH_ERR_RANGE, "more than 2^26 cell-list cells");
+  g.hoff[num_level] = hoff;
+  if (hoff > (1ll << 28)) return fail(h, MRSPH_ERR_RANGE, "more than 2^25 (3D) / 2^26 (2D) cell-list cells");
   const int lm = num_level - 1;
   for (int d = 0; d < 3; d++) {
     g.A[d] = g.dcell[lm][d];

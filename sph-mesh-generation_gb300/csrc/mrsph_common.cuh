@@ -47,6 +47,10 @@ struct CellGeo {
   long long off[MAX_CL + 1];
   double A[3];  // anchor cell of the FP32-split position = finest cell
   float Af[3];
+  // sort table: half-size cells (2 per reference cell per axis), row-major per level
+  int hn[MAX_CL][3];
+  double hs[MAX_CL][3];  // half-cell size = dcell / 2
+  long long hoff[MAX_CL + 1];
 };
 
 struct Params {
@@ -65,6 +69,8 @@ struct DevScalars {
   unsigned int remap, nsurf, flags, spill;
   unsigned int step;
   unsigned int maxcnt;  // largest neighbour count of the last density phase
+  unsigned long long hmax[MAX_CL];  // FP64 bits of the largest h per level (this step)
+  unsigned int lcount[MAX_CL];      // particles per level (this step)
 };
 
 // ---------------------------------------------------------------- Philox

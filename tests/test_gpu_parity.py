@@ -101,11 +101,31 @@ def test_fp64_step_phase_parity(warmed):
     gpu_post_map_to_oracle(o2, gp, st)
     oc = o2.cells()
     assert np.array_equal(lc, oc), "cell binning differs"
-    # storage order: cells contiguous, ids ascending inside a cell
-    key = [tuple(lc[i]) for i in ids]
-    for a in range(1, len(ids)):
-        if key[a] == key[a - 1]:
-            assert ids[a] > ids[a - 1]
+    # storage order: levels, then half cells (dcell / 2) row-major, ids ascending
+    # inside a half cell; half-cell keys recomputed on the host from the GPU
+    # positions exactly as the engine bins them
+    lv = o2.levels()
+    dim = case.params["dim"]
+    box_l = np.array(case.params["box_l"])
+    hoff = [0]
+    for L in range(lv["ncl"]):
+        hoff.append(hoff[-1] + int(np.prod([2 * lv["ncell"][L][d] for d in range(dim)])))
+    key = np.zeros(len(ids), dtype=np.int64)
+    for a, i in enumerate(ids):
+        L = int(lc[i][0])
+        k = 0
+        for d in (2, 1, 0):
+            hn = 2 * lv["ncell"][L][d] if d < dim else 1
+            hq = 0
+            if d < dim:
+                hq = int(np.floor((gp["xyz"][i][d] - box_l[d]) / (0.5 * lv["dcell"][L][d])))
+                hq = min(max(hq, 0), hn - 1)
+                assert hq >> 1 == lc[i][1 + d]
+            k = k * hn + hq
+        key[a] = hoff[L] + k
+    assert np.all(np.diff(key) >= 0), "storage order is not grouped by half cell"
+    same = np.diff(key) == 0
+    assert np.all(np.diff(ids)[same] > 0), "ids not ascending inside a half cell"
     ooff, onb = o2.neighbors()
     assert np.array_equal(off, ooff), "neighbour counts differ"
     assert np.array_equal(nb, onb), "neighbour sets differ"
