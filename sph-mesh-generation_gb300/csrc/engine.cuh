@@ -542,6 +542,114 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
   }
 }
 
+// Warp-cooperative form of scan_candidates, called by all 32 lanes of a warp
+// (inactive lanes pass active = false).  Per level, when the warp's particles
+// sit within a 4 x 2 x 2 block of half cells (dense regions), the warp walks the
+// union of its lanes' rows: each 32-candidate chunk of a row is loaded once,
+// coalesced, into the warp's shared-memory tile and every lane tests the
+// chunk from there.  Otherwise each lane walks its own rows from global
+// memory.  Either way a lane visits its own candidates in the same order
+// (levels, rows, storage order), so its accepted neighbours and their order
+// do not depend on the mode; lanes also see extra candidates of the union,
+// which the candidate test rejects.
+template <int D, class T4, class F>
+__device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, const T4* __restrict__ rec,
+                                 bool active, const double* xr, double hi, T4 (*tile)[2], F&& f) {
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const double hic = hi * c.prm.cutoff;
+  for (int L = 0; L < c.geo.ncl; L++) {
+    if (c.sc->lcount[L] == 0) continue;
+    const double Rw = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
+    const float R = (float)(Rw * (1.0 + 1.e-5));
+    const float R2 = R * R;
+    int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {-1, -1, -1}, hn[3];
+    float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
+    for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
+    if (D == 2) { lo[2] = 0; up[2] = 0; }
+    if (active) {
+      for (int d = 0; d < D; d++) {
+        double u = xr[d] / c.geo.hs[L][d];
+        u = fmax(-1.0e6, fmin(u, 1.0e9));
+        const double fl = floor(u);
+        q[d] = (int)fl;
+        fr[d] = (float)(u - fl);
+        hs[d] = (float)c.geo.hs[L][d];
+        const float rr = R / hs[d];
+        lo[d] = max(q[d] + (int)floorf(fr[d] - rr), 0);
+        up[d] = min(q[d] + (int)floorf(fr[d] + rr), hn[d] - 1);
+      }
+    }
+    // own x range of row (z, y); empty when the row is outside the lane's sphere
+    auto row_range = [&](int z, int y, int& xl, int& xh) {
+      xl = 0x7fffffff;
+      xh = -1;
+      if (!active || z < lo[2] || z > up[2] || y < lo[1] || y > up[1]) return;
+      float gz = 0.f;
+      if (D == 3) {
+        const int m = z - q[2];
+        if (z > 0) gz = fmaxf(gz, (float)m - fr[2]);
+        if (z < hn[2] - 1) gz = fmaxf(gz, fr[2] - (float)(m + 1));
+        gz *= hs[2];
+      }
+      const int m = y - q[1];
+      float gy = 0.f;
+      if (y > 0) gy = fmaxf(gy, (float)m - fr[1]);
+      if (y < hn[1] - 1) gy = fmaxf(gy, fr[1] - (float)(m + 1));
+      gy *= hs[1];
+      const float rem = R2 - gy * gy - gz * gz;
+      if (rem < 0.f) return;
+      const float w = sqrtf(rem) / hs[0];
+      xl = max(q[0] + (int)floorf(fr[0] - w), 0);
+      xh = min(q[0] + (int)floorf(fr[0] + w), hn[0] - 1);
+    };
+    const long long base = c.geo.hoff[L];
+    // warp compactness at this level
+    const int BIG = 0x3fffffff;
+    bool uni = true;
+    for (int d = 0; d < D; d++) {
+      const int qmin = __reduce_min_sync(FULL, active ? q[d] : BIG);
+      const int qmax = __reduce_max_sync(FULL, active ? q[d] : -BIG);
+      uni = uni && (qmax - qmin <= (d == 0 ? 3 : 1));
+    }
+    if (uni) {
+      const int zl = __reduce_min_sync(FULL, active ? lo[2] : BIG), zu = __reduce_max_sync(FULL, active ? up[2] : -BIG);
+      const int yl = __reduce_min_sync(FULL, active ? lo[1] : BIG), yu = __reduce_max_sync(FULL, active ? up[1] : -BIG);
+      for (int z = zl; z <= zu; z++)
+        for (int y = yl; y <= yu; y++) {
+          int xl, xh;
+          row_range(z, y, xl, xh);
+          const int ul = __reduce_min_sync(FULL, xl), uh = __reduce_max_sync(FULL, xh);
+          if (ul > uh) continue;
+          const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
+          const int s0 = __ldg(&cstart[rb + ul]), e0 = __ldg(&cstart[rb + uh + 1]);
+          for (int t0 = s0; t0 < e0; t0 += 32) {
+            const int k = t0 + lane;
+            if (k < e0) {
+              tile[lane][0] = rec[2 * (long long)k];
+              tile[lane][1] = rec[2 * (long long)k + 1];
+            }
+            __syncwarp();
+            const int m = min(32, e0 - t0);
+            if (active)
+              for (int t = 0; t < m; t++) f(t0 + t, tile[t][0], tile[t][1]);
+            __syncwarp();
+          }
+        }
+    } else if (active) {
+      for (int z = lo[2]; z <= up[2]; z++)
+        for (int y = lo[1]; y <= up[1]; y++) {
+          int xl, xh;
+          row_range(z, y, xl, xh);
+          if (xl > xh) continue;
+          const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
+          const int s0 = __ldg(&cstart[rb + xl]), e0 = __ldg(&cstart[rb + xh + 1]);
+          for (int j = s0; j < e0; j++) f(j, rec[2 * (long long)j], rec[2 * (long long)j + 1]);
+        }
+    }
+  }
+}
+
 // Neighbour criterion, level_infor.cpp:491-500.
 __device__ inline bool nb_test(double d2, double hi, double hj, double cutoff, double& dist) {
   double R = fmax(hi, hj) * cutoff + 1.e-10;
@@ -552,7 +660,7 @@ __device__ inline bool nb_test(double d2, double hi, double hj, double cutoff, d
 __device__ inline bool nb_test(float d2, float hi, float hj, double cutoff, float& dist) {
   float R = fmaxf(hi, hj) * (float)cutoff;
   if (d2 > R * R) return false;
-  dist = sqrtf(d2);
+  dist = pair_dist(d2);
   return true;
 }
 
@@ -573,47 +681,55 @@ __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
+  __shared__ T4 s_tile[8][32][2];
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < c.n;
   unsigned long long pairs = 0;
-  if (i < c.n) {
-    const T4 a0 = b.rec[2 * i], a1 = b.rec[2 * i + 1];
-    const int mi = b.meta[i];
-    const int ti = mi & 0xFF;
-    R ni[3] = {0, 0, 0};
+  T4 a0 = mk4<R>(0, 0, 0, 0), a1 = mk4<R>(0, 0, 0, 0);
+  int ti = REAL_P;
+  R ni[3] = {0, 0, 0};
+  double xr[3] = {0.0, 0.0, 0.0};
+  if (active) {
+    a0 = b.rec[2 * i];
+    a1 = b.rec[2 * i + 1];
+    ti = b.meta[i] & 0xFF;
     if (ti == SURFACE_P) {
       const T4 nri = b.nr[i];
       ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
     }
-    const R hi = a0.w;
-    const R cos_t = (R)c.prm.cos_thres;
-    double xr[3];
     P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
-    R sum = 0;
-    int ncount = 0, cnt = 0;
-    int* row = w.nbl + i * (long long)w.cap;
-    scan_candidates<D>(c, w.cstart, xr, (double)hi, [&](int j) {
-      const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
-      R dr[3];
-      Q::rel(c, a0, a1, b0, b1, dr);
-      R dist;
-      if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
-      if (cnt < w.cap) row[cnt] = j;
-      cnt++;
-      if (ti == REAL_P) {
-        sum += kernel_W<R>(c.prm.kernel, D, dist, hi);
+  }
+  const R hi = a0.w;
+  const R inv_hi = active ? r_rcp(hi) : (R)0;
+  const int kind = c.prm.kernel;
+  const R cos_t = (R)c.prm.cos_thres;
+  R sum = 0;
+  int ncount = 0, cnt = 0;
+  int* row = w.nbl + (active ? i : 0) * (long long)w.cap;
+  warp_scan<D>(c, w.cstart, b.rec, active, xr, (double)hi, s_tile[threadIdx.x >> 5],
+               [&](int j, const T4& b0, const T4& b1) {
+    R dr[3];
+    Q::rel(c, a0, a1, b0, b1, dr);
+    R dist;
+    if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
+    if (cnt < w.cap) row[cnt] = j;
+    cnt++;
+    if (ti == REAL_P) {
+      sum += pair_W(kind, D, dist, hi, inv_hi);
+      ncount++;
+    } else if (ti == SURFACE_P && b1.w < (R)0) {  // surface neighbour of a surface particle
+      R dn = dot3<D, R>(dr, ni);
+      R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
+      R pd = pair_dist(dot3<D, R>(pr, pr));
+      const T4 nrj = b.nr[j];
+      const R nj[3] = {nrj.x, nrj.y, nrj.z};
+      if (r_fabs(dot3<D, R>(ni, nj)) > cos_t) {
+        sum += pair_W(kind, D - 1, pd, hi, inv_hi);
         ncount++;
-      } else if (ti == SURFACE_P && b1.w < (R)0) {  // surface neighbour of a surface particle
-        R dn = dot3<D, R>(dr, ni);
-        R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
-        R pd = r_sqrt(dot3<D, R>(pr, pr));
-        const T4 nrj = b.nr[j];
-        const R nj[3] = {nrj.x, nrj.y, nrj.z};
-        if (r_fabs(dot3<D, R>(ni, nj)) > cos_t) {
-          sum += kernel_W<R>(c.prm.kernel, D - 1, pd, hi);
-          ncount++;
-        }
       }
-    });
+    }
+  });
+  if (active) {
     if (ncount > 1) sum = (R)1. / (sum + (R)1.e-15);
     w.sum[i] = sum;
     w.cnt[i] = cnt;
@@ -670,20 +786,20 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
       const R hij = (R)0.5 * (h + b0.w);
       if (ti == REAL_P) {
         dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
-        R dist = r_sqrt(dot3<D, R>(dr, dr));
-        aw = kernel_dW<R>(c.prm.kernel, D, dist, hij);
+        R dist = pair_dist(dot3<D, R>(dr, dr));
+        aw = pair_dW(c.prm.kernel, D, dist, hij);
       } else {
         R dn = dot3<D, R>(vec, ni);
         dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
-        R dist = r_sqrt(dot3<D, R>(dr, dr));
+        R dist = pair_dist(dot3<D, R>(dr, dr));
         const T4 nrj = b.nr[j];
         const R nj[3] = {nrj.x, nrj.y, nrj.z};
         if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return;
-        aw = kernel_dW<R>(c.prm.kernel, D - 1, dist, hij);
+        aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
       }
       const R rho_j = r_fabs(b1.w);
       if (STAGE == 1) {
-        const R vol_j = (R)1.0 / (rho_j * rho_j);
+        const R vol_j = r_rcp(rho_j * rho_j);
         const R P_ij = sum * (vol_i + vol_j);
         for (int d = 0; d < D; d++) F[d] = F[d] + (dr[d] * aw) * -P_ij;
       } else {
@@ -696,8 +812,8 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
         }
         const R nu_j = anj.w;
         const R eta_i = nu * rho, eta_j = nu_j * rho_j;
-        const R eta_ij = (R)2. * eta_j * eta_i / (eta_i + eta_j + (R)1.e-15);
-        const R temp0 = aw * eta_ij * ((R)1. / rho / rho + (R)1. / rho_j / rho_j);
+        const R eta_ij = r_div((R)2. * eta_j * eta_i, eta_i + eta_j + (R)1.e-15);
+        const R temp0 = aw * eta_ij * (inv_sq(rho) + inv_sq(rho_j));
         for (int d = 0; d < D; d++) F[d] = F[d] + (vi[d] - vj[d]) * temp0;
       }
     };

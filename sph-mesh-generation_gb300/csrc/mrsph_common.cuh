@@ -225,6 +225,130 @@ __device__ inline R kernel_dW(int kind, int D, R dist, R h) {
   return val;
 }
 
+// ------------------------------------------------- pair arithmetic per path
+// FP64 plain keeps the reference's operations (divisions, sqrt) so that its
+// results stay within 1e-12 of the FP64 oracle.  FP32-split evaluates the
+// same formulas without divisions: 1/h and the normalisation constants are
+// hoisted, and reciprocals and square roots come from the hardware
+// approximation units (relative error about 1e-7, well inside the FP32
+// path's tolerance).
+__device__ inline double r_rcp(double x) { return 1.0 / x; }
+__device__ inline float r_rcp(float x) { return __fdividef(1.0f, x); }
+__device__ inline double r_div(double a, double b) { return a / b; }
+__device__ inline float r_div(float a, float b) { return __fdividef(a, b); }
+__device__ inline double pair_dist(double d2) { return sqrt(d2); }
+__device__ inline double inv_sq(double r) { return 1. / r / r; }
+__device__ inline float inv_sq(float r) { return __fdividef(1.f, r * r); }
+__device__ inline float pair_dist(float d2) { return d2 > 0.f ? d2 * rsqrtf(d2) : 0.f; }
+
+// C * h^D of W (particle.cpp:31-401); dW uses the same constants with one
+// more power of h for the hyperbolic and cubic kernels.
+__host__ __device__ constexpr double kern_norm(int kind, int D) {
+  return kind == K_WEN ? (D == 2 ? 1.0 / PI_REF * 7. / 4. : D == 3 ? 1.0 / PI_REF * 21. / 16. : 0.0)
+       : kind == K_HYP ? (D == 1 ? 1.0 / 7.0 : D == 2 ? 1.0 / (3.0 * PI_REF) : 15.0 / (62.0 * PI_REF))
+       : kind == K_CUB ? (D == 1 ? 0.666666667 : D == 2 ? 0.454728408 : 0.318309886)
+       : kind == K_QUI ? (D == 1 ? 1.0 / 120. : D == 2 ? 1.0 / PI_REF * 7. / 478. : 1.0 / PI_REF * 3. / 359.)
+       : 0.0;
+}
+
+// FP32 W(dist, h) given inv_h = 1/h
+__device__ inline float kernel_W_fast(int kind, int D, float dist, float inv_h) {
+  const float s = dist * inv_h;
+  float ih = inv_h, C;
+  float hD = ih;
+  if (D >= 2) hD *= ih;
+  if (D >= 3) hD *= ih;
+  if (kind == K_WEN) {
+    if (D == 1) return 0.f;
+    C = (float)kern_norm(K_WEN, 2) * hD;
+    if (D == 3) C = (float)kern_norm(K_WEN, 3) * hD;
+    if (!(s < 2.f)) return 0.f;
+    const float t = 1.f - 0.5f * s, t2 = t * t;
+    return C * (t2 * t2) * (1.f + 2.f * s);
+  }
+  if (kind == K_HYP) {
+    C = (float)(D == 1 ? kern_norm(K_HYP, 1) : D == 2 ? kern_norm(K_HYP, 2) : kern_norm(K_HYP, 3)) * hD;
+    if (s < 1.f) return C * (6.f - 6.f * s + s * s * s);
+    if (s < 2.f) { const float t = 2.f - s; return C * t * t * t; }
+    return 0.f;
+  }
+  if (kind == K_CUB) {
+    C = (float)(D == 1 ? kern_norm(K_CUB, 1) : D == 2 ? kern_norm(K_CUB, 2) : kern_norm(K_CUB, 3)) * hD;
+    if (s < 1.f) return C * (1.f - 1.5f * s * s + 0.75f * s * s * s);
+    if (s < 2.f) { const float t = 2.f - s; return C * 0.25f * t * t * t; }
+    return 0.f;
+  }
+  if (kind == K_GAU) {
+    const float fac = 0.5f * 2.f / sqrtf((float)PI_REF);
+    float f = fac;
+    if (D > 1) f *= fac;
+    if (D > 2) f *= fac;
+    if (!(s < 3.f)) return 0.f;
+    return __expf(-s * s) * f * hD;
+  }
+  C = (float)(D == 1 ? kern_norm(K_QUI, 1) : D == 2 ? kern_norm(K_QUI, 2) : kern_norm(K_QUI, 3)) * hD;
+  const float a = 3.f - s, b = 2.f - s, c = 1.f - s;
+  const float a5 = a * a * a * a * a, b5 = b * b * b * b * b, c5 = c * c * c * c * c;
+  if (s < 1.f) return C * (a5 - 6.f * b5 + 15.f * c5);
+  if (s < 2.f) return C * (a5 - 6.f * b5);
+  if (s < 3.f) return C * a5;
+  return 0.f;
+}
+
+// FP32 dW/dr / dist (Derivative_kernel_function, particle.cpp:405-807)
+__device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
+  const float ih = r_rcp(h);
+  const float s = dist * ih;
+  float hD = ih;
+  if (D >= 2) hD *= ih;
+  if (D >= 3) hD *= ih;
+  if (kind == K_WEN) {
+    if (D == 1 || !(s < 2.f)) return 0.f;
+    const float C = (float)(D == 2 ? kern_norm(K_WEN, 2) : kern_norm(K_WEN, 3)) * hD;
+    const float t = 1.f - 0.5f * s;
+    return -5.f * C * (t * t * t) * s * ih * r_rcp(dist + 1.e-15f);
+  }
+  if (kind == K_HYP) {
+    const float C = (float)(D == 1 ? kern_norm(K_HYP, 1) : D == 2 ? kern_norm(K_HYP, 2) : kern_norm(K_HYP, 3)) *
+                    hD * ih;
+    float v = 0.f;
+    if (s < 1.f) v = C * (-6.f + 3.f * s * s);
+    else if (s < 2.f) { const float t = 2.f - s; v = C * -3.f * t * t; }
+    return v * r_rcp(dist + 1.e-20f);
+  }
+  if (kind == K_CUB) {
+    const float C = (float)(D == 1 ? kern_norm(K_CUB, 1) : D == 2 ? kern_norm(K_CUB, 2) : kern_norm(K_CUB, 3)) *
+                    hD * ih;
+    float v = 0.f;
+    if (s < 1.f) v = 3.f * C * (-s + 0.75f * s * s);
+    else if (s < 2.f) { const float t = 2.f - s; v = -0.75f * C * t * t; }
+    return v * r_rcp(dist + 1.e-20f);
+  }
+  if (kind == K_GAU) {
+    const float fac = 0.5f * 2.f / sqrtf((float)PI_REF);
+    float f = fac;
+    if (D > 1) f *= fac;
+    if (D > 2) f *= fac;
+    if (!(s < 3.f)) return 0.f;
+    return -2.f * s * __expf(-s * s) * f * hD * ih * r_rcp(dist + 1.e-15f);
+  }
+  const float C = (float)(D == 1 ? kern_norm(K_QUI, 1) : D == 2 ? kern_norm(K_QUI, 2) : kern_norm(K_QUI, 3)) * hD;
+  const float a = 3.f - s, b = 2.f - s, c = 1.f - s;
+  const float a4 = a * a * a * a, b4 = b * b * b * b, c4 = c * c * c * c;
+  float v;
+  if (s < 1.f) v = C * (-5.f * a4 + 30.f * b4 - 75.f * c4);
+  else if (s < 2.f) v = C * (-5.f * a4 + 30.f * b4);
+  else if (s < 3.f) v = C * (-5.f * a4);
+  else return 0.f;
+  return v * ih * r_rcp(dist + 1.e-15f);
+}
+
+// path dispatch: FP64 keeps the reference arithmetic
+__device__ inline double pair_W(int kind, int D, double dist, double h, double) { return kernel_W<double>(kind, D, dist, h); }
+__device__ inline float pair_W(int kind, int D, float dist, float, float inv_h) { return kernel_W_fast(kind, D, dist, inv_h); }
+__device__ inline double pair_dW(int kind, int D, double dist, double h) { return kernel_dW<double>(kind, D, dist, h); }
+__device__ inline float pair_dW(int kind, int D, float dist, float h) { return kernel_dW_fast(kind, D, dist, h); }
+
 // ---------------------------------------------------------------- level set
 __device__ inline long long ls_index(const LsLevel& L, int D, int gi, int gj, int gk) {
   long long a0 = gi + 4 * L.margin, a1 = gj + 4 * L.margin, a2 = (D == 3) ? gk + 4 * L.margin : 0;

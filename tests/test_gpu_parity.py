@@ -69,8 +69,8 @@ def test_levelset_sampling(name, prec):
     gpu.close()
 
 
-def _gpu_step_taps(case, prec, st):
-    gpu = make_gpu(case, prec)
+def _gpu_step_taps(case, prec, st, cap=0):
+    gpu = make_gpu(case, prec, cap)
     gpu.set_state(oracle_state_to_gpu(st))
     gpu.run_phase(L.PHASE_FORCE2)
     gp = gpu.particles()
@@ -224,3 +224,34 @@ def test_seed_matches_oracle_fp64():
     assert np.max(np.abs(gp["xyz"] - oxyz)) < 1e-12
     assert np.array_equal(gp["type"], o["type"])
     gpu.close()
+
+
+@pytest.mark.parametrize("kernel", ["hyperbolic", "cubic", "wendland", "gaussian", "quintic"])
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_all_kernels_single_step(kernel, dim, prec):
+    """Density sums and both force stages for every smoothing kernel
+    (particle.cpp:31-807), 2D and 3D, from the GPU's own post-map state."""
+    from mrsph import cases
+    if dim == 2:
+        case = cases.disc_hole_2d(spacing=0.02, grid=64, kernel=kernel)
+    else:
+        case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2, kernel=kernel)
+    orc = warm_oracle(case, max_steps=2, need_surface=False)
+    st = orc.get_state()
+    gp, lc, ids, off, nb, stats = _gpu_step_taps(case, prec, st, cap=2048 if dim == 3 else 0)
+    o2 = oracle.Oracle(case)
+    gpu_post_map_to_oracle(o2, gp, st)
+    ooff, onb = o2.neighbors()
+    tol_sum, tol_f = (1e-12, 1e-12) if prec == "fp64" else (1e-5, 1e-4)
+    o2.density(ooff, onb)
+    s = o2.get_state()
+    real = gp["type"] == 0
+    assert rel_err(gp["sum"][real], s["sum"][real]) < tol_sum
+    o2.force(ooff, onb, 1)
+    s1 = o2.get_state()
+    assert rel_err(gp["a1"], np.stack([s1["ax"], s1["ay"], s1["az"]], 1)) < tol_f
+    o2.force(ooff, onb, 2)
+    s2 = o2.get_state()
+    assert rel_err(gp["a2"], np.stack([s2["ax"], s2["ay"], s2["az"]], 1), floor=1e-300) < \
+        (tol_f if prec == "fp64" else 1e-3)
