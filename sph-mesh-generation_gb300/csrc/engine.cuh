@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "engine_iface.h"
@@ -50,12 +51,19 @@ struct Buf {  // persistent per-particle state, one ping-pong half
   typename V4<R>::T* rec;   // packed neighbour-pass record, 2 words per particle
 };
 
+// Neighbour-list layout: column-major inside blocks of 32 particles (one
+// warp), so the lanes of a warp reading their q-th entries touch one 128-byte
+// line and a warp's appends stay inside its own block of cap x 32 entries.
+__host__ __device__ inline long long nb_slot(long long s, int q, int cap) {
+  return (((s >> 5) * cap + q) << 5) + (s & 31);
+}
+
 template <class R>
 struct Work {  // per-step arrays in sorted order
   R* sum;
   typename V4<R>::T* a1;
   int* cnt;
-  int* nbl;  // neighbour lists, one row of `cap` entries per particle
+  int* nbl;  // neighbour lists, entry q < cap of particle s at nbl[nb_slot(s, q, cap)]
   int cap;
   int* counts;
   int* cstart;
@@ -74,6 +82,19 @@ struct KCtx {
 };
 
 enum { MAP_STEP = 0, MAP_PRE = 1 };
+
+// Tuning of the FP32 neighbour passes: resident 256-thread blocks per SM the
+// register allocation must allow, and the unroll of the tile loop.
+#ifndef MRSPH_DENSITY_MIN_BLOCKS
+#define MRSPH_DENSITY_MIN_BLOCKS 6
+#endif
+#ifndef MRSPH_FORCE_MIN_BLOCKS
+#define MRSPH_FORCE_MIN_BLOCKS 4
+#endif
+#ifndef MRSPH_TILE_UNROLL
+#define MRSPH_TILE_UNROLL 1
+#endif
+constexpr int kTileUnroll = MRSPH_TILE_UNROLL;
 
 // ---------------------------------------------------------------------------
 // position representations
@@ -552,9 +573,12 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
 // (levels, rows, storage order), so its accepted neighbours and their order
 // do not depend on the mode; lanes also see extra candidates of the union,
 // which the candidate test rejects.
-template <int D, class T4, class F>
-__device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, const T4* __restrict__ rec,
-                                 bool active, const double* xr, double hi, T4 (*tile)[2], F&& f) {
+// load(k) builds the tile entry of candidate k (uniform mode), vtile(j, e)
+// visits it, vglob(j) visits candidate j straight from global memory
+// (per-lane mode).
+template <int D, class E, class FL, class FT, class FG>
+__device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, bool active, const double* xr,
+                                 double hi, E* tile, FL&& load, FT&& vtile, FG&& vglob) {
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const double hic = hi * c.prm.cutoff;
@@ -625,14 +649,17 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
           const int s0 = __ldg(&cstart[rb + ul]), e0 = __ldg(&cstart[rb + uh + 1]);
           for (int t0 = s0; t0 < e0; t0 += 32) {
             const int k = t0 + lane;
-            if (k < e0) {
-              tile[lane][0] = rec[2 * (long long)k];
-              tile[lane][1] = rec[2 * (long long)k + 1];
-            }
+            if (k < e0) tile[lane] = load(k);
             __syncwarp();
             const int m = min(32, e0 - t0);
-            if (active)
-              for (int t = 0; t < m; t++) f(t0 + t, tile[t][0], tile[t][1]);
+            if (active) {
+              if (m == 32) {
+#pragma unroll kTileUnroll
+                for (int t = 0; t < 32; t++) vtile(t0 + t, tile[t]);
+              } else {
+                for (int t = 0; t < m; t++) vtile(t0 + t, tile[t]);
+              }
+            }
             __syncwarp();
           }
         }
@@ -644,7 +671,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
           if (xl > xh) continue;
           const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
           const int s0 = __ldg(&cstart[rb + xl]), e0 = __ldg(&cstart[rb + xh + 1]);
-          for (int j = s0; j < e0; j++) f(j, rec[2 * (long long)j], rec[2 * (long long)j + 1]);
+          for (int j = s0; j < e0; j++) vglob(j);
         }
     }
   }
@@ -674,14 +701,20 @@ template <class R> __device__ inline R d2_of(const R* dr, int D) {
 
 // A6 + A7: Refresh_neighbor_info (level_infor.cpp:469-506) and
 // Get_kernel_summation (particle_mesh_generation.cpp:690-765).  The
-// neighbour list is written row-major (one row of `cap` entries per
-// particle), in the fixed scan order.
+// neighbour list is written in the fixed scan order.
+template <class R> struct RecPair { typename V4<R>::T a, b; };
+
+
 template <int D, class R>
-__global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DENSITY_MIN_BLOCKS : 1)) k_density(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
-  __shared__ T4 s_tile[8][32][2];
+  constexpr bool F32 = std::is_same<R, float>::value;
+  // FP32 tile entry: position relative to the warp's anchor cell and
+  // (cutoff*h)^2, negative for a SURFACE particle; FP64: the packed record
+  using E = typename std::conditional<F32, float4, RecPair<R>>::type;
+  __shared__ E s_tile[8][32];
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < c.n;
   unsigned long long pairs = 0;
@@ -703,21 +736,18 @@ __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
   const R inv_hi = active ? r_rcp(hi) : (R)0;
   const int kind = c.prm.kernel;
   const R cos_t = (R)c.prm.cos_thres;
+  const R cut = (R)c.prm.cutoff;
   R sum = 0;
   int ncount = 0, cnt = 0;
-  int* row = w.nbl + (active ? i : 0) * (long long)w.cap;
-  warp_scan<D>(c, w.cstart, b.rec, active, xr, (double)hi, s_tile[threadIdx.x >> 5],
-               [&](int j, const T4& b0, const T4& b1) {
-    R dr[3];
-    Q::rel(c, a0, a1, b0, b1, dr);
-    R dist;
-    if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
-    if (cnt < w.cap) row[cnt] = j;
+  int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[q * 32]
+  // accepted neighbour j at distance vector dr (i - j), |dr| = dist
+  auto accept = [&](int j, const R* dr, R dist, bool surf_j) {
+    if (cnt < w.cap) row[cnt * 32] = j;
     cnt++;
     if (ti == REAL_P) {
       sum += pair_W(kind, D, dist, hi, inv_hi);
       ncount++;
-    } else if (ti == SURFACE_P && b1.w < (R)0) {  // surface neighbour of a surface particle
+    } else if (ti == SURFACE_P && surf_j) {  // surface neighbour of a surface particle
       R dn = dot3<D, R>(dr, ni);
       R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
       R pd = pair_dist(dot3<D, R>(pr, pr));
@@ -728,7 +758,54 @@ __global__ void __launch_bounds__(256) k_density(KCtx c, Buf<R> b, Work<R> w) {
         ncount++;
       }
     }
-  });
+  };
+  auto vglob = [&](int j) {
+    const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
+    R dr[3];
+    Q::rel(c, a0, a1, b0, b1, dr);
+    R dist;
+    if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
+    accept(j, dr, dist, b1.w < (R)0);
+  };
+  if constexpr (F32) {
+    // warp anchor: lane 0's anchor cell (lane 0 is active whenever any lane is)
+    const float wa[3] = {__shfl_sync(0xffffffffu, (float)a1.x, 0), __shfl_sync(0xffffffffu, (float)a1.y, 0),
+                         __shfl_sync(0xffffffffu, (float)a1.z, 0)};
+    const float Af[3] = {c.geo.Af[0], c.geo.Af[1], c.geo.Af[2]};
+    const float pi[3] = {((float)a1.x - wa[0]) * Af[0] + (float)a0.x, ((float)a1.y - wa[1]) * Af[1] + (float)a0.y,
+                         D == 3 ? ((float)a1.z - wa[2]) * Af[2] + (float)a0.z : 0.f};
+    const float ri = (float)hi * (float)cut;
+    const float R2i = ri * ri;
+    auto load = [&](int k) {
+      const float4 b0 = b.rec[2 * (long long)k], b1 = b.rec[2 * (long long)k + 1];
+      const float rj = b0.w * (float)cut;
+      const float r2 = rj * rj;
+      return make_float4((b1.x - wa[0]) * Af[0] + b0.x, (b1.y - wa[1]) * Af[1] + b0.y,
+                         D == 3 ? (b1.z - wa[2]) * Af[2] + b0.z : 0.f, b1.w < 0.f ? -r2 : r2);
+    };
+    auto vtile = [&](int j, const float4& e) {
+      float dr[3] = {pi[0] - e.x, pi[1] - e.y, D == 3 ? pi[2] - e.z : 0.f};
+      const float d2 = d2_of(dr, D);
+      if (d2 > fmaxf(R2i, fabsf(e.w))) return;
+      accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
+    };
+    warp_scan<D>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+  } else {
+    auto load = [&](int k) {
+      RecPair<R> e;
+      e.a = b.rec[2 * (long long)k];
+      e.b = b.rec[2 * (long long)k + 1];
+      return e;
+    };
+    auto vtile = [&](int j, const RecPair<R>& e) {
+      R dr[3];
+      Q::rel(c, a0, a1, e.a, e.b, dr);
+      R dist;
+      if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) return;
+      accept(j, dr, dist, e.b.w < (R)0);
+    };
+    warp_scan<D>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+  }
   if (active) {
     if (ncount > 1) sum = (R)1. / (sum + (R)1.e-15);
     w.sum[i] = sum;
@@ -747,7 +824,7 @@ static __global__ void k_accum_pairs(DevScalars* sc) { sc->pairs_total += sc->pa
 // A8 force stages + A9 timestep (Set_timestep(stage), particle_mesh_generation.cpp:127-145).
 // Stage 1 stores (a1, nu) so that stage 2 reads one vector per neighbour.
 template <int D, class R, int STAGE>
-__global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FORCE_MIN_BLOCKS : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
@@ -820,9 +897,9 @@ __global__ void __launch_bounds__(256) k_force(KCtx c, Buf<R> b, Work<R> w) {
     if (ti == REAL_P || ti == SURFACE_P) {
       const int cnt = w.cnt[i];
       if (cnt <= w.cap) {
-        const int* row = w.nbl + i * (long long)w.cap;
+        const int* row = w.nbl + nb_slot(i, 0, w.cap);
         for (int q = 0; q < cnt; q++) {
-          const int j = __ldg(&row[q]);
+          const int j = __ldg(&row[q * 32]);
           const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
           R vec[3];
           Q::rel(c, a0, a1r, b0, b1, vec);
@@ -920,10 +997,10 @@ __global__ void k_export_tri(KCtx c, Buf<R> b, Work<R> w, double* __restrict__ x
   int m = w.cnt[s];
   if (m > w.cap || m > rowcap) { atomicOr(flags, 4u); m = min(w.cap, rowcap); }
   cnt[k] = m;
-  const int* src = w.nbl + (long long)s * w.cap;
+  const int* src = w.nbl + nb_slot(s, 0, w.cap);
   int* dst = rows + k * rowcap;
   for (int q = 0; q < m; q++) {  // insertion sort by id
-    int v = b.id[src[q]];
+    int v = b.id[src[q * 32]];
     int p = q;
     while (p > 0 && dst[p - 1] > v) { dst[p] = dst[p - 1]; p--; }
     dst[p] = v;
@@ -1103,11 +1180,12 @@ class Engine : public EngineBase {
     if ((int)mc <= w_.cap || cfg_.neighbor_cap > 0) return 0;
     long long want = ((long long)mc * 5 / 4 + 31) / 32 * 32;
     const long long budget = 24ll << 30;  // bytes for the list
-    long long maxcap = budget / (4 * n_);
+    const long long n32 = (n_ + 31) / 32 * 32;  // nb_slot blocks of 32 particles
+    long long maxcap = budget / (4 * n32);
     if (want > maxcap) want = maxcap;
     if (want <= w_.cap) return 0;
     int* nb = nullptr;
-    cudaError_t e = cudaMalloc(&nb, sizeof(int) * (size_t)want * n_);
+    cudaError_t e = cudaMalloc(&nb, sizeof(int) * (size_t)want * n32);
     if (e != cudaSuccess) { cudaGetLastError(); return 0; }
     for (auto& p : allocs_)
       if (p == w_.nbl) { cudaFree(p); p = nb; }
@@ -1224,13 +1302,14 @@ class Engine : public EngineBase {
     if (total) *total = tot;
     if (!nb) return 0;
     if (cap < tot || !off) { err = "neighbour buffer too small"; return MRSPH_ERR_ARG; }
-    std::vector<int> nbl((size_t)w_.cap * n_);
-    MR_CK(cudaMemcpy(nbl.data(), w_.nbl, sizeof(int) * (size_t)w_.cap * n_, cudaMemcpyDeviceToHost));
+    const size_t nbl_len = (size_t)w_.cap * ((n_ + 31) / 32 * 32);
+    std::vector<int> nbl(nbl_len);
+    MR_CK(cudaMemcpy(nbl.data(), w_.nbl, sizeof(int) * nbl_len, cudaMemcpyDeviceToHost));
     off[0] = 0;
     for (long long k = 0; k < n_; k++) off[k + 1] = off[k] + byid_cnt[k];
     for (long long s = 0; s < n_; s++) {
       long long base = off[ids[s]];
-      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nbl[(size_t)s * w_.cap + q]];
+      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nbl[nb_slot(s, q, w_.cap)]];
       std::sort(nb + base, nb + base + cnt[s]);
     }
     return 0;
@@ -1451,7 +1530,7 @@ class Engine : public EngineBase {
       rc |= A((void**)&w_.sum, sizeof(R) * n);
       rc |= A((void**)&w_.a1, sizeof(T4) * n);
       rc |= A((void**)&w_.cnt, sizeof(int) * n);
-      rc |= A((void**)&w_.nbl, sizeof(int) * (size_t)cap * n);
+      rc |= A((void**)&w_.nbl, sizeof(int) * (size_t)cap * ((n + 31) / 32 * 32));
       rc |= A((void**)&w_.counts, sizeof(int) * ncells_);
       rc |= A((void**)&w_.cstart, sizeof(int) * (ncells_ + 1));
       rc |= A((void**)&w_.perm, sizeof(int) * n);

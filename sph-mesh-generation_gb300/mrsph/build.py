@@ -50,6 +50,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     headers.append(os.path.join(os.path.dirname(ROOT), "include", "mrsph_relax.h"))
     base = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
             "--expt-relaxed-constexpr", "-I", CSRC]
+    # tuning macros of the neighbour passes (e.g. "-DMRSPH_DENSITY_MIN_BLOCKS=4")
+    base += os.environ.get("MRSPH_NVCC_DEFINES", "").split()
     jobs = []
     objs = []
     for src, extra in SOURCES.items():
