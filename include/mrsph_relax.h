@@ -85,7 +85,7 @@ typedef struct {
   double box_l[3];      /* domain (SPH::box_l, box_r) = level-set level-0 interior box */
   double box_r[3];
   unsigned long long seed; /* Philox4x32-10 key for seeding and re-seeding */
-  int neighbor_cap;     /* neighbour-list capacity per particle; 0 = automatic */
+  int neighbor_cap;     /* neighbour-list capacity per particle (rounded up to a multiple of 8); 0 = automatic */
   int device;           /* CUDA device ordinal */
 } mrsph_params;
 

@@ -51,11 +51,13 @@ struct Buf {  // persistent per-particle state, one ping-pong half
   typename V4<R>::T* rec;   // packed neighbour-pass record, 2 words per particle
 };
 
-// Neighbour-list layout: column-major inside blocks of 32 particles (one
-// warp), so the lanes of a warp reading their q-th entries touch one 128-byte
-// line and a warp's appends stay inside its own block of cap x 32 entries.
+// Neighbour-list layout: blocks of 32 particles (one warp); inside a block,
+// chunks of 8 consecutive entries (one 32-byte sector) per particle,
+// interleaved over the 32 particles.  A particle's appends fill whole sectors
+// in turn (as a row-major list would), and the lanes of a warp reading their
+// q-th entries touch 8 lines instead of 32.  cap is a multiple of 8.
 __host__ __device__ inline long long nb_slot(long long s, int q, int cap) {
-  return (((s >> 5) * cap + q) << 5) + (s & 31);
+  return (((((s >> 5) * (cap >> 3) + (q >> 3)) << 5) + (s & 31)) << 3) + (q & 7);
 }
 
 template <class R>
@@ -739,10 +741,10 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   const R cut = (R)c.prm.cutoff;
   R sum = 0;
   int ncount = 0, cnt = 0;
-  int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[q * 32]
+  int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[(q >> 3) * 256 + (q & 7)]
   // accepted neighbour j at distance vector dr (i - j), |dr| = dist
   auto accept = [&](int j, const R* dr, R dist, bool surf_j) {
-    if (cnt < w.cap) row[cnt * 32] = j;
+    if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = j;
     cnt++;
     if (ti == REAL_P) {
       sum += pair_W(kind, D, dist, hi, inv_hi);
@@ -899,7 +901,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FO
       if (cnt <= w.cap) {
         const int* row = w.nbl + nb_slot(i, 0, w.cap);
         for (int q = 0; q < cnt; q++) {
-          const int j = __ldg(&row[q * 32]);
+          const int j = __ldg(&row[((q >> 3) << 8) + (q & 7)]);
           const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
           R vec[3];
           Q::rel(c, a0, a1r, b0, b1, vec);
@@ -1000,7 +1002,7 @@ __global__ void k_export_tri(KCtx c, Buf<R> b, Work<R> w, double* __restrict__ x
   const int* src = w.nbl + nb_slot(s, 0, w.cap);
   int* dst = rows + k * rowcap;
   for (int q = 0; q < m; q++) {  // insertion sort by id
-    int v = b.id[src[q * 32]];
+    int v = b.id[src[((q >> 3) << 8) + (q & 7)]];
     int p = q;
     while (p > 0 && dst[p - 1] > v) { dst[p] = dst[p - 1]; p--; }
     dst[p] = v;
@@ -1501,7 +1503,7 @@ class Engine : public EngineBase {
     n_ = n;
     kc_.n = n;
     ncells_ = kc_.geo.hoff[kc_.geo.ncl];
-    int cap = cfg_.neighbor_cap > 0 ? cfg_.neighbor_cap : (D == 2 ? 64 : 192);
+    int cap = cfg_.neighbor_cap > 0 ? (cfg_.neighbor_cap + 7) / 8 * 8 : (D == 2 ? 64 : 192);
     w_.cap = cap;
     auto A = [&](void** p, size_t bytes) -> int {
       cudaError_t e = cudaMalloc(p, bytes);
