@@ -1,11 +1,12 @@
 // mrsph_cvp.cu — centroidal Voronoi partitioning of the particles (row A13),
 // Voronoi::Partitioning (CVP/voronoi.cpp:1376-1446) on the GPU.
 //
-// One iteration = five kernels:
+// One iteration = six kernels:
 //   k_cvp_assign    nearest VP per point, strict '<' (Get_CPU_id, voronoi.cpp:480-493)
 //   k_cvp_partials  per (VP, 2048-point chunk) mass, mass centre and energy,
 //                   points in order (voronoi.cpp:617-631)
 //   k_cvp_reduce    per VP: chunk partials in order, centroid, pressure, error
+//   k_cvp_planes    bisector plane of every VP pair
 //   k_cvp_faces     per (VP, plane) the exact Voronoi face inside the box: the
 //                   plane's polygon clipped by every other bisector half-space
 //                   (replaces voro++, voronoi.cpp:724-790)
@@ -92,17 +93,47 @@ __device__ void cplane(const CvpGeo& G, const double* vp, int k, int p, double* 
   }
 }
 
+// Nearest VP, strict '<' on the FP64 distance (lowest index wins a tie).  An
+// FP32 pass finds the smallest FP32 distance first; only VPs within twice the
+// FP32 error bound of it (1e-6 x (coordinate magnitude + distance), several
+// times the bound) are then compared in FP64, in index order.  Every VP whose
+// FP64 distance ties the minimum is among them, so the label is the one the
+// full FP64 scan gives.
 __global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int K, const double* __restrict__ vp,
                              int D, int* __restrict__ label) {
   __shared__ double s_vp[3 * CVP_MAX_K];
+  __shared__ float4 s_vf[CVP_MAX_K];
+  __shared__ float s_lvp;
   for (int t = threadIdx.x; t < 3 * K; t += blockDim.x) s_vp[t] = vp[t];
+  __syncthreads();
+  for (int t = threadIdx.x; t < K; t += blockDim.x)
+    s_vf[t] = make_float4((float)s_vp[3 * t], (float)s_vp[3 * t + 1], (float)s_vp[3 * t + 2], 0.f);
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int t = 0; t < 3 * K; t++) m = fmax(m, fabs(s_vp[t]));
+    s_lvp = (float)m;
+  }
   __syncthreads();
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  const float xf[3] = {(float)x[0], (float)x[1], D == 3 ? (float)x[2] : 0.f};
+  float bf = 3.4e38f;
+  for (int k = 0; k < K; k++) {
+    const float4 v = s_vf[k];
+    const float dx = xf[0] - v.x, dy = xf[1] - v.y, dz = D == 3 ? xf[2] - v.z : 0.f;
+    bf = fminf(bf, dx * dx + dy * dy + dz * dz);
+  }
+  const float L = fmaxf(s_lvp, fmaxf(fabsf(xf[0]), fmaxf(fabsf(xf[1]), fabsf(xf[2]))));
+  const float df = sqrtf(bf);
+  const float thr = df + 2.e-6f * (L + df) + 1.e-30f;
+  const float T = thr * thr * 1.0001f;
   double best = 1.e20;
   int idx = 0;
   for (int k = 0; k < K; k++) {
+    const float4 v = s_vf[k];
+    const float dx = xf[0] - v.x, dy = xf[1] - v.y, dz = D == 3 ? xf[2] - v.z : 0.f;
+    if (dx * dx + dy * dy + dz * dz > T) continue;
     double dd = cdist(D, x, s_vp + 3 * k);
     if (dd < best) { best = dd; idx = k; }
   }
@@ -170,8 +201,38 @@ __global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __res
   err[k] = fabs(m - target) / target;
 }
 
-// face of VP k on plane p; out: exists, area, n (3), dist
-__global__ void k_cvp_faces(CvpGeo G, const double* __restrict__ vp, double* __restrict__ face) {
+// bisector planes of every VP pair, computed once per iteration
+__global__ void k_cvp_planes(CvpGeo G, const double* __restrict__ vp, double* __restrict__ planes) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)G.K * G.K) return;
+  int k = (int)(t / G.K), m = (int)(t % G.K);
+  if (k == m) return;
+  double n[3], d;
+  cplane(G, vp, k, m, n, &d);
+  double* o = planes + 4 * t;
+  o[0] = n[0]; o[1] = n[1]; o[2] = n[2]; o[3] = d;
+}
+
+// bounding sphere of a polygon (centre = vertex mean)
+__device__ inline void cbound(double (*v)[3], int nv, double* C, double* r) {
+  C[0] = C[1] = C[2] = 0.0;
+  for (int a = 0; a < nv; a++)
+    for (int q = 0; q < 3; q++) C[q] += v[a][q];
+  for (int q = 0; q < 3; q++) C[q] /= (double)(nv > 0 ? nv : 1);
+  double r2 = 0.0;
+  for (int a = 0; a < nv; a++) {
+    double e[3] = {v[a][0] - C[0], v[a][1] - C[1], v[a][2] - C[2]};
+    r2 = fmax(r2, cdot(e, e));
+  }
+  *r = sqrt(r2);
+}
+
+// face of VP k on plane p; out: exists, area, n (3), dist.  A clip whose
+// plane lies beyond the polygon's bounding sphere (with a 1e-9 relative
+// margin) would keep every vertex in order, so it is skipped: the result is
+// the one of clipping by every plane in turn.
+__global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __restrict__ vp,
+                                                   const double* __restrict__ planes, double* __restrict__ face) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)G.K * G.NP) return;
   int k = (int)(t / G.NP), p = (int)(t % G.NP);
@@ -179,7 +240,12 @@ __global__ void k_cvp_faces(CvpGeo G, const double* __restrict__ vp, double* __r
   out[0] = 0.0;
   if (p < G.K && p == k) return;
   double n[3], d;
-  cplane(G, vp, k, p, n, &d);
+  if (p < G.K) {
+    const double* pl = planes + 4 * ((long long)k * G.K + p);
+    n[0] = pl[0]; n[1] = pl[1]; n[2] = pl[2]; d = pl[3];
+  } else {
+    cplane(G, vp, k, p, n, &d);
+  }
   double lo[3], hi[3];
   for (int q = 0; q < 3; q++) {
     lo[q] = q < G.dim ? G.box_l[q] : -0.5;
@@ -200,26 +266,36 @@ __global__ void k_cvp_faces(CvpGeo G, const double* __restrict__ vp, double* __r
   double w[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2], n[0] * u[1] - n[1] * u[0]};
   double off = d - cdot(n, c);
   double p0[3] = {c[0] + n[0] * off, c[1] + n[1] * off, c[2] + n[2] * off};
-  double A[CVP_MAXV][3], B[CVP_MAXV][3];
+  double BA[CVP_MAXV][3], BB[CVP_MAXV][3];
+  double (*A)[3] = BA, (*B)[3] = BB;
   const double sg[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
   for (int a = 0; a < 4; a++)
     for (int q = 0; q < 3; q++) A[a][q] = p0[q] + u[q] * (sg[a][0] * S) + w[q] * (sg[a][1] * S);
   int nv = 4;
+  double C[3], r;
+  cbound(A, nv, C, &r);
+  auto clip = [&](const double* cn, double cd) {
+    const double sc = cdot(cn, C) - cd;
+    if (sc + r < -1.e-9 * (fabs(cd) + fabs(cdot(cn, C)) + r + S)) return;  // all vertices inside
+    nv = cclip(A, nv, cn, cd, B);
+    double (*tmp)[3] = A;
+    A = B;
+    B = tmp;
+    cbound(A, nv, C, &r);
+  };
   for (int wq = 0; wq < 6 && nv > 0; wq++) {
     if (p >= G.K && wq == p - G.K) continue;
     int axw = wq / 2, hw = wq % 2;
     double wn[3] = {0, 0, 0};
     wn[axw] = hw ? 1.0 : -1.0;
     double wd = hw ? hi[axw] : -lo[axw];
-    nv = cclip(A, nv, wn, wd, B);
-    for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
+    clip(wn, wd);
   }
+  const double* pk = planes + 4 * (long long)k * G.K;
   for (int m = 0; m < G.K && nv > 0; m++) {
     if (m == k || m == p) continue;
-    double bn[3], bd;
-    cplane(G, vp, k, m, bn, &bd);
-    nv = cclip(A, nv, bn, bd, B);
-    for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
+    const double bn[3] = {pk[4 * m], pk[4 * m + 1], pk[4 * m + 2]};
+    clip(bn, pk[4 * m + 3]);
   }
   if (nv < 3) return;
   double ar = 0.0;
@@ -242,21 +318,22 @@ __global__ void k_cvp_faces(CvpGeo G, const double* __restrict__ vp, double* __r
   out[5] = fabs(cdot(dx, n)) * 2.;
 }
 
-// Sequential VP update, one thread (K is at most 1024).
-__global__ void k_cvp_update(CvpGeo G, double* vp, const double* __restrict__ face, const double* mass,
-                             const double* mc, const double* energy, const double* P, const double* err,
-                             double* f, double* hk, double* shift, CvpState* st, double error_tolerance,
-                             int pressure_step) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// VP update, one block: per-VP work in parallel (thread k handles VPs
+// k, k + blockDim, ...), the order-sensitive scalars (error and energy sums,
+// the two global minima) on thread 0 in VP order, as the reference loops do.
+__global__ void __launch_bounds__(1024) k_cvp_update(CvpGeo G, double* vp, const double* __restrict__ face,
+                                                     const double* mass, const double* mc, const double* energy,
+                                                     const double* P, const double* err, double* f, double* hk,
+                                                     double* shift, CvpState* st, double error_tolerance,
+                                                     int pressure_step) {
+  __shared__ double s_ts[CVP_MAX_K];
+  __shared__ double s_g;
+  __shared__ int s_conv;
   const int K = G.K, D = G.dim, NP = G.NP;
   const int iter = st->iter;
-  double scale_coeff = 0.25 + 1.75 * (1. - cmin((iter - 1) / 500., 1.));
-  double error_max = 0.0, total_energy = 0.0;
-  for (int k = 0; k < K; k++) {
-    error_max = cmax(error_max, err[k]);
-    total_energy += energy[k];
-  }
-  for (int k = 0; k < K; k++) {
+  const double relax = st->relax;  // read by every thread before thread 0 updates it
+  const double scale_coeff = 0.25 + 1.75 * (1. - cmin((iter - 1) / 500., 1.));
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
     double fx = 0.0, fy = 0.0, fz = 0.0, sr = 0.0;
     int nnb = 0;
     for (int p = 0; p < NP; p++) {
@@ -274,18 +351,25 @@ __global__ void k_cvp_update(CvpGeo G, double* vp, const double* __restrict__ fa
     f[3 * k] = fx; f[3 * k + 1] = fy; f[3 * k + 2] = fz;
     hk[k] = scale_coeff * sr / (double)nnb;
   }
-  st->error_record = st->error_record + error_max;
-  if (iter % 40 == 0) {
-    st->error_record /= 40.;
-    if (error_max <= error_tolerance && st->error_record <= error_tolerance) st->converged = 1;
-    st->error_record = 0.;
-  }
-  st->error_max = error_max;
-  st->total_energy = total_energy;
-  const double relax = st->relax;
-  if (st->converged == 0) {
-    double gdt = 1.e20;
+  if (threadIdx.x == 0) {
+    double error_max = 0.0, total_energy = 0.0;
     for (int k = 0; k < K; k++) {
+      error_max = cmax(error_max, err[k]);
+      total_energy += energy[k];
+    }
+    st->error_record = st->error_record + error_max;
+    if (iter % 40 == 0) {
+      st->error_record /= 40.;
+      if (error_max <= error_tolerance && st->error_record <= error_tolerance) st->converged = 1;
+      st->error_record = 0.;
+    }
+    st->error_max = error_max;
+    st->total_energy = total_energy;
+    s_conv = st->converged;
+  }
+  __syncthreads();
+  if (s_conv == 0) {
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
       double inv = 1. / mass[k];
       double acc = 0.0;
       for (int q = 0; q < D; q++) {
@@ -293,11 +377,17 @@ __global__ void k_cvp_update(CvpGeo G, double* vp, const double* __restrict__ fa
         acc += a * a;
       }
       acc = sqrt(acc);
-      double ts = 0.25 * sqrt(hk[k] / (acc + 1.e-20));
-      gdt = cmin(ts, gdt);
+      s_ts[k] = 0.25 * sqrt(hk[k] / (acc + 1.e-20));
     }
-    double gcvt = 1.e20;
-    for (int k = 0; k < K; k++) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double gdt = 1.e20;
+      for (int k = 0; k < K; k++) gdt = cmin(s_ts[k], gdt);
+      s_g = gdt;
+    }
+    __syncthreads();
+    const double gdt = s_g;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
       double inv = 1. / mass[k];
       double fac = gdt * gdt * 0.5 * relax;
       for (int q = 0; q < D; q++) {
@@ -312,18 +402,28 @@ __global__ void k_cvp_update(CvpGeo G, double* vp, const double* __restrict__ fa
       }
       sh = sqrt(sh);
       double sc = cmin(sh, 1. / 32. * hk[k]);
-      gcvt = cmin(sc / (sh + 1.e-20), gcvt);
+      s_ts[k] = sc / (sh + 1.e-20);
     }
-    for (int k = 0; k < K; k++)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double gcvt = 1.e20;
+      for (int k = 0; k < K; k++) gcvt = cmin(s_ts[k], gcvt);
+      s_g = gcvt;
+    }
+    __syncthreads();
+    const double gcvt = s_g;
+    for (int k = threadIdx.x; k < K; k += blockDim.x)
       for (int q = 0; q < D; q++) {
         double v = vp[3 * k + q] + shift[3 * k + q] * (gcvt * (1 - relax));
         vp[3 * k + q] = cmax(G.box_l[q] + 1.e-20, cmin(v, G.box_r[q] - 1.e-20));
       }
   }
-  double r = relax;
-  if (iter % 600 == 0) r = 1.02 * r;
-  st->relax = cmin(r, 0.90);
-  st->iter = iter + 1;
+  if (threadIdx.x == 0) {
+    double r = relax;
+    if (iter % 600 == 0) r = 1.02 * r;
+    st->relax = cmin(r, 0.90);
+    st->iter = iter + 1;
+  }
 }
 
 int cfail(mrsph_handle* h, int code, const std::string& msg) {
@@ -353,7 +453,7 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
   cudaStream_t s = h->stream;
   int rc = 0;
   std::vector<void*> mem;
-  double *d_vp = nullptr, *d_part = nullptr, *d_face = nullptr, *d_k = nullptr, *d_tm = nullptr;
+  double *d_vp = nullptr, *d_part = nullptr, *d_face = nullptr, *d_k = nullptr, *d_tm = nullptr, *d_planes = nullptr;
   int* d_label = nullptr;
   CvpState* d_st = nullptr;
   CvpState hs;
@@ -367,6 +467,7 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
   CV_CK(A((void**)&d_vp, sizeof(double) * 3 * K));
   CV_CK(A((void**)&d_part, sizeof(double) * 5 * K * nchunk));
   CV_CK(A((void**)&d_face, sizeof(double) * 6 * (size_t)K * G.NP));
+  CV_CK(A((void**)&d_planes, sizeof(double) * 4 * (size_t)K * K));
   CV_CK(A((void**)&d_k, sizeof(double) * 12 * K));  // mass, mc(3), energy, P, err, f(3), hk, pad
   CV_CK(A((void**)&d_tm, sizeof(double) * nchunk));
   CV_CK(A((void**)&d_label, sizeof(int) * n));
@@ -388,9 +489,10 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
       dim3 g((K + 63) / 64, (unsigned)nchunk);
       k_cvp_partials<<<g, 64, 0, s>>>(n, d_xyz, d_pm, d_label, K, d_vp, D, d_part);
       k_cvp_reduce<<<(K + 127) / 128, 128, 0, s>>>(nchunk, K, D, d_part, d_st, mass, mc, energy, P, err);
-      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_face);
-      k_cvp_update<<<1, 32, 0, s>>>(G, d_vp, d_face, mass, mc, energy, P, err, f, hk, vp3, d_st,
-                                    p->error_tolerance, p->pressure_step);
+      k_cvp_planes<<<(K * K + 255) / 256, 256, 0, s>>>(G, d_vp, d_planes);
+      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_planes, d_face);
+      k_cvp_update<<<1, (K + 31) / 32 * 32, 0, s>>>(G, d_vp, d_face, mass, mc, energy, P, err, f, hk, vp3, d_st,
+                                                   p->error_tolerance, p->pressure_step);
       CV_CK(cudaGetLastError());
       CV_CK(cudaMemcpyAsync(&hs, d_st, sizeof(hs), cudaMemcpyDeviceToHost, s));
       CV_CK(cudaStreamSynchronize(s));
