@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cvp-vps", type=int, default=256)
     ap.add_argument("--cvp-iters", type=int, default=50)
+    ap.add_argument("--batch-geoms", type=int, default=64, help="star-shaped geometries of the batched run (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=50)
     return ap.parse_args()
 
 
@@ -223,6 +225,57 @@ def run_reference(args, ws, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, dev, dist):
+    """Many independent star-shaped 2D/3D geometries relaxed together (one
+    graph launch per step), against stepping them one at a time in FP32 and
+    in FP64.  All three are timed on steps 2-4 after seeding; the batch also
+    on the batch_steps steps that follow."""
+    from mrsph import BatchRelaxation, SPHMeshGeneration, cases
+    t0 = time.perf_counter()
+    geoms = cases.star_batch(args.batch_geoms)
+    gen_s = time.perf_counter() - t0
+    ntot = sum(c.n_particles for c in geoms)
+    hs = [SPHMeshGeneration(c, precision="fp32", device=dev) for c in geoms]
+    for h in hs:
+        h.Initialize_case()
+    b = BatchRelaxation(hs)
+    b.SPH_run_mesh_generation(1)
+    b.sync()
+    barrier(dist)
+    ms_win = max_over_ranks(b.step_timed(3), dist)
+    ms_long = max_over_ranks(b.step_timed(args.batch_steps), dist)
+    flags = 0
+    for h in hs:
+        flags |= h.stats()["flags"]
+    b.close()
+    for h in hs:
+        h.close()
+    seq = {}
+    for prec in ("fp32", "fp64"):
+        tot = 0.0
+        for c in geoms:
+            g = SPHMeshGeneration(c, precision=prec, device=dev)
+            g.Initialize_case()
+            g.SPH_run_mesh_generation(1)
+            g.sync()
+            tot += g.step_timed(3)
+            g.close()
+        seq[prec] = max_over_ranks(tot, dist)
+    rate = lambda steps, ms: ntot * steps / (ms / 1000.0)
+    return {"geometries": len(geoms), "particles": ntot,
+            "n_range": [min(c.n_particles for c in geoms), max(c.n_particles for c in geoms)],
+            "value": rate(args.batch_steps, ms_long), "unit": "particle-steps/s",
+            "steps": args.batch_steps, "window": "steps 5..%d after seeding" % (4 + args.batch_steps),
+            "steps_2_4": {"batched_fp32": rate(3, ms_win), "one_at_a_time_fp32": rate(3, seq["fp32"]),
+                          "one_at_a_time_fp64": rate(3, seq["fp64"])},
+            "batched_fp32_over_fp64_plain": seq["fp64"] / ms_win,
+            "batched_over_one_at_a_time_fp32": seq["fp32"] / ms_win,
+            "generation_s": gen_s, "device_flags": flags,
+            "workload": "star-shaped bodies, 8-32 radial harmonics, sum of amplitudes <= 0.3, even ids 2D "
+                        "(128^2 level set) and odd 3D (64^3), counts log-uniform 2k-200k, constant spacing, "
+                        "Wendland C2, h = 1.3 dx, FP32-split"}
+
+
 def run_mrsph(args, ws, rank, local, dist):
     import numpy as np
     from mrsph import SPHMeshGeneration
@@ -335,6 +388,8 @@ def run_mrsph(args, ws, rank, local, dist):
                 "ms_per_step": win["fp64"]["ms_per_step"], "window": f"steps 2..{1 + args.fp64_steps} after seeding",
                 "fp32_same_window": win["fp32"]}
 
+    batched = run_batched(args, dev, dist) if args.batch_geoms > 0 else None
+
     if rank != 0:
         return
     cpu = None
@@ -351,7 +406,7 @@ def run_mrsph(args, ws, rank, local, dist):
             "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
             "fp64_plain": fp64,
             "fp32_over_fp64": (fp64["fp32_same_window"]["value"] / fp64["value"]) if fp64 else None,
-            "phase_ms": prof, "cvp": cvp, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "phase_ms": prof, "cvp": cvp, "batched": batched, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": 12 * args.steps, "clocks": clocks, "device_flags": flags}
     print(json.dumps(line), flush=True)
 

@@ -284,6 +284,24 @@ typedef struct {
  * cap >= *ntri.  quality may be NULL.  2D handles only. */
 int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri, mrsph_tri_quality* quality);
 
+/* Batched relaxation of independent geometries (no counterpart in the
+ * reference, which relaxes one geometry per run, SPH_run_mesh_generation,
+ * sph_mesh_generation.cpp:1371-1463).  A batch steps seeded handles of one
+ * device together: one CUDA graph launch per step, whose nodes are the
+ * handles' own step graphs, so each handle's results equal those of stepping
+ * it alone.  Work queued on a handle before mrsph_batch_step completes first;
+ * work queued on it afterwards waits for the batch.  A handle may be stepped
+ * alone between batch calls; it must not be destroyed while in a batch. */
+typedef struct mrsph_batch mrsph_batch;
+int mrsph_batch_create(mrsph_handle* const* handles, int count, mrsph_batch** out);
+int mrsph_batch_destroy(mrsph_batch* b);
+int mrsph_batch_last_error(mrsph_batch* b, char* buf, size_t len);
+/* nsteps steps of every handle (asynchronous; capacity checks every 32 steps). */
+int mrsph_batch_step(mrsph_batch* b, int nsteps);
+/* Same, device-timed with CUDA events on the batch stream (ms for all steps). */
+int mrsph_batch_step_timed(mrsph_batch* b, int nsteps, double* ms);
+int mrsph_batch_sync(mrsph_batch* b);
+
 /* e2e helpers: positions in id order (n x 3), host memory (pinned or not). */
 int mrsph_upload_positions(mrsph_handle* h, const double* xyz);
 int mrsph_download_positions(mrsph_handle* h, double* xyz);

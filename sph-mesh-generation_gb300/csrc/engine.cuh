@@ -1193,8 +1193,7 @@ class Engine : public EngineBase {
       if (p == w_.nbl) { cudaFree(p); p = nb; }
     w_.nbl = nb;
     w_.cap = (int)want;
-    for (int p = 0; p < 2; p++)
-      if (graph_[p]) { cudaGraphExecDestroy(graph_[p]); graph_[p] = nullptr; }
+    drop_graphs();
     return 0;
   }
 
@@ -1211,11 +1210,38 @@ class Engine : public EngineBase {
         if (rc) return rc;
         if (ee != cudaSuccess) { err = cudaGetErrorString(ee); return MRSPH_ERR_CUDA; }
         MR_CK(cudaGraphInstantiate(&graph_[p], g, 0));
-        cudaGraphDestroy(g);
+        gsrc_[p] = g;  // kept for batch graphs
       }
     }
     return 0;
   }
+
+  void drop_graphs() {
+    for (int p = 0; p < 2; p++) {
+      if (graph_[p]) { cudaGraphExecDestroy(graph_[p]); graph_[p] = nullptr; }
+      if (gsrc_[p]) { cudaGraphDestroy(gsrc_[p]); gsrc_[p] = nullptr; }
+    }
+    graph_version_++;
+  }
+
+  int step_graph(int offset, cudaGraph_t* g) override {
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    int rc = build_graphs();
+    if (rc) return rc;
+    *g = gsrc_[cur_ ^ (offset & 1)];
+    return 0;
+  }
+
+  void batch_advanced(int nsteps) override {
+    if (nsteps <= 0) return;
+    cur_ ^= (nsteps & 1);
+    have_work_ = true;
+  }
+
+  int check_capacity() override { return have_work_ ? maybe_grow_cap() : 0; }
+
+  unsigned graph_version() const override { return graph_version_; }
+  int parity() const override { return cur_; }
 
   int stats(mrsph_stats* o) override {
     DevScalars h;
@@ -1552,8 +1578,7 @@ class Engine : public EngineBase {
   }
 
   void release() {
-    for (int p = 0; p < 2; p++)
-      if (graph_[p]) { cudaGraphExecDestroy(graph_[p]); graph_[p] = nullptr; }
+    drop_graphs();
     for (void* p : allocs_) cudaFree(p);
     allocs_.clear();
     n_ = 0;
@@ -1573,6 +1598,8 @@ class Engine : public EngineBase {
   bool have_work_ = false;
   int countdown_ = 0;
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  cudaGraph_t gsrc_[2] = {nullptr, nullptr};
+  unsigned graph_version_ = 0;
   std::vector<void*> allocs_;
 };
 

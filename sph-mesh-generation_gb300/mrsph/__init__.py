@@ -2,6 +2,6 @@
 core of the SPH mesh generator Xiangyu-Hu/SPH-mesh-generation) behind the C
 ABI of include/mrsph_relax.h."""
 from . import cases  # noqa: F401
-from .solver import SPHMeshGeneration  # noqa: F401
+from .solver import BatchRelaxation, SPHMeshGeneration  # noqa: F401
 
-__all__ = ["cases", "SPHMeshGeneration"]
+__all__ = ["cases", "SPHMeshGeneration", "BatchRelaxation"]

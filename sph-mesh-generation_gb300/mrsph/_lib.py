@@ -94,6 +94,12 @@ EXPORTS = {
                           C.c_void_p, C.c_void_p, C.POINTER(CvpResult)], C.c_int),
     "mrsph_triangulate": ([C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(TriQuality)],
                           C.c_int),
+    "mrsph_batch_create": ([C.c_void_p, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+    "mrsph_batch_destroy": ([C.c_void_p], C.c_int),
+    "mrsph_batch_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),
+    "mrsph_batch_step": ([C.c_void_p, C.c_int], C.c_int),
+    "mrsph_batch_step_timed": ([C.c_void_p, C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "mrsph_batch_sync": ([C.c_void_p], C.c_int),
     "mrsph_upload_positions": ([C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_download_positions": ([C.c_void_p, C.c_void_p], C.c_int),
 }

@@ -243,6 +243,82 @@ def torus_3d(dx_min: float = 0.005, dx_max: float = 0.02, kernel: str = "wendlan
     return Case("torus_3d", p, levels, n, steps=steps)
 
 
+def star_shape(dim: int, seed: int, n_target: int, kernel: str = "wendland", h_over_dx: float = 1.3,
+               precision: str = "fp32") -> Case:
+    """A random star-shaped body: r = r0 (1 + sum_k a_k g_k(direction)) with
+    M = 8..32 harmonics, sum |a_k| <= 0.3, phi = r(direction) - |x| (positive
+    inside; not an exact distance away from the surface).  2D: g_k =
+    cos(k theta + phase) on a 128^2 grid; 3D: g_k = sin(pol)^p cos(p az +
+    phase) cos(q pol + phase') on a 64^3 grid (continuous at the poles).
+    Constant spacing chosen so that the spacing integral is about n_target."""
+    rng = np.random.default_rng(seed)
+    M = int(rng.integers(8, 33))
+    a = rng.random(M)
+    a *= 0.3 * (0.5 + 0.5 * rng.random()) / a.sum()
+    ph = rng.uniform(0.0, 2 * np.pi, M)
+    r0 = 1.0
+    if dim == 2:
+        ks = np.arange(1, M + 1)
+
+        def radius(X, Y, Z):
+            th = np.arctan2(Y, X)
+            r = np.ones_like(th)
+            for k, ak, pk in zip(ks, a, ph):
+                r += ak * np.cos(k * th + pk)
+            return r0 * r
+    else:
+        pk_ = rng.integers(1, 7, M)
+        qk_ = rng.integers(0, 7, M)
+        ph2 = rng.uniform(0.0, 2 * np.pi, M)
+
+        def radius(X, Y, Z):
+            az = np.arctan2(Y, X)
+            pol = np.arctan2(np.sqrt(X * X + Y * Y), Z)
+            sp = np.sin(pol)
+            r = np.ones_like(az)
+            for ak, p_, q_, f1, f2 in zip(a, pk_, qk_, ph, ph2):
+                r += ak * sp ** p_ * np.cos(p_ * az + f1) * np.cos(q_ * pol + f2)
+            return r0 * r
+
+    def sdf(X, Y, Z):
+        return radius(X, Y, Z) - np.sqrt(X * X + Y * Y + Z * Z)
+
+    npk = 32 if dim == 2 else 16          # 128^2 / 64^3 interior cells
+    half = 1.5 * r0                        # body within 1.3 r0; one package of clearance
+    dpkg = 2 * half / npk
+    box_l = [-half, -half, -half if dim == 3 else 0.0]
+    box_r = [half, half, half if dim == 3 else 0.0]
+    # volume of the body from sampled directions, for the spacing
+    u = rng.normal(size=(20000, 3))
+    if dim == 2:
+        u[:, 2] = 0.0
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    rr = radius(u[:, 0], u[:, 1], u[:, 2])
+    vol = np.pi * np.mean(rr ** 2) if dim == 2 else 4.0 / 3.0 * np.pi * np.mean(rr ** 3)
+    dx = (vol / n_target) ** (1.0 / dim)
+    p = default_params(dim)
+    cell_ratio = 2.0 * h_over_dx
+    while not cell_levels_consistent(box_l, box_r, dim, dx * cell_ratio, dx * cell_ratio):
+        dx *= 1.001
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=dx, max_dl=dx,
+             cell_ratio=cell_ratio, box_l=box_l, box_r=box_r, seed=seed)
+    num = [npk, npk, npk if dim == 3 else 1]
+    lv = make_level(sdf, dim, box_l, [dpkg, dpkg, dpkg if dim == 3 else 1.0], num)
+    n = particle_count([lv], p)
+    return Case(f"star_{dim}d_{seed}", p, [lv], n, steps=300)
+
+
+def star_batch(count: int = 512, seed: int = 11, n_min: int = 2000, n_max: int = 200000,
+               precision: str = "fp32") -> List[Case]:
+    """count independent star-shaped geometries, even indices 2D and odd 3D,
+    particle counts log-uniform in [n_min, n_max] (about 20M in total for
+    512 geometries)."""
+    rng = np.random.default_rng(seed)
+    targets = np.exp(rng.uniform(np.log(n_min), np.log(n_max), count))
+    return [star_shape(2 if g % 2 == 0 else 3, seed * 100003 + g, int(targets[g]), precision=precision)
+            for g in range(count)]
+
+
 def case_by_name(name: str, **kw) -> Case:
     if name == "disc_hole_2d":
         return disc_hole_2d(**kw)

@@ -281,3 +281,47 @@ class SPHMeshGeneration:
     def download_positions(self, out: np.ndarray):
         L.check(self.lib.mrsph_download_positions(self.h, _ptr(out)), self.h, "mrsph_download_positions")
         return out
+
+
+class BatchRelaxation:
+    """Many independent geometries relaxed together (one CUDA graph launch per
+    step over all handles; mrsph_batch_*).  Each handle's results equal those
+    of stepping it alone."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        self.lib = L.load()
+        arr = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
+        b = C.c_void_p()
+        rc = self.lib.mrsph_batch_create(arr, len(self.solvers), C.byref(b))
+        if rc != 0:
+            raise L.MrsphError(f"mrsph_batch_create failed ({rc})")
+        self.b = b
+
+    def _check(self, rc, what):
+        if rc != 0:
+            buf = C.create_string_buffer(1024)
+            self.lib.mrsph_batch_last_error(self.b, buf, 1024)
+            raise L.MrsphError(f"{what} failed ({rc}): {buf.value.decode(errors='replace')}")
+
+    def SPH_run_mesh_generation(self, nsteps: int = 1):
+        self._check(self.lib.mrsph_batch_step(self.b, int(nsteps)), "mrsph_batch_step")
+
+    def step_timed(self, nsteps: int) -> float:
+        ms = C.c_double(0)
+        self._check(self.lib.mrsph_batch_step_timed(self.b, int(nsteps), C.byref(ms)), "mrsph_batch_step_timed")
+        return ms.value
+
+    def sync(self):
+        self._check(self.lib.mrsph_batch_sync(self.b), "mrsph_batch_sync")
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.mrsph_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
