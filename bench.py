@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cvp-iters", type=int, default=50)
     ap.add_argument("--batch-geoms", type=int, default=64, help="star-shaped geometries of the batched run (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--accuracy-steps", type=int, default=100, help="relaxation steps of the accuracy leg (0: skip)")
     return ap.parse_args()
 
 
@@ -276,6 +277,68 @@ def run_batched(args, dev, dist):
                         "Wendland C2, h = 1.3 dx, FP32-split"}
 
 
+def spacing_stats(xyz, h, h_over_dx, dim):
+    """Nearest-neighbour distance over the target spacing (h / (h/dx))."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+    pts = xyz[:, :dim]
+    d, _ = cKDTree(pts).query(pts, k=2)
+    r = d[:, 1] / (h / h_over_dx)
+    hist, _ = np.histogram(r, bins=40, range=(0.0, 2.0))
+    return {"median": float(np.median(r)), "p05": float(np.percentile(r, 5)), "p95": float(np.percentile(r, 95)),
+            "min_ratio": float(r.min()), "min_distance": float(d[:, 1].min()), "hist": hist.tolist()}
+
+
+def run_accuracy(args, dev):
+    """FP32-split against FP64-plain on the GPU (FP64-plain is held to the FP64
+    oracle at 1e-12 by the parity tests) on torus_3d_small: single-step
+    accelerations from one injected state, and spacing statistics after
+    accuracy_steps steps from the same seed."""
+    import numpy as np
+    from mrsph import SPHMeshGeneration
+    case = workload("torus_3d_small", "fp32")
+    dim = case.params["dim"]
+    hdx = case.params["cell_ratio"] / case.params["cutoff"]
+    # one state after 20 FP64 steps, injected into both paths
+    g = SPHMeshGeneration(case, precision="fp64", device=dev)
+    g.Initialize_case()
+    g.SPH_run_mesh_generation(20)
+    st = g.particles(("xyz", "v", "type", "h", "level", "nu"))
+    s0 = g.stats()
+    g.close()
+    st["dt"] = s0["dt"]
+    st["step"] = s0["step"]
+    acc = {}
+    for prec in ("fp64", "fp32"):
+        g = SPHMeshGeneration(case, precision=prec, device=dev, neighbor_cap=1024)
+        g.set_state(st)
+        g.run_phase(5)
+        acc[prec] = g.particles(("a1", "a2"))
+        g.close()
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+    force = {"stage1_max_rel": rel(acc["fp32"]["a1"], acc["fp64"]["a1"]),
+             "stage2_max_rel": rel(acc["fp32"]["a2"], acc["fp64"]["a2"]),
+             "normalisation": "max |a_fp32 - a_fp64| / max |a_fp64| over particles"}
+    stats = {}
+    for prec in ("fp64", "fp32"):
+        g = SPHMeshGeneration(case, precision=prec, device=dev)
+        g.Initialize_case()
+        g.SPH_run_mesh_generation(args.accuracy_steps)
+        p = g.particles(("xyz", "h"))
+        g.close()
+        stats[prec] = spacing_stats(p["xyz"], p["h"], hdx, dim)
+    dif = {k: abs(stats["fp32"][k] - stats["fp64"][k]) / abs(stats["fp64"][k])
+           for k in ("median", "p05", "p95", "min_distance")}
+    return {"workload": f"torus_3d_small (N={case.n_particles})", "reference": "fp64_plain GPU path",
+            "single_step_force": force, "steps": args.accuracy_steps,
+            "spacing_ratio": {"fp32": {k: v for k, v in stats["fp32"].items() if k != "hist"},
+                              "fp64": {k: v for k, v in stats["fp64"].items() if k != "hist"},
+                              "hist_bins": "40 bins over [0, 2)", "hist_fp32": stats["fp32"]["hist"],
+                              "hist_fp64": stats["fp64"]["hist"]},
+            "fp32_vs_fp64_rel_diff": dif}
+
+
 def run_mrsph(args, ws, rank, local, dist):
     import numpy as np
     from mrsph import SPHMeshGeneration
@@ -389,6 +452,7 @@ def run_mrsph(args, ws, rank, local, dist):
                 "fp32_same_window": win["fp32"]}
 
     batched = run_batched(args, dev, dist) if args.batch_geoms > 0 else None
+    accuracy = run_accuracy(args, dev) if (args.accuracy_steps > 0 and rank == 0) else None
 
     if rank != 0:
         return
@@ -406,7 +470,7 @@ def run_mrsph(args, ws, rank, local, dist):
             "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
             "fp64_plain": fp64,
             "fp32_over_fp64": (fp64["fp32_same_window"]["value"] / fp64["value"]) if fp64 else None,
-            "phase_ms": prof, "cvp": cvp, "batched": batched, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "phase_ms": prof, "cvp": cvp, "batched": batched, "accuracy": accuracy, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": 12 * args.steps, "clocks": clocks, "device_flags": flags}
     print(json.dumps(line), flush=True)
 
