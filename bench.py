@@ -63,6 +63,8 @@ def workload(name: str, precision: str):
         return cases.disc_hole_2d(precision=precision)
     if name == "torus_3d_small":
         return cases.torus_3d(dx_min=0.01, dx_max=0.04, precision=precision)
+    if name == "ellipses_2d":
+        return cases.ellipses_2d(precision=precision)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -396,6 +398,18 @@ def run_mrsph(args, ws, rank, local, dist):
         cvp = {"num_vp": args.cvp_vps, "iterations": cres["iterations"], "seconds": cvp_s,
                "ms_per_iteration": 1000.0 * cvp_s / max(cres["iterations"], 1), "error_max": cres["error_max"],
                "points": n, "timer": "host wall clock around mrsph_cvp (FP64, bit-exact vs the oracle)"}
+    # 2D: neighbour-graph triangulation of the relaxed particles
+    tri = None
+    if dim == 2:
+        gpu.sync()
+        t0 = time.perf_counter()
+        tris, q = gpu.Reconstruct_tris()
+        tri_s = time.perf_counter() - t0
+        tri = {"seconds": tri_s, "timer": "host wall clock around mrsph_triangulate (incl. copies)",
+               "triangles": int(q["ntri"]), "edges": int(q["nedge"]), "deleted_edges": int(q["ndeleted"]),
+               "error_edges": int(q["nerror"]), "min_angle": q["min_angle"], "min_angle_avg": q["min_angle_avg"],
+               "max_aspect": q["max_aspect"], "G_avg": q["G_avg"], "theta_30": q["theta_30"],
+               "total_area": q["total_area"], "angle_hist_4deg": [int(v) for v in q["hist"]]}
     gpu.close()
 
     # e2e through the C ABI with host buffers (pinned when torch is available):
@@ -470,7 +484,7 @@ def run_mrsph(args, ws, rank, local, dist):
             "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
             "fp64_plain": fp64,
             "fp32_over_fp64": (fp64["fp32_same_window"]["value"] / fp64["value"]) if fp64 else None,
-            "phase_ms": prof, "cvp": cvp, "batched": batched, "accuracy": accuracy, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "phase_ms": prof, "cvp": cvp, "triangulation": tri, "batched": batched, "accuracy": accuracy, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": 12 * args.steps, "clocks": clocks, "device_flags": flags}
     print(json.dumps(line), flush=True)
 

@@ -319,6 +319,110 @@ def star_batch(count: int = 512, seed: int = 11, n_min: int = 2000, n_max: int =
             for g in range(count)]
 
 
+def _ellipse_root(r0, z0, z1, g, iters=160):
+    """Bisection for the root s of (r0 z0/(s+r0))^2 + (z1/(s+1))^2 = 1 on
+    [z1 - 1, |(r0 z0, z1)| - 1] (Eberly, "Distance from a point to an
+    ellipse, an ellipsoid, or a hyperellipsoid", 2013), vectorised; stops per
+    point when the midpoint no longer moves."""
+    n0 = r0 * z0
+    s0 = z1 - 1.0
+    s1 = np.where(g < 0, 0.0, np.hypot(n0, z1) - 1.0)
+    s = 0.5 * (s0 + s1)
+    live = np.ones_like(s, dtype=bool)
+    for _ in range(iters):
+        s = np.where(live, 0.5 * (s0 + s1), s)
+        live &= (s != s0) & (s != s1)
+        if not live.any():
+            break
+        gg = (n0 / (s + r0)) ** 2 + (z1 / (s + 1.0)) ** 2 - 1.0
+        s0 = np.where(live & (gg > 0), s, s0)
+        s1 = np.where(live & (gg < 0), s, s1)
+        live &= gg != 0
+    return s
+
+
+def ellipse_distance(px, py, cx, cy, a, b, ang):
+    """Signed distance from points to an ellipse (semi-axes a >= b, rotated by
+    ang about its centre), positive outside: Eberly's robust method in the
+    first quadrant of the ellipse frame."""
+    ca, sa = np.cos(ang), np.sin(ang)
+    dx, dy = px - cx, py - cy
+    y0 = np.abs(ca * dx + sa * dy)
+    y1 = np.abs(-sa * dx + ca * dy)
+    e0, e1 = a, b
+    dist = np.empty_like(y0)
+    m_a = (y1 > 0) & (y0 > 0)
+    z0 = y0[m_a] / e0
+    z1 = y1[m_a] / e1
+    g = z0 * z0 + z1 * z1 - 1.0
+    r0 = (e0 / e1) ** 2
+    sbar = _ellipse_root(r0, z0, z1, g)
+    x0 = r0 * y0[m_a] / (sbar + r0)
+    x1 = y1[m_a] / (sbar + 1.0)
+    dist[m_a] = np.where(g != 0, np.hypot(x0 - y0[m_a], x1 - y1[m_a]), 0.0)
+    m_b = (y1 > 0) & ~(y0 > 0)
+    dist[m_b] = np.abs(y1[m_b] - e1)
+    m_c = ~(y1 > 0)
+    numer0 = e0 * y0[m_c]
+    denom0 = e0 * e0 - e1 * e1
+    inside = numer0 < denom0
+    xde0 = np.where(inside, numer0 / max(denom0, 1e-300), 1.0)
+    d_in = np.hypot(e0 * xde0 - y0[m_c], e1 * np.sqrt(np.maximum(1.0 - xde0 * xde0, 0.0)))
+    dist[m_c] = np.where(inside, d_in, np.abs(y0[m_c] - e0))
+    outside = (y0 / e0) ** 2 + (y1 / e1) ** 2 > 1.0
+    return np.where(outside, dist, -dist)
+
+
+def ellipses_2d(n_ellipses: int = 64, seed: int = 11, dx_min: float = 0.0005, dx_max: float = 0.004,
+                grid: int = 1024, axes=(0.01, 0.05), kernel: str = "wendland", h_over_dx: float = 1.3,
+                precision: str = "fp32", steps: int = 400) -> Case:
+    """Unit square minus non-overlapping random ellipses (semi-axes uniform in
+    `axes`, uniform orientation; rejection of overlapping bounding circles,
+    0.01 apart, and of circles within 0.02 of the square), exact signed
+    distance by Eberly's method; spacing dx_min..dx_max by the reference's
+    tanh law.  grid cells per unit length; the domain adds grid/16 cells (or
+    more, for a consistent cell-list plan) on every side."""
+    rng = np.random.default_rng(seed)
+    el = []
+    tries = 0
+    while len(el) < n_ellipses and tries < 200000:
+        tries += 1
+        a, b = np.sort(rng.uniform(axes[0], axes[1], 2))[::-1]
+        cx, cy = rng.uniform(0.02 + a, 0.98 - a, 2)
+        if all(np.hypot(cx - e[0], cy - e[1]) > a + e[2] + 0.01 for e in el):
+            el.append((cx, cy, a, b, rng.uniform(0.0, np.pi)))
+    p = default_params(2)
+    npkg_unit = grid // 4
+    dpkg = 1.0 / npkg_unit
+    cell_ratio = 2.0 * h_over_dx
+    margin_pkg = max(npkg_unit // 16, 1)
+    while not cell_levels_consistent([-margin_pkg * dpkg] * 2, [1.0 + margin_pkg * dpkg] * 2, 2,
+                                     dx_max * cell_ratio, dx_min * cell_ratio):
+        margin_pkg += 1
+    lo, hi = -margin_pkg * dpkg, 1.0 + margin_pkg * dpkg
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=dx_min, max_dl=dx_max,
+             cell_ratio=cell_ratio, box_l=[lo, lo, 0.0], box_r=[hi, hi, 0.0], seed=seed)
+    window = 0.25
+
+    def sdf(X, Y, Z):
+        phi = np.minimum(np.minimum(X, 1.0 - X), np.minimum(Y, 1.0 - Y))
+        for (cx, cy, a, b, ang) in el:
+            near = (np.abs(X - cx) < a + window) & (np.abs(Y - cy) < a + window)
+            lower = np.hypot(X[near] - cx, Y[near] - cy) - a  # distance to the ellipse >= this
+            cur = phi[near]
+            need = lower < cur
+            d = cur.copy()
+            d[need] = np.minimum(cur[need], ellipse_distance(X[near][need], Y[near][need], cx, cy, a, b, ang))
+            phi[near] = d
+        return phi
+
+    lv = make_level(sdf, 2, [lo, lo, 0.0], [dpkg, dpkg, 1.0], [npkg_unit + 2 * margin_pkg] * 2 + [1])
+    n = particle_count([lv], p)
+    c = Case("ellipses_2d", p, [lv], n, steps=steps)
+    c.extra["ellipses"] = el
+    return c
+
+
 def case_by_name(name: str, **kw) -> Case:
     if name == "disc_hole_2d":
         return disc_hole_2d(**kw)

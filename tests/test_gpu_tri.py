@@ -86,3 +86,18 @@ def test_tri_small_buffer_and_3d_rejected():
     with pytest.raises(MrsphError):
         g3.Reconstruct_tris()
     g3.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_tri_relaxed_ellipses(prec):
+    """Unit square minus 64 random ellipses with feature-adaptive spacing
+    (several cell-list levels), relaxed on the GPU, then triangulated: the
+    triangle list equals the oracle's on the same final positions."""
+    case = cases.ellipses_2d(grid=256, dx_min=0.002, dx_max=0.016)
+    gpu = make_gpu(case, prec, cap=256)
+    gpu.Initialize_case()
+    gpu.SPH_run_mesh_generation(100)
+    tris, q = _compare(gpu, case)
+    assert q["ntri"] > gpu.n
+    assert int(np.sum(q["hist"])) == 3 * q["ntri"]
+    gpu.close()
