@@ -65,6 +65,8 @@ def workload(name: str, precision: str):
         return cases.torus_3d(dx_min=0.01, dx_max=0.04, precision=precision)
     if name == "ellipses_2d":
         return cases.ellipses_2d(precision=precision)
+    if name == "spheres_3d":
+        return cases.spheres_3d(precision=precision)
     raise SystemExit(f"unknown workload {name}")
 
 

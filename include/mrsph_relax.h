@@ -87,6 +87,11 @@ typedef struct {
   unsigned long long seed; /* Philox4x32-10 key for seeding and re-seeding */
   int neighbor_cap;     /* neighbour-list capacity per particle (rounded up to a multiple of 8); 0 = automatic */
   int device;           /* CUDA device ordinal */
+  int scale_law;        /* target spacing: 0 = the reference's tanh law of phi (Levelset::Get_scale,
+                           level_set.cpp:311-351); 1 = curvature law: at the surface from min_dl
+                           (largest |curvature| of the cut cells) to middle_dl (smallest), then the
+                           tanh law of phi up to max_dl */
+  double middle_dl;     /* middle spacing of law 1; <= 0: 5 x the level-0 level-set cell (middel_dl) */
 } mrsph_params;
 
 /* One level of a (possibly nested) level set: packages of 4^D cells covering

@@ -218,6 +218,11 @@ struct orc_ctx {
   double cl_dcell[16][3];
   int cl_ncell[16][3];
   double cl_scale[16];
+  // spacing law: 0 = the reference's active tanh law; 1 = the curvature law
+  // below (max/min |curvature| over CUT cells of all levels, filled from
+  // orc_ls_build results by the caller)
+  int scale_law;
+  double middle_dl, max_curv, min_curv;
 };
 
 struct orc_state {
@@ -484,12 +489,24 @@ int cell_tag(const orc_ctx& c, const double* x) {
   return L.tag[ls_index(L, D, g[0], g[1], g[2])];
 }
 
-// Levelset::Get_scale, level_set.cpp:311-351 (active tanh law)
-inline double get_scale(const orc_ctx& c, int D, double phi) {
+// Levelset::Get_scale, level_set.cpp:311-351.  Law 0: the active tanh law.
+// Law 1 (a law of this build, in the spirit of the commented-out curvature
+// variants of :319-339): at the surface the spacing runs from minimum_dl at
+// the largest |curvature| of the CUT cells to middle_dl at the smallest,
+// q = clamp((max_curv - |curv|) / (max_curv - min_curv + 1e-20), 0, 1),
+// s0 = minimum_dl + q^2 (middle_dl - minimum_dl), and grows with |phi| by the
+// tanh law from s0 to maximum_dl.
+inline double get_scale(const orc_ctx& c, int D, double phi, double curv) {
   double dl0 = ls_dl(c.ls[0], D);
   if (phi > 0. || std::fabs(phi) < dl0) {
     double factor = 2.5;
-    return c.min_dl + std::tanh(factor * std::fabs(phi) / c.max_phi) / std::tanh(factor) * (c.max_dl - c.min_dl);
+    double lo = c.min_dl;
+    if (c.scale_law == 1) {
+      double q = (c.max_curv - std::fabs(curv)) / (c.max_curv - c.min_curv + 1.e-20);
+      q = AMAX1(0., AMIN1(q, 1.));
+      lo = c.min_dl + q * q * (c.middle_dl - c.min_dl);
+    }
+    return lo + std::tanh(factor * std::fabs(phi) / c.max_phi) / std::tanh(factor) * (c.max_dl - lo);
   }
   return c.min_dl;
 }
@@ -497,7 +514,7 @@ inline double get_scale(const orc_ctx& c, int D, double phi) {
 // Particle_mesh_generation::Set_particle_info, particle_mesh_generation.cpp:361-381
 template <int D>
 inline void set_info(const orc_ctx& c, orc_state& s, long long i) {
-  double h_tmp = get_scale(c, D, s.phi[i]);
+  double h_tmp = get_scale(c, D, s.phi[i], s.curv[i]);
   s.h[i] = h_tmp * c.cell_ratio / c.cutoff;
   // pow(h_tmp, DIM): for DIM = 2 the correctly rounded square, h_tmp*h_tmp
   s.vol[i] = (D == 2) ? h_tmp * h_tmp : std::pow(h_tmp, 3.0);
@@ -1067,7 +1084,23 @@ void orc_kernel_W(int kind, int D, long long n, const double* dist, double h, do
 void orc_kernel_dW(int kind, int D, long long n, const double* dist, double h, double* out) {
   for (long long i = 0; i < n; i++) out[i] = kernel_dW(kind, D, dist[i], h);
 }
-double orc_get_scale(const orc_ctx* c, double phi) { return get_scale(*c, c->dim, phi); }
+double orc_get_scale(const orc_ctx* c, double phi, double curv) { return get_scale(*c, c->dim, phi, curv); }
+
+// max / min |curvature| over the CUT cells of one level (Levelset_package::
+// Get_global_scale, lset_package.cpp:765-785); min stays 1e20 without CUT cells
+void orc_ls_curv_range(const orc_ctx* c, int level, double* cmax, double* cmin) {
+  const orc_level& L = c->ls[level];
+  long long ntot = 1;
+  for (int d = 0; d < 3; d++) ntot *= (d < c->dim) ? ls_ncell(L, d) : 1;
+  double mx = 0., mn = 1.e20;
+  for (long long a = 0; a < ntot; a++)
+    if (L.tag[a] == CUT_CELL) {
+      mx = AMAX1(mx, std::fabs(L.curv[a]));
+      mn = AMIN1(mn, std::fabs(L.curv[a]));
+    }
+  *cmax = mx;
+  *cmin = mn;
+}
 
 void orc_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed, uint32_t* out) {
   U4 r = philox(c0, c1, c2, c3, seed);
@@ -1350,11 +1383,18 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
       }
       mass[k] = m;
       energy[k] = e;
-      double inv = 1. / m;  // voronoi.cpp:672-687
-      mc[3 * k] = x * inv;
-      mc[3 * k + 1] = y * inv;
-      mc[3 * k + 2] = (D == 3) ? z * inv : 0.0;
-      Pk[k] = target / m;
+      if (m > 0.) {
+        double inv = 1. / m;  // voronoi.cpp:672-687
+        mc[3 * k] = x * inv;
+        mc[3 * k + 1] = y * inv;
+        mc[3 * k + 2] = (D == 3) ? z * inv : 0.0;
+        Pk[k] = target / m;
+      } else {
+        // a cell without points (the reference divides by its zero mass):
+        // centroid = its position, no pressure; it does not move (below)
+        for (int q = 0; q < 3; q++) mc[3 * k + q] = vp[3 * k + q];
+        Pk[k] = 0.;
+      }
       err[k] = std::fabs(m - target) / target;
     }
     for (int k = 0; k < K; k++) {
@@ -1406,6 +1446,7 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
       double gdt = 1.e20;
       std::vector<double> a(3 * K);
       for (int k = 0; k < K; k++) {
+        if (!(mass[k] > 0.)) continue;  // an empty cell neither moves nor limits the step
         double inv = 1. / mass[k];
         for (int q = 0; q < 3; q++) a[3 * k + q] = f[3 * k + q] * inv;
         double acc = 0.0;
@@ -1428,7 +1469,7 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
         }
         sh = std::sqrt(sh);
         double sc = AMIN1(sh, 1. / 32. * hk[k]);
-        tcvt[k] = sc / (sh + 1.e-20);
+        tcvt[k] = (mass[k] > 0.) ? sc / (sh + 1.e-20) : 1.e20;
         gcvt = AMIN1(tcvt[k], gcvt);
       }
       // Update_position_CVT (voronoi.cpp:901-992)

@@ -47,7 +47,8 @@ class OrcCtx(C.Structure):
                 ("nls", C.c_int), ("ls", C.POINTER(OrcLevel)), ("ncl", C.c_int),
                 ("max_scale", C.c_double), ("min_scale", C.c_double), ("ini_num_cell", C.c_int * 3),
                 ("cl_dcell", (C.c_double * 3) * 16), ("cl_ncell", (C.c_int * 3) * 16),
-                ("cl_scale", C.c_double * 16)]
+                ("cl_scale", C.c_double * 16), ("scale_law", C.c_int), ("middle_dl", C.c_double),
+                ("max_curv", C.c_double), ("min_curv", C.c_double)]
 
 
 _DBL_FIELDS = ["x", "y", "z", "vx", "vy", "vz"]
@@ -95,7 +96,8 @@ def lib():
         L.orc_ls_build.argtypes = [C.POINTER(OrcCtx), C.c_int, C.POINTER(C.c_double)]
         L.orc_kernel_W.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_void_p, C.c_double, C.c_void_p]
         L.orc_kernel_dW.argtypes = L.orc_kernel_W.argtypes
-        L.orc_get_scale.argtypes = [C.POINTER(OrcCtx), C.c_double]
+        L.orc_get_scale.argtypes = [C.POINTER(OrcCtx), C.c_double, C.c_double]
+        L.orc_ls_curv_range.argtypes = [C.POINTER(OrcCtx), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_get_scale.restype = C.c_double
         L.orc_philox.argtypes = [C.c_uint32] * 4 + [C.c_ulonglong, C.c_void_p]
         L.orc_sample.argtypes = [C.POINTER(OrcCtx), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -124,6 +126,16 @@ def lib():
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def middle_dl_of(p: dict, levels) -> float:
+    """middle_dl of the curvature law: the given value, or 5 x the level-0
+    level-set cell (fac_middel_dl = 5, sph_mesh_generation.cpp:271, level_set.cpp:940)."""
+    m = float(p.get("middle_dl", 0.0))
+    if m > 0:
+        return m
+    dim = p["dim"]
+    return 5.0 * min(levels[0].dpkg[d] / 4.0 for d in range(dim))
 
 
 class Oracle:
@@ -180,11 +192,18 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"orc_define_levels failed ({rc})")
         mp = 0.0
+        cmax, cmin = 0.0, 1.e20
         for i in range(len(levels)):
             m = C.c_double(0.0)
             lib().orc_ls_build(C.byref(c), i, C.byref(m))
             mp = max(mp, m.value)
+            a_, b_ = C.c_double(0.0), C.c_double(0.0)
+            lib().orc_ls_curv_range(C.byref(c), i, C.byref(a_), C.byref(b_))
+            cmax, cmin = max(cmax, a_.value), min(cmin, b_.value)
         c.max_phi = mp
+        c.max_curv, c.min_curv = cmax, cmin
+        c.scale_law = int(p.get("scale_law", 0))
+        c.middle_dl = middle_dl_of(p, levels)
         self.state = None
         self.arrays = {}
 
@@ -290,8 +309,8 @@ class Oracle:
         qd["hist"] = list(q.hist)
         return tris[:ntri], qd
 
-    def get_scale(self, phi: float) -> float:
-        return lib().orc_get_scale(C.byref(self.ctx), phi)
+    def get_scale(self, phi: float, curv: float = 0.0) -> float:
+        return lib().orc_get_scale(C.byref(self.ctx), phi, curv)
 
     def levels(self):
         c = self.ctx

@@ -226,8 +226,8 @@ __device__ inline R dot3(const R* a, const R* b) {
 
 // Set_particle_info, particle_mesh_generation.cpp:361-381 (mass = 1)
 template <int D, class R>
-__device__ inline void set_info(const KCtx& c, R phi, R& h, R& rho) {
-  R h_tmp = get_scale<R>(c.ls, phi);
+__device__ inline void set_info(const KCtx& c, R phi, R curv, R& h, R& rho) {
+  R h_tmp = get_scale<R>(c.ls, phi, curv);
   h = h_tmp * (R)c.prm.cell_ratio / (R)c.prm.cutoff;
   R vol = (D == 2) ? h_tmp * h_tmp : (R)pow((double)h_tmp, 3.0);
   rho = (R)1.0 / vol;
@@ -276,7 +276,7 @@ __global__ void k_seed(KCtx c, Buf<R> b, unsigned max_att) {
       x[d] = xd;
     }
     ls_sample<D, R>(c.ls, x, phi, n, curv);
-    set_info<D, R>(c, phi, h, rho);
+    set_info<D, R>(c, phi, curv, h, rho);
     if (phi > h) ok = true;
   }
   if (!ok) atomicOr(&c.sc->flags, (unsigned)FLAG_SEED);
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
     P::world(c, p, key, x);
     R phi, n[3], curv, rho = 0;
     ls_sample<D, R>(c.ls, x, phi, n, curv);  // A2 Get_particle_info
-    if (mode == MAP_PRE) set_info<D, R>(c, phi, h, rho);
+    if (mode == MAP_PRE) set_info<D, R>(c, phi, curv, h, rho);
     // A3 Find_and_map_particle (:408-467) + driver loop (sph_mesh_generation.cpp:1506-1545)
     int tag = ls_tag<D>(c.ls, x);
     R nl = r_sqrt(dot3<D, R>(n, n));
@@ -382,10 +382,10 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
       if (!ok) atomicOr(&c.sc->flags, (unsigned)FLAG_REMAP);
       P::set_world(c, p, key, x);
       type = REAL_P;
-      set_info<D, R>(c, phi, h, rho);
+      set_info<D, R>(c, phi, curv, h, rho);
     }
     // A4 Set_particle_scale (:361-381)
-    if (mode == MAP_STEP) set_info<D, R>(c, phi, h, rho);
+    if (mode == MAP_STEP) set_info<D, R>(c, phi, curv, h, rho);
     // Particle_base::Set_particle_scale, particle.cpp:957-975 (scale = max_scale*2^-e)
     {
       R sc = (R)ldexp(c.geo.max_scale, -e);

@@ -121,6 +121,7 @@ int mrsph_create(const mrsph_params* p, mrsph_handle** out) {
   if (p->kernel < 0 || p->kernel > 4) return fail(nullptr, MRSPH_ERR_ARG, "unknown kernel id");
   if (p->precision != MRSPH_FP64_PLAIN && p->precision != MRSPH_FP32_SPLIT)
     return fail(nullptr, MRSPH_ERR_ARG, "unknown precision mode");
+  if (p->scale_law != 0 && p->scale_law != 1) return fail(nullptr, MRSPH_ERR_ARG, "scale_law must be 0 or 1");
   if (!(p->cutoff > 0) || !(p->cell_ratio > 0) || !(p->min_dl > 0) || !(p->max_dl >= p->min_dl))
     return fail(nullptr, MRSPH_ERR_ARG, "invalid spacing parameters");
   mrsph_handle* h = new mrsph_handle();
@@ -171,9 +172,14 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
   for (void* p : h->ls_allocs) cudaFree(p);
   h->ls_allocs.clear();
   unsigned long long* d_max = nullptr;
-  API_CK(h, cudaMalloc(&d_max, sizeof(unsigned long long)));
+  API_CK(h, cudaMalloc(&d_max, 3 * sizeof(unsigned long long)));  // max phi, max |curv|, min |curv|
   h->ls_allocs.push_back(d_max);
-  API_CK(h, cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), h->stream));
+  {
+    double init_d[3] = {0.0, 0.0, 1.e20};
+    unsigned long long init[3];
+    std::memcpy(init, init_d, sizeof(init));
+    API_CK(h, cudaMemcpy(d_max, init, sizeof(init), cudaMemcpyHostToDevice));
+  }
   LsSet& ls = h->ls;
   std::memset(&ls, 0, sizeof(ls));
   ls.nls = nlevels;
@@ -234,16 +240,21 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
     L.tag = tag;
     L.active = act;
   }
-  unsigned long long mb = 0;
-  API_CK(h, cudaMemcpyAsync(&mb, d_max, sizeof(mb), cudaMemcpyDeviceToHost, h->stream));
+  unsigned long long mb[3] = {0, 0, 0};
+  API_CK(h, cudaMemcpyAsync(mb, d_max, sizeof(mb), cudaMemcpyDeviceToHost, h->stream));
   API_CK(h, cudaStreamSynchronize(h->stream));
-  std::memcpy(&ls.max_phi, &mb, sizeof(double));
+  std::memcpy(&ls.max_phi, &mb[0], sizeof(double));
+  std::memcpy(&ls.max_curv, &mb[1], sizeof(double));
+  std::memcpy(&ls.min_curv, &mb[2], sizeof(double));
   if (!(ls.max_phi > 0)) return fail(h, MRSPH_ERR_ARG, "level set has no positive phi");
   double dl0 = 1.e20;
   for (int d = 0; d < D; d++) dl0 = std::min(ls.lv[0].dcell[d], dl0);
   ls.dl0 = dl0;
   ls.min_dl = h->prm.min_dl;
   ls.max_dl = h->prm.max_dl;
+  ls.law = h->prm.scale_law;
+  // middel_dl = fac_middel_dl * dl of level 0, fac 5 (level_set.cpp:940, sph_mesh_generation.cpp:271)
+  ls.middle_dl = h->prm.middle_dl > 0 ? h->prm.middle_dl : 5.0 * dl0;
   EngineConfig cfg;
   cfg.prm.dim = D;
   cfg.prm.kernel = h->prm.kernel;

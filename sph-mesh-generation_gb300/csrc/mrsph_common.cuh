@@ -32,6 +32,8 @@ struct LsLevel {
 struct LsSet {
   int nls;
   double max_phi, dl0, min_dl, max_dl;
+  int law;                              // 0: tanh law of phi; 1: curvature law
+  double middle_dl, max_curv, min_curv; // curvature law (|curv| range over CUT cells)
   LsLevel lv[MAX_LS];
 };
 
@@ -457,12 +459,23 @@ __device__ inline int ls_tag(const LsSet& ls, const double* x) {
   return L.tag[ls_index(L, D, g[0], g[1], g[2])];
 }
 
-// Levelset::Get_scale, level_set.cpp:311-351 (active tanh law)
+// Levelset::Get_scale, level_set.cpp:311-351.  Law 0: the active tanh law.
+// Law 1 (this build's curvature law): at the surface the spacing runs from
+// minimum_dl at the largest |curvature| of the CUT cells to middle_dl at the
+// smallest, q = clamp((max_curv - |curv|) / (max_curv - min_curv + 1e-20),
+// 0, 1), s0 = minimum_dl + q^2 (middle_dl - minimum_dl), and grows with |phi|
+// by the tanh law from s0 to maximum_dl.
 template <class R>
-__device__ inline R get_scale(const LsSet& ls, R phi) {
+__device__ inline R get_scale(const LsSet& ls, R phi, R curv) {
   if (phi > 0 || r_fabs(phi) < (R)ls.dl0) {
     R factor = (R)2.5;
-    return (R)ls.min_dl + r_tanh(factor * r_fabs(phi) / (R)ls.max_phi) / r_tanh(factor) * ((R)ls.max_dl - (R)ls.min_dl);
+    R lo = (R)ls.min_dl;
+    if (ls.law == 1) {
+      R q = ((R)ls.max_curv - r_fabs(curv)) / ((R)ls.max_curv - (R)ls.min_curv + (R)1.e-20);
+      q = AMAX1((R)0., AMIN1(q, (R)1.));
+      lo = (R)ls.min_dl + q * q * ((R)ls.middle_dl - (R)ls.min_dl);
+    }
+    return lo + r_tanh(factor * r_fabs(phi) / (R)ls.max_phi) / r_tanh(factor) * ((R)ls.max_dl - lo);
   }
   return (R)ls.min_dl;
 }

@@ -181,8 +181,8 @@ __global__ void k_cvp_partials(long long n, const double* __restrict__ xyz, cons
 }
 
 __global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __restrict__ part,
-                             const CvpState* st, double* mass, double* mc, double* energy, double* P,
-                             double* err) {
+                             const CvpState* st, const double* __restrict__ vp, double* mass, double* mc,
+                             double* energy, double* P, double* err) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
   double m = 0.0, x = 0.0, y = 0.0, z = 0.0, e = 0.0;
@@ -192,12 +192,19 @@ __global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __res
   }
   mass[k] = m;
   energy[k] = e;
-  double inv = 1. / m;
-  mc[3 * k] = x * inv;
-  mc[3 * k + 1] = y * inv;
-  mc[3 * k + 2] = (D == 3) ? z * inv : 0.0;
   double target = st->target;
-  P[k] = target / m;
+  if (m > 0.) {
+    double inv = 1. / m;
+    mc[3 * k] = x * inv;
+    mc[3 * k + 1] = y * inv;
+    mc[3 * k + 2] = (D == 3) ? z * inv : 0.0;
+    P[k] = target / m;
+  } else {
+    // a cell without points (the reference divides by its zero mass):
+    // centroid = its position, no pressure; it does not move (k_cvp_update)
+    for (int q = 0; q < 3; q++) mc[3 * k + q] = vp[3 * k + q];
+    P[k] = 0.;
+  }
   err[k] = fabs(m - target) / target;
 }
 
@@ -370,6 +377,10 @@ __global__ void __launch_bounds__(1024) k_cvp_update(CvpGeo G, double* vp, const
   __syncthreads();
   if (s_conv == 0) {
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      if (!(mass[k] > 0.)) {  // an empty cell neither moves nor limits the step
+        s_ts[k] = 1.e20;
+        continue;
+      }
       double inv = 1. / mass[k];
       double acc = 0.0;
       for (int q = 0; q < D; q++) {
@@ -388,10 +399,11 @@ __global__ void __launch_bounds__(1024) k_cvp_update(CvpGeo G, double* vp, const
     __syncthreads();
     const double gdt = s_g;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
-      double inv = 1. / mass[k];
+      const bool full = mass[k] > 0.;
+      double inv = full ? 1. / mass[k] : 0.;
       double fac = gdt * gdt * 0.5 * relax;
       for (int q = 0; q < D; q++) {
-        double a = f[3 * k + q] * inv;
+        double a = full ? f[3 * k + q] * inv : 0.0;
         double v = pressure_step ? vp[3 * k + q] + a * fac : vp[3 * k + q];
         vp[3 * k + q] = cmax(G.box_l[q] + 1.e-20, cmin(v, G.box_r[q] - 1.e-20));
       }
@@ -402,7 +414,7 @@ __global__ void __launch_bounds__(1024) k_cvp_update(CvpGeo G, double* vp, const
       }
       sh = sqrt(sh);
       double sc = cmin(sh, 1. / 32. * hk[k]);
-      s_ts[k] = sc / (sh + 1.e-20);
+      s_ts[k] = full ? sc / (sh + 1.e-20) : 1.e20;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -488,7 +500,7 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
       k_cvp_assign<<<nb, 256, 0, s>>>(n, d_xyz, K, d_vp, D, d_label);
       dim3 g((K + 63) / 64, (unsigned)nchunk);
       k_cvp_partials<<<g, 64, 0, s>>>(n, d_xyz, d_pm, d_label, K, d_vp, D, d_part);
-      k_cvp_reduce<<<(K + 127) / 128, 128, 0, s>>>(nchunk, K, D, d_part, d_st, mass, mc, energy, P, err);
+      k_cvp_reduce<<<(K + 127) / 128, 128, 0, s>>>(nchunk, K, D, d_part, d_st, d_vp, mass, mc, energy, P, err);
       k_cvp_planes<<<(K * K + 255) / 256, 256, 0, s>>>(G, d_vp, d_planes);
       k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_planes, d_face);
       k_cvp_update<<<1, (K + 31) / 32 * 32, 0, s>>>(G, d_vp, d_face, mass, mc, energy, P, err, f, hk, vp3, d_st,

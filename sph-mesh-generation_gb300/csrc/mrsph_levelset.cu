@@ -81,7 +81,7 @@ __global__ void k_ls_tag_curv(LsBuildDesc L, const double* __restrict__ phi, uin
                               double* __restrict__ curv, unsigned long long* __restrict__ max_phi_bits) {
   long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long ntot = (long long)L.n[0] * L.n[1] * L.n[2];
-  double my_max = 0.0;
+  double my_max = 0.0, my_cmax = 0.0, my_cmin = 1.e20;
   if (a < ntot) {
     int ai = (int)(a % L.n[0]);
     int aj = (int)((a / L.n[0]) % L.n[1]);
@@ -149,10 +149,22 @@ __global__ void k_ls_tag_curv(LsBuildDesc L, const double* __restrict__ phi, uin
         double cl = c >= lo ? c : lo;
         cl = cl <= hi ? cl : hi;
         cv = fabs(cl);
+        my_cmax = cv;
+        my_cmin = cv;
       }
     }
     tag[a] = t;
     curv[a] = cv;
+  }
+  // |curvature| range over CUT cells (Get_global_scale, lset_package.cpp:765-785):
+  // non-negative values, so the FP64 bit patterns order like the values
+  for (int o = 16; o > 0; o >>= 1) {
+    my_cmax = fmax(my_cmax, __shfl_xor_sync(0xffffffffu, my_cmax, o));
+    my_cmin = fmin(my_cmin, __shfl_xor_sync(0xffffffffu, my_cmin, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (my_cmax > 0.0) atomicMax(max_phi_bits + 1, (unsigned long long)__double_as_longlong(my_cmax));
+    if (my_cmin < 1.e20) atomicMin(max_phi_bits + 2, (unsigned long long)__double_as_longlong(my_cmin));
   }
   // block max of non-negative values -> global bit atomic
   for (int o = 16; o > 0; o >>= 1) my_max = fmax(my_max, __shfl_xor_sync(0xffffffffu, my_max, o));
@@ -180,7 +192,8 @@ __global__ void k_ls_to32(long long ntot, const double4* __restrict__ g, const d
 }  // namespace
 
 // Builds one level in place: g64 (phi, n), c64, tag, and its float copies.
-// max_phi_bits accumulates the maximum positive interior phi.
+// max_phi_bits[0] accumulates the maximum positive interior phi, [1] and [2]
+// the maximum and minimum |curvature| of CUT cells (FP64 bit patterns).
 cudaError_t ls_build_level(const LsBuildDesc& L, const double* d_phi, double4* g64, double* c64, float4* g32,
                            float* c32, uint8_t* tag, unsigned long long* max_phi_bits, cudaStream_t s) {
   long long ntot = (long long)L.n[0] * L.n[1] * L.n[2];

@@ -25,7 +25,7 @@ class Params(C.Structure):
                 ("cutoff", C.c_double), ("angle_thres", C.c_double), ("nu_coeff", C.c_double),
                 ("damp_coeff", C.c_double), ("min_dl", C.c_double), ("max_dl", C.c_double),
                 ("box_l", C.c_double * 3), ("box_r", C.c_double * 3), ("seed", C.c_ulonglong),
-                ("neighbor_cap", C.c_int), ("device", C.c_int)]
+                ("neighbor_cap", C.c_int), ("device", C.c_int), ("scale_law", C.c_int), ("middle_dl", C.c_double)]
 
 
 class LevelsetLevel(C.Structure):

@@ -68,6 +68,8 @@ def default_params(dim: int) -> dict:
         "box_r": [1.0, 1.0, 1.0],
         "seed": 0,
         "neighbor_cap": 0,
+        "scale_law": 0,      # 0: tanh law of phi (the reference's); 1: curvature law
+        "middle_dl": 0.0,    # law 1; <= 0: 5 x the level-0 level-set cell
     }
 
 
@@ -113,6 +115,49 @@ def scale_law(phi, min_dl, max_dl, max_phi, dl0):
     return np.where((phi > 0) | (np.abs(phi) < dl0), s, min_dl)
 
 
+def curvature_estimate(lv: LevelGrid, dim: int) -> np.ndarray:
+    """|curvature| of phi on the cells next to the interface (0 elsewhere) by
+    the level-set build's difference formulas, clamped to 2 / |cell|; the
+    interface test is a sign change over the 3^D neighbourhood.  Used only to
+    count particles under the curvature law."""
+    ph = lv.phi if dim == 3 else lv.phi[0]
+    dc = [lv.dpkg[d] / 4.0 for d in range(dim)]
+    ax = list(range(dim))[::-1]  # array axis of coordinate d
+    def sh(a, d, k):
+        return np.roll(a, -k, axis=ax[d])
+    g1 = [(8.0 * (sh(ph, d, 1) - sh(ph, d, -1)) - (sh(ph, d, 2) - sh(ph, d, -2))) / dc[d] / 12.0 for d in range(dim)]
+    g2 = [(sh(ph, d, 1) - 2 * ph + sh(ph, d, -1)) / dc[d] / dc[d] for d in range(dim)]
+    def mixed(a, b):
+        return 0.25 * (sh(sh(ph, a, 1), b, 1) - sh(sh(ph, a, -1), b, 1) - sh(sh(ph, a, 1), b, -1)
+                       + sh(sh(ph, a, -1), b, -1)) / dc[a] / dc[b]
+    if dim == 2:
+        px, py = g1
+        pxx, pyy = g2
+        pxy = mixed(0, 1)
+        num = px * px * pyy - 2 * px * py * pxy + py * py * pxx
+        den = (px * px + py * py) ** 1.5
+    else:
+        px, py, pz = g1
+        pxx, pyy, pzz = g2
+        pxy, pxz, pyz = mixed(0, 1), mixed(0, 2), mixed(1, 2)
+        num = (px * px * pyy - 2 * px * py * pxy + py * py * pxx + px * px * pzz - 2 * px * pz * pxz
+               + pz * pz * pxx + py * py * pzz - 2 * py * pz * pyz + pz * pz * pyy)
+        den = (px * px + py * py + pz * pz) ** 1.5
+    with np.errstate(divide="ignore", invalid="ignore"):
+        c = np.where(den > 0, num / den, 0.0)
+    cd = np.sqrt(sum(v * v for v in dc))
+    c = np.abs(np.clip(c, -2.0 / cd, 2.0 / cd))
+    lo = ph.copy()
+    hi = ph.copy()
+    for d in range(dim):
+        for k in (-1, 1):
+            lo = np.minimum(lo, sh(ph, d, k))
+            hi = np.maximum(hi, sh(ph, d, k))
+    cut = (lo < 0) & (hi > 0)
+    out = np.where(cut, c, 0.0)
+    return out.reshape(lv.phi.shape)
+
+
 def particle_count(levels: List[LevelGrid], params: dict) -> int:
     """Target count from the spacing integral over phi > 0 (the reference's
     total_mass = sum vol/scale^D, lset_package.cpp:1283-1397, without the
@@ -130,7 +175,20 @@ def particle_count(levels: List[LevelGrid], params: dict) -> int:
     for d in range(dim):
         dV *= fine.dpkg[d] / 4.0
     dl0 = min(levels[0].dpkg[d] / 4.0 for d in range(dim))
-    sc = scale_law(inner, params["min_dl"], params["max_dl"], mp, dl0)
+    if params.get("scale_law", 0) == 1:
+        cv = curvature_estimate(fine, dim)
+        cv = cv[0][sl[1], sl[0]] if dim == 2 else cv[sl[2], sl[1], sl[0]]
+        cut = cv > 0
+        cmax, cmin = (cv[cut].max(), cv[cut].min()) if cut.any() else (0.0, 1e20)
+        mid = params.get("middle_dl", 0.0)
+        if mid <= 0:
+            mid = 5.0 * dl0
+        q = np.clip((cmax - cv) / (cmax - cmin + 1e-20), 0.0, 1.0)
+        lo = params["min_dl"] + q * q * (mid - params["min_dl"])
+        t = np.tanh(2.5 * np.abs(inner) / mp) / np.tanh(2.5)
+        sc = np.where((inner > 0) | (np.abs(inner) < dl0), lo + t * (params["max_dl"] - lo), params["min_dl"])
+    else:
+        sc = scale_law(inner, params["min_dl"], params["max_dl"], mp, dl0)
     return int(np.sum(np.where(inner > 0, dV / sc ** dim, 0.0)))
 
 
@@ -241,6 +299,50 @@ def torus_3d(dx_min: float = 0.005, dx_max: float = 0.02, kernel: str = "wendlan
         levels.append(lv)
     n = particle_count(levels, p)
     return Case("torus_3d", p, levels, n, steps=steps)
+
+
+def spheres_3d(n_spheres: int = 32, seed: int = 7, dx_min: float = 0.0025, dx_max: float = 0.012,
+               middle_dl: float = 0.004, radii=(0.05, 0.3), fine_pkg: int = 64, nlevels: int = 3,
+               kernel: str = "wendland", h_over_dx: float = 1.3, precision: str = "fp32",
+               steps: int = 500) -> Case:
+    """Union of n_spheres spheres, radii log-uniform in `radii`, centres
+    uniform in [0, 1]^3, phi = max_k (r_k - |x - c_k|), on nested level sets of
+    fine_pkg >> (nlevels - 1) ... fine_pkg packages per axis over the box
+    [-0.45, 1.45]^3 (4 cells per package; finer levels active within 4 cells
+    of the next-coarser level's surface), curvature spacing law (law 1):
+    dx_min at the sharpest interface features, middle_dl at the flattest,
+    growing with phi to dx_max."""
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(np.log(radii[0]), np.log(radii[1]), n_spheres))
+    c = rng.random((n_spheres, 3))
+
+    def sdf(X, Y, Z):
+        out = np.full(X.shape, -1.0e9)
+        for (cx, cy, cz), rk in zip(c, r):
+            np.maximum(out, rk - np.sqrt((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2), out=out)
+        return out
+
+    p = default_params(3)
+    npx0 = fine_pkg >> (nlevels - 1)
+    box_l = [-0.45] * 3
+    box_r = [1.45] * 3
+    dpkg0 = 1.9 / npx0
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=dx_min, max_dl=dx_max,
+             cell_ratio=2.0 * h_over_dx, box_l=box_l, box_r=box_r, seed=seed, scale_law=1, middle_dl=middle_dl)
+    if not cell_levels_consistent(box_l, box_r, 3, dx_max * p["cell_ratio"], dx_min * p["cell_ratio"]):
+        raise ValueError("spheres box gives an inconsistent cell-list level plan")
+    levels = []
+    for l in range(nlevels):
+        f = 1 << l
+        dp = dpkg0 / f
+        lv = make_level(sdf, 3, box_l, [dp, dp, dp], [npx0 * f] * 3)
+        if l > 0:
+            lv.active = nested_active(lv, 4.0 * (dp * 2 / 4.0), 3)
+        levels.append(lv)
+    n = particle_count(levels, p)
+    cs = Case("spheres_3d", p, levels, n, steps=steps)
+    cs.extra["spheres"] = (c, r)
+    return cs
 
 
 def star_shape(dim: int, seed: int, n_target: int, kernel: str = "wendland", h_over_dx: float = 1.3,

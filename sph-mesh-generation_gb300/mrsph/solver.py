@@ -49,6 +49,8 @@ class SPHMeshGeneration:
         prm.seed = p["seed"]
         prm.neighbor_cap = neighbor_cap or p.get("neighbor_cap", 0)
         prm.device = device
+        prm.scale_law = int(p.get("scale_law", 0))
+        prm.middle_dl = float(p.get("middle_dl", 0.0))
         h = C.c_void_p()
         L.check(self.lib.mrsph_create(C.byref(prm), C.byref(h)), None, "mrsph_create")
         self.h = h

@@ -16,6 +16,8 @@ def small_cases():
         "disc2d_hyperbolic": lambda: cases.disc_hole_2d(spacing=0.02, grid=64, kernel="hyperbolic",
                                                         h_over_dx=1.0),
         "torus3d_adaptive": lambda: cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2),
+        "spheres3d_curvature": lambda: cases.spheres_3d(fine_pkg=16, nlevels=2, dx_min=0.015, middle_dl=0.035,
+                                                        dx_max=0.09),
     }
 
 
@@ -66,7 +68,7 @@ def neighbor_sets(off, nb):
 
 def make_gpu(case, precision, cap=0):
     if cap == 0:
-        cap = 64 if case.params["dim"] == 2 else 512  # taps need unspilled lists
+        cap = 64 if case.params["dim"] == 2 else 2048  # taps need unspilled lists
     return SPHMeshGeneration(case, precision=precision, neighbor_cap=cap)
 
 

@@ -68,3 +68,23 @@ def test_cvp_of_relaxed_particles(prec):
     assert np.array_equal(gv, ov)
     assert gm.sum() == len(xyz)
     gpu.close()
+
+
+def test_cvp_disconnected_points_with_empty_cells():
+    """Points on a union of separated spheres: some cells lose all their
+    points.  Labels, VP positions and masses still match the oracle bit for
+    bit, and the partition does not collapse (an empty cell keeps its
+    position instead of dividing by its zero mass)."""
+    case = cases.spheres_3d(fine_pkg=16, nlevels=2, dx_min=0.012, middle_dl=0.03, dx_max=0.08)
+    orc = warm_oracle(case, max_steps=5, need_surface=False)
+    st = orc.get_state()
+    xyz = np.stack([st["x"], st["y"], st["z"]], 1)
+    rng = np.random.default_rng(0)
+    vp = xyz[rng.choice(len(xyz), 64, replace=False)].copy()
+    gpu = SPHMeshGeneration(case, precision="fp64")
+    p = case.params
+    gv, gl, gm, gr = _compare(gpu, 3, p["box_l"], p["box_r"], xyz, vp, 49)
+    assert (gm == 0).any()
+    assert np.isfinite(gv).all()
+    assert gr["error_max"] < 5.0
+    gpu.close()

@@ -211,8 +211,11 @@ def test_multistep_statistics(prec):
     gpu.close()
 
 
-def test_seed_matches_oracle_fp64():
-    case = CASES["disc2d_hyperbolic"]()
+@pytest.mark.parametrize("name", ["disc2d_hyperbolic", "spheres3d_curvature"])
+def test_seed_matches_oracle_fp64(name):
+    """Seeding + pre-run: the acceptance test phi > h runs the spacing law
+    (the curvature law for the spheres), so positions match only if it does."""
+    case = CASES[name]()
     orc = oracle.Oracle(case)
     orc.seed(case.n_particles)
     orc.pre_run()

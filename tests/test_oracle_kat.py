@@ -199,3 +199,37 @@ def test_triangulation_with_full_rows_is_delaunay():
     sep = len(got) - len(want)  # separating 3-cycles add area
     if sep == 0:
         assert abs(q["total_area"] - hull_area) < 1e-12
+
+
+def test_curvature_spacing_law():
+    """Spacing law 1: min_dl at the largest cut-cell |curvature| on the
+    surface, middle_dl at the smallest, max_dl at max phi, monotone in |phi|;
+    below -dl the reference's minimum."""
+    case = cases.spheres_3d(fine_pkg=16, nlevels=2, dx_min=0.015, middle_dl=0.035, dx_max=0.09)
+    orc = oracle.Oracle(case)
+    c = orc.ctx
+    assert c.scale_law == 1 and c.max_curv > c.min_curv > 0
+    assert orc.get_scale(0.0, c.max_curv) == pytest.approx(c.min_dl, rel=1e-12)
+    assert orc.get_scale(0.0, c.min_curv) == pytest.approx(c.middle_dl, rel=1e-12)
+    mid = 0.5 * (c.max_curv + c.min_curv)
+    s_mid = orc.get_scale(0.0, mid)
+    assert s_mid == pytest.approx(c.min_dl + 0.25 * (c.middle_dl - c.min_dl), rel=1e-9)
+    assert orc.get_scale(c.max_phi, mid) == pytest.approx(c.max_dl, rel=1e-12)
+    vals = [orc.get_scale(f * c.max_phi, mid) for f in np.linspace(0, 1, 11)]
+    assert all(b >= a for a, b in zip(vals, vals[1:]))
+    assert orc.get_scale(-1.0, mid) == c.min_dl
+
+
+def test_cvp_empty_cell_does_not_collapse():
+    """Two far-apart clusters and a VP between them that loses its points:
+    the partition stays finite and keeps every point assigned."""
+    rng = np.random.default_rng(2)
+    a = rng.normal(size=(3000, 3)) * 0.03 + [0.2, 0.2, 0.2]
+    b = rng.normal(size=(3000, 3)) * 0.03 + [0.8, 0.8, 0.8]
+    xyz = np.concatenate([a, b])
+    vp = np.array([[0.2, 0.2, 0.2], [0.8, 0.8, 0.8], [0.5, 0.5, 0.5], [0.25, 0.2, 0.2]])
+    v, lab, m, r = oracle.cvp(3, [0, 0, 0], [1, 1, 1], xyz, vp, max_iter=60)
+    assert np.isfinite(v).all()
+    assert m.sum() == len(xyz)
+    assert np.bincount(lab, minlength=4).sum() == len(xyz)
+    assert (m > 0).sum() >= 2  # both clusters keep a cell
