@@ -85,13 +85,16 @@ struct KCtx {
 
 enum { MAP_STEP = 0, MAP_PRE = 1 };
 
-// Tuning of the FP32 neighbour passes: resident 256-thread blocks per SM the
+// Tuning of the FP32 map and neighbour passes: resident 256-thread blocks per SM the
 // register allocation must allow, and the unroll of the tile loop.
 #ifndef MRSPH_DENSITY_MIN_BLOCKS
 #define MRSPH_DENSITY_MIN_BLOCKS 6
 #endif
 #ifndef MRSPH_FORCE_MIN_BLOCKS
 #define MRSPH_FORCE_MIN_BLOCKS 4
+#endif
+#ifndef MRSPH_MAP_MIN_BLOCKS
+#define MRSPH_MAP_MIN_BLOCKS 3
 #endif
 #ifndef MRSPH_TILE_UNROLL
 #define MRSPH_TILE_UNROLL 1
@@ -229,7 +232,9 @@ template <int D, class R>
 __device__ inline void set_info(const KCtx& c, R phi, R curv, R& h, R& rho) {
   R h_tmp = get_scale<R>(c.ls, phi, curv);
   h = h_tmp * (R)c.prm.cell_ratio / (R)c.prm.cutoff;
-  R vol = (D == 2) ? h_tmp * h_tmp : (R)pow((double)h_tmp, 3.0);
+  R vol;
+  if constexpr (std::is_same<R, float>::value) vol = (D == 2) ? h_tmp * h_tmp : h_tmp * h_tmp * h_tmp;
+  else vol = (D == 2) ? h_tmp * h_tmp : pow(h_tmp, 3.0);  // pow(h, DIM) as the reference
   rho = (R)1.0 / vol;
 }
 
@@ -300,7 +305,8 @@ __global__ void k_seed(KCtx c, Buf<R> b, unsigned max_att) {
 // map part of Pre_run (sph_mesh_generation.cpp:1010-1050): no advection,
 // Set_particle_info before Find_and_map.
 template <int D, class R>
-__global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int mode, unsigned max_att) {
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_MAP_MIN_BLOCKS : 1))
+k_map(KCtx c, Buf<R> b, int* counts, int mode, unsigned max_att) {
   using P = PosOps<D, R>;
   __shared__ unsigned long long s_hmax[MAX_CL];
   __shared__ unsigned s_lcount[MAX_CL];
@@ -335,7 +341,7 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
     ls_sample<D, R>(c.ls, x, phi, n, curv);  // A2 Get_particle_info
     if (mode == MAP_PRE) set_info<D, R>(c, phi, curv, h, rho);
     // A3 Find_and_map_particle (:408-467) + driver loop (sph_mesh_generation.cpp:1506-1545)
-    int tag = ls_tag<D>(c.ls, x);
+    int tag = ls_tag<D, R>(c.ls, x);
     R nl = r_sqrt(dot3<D, R>(n, n));
     if (tag == CUT_CELL && (type == REAL_P || type == SURFACE_P)) {
       type = SURFACE_P;
@@ -407,7 +413,7 @@ __global__ void __launch_bounds__(256) k_map(KCtx c, Buf<R> b, int* counts, int 
     P::xrel(c, p, key, xr);
     int hq[3] = {0, 0, 0};
     for (int d = 0; d < D; d++) {
-      double u = floor(xr[d] / c.geo.hs[L][d]);
+      double u = floor(std::is_same<R, float>::value ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d]);
       u = fmax(0.0, fmin(u, (double)(c.geo.hn[L][d] - 1)));
       hq[d] = (int)u;
     }
@@ -513,9 +519,10 @@ __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict_
 // sphere.  Edge rows extend to infinity (keys are clamped into the table).
 // R_L carries a 1e-5 relative pad for the rounding of the keys and of the
 // FP32 row arithmetic; the candidate test itself decides membership.
-template <int D, class F>
+template <int D, class R, class F>
 __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart, const double* xr,
                                        double hi, F&& f) {
+  constexpr bool F32 = std::is_same<R, float>::value;
   const double hic = hi * c.prm.cutoff;
   for (int L = 0; L < c.geo.ncl; L++) {
     if (c.sc->lcount[L] == 0) continue;
@@ -525,7 +532,7 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
     for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
     for (int d = 0; d < D; d++) {
-      double u = xr[d] / c.geo.hs[L][d];
+      double u = F32 ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d];
       u = fmax(-1.0e6, fmin(u, 1.0e9));
       const double fl = floor(u);
       q[d] = (int)fl;
@@ -578,9 +585,10 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
 // load(k) builds the tile entry of candidate k (uniform mode), vtile(j, e)
 // visits it, vglob(j) visits candidate j straight from global memory
 // (per-lane mode).
-template <int D, class E, class FL, class FT, class FG>
+template <int D, class R, class E, class FL, class FT, class FG>
 __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, bool active, const double* xr,
                                  double hi, E* tile, FL&& load, FT&& vtile, FG&& vglob) {
+  constexpr bool F32 = std::is_same<R, float>::value;
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const double hic = hi * c.prm.cutoff;
@@ -595,7 +603,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
     if (D == 2) { lo[2] = 0; up[2] = 0; }
     if (active) {
       for (int d = 0; d < D; d++) {
-        double u = xr[d] / c.geo.hs[L][d];
+        double u = F32 ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d];
         u = fmax(-1.0e6, fmin(u, 1.0e9));
         const double fl = floor(u);
         q[d] = (int)fl;
@@ -791,7 +799,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (d2 > fmaxf(R2i, fabsf(e.w))) return;
       accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
     };
-    warp_scan<D>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   } else {
     auto load = [&](int k) {
       RecPair<R> e;
@@ -806,7 +814,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) return;
       accept(j, dr, dist, e.b.w < (R)0);
     };
-    warp_scan<D>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   }
   if (active) {
     if (ncount > 1) sum = (R)1. / (sum + (R)1.e-15);
@@ -910,7 +918,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FO
       } else {
         double xr[3];
         P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
-        scan_candidates<D>(c, w.cstart, xr, (double)h, [&](int j) {
+        scan_candidates<D, R>(c, w.cstart, xr, (double)h, [&](int j) {
           const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
           R vec[3];
           Q::rel(c, a0, a1r, b0, b1, vec);
@@ -1069,7 +1077,7 @@ __global__ void k_sample_points(KCtx c, long long n, const double* __restrict__ 
   out[6 * i + 2] = nn[1];
   out[6 * i + 3] = nn[2];
   out[6 * i + 4] = curv;
-  out[6 * i + 5] = (double)ls_tag<D>(c.ls, x);
+  out[6 * i + 5] = (double)ls_tag<D, R>(c.ls, x);
 }
 
 // ---------------------------------------------------------------------------

@@ -84,6 +84,7 @@ static int plan_levels(mrsph_handle* h) {
       // exactly, since halving commutes with rounding
       g.hn[l][d] = (d < D) ? 2 * g.n[l][d] : 1;
       g.hs[l][d] = (d < D) ? 0.5 * g.dcell[l][d] : 1.0;
+      g.ihs[l][d] = 1.0 / g.hs[l][d];
       hc *= g.hn[l][d];
     }
     // the engine keys levels by exponent: scale = max_scale * 2^-l (sph.cpp:247-276)
@@ -197,6 +198,8 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
       L.dpkg[d] = in.dpkg[d];
       L.num_pkg[d] = in.num_pkg[d];
       L.dcell[d] = in.dpkg[d] / 4.0;
+      L.inv_dpkg[d] = 1.0 / L.dpkg[d];
+      L.inv_dcell[d] = 1.0 / L.dcell[d];
       L.n[d] = (d < D) ? (in.num_pkg[d] + 2 * in.margin) * 4 : 1;
       if (d < D && in.num_pkg[d] < 1) return fail(h, MRSPH_ERR_ARG, "num_pkg must be positive");
       bd.num_pkg[d] = in.num_pkg[d];

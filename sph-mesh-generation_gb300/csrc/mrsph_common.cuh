@@ -3,6 +3,8 @@
 // functions and level-set sampling.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <type_traits>
 #include <stdint.h>
 
 namespace mrsph {
@@ -20,6 +22,7 @@ enum { RNG_SEED = 1, RNG_REMAP = 2 };
 // One nested level-set level on the device (dense, margins included).
 struct LsLevel {
   double box_l[3], dpkg[3], dcell[3];
+  double inv_dpkg[3], inv_dcell[3];  // FP32-split locates with products instead of divisions
   int num_pkg[3], margin, n[3];
   const double4* g64;  // (phi, nx, ny, nz)
   const double* c64;   // curvature
@@ -49,6 +52,7 @@ struct CellGeo {
   long long off[MAX_CL + 1];
   double A[3];  // anchor cell of the FP32-split position = finest cell
   float Af[3];
+  double ihs[MAX_CL][3];  // 1 / half-cell size (FP32-split keys)
   // sort table: half-size cells (2 per reference cell per axis), row-major per level
   int hn[MAX_CL][3];
   double hs[MAX_CL][3];  // half-cell size = dcell / 2
@@ -359,8 +363,9 @@ __device__ inline long long ls_index(const LsLevel& L, int D, int gi, int gj, in
 
 // Finest nested level whose interior contains x and whose package is active
 // (build extension for a multi-level level set; the reference has one level).
-template <int D>
+template <int D, class R>
 __device__ inline int ls_pick(const LsSet& ls, const double* x) {
+  constexpr bool F32 = std::is_same<R, float>::value;
   for (int l = ls.nls - 1; l >= 1; l--) {
     const LsLevel& L = ls.lv[l];
     int pk[3] = {0, 0, 0};
@@ -369,7 +374,7 @@ __device__ inline int ls_pick(const LsSet& ls, const double* x) {
       double cs = x[d] - L.box_l[d];
       double dom = L.dpkg[d] * L.num_pkg[d];
       if (!(cs >= 0.0 && cs < dom)) { inside = false; break; }
-      pk[d] = (int)floor(cs / L.dpkg[d]);
+      pk[d] = (int)floor(F32 ? cs * L.inv_dpkg[d] : cs / L.dpkg[d]);
       if (pk[d] < 0 || pk[d] >= L.num_pkg[d]) { inside = false; break; }
     }
     if (!inside) continue;
@@ -396,24 +401,26 @@ template <> __device__ inline void ls_fetch<float>(const LsLevel& L, long long a
 }
 
 // Calculate_particle_infor, particle_mesh_generation.cpp:175-265.  Cell
-// location and weights in FP64 (as the reference); accumulation in R.  The
+// location in FP64 (FP64-plain: the reference's divisions; FP32-split:
+// products with the reciprocals), weights and accumulation in R.  The
 // interpolated normal is not renormalised (reference quirk Q1).
 template <int D, class R>
 __device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n, R& curv) {
-  const LsLevel& L = ls.lv[ls_pick<D>(ls, x)];
+  constexpr bool F32 = std::is_same<R, float>::value;
+  const LsLevel& L = ls.lv[ls_pick<D, R>(ls, x)];
   int pos[3] = {0, 0, 0}, im[3] = {0, 0, 0};
-  double w[3] = {0, 0, 0};
+  R w[3] = {0, 0, 0};
   for (int d = 0; d < D; d++) {
     double dom = L.dpkg[d] * L.num_pkg[d];
     double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
-    int p = (int)floor(cs / L.dpkg[d]);
+    int p = (int)floor(F32 ? cs * L.inv_dpkg[d] : cs / L.dpkg[d]);
     p = max(-L.margin, min(p, L.num_pkg[d] + L.margin - 1));
     pos[d] = p;
     double csp = cs - L.dpkg[d] * p;
-    double rr = csp / L.dcell[d] - 0.5;
+    double rr = (F32 ? csp * L.inv_dcell[d] : csp / L.dcell[d]) - 0.5;
     rr = AMAX1(-0.5, AMIN1(rr, 4.0 - 0.5));
     im[d] = (int)floor(rr);
-    w[d] = rr - (double)im[d];
+    w[d] = (R)(rr - (double)im[d]);
   }
   R ph = 0, n0 = 0, n1 = 0, n2 = 0, cv = 0;
 #pragma unroll
@@ -425,8 +432,8 @@ __device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n,
         int gi = pos[0] * 4 + im[0] + r, gj = pos[1] * 4 + im[1] + s;
         int gk = (D == 3) ? pos[2] * 4 + im[2] + t : 0;
         long long a = ls_index(L, D, gi, gj, gk);
-        double cf = fabs(w[0] - (1.0 - r)) * fabs(w[1] - (1.0 - s)) * ((D == 3) ? fabs(w[2] - (1.0 - t)) : 1.0);
-        R coef = (R)cf;
+        R coef = r_fabs(w[0] - (R)(1.0 - r)) * r_fabs(w[1] - (R)(1.0 - s)) *
+                 ((D == 3) ? r_fabs(w[2] - (R)(1.0 - t)) : (R)1.0);
         R p_, x_, y_, z_, c_;
         ls_fetch<R>(L, a, p_, x_, y_, z_, c_);
         ph += p_ * coef;
@@ -442,17 +449,18 @@ __device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n,
 
 // Get_level_set_char_cell_tag_and_idx (particle_mesh_generation.cpp:552-573)
 // via Get_id_pkg_cell (lset_level_infor.cpp:350-366).
-template <int D>
+template <int D, class R>
 __device__ inline int ls_tag(const LsSet& ls, const double* x) {
-  const LsLevel& L = ls.lv[ls_pick<D>(ls, x)];
+  constexpr bool F32 = std::is_same<R, float>::value;
+  const LsLevel& L = ls.lv[ls_pick<D, R>(ls, x)];
   int g[3] = {0, 0, 0};
   for (int d = 0; d < D; d++) {
     double dom = L.dpkg[d] * L.num_pkg[d];
     double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
-    int p = (int)floor(cs / L.dpkg[d]);
+    int p = (int)floor(F32 ? cs * L.inv_dpkg[d] : cs / L.dpkg[d]);
     p = max(-L.margin, min(p, L.num_pkg[d] + L.margin - 1));
     double csp = cs - L.dpkg[d] * p;
-    int ci = (int)floor(csp / L.dcell[d]);
+    int ci = (int)floor(F32 ? csp * L.inv_dcell[d] : csp / L.dcell[d]);
     ci = max(0, min(ci, 3));
     g[d] = p * 4 + ci;
   }
