@@ -68,6 +68,7 @@ struct Work {  // per-step arrays in sorted order
   int* nbl;  // neighbour lists, entry q < cap of particle s at nbl[nb_slot(s, q, cap)]
   int cap;
   int* counts;
+  unsigned* lhmax;  // [level][level-0 cell]: largest h (FP32 bits, rounded up) this step, 0 if none
   int* cstart;
   int* perm;
   int* perm2;
@@ -306,7 +307,7 @@ __global__ void k_seed(KCtx c, Buf<R> b, unsigned max_att) {
 // Set_particle_info before Find_and_map.
 template <int D, class R>
 __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_MAP_MIN_BLOCKS : 1))
-k_map(KCtx c, Buf<R> b, int* counts, int mode, unsigned max_att) {
+k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att) {
   using P = PosOps<D, R>;
   __shared__ unsigned long long s_hmax[MAX_CL];
   __shared__ unsigned s_lcount[MAX_CL];
@@ -419,6 +420,14 @@ k_map(KCtx c, Buf<R> b, int* counts, int mode, unsigned max_att) {
     }
     int ck = (int)(c.geo.hoff[L] + ((long long)hq[2] * c.geo.hn[L][1] + hq[1]) * c.geo.hn[L][0] + hq[0]);
     atomicAdd(&counts[ck], 1);
+    {  // local h maximum of level L in the particle's level-0 cell
+      long long c0 = 0;
+      for (int d = D - 1; d >= 0; d--) {
+        int q0 = (int)fmax(0.0, fmin(floor(xr[d] * c.geo.idc0[d]), (double)(c.geo.n[0][d] - 1)));
+        c0 = c0 * c.geo.n[0][d] + q0;
+      }
+      atomicMax(&lhmax[L * c.geo.nc0 + c0], __float_as_uint(__double2float_ru((double)h)));
+    }
     atomicMax(&s_hmax[L], dbits((double)h));
     atomicAdd(&s_lcount[L], 1u);
     p.w = h;
@@ -507,6 +516,28 @@ __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict_
   slot_of_id[id] = (int)s;
 }
 
+// Largest h of level-L particles in the level-0 cells overlapping
+// [x - R, x + R] (0: none).  R is the level-wide bound, so every level-L
+// particle that can pair with x lies in one of these cells and its h is at
+// most the value returned; the candidate search then uses this local bound.
+template <int D>
+__device__ inline float level_hmax_near(const KCtx& c, const unsigned* __restrict__ lhmax, int L, const double* xr,
+                                        double R) {
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    const double top = (double)(c.geo.n[0][d] - 1);
+    lo[d] = (int)fmax(0.0, fmin(floor((xr[d] - R) * c.geo.idc0[d]), top));
+    hi[d] = (int)fmax(0.0, fmin(floor((xr[d] + R) * c.geo.idc0[d]), top));
+  }
+  const unsigned* o = lhmax + (long long)L * c.geo.nc0;
+  unsigned m = 0;
+  for (int z = lo[2]; z <= hi[2]; z++)
+    for (int y = lo[1]; y <= hi[1]; y++)
+      for (int x = lo[0]; x <= hi[0]; x++)
+        m = max(m, __ldg(&o[((long long)z * c.geo.n[0][1] + y) * c.geo.n[0][0] + x]));
+  return __uint_as_float(m);
+}
+
 // Candidates of particle i over all cell-list levels.  The reference walks
 // the 3^D cells of i's level, whose lists hold the particles of that level and
 // of every finer one, and links i and j when r <= 2 h_i or r <= 2 h_j
@@ -520,13 +551,16 @@ __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict_
 // R_L carries a 1e-5 relative pad for the rounding of the keys and of the
 // FP32 row arithmetic; the candidate test itself decides membership.
 template <int D, class R, class F>
-__device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart, const double* xr,
-                                       double hi, F&& f) {
+__device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart,
+                                       const unsigned* __restrict__ lhmax, const double* xr, double hi, F&& f) {
   constexpr bool F32 = std::is_same<R, float>::value;
   const double hic = hi * c.prm.cutoff;
   for (int L = 0; L < c.geo.ncl; L++) {
     if (c.sc->lcount[L] == 0) continue;
-    const double Rw = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
+    const double Rg = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
+    const float hloc = level_hmax_near<D>(c, lhmax, L, xr, Rg * (1.0 + 1.e-5));
+    if (!(hloc > 0.f)) continue;
+    const double Rw = fmax(hic, (double)hloc * c.prm.cutoff) + 1.e-10;
     const float R = (float)(Rw * (1.0 + 1.e-5));
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {0, 0, 0}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
@@ -586,22 +620,27 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
 // visits it, vglob(j) visits candidate j straight from global memory
 // (per-lane mode).
 template <int D, class R, class E, class FL, class FT, class FG>
-__device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, bool active, const double* xr,
-                                 double hi, E* tile, FL&& load, FT&& vtile, FG&& vglob) {
+__device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, const unsigned* __restrict__ lhmax,
+                                 bool active, const double* xr, double hi, E* tile, FL&& load, FT&& vtile,
+                                 FG&& vglob) {
   constexpr bool F32 = std::is_same<R, float>::value;
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const double hic = hi * c.prm.cutoff;
   for (int L = 0; L < c.geo.ncl; L++) {
     if (c.sc->lcount[L] == 0) continue;
-    const double Rw = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
+    const double Rg = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
+    const float hloc = active ? level_hmax_near<D>(c, lhmax, L, xr, Rg * (1.0 + 1.e-5)) : 0.f;
+    const bool need = hloc > 0.f;
+    if (!__any_sync(FULL, need)) continue;
+    const double Rw = fmax(hic, (double)hloc * c.prm.cutoff) + 1.e-10;
     const float R = (float)(Rw * (1.0 + 1.e-5));
     const float R2 = R * R;
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {-1, -1, -1}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
     for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
     if (D == 2) { lo[2] = 0; up[2] = 0; }
-    if (active) {
+    if (need) {
       for (int d = 0; d < D; d++) {
         double u = F32 ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d];
         u = fmax(-1.0e6, fmin(u, 1.0e9));
@@ -618,7 +657,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
     auto row_range = [&](int z, int y, int& xl, int& xh) {
       xl = 0x7fffffff;
       xh = -1;
-      if (!active || z < lo[2] || z > up[2] || y < lo[1] || y > up[1]) return;
+      if (!need || z < lo[2] || z > up[2] || y < lo[1] || y > up[1]) return;
       float gz = 0.f;
       if (D == 3) {
         const int m = z - q[2];
@@ -642,13 +681,13 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
     const int BIG = 0x3fffffff;
     bool uni = true;
     for (int d = 0; d < D; d++) {
-      const int qmin = __reduce_min_sync(FULL, active ? q[d] : BIG);
-      const int qmax = __reduce_max_sync(FULL, active ? q[d] : -BIG);
+      const int qmin = __reduce_min_sync(FULL, need ? q[d] : BIG);
+      const int qmax = __reduce_max_sync(FULL, need ? q[d] : -BIG);
       uni = uni && (qmax - qmin <= (d == 0 ? 3 : 1));
     }
     if (uni) {
-      const int zl = __reduce_min_sync(FULL, active ? lo[2] : BIG), zu = __reduce_max_sync(FULL, active ? up[2] : -BIG);
-      const int yl = __reduce_min_sync(FULL, active ? lo[1] : BIG), yu = __reduce_max_sync(FULL, active ? up[1] : -BIG);
+      const int zl = __reduce_min_sync(FULL, need ? lo[2] : BIG), zu = __reduce_max_sync(FULL, need ? up[2] : -BIG);
+      const int yl = __reduce_min_sync(FULL, need ? lo[1] : BIG), yu = __reduce_max_sync(FULL, need ? up[1] : -BIG);
       for (int z = zl; z <= zu; z++)
         for (int y = yl; y <= yu; y++) {
           int xl, xh;
@@ -662,7 +701,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
             if (k < e0) tile[lane] = load(k);
             __syncwarp();
             const int m = min(32, e0 - t0);
-            if (active) {
+            if (need) {
               if (m == 32) {
 #pragma unroll kTileUnroll
                 for (int t = 0; t < 32; t++) vtile(t0 + t, tile[t]);
@@ -673,7 +712,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
             __syncwarp();
           }
         }
-    } else if (active) {
+    } else if (need) {
       for (int z = lo[2]; z <= up[2]; z++)
         for (int y = lo[1]; y <= up[1]; y++) {
           int xl, xh;
@@ -799,7 +838,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (d2 > fmaxf(R2i, fabsf(e.w))) return;
       accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
     };
-    warp_scan<D, R>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R>(c, w.cstart, w.lhmax, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   } else {
     auto load = [&](int k) {
       RecPair<R> e;
@@ -814,7 +853,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) return;
       accept(j, dr, dist, e.b.w < (R)0);
     };
-    warp_scan<D, R>(c, w.cstart, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R>(c, w.cstart, w.lhmax, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   }
   if (active) {
     if (ncount > 1) sum = (R)1. / (sum + (R)1.e-15);
@@ -918,7 +957,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FO
       } else {
         double xr[3];
         P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
-        scan_candidates<D, R>(c, w.cstart, xr, (double)h, [&](int j) {
+        scan_candidates<D, R>(c, w.cstart, w.lhmax, xr, (double)h, [&](int j) {
           const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
           R vec[3];
           Q::rel(c, a0, a1r, b0, b1, vec);
@@ -1434,7 +1473,8 @@ class Engine : public EngineBase {
   // map (mode) + counting sort + reorder; swaps cur_.
   int run_map_and_bin(int mode) {
     const long long n = n_;
-    k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, mode, 1000000u);
+    MR_CK(cudaMemsetAsync(w_.lhmax, 0, sizeof(unsigned) * kc_.geo.nc0 * kc_.geo.ncl, st_));
+    k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, w_.lhmax, mode, 1000000u);
     MR_CK(cudaGetLastError());
     return bin(1);
   }
@@ -1456,7 +1496,8 @@ class Engine : public EngineBase {
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st_); };
     mark(0);
     k_begin_step<<<1, 1, 0, st_>>>(kc_.sc, 1);
-    k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, MAP_STEP, 1000000u);
+    MR_CK(cudaMemsetAsync(w_.lhmax, 0, sizeof(unsigned) * kc_.geo.nc0 * kc_.geo.ncl, st_));
+    k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, w_.lhmax, MAP_STEP, 1000000u);
     MR_CK(cudaGetLastError());
     mark(1);
     if (phase < MRSPH_PHASE_BIN) return 0;
@@ -1568,6 +1609,7 @@ class Engine : public EngineBase {
       rc |= A((void**)&w_.cnt, sizeof(int) * n);
       rc |= A((void**)&w_.nbl, sizeof(int) * (size_t)cap * ((n + 31) / 32 * 32));
       rc |= A((void**)&w_.counts, sizeof(int) * ncells_);
+      rc |= A((void**)&w_.lhmax, sizeof(unsigned) * kc_.geo.nc0 * kc_.geo.ncl);
       rc |= A((void**)&w_.cstart, sizeof(int) * (ncells_ + 1));
       rc |= A((void**)&w_.perm, sizeof(int) * n);
       rc |= A((void**)&w_.perm2, sizeof(int) * n);

@@ -97,10 +97,12 @@ static int plan_levels(mrsph_handle* h) {
   }
   g.off[num_level] = off;
   g.hoff[num_level] = hoff;
+  g.nc0 = (long long)g.n[0][0] * g.n[0][1] * g.n[0][2];
   if (hoff > (1ll << 28)) return fail(h, MRSPH_ERR_RANGE, "more than 2^25 (3D) / 2^26 (2D) cell-list cells");
   const int lm = num_level - 1;
   for (int d = 0; d < 3; d++) {
     g.A[d] = g.dcell[lm][d];
+    g.idc0[d] = 1.0 / g.dcell[0][d];
     g.Af[d] = (float)g.A[d];
   }
   if (p.precision == MRSPH_FP32_SPLIT) {

@@ -53,6 +53,8 @@ struct CellGeo {
   double A[3];  // anchor cell of the FP32-split position = finest cell
   float Af[3];
   double ihs[MAX_CL][3];  // 1 / half-cell size (FP32-split keys)
+  double idc0[3];         // 1 / level-0 cell size (local h maxima)
+  long long nc0;          // level-0 cells
   // sort table: half-size cells (2 per reference cell per axis), row-major per level
   int hn[MAX_CL][3];
   double hs[MAX_CL][3];  // half-cell size = dcell / 2
