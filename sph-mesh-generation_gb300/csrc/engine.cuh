@@ -1500,7 +1500,10 @@ class Engine : public EngineBase {
     k_map<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_.counts, w_.lhmax, MAP_STEP, 1000000u);
     MR_CK(cudaGetLastError());
     mark(1);
-    if (phase < MRSPH_PHASE_BIN) return 0;
+    if (phase < MRSPH_PHASE_BIN) {  // the histogram is not consumed by a scatter: clear it
+      MR_CK(cudaMemsetAsync(w_.counts, 0, sizeof(int) * ncells_, st_));
+      return 0;
+    }
     cell_scan(w_.counts, w_.cstart, w_.blocksums, ncells_, (int)n, st_);
     mark(2);
     cell_scatter(buf_[cur_].cellkey, w_.counts, w_.cstart, w_.perm, n, st_);

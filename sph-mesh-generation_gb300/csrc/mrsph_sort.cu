@@ -113,7 +113,7 @@ __global__ void k_scatter(const int* __restrict__ cellkey, int* cursor, const in
   if (i >= n) return;
   int c = cellkey[i];
   int slot = cstart[c] + atomicSub(&cursor[c], 1) - 1;
-  perm[slot] = (int)i;
+  if (slot >= 0 && slot < n) perm[slot] = (int)i;  // a histogram out of step with the keys cannot write outside
 }
 
 // Canonical order inside a cell: ascending particle id.

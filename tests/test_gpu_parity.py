@@ -258,3 +258,25 @@ def test_all_kernels_single_step(kernel, dim, prec):
     s2 = o2.get_state()
     assert rel_err(gp["a2"], np.stack([s2["ax"], s2["ay"], s2["az"]], 1), floor=1e-300) < \
         (tol_f if prec == "fp64" else 1e-3)
+
+
+def test_map_only_phases_then_steps():
+    """mrsph_run_phase(MAP) stops before the sort: the next steps still bin
+    every particle once (storage order a permutation, symmetric neighbour
+    sets, no device flags)."""
+    case = CASES["disc2d_wendland"]()
+    gpu = make_gpu(case, "fp64")
+    gpu.Initialize_case()
+    gpu.run_phase(L.PHASE_MAP)
+    gpu.run_phase(L.PHASE_MAP)
+    gpu.SPH_run_mesh_generation(3)
+    gpu.sync()
+    lc, ids = gpu.cells()
+    assert np.array_equal(np.sort(ids), np.arange(gpu.n))
+    off, nb = gpu.neighbors()
+    sets = neighbor_sets(off, nb)
+    for i in range(0, gpu.n, 5):
+        for j in sets[i]:
+            assert i in sets[j]
+    assert gpu.stats()["flags"] & ~L.FLAG_NEIGHBOR_SPILL == 0
+    gpu.close()
