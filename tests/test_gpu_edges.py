@@ -1,0 +1,79 @@
+"""Edge cases of the relaxation engine on the GPU: spilled neighbour lists
+(the force passes re-scan), a single particle, an empty request, particles
+placed outside the domain box."""
+import numpy as np
+import pytest
+
+from mrsph import SPHMeshGeneration, cases
+from mrsph._lib import MrsphError
+from paritylib import make_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_spilled_lists_match_unspilled(prec):
+    """A capacity far below the neighbour count makes every force pass
+    re-scan the cells; it visits the same neighbours in the same order, so
+    the trajectory is bit-identical to one with room for every list."""
+    case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    out = []
+    for cap in (16, 4096):
+        g = SPHMeshGeneration(case, precision=prec, neighbor_cap=cap)
+        g.Initialize_case()
+        g.SPH_run_mesh_generation(6)
+        out.append(g.particles(("xyz", "h", "a1", "a2")))
+        s = g.stats()
+        g.close()
+    assert s["flags"] == 0
+    for k in ("xyz", "h", "a1", "a2"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_single_particle(dim):
+    case = cases.disc_hole_2d(spacing=0.02, grid=64) if dim == 2 else \
+        cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    g = make_gpu(case, "fp64")
+    g.Initialize_case(1)
+    g.SPH_run_mesh_generation(3)
+    p = g.particles(("xyz", "a1"))
+    s = g.stats()
+    assert s["n"] == 1 and s["step"] == 3 and s["pairs"] == 0
+    assert np.isfinite(p["xyz"]).all()
+    assert np.all(p["a1"] == 0.0)
+    g.close()
+
+
+def test_empty_and_oversized_requests_rejected():
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    g = make_gpu(case, "fp64")
+    with pytest.raises(MrsphError):
+        g.Initialize_case(0)
+    with pytest.raises(MrsphError):
+        g.Initialize_case(1 << 31)
+    g.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_particles_outside_the_box(prec):
+    """Positions outside the domain box are binned into the edge cells (the
+    reference clamps get_cell_id); the step runs and the REAL ones outside
+    the body are re-seeded inside."""
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    g = make_gpu(case, prec)
+    rng = np.random.default_rng(4)
+    n = 400
+    xyz = np.zeros((n, 3))
+    xyz[:, :2] = rng.uniform(0.05, 0.95, (n, 2))
+    xyz[:10, 0] = -0.5      # left of the box
+    xyz[10:20, 1] = 1.5     # above the box
+    g.set_state({"xyz": xyz, "h": np.full(n, 0.026), "type": np.zeros(n, dtype=np.int32)})
+    g.SPH_run_mesh_generation(2)
+    p = g.particles(("xyz", "type"))
+    s = g.stats()
+    assert np.isfinite(p["xyz"]).all()
+    lo, hi = np.array(case.params["box_l"][:2]), np.array(case.params["box_r"][:2])
+    assert np.all(p["xyz"][:20, :2] >= lo) and np.all(p["xyz"][:20, :2] <= hi)
+    assert s["flags"] & 1 == 0  # no re-seed loop ran out of attempts
+    g.close()
