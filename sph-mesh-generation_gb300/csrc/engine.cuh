@@ -66,6 +66,7 @@ struct Work {  // per-step arrays in sorted order
   typename V4<R>::T* a1;
   int* cnt;
   int* nbl;  // neighbour lists, entry q < cap of particle s at nbl[nb_slot(s, q, cap)]
+  R* pc;     // stage-1 pair coefficients aw * (1/rho_i^2 + 1/rho_j^2), 0 for a skipped pair; nbl's layout
   int cap;
   int* counts;
   unsigned* lhmax;  // [level][level-0 cell]: largest h (FP32 bits, rounded up) this step, 0 if none
@@ -92,7 +93,14 @@ enum { MAP_STEP = 0, MAP_PRE = 1 };
 #define MRSPH_DENSITY_MIN_BLOCKS 6
 #endif
 #ifndef MRSPH_FORCE_MIN_BLOCKS
-#define MRSPH_FORCE_MIN_BLOCKS 4
+#define MRSPH_FORCE_MIN_BLOCKS 5
+#endif
+#ifndef MRSPH_FORCE2_MIN_BLOCKS
+#define MRSPH_FORCE2_MIN_BLOCKS 6
+#endif
+// list entries (indices, pair coefficients) moved per vector access in the force passes: 1 or 4
+#ifndef MRSPH_FORCE_VEC
+#define MRSPH_FORCE_VEC 4
 #endif
 #ifndef MRSPH_MAP_MIN_BLOCKS
 #define MRSPH_MAP_MIN_BLOCKS 3
@@ -870,10 +878,33 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
 
 static __global__ void k_accum_pairs(DevScalars* sc) { sc->pairs_total += sc->pairs; }
 
+// four consecutive pair coefficients (16-byte aligned)
+__device__ inline void store4(float* p, const float* v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ inline void store4(double* p, const double* v) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+__device__ inline void load4(const float* p, float* v) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ inline void load4(const double* p, double* v) {
+  const double2 t0 = __ldg(reinterpret_cast<const double2*>(p)), t1 = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
+}
+
 // A8 force stages + A9 timestep (Set_timestep(stage), particle_mesh_generation.cpp:127-145).
-// Stage 1 stores (a1, nu) so that stage 2 reads one vector per neighbour.
+// Stage 1 evaluates each pair's kernel gradient aw and stores, in the
+// neighbour list's layout, the pair coefficient c_ij = aw * (1/rho_i^2 +
+// 1/rho_j^2) (0 for a pair the forces skip), and per particle (a1, eta),
+// eta = nu * rho, negated for a SURFACE particle.  The stage-2 viscous term
+// of a pair is c_ij * eta_ij * (v_i - v_j) (:1021-1049), so stage 2 reads the
+// coefficient and one vector per neighbour; a particle whose list spilled
+// re-scans its cells and recomputes c_ij in both stages.
 template <int D, class R, int STAGE>
-__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FORCE_MIN_BLOCKS : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE == 1 ? MRSPH_FORCE_MIN_BLOCKS : MRSPH_FORCE2_MIN_BLOCKS) : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
@@ -891,24 +922,26 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FO
     const R rho = r_fabs(a1r.w), h = a0.w;
     const R cos_t = (R)c.prm.cos_thres;
     const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
-    R nu = 0;
+    R nu = 0, eta_i = 0;
     R hdt1 = 0;
     R vi[3] = {0, 0, 0};
     if (STAGE == 2) {
       hdt1 = (R)(0.5 * bitsd(c.sc->dt1));
       T4 an = w.a1[i];
       vi[0] = an.x * hdt1; vi[1] = an.y * hdt1; vi[2] = an.z * hdt1;
-      nu = an.w;
+      eta_i = r_fabs(an.w);
     } else {
       nu = b.nu[i];
     }
     R F[3] = {0, 0, 0};
     const R vol_i = (R)1.0 / (rho * rho);
-    auto pair = [&](int j, const T4& b0, const T4& b1, const R* vec) {
-      if (j == (int)i) return;
+    // pair (i, j) at relative position vec: the skip rules of :1019-1031 and
+    // :904-920, the direction dr the force acts along and the coefficient
+    auto coef = [&](int j, const T4& b0, const T4& b1, const R* vec, R* dr, R& cij) -> bool {
+      if (j == (int)i) return false;
       const bool surf_j = b1.w < (R)0;
-      if (ti == SURFACE_P && !surf_j) return;
-      R dr[3], aw;
+      if (ti == SURFACE_P && !surf_j) return false;
+      R aw;
       const R hij = (R)0.5 * (h + b0.w);
       if (ti == REAL_P) {
         dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
@@ -920,49 +953,94 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FO
         R dist = pair_dist(dot3<D, R>(dr, dr));
         const T4 nrj = b.nr[j];
         const R nj[3] = {nrj.x, nrj.y, nrj.z};
-        if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return;
+        if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return false;
         aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
       }
       const R rho_j = r_fabs(b1.w);
+      const R vol_ij = vol_i + r_rcp(rho_j * rho_j);
       if (STAGE == 1) {
-        const R vol_j = r_rcp(rho_j * rho_j);
-        const R P_ij = sum * (vol_i + vol_j);
+        const R P_ij = sum * vol_ij;
         for (int d = 0; d < D; d++) F[d] = F[d] + (dr[d] * aw) * -P_ij;
-      } else {
-        const T4 anj = w.a1[j];
-        R vj[3];
-        if (ti == REAL_P && surf_j) {
-          vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
-        } else {
-          vj[0] = anj.x * hdt1; vj[1] = anj.y * hdt1; vj[2] = anj.z * hdt1;
-        }
-        const R nu_j = anj.w;
-        const R eta_i = nu * rho, eta_j = nu_j * rho_j;
-        const R eta_ij = r_div((R)2. * eta_j * eta_i, eta_i + eta_j + (R)1.e-15);
-        const R temp0 = aw * eta_ij * (inv_sq(rho) + inv_sq(rho_j));
-        for (int d = 0; d < D; d++) F[d] = F[d] + (vi[d] - vj[d]) * temp0;
       }
+      cij = aw * vol_ij;
+      return true;
+    };
+    auto visc = [&](int j, R cij) {
+      const T4 anj = w.a1[j];
+      const bool surf_j = signbit(anj.w);
+      R vj[3];
+      if (ti == REAL_P && surf_j) {
+        vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
+      } else {
+        vj[0] = anj.x * hdt1; vj[1] = anj.y * hdt1; vj[2] = anj.z * hdt1;
+      }
+      const R eta_j = r_fabs(anj.w);
+      const R eta_ij = r_div((R)2. * eta_j * eta_i, eta_i + eta_j + (R)1.e-15);
+      const R temp0 = cij * eta_ij;
+      for (int d = 0; d < D; d++) F[d] = F[d] + (vi[d] - vj[d]) * temp0;
     };
     if (ti == REAL_P || ti == SURFACE_P) {
       const int cnt = w.cnt[i];
       if (cnt <= w.cap) {
-        const int* row = w.nbl + nb_slot(i, 0, w.cap);
-        for (int q = 0; q < cnt; q++) {
-          const int j = __ldg(&row[((q >> 3) << 8) + (q & 7)]);
-          const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
-          R vec[3];
-          Q::rel(c, a0, a1r, b0, b1, vec);
-          pair(j, b0, b1, vec);
+        const long long base = nb_slot(i, 0, w.cap);
+        const int* row = w.nbl + base;
+        R* crow = w.pc + base;
+        if (MRSPH_FORCE_VEC == 4) {
+          // four entries per access: q0 is a multiple of 4, so row + o and
+          // crow + o are 16-byte aligned; entries past cnt inside the group
+          // lie within the particle's cap and are ignored (stage 1 stores 0)
+          for (int q0 = 0; q0 < cnt; q0 += 4) {
+            const int o = ((q0 >> 3) << 8) + (q0 & 7);
+            const int4 j4 = __ldg(reinterpret_cast<const int4*>(row + o));
+            const int jj[4] = {j4.x, j4.y, j4.z, j4.w};
+            R cc[4];
+            if (STAGE == 1) {
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                cc[k] = 0;
+                if (q0 + k < cnt) {
+                  const int j = jj[k];
+                  const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
+                  R vec[3], dr[3];
+                  Q::rel(c, a0, a1r, b0, b1, vec);
+                  coef(j, b0, b1, vec, dr, cc[k]);
+                }
+              }
+              store4(crow + o, cc);
+            } else {
+              load4(crow + o, cc);
+#pragma unroll
+              for (int k = 0; k < 4; k++)
+                if (q0 + k < cnt && cc[k] != (R)0) visc(jj[k], cc[k]);
+            }
+          }
+        } else {
+          for (int q = 0; q < cnt; q++) {
+            const int o = ((q >> 3) << 8) + (q & 7);
+            if (STAGE == 1) {
+              const int j = __ldg(&row[o]);
+              const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
+              R vec[3], dr[3], cij = 0;
+              Q::rel(c, a0, a1r, b0, b1, vec);
+              coef(j, b0, b1, vec, dr, cij);
+              crow[o] = cij;
+            } else {
+              const R cij = __ldg(&crow[o]);
+              if (cij == (R)0) continue;
+              visc(__ldg(&row[o]), cij);
+            }
+          }
         }
       } else {
         double xr[3];
         P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
         scan_candidates<D, R>(c, w.cstart, w.lhmax, xr, (double)h, [&](int j) {
           const T4 b0 = b.rec[2 * (long long)j], b1 = b.rec[2 * (long long)j + 1];
-          R vec[3];
+          R vec[3], dr[3], cij = 0;
           Q::rel(c, a0, a1r, b0, b1, vec);
           R dist;
-          if (nb_test(d2_of(vec, D), h, b0.w, c.prm.cutoff, dist)) pair(j, b0, b1, vec);
+          if (!nb_test(d2_of(vec, D), h, b0.w, c.prm.cutoff, dist)) return;
+          if (coef(j, b0, b1, vec, dr, cij) && STAGE == 2 && cij != (R)0) visc(j, cij);
         });
       }
     }
@@ -987,7 +1065,8 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_FO
       b.v1[i] = mk4<R>(vi[0], vi[1], vi[2], U);
       b.a2[i] = mk4<R>(a[0], a[1], a[2], 0);
     } else {
-      w.a1[i] = mk4<R>(a[0], a[1], a[2], nu);
+      const R eta = nu * rho;
+      w.a1[i] = mk4<R>(a[0], a[1], a[2], ti == SURFACE_P ? -eta : eta);
     }
     my_dt = (double)ts;
     my_v = (double)U;
@@ -1228,17 +1307,25 @@ class Engine : public EngineBase {
     MR_CK(cudaStreamSynchronize(st_));
     if ((int)mc <= w_.cap || cfg_.neighbor_cap > 0) return 0;
     long long want = ((long long)mc * 5 / 4 + 31) / 32 * 32;
-    const long long budget = 24ll << 30;  // bytes for the list
+    const long long budget = 48ll << 30;  // bytes for the lists and their pair coefficients
     const long long n32 = (n_ + 31) / 32 * 32;  // nb_slot blocks of 32 particles
-    long long maxcap = budget / (4 * n32);
+    long long maxcap = budget / ((long long)(sizeof(int) + sizeof(R)) * n32) / 8 * 8;
     if (want > maxcap) want = maxcap;
     if (want <= w_.cap) return 0;
     int* nb = nullptr;
+    R* pc = nullptr;
     cudaError_t e = cudaMalloc(&nb, sizeof(int) * (size_t)want * n32);
+    if (e == cudaSuccess) {
+      e = cudaMalloc(&pc, sizeof(R) * (size_t)want * n32);
+      if (e != cudaSuccess) cudaFree(nb);
+    }
     if (e != cudaSuccess) { cudaGetLastError(); return 0; }
-    for (auto& p : allocs_)
+    for (auto& p : allocs_) {
       if (p == w_.nbl) { cudaFree(p); p = nb; }
+      else if (p == w_.pc) { cudaFree(p); p = pc; }
+    }
     w_.nbl = nb;
+    w_.pc = pc;
     w_.cap = (int)want;
     drop_graphs();
     return 0;
@@ -1611,6 +1698,7 @@ class Engine : public EngineBase {
       rc |= A((void**)&w_.a1, sizeof(T4) * n);
       rc |= A((void**)&w_.cnt, sizeof(int) * n);
       rc |= A((void**)&w_.nbl, sizeof(int) * (size_t)cap * ((n + 31) / 32 * 32));
+      rc |= A((void**)&w_.pc, sizeof(R) * (size_t)cap * ((n + 31) / 32 * 32));
       rc |= A((void**)&w_.counts, sizeof(int) * ncells_);
       rc |= A((void**)&w_.lhmax, sizeof(unsigned) * kc_.geo.nc0 * kc_.geo.ncl);
       rc |= A((void**)&w_.cstart, sizeof(int) * (ncells_ + 1));
