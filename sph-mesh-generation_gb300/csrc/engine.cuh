@@ -762,7 +762,8 @@ template <class R> __device__ inline R d2_of(const R* dr, int D) {
 template <class R> struct RecPair { typename V4<R>::T a, b; };
 
 
-template <int D, class R>
+// KK: the kernel kind fixed at compile time (FP32 Wendland C2), or -1
+template <int D, class R, int KK>
 __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DENSITY_MIN_BLOCKS : 1)) k_density(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
@@ -791,19 +792,30 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   }
   const R hi = a0.w;
   const R inv_hi = active ? r_rcp(hi) : (R)0;
-  const int kind = c.prm.kernel;
+  const int kind = KK >= 0 ? KK : c.prm.kernel;
+  // FP32 Wendland C2: a REAL particle sums (1 - s/2)^4 (1 + 2s), s = r/h,
+  // clamped at s = 2, and applies the normalisation C/h^D once at the end
+  constexpr bool WEN32 = F32 && KK == K_WEN;
   const R cos_t = (R)c.prm.cos_thres;
   const R cut = (R)c.prm.cutoff;
   R sum = 0;
   int ncount = 0, cnt = 0;
   int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[(q >> 3) * 256 + (q & 7)]
+  int o = 0;  // offset of entry cnt
   // accepted neighbour j at distance vector dr (i - j), |dr| = dist
   auto accept = [&](int j, const R* dr, R dist, bool surf_j) {
-    if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = j;
+    if (cnt < w.cap) row[o] = j;
+    o += ((o & 7) == 7) ? 249 : 1;
     cnt++;
     if (ti == REAL_P) {
-      sum += pair_W(kind, D, dist, hi, inv_hi);
-      ncount++;
+      if constexpr (WEN32) {
+        const float s = (float)dist * (float)inv_hi;
+        const float t = fmaxf(fmaf(-0.5f, s, 1.f), 0.f), t2 = t * t;
+        sum += (t2 * t2) * fmaf(2.f, s, 1.f);
+      } else {
+        sum += pair_W(kind, D, dist, hi, inv_hi);
+        ncount++;
+      }
     } else if (ti == SURFACE_P && surf_j) {  // surface neighbour of a surface particle
       R dn = dot3<D, R>(dr, ni);
       R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
@@ -864,6 +876,10 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
     warp_scan<D, R>(c, w.cstart, w.lhmax, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   }
   if (active) {
+    if (WEN32 && ti == REAL_P) {
+      sum *= (R)((float)kern_norm(K_WEN, D) * (D == 3 ? inv_hi * inv_hi * inv_hi : inv_hi * inv_hi));
+      ncount = cnt;
+    }
     if (ncount > 1) sum = (R)1. / (sum + (R)1.e-15);
     w.sum[i] = sum;
     w.cnt[i] = cnt;
@@ -1602,7 +1618,10 @@ class Engine : public EngineBase {
     cur_ ^= 1;
     mark(4);
     if (phase < MRSPH_PHASE_DENSITY) return 0;
-    k_density<D, R><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    if (sizeof(R) == 4 && kc_.prm.kernel == K_WEN)
+      k_density<D, R, (sizeof(R) == 4 ? K_WEN : -1)><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    else
+      k_density<D, R, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
     k_accum_pairs<<<1, 1, 0, st_>>>(kc_.sc);
     have_work_ = true;
     mark(5);
