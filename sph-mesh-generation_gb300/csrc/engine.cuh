@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -103,7 +104,7 @@ enum { MAP_STEP = 0, MAP_PRE = 1 };
 #define MRSPH_FORCE_VEC 4
 #endif
 #ifndef MRSPH_MAP_MIN_BLOCKS
-#define MRSPH_MAP_MIN_BLOCKS 3
+#define MRSPH_MAP_MIN_BLOCKS 4
 #endif
 #ifndef MRSPH_TILE_UNROLL
 #define MRSPH_TILE_UNROLL 1
@@ -332,6 +333,7 @@ template <int D, class R>
 __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_MAP_MIN_BLOCKS : 1))
 k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att) {
   using P = PosOps<D, R>;
+  constexpr bool F32 = std::is_same<R, float>::value;
   __shared__ unsigned long long s_hmax[MAX_CL];
   __shared__ unsigned s_lcount[MAX_CL];
   if (threadIdx.x < MAX_CL) {
@@ -359,13 +361,37 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
       R dl[3] = {v[0] * dtr, v[1] * dtr, (D == 3) ? v[2] * dtr : (R)0};
       P::add(c, p, key, dl);
     }
-    double x[3];
-    P::world(c, p, key, x);
+    // A2 at the particle's position: from FP64 world coordinates (FP64-plain)
+    // or in FP32 from the anchor representation (FP32-split)
+    auto sample_here = [&](R& ph, R* nn, R& cv) {
+      if constexpr (F32) {
+        int k[3];
+        P::unpack(key, k);
+        const float o[3] = {p.x, p.y, p.z};
+        ls_sample_anchor<D>(c.ls, k, o, ph, nn, cv);
+      } else {
+        double xw[3];
+        P::world(c, p, key, xw);
+        ls_sample<D, R>(c.ls, xw, ph, nn, cv);
+      }
+    };
+    auto tag_here = [&]() -> int {
+      if constexpr (F32) {
+        int k[3];
+        P::unpack(key, k);
+        const float o[3] = {p.x, p.y, p.z};
+        return ls_tag_anchor<D>(c.ls, k, o);
+      } else {
+        double xw[3];
+        P::world(c, p, key, xw);
+        return ls_tag<D, R>(c.ls, xw);
+      }
+    };
     R phi, n[3], curv, rho = 0;
-    ls_sample<D, R>(c.ls, x, phi, n, curv);  // A2 Get_particle_info
+    sample_here(phi, n, curv);  // A2 Get_particle_info
     if (mode == MAP_PRE) set_info<D, R>(c, phi, curv, h, rho);
     // A3 Find_and_map_particle (:408-467) + driver loop (sph_mesh_generation.cpp:1506-1545)
-    int tag = ls_tag<D, R>(c.ls, x);
+    int tag = tag_here();
     R nl = r_sqrt(dot3<D, R>(n, n));
     if (tag == CUT_CELL && (type == REAL_P || type == SURFACE_P)) {
       type = SURFACE_P;
@@ -392,9 +418,9 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
       }
       P::add(c, p, key, dl);
     }
-    P::world(c, p, key, x);
-    ls_sample<D, R>(c.ls, x, phi, n, curv);
+    sample_here(phi, n, curv);
     if (phi < (R)0 && type == REAL_P) {
+      double x[3];
       // Remap_this_particle_to_positive_phase, sph_mesh_generation.cpp:1885-1928
       atomicAdd(&c.sc->remap, 1u);
       bool ok = false;
@@ -418,7 +444,7 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
     if (mode == MAP_STEP) set_info<D, R>(c, phi, curv, h, rho);
     // Particle_base::Set_particle_scale, particle.cpp:957-975 (scale = max_scale*2^-e)
     {
-      R sc = (R)ldexp(c.geo.max_scale, -e);
+      R sc = F32 ? (R)ldexpf((float)c.geo.max_scale, -e) : (R)ldexp(c.geo.max_scale, -e);
       R hc = h * (R)c.prm.cutoff;
       for (int it = 0; it < 64; it++) {
         if (hc > sc + (R)1.e-15) { sc *= 2; e--; }
@@ -433,24 +459,38 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
       e = L;
     }
     // sort key: level-L half cell (get_cell_id, glbfunc.h:196-208, at dcell/2)
-    double xr[3];
-    P::xrel(c, p, key, xr);
     int hq[3] = {0, 0, 0};
-    for (int d = 0; d < D; d++) {
-      double u = floor(std::is_same<R, float>::value ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d]);
-      u = fmax(0.0, fmin(u, (double)(c.geo.hn[L][d] - 1)));
-      hq[d] = (int)u;
-    }
-    int ck = (int)(c.geo.hoff[L] + ((long long)hq[2] * c.geo.hn[L][1] + hq[1]) * c.geo.hn[L][0] + hq[0]);
-    atomicAdd(&counts[ck], 1);
-    {  // local h maximum of level L in the particle's level-0 cell
-      long long c0 = 0;
+    long long c0 = 0;  // level-0 cell, for the local h maximum of level L
+    if constexpr (F32) {
+      // a level-L cell is 2^sh anchor cells: the half cell follows from the
+      // anchor index and the FP32 position inside the level-L cell
+      int k[3];
+      P::unpack(key, k);
+      const float o[3] = {p.x, p.y, p.z};
+      const int sh = c.geo.ncl - 1 - L;
+      for (int d = 0; d < D; d++) {
+        const int cc = k[d] >> sh;
+        const float pos = fmaf((float)(k[d] - (cc << sh)), c.geo.Af[d], o[d]);
+        const int hl = (int)floorf(pos * c.geo.ihs_f[L][d]);
+        hq[d] = max(0, min(2 * cc + hl, c.geo.hn[L][d] - 1));
+      }
+      for (int d = D - 1; d >= 0; d--) c0 = c0 * c.geo.n[0][d] + (k[d] >> (c.geo.ncl - 1));
+    } else {
+      double xr[3];
+      P::xrel(c, p, key, xr);
+      for (int d = 0; d < D; d++) {
+        double u = floor(xr[d] / c.geo.hs[L][d]);
+        u = fmax(0.0, fmin(u, (double)(c.geo.hn[L][d] - 1)));
+        hq[d] = (int)u;
+      }
       for (int d = D - 1; d >= 0; d--) {
         int q0 = (int)fmax(0.0, fmin(floor(xr[d] * c.geo.idc0[d]), (double)(c.geo.n[0][d] - 1)));
         c0 = c0 * c.geo.n[0][d] + q0;
       }
-      atomicMax(&lhmax[L * c.geo.nc0 + c0], __float_as_uint(__double2float_ru((double)h)));
     }
+    int ck = (int)(c.geo.hoff[L] + ((long long)hq[2] * c.geo.hn[L][1] + hq[1]) * c.geo.hn[L][0] + hq[0]);
+    atomicAdd(&counts[ck], 1);
+    atomicMax(&lhmax[L * c.geo.nc0 + c0], __float_as_uint(F32 ? (float)h : __double2float_ru((double)h)));
     atomicMax(&s_hmax[L], dbits((double)h));
     atomicAdd(&s_lcount[L], 1u);
     p.w = h;
@@ -1257,8 +1297,12 @@ class Engine : public EngineBase {
     kc_.n = 0;
     kc_.sc = nullptr;
     st_ = cfg.stream;
+    if (std::is_same<R, float>::value) init_rc_ = anchor_tables();
   }
-  ~Engine() override { release(); }
+  ~Engine() override {
+    release();
+    for (void* p : anc_allocs_) cudaFree(p);
+  }
 
   int seed(long long n) override {
     int rc = alloc(n);
@@ -1587,6 +1631,15 @@ class Engine : public EngineBase {
     k_begin_step<<<1, 1, 0, st_>>>(kc_.sc, 0);
     int rc = run_map_and_bin(MAP_PRE);
     if (rc) return rc;
+    // Pre_run (sph_mesh_generation.cpp:1010-1050) leaves v = 0 (Reset_particle_force)
+    // and nu = 0 (Set_timestep(2) at v = 0), so the first step's
+    // Update_coord_full_step moves nothing; the advection step is set to 0
+    Buf<R>& b = buf_[cur_];
+    MR_CK(cudaMemsetAsync(b.v1, 0, sizeof(T4) * n_, st_));
+    MR_CK(cudaMemsetAsync(b.a2, 0, sizeof(T4) * n_, st_));
+    MR_CK(cudaMemsetAsync(b.nu, 0, sizeof(R) * n_, st_));
+    MR_CK(cudaMemsetAsync(b.nu_next, 0, sizeof(R) * n_, st_));
+    MR_CK(cudaMemsetAsync(&kc_.sc->dt2, 0, sizeof(unsigned long long), st_));
     MR_CK(cudaStreamSynchronize(st_));
     have_work_ = false;
     return 0;
@@ -1700,7 +1753,46 @@ class Engine : public EngineBase {
 
  private:
 
+  // FP32-split level-set location: per level-set level and axis, the
+  // package of each anchor cell's lower corner and the corner's FP32 offset
+  // inside it (computed here in FP64, once per level set)
+  int anchor_tables() {
+    const int lm = kc_.geo.ncl - 1;
+    for (int l = 0; l < kc_.ls.nls; l++) {
+      LsLevel& L = kc_.ls.lv[l];
+      for (int d = 0; d < 3; d++) {
+        L.anc[d] = nullptr;
+        L.dpkg_f[d] = (float)L.dpkg[d];
+        L.inv_dpkg_f[d] = (float)L.inv_dpkg[d];
+        L.inv_dcell_f[d] = (float)L.inv_dcell[d];
+        if (d >= D) continue;
+        const int na = kc_.geo.n[lm][d];
+        std::vector<int2> t(na);
+        for (int k = 0; k < na; k++) {
+          const double base = (kc_.geo.box_l[d] - L.box_l[d]) + (double)k * kc_.geo.A[d];
+          const double p0 = std::floor(base / L.dpkg[d]);
+          const float rem = (float)(base - p0 * L.dpkg[d]);
+          t[k].x = (int)p0;
+          std::memcpy(&t[k].y, &rem, sizeof(float));
+        }
+        int2* dv = nullptr;
+        if (cudaMalloc(&dv, sizeof(int2) * na) != cudaSuccess) {
+          err = "cudaMalloc failed (anchor tables)";
+          return MRSPH_ERR_OOM;
+        }
+        anc_allocs_.push_back(dv);
+        if (cudaMemcpy(dv, t.data(), sizeof(int2) * na, cudaMemcpyHostToDevice) != cudaSuccess) {
+          err = "cudaMemcpy failed (anchor tables)";
+          return MRSPH_ERR_CUDA;
+        }
+        L.anc[d] = dv;
+      }
+    }
+    return 0;
+  }
+
   int alloc(long long n) {
+    if (init_rc_) return init_rc_;
     if (n <= 0 || n > (1ll << 30)) { err = "particle count out of range"; return MRSPH_ERR_RANGE; }
     release();
     n_ = n;
@@ -1780,6 +1872,8 @@ class Engine : public EngineBase {
   cudaGraph_t gsrc_[2] = {nullptr, nullptr};
   unsigned graph_version_ = 0;
   std::vector<void*> allocs_;
+  std::vector<void*> anc_allocs_;  // anchor tables, kept across re-allocations
+  int init_rc_ = 0;
 };
 
 }  // namespace mrsph

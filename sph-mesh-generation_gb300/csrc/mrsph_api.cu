@@ -85,6 +85,7 @@ static int plan_levels(mrsph_handle* h) {
       g.hn[l][d] = (d < D) ? 2 * g.n[l][d] : 1;
       g.hs[l][d] = (d < D) ? 0.5 * g.dcell[l][d] : 1.0;
       g.ihs[l][d] = 1.0 / g.hs[l][d];
+      g.ihs_f[l][d] = (float)g.ihs[l][d];
       hc *= g.hn[l][d];
     }
     // the engine keys levels by exponent: scale = max_scale * 2^-l (sph.cpp:247-276)

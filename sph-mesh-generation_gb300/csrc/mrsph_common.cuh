@@ -30,6 +30,12 @@ struct LsLevel {
   const float* c32;
   const uint8_t* tag;
   const uint8_t* active;  // per package incl. margins, or nullptr
+  // FP32-split location (set by the FP32 engine): per axis, for every anchor
+  // cell k of the cell list, the package of the anchor's lower corner (.x)
+  // and the corner's offset inside that package as FP32 bits (.y); FP32
+  // copies of the package and cell sizes
+  const int2* anc[3];
+  float dpkg_f[3], inv_dpkg_f[3], inv_dcell_f[3];
 };
 
 struct LsSet {
@@ -53,6 +59,7 @@ struct CellGeo {
   double A[3];  // anchor cell of the FP32-split position = finest cell
   float Af[3];
   double ihs[MAX_CL][3];  // 1 / half-cell size (FP32-split keys)
+  float ihs_f[MAX_CL][3];
   double idc0[3];         // 1 / level-0 cell size (local h maxima)
   long long nc0;          // level-0 cells
   // sort table: half-size cells (2 per reference cell per axis), row-major per level
@@ -406,24 +413,12 @@ template <> __device__ inline void ls_fetch<float>(const LsLevel& L, long long a
 // location in FP64 (FP64-plain: the reference's divisions; FP32-split:
 // products with the reciprocals), weights and accumulation in R.  The
 // interpolated normal is not renormalised (reference quirk Q1).
+// Interpolation of phi, n and curvature over the 2^D cells around in-package
+// position rr of package pos (weights w = rr - floor(rr)), the second half
+// of Calculate_particle_infor.
 template <int D, class R>
-__device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n, R& curv) {
-  constexpr bool F32 = std::is_same<R, float>::value;
-  const LsLevel& L = ls.lv[ls_pick<D, R>(ls, x)];
-  int pos[3] = {0, 0, 0}, im[3] = {0, 0, 0};
-  R w[3] = {0, 0, 0};
-  for (int d = 0; d < D; d++) {
-    double dom = L.dpkg[d] * L.num_pkg[d];
-    double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
-    int p = (int)floor(F32 ? cs * L.inv_dpkg[d] : cs / L.dpkg[d]);
-    p = max(-L.margin, min(p, L.num_pkg[d] + L.margin - 1));
-    pos[d] = p;
-    double csp = cs - L.dpkg[d] * p;
-    double rr = (F32 ? csp * L.inv_dcell[d] : csp / L.dcell[d]) - 0.5;
-    rr = AMAX1(-0.5, AMIN1(rr, 4.0 - 0.5));
-    im[d] = (int)floor(rr);
-    w[d] = (R)(rr - (double)im[d]);
-  }
+__device__ inline void ls_interp(const LsLevel& L, const int* pos, const int* im, const R* w, R& phi, R* n,
+                                 R& curv) {
   R ph = 0, n0 = 0, n1 = 0, n2 = 0, cv = 0;
 #pragma unroll
   for (int r = 0; r <= 1; r++)
@@ -447,6 +442,107 @@ __device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n,
   phi = ph;
   n[0] = n0; n[1] = n1; n[2] = (D == 3) ? n2 : (R)0;
   curv = cv;
+}
+
+// Calculate_particle_infor, particle_mesh_generation.cpp:175-265.  Cell
+// location in FP64 (FP64-plain: the reference's divisions; FP32-split:
+// products with the reciprocals), weights and accumulation in R.  The
+// interpolated normal is not renormalised (reference quirk Q1).
+template <int D, class R>
+__device__ inline void ls_sample(const LsSet& ls, const double* x, R& phi, R* n, R& curv) {
+  constexpr bool F32 = std::is_same<R, float>::value;
+  const LsLevel& L = ls.lv[ls_pick<D, R>(ls, x)];
+  int pos[3] = {0, 0, 0}, im[3] = {0, 0, 0};
+  R w[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    double dom = L.dpkg[d] * L.num_pkg[d];
+    double cs = AMIN1(AMAX1(x[d] - L.box_l[d], 0.), dom - 1.e-8);
+    int p = (int)floor(F32 ? cs * L.inv_dpkg[d] : cs / L.dpkg[d]);
+    p = max(-L.margin, min(p, L.num_pkg[d] + L.margin - 1));
+    pos[d] = p;
+    double csp = cs - L.dpkg[d] * p;
+    double rr = (F32 ? csp * L.inv_dcell[d] : csp / L.dcell[d]) - 0.5;
+    rr = AMAX1(-0.5, AMIN1(rr, 4.0 - 0.5));
+    im[d] = (int)floor(rr);
+    w[d] = (R)(rr - (double)im[d]);
+  }
+  ls_interp<D, R>(L, pos, im, w, phi, n, curv);
+}
+
+// FP32-split location of a point given as anchor cell k and FP32 offset o
+// (the particle representation): per axis the package P and the position csp
+// inside it, from the anchor tables, in FP32 relative to the anchor corner.
+template <int D>
+__device__ inline void ls_loc_anchor(const LsLevel& L, const int* k, const float* o, int* P, float* csp) {
+  for (int d = 0; d < D; d++) {
+    const int2 t = __ldg(&L.anc[d][k[d]]);
+    const float cs = __int_as_float(t.y) + o[d];
+    const float q = floorf(cs * L.inv_dpkg_f[d]);
+    P[d] = t.x + (int)q;
+    csp[d] = fmaf(-q, L.dpkg_f[d], cs);
+  }
+}
+
+// ls_pick on the anchor representation: the finest level containing the
+// point with an active package, and the point's location on it.
+template <int D>
+__device__ inline int ls_pick_anchor(const LsSet& ls, const int* k, const float* o, int* P, float* csp) {
+  for (int l = ls.nls - 1; l >= 1; l--) {
+    const LsLevel& L = ls.lv[l];
+    ls_loc_anchor<D>(L, k, o, P, csp);
+    bool inside = true;
+    for (int d = 0; d < D; d++) inside = inside && P[d] >= 0 && P[d] < L.num_pkg[d];
+    if (!inside) continue;
+    if (L.active) {
+      long long np0 = L.num_pkg[0] + 2 * L.margin, np1 = L.num_pkg[1] + 2 * L.margin;
+      long long pidx = ((long long)((D == 3) ? P[2] + L.margin : 0) * np1 + (P[1] + L.margin)) * np0 + (P[0] + L.margin);
+      if (!L.active[pidx]) continue;
+    }
+    return l;
+  }
+  ls_loc_anchor<D>(ls.lv[0], k, o, P, csp);
+  return 0;
+}
+
+// ls_sample for the FP32-split particle representation: the location runs
+// in FP32 relative to the anchor corner (points outside a level's packages
+// are clamped to its boundary, as the FP64 location clamps them).
+template <int D>
+__device__ inline void ls_sample_anchor(const LsSet& ls, const int* k, const float* o, float& phi, float* n,
+                                        float& curv) {
+  int P[3] = {0, 0, 0};
+  float csp[3] = {0.f, 0.f, 0.f};
+  const LsLevel& L = ls.lv[ls_pick_anchor<D>(ls, k, o, P, csp)];
+  int pos[3] = {0, 0, 0}, im[3] = {0, 0, 0};
+  float w[3] = {0.f, 0.f, 0.f};
+  for (int d = 0; d < D; d++) {
+    int p = P[d];
+    float cp = csp[d];
+    if (p < 0) { p = 0; cp = 0.f; }
+    else if (p >= L.num_pkg[d]) { p = L.num_pkg[d] - 1; cp = L.dpkg_f[d]; }
+    pos[d] = p;
+    const float rr = fmaxf(-0.5f, fminf(fmaf(cp, L.inv_dcell_f[d], -0.5f), 3.5f));
+    im[d] = (int)floorf(rr);
+    w[d] = rr - (float)im[d];
+  }
+  ls_interp<D, float>(L, pos, im, w, phi, n, curv);
+}
+
+// ls_tag for the FP32-split particle representation.
+template <int D>
+__device__ inline int ls_tag_anchor(const LsSet& ls, const int* k, const float* o) {
+  int P[3] = {0, 0, 0};
+  float csp[3] = {0.f, 0.f, 0.f};
+  const LsLevel& L = ls.lv[ls_pick_anchor<D>(ls, k, o, P, csp)];
+  int g[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    int p = P[d], ci;
+    if (p < 0) { p = 0; ci = 0; }
+    else if (p >= L.num_pkg[d]) { p = L.num_pkg[d] - 1; ci = 3; }
+    else ci = max(0, min((int)floorf(csp[d] * L.inv_dcell_f[d]), 3));
+    g[d] = p * 4 + ci;
+  }
+  return L.tag[ls_index(L, D, g[0], g[1], g[2])];
 }
 
 // Get_level_set_char_cell_tag_and_idx (particle_mesh_generation.cpp:552-573)

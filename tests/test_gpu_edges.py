@@ -77,3 +77,47 @@ def test_particles_outside_the_box(prec):
     assert np.all(p["xyz"][:20, :2] >= lo) and np.all(p["xyz"][:20, :2] <= hi)
     assert s["flags"] & 1 == 0  # no re-seed loop ran out of attempts
     g.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_first_steps_after_seed_match_oracle(dim):
+    """Pre_run leaves v = 0 and a zero advection step (sph_mesh_generation.cpp:
+    1010-1050), so the first step's Update_coord_full_step moves nothing and
+    re-seeds nothing; the first steps from the seed follow the oracle's."""
+    import oracle
+    case = cases.disc_hole_2d(spacing=0.02, grid=64) if dim == 2 else \
+        cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    orc = oracle.Oracle(case)
+    orc.seed(case.n_particles)
+    orc.pre_run()
+    orc.steps(3)
+    o = orc.get_state()
+    g = make_gpu(case, "fp64")
+    g.Initialize_case(case.n_particles)
+    g.SPH_run_mesh_generation(1)
+    assert g.stats()["remapped"] == 0
+    g.SPH_run_mesh_generation(2)
+    p = g.particles(("xyz", "type"))
+    oxyz = np.stack([o["x"], o["y"], o["z"]], 1)
+    assert np.max(np.abs(p["xyz"] - oxyz)) < 1e-10
+    assert np.array_equal(p["type"], o["type"])
+    g.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_first_steps_after_seed_fp32(dim):
+    case = cases.disc_hole_2d(spacing=0.02, grid=64) if dim == 2 else \
+        cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    out = []
+    for prec in ("fp64", "fp32"):
+        g = make_gpu(case, prec)
+        g.Initialize_case(case.n_particles)
+        g.SPH_run_mesh_generation(1)
+        assert g.stats()["remapped"] == 0
+        g.SPH_run_mesh_generation(2)
+        out.append(g.particles(("xyz",))["xyz"])
+        g.close()
+    assert np.isfinite(out[1]).all()
+    # a particle within FP32 rounding of a cut-cell boundary may be projected
+    # in one precision and not the other
+    assert np.mean(np.max(np.abs(out[1] - out[0]), axis=1) < 1e-5) > 0.999
