@@ -579,19 +579,10 @@ __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict_
   slot_of_id[id] = (int)s;
 }
 
-// Largest h of level-L particles in the level-0 cells overlapping
-// [x - R, x + R] (0: none).  R is the level-wide bound, so every level-L
-// particle that can pair with x lies in one of these cells and its h is at
-// most the value returned; the candidate search then uses this local bound.
-template <int D>
-__device__ inline float level_hmax_near(const KCtx& c, const unsigned* __restrict__ lhmax, int L, const double* xr,
-                                        double R) {
-  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-  for (int d = 0; d < D; d++) {
-    const double top = (double)(c.geo.n[0][d] - 1);
-    lo[d] = (int)fmax(0.0, fmin(floor((xr[d] - R) * c.geo.idc0[d]), top));
-    hi[d] = (int)fmax(0.0, fmin(floor((xr[d] + R) * c.geo.idc0[d]), top));
-  }
+// Largest h of level-L particles (lhmax entries) over the level-0 cells
+// lo..hi (0: none).
+__device__ inline float lhmax_over(const KCtx& c, const unsigned* __restrict__ lhmax, int L, const int* lo,
+                                   const int* hi) {
   const unsigned* o = lhmax + (long long)L * c.geo.nc0;
   unsigned m = 0;
   for (int z = lo[2]; z <= hi[2]; z++)
@@ -599,6 +590,91 @@ __device__ inline float level_hmax_near(const KCtx& c, const unsigned* __restric
       for (int x = lo[0]; x <= hi[0]; x++)
         m = max(m, __ldg(&o[((long long)z * c.geo.n[0][1] + y) * c.geo.n[0][0] + x]));
   return __uint_as_float(m);
+}
+
+// Search origin of a particle: its box-relative FP64 position (FP64-plain) or
+// its anchor cell and FP32 offset (FP32-split).
+template <int D, class R> struct SOrigin;
+template <int D> struct SOrigin<D, double> {
+  double xr[3];
+  __device__ SOrigin(const KCtx& c, const double4& p, int key) { PosOps<D, double>::xrel(c, p, key, xr); }
+};
+template <int D> struct SOrigin<D, float> {
+  int k[3];
+  float o[3];
+  __device__ SOrigin(const KCtx&, const float4& p, int key) {
+    PosOps<D, float>::unpack(key, k);
+    o[0] = p.x; o[1] = p.y; o[2] = p.z;
+  }
+};
+
+// Level L of the candidate search from origin so with smoothing length hi:
+// R_L = cutoff * max(hi, local h maximum of level L) + 1e-10 with a 1e-5
+// relative pad (0 when no level-L particle can pair with the origin), and the
+// origin's half-cell coordinate q + fr on level L.  The local h maximum is
+// the largest lhmax entry over the level-0 cells overlapping the cube of the
+// level-wide bound (every level-L particle that can pair with the origin lies
+// in one of them).  FP64-plain keeps the box-relative FP64 arithmetic;
+// FP32-split works in FP32 relative to the anchor: a level-L cell is
+// 2^(finest - L) anchor cells, so the position inside the origin's level-L
+// (or level-0) cell is (anchor index - cell's first anchor) * A + offset.
+template <int D>
+__device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__ lhmax, int L,
+                                     const SOrigin<D, double>& so, double hi, bool active, int* q, float* fr) {
+  const double hic = hi * c.prm.cutoff;
+  const double Rg = (fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10) * (1.0 + 1.e-5);
+  float hloc = 0.f;
+  if (active) {
+    int lo[3] = {0, 0, 0}, up[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      const double top = (double)(c.geo.n[0][d] - 1);
+      lo[d] = (int)fmax(0.0, fmin(floor((so.xr[d] - Rg) * c.geo.idc0[d]), top));
+      up[d] = (int)fmax(0.0, fmin(floor((so.xr[d] + Rg) * c.geo.idc0[d]), top));
+    }
+    hloc = lhmax_over(c, lhmax, L, lo, up);
+  }
+  if (!(hloc > 0.f)) return 0.f;
+  const double Rw = fmax(hic, (double)hloc * c.prm.cutoff) + 1.e-10;
+  for (int d = 0; d < D; d++) {
+    double u = so.xr[d] / c.geo.hs[L][d];
+    u = fmax(-1.0e6, fmin(u, 1.0e9));
+    const double fl = floor(u);
+    q[d] = (int)fl;
+    fr[d] = (float)(u - fl);
+  }
+  return (float)(Rw * (1.0 + 1.e-5));
+}
+template <int D>
+__device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__ lhmax, int L,
+                                     const SOrigin<D, float>& so, float hi, bool active, int* q, float* fr) {
+  const float cut = (float)c.prm.cutoff;
+  const float hic = hi * cut;
+  const float Rg = (fmaxf(hic, (float)bitsd(c.sc->hmax[L]) * cut) + 1.e-10f) * (1.f + 1.e-5f);
+  float hloc = 0.f;
+  if (active) {
+    const int sh0 = c.geo.ncl - 1;
+    int lo[3] = {0, 0, 0}, up[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      const int c0 = so.k[d] >> sh0;
+      const float u0 = fmaf((float)(so.k[d] - (c0 << sh0)), c.geo.Af[d], so.o[d]) * c.geo.idc0_f[d];
+      const float r0 = Rg * c.geo.idc0_f[d];
+      const int top = c.geo.n[0][d] - 1;
+      lo[d] = max(0, min(c0 + (int)floorf(fmaxf(u0 - r0, -1.0e6f)), top));
+      up[d] = max(0, min(c0 + (int)floorf(fminf(u0 + r0, 1.0e6f)), top));
+    }
+    hloc = lhmax_over(c, lhmax, L, lo, up);
+  }
+  if (!(hloc > 0.f)) return 0.f;
+  const int sh = c.geo.ncl - 1 - L;
+  for (int d = 0; d < D; d++) {
+    const int cc = so.k[d] >> sh;
+    float u = fmaf((float)(so.k[d] - (cc << sh)), c.geo.Af[d], so.o[d]) * c.geo.ihs_f[L][d];
+    u = fmaxf(-1.0e6f, fminf(u, 1.0e6f));
+    const float fl = floorf(u);
+    q[d] = 2 * cc + (int)fl;
+    fr[d] = u - fl;
+  }
+  return (fmaxf(hic, hloc * cut) + 1.e-10f) * (1.f + 1.e-5f);
 }
 
 // Candidates of particle i over all cell-list levels.  The reference walks
@@ -615,26 +691,16 @@ __device__ inline float level_hmax_near(const KCtx& c, const unsigned* __restric
 // FP32 row arithmetic; the candidate test itself decides membership.
 template <int D, class R, class F>
 __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart,
-                                       const unsigned* __restrict__ lhmax, const double* xr, double hi, F&& f) {
-  constexpr bool F32 = std::is_same<R, float>::value;
-  const double hic = hi * c.prm.cutoff;
+                                       const unsigned* __restrict__ lhmax, const SOrigin<D, R>& so, R hi, F&& f) {
   for (int L = 0; L < c.geo.ncl; L++) {
     if (c.sc->lcount[L] == 0) continue;
-    const double Rg = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
-    const float hloc = level_hmax_near<D>(c, lhmax, L, xr, Rg * (1.0 + 1.e-5));
-    if (!(hloc > 0.f)) continue;
-    const double Rw = fmax(hic, (double)hloc * c.prm.cutoff) + 1.e-10;
-    const float R = (float)(Rw * (1.0 + 1.e-5));
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {0, 0, 0}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
+    const float R = level_origin<D>(c, lhmax, L, so, hi, true, q, fr);
+    if (!(R > 0.f)) continue;
     for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
     for (int d = 0; d < D; d++) {
-      double u = F32 ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d];
-      u = fmax(-1.0e6, fmin(u, 1.0e9));
-      const double fl = floor(u);
-      q[d] = (int)fl;
-      fr[d] = (float)(u - fl);
-      hs[d] = (float)c.geo.hs[L][d];
+      hs[d] = c.geo.hs_f[L][d];
       const float rr = R / hs[d];
       lo[d] = max(q[d] + (int)floorf(fr[d] - rr), 0);
       up[d] = min(q[d] + (int)floorf(fr[d] + rr), hn[d] - 1);
@@ -684,33 +750,23 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
 // (per-lane mode).
 template <int D, class R, class E, class FL, class FT, class FG>
 __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, const unsigned* __restrict__ lhmax,
-                                 bool active, const double* xr, double hi, E* tile, FL&& load, FT&& vtile,
+                                 bool active, const SOrigin<D, R>& so, R hi, E* tile, FL&& load, FT&& vtile,
                                  FG&& vglob) {
-  constexpr bool F32 = std::is_same<R, float>::value;
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
-  const double hic = hi * c.prm.cutoff;
   for (int L = 0; L < c.geo.ncl; L++) {
     if (c.sc->lcount[L] == 0) continue;
-    const double Rg = fmax(hic, bitsd(c.sc->hmax[L]) * c.prm.cutoff) + 1.e-10;
-    const float hloc = active ? level_hmax_near<D>(c, lhmax, L, xr, Rg * (1.0 + 1.e-5)) : 0.f;
-    const bool need = hloc > 0.f;
-    if (!__any_sync(FULL, need)) continue;
-    const double Rw = fmax(hic, (double)hloc * c.prm.cutoff) + 1.e-10;
-    const float R = (float)(Rw * (1.0 + 1.e-5));
-    const float R2 = R * R;
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {-1, -1, -1}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
+    const float R = level_origin<D>(c, lhmax, L, so, hi, active, q, fr);
+    const bool need = R > 0.f;
+    if (!__any_sync(FULL, need)) continue;
+    const float R2 = R * R;
     for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
     if (D == 2) { lo[2] = 0; up[2] = 0; }
     if (need) {
       for (int d = 0; d < D; d++) {
-        double u = F32 ? xr[d] * c.geo.ihs[L][d] : xr[d] / c.geo.hs[L][d];
-        u = fmax(-1.0e6, fmin(u, 1.0e9));
-        const double fl = floor(u);
-        q[d] = (int)fl;
-        fr[d] = (float)(u - fl);
-        hs[d] = (float)c.geo.hs[L][d];
+        hs[d] = c.geo.hs_f[L][d];
         const float rr = R / hs[d];
         lo[d] = max(q[d] + (int)floorf(fr[d] - rr), 0);
         up[d] = min(q[d] + (int)floorf(fr[d] + rr), hn[d] - 1);
@@ -834,7 +890,6 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   T4 a0 = mk4<R>(0, 0, 0, 0), a1 = mk4<R>(0, 0, 0, 0);
   int ti = REAL_P;
   R ni[3] = {0, 0, 0};
-  double xr[3] = {0.0, 0.0, 0.0};
   if (active) {
     a0 = b.rec[2 * i];
     a1 = b.rec[2 * i + 1];
@@ -843,8 +898,8 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       const T4 nri = b.nr[i];
       ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
     }
-    P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
   }
+  const SOrigin<D, R> so(c, active ? b.posh[i] : mk4<R>(0, 0, 0, 0), (active && b.key) ? b.key[i] : 0);
   const R hi = a0.w;
   const R inv_hi = active ? r_rcp(hi) : (R)0;
   const int kind = KK >= 0 ? KK : c.prm.kernel;
@@ -915,7 +970,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (d2 > fmaxf(R2i, fabsf(e.w))) return;
       accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
     };
-    warp_scan<D, R>(c, w.cstart, w.lhmax, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   } else {
     auto load = [&](int k) {
       RecPair<R> e;
@@ -929,7 +984,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) return;
       accept(j, dr, dist, e.b.w < (R)0);
     };
-    warp_scan<D, R>(c, w.cstart, w.lhmax, active, xr, (double)hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   }
   if (active) {
     if (WEN32 && ti == REAL_P) {
@@ -1106,9 +1161,8 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
           }
         }
       } else {
-        double xr[3];
-        P::xrel(c, b.posh[i], b.key ? b.key[i] : 0, xr);
-        scan_candidates<D, R>(c, w.cstart, w.lhmax, xr, (double)h, [&](int j) {
+        const SOrigin<D, R> so(c, b.posh[i], b.key ? b.key[i] : 0);
+        scan_candidates<D, R>(c, w.cstart, w.lhmax, so, h, [&](int j) {
           T4 b0, b1;
           ld_rec(b.rec, j, b0, b1);
           R vec[3], dr[3], cij = 0;

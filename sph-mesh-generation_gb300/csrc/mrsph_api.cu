@@ -86,6 +86,7 @@ static int plan_levels(mrsph_handle* h) {
       g.hs[l][d] = (d < D) ? 0.5 * g.dcell[l][d] : 1.0;
       g.ihs[l][d] = 1.0 / g.hs[l][d];
       g.ihs_f[l][d] = (float)g.ihs[l][d];
+      g.hs_f[l][d] = (float)g.hs[l][d];
       hc *= g.hn[l][d];
     }
     // the engine keys levels by exponent: scale = max_scale * 2^-l (sph.cpp:247-276)
@@ -104,6 +105,7 @@ static int plan_levels(mrsph_handle* h) {
   for (int d = 0; d < 3; d++) {
     g.A[d] = g.dcell[lm][d];
     g.idc0[d] = 1.0 / g.dcell[0][d];
+    g.idc0_f[d] = (float)g.idc0[d];
     g.Af[d] = (float)g.A[d];
   }
   if (p.precision == MRSPH_FP32_SPLIT) {

@@ -61,6 +61,8 @@ struct CellGeo {
   double ihs[MAX_CL][3];  // 1 / half-cell size (FP32-split keys)
   float ihs_f[MAX_CL][3];
   double idc0[3];         // 1 / level-0 cell size (local h maxima)
+  float idc0_f[3];
+  float hs_f[MAX_CL][3];  // FP32 half-cell size
   long long nc0;          // level-0 cells
   // sort table: half-size cells (2 per reference cell per axis), row-major per level
   int hn[MAX_CL][3];
