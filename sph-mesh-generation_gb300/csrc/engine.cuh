@@ -110,6 +110,14 @@ enum { MAP_STEP = 0, MAP_PRE = 1 };
 #define MRSPH_TILE_UNROLL 1
 #endif
 constexpr int kTileUnroll = MRSPH_TILE_UNROLL;
+// largest spread of a warp's half cells (max - min per axis) for which the
+// warp scans the union of its lanes' rows through shared-memory tiles
+#ifndef MRSPH_TILE_SPAN_X
+#define MRSPH_TILE_SPAN_X 3
+#endif
+#ifndef MRSPH_TILE_SPAN_YZ
+#define MRSPH_TILE_SPAN_YZ 1
+#endif
 
 // ---------------------------------------------------------------------------
 // position representations
@@ -802,7 +810,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
     for (int d = 0; d < D; d++) {
       const int qmin = __reduce_min_sync(FULL, need ? q[d] : BIG);
       const int qmax = __reduce_max_sync(FULL, need ? q[d] : -BIG);
-      uni = uni && (qmax - qmin <= (d == 0 ? 3 : 1));
+      uni = uni && (qmax - qmin <= (d == 0 ? MRSPH_TILE_SPAN_X : MRSPH_TILE_SPAN_YZ));
     }
     if (uni) {
       const int zl = __reduce_min_sync(FULL, need ? lo[2] : BIG), zu = __reduce_max_sync(FULL, need ? up[2] : -BIG);
