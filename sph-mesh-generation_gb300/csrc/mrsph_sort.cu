@@ -53,15 +53,30 @@ __device__ inline int block_excl_scan(int v, int* total) {
   return res;
 }
 
+// The 16 counts of a thread: four 16-byte loads when the group lies inside
+// the table (base is a multiple of 16, so the loads are aligned).
+__device__ inline void load16(const int* __restrict__ counts, long long base, long long n, int* v) {
+  if (base + SCAN_ITEMS <= n) {
+    const int4* p = reinterpret_cast<const int4*>(counts + base);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; k++) {
+      const int4 t = __ldg(p + k);
+      v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? counts[base + k] : 0;
+  }
+}
+
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const int* __restrict__ counts, long long n,
                                                              int* __restrict__ blocksums) {
   long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
+  int v[SCAN_ITEMS];
+  load16(counts, base, n, v);
   int s = 0;
 #pragma unroll
-  for (int k = 0; k < SCAN_ITEMS; k++) {
-    long long c = base + k;
-    if (c < n) s += counts[c];
-  }
+  for (int k = 0; k < SCAN_ITEMS; k++) s += v[k];
   int tot;
   block_excl_scan(s, &tot);
   if (threadIdx.x == 0) blocksums[blockIdx.x] = tot;
@@ -90,19 +105,29 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(int* __restrict__ co
                                                            int* __restrict__ cstart, int ntotal) {
   long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_ITEMS;
   int v[SCAN_ITEMS];
+  load16(counts, base, n, v);
   int s = 0;
 #pragma unroll
-  for (int k = 0; k < SCAN_ITEMS; k++) {
-    long long c = base + k;
-    v[k] = (c < n) ? counts[c] : 0;
-    s += v[k];
-  }
+  for (int k = 0; k < SCAN_ITEMS; k++) s += v[k];
   int off = block_excl_scan(s, nullptr) + blocksums[blockIdx.x];
+  if (base + SCAN_ITEMS <= n) {
+    int4* p = reinterpret_cast<int4*>(cstart + base);
 #pragma unroll
-  for (int k = 0; k < SCAN_ITEMS; k++) {
-    long long c = base + k;
-    if (c < n) cstart[c] = off;
-    off += v[k];
+    for (int k = 0; k < SCAN_ITEMS / 4; k++) {
+      int4 t;
+      t.x = off; off += v[4 * k];
+      t.y = off; off += v[4 * k + 1];
+      t.z = off; off += v[4 * k + 2];
+      t.w = off; off += v[4 * k + 3];
+      p[k] = t;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+      long long c = base + k;
+      if (c < n) cstart[c] = off;
+      off += v[k];
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) cstart[n] = ntotal;
 }
