@@ -1,0 +1,343 @@
+"""Output and restart files of the relaxation: the host side of the
+reference's writers (Particle_binary_writer, particle_binary_writer.cpp:12-400;
+Mesh_binary_writer, mesh_binary_writer.cpp:36-390) and of its particle restart
+(Save_particle_post_file / Load_data_for_post, sph_mesh_generation.cpp:2624-2660,
+426-590).  The GPU engine holds the state; these functions read it through
+the C ABI (mrsph_get_particles, mrsph_get_neighbors, mrsph_triangulate) and
+write the same files, under the same names, a reference run writes:
+
+  outdata/particle_rank_<r>_step_<n>.vtu, particle_step_<n>.pvtu, particle.pvd
+  outdata/mesh_tris_rank_<r>_step_<n>.vtu, mesh_tris_step_<n>.pvtu, mesh_tris.pvd
+  rstfile_particles/step_<run_time>_rank_<r>.pst, rstfile_particles/list.csv
+
+VTU files are VTK XML UnstructuredGrid pieces with raw appended data: every
+array is a little-endian UInt32 byte count followed by its values (the
+header's offsets count from the byte after the '_' marker).  A .pst file is an
+int32 particle count followed by x, y, z as float64 per particle.
+"""
+from __future__ import annotations
+
+import os
+import struct
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+# VTK XML type names of the numpy dtypes the writers use
+_VTK_TYPE = {np.dtype("<i4"): "Int32", np.dtype("<f4"): "Float32", np.dtype("<f8"): "Float64",
+             np.dtype("u1"): "UInt8"}
+
+# Fields written per particle by default (Particle_binary_writer::Particle_binary_writer,
+# particle_binary_writer.cpp:12-30): id, local_id, type, h, NN, color, norm.
+PARTICLE_FIELDS_DEFAULT = ("id", "local_id", "type", "h", "NN", "color", "norm")
+PARTICLE_FIELDS_ALL = ("id", "local_id", "type", "phi", "h", "scale", "curv", "NN", "color", "norm", "accel",
+                       "vel", "timestep")
+
+
+# ----------------------------------------------------------------------- VTU
+def _le(a: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(a)
+    if a.dtype.byteorder == ">":
+        a = a.astype(a.dtype.newbyteorder("<"))
+    return a
+
+
+def vtu_bytes(points: np.ndarray, cells: np.ndarray, cell_type: int,
+              point_data: Sequence[Tuple[str, np.ndarray]] = (),
+              cell_data: Sequence[Tuple[str, np.ndarray]] = ()) -> bytes:
+    """One VTK XML UnstructuredGrid piece with raw appended arrays.
+
+    points: (n, 3) positions (written as Float32 'Position', as the reference
+    does); cells: (m, k) point indices per cell, all of one VTK cell type
+    (1 vertex, 5 triangle, 10 tetrahedron); point_data / cell_data: (name,
+    array) pairs, arrays of shape (n,) or (n, c) in int32, float32 or
+    float64."""
+    points = _le(np.asarray(points, dtype="<f4").reshape(-1, 3))
+    cells = _le(np.asarray(cells, dtype="<i4"))
+    if cells.ndim == 1:
+        cells = cells.reshape(-1, 1)
+    n, m, k = len(points), len(cells), cells.shape[1]
+    blobs: List[bytes] = []
+    offset = 0
+    head: List[str] = []
+
+    def add(name: str, arr: np.ndarray, indent: str, components: bool = True) -> None:
+        nonlocal offset
+        arr = _le(arr)
+        t = _VTK_TYPE[arr.dtype]
+        nc = f' NumberOfComponents="{1 if arr.ndim == 1 else arr.shape[1]}"' if components else ""
+        head.append(f'{indent}<DataArray type="{t}" Name="{name}"{nc} format="appended" offset="{offset}"/>')
+        raw = arr.tobytes()
+        blobs.append(struct.pack("<I", len(raw)) + raw)
+        offset += 4 + len(raw)
+
+    head.append('<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian">')
+    head.append(" <UnstructuredGrid>")
+    head.append(f'  <Piece NumberOfPoints="{n}" NumberOfCells="{m}">')
+    head.append('    <PointData Vectors="vector">')
+    for name, arr in point_data:
+        add(name, np.asarray(arr), "      ")
+    head.append("    </PointData>")
+    if cell_data:
+        head.append('    <CellData Vectors="vector">')
+        for name, arr in cell_data:
+            add(name, np.asarray(arr), "      ")
+        head.append("    </CellData>")
+    head.append("    <Points>")
+    add("Position", points, "      ")
+    head.append("    </Points>")
+    head.append("    <Cells>")
+    add("connectivity", cells.reshape(-1), "      ", components=False)
+    add("offsets", (np.arange(1, m + 1, dtype="<i4") * k), "      ", components=False)
+    add("types", np.full(m, cell_type, dtype="u1"), "      ", components=False)
+    head.append("    </Cells>")
+    head.append("  </Piece>")
+    head.append(" </UnstructuredGrid>")
+    head.append(' <AppendedData encoding="raw">')
+    text = "\n".join(head) + "\n _"
+    tail = "\n </AppendedData>\n</VTKFile>\n"
+    return text.encode("ascii") + b"".join(blobs) + tail.encode("ascii")
+
+
+def read_vtu(path: str) -> Dict[str, np.ndarray]:
+    """Arrays of a VTU piece with raw appended data, by name ('Position',
+    'connectivity', 'offsets', 'types' and the point / cell fields)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    mark = data.index(b'<AppendedData encoding="raw">')
+    start = data.index(b"_", mark) + 1
+    header = data[:mark].decode("ascii")
+    out: Dict[str, np.ndarray] = {}
+    inv = {v: k for k, v in _VTK_TYPE.items()}
+    for line in header.splitlines():
+        line = line.strip()
+        if not line.startswith("<DataArray"):
+            continue
+        attrs = dict(kv.split("=", 1) for kv in line[len("<DataArray"):-2].split())
+        attrs = {k: v.strip('"') for k, v in attrs.items()}
+        dt = inv[attrs["type"]]
+        off = start + int(attrs["offset"])
+        nbytes = struct.unpack("<I", data[off:off + 4])[0]
+        arr = np.frombuffer(data[off + 4:off + 4 + nbytes], dtype=dt).copy()
+        comps = int(attrs.get("NumberOfComponents", "1"))
+        if comps > 1:
+            arr = arr.reshape(-1, comps)
+        out[attrs["Name"]] = arr
+    return out
+
+
+def _pvtu_text(piece_files: Sequence[str], point_fields: Sequence[Tuple[str, str, int]],
+               cell_fields: Sequence[Tuple[str, str, int]] = ()) -> str:
+    lines = ['<VTKFile type="PUnstructuredGrid" version="0.1" byte_order="LittleEndian">',
+             ' <PUnstructuredGrid GhostLevel="0">', "  <PPointData>"]
+    for name, t, c in point_fields:
+        lines.append(f'    <PDataArray type="{t}" Name="{name}" NumberOfComponents="{c}"/>')
+    lines.append("  </PPointData>")
+    if cell_fields:
+        lines.append("  <PCellData>")
+        for name, t, c in cell_fields:
+            lines.append(f'    <PDataArray type="{t}" Name="{name}" NumberOfComponents="{c}"/>')
+        lines.append("  </PCellData>")
+    lines += ["  <PPoints>", '    <PDataArray type="Float32" Name="Position" NumberOfComponents="3"/>',
+              "  </PPoints>"]
+    for p in piece_files:
+        lines.append(f'  <Piece Source="{p}"/>')
+    lines += [" </PUnstructuredGrid>", "</VTKFile>"]
+    return "\n".join(lines) + "\n"
+
+
+def update_pvd(path: str, n_out: int, timestep: float, dataset: str) -> None:
+    """The collection file of a series: rewritten with one DataSet entry per
+    output so far (Output_pvd_file, particle_binary_writer.cpp:53-93; a
+    first output, n_out = 0, starts a new collection)."""
+    entries: List[str] = []
+    if n_out != 0 and os.path.exists(path):
+        with open(path) as f:
+            entries = [ln.rstrip("\n") for ln in f if ln.strip().startswith("<DataSet")]
+    entries.append(f'    <DataSet timestep="{timestep}" group="" part="0" file="{dataset}"/>')
+    with open(path, "w") as f:
+        f.write('<VTKFile type="Collection" version="0.1">\n  <Collection>\n')
+        f.write("\n".join(entries) + "\n")
+        f.write("  </Collection>\n</VTKFile>\n")
+
+
+def _fields_meta(fields: Sequence[Tuple[str, np.ndarray]]) -> List[Tuple[str, str, int]]:
+    out = []
+    for name, a in fields:
+        a = np.asarray(a)
+        out.append((name, _VTK_TYPE[_le(a).dtype], 1 if a.ndim == 1 else a.shape[1]))
+    return out
+
+
+# ----------------------------------------------------------- particle output
+def particle_point_data(sim, fields: Sequence[str] = PARTICLE_FIELDS_DEFAULT) -> List[Tuple[str, np.ndarray]]:
+    """Per-particle arrays in particle-id order, named and typed as the
+    reference writes them (Int32 ids, type, NN, color; Float32 scalars and
+    3-vectors).  NN is the neighbour count of the last density pass, the
+    particle itself included; color is the rank (0 on one GPU)."""
+    need = {"xyz"}
+    if "type" in fields:
+        need.add("type")
+    if "phi" in fields:
+        need.add("phi")
+    if "h" in fields:
+        need.add("h")
+    if "curv" in fields:
+        need.add("curv")
+    if "norm" in fields:
+        need.add("norm")
+    if "accel" in fields:
+        need.add("a2")
+    if "vel" in fields:
+        need.add("v")
+    if "scale" in fields:
+        need.add("h")
+    p = sim.particles(tuple(sorted(need)))
+    n = sim.n
+    out: List[Tuple[str, np.ndarray]] = []
+    for f in fields:
+        if f in ("id", "local_id"):
+            a = np.arange(n, dtype="<i4")
+        elif f == "type":
+            a = p["type"].astype("<i4")
+        elif f == "NN":
+            off, _ = sim.neighbors()
+            a = np.diff(off).astype("<i4")
+        elif f == "color":
+            a = np.zeros(n, dtype="<i4")
+        elif f == "norm":
+            a = p["norm"].astype("<f4")
+        elif f == "accel":
+            a = p["a2"].astype("<f4")
+        elif f == "vel":
+            a = p["v"].astype("<f4")
+        elif f == "scale":
+            # scale = h * CUT_OFF / CELL_RATIO (Set_particle_info, particle_mesh_generation.cpp:361-381)
+            prm = sim.case.params
+            a = (p["h"] * prm["cutoff"] / prm["cell_ratio"]).astype("<f4")
+        elif f == "timestep":
+            a = np.full(n, sim.stats()["dt"], dtype="<f4")
+        else:
+            a = p[f].astype("<f4")
+        out.append((f, a))
+    return out
+
+
+class ParticleWriter:
+    """Particle_binary_writer: one VTU piece per output (rank 0), its PVTU
+    and the PVD collection under outdir."""
+
+    def __init__(self, outdir: str = "outdata", fields: Sequence[str] = PARTICLE_FIELDS_DEFAULT):
+        unknown = set(fields) - set(PARTICLE_FIELDS_ALL)
+        if unknown:
+            raise ValueError(f"unknown particle fields {sorted(unknown)}")
+        self.outdir = outdir
+        self.fields = tuple(fields)
+
+    def Output_particle(self, n_out: int, sim, run_time: Optional[float] = None) -> str:
+        os.makedirs(self.outdir, exist_ok=True)
+        pd = particle_point_data(sim, self.fields)
+        xyz = sim.particles(("xyz",))["xyz"]
+        piece = f"particle_rank_0_step_{n_out}.vtu"
+        with open(os.path.join(self.outdir, piece), "wb") as f:
+            f.write(vtu_bytes(xyz, np.arange(len(xyz), dtype="<i4"), 1, pd))
+        pvtu = f"particle_step_{n_out}.pvtu"
+        with open(os.path.join(self.outdir, pvtu), "w") as f:
+            f.write(_pvtu_text([piece], _fields_meta(pd)))
+        t = sim.stats()["step"] if run_time is None else run_time
+        update_pvd(os.path.join(self.outdir, "particle.pvd"), n_out, t, f"./{pvtu}")
+        return os.path.join(self.outdir, piece)
+
+
+# --------------------------------------------------------------- mesh output
+def triangle_quality(xyz: np.ndarray, tris: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+    """Area and aspect ratio (longest / shortest edge) of every triangle, the
+    per-triangle 'vol' and 'aspect' of Tri_quality_statistics
+    (geometry_tools/graph_mesh.cpp:411-670)."""
+    p = np.asarray(xyz, dtype=np.float64)[:, :2]
+    a, b, c = p[tris[:, 0]], p[tris[:, 1]], p[tris[:, 2]]
+    e = np.stack([np.linalg.norm(b - a, axis=1), np.linalg.norm(c - b, axis=1), np.linalg.norm(a - c, axis=1)], 1)
+    area = 0.5 * np.abs((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]))
+    return area, e.max(1) / e.min(1)
+
+
+class MeshWriter:
+    """Mesh_binary_writer for the 2D triangle mesh: a VTU piece with one
+    triangle cell per triangle (point fields as for particles, cell fields
+    'vol' and 'aspect'), its PVTU and the mesh_tris.pvd collection."""
+
+    def __init__(self, outdir: str = "outdata", fields: Sequence[str] = PARTICLE_FIELDS_DEFAULT):
+        self.outdir = outdir
+        self.fields = tuple(fields)
+
+    def Output_mesh(self, n_out: int, sim, tris: Optional[np.ndarray] = None, run_time: Optional[float] = None) -> str:
+        os.makedirs(self.outdir, exist_ok=True)
+        if tris is None:
+            tris, _ = sim.Reconstruct_tris()
+        tris = np.asarray(tris, dtype="<i4").reshape(-1, 3)
+        xyz = sim.particles(("xyz",))["xyz"]
+        pd = particle_point_data(sim, self.fields)
+        vol, aspect = triangle_quality(xyz, tris)
+        cd = [("vol", vol.astype("<f4")), ("aspect", aspect.astype("<f4"))]
+        piece = f"mesh_tris_rank_0_step_{n_out}.vtu"
+        with open(os.path.join(self.outdir, piece), "wb") as f:
+            f.write(vtu_bytes(xyz, tris, 5, pd, cd))
+        pvtu = f"mesh_tris_step_{n_out}.pvtu"
+        with open(os.path.join(self.outdir, pvtu), "w") as f:
+            f.write(_pvtu_text([piece], _fields_meta(pd), _fields_meta(cd)))
+        t = sim.stats()["step"] if run_time is None else run_time
+        update_pvd(os.path.join(self.outdir, "mesh_tris.pvd"), n_out, t, f"./{pvtu}")
+        return os.path.join(self.outdir, piece)
+
+
+# ------------------------------------------------------------------ restarts
+def write_pst(path: str, xyz: np.ndarray) -> None:
+    """int32 count, then x, y, z (float64) per particle."""
+    xyz = np.ascontiguousarray(np.asarray(xyz, dtype="<f8").reshape(-1, 3))
+    with open(path, "wb") as f:
+        f.write(struct.pack("<i", len(xyz)))
+        f.write(xyz.tobytes())
+
+
+def read_pst(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        n = struct.unpack("<i", f.read(4))[0]
+        xyz = np.frombuffer(f.read(24 * n), dtype="<f8")
+    if len(xyz) != 3 * n:
+        raise ValueError(f"{path}: truncated particle file ({len(xyz) // 3} of {n} particles)")
+    return xyz.reshape(n, 3).copy()
+
+
+def save_particle_post_file(sim, root: str = ".", run_time: Optional[int] = None, first: bool = False) -> str:
+    """Save_particle_post_file (sph_mesh_generation.cpp:2624-2660): positions
+    of every particle (in id order) to rstfile_particles/step_<run_time>_rank_0.pst
+    and a '<run_time> <particle count>' line in rstfile_particles/list.csv,
+    whose first line is the rank count (written when first is true)."""
+    d = os.path.join(root, "rstfile_particles")
+    os.makedirs(d, exist_ok=True)
+    t = int(sim.stats()["step"] if run_time is None else run_time)
+    lst = os.path.join(d, "list.csv")
+    mode = "w" if first or not os.path.exists(lst) else "a"
+    with open(lst, mode) as f:
+        if mode == "w":
+            f.write("1\n")
+        f.write(f"{t} {sim.n}\n")
+    path = os.path.join(d, f"step_{t}_rank_0.pst")
+    write_pst(path, sim.particles(("xyz",))["xyz"])
+    return path
+
+
+def read_particle_list(root: str = ".") -> Tuple[int, List[Tuple[int, int]]]:
+    """(rank count, [(run_time, particle count), ...]) of list.csv."""
+    with open(os.path.join(root, "rstfile_particles", "list.csv")) as f:
+        lines = [ln.split() for ln in f if ln.strip()]
+    return int(lines[0][0]), [(int(a), int(b)) for a, b in lines[1:]]
+
+
+def load_data_for_post(sim, path: str, pre_run: bool = True) -> int:
+    """Load_data_for_post (sph_mesh_generation.cpp:426-590) for positions: the
+    particles of a .pst file become the state (REAL, zero velocity); with
+    pre_run the map and Pre_run follow, as in the reference."""
+    xyz = read_pst(path)
+    sim.set_state({"xyz": xyz}, pre_run=pre_run)
+    return len(xyz)

@@ -1,0 +1,124 @@
+"""Writers and restart files (mrsph/io.py) on the CPU: the byte layout of
+.pst restarts and list.csv, VTU pieces read back array by array, PVTU / PVD
+collections, and the particle and mesh writers over a stand-in for a solver
+handle (the GPU round trip is in test_gpu_io.py)."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from mrsph import io
+
+
+class FakeSim:
+    """The slice of SPHMeshGeneration the writers read."""
+
+    def __init__(self, n=50, seed=0):
+        rng = np.random.default_rng(seed)
+        self.n = n
+        self.xyz = rng.random((n, 3))
+        self.xyz[:, 2] = 0.0
+        self.type = (rng.random(n) < 0.3).astype(np.int32)
+        self.h = 0.01 + 0.01 * rng.random(n)
+        self.norm = rng.standard_normal((n, 3))
+        self.cnt = rng.integers(1, 30, n)
+        self.case = type("C", (), {"params": {"cutoff": 2.0, "cell_ratio": 2.0}})()
+        self.loaded = None
+
+    def particles(self, fields):
+        src = {"xyz": self.xyz, "type": self.type, "h": self.h, "norm": self.norm, "phi": self.h * 3,
+               "curv": self.h * 0, "a2": self.norm * 2, "v": self.norm * 3}
+        return {f: src[f].copy() for f in fields}
+
+    def neighbors(self):
+        off = np.concatenate([[0], np.cumsum(self.cnt)])
+        return off, np.zeros(off[-1], dtype=np.int32)
+
+    def stats(self):
+        return {"step": 7, "dt": 0.5}
+
+    def set_state(self, st, pre_run=False):
+        self.loaded = (np.asarray(st["xyz"]).copy(), pre_run)
+
+
+def test_pst_layout_and_round_trip(tmp_path):
+    xyz = np.random.default_rng(1).random((17, 3))
+    p = tmp_path / "a.pst"
+    io.write_pst(str(p), xyz)
+    raw = p.read_bytes()
+    assert len(raw) == 4 + 17 * 24
+    assert struct.unpack("<i", raw[:4])[0] == 17
+    assert np.array_equal(np.frombuffer(raw[4:], dtype="<f8").reshape(17, 3), xyz)
+    assert np.array_equal(io.read_pst(str(p)), xyz)
+    p.write_bytes(raw[:-8])
+    with pytest.raises(ValueError):
+        io.read_pst(str(p))
+
+
+def test_save_and_load_post_file(tmp_path):
+    sim = FakeSim()
+    path = io.save_particle_post_file(sim, str(tmp_path), run_time=0, first=True)
+    io.save_particle_post_file(sim, str(tmp_path), run_time=100)
+    assert os.path.basename(path) == "step_0_rank_0.pst"
+    assert (tmp_path / "rstfile_particles" / "list.csv").read_text() == "1\n0 50\n100 50\n"
+    assert io.read_particle_list(str(tmp_path)) == (1, [(0, 50), (100, 50)])
+    other = FakeSim(seed=3)
+    assert io.load_data_for_post(other, path) == 50
+    assert np.array_equal(other.loaded[0], sim.xyz) and other.loaded[1] is True
+
+
+def test_vtu_arrays_round_trip(tmp_path):
+    rng = np.random.default_rng(2)
+    pts = rng.random((9, 3))
+    tris = np.array([[0, 1, 2], [2, 3, 4], [5, 6, 7]], dtype=np.int32)
+    pd = [("id", np.arange(9, dtype="<i4")), ("h", rng.random(9).astype("<f4")),
+          ("norm", rng.random((9, 3)).astype("<f4"))]
+    cd = [("vol", rng.random(3).astype("<f4"))]
+    p = tmp_path / "m.vtu"
+    p.write_bytes(io.vtu_bytes(pts, tris, 5, pd, cd))
+    r = io.read_vtu(str(p))
+    assert np.array_equal(r["Position"], pts.astype("<f4"))
+    assert np.array_equal(r["connectivity"], tris.reshape(-1))
+    assert np.array_equal(r["offsets"], [3, 6, 9])
+    assert np.array_equal(r["types"], [5, 5, 5])
+    for name, a in pd + cd:
+        assert np.array_equal(r[name], a), name
+    head = p.read_bytes().split(b"<AppendedData")[0].decode()
+    assert 'NumberOfPoints="9" NumberOfCells="3"' in head
+    assert head.count("<DataArray") == 8
+
+
+def test_particle_writer_series(tmp_path):
+    sim = FakeSim()
+    w = io.ParticleWriter(str(tmp_path / "outdata"), fields=io.PARTICLE_FIELDS_ALL)
+    f0 = w.Output_particle(0, sim, run_time=0)
+    w.Output_particle(1, sim, run_time=10)
+    r = io.read_vtu(f0)
+    assert np.array_equal(r["id"], np.arange(50))
+    assert np.array_equal(r["type"], sim.type)
+    assert np.array_equal(r["NN"], sim.cnt)
+    assert np.allclose(r["h"], sim.h.astype(np.float32))
+    assert np.allclose(r["scale"], (sim.h * 2.0 / 2.0).astype(np.float32))
+    assert np.allclose(r["accel"], (sim.norm * 2).astype(np.float32))
+    assert r["norm"].shape == (50, 3) and np.array_equal(r["types"], np.ones(50))
+    pvd = (tmp_path / "outdata" / "particle.pvd").read_text()
+    assert pvd.count("<DataSet") == 2 and 'file="./particle_step_1.pvtu"' in pvd
+    pvtu = (tmp_path / "outdata" / "particle_step_0.pvtu").read_text()
+    assert '<Piece Source="particle_rank_0_step_0.vtu"/>' in pvtu
+    assert pvtu.count("<PDataArray") == len(io.PARTICLE_FIELDS_ALL) + 1
+    with pytest.raises(ValueError):
+        io.ParticleWriter(str(tmp_path), fields=("nope",))
+
+
+def test_mesh_writer_and_quality(tmp_path):
+    sim = FakeSim(n=4)
+    sim.xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]], dtype=np.float64)
+    tris = np.array([[0, 1, 2], [1, 3, 2]])
+    area, aspect = io.triangle_quality(sim.xyz, tris)
+    assert np.allclose(area, [0.5, 0.5]) and np.allclose(aspect, [np.sqrt(2), np.sqrt(2)])
+    f = io.MeshWriter(str(tmp_path)).Output_mesh(0, sim, tris=tris, run_time=3)
+    r = io.read_vtu(f)
+    assert np.array_equal(r["connectivity"], tris.reshape(-1)) and np.array_equal(r["types"], [5, 5])
+    assert np.allclose(r["vol"], 0.5) and np.allclose(r["aspect"], np.sqrt(2))
+    assert 'timestep="3"' in (tmp_path / "mesh_tris.pvd").read_text()
