@@ -1484,8 +1484,10 @@ class Engine : public EngineBase {
         cur_ = saved;
         if (rc) return rc;
         if (ee != cudaSuccess) { err = cudaGetErrorString(ee); return MRSPH_ERR_CUDA; }
-        MR_CK(cudaGraphInstantiate(&graph_[p], g, 0));
-        gsrc_[p] = g;  // kept for batch graphs
+        cudaError_t ie = cudaGraphInstantiate(&graph_[p], g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) { graph_[p] = nullptr; err = cudaGetErrorString(ie); return MRSPH_ERR_CUDA; }
+        MR_CK(cudaGraphUpload(graph_[p], st_));  // upload now, not at the first (timed) launch
       }
     }
     return 0;
@@ -1494,29 +1496,24 @@ class Engine : public EngineBase {
   void drop_graphs() {
     for (int p = 0; p < 2; p++) {
       if (graph_[p]) { cudaGraphExecDestroy(graph_[p]); graph_[p] = nullptr; }
-      if (gsrc_[p]) { cudaGraphDestroy(gsrc_[p]); gsrc_[p] = nullptr; }
     }
-    graph_version_++;
   }
 
-  int step_graph(int offset, cudaGraph_t* g) override {
+  // One step of a batch: the step graph of the current parity launched on the
+  // handle's stream, without the periodic capacity check (the batch makes it).
+  int step_batched() override {
     if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
     int rc = build_graphs();
     if (rc) return rc;
-    *g = gsrc_[cur_ ^ (offset & 1)];
+    MR_CK(cudaGraphLaunch(graph_[cur_], st_));
+    cur_ ^= 1;
+    have_work_ = true;
     return 0;
   }
 
-  void batch_advanced(int nsteps) override {
-    if (nsteps <= 0) return;
-    cur_ ^= (nsteps & 1);
-    have_work_ = true;
-  }
+  int prepare_steps() override { return n_ ? build_graphs() : 0; }
 
   int check_capacity() override { return have_work_ ? maybe_grow_cap() : 0; }
-
-  unsigned graph_version() const override { return graph_version_; }
-  int parity() const override { return cur_; }
 
   int stats(mrsph_stats* o) override {
     DevScalars h;
@@ -1931,8 +1928,6 @@ class Engine : public EngineBase {
   bool have_work_ = false;
   int countdown_ = 0;
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
-  cudaGraph_t gsrc_[2] = {nullptr, nullptr};
-  unsigned graph_version_ = 0;
   std::vector<void*> allocs_;
   std::vector<void*> anc_allocs_;  // anchor tables, kept across re-allocations
   int init_rc_ = 0;

@@ -45,16 +45,13 @@ class EngineBase {
   virtual int export_tri(double* d_xyz, int* d_type, double* d_phi, int* d_rows, int* d_cnt, int rowcap,
                          unsigned* d_flags) = 0;
   virtual int neighbor_capacity() const = 0;
-  // Batched stepping: the captured step graph of the step `offset` steps
-  // ahead (its buffer parity), valid until graph_version() changes; the host
-  // bookkeeping of steps launched through a batch graph; the neighbour-list
-  // capacity check a solo step makes every 32 steps (the handle's stream
-  // must be idle; the graphs may be rebuilt).
-  virtual int step_graph(int offset, cudaGraph_t* g) = 0;
-  virtual void batch_advanced(int nsteps) = 0;
+  // Batched stepping: one step launched on the handle's stream without the
+  // periodic capacity check; the step graphs built ahead of a timed region;
+  // the neighbour-list capacity check a solo step makes every 32 steps (the
+  // handle's stream must be idle; the graphs may be rebuilt).
+  virtual int step_batched() = 0;
+  virtual int prepare_steps() = 0;
   virtual int check_capacity() = 0;
-  virtual unsigned graph_version() const = 0;
-  virtual int parity() const = 0;  // buffer parity of the next step
   std::string err;
 };
 
