@@ -292,10 +292,11 @@ int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri
 /* Batched relaxation of independent geometries (no counterpart in the
  * reference, which relaxes one geometry per run, SPH_run_mesh_generation,
  * sph_mesh_generation.cpp:1371-1463).  A batch steps seeded handles of one
- * device together: one CUDA graph launch per step, whose nodes are the
- * handles' own step graphs, so each handle's results equal those of stepping
- * it alone.  Work queued on a handle before mrsph_batch_step completes first;
- * work queued on it afterwards waits for the batch.  A handle may be stepped
+ * device together: each step launches every handle's own step graph on the
+ * handle's own stream, so the geometries run concurrently and each handle's
+ * results equal those of stepping it alone.  Work queued on a handle before
+ * mrsph_batch_step runs first; work queued on it afterwards runs after the
+ * batch's steps.  A handle may be stepped
  * alone between batch calls; it must not be destroyed while in a batch. */
 typedef struct mrsph_batch mrsph_batch;
 int mrsph_batch_create(mrsph_handle* const* handles, int count, mrsph_batch** out);
@@ -303,7 +304,8 @@ int mrsph_batch_destroy(mrsph_batch* b);
 int mrsph_batch_last_error(mrsph_batch* b, char* buf, size_t len);
 /* nsteps steps of every handle (asynchronous; capacity checks every 32 steps). */
 int mrsph_batch_step(mrsph_batch* b, int nsteps);
-/* Same, device-timed with CUDA events on the batch stream (ms for all steps). */
+/* Same, device-timed with CUDA events (ms from before the first handle's first
+ * step to after every handle's last step). */
 int mrsph_batch_step_timed(mrsph_batch* b, int nsteps, double* ms);
 int mrsph_batch_sync(mrsph_batch* b);
 
