@@ -522,15 +522,18 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
 
 // Packed record read by the neighbour passes, two V4 words per particle so
 // that one candidate costs one 32-byte sector (FP32):
-//   FP32: w0 = (offset x, y, z, h), w1 = (anchor x, y, z as exact floats, +-rho)
-//   FP64: w0 = (x, y, z, h),        w1 = (0, 0, 0, +-rho)
-// The sign of rho carries the type: negative for a SURFACE particle.
+//   FP32: w0 = (offset x, y, z, h), w1 = (anchor x, y, z as exact floats, +-1/rho^2)
+//   FP64: w0 = (x, y, z, h),        w1 = (0, 0, 0, +-1/rho^2)
+// The sign carries the type: negative for a SURFACE particle.  1/rho^2 is the
+// neighbour's share of the pair coefficient of the force stages, computed once
+// per particle (as 1 / (rho * rho), the forces' own expression).
 template <int D, class R> struct RecOps;
 template <int D>
 struct RecOps<D, double> {
   __device__ static void pack(const KCtx&, const double4& p, int, int type, double rho, double4& w0, double4& w1) {
     w0 = p;
-    w1 = make_double4(0.0, 0.0, 0.0, type == SURFACE_P ? -rho : rho);
+    const double vol = r_rcp(rho * rho);
+    w1 = make_double4(0.0, 0.0, 0.0, type == SURFACE_P ? -vol : vol);
   }
   __device__ static void rel(const KCtx&, const double4& a0, const double4&, const double4& b0, const double4&,
                              double* dr) {
@@ -545,7 +548,8 @@ struct RecOps<D, float> {
     int k[3];
     PosOps<D, float>::unpack(key, k);
     w0 = p;
-    w1 = make_float4((float)k[0], (float)k[1], (float)k[2], type == SURFACE_P ? -rho : rho);
+    const float vol = r_rcp(rho * rho);
+    w1 = make_float4((float)k[0], (float)k[1], (float)k[2], type == SURFACE_P ? -vol : vol);
   }
   __device__ static void rel(const KCtx& c, const float4& a0, const float4& a1, const float4& b0, const float4& b1,
                              float* dr) {
@@ -1038,10 +1042,26 @@ __device__ inline void load4(const double* p, double* v) {
 // of a pair is c_ij * eta_ij * (v_i - v_j) (:1021-1049), so stage 2 reads the
 // coefficient and one vector per neighbour; a particle whose list spilled
 // re-scans its cells and recomputes c_ij in both stages.
-template <int D, class R, int STAGE>
+// FP32 Wendland C2 gradient over distance in DK dimensions (0 in 1D, the
+// reference's quirk), Derivative_kernel_function (particle.cpp:732-750):
+// -5 C (1 - s/2)^3 s / h / (r + 1e-15) with C = norm / h^DK and s = r / h,
+// which is -5 norm (1 - s/2)^3 / h^(DK+2) for r > 0 in FP32, and 0 at r = 0.
+template <int DK>
+__device__ inline float wendland_aw(float dist, float h) {
+  if (DK == 1) return 0.f;
+  const float ih = r_rcp(h);
+  const float t = fmaxf(fmaf(-0.5f * ih, dist, 1.f), 0.f);
+  float ihp = (ih * ih) * (ih * ih);
+  if (DK == 3) ihp *= ih;
+  return dist > 0.f ? (-5.f * (float)kern_norm(K_WEN, DK)) * ihp * (t * t * t) : 0.f;
+}
+
+// KK: the kernel kind fixed at compile time (FP32 Wendland C2), or -1
+template <int D, class R, int STAGE, int KK>
 __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE == 1 ? MRSPH_FORCE_MIN_BLOCKS : MRSPH_FORCE2_MIN_BLOCKS) : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
+  constexpr bool WEN32 = std::is_same<R, float>::value && KK == K_WEN;
   using T4 = typename V4<R>::T;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double my_dt = 1.e300, my_v = 0.0;
@@ -1054,7 +1074,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
       const T4 nri = b.nr[i];
       ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
     }
-    const R rho = r_fabs(a1r.w), h = a0.w;
+    const R rho = b.nr[i].w, h = a0.w;
     const R cos_t = (R)c.prm.cos_thres;
     const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
     R nu = 0, eta_i = 0;
@@ -1081,7 +1101,8 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
       if (ti == REAL_P) {
         dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
         R dist = pair_dist(dot3<D, R>(dr, dr));
-        aw = pair_dW(c.prm.kernel, D, dist, hij);
+        if constexpr (WEN32) aw = wendland_aw<D>(dist, hij);
+        else aw = pair_dW(c.prm.kernel, D, dist, hij);
       } else {
         R dn = dot3<D, R>(vec, ni);
         dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
@@ -1089,10 +1110,10 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
         const T4 nrj = b.nr[j];
         const R nj[3] = {nrj.x, nrj.y, nrj.z};
         if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return false;
-        aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
+        if constexpr (WEN32) aw = wendland_aw<D - 1>(dist, hij);
+        else aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
       }
-      const R rho_j = r_fabs(b1.w);
-      const R vol_ij = vol_i + r_rcp(rho_j * rho_j);
+      const R vol_ij = vol_i + r_fabs(b1.w);
       if (STAGE == 1) {
         const R P_ij = sum * vol_ij;
         for (int d = 0; d < D; d++) F[d] = F[d] + (dr[d] * aw) * -P_ij;
@@ -1757,10 +1778,16 @@ class Engine : public EngineBase {
     have_work_ = true;
     mark(5);
     if (phase < MRSPH_PHASE_FORCE1) return 0;
-    k_force<D, R, 1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    if (sizeof(R) == 4 && kc_.prm.kernel == K_WEN)
+      k_force<D, R, 1, (sizeof(R) == 4 ? K_WEN : -1)><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    else
+      k_force<D, R, 1, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
     mark(6);
     if (phase < MRSPH_PHASE_FORCE2) return 0;
-    k_force<D, R, 2><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    if (sizeof(R) == 4 && kc_.prm.kernel == K_WEN)
+      k_force<D, R, 2, (sizeof(R) == 4 ? K_WEN : -1)><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    else
+      k_force<D, R, 2, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
     mark(7);
     MR_CK(cudaGetLastError());
     return 0;
