@@ -1540,8 +1540,8 @@ class Engine : public EngineBase {
     DevScalars h;
     MR_CK(cudaMemcpyAsync(&h, kc_.sc, sizeof(h), cudaMemcpyDeviceToHost, st_));
     MR_CK(cudaStreamSynchronize(st_));
-    unsigned zero = 0;
-    MR_CK(cudaMemcpy(&kc_.sc->flags, &zero, sizeof(unsigned), cudaMemcpyHostToDevice));
+    // cleared on the engine stream, ordered before the next step's kernels
+    MR_CK(cudaMemsetAsync(&kc_.sc->flags, 0, sizeof(unsigned), st_));
     o->dt = bitsd_host(h.dt2);
     o->dt_stage1 = bitsd_host(h.dt1);
     o->max_v = bitsd_host(h.vmax2);
@@ -1867,7 +1867,10 @@ class Engine : public EngineBase {
           return MRSPH_ERR_OOM;
         }
         anc_allocs_.push_back(dv);
-        if (cudaMemcpy(dv, t.data(), sizeof(int2) * na, cudaMemcpyHostToDevice) != cudaSuccess) {
+        // on the engine stream (the kernels that read the table run there) and
+        // complete before the host vector goes out of scope
+        if (cudaMemcpyAsync(dv, t.data(), sizeof(int2) * na, cudaMemcpyHostToDevice, st_) != cudaSuccess ||
+            cudaStreamSynchronize(st_) != cudaSuccess) {
           err = "cudaMemcpy failed (anchor tables)";
           return MRSPH_ERR_CUDA;
         }

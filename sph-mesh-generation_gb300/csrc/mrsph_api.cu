@@ -184,7 +184,9 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
     double init_d[3] = {0.0, 0.0, 1.e20};
     unsigned long long init[3];
     std::memcpy(init, init_d, sizeof(init));
-    API_CK(h, cudaMemcpy(d_max, init, sizeof(init), cudaMemcpyHostToDevice));
+    // ordered before the level-set build kernels on the handle's stream
+    API_CK(h, cudaMemcpyAsync(d_max, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    API_CK(h, cudaStreamSynchronize(h->stream));
   }
   LsSet& ls = h->ls;
   std::memset(&ls, 0, sizeof(ls));
