@@ -8,6 +8,7 @@ write the same files, under the same names, a reference run writes:
 
   outdata/particle_rank_<r>_step_<n>.vtu, particle_step_<n>.pvtu, particle.pvd
   outdata/mesh_tris_rank_<r>_step_<n>.vtu, mesh_tris_step_<n>.pvtu, mesh_tris.pvd
+  outdata/mesh_lset_rank_<r>_step_<n>.vti, mesh_lset_step_<n>.pvti, mesh_lset.pvd
   rstfile_particles/step_<run_time>_rank_<r>.pst, rstfile_particles/list.csv
 
 VTU files are VTK XML UnstructuredGrid pieces with raw appended data: every
@@ -287,6 +288,128 @@ class MeshWriter:
             f.write(_pvtu_text([piece], _fields_meta(pd), _fields_meta(cd)))
         t = sim.stats()["step"] if run_time is None else run_time
         update_pvd(os.path.join(self.outdir, "mesh_tris.pvd"), n_out, t, f"./{pvtu}")
+        return os.path.join(self.outdir, piece)
+
+
+# ---------------------------------------------------------- level-set output
+def vti_bytes(extent: Sequence[int], origin: Sequence[float], spacing: Sequence[float],
+              point_data: Sequence[Tuple[str, np.ndarray]] = (),
+              cell_data: Sequence[Tuple[str, np.ndarray]] = ()) -> bytes:
+    """One VTK XML ImageData piece with raw appended arrays; extent is the
+    number of cells per axis (points are one more), arrays in x-fastest order."""
+    ext = " ".join(f"0 {int(e)}" for e in extent)
+    blobs: List[bytes] = []
+    offset = 0
+    head = ['<VTKFile type="ImageData" version="0.1" byte_order="LittleEndian">',
+            f' <ImageData WholeExtent="{ext}" Origin="{" ".join(repr(float(o)) for o in origin)}" '
+            f'Spacing="{" ".join(repr(float(h)) for h in spacing)}">',
+            f'  <Piece Extent="{ext}">']
+
+    def block(tag: str, fields: Sequence[Tuple[str, np.ndarray]]) -> None:
+        nonlocal offset
+        head.append(f'    <{tag} Vectors="vector">')
+        for name, arr in fields:
+            arr = _le(np.asarray(arr))
+            comps = 1 if arr.ndim <= 3 else arr.shape[-1]
+            head.append(f'      <DataArray type="{_VTK_TYPE[arr.dtype]}" Name="{name}" NumberOfComponents="{comps}" '
+                        f'format="appended" offset="{offset}"/>')
+            raw = arr.tobytes()
+            blobs.append(struct.pack("<I", len(raw)) + raw)
+            offset += 4 + len(raw)
+        head.append(f"    </{tag}>")
+
+    block("PointData", point_data)
+    block("CellData", cell_data)
+    head += ["  </Piece>", " </ImageData>", ' <AppendedData encoding="raw">']
+    return ("\n".join(head) + "\n _").encode("ascii") + b"".join(blobs) + \
+        "\n </AppendedData>\n</VTKFile>\n".encode("ascii")
+
+
+def corner_average(cells: np.ndarray, margin_cells: int, dim: int) -> np.ndarray:
+    """Values at the corners of a level's interior cells: the mean of the 2^D
+    cells around each corner (the margin supplies the outer ring), as
+    Output_vti_file_lset averages cell values (lset_binary_writer.cpp:87-130).
+    cells: (nz, ny, nx) with nz = 1 in 2D."""
+    m = margin_cells
+    if dim == 2:
+        c = cells[0]
+        inner = c[m - 1:c.shape[0] - m + 1, m - 1:c.shape[1] - m + 1]
+        return 0.25 * (inner[:-1, :-1] + inner[1:, :-1] + inner[:-1, 1:] + inner[1:, 1:])[None]
+    inner = cells[m - 1:cells.shape[0] - m + 1, m - 1:cells.shape[1] - m + 1, m - 1:cells.shape[2] - m + 1]
+    acc = np.zeros(tuple(s - 1 for s in inner.shape))
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                acc += inner[dz:dz + acc.shape[0], dy:dy + acc.shape[1], dx:dx + acc.shape[2]]
+    return 0.125 * acc
+
+
+def cell_scale(sim, level: int) -> np.ndarray:
+    """Levelset::Get_scale (level_set.cpp:311-351) on every cell of a level:
+    the tanh law of phi, or the curvature law (|curvature| range over the CUT
+    cells of all levels) when the case selects it."""
+    prm = sim.case.params
+    dim = prm["dim"]
+    lv = sim.case.levels[level]
+    f = sim.levelset_fields(level)
+    phi = lv.phi
+    mp = f["max_phi"]
+    dl0 = min(sim.case.levels[0].dpkg[d] / 4.0 for d in range(dim))
+    lo = np.full(phi.shape, float(prm["min_dl"]))
+    if prm.get("scale_law", 0) == 1:
+        cut = [sim.levelset_fields(l) for l in range(len(sim.case.levels))]
+        vals = np.concatenate([np.abs(g["curv"][g["tag"] == 1]) for g in cut])
+        cmax, cmin = (vals.max(), vals.min()) if vals.size else (0.0, 1e20)
+        mid = prm.get("middle_dl", 0.0) or 5.0 * dl0
+        q = np.clip((cmax - np.abs(f["curv"])) / (cmax - cmin + 1e-20), 0.0, 1.0)
+        lo = prm["min_dl"] + q * q * (mid - prm["min_dl"])
+    s = lo + np.tanh(2.5 * np.abs(phi) / mp) / np.tanh(2.5) * (prm["max_dl"] - lo)
+    return np.where((phi > 0) | (np.abs(phi) < dl0), s, prm["min_dl"])
+
+
+class LevelSetWriter:
+    """Level_set_binary_writer (lset_binary_writer.cpp:12-510) for one level:
+    an ImageData piece over the level's interior cells with phi, curv and
+    scale at the cell corners and the cut-cell tag ('interface') and
+    characteristic tag ('char', none in these geometries) per cell, its PVTI
+    and the mesh_lset.pvd collection.  The reference's cut-cell 'vol' and
+    'area' fields need its cut-cell geometry (not built) and are left out."""
+
+    def __init__(self, outdir: str = "outdata"):
+        self.outdir = outdir
+
+    def Output_lset(self, n_out: int, sim, level: int = 0, run_time: Optional[float] = None) -> str:
+        os.makedirs(self.outdir, exist_ok=True)
+        dim = sim.case.params["dim"]
+        lv = sim.case.levels[level]
+        f = sim.levelset_fields(level)
+        m = 4 * lv.margin
+        ncell = [4 * lv.num_pkg[d] if d < dim else 0 for d in range(3)]
+        spacing = [lv.dpkg[d] / 4.0 if d < dim else 1.0 for d in range(3)]
+        origin = [lv.box_l[d] if d < dim else 0.0 for d in range(3)]
+        pd = [("phi", corner_average(lv.phi, m, dim).astype("<f4")),
+              ("curv", corner_average(f["curv"], m, dim).astype("<f4")),
+              ("scale", corner_average(cell_scale(sim, level), m, dim).astype("<f4"))]
+        sl = (slice(None),) if dim == 2 else (slice(m, -m),)
+        tag = f["tag"][sl + (slice(m, -m), slice(m, -m))].astype("<i4")
+        cd = [("interface", tag), ("char", np.zeros_like(tag))]
+        piece = f"mesh_lset_rank_0_step_{n_out}.vti"
+        with open(os.path.join(self.outdir, piece), "wb") as fh:
+            fh.write(vti_bytes(ncell, origin, spacing, pd, cd))
+        pvti = f"mesh_lset_step_{n_out}.pvti"
+        ext = " ".join(f"0 {e}" for e in ncell)
+        with open(os.path.join(self.outdir, pvti), "w") as fh:
+            fh.write(f'<VTKFile type="PImageData" version="0.1" byte_order="LittleEndian">\n'
+                     f' <PImageData WholeExtent="{ext}" GhostLevel="0" Origin="{" ".join(map(repr, map(float, origin)))}" '
+                     f'Spacing="{" ".join(map(repr, map(float, spacing)))}">\n  <PPointData>\n')
+            for name, t, c in _fields_meta(pd):
+                fh.write(f'    <PDataArray type="{t}" Name="{name}" NumberOfComponents="{c}"/>\n')
+            fh.write("  </PPointData>\n  <PCellData>\n")
+            for name, t, c in _fields_meta(cd):
+                fh.write(f'    <PDataArray type="{t}" Name="{name}" NumberOfComponents="{c}"/>\n')
+            fh.write(f'  </PCellData>\n  <Piece Extent="{ext}" Source="{piece}"/>\n </PImageData>\n</VTKFile>\n')
+        t = sim.stats()["step"] if run_time is None else run_time
+        update_pvd(os.path.join(self.outdir, "mesh_lset.pvd"), n_out, t, f"./{pvti}")
         return os.path.join(self.outdir, piece)
 
 

@@ -1,6 +1,7 @@
 """Writers and restarts through a live GPU handle: the particle VTU, the
-triangle-mesh VTU and the .pst restart read back equal to the engine's
-state, and a restart loaded into a new handle reproduces the positions."""
+triangle-mesh VTU, the level-set VTI and the .pst restart read back equal to
+the engine's state, and a restart loaded into a new handle reproduces the
+positions."""
 import numpy as np
 import pytest
 
@@ -27,6 +28,11 @@ def test_writers_and_restart_round_trip(tmp_path):
     m = io.read_vtu(io.MeshWriter(str(tmp_path / "outdata")).Output_mesh(0, g, tris=tris))
     assert np.array_equal(m["connectivity"].reshape(-1, 3), np.asarray(tris))
     assert len(m["vol"]) == len(tris) and np.all(m["aspect"] >= 1.0)
+    lf = io.read_vtu(io.LevelSetWriter(str(tmp_path / "outdata")).Output_lset(0, g))
+    f0 = g.levelset_fields(0)
+    mm = 4 * case.levels[0].margin
+    assert lf["interface"].sum() == (f0["tag"][0, mm:-mm, mm:-mm] == 1).sum() > 0
+    assert np.allclose(lf["curv"], io.corner_average(f0["curv"], mm, 2).ravel().astype(np.float32))
     pst = io.save_particle_post_file(g, str(tmp_path), first=True)
     assert np.array_equal(io.read_pst(pst), p["xyz"])
     g.close()

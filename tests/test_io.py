@@ -122,3 +122,43 @@ def test_mesh_writer_and_quality(tmp_path):
     assert np.array_equal(r["connectivity"], tris.reshape(-1)) and np.array_equal(r["types"], [5, 5])
     assert np.allclose(r["vol"], 0.5) and np.allclose(r["aspect"], np.sqrt(2))
     assert 'timestep="3"' in (tmp_path / "mesh_tris.pvd").read_text()
+
+
+def test_corner_average_and_levelset_writer(tmp_path):
+    from mrsph import cases
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    lv = case.levels[0]
+    m = 4 * lv.margin
+    # a linear phi averages to its value at the corners
+    ny, nx = lv.phi.shape[1:]
+    xc = np.arange(nx)[None, :] + 0.0 * np.arange(ny)[:, None]
+    lin = (2.0 * xc + 3.0 * np.arange(ny)[:, None])[None]
+    cor = io.corner_average(lin, m, 2)
+    assert cor.shape == (1, ny - 2 * m + 1, nx - 2 * m + 1)
+    assert np.allclose(cor[0, 0, 0], 2.0 * (m - 0.5) + 3.0 * (m - 0.5))
+
+    class LsSim(FakeSim):
+        def __init__(self):
+            super().__init__()
+            self.case = case
+
+        def levelset_fields(self, level):
+            shp = case.levels[level].phi.shape
+            tag = (np.abs(case.levels[level].phi) < 0.02).astype(np.uint8)
+            return {"curv": np.ones(shp), "tag": tag, "max_phi": float(case.levels[level].phi.max()),
+                    "nx": np.zeros(shp), "ny": np.zeros(shp), "nz": np.zeros(shp)}
+
+    sim = LsSim()
+    f = io.LevelSetWriter(str(tmp_path)).Output_lset(0, sim, run_time=0)
+    r = io.read_vtu(f)
+    nc = 4 * lv.num_pkg[0]
+    assert r["phi"].size == (nc + 1) * (4 * lv.num_pkg[1] + 1)
+    assert np.allclose(r["phi"].reshape(cor.shape[1:]), io.corner_average(lv.phi, m, 2)[0].astype(np.float32))
+    assert np.allclose(r["curv"], 1.0)
+    assert r["interface"].size == nc * 4 * lv.num_pkg[1]
+    assert r["interface"].sum() == sim.levelset_fields(0)["tag"][0, m:-m, m:-m].sum()
+    sc = r["scale"]
+    assert sc.min() >= case.params["min_dl"] - 1e-7 and sc.max() <= case.params["max_dl"] + 1e-7
+    head = open(f, "rb").read().split(b"<AppendedData")[0].decode()
+    assert f'WholeExtent="0 {nc} 0 {4 * lv.num_pkg[1]} 0 0"' in head
+    assert (tmp_path / "mesh_lset_step_0.pvti").exists() and (tmp_path / "mesh_lset.pvd").exists()
