@@ -4,7 +4,8 @@
 // One iteration = six kernels:
 //   k_cvp_assign    nearest VP per point, strict '<' (Get_CPU_id, voronoi.cpp:480-493)
 //   k_cvp_partials  per (VP, 2048-point chunk) mass, mass centre and energy,
-//                   points in order (voronoi.cpp:617-631)
+//                   points in order (voronoi.cpp:617-631); one block per chunk
+//                   groups its points by VP first
 //   k_cvp_reduce    per VP: chunk partials in order, centroid, pressure, error
 //   k_cvp_planes    bisector plane of every VP pair
 //   k_cvp_faces     per (VP, plane) the exact Voronoi face inside the box: the
@@ -118,16 +119,23 @@ __global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int K,
   if (i >= n) return;
   double x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
   const float xf[3] = {(float)x[0], (float)x[1], D == 3 ? (float)x[2] : 0.f};
-  float bf = 3.4e38f;
+  float bf = 3.4e38f, b2 = 3.4e38f;  // smallest and second smallest FP32 distance
+  int bk = 0;
   for (int k = 0; k < K; k++) {
     const float4 v = s_vf[k];
     const float dx = xf[0] - v.x, dy = xf[1] - v.y, dz = D == 3 ? xf[2] - v.z : 0.f;
-    bf = fminf(bf, dx * dx + dy * dy + dz * dz);
+    const float dd = dx * dx + dy * dy + dz * dz;
+    if (dd < bf) { b2 = bf; bf = dd; bk = k; }
+    else if (dd < b2) b2 = dd;
   }
   const float L = fmaxf(s_lvp, fmaxf(fabsf(xf[0]), fmaxf(fabsf(xf[1]), fabsf(xf[2]))));
   const float df = sqrtf(bf);
   const float thr = df + 2.e-6f * (L + df) + 1.e-30f;
   const float T = thr * thr * 1.0001f;
+  if (b2 > T) {  // no other VP within the bound: the FP64 scan would pick bk
+    label[i] = bk;
+    return;
+  }
   double best = 1.e20;
   int idx = 0;
   for (int k = 0; k < K; k++) {
@@ -156,28 +164,84 @@ __global__ void k_cvp_target(long long nchunk, const double* tm, int K, CvpState
   st->target = t / K;
 }
 
-// thread (k, chunk c): points of the chunk in order
-__global__ void k_cvp_partials(long long n, const double* __restrict__ xyz, const double* __restrict__ pm,
-                               const int* __restrict__ label, int K, const double* __restrict__ vp, int D,
-                               double* __restrict__ part) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  long long c = blockIdx.y;
-  if (k >= K) return;
-  const double ck[3] = {vp[3 * k], vp[3 * k + 1], vp[3 * k + 2]};
-  double m = 0.0, x = 0.0, y = 0.0, z = 0.0, e = 0.0;
-  long long end = min(n, (c + 1) * (long long)CVP_CHUNK);
-  for (long long i = c * CVP_CHUNK; i < end; i++) {
-    if (__ldg(&label[i]) != k) continue;
-    double w = pm[i];
-    const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
-    m += w;
-    x = x + p[0] * w;
-    y = y + p[1] * w;
-    z = z + p[2] * w;
-    e += w * cdist(D, ck, p);
+// Per 2048-point chunk (one block): the chunk's points grouped by VP in point
+// order (a stable counting sort in shared memory), then each VP's mass, mass
+// centre and energy summed over its points in order, so every (VP, chunk)
+// partial adds the same points in the same order as a scan of the chunk per
+// VP would, in O(chunk) work instead of O(K x chunk).
+__global__ void __launch_bounds__(256) k_cvp_partials(long long n, const double* __restrict__ xyz,
+                                                      const double* __restrict__ pm,
+                                                      const int* __restrict__ label, int K,
+                                                      const double* __restrict__ vp, int D,
+                                                      double* __restrict__ part) {
+  __shared__ int s_lab[CVP_CHUNK];
+  __shared__ short s_list[CVP_CHUNK];
+  __shared__ int s_start[CVP_MAX_K + 1];
+  __shared__ int s_cur[CVP_MAX_K];
+  const long long c = blockIdx.x;
+  const long long b = c * (long long)CVP_CHUNK;
+  const int m = (int)min((long long)CVP_CHUNK, n - b);
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int k = tid; k < K; k += blockDim.x) s_cur[k] = 0;
+  __syncthreads();
+  for (int t = tid; t < m; t += blockDim.x) {
+    const int l = __ldg(&label[b + t]);
+    s_lab[t] = l;
+    atomicAdd(&s_cur[l], 1);
   }
-  double* q = part + ((size_t)c * K + k) * 5;
-  q[0] = m; q[1] = x; q[2] = y; q[3] = z; q[4] = e;
+  __syncthreads();
+  if (tid < 32) {  // exclusive scan of the counts; s_cur becomes each VP's fill cursor
+    int run = 0;
+    for (int k0 = 0; k0 < K; k0 += 32) {
+      const int k = k0 + lane;
+      const int v = k < K ? s_cur[k] : 0;
+      int inc = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+      }
+      if (k < K) {
+        s_start[k] = run + inc - v;
+        s_cur[k] = run + inc - v;
+      }
+      run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) s_start[K] = run;
+    __syncwarp();
+    // stable fill: 32 points at a time in point order; lanes with the same VP
+    // take consecutive slots in lane order
+    for (int t0 = 0; t0 < m; t0 += 32) {
+      const int t = t0 + lane;
+      const bool ok = t < m;
+      const unsigned act = __ballot_sync(0xffffffffu, ok);
+      if (ok) {
+        const int l = s_lab[t];
+        const unsigned peers = __match_any_sync(act, l);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        s_list[s_cur[l] + rank] = (short)t;
+        __syncwarp(act);
+        if (rank == 0) s_cur[l] += __popc(peers);
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int k = tid; k < K; k += blockDim.x) {
+    const double ck[3] = {vp[3 * k], vp[3 * k + 1], vp[3 * k + 2]};
+    double ms = 0.0, x = 0.0, y = 0.0, z = 0.0, en = 0.0;
+    for (int q = s_start[k]; q < s_start[k + 1]; q++) {
+      const long long i = b + s_list[q];
+      const double w = pm[i];
+      const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+      ms += w;
+      x = x + p[0] * w;
+      y = y + p[1] * w;
+      z = z + p[2] * w;
+      en += w * cdist(D, ck, p);
+    }
+    double* o = part + ((size_t)c * K + k) * 5;
+    o[0] = ms; o[1] = x; o[2] = y; o[3] = z; o[4] = en;
+  }
 }
 
 __global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __restrict__ part,
@@ -209,7 +273,8 @@ __global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __res
 }
 
 // bisector planes of every VP pair, computed once per iteration
-__global__ void k_cvp_planes(CvpGeo G, const double* __restrict__ vp, double* __restrict__ planes) {
+__global__ void k_cvp_planes(CvpGeo G, const double* __restrict__ vp, double* __restrict__ planes,
+                             float4* __restrict__ planes_f) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)G.K * G.K) return;
   int k = (int)(t / G.K), m = (int)(t % G.K);
@@ -218,6 +283,7 @@ __global__ void k_cvp_planes(CvpGeo G, const double* __restrict__ vp, double* __
   cplane(G, vp, k, m, n, &d);
   double* o = planes + 4 * t;
   o[0] = n[0]; o[1] = n[1]; o[2] = n[2]; o[3] = d;
+  planes_f[t] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)d);
 }
 
 // bounding sphere of a polygon (centre = vertex mean)
@@ -237,9 +303,12 @@ __device__ inline void cbound(double (*v)[3], int nv, double* C, double* r) {
 // face of VP k on plane p; out: exists, area, n (3), dist.  A clip whose
 // plane lies beyond the polygon's bounding sphere (with a 1e-9 relative
 // margin) would keep every vertex in order, so it is skipped: the result is
-// the one of clipping by every plane in turn.
+// the one of clipping by every plane in turn.  A bisector is first tested in
+// FP32 with a margin (4e-6 of the magnitudes) far above the FP32 rounding, so
+// an FP32 skip is always an FP64 skip; the others take the FP64 test.
 __global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __restrict__ vp,
-                                                   const double* __restrict__ planes, double* __restrict__ face) {
+                                                   const double* __restrict__ planes,
+                                                   const float4* __restrict__ planes_f, double* __restrict__ face) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)G.K * G.NP) return;
   int k = (int)(t / G.NP), p = (int)(t % G.NP);
@@ -281,6 +350,8 @@ __global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __res
   int nv = 4;
   double C[3], r;
   cbound(A, nv, C, &r);
+  float Cf[3] = {(float)C[0], (float)C[1], (float)C[2]}, rf = (float)r;
+  const float Sf = (float)S;
   auto clip = [&](const double* cn, double cd) {
     const double sc = cdot(cn, C) - cd;
     if (sc + r < -1.e-9 * (fabs(cd) + fabs(cdot(cn, C)) + r + S)) return;  // all vertices inside
@@ -289,6 +360,8 @@ __global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __res
     A = B;
     B = tmp;
     cbound(A, nv, C, &r);
+    Cf[0] = (float)C[0]; Cf[1] = (float)C[1]; Cf[2] = (float)C[2];
+    rf = (float)r;
   };
   for (int wq = 0; wq < 6 && nv > 0; wq++) {
     if (p >= G.K && wq == p - G.K) continue;
@@ -299,8 +372,13 @@ __global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __res
     clip(wn, wd);
   }
   const double* pk = planes + 4 * (long long)k * G.K;
+  const float4* pkf = planes_f + (long long)k * G.K;
   for (int m = 0; m < G.K && nv > 0; m++) {
     if (m == k || m == p) continue;
+    const float4 pf = __ldg(&pkf[m]);
+    const float scf = (pf.x * Cf[0] + pf.y * Cf[1] + pf.z * Cf[2]) - pf.w;
+    const float magf = fabsf(pf.w) + (fabsf(Cf[0]) + fabsf(Cf[1]) + fabsf(Cf[2])) + rf + Sf;
+    if (scf + rf < -4.001e-6f * magf) continue;  // the FP64 test skips it as well
     const double bn[3] = {pk[4 * m], pk[4 * m + 1], pk[4 * m + 2]};
     clip(bn, pk[4 * m + 3]);
   }
@@ -466,6 +544,7 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
   int rc = 0;
   std::vector<void*> mem;
   double *d_vp = nullptr, *d_part = nullptr, *d_face = nullptr, *d_k = nullptr, *d_tm = nullptr, *d_planes = nullptr;
+  float4* d_planes_f = nullptr;
   int* d_label = nullptr;
   CvpState* d_st = nullptr;
   CvpState hs;
@@ -480,6 +559,7 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
   CV_CK(A((void**)&d_part, sizeof(double) * 5 * K * nchunk));
   CV_CK(A((void**)&d_face, sizeof(double) * 6 * (size_t)K * G.NP));
   CV_CK(A((void**)&d_planes, sizeof(double) * 4 * (size_t)K * K));
+  CV_CK(A((void**)&d_planes_f, sizeof(float4) * (size_t)K * K));
   CV_CK(A((void**)&d_k, sizeof(double) * 12 * K));  // mass, mc(3), energy, P, err, f(3), hk, pad
   CV_CK(A((void**)&d_tm, sizeof(double) * nchunk));
   CV_CK(A((void**)&d_label, sizeof(int) * n));
@@ -498,11 +578,10 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
     int it = 0;
     for (; it <= p->max_iter; it++) {
       k_cvp_assign<<<nb, 256, 0, s>>>(n, d_xyz, K, d_vp, D, d_label);
-      dim3 g((K + 63) / 64, (unsigned)nchunk);
-      k_cvp_partials<<<g, 64, 0, s>>>(n, d_xyz, d_pm, d_label, K, d_vp, D, d_part);
+      k_cvp_partials<<<(unsigned)nchunk, 256, 0, s>>>(n, d_xyz, d_pm, d_label, K, d_vp, D, d_part);
       k_cvp_reduce<<<(K + 127) / 128, 128, 0, s>>>(nchunk, K, D, d_part, d_st, d_vp, mass, mc, energy, P, err);
-      k_cvp_planes<<<(K * K + 255) / 256, 256, 0, s>>>(G, d_vp, d_planes);
-      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_planes, d_face);
+      k_cvp_planes<<<(K * K + 255) / 256, 256, 0, s>>>(G, d_vp, d_planes, d_planes_f);
+      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_planes, d_planes_f, d_face);
       k_cvp_update<<<1, (K + 31) / 32 * 32, 0, s>>>(G, d_vp, d_face, mass, mc, energy, P, err, f, hk, vp3, d_st,
                                                    p->error_tolerance, p->pressure_step);
       CV_CK(cudaGetLastError());
