@@ -1,0 +1,347 @@
+// sph_mesh_generation.cpp — C++ host layer over the C ABI (see the header).
+#include "sph_mesh_generation.hpp"
+
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+
+namespace mrsph_host {
+
+namespace {
+constexpr double PI_REF = 3.1415926;  // glbparam.h:186
+
+std::string last_error(mrsph_handle* h) {
+  char buf[512] = {0};
+  mrsph_last_error(h, buf, sizeof(buf));
+  return std::string(buf);
+}
+
+void make_dir(const std::string& d) { mkdir(d.c_str(), 0755); }
+}  // namespace
+
+mrsph_params default_params(int dim) {
+  mrsph_params p{};
+  p.dim = dim;
+  p.kernel = MRSPH_KERNEL_HYPERBOLIC;
+  p.precision = MRSPH_FP64_PLAIN;
+  p.cell_ratio = dim == 2 ? 2.0 : 1.45;
+  p.cutoff = 2.0;
+  p.angle_thres = PI_REF * 0.4;
+  p.nu_coeff = 0.1;
+  p.damp_coeff = 0.0;
+  p.min_dl = 0.01;
+  p.max_dl = 0.01;
+  for (int d = 0; d < 3; d++) {
+    p.box_l[d] = 0.0;
+    p.box_r[d] = 1.0;
+  }
+  p.seed = 0;
+  p.neighbor_cap = 0;
+  p.device = 0;
+  p.scale_law = 0;
+  p.middle_dl = 0.0;
+  return p;
+}
+
+LevelGrid make_level(const std::function<double(double, double, double)>& sdf, int dim,
+                     const std::array<double, 3>& box_l, const std::array<double, 3>& dpkg,
+                     const std::array<int, 3>& num_pkg, int margin) {
+  LevelGrid L;
+  L.box_l = box_l;
+  L.dpkg = dpkg;
+  L.num_pkg = num_pkg;
+  L.margin = margin;
+  std::array<std::vector<double>, 3> ax;
+  for (int d = 0; d < 3; d++) {
+    if (d >= dim) {
+      ax[d] = {0.0};
+      continue;
+    }
+    const double dcell = dpkg[d] / 4.0;
+    for (int pk = -margin; pk < num_pkg[d] + margin; pk++)
+      for (int cl = 0; cl < 4; cl++) ax[d].push_back((double)pk * dpkg[d] + ((double)cl + 0.5) * dcell + box_l[d]);
+  }
+  L.phi.reserve(ax[0].size() * ax[1].size() * ax[2].size());
+  for (double z : ax[2])
+    for (double y : ax[1])
+      for (double x : ax[0]) L.phi.push_back(sdf(x, y, z));
+  return L;
+}
+
+// package mask of a finer nested level: active where some cell has |phi| < band
+static std::vector<unsigned char> nested_active(const LevelGrid& L, double band, int dim) {
+  const int m = L.margin;
+  const int nx = L.num_pkg[0] + 2 * m, ny = L.num_pkg[1] + 2 * m, nz = dim == 3 ? L.num_pkg[2] + 2 * m : 1;
+  const int cx = 4 * nx, cy = 4 * ny;
+  std::vector<unsigned char> act((size_t)nx * ny * nz, 0);
+  for (int pz = 0; pz < nz; pz++)
+    for (int py = 0; py < ny; py++)
+      for (int px = 0; px < nx; px++) {
+        double mn = 1e300;
+        for (int c = 0; c < (dim == 3 ? 4 : 1); c++)
+          for (int b = 0; b < 4; b++)
+            for (int a = 0; a < 4; a++) {
+              const int z = dim == 3 ? 4 * pz + c : 0;
+              mn = std::min(mn, std::fabs(L.phi[((size_t)z * cy + (4 * py + b)) * cx + (4 * px + a)]));
+            }
+        act[((size_t)pz * ny + py) * nx + px] = mn < band ? 1 : 0;
+      }
+  return act;
+}
+
+static double max_phi(const std::vector<LevelGrid>& levels, int dim) {
+  double mp = 0.0;
+  for (const auto& L : levels) {
+    const int m = 4 * L.margin;
+    const int cx = 4 * (L.num_pkg[0] + 2 * L.margin), cy = 4 * (L.num_pkg[1] + 2 * L.margin);
+    const int cz = dim == 3 ? 4 * (L.num_pkg[2] + 2 * L.margin) : 1;
+    for (int z = (dim == 3 ? m : 0); z < (dim == 3 ? cz - m : 1); z++)
+      for (int y = m; y < cy - m; y++)
+        for (int x = m; x < cx - m; x++) {
+          const double v = L.phi[((size_t)z * cy + y) * cx + x];
+          if (v > 0) mp = std::max(mp, v);
+        }
+  }
+  return mp;
+}
+
+long long particle_count(const std::vector<LevelGrid>& levels, const mrsph_params& p) {
+  const int dim = p.dim;
+  const double mp = max_phi(levels, dim);
+  const LevelGrid& F = levels.back();
+  double dl0 = 1e20;
+  for (int d = 0; d < dim; d++) dl0 = std::min(dl0, levels[0].dpkg[d] / 4.0);
+  double dV = 1.0;
+  for (int d = 0; d < dim; d++) dV *= F.dpkg[d] / 4.0;
+  const int m = 4 * F.margin;
+  const int cx = 4 * (F.num_pkg[0] + 2 * F.margin), cy = 4 * (F.num_pkg[1] + 2 * F.margin);
+  const int cz = dim == 3 ? 4 * (F.num_pkg[2] + 2 * F.margin) : 1;
+  double tot = 0.0;
+  for (int z = (dim == 3 ? m : 0); z < (dim == 3 ? cz - m : 1); z++)
+    for (int y = m; y < cy - m; y++)
+      for (int x = m; x < cx - m; x++) {
+        const double phi = F.phi[((size_t)z * cy + y) * cx + x];
+        if (!(phi > 0)) continue;
+        // Levelset::Get_scale, level_set.cpp:311-351 (tanh law)
+        const double s = p.min_dl + std::tanh(2.5 * std::fabs(phi) / mp) / std::tanh(2.5) * (p.max_dl - p.min_dl);
+        tot += dV / std::pow(s, dim);
+      }
+  return (long long)tot;
+}
+
+bool cell_levels_consistent(const double* box_l, const double* box_r, int dim, double max_scale,
+                            double min_scale) {
+  double dom[3], st = 1e300;
+  for (int d = 0; d < dim; d++) {
+    dom[d] = box_r[d] - box_l[d];
+    st = std::min(st, dom[d]);
+  }
+  const double temp = std::floor(st / max_scale);
+  if (temp < 1) return false;
+  const double ini = st / temp;
+  double sc = ini;
+  int nl = 1;
+  while (sc + 1.e-6 > min_scale) {
+    sc /= 2;
+    nl++;
+  }
+  nl -= 1;
+  int n0[3];
+  for (int d = 0; d < dim; d++) n0[d] = (int)(dom[d] / ini);
+  for (int l = 0; l < nl; l++) {
+    double s = 1e300;
+    for (int d = 0; d < dim; d++) s = std::min(s, dom[d] / (n0[d] * std::ldexp(1.0, l)));
+    if (std::fabs(s - std::ldexp(ini, -l)) > 1.e-10) return false;
+  }
+  return true;
+}
+
+Case disc_hole_2d(double spacing, int grid, int kernel, double h_over_dx, int precision, unsigned long long seed) {
+  Case c;
+  c.name = "disc_hole_2d";
+  mrsph_params p = default_params(2);
+  const int npkg_unit = grid / 4;
+  const double dpkg = 1.0 / npkg_unit;
+  const double cell_ratio = 2.0 * h_over_dx;
+  int margin_pkg = std::max(npkg_unit / 16, 1);
+  for (;;) {
+    const double bl[2] = {-margin_pkg * dpkg, -margin_pkg * dpkg};
+    const double br[2] = {1.0 + margin_pkg * dpkg, 1.0 + margin_pkg * dpkg};
+    if (cell_levels_consistent(bl, br, 2, spacing * cell_ratio, spacing * cell_ratio)) break;
+    margin_pkg++;
+  }
+  const double lo = -margin_pkg * dpkg, hi = 1.0 + margin_pkg * dpkg;
+  const int npkg = npkg_unit + 2 * margin_pkg;
+  p.kernel = kernel;
+  p.precision = precision;
+  p.min_dl = spacing;
+  p.max_dl = spacing;
+  p.cell_ratio = cell_ratio;
+  p.box_l[0] = p.box_l[1] = lo;
+  p.box_r[0] = p.box_r[1] = hi;
+  p.box_l[2] = p.box_r[2] = 0.0;
+  p.seed = seed;
+  auto sdf = [](double X, double Y, double) {
+    const double disc = std::sqrt((X - 0.5) * (X - 0.5) + (Y - 0.5) * (Y - 0.5)) - 0.2;
+    return std::min(std::min(std::min(X, 1.0 - X), std::min(Y, 1.0 - Y)), disc);
+  };
+  c.params = p;
+  c.levels.push_back(make_level(sdf, 2, {lo, lo, 0.0}, {dpkg, dpkg, 1.0}, {npkg, npkg, 1}));
+  c.n_particles = particle_count(c.levels, p);
+  c.steps = 200;
+  return c;
+}
+
+Case torus_3d(double dx_min, double dx_max, int kernel, double h_over_dx, int precision, unsigned long long seed,
+              int fine_pkg, int nlevels) {
+  Case c;
+  c.name = "torus_3d";
+  mrsph_params p = default_params(3);
+  const int npx0 = fine_pkg >> (nlevels - 1);
+  const double dpkg0 = 3.2 / npx0;
+  const int npz0 = (int)std::nearbyint(1.2 / dpkg0);
+  const double zhalf = 0.5 * npz0 * dpkg0;
+  const std::array<double, 3> box_l{{-1.6, -1.6, -zhalf}};
+  p.kernel = kernel;
+  p.precision = precision;
+  p.min_dl = dx_min;
+  p.max_dl = dx_max;
+  p.cell_ratio = 2.0 * h_over_dx;
+  p.box_l[0] = -1.6; p.box_l[1] = -1.6; p.box_l[2] = -zhalf;
+  p.box_r[0] = 1.6; p.box_r[1] = 1.6; p.box_r[2] = zhalf;
+  p.seed = seed;
+  if (!cell_levels_consistent(p.box_l, p.box_r, 3, dx_max * p.cell_ratio, dx_min * p.cell_ratio))
+    throw Error(MRSPH_ERR_ARG, "torus box gives an inconsistent cell-list level plan");
+  auto sdf = [](double X, double Y, double Z) {
+    const double a = std::sqrt(X * X + Y * Y) - 1.0;
+    return 0.35 - std::sqrt(a * a + Z * Z);
+  };
+  for (int l = 0; l < nlevels; l++) {
+    const int f = 1 << l;
+    const double dp = dpkg0 / f;
+    LevelGrid L = make_level(sdf, 3, box_l, {dp, dp, dp}, {npx0 * f, npx0 * f, npz0 * f});
+    if (l > 0) L.active = nested_active(L, 4.0 * (dp * 2 / 4.0), 3);
+    c.levels.push_back(std::move(L));
+  }
+  c.params = p;
+  c.n_particles = particle_count(c.levels, p);
+  c.steps = 500;
+  return c;
+}
+
+// ------------------------------------------------------------------ solver
+SPH_mesh_generation::SPH_mesh_generation(const Case& c, int device) : case_(c) {
+  case_.params.device = device;
+  if (int rc = mrsph_create(&case_.params, &h_)) throw Error(rc, "mrsph_create: " + last_error(nullptr));
+  std::vector<mrsph_levelset_level> lv(case_.levels.size());
+  for (size_t l = 0; l < lv.size(); l++) {
+    const LevelGrid& L = case_.levels[l];
+    for (int d = 0; d < 3; d++) {
+      lv[l].box_l[d] = L.box_l[d];
+      lv[l].dpkg[d] = L.dpkg[d];
+      lv[l].num_pkg[d] = L.num_pkg[d];
+    }
+    lv[l].margin = L.margin;
+    lv[l].phi = L.phi.data();
+    lv[l].active = L.active.empty() ? nullptr : L.active.data();
+  }
+  check(mrsph_set_levelset(h_, (int)lv.size(), lv.data()), "mrsph_set_levelset");
+}
+
+SPH_mesh_generation::~SPH_mesh_generation() {
+  if (h_) mrsph_destroy(h_);
+}
+
+void SPH_mesh_generation::check(int rc, const char* what) {
+  if (rc) throw Error(rc, std::string(what) + ": " + last_error(h_));
+}
+
+void SPH_mesh_generation::Initialize_case(long long n) {
+  n_ = n < 0 ? case_.n_particles : n;
+  check(mrsph_seed(h_, n_), "mrsph_seed");
+}
+
+void SPH_mesh_generation::SPH_run_mesh_generation(int nsteps) { check(mrsph_step(h_, nsteps), "mrsph_step"); }
+
+mrsph_stats SPH_mesh_generation::Stats() {
+  mrsph_stats s{};
+  check(mrsph_get_stats(h_, &s), "mrsph_get_stats");
+  return s;
+}
+
+double SPH_mesh_generation::Get_timestep() { return Stats().dt; }
+
+std::vector<double> SPH_mesh_generation::Positions() {
+  std::vector<double> xyz((size_t)3 * n_);
+  check(mrsph_download_positions(h_, xyz.data()), "mrsph_download_positions");
+  return xyz;
+}
+
+std::string SPH_mesh_generation::Save_particle_post_file(const std::string& root, long long run_time, bool first) {
+  const std::string dir = root + "/rstfile_particles";
+  make_dir(root);
+  make_dir(dir);
+  {
+    std::ofstream lst(dir + "/list.csv", first ? std::ios::trunc : std::ios::app);
+    if (first) lst << 1 << "\n";
+    lst << run_time << " " << n_ << "\n";
+  }
+  const std::string path = dir + "/step_" + std::to_string(run_time) + "_rank_0.pst";
+  write_pst(path, Positions());
+  return path;
+}
+
+void SPH_mesh_generation::Load_data_for_post(const std::string& pst, bool pre_run) {
+  std::vector<double> xyz = read_pst(pst);
+  mrsph_state_in st{};
+  st.xyz = xyz.data();
+  n_ = (long long)(xyz.size() / 3);
+  check(mrsph_set_state(h_, n_, &st, pre_run ? 1 : 0), "mrsph_set_state");
+}
+
+double Solver::SPH_Mesh_Generation_Solver(int total_steps, int output_interval, const std::string& output_root) {
+  double ms_total = 0.0;
+  int done = 0;
+  bool first = true;
+  const int chunk = output_interval > 0 ? output_interval : total_steps;
+  while (done < total_steps) {
+    const int k = std::min(chunk, total_steps - done);
+    double ms = 0.0;
+    int rc = mrsph_step_timed(sim_.handle(), k, &ms);
+    if (rc) throw Error(rc, "mrsph_step_timed: " + last_error(sim_.handle()));
+    ms_total += ms;
+    done += k;
+    if (!output_root.empty()) {
+      sim_.Save_particle_post_file(output_root, (long long)sim_.Stats().step, first);
+      first = false;
+    }
+  }
+  return ms_total;
+}
+
+void write_pst(const std::string& path, const std::vector<double>& xyz) {
+  std::ofstream f(path, std::ios::binary | std::ios::trunc);
+  if (!f) throw Error(MRSPH_ERR_ARG, "cannot write " + path);
+  const int32_t n = (int32_t)(xyz.size() / 3);
+  f.write(reinterpret_cast<const char*>(&n), sizeof(n));
+  f.write(reinterpret_cast<const char*>(xyz.data()), (std::streamsize)(sizeof(double) * xyz.size()));
+}
+
+std::vector<double> read_pst(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error(MRSPH_ERR_ARG, "cannot read " + path);
+  int32_t n = 0;
+  f.read(reinterpret_cast<char*>(&n), sizeof(n));
+  if (!f || n < 0) throw Error(MRSPH_ERR_ARG, path + ": bad particle count");
+  std::vector<double> xyz((size_t)3 * n);
+  f.read(reinterpret_cast<char*>(xyz.data()), (std::streamsize)(sizeof(double) * xyz.size()));
+  if (f.gcount() != (std::streamsize)(sizeof(double) * xyz.size()))
+    throw Error(MRSPH_ERR_ARG, path + ": truncated particle file");
+  return xyz;
+}
+
+}  // namespace mrsph_host

@@ -1,0 +1,132 @@
+// sph_mesh_generation.hpp — C++ host layer over the C ABI of mrsph_relax.h.
+//
+// It keeps the reference's host-side entry points for the relaxation path,
+// so a C++ driver written against the reference reads the same:
+//   SPH_mesh_generation (src/sph_mesh_generation/sph_mesh_generation.h:10-154):
+//     Initialize_case, SPH_run_mesh_generation, Get_timestep,
+//     Save_particle_post_file, Load_data_for_post;
+//   Solver::SPH_Mesh_Generation_Solver (src/solver.cpp:257-321): the step loop
+//     with periodic particle restarts.
+// The particle state lives on the GPU; these classes own one engine handle
+// each and translate its status codes into exceptions (the reference prints
+// and aborts).  Workloads are built here from analytic signed-distance
+// functions, as the Python workloads are (mrsph/cases.py), so the host layer
+// runs without Python.
+#pragma once
+
+#include <array>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mrsph_relax.h"
+
+namespace mrsph_host {
+
+// A level-set level (see mrsph_levelset_level): cell-centred phi incl.
+// margins, x fastest, positive inside; active: per package incl. margins, or
+// empty for all active.
+struct LevelGrid {
+  std::array<double, 3> box_l{{0, 0, 0}};
+  std::array<double, 3> dpkg{{1, 1, 1}};
+  std::array<int, 3> num_pkg{{1, 1, 1}};
+  int margin = 1;
+  std::vector<double> phi;
+  std::vector<unsigned char> active;
+};
+
+struct Case {
+  std::string name;
+  mrsph_params params{};
+  std::vector<LevelGrid> levels;
+  long long n_particles = 0;
+  int steps = 0;
+};
+
+// Reference defaults (sph_mesh_generation.cpp:688-703, glbparam.h:171-183).
+mrsph_params default_params(int dim);
+
+// Samples sdf(x, y, z) at the cell centres of one level (incl. margin packages).
+LevelGrid make_level(const std::function<double(double, double, double)>& sdf, int dim,
+                     const std::array<double, 3>& box_l, const std::array<double, 3>& dpkg,
+                     const std::array<int, 3>& num_pkg, int margin = 1);
+
+// Particle count from the spacing integral over phi > 0 of the finest level
+// (the reference's total_mass = sum vol / scale^D, lset_package.cpp:1283-1397,
+// without the cut-cell refinement), tanh spacing law.
+long long particle_count(const std::vector<LevelGrid>& levels, const mrsph_params& p);
+
+// True when the reference's level plan (sph.cpp:144-180) gives every cell-list
+// level a cell of max_scale / 2^l (the library rejects other domains).
+bool cell_levels_consistent(const double* box_l, const double* box_r, int dim, double max_scale,
+                            double min_scale);
+
+// Unit square minus a disc (r = 0.2 at (0.5, 0.5)), constant spacing.
+Case disc_hole_2d(double spacing = 0.01, int grid = 256, int kernel = MRSPH_KERNEL_WENDLAND,
+                  double h_over_dx = 1.3, int precision = MRSPH_FP64_PLAIN, unsigned long long seed = 0);
+// Inside of a torus (R = 1, r = 0.35) on nested level sets, tanh spacing law.
+Case torus_3d(double dx_min = 0.005, double dx_max = 0.02, int kernel = MRSPH_KERNEL_WENDLAND,
+              double h_over_dx = 1.3, int precision = MRSPH_FP32_SPLIT, unsigned long long seed = 0,
+              int fine_pkg = 64, int nlevels = 3);
+
+class Error : public std::runtime_error {
+ public:
+  Error(int code, const std::string& what) : std::runtime_error(what), code(code) {}
+  int code;
+};
+
+class SPH_mesh_generation {
+ public:
+  // The constructor and the level-set set-up of Initialize_case
+  // (sph_mesh_generation.cpp:8-152, 594-712): engine handle, level-set build.
+  explicit SPH_mesh_generation(const Case& c, int device = 0);
+  ~SPH_mesh_generation();
+  SPH_mesh_generation(const SPH_mesh_generation&) = delete;
+  SPH_mesh_generation& operator=(const SPH_mesh_generation&) = delete;
+
+  // Random_particle_distribution + Pre_run (sph_mesh_generation.cpp:1302-1367,
+  // 1010-1050); n < 0 takes the case's particle count.
+  void Initialize_case(long long n = -1);
+  // SPH_run_mesh_generation x nsteps (sph_mesh_generation.cpp:1371-1463).
+  void SPH_run_mesh_generation(int nsteps = 1);
+  // glbl_timestep after the last step (SPH::Get_timestep, sph.cpp:224-227).
+  double Get_timestep();
+  mrsph_stats Stats();
+  // Particle positions in id order, n x 3.
+  std::vector<double> Positions();
+  // rstfile_particles/step_<run_time>_rank_0.pst and list.csv under root
+  // (Save_particle_post_file, sph_mesh_generation.cpp:2624-2660).
+  std::string Save_particle_post_file(const std::string& root, long long run_time, bool first);
+  // Positions of a .pst file as the state (Load_data_for_post,
+  // sph_mesh_generation.cpp:426-590); with pre_run the map and Pre_run follow.
+  void Load_data_for_post(const std::string& pst, bool pre_run = true);
+
+  long long num_particles() const { return n_; }
+  mrsph_handle* handle() { return h_; }
+
+ private:
+  void check(int rc, const char* what);
+  mrsph_handle* h_ = nullptr;
+  Case case_;
+  long long n_ = 0;
+};
+
+// Solver::SPH_Mesh_Generation_Solver (src/solver.cpp:257-321): total_steps
+// relaxation steps, a particle restart every output_interval steps (and at
+// the end) when output_root is not empty.  Returns the device-timed
+// milliseconds of the steps.
+class Solver {
+ public:
+  explicit Solver(SPH_mesh_generation& sim) : sim_(sim) {}
+  double SPH_Mesh_Generation_Solver(int total_steps, int output_interval = 0, const std::string& output_root = "");
+
+ private:
+  SPH_mesh_generation& sim_;
+};
+
+// .pst restart files: int32 count, then x, y, z (float64) per particle.
+void write_pst(const std::string& path, const std::vector<double>& xyz);
+std::vector<double> read_pst(const std::string& path);
+
+}  // namespace mrsph_host

@@ -79,6 +79,44 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+HOST = os.path.join(ROOT, "host")
+HOST_LIB = os.path.join(ROOT, "libmrsph_host.so")
+HOST_BIN = os.path.join(ROOT, "mrsph_relax")
+
+
+def gxx() -> str:
+    for c in (shutil.which("g++"), "/usr/bin/g++"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("g++ not found")
+
+
+def build_host(force: bool = False) -> str:
+    """The C++ host layer (host/*.cpp, the reference's SPH_mesh_generation and
+    Solver entry points over the C ABI) as libmrsph_host.so, and its
+    command-line driver mrsph_relax, both linked against libmrsph_relax.so."""
+    lib = build(force=force)
+    srcs = [os.path.join(HOST, "sph_mesh_generation.cpp")]
+    deps = srcs + [os.path.join(HOST, "sph_mesh_generation.hpp"),
+                   os.path.join(os.path.dirname(ROOT), "include", "mrsph_relax.h"), lib]
+    flags = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", HOST]
+    link = ["-L", ROOT, "-lmrsph_relax", "-Wl,-rpath,$ORIGIN"]
+    if force or _stale(HOST_LIB, deps):
+        r = subprocess.run([gxx(), *flags, "-shared", "-o", HOST_LIB + ".tmp", *srcs, *link],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed (host library):\n" + r.stdout + r.stderr)
+        os.replace(HOST_LIB + ".tmp", HOST_LIB)
+    main = os.path.join(HOST, "mrsph_relax_main.cpp")
+    if force or _stale(HOST_BIN, deps + [main, HOST_LIB]):
+        r = subprocess.run([gxx(), *flags, "-o", HOST_BIN + ".tmp", main, "-L", ROOT, "-lmrsph_host",
+                            *link], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed (mrsph_relax):\n" + r.stdout + r.stderr)
+        os.replace(HOST_BIN + ".tmp", HOST_BIN)
+    return HOST_BIN
+
+
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
