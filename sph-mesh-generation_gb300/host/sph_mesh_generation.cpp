@@ -323,6 +323,12 @@ double Solver::SPH_Mesh_Generation_Solver(int total_steps, int output_interval, 
   return ms_total;
 }
 
+double Solver::Load_solver(const Initialization& ini, const std::string& output_root) {
+  const int every = (int)ini.Get_dt();
+  if (every < 1) throw Error(MRSPH_ERR_ARG, "output interval below one step");
+  return SPH_Mesh_Generation_Solver(ini.Get_num_timestep() * every, every, output_root);
+}
+
 void write_pst(const std::string& path, const std::vector<double>& xyz) {
   std::ofstream f(path, std::ios::binary | std::ios::trunc);
   if (!f) throw Error(MRSPH_ERR_ARG, "cannot write " + path);

@@ -15,6 +15,7 @@
 #pragma once
 
 #include <array>
+#include <cmath>
 #include <functional>
 #include <stdexcept>
 #include <string>
@@ -112,6 +113,17 @@ class SPH_mesh_generation {
   long long n_ = 0;
 };
 
+// System parameters (Initialization, src/system.cpp:12-32): the run spans
+// [start_time, end_time) in steps, with an output every output_dt steps.
+struct Initialization {
+  double start_time = 0.0;
+  double end_time = 20000;
+  double output_dt = 100;
+  int Get_num_timestep() const { return (int)std::ceil((end_time - start_time) / output_dt); }
+  double Get_start_time() const { return start_time; }
+  double Get_dt() const { return output_dt; }
+};
+
 // Solver::SPH_Mesh_Generation_Solver (src/solver.cpp:257-321): total_steps
 // relaxation steps, a particle restart every output_interval steps (and at
 // the end) when output_root is not empty.  Returns the device-timed
@@ -120,6 +132,10 @@ class Solver {
  public:
   explicit Solver(SPH_mesh_generation& sim) : sim_(sim) {}
   double SPH_Mesh_Generation_Solver(int total_steps, int output_interval = 0, const std::string& output_root = "");
+  // Solver::Load_solver (src/solver.cpp:35-101) for the relaxation path:
+  // Get_num_timestep() outputs, Get_dt() steps apart, with a particle restart
+  // at each.  Returns the device-timed milliseconds of the steps.
+  double Load_solver(const Initialization& ini, const std::string& output_root = "");
 
  private:
   SPH_mesh_generation& sim_;
