@@ -329,11 +329,16 @@ def run_accuracy(args, dev):
         g = SPHMeshGeneration(case, precision=prec, device=dev)
         g.Initialize_case()
         g.SPH_run_mesh_generation(args.accuracy_steps)
-        p = g.particles(("xyz", "h"))
+        p = g.particles(("xyz", "h", "type", "phi"))
         g.close()
         stats[prec] = spacing_stats(p["xyz"], p["h"], hdx, dim)
-    dif = {k: abs(stats["fp32"][k] - stats["fp64"][k]) / abs(stats["fp64"][k])
-           for k in ("median", "p05", "p95", "min_distance")}
+        # surface deviation: |phi| of the SURFACE particles over their target spacing
+        surf = p["type"] == 1
+        dev_s = np.abs(p["phi"][surf]) / (p["h"][surf] / hdx) if surf.any() else np.zeros(1)
+        stats[prec].update({"surface_count": int(surf.sum()), "surface_dev_mean": float(dev_s.mean()),
+                            "surface_dev_max": float(dev_s.max())})
+    dif = {k: abs(stats["fp32"][k] - stats["fp64"][k]) / max(abs(stats["fp64"][k]), 1e-300)
+           for k in ("median", "p05", "p95", "min_distance", "surface_count", "surface_dev_mean")}
     return {"workload": f"torus_3d_small (N={case.n_particles})", "reference": "fp64_plain GPU path",
             "single_step_force": force, "steps": args.accuracy_steps,
             "spacing_ratio": {"fp32": {k: v for k, v in stats["fp32"].items() if k != "hist"},

@@ -267,6 +267,8 @@ void SPH_mesh_generation::Initialize_case(long long n) {
 
 void SPH_mesh_generation::SPH_run_mesh_generation(int nsteps) { check(mrsph_step(h_, nsteps), "mrsph_step"); }
 
+void SPH_mesh_generation::Run_phase(int phase) { check(mrsph_run_phase(h_, phase), "mrsph_run_phase"); }
+
 mrsph_stats SPH_mesh_generation::Stats() {
   mrsph_stats s{};
   check(mrsph_get_stats(h_, &s), "mrsph_get_stats");

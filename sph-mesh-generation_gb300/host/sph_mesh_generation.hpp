@@ -103,6 +103,14 @@ class SPH_mesh_generation {
   // sph_mesh_generation.cpp:426-590); with pre_run the map and Pre_run follow.
   void Load_data_for_post(const std::string& pst, bool pre_run = true);
 
+  // One step up to and including a phase (MRSPH_PHASE_*), the groups of the
+  // reference's per-particle methods in step order: MAP = Update_coord_full_step,
+  // Get_particle_info, Find_and_map_particle, Set_particle_scale; BIN = the
+  // cell binning of Prepare_for_the_current_step; DENSITY = neighbour search and
+  // Get_kernel_summation; FORCE1 / FORCE2 = Accumulate_particle_force (1 / 2)
+  // with Set_timestep and the half-step kicks (sph_mesh_generation.cpp:1371-1463).
+  void Run_phase(int phase);
+
   long long num_particles() const { return n_; }
   mrsph_handle* handle() { return h_; }
 
