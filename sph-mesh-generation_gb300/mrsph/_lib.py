@@ -10,7 +10,9 @@ import os
 
 from . import build as _build
 
-LIB_PATH = _build.LIB
+# MRSPH_LIB selects another build of the library (the autotuner times its
+# candidates through it)
+LIB_PATH = os.environ.get("MRSPH_LIB", _build.LIB)
 
 KERNEL_HYPERBOLIC, KERNEL_CUBIC, KERNEL_WENDLAND, KERNEL_GAUSSIAN, KERNEL_QUINTIC = range(5)
 FP64_PLAIN, FP32_SPLIT = 0, 1

@@ -45,21 +45,44 @@ def _stale(out: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+TUNED = os.path.join(PKG, "tuned.json")
+
+
+def tuned_defines() -> list:
+    """Tuning macros of the neighbour passes: MRSPH_NVCC_DEFINES when set
+    (e.g. "-DMRSPH_DENSITY_MIN_BLOCKS=4"), else those an autotuner run wrote
+    to mrsph/tuned.json (mrsph/autotune.py), else none (the engine's
+    defaults, tuned on a GB300 for the 3D torus)."""
+    env = os.environ.get("MRSPH_NVCC_DEFINES")
+    if env is not None:
+        return env.split()
+    if os.path.exists(TUNED):
+        import json
+        with open(TUNED) as f:
+            return ["-DMRSPH_%s=%d" % (k, int(v)) for k, v in sorted(json.load(f)["defines"].items())]
+    return []
+
+
+def build(force: bool = False, verbose: bool = False, defines: list = None, build_dir: str = None,
+          lib_path: str = None) -> str:
+    """Compile the library; defines / build_dir / lib_path override the tuning
+    macros and the output locations (the autotuner builds its candidates
+    side by side)."""
+    bdir = build_dir or BUILD
+    out_lib = lib_path or LIB
+    os.makedirs(bdir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(os.path.dirname(ROOT), "include", "mrsph_relax.h"))
     base = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
             "--expt-relaxed-constexpr", "-I", CSRC]
-    # tuning macros of the neighbour passes (e.g. "-DMRSPH_DENSITY_MIN_BLOCKS=4")
-    base += os.environ.get("MRSPH_NVCC_DEFINES", "").split()
+    base += tuned_defines() if defines is None else list(defines)
     jobs = []
     objs = []
     for src, extra in SOURCES.items():
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(bdir, src.replace(".cu", ".o"))
         objs.append(o)
-        if force or _stale(o, [s, *headers]):
+        if force or _stale(o, [s, *headers] + ([TUNED] if os.path.exists(TUNED) else [])):
             jobs.append(base + extra + ["-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
@@ -70,13 +93,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
                     raise RuntimeError("nvcc failed:\n" + " ".join(j) + "\n" + r.stdout + r.stderr)
                 if verbose:
                     print(r.stdout + r.stderr)
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
+    if force or jobs or _stale(out_lib, objs):
+        tmp = out_lib + ".tmp"
         r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, out_lib)
+    return out_lib
 
 
 HOST = os.path.join(ROOT, "host")
