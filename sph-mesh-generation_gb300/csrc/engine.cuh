@@ -264,7 +264,7 @@ __device__ inline R dot3(const R* a, const R* b) {
 template <int D, class R>
 __device__ inline void set_info(const KCtx& c, R phi, R curv, R& h, R& rho) {
   R h_tmp = get_scale<R>(c.ls, phi, curv);
-  h = h_tmp * (R)c.prm.cell_ratio / (R)c.prm.cutoff;
+  h = h_tmp * pick<R>(c.prm.cell_ratio, c.prm.cell_ratio_f) / pick<R>(c.prm.cutoff, c.prm.cutoff_f);
   R vol;
   if constexpr (std::is_same<R, float>::value) vol = (D == 2) ? h_tmp * h_tmp : h_tmp * h_tmp * h_tmp;
   else vol = (D == 2) ? h_tmp * h_tmp : pow(h_tmp, 3.0);  // pow(h, DIM) as the reference
@@ -276,6 +276,8 @@ __device__ inline void set_info(const KCtx& c, R phi, R curv, R& h, R& rho) {
 // ---------------------------------------------------------------------------
 static __global__ void k_begin_step(DevScalars* sc, int inc) {
   sc->dt_adv = sc->dt2;
+  sc->dt_adv_f = (float)bitsd(sc->dt2);
+  sc->hdt_adv_f = (float)(0.5 * bitsd(sc->dt2));
   sc->dt1 = 0x7FF0000000000000ull;  // +inf
   sc->dt2 = 0x7FF0000000000000ull;
   sc->vmax1 = 0;
@@ -362,9 +364,16 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
     // A1 Update_coord_full_step (particle_mesh_generation.cpp:1139-1179), with
     // the stage-2 half kick of the previous step folded in (:1130-1135)
     if (mode == MAP_STEP && type != SINGULARITY_P) {
-      double dt2 = bitsd(c.sc->dt_adv);
       typename V4<R>::T v1 = b.v1[i], a2 = b.a2[i];
-      R hdt = (R)(0.5 * dt2), dtr = (R)dt2;
+      R hdt, dtr;
+      if constexpr (F32) {
+        hdt = c.sc->hdt_adv_f;
+        dtr = c.sc->dt_adv_f;
+      } else {
+        const double dt2 = bitsd(c.sc->dt_adv);
+        hdt = (R)(0.5 * dt2);
+        dtr = (R)dt2;
+      }
       R v[3] = {v1.x + a2.x * hdt, v1.y + a2.y * hdt, v1.z + a2.z * hdt};
       R dl[3] = {v[0] * dtr, v[1] * dtr, (D == 3) ? v[2] * dtr : (R)0};
       P::add(c, p, key, dl);
@@ -452,8 +461,8 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
     if (mode == MAP_STEP) set_info<D, R>(c, phi, curv, h, rho);
     // Particle_base::Set_particle_scale, particle.cpp:957-975 (scale = max_scale*2^-e)
     {
-      R sc = F32 ? (R)ldexpf((float)c.geo.max_scale, -e) : (R)ldexp(c.geo.max_scale, -e);
-      R hc = h * (R)c.prm.cutoff;
+      R sc = F32 ? (R)ldexpf(c.geo.max_scale_f, -e) : (R)ldexp(c.geo.max_scale, -e);
+      R hc = h * pick<R>(c.prm.cutoff, c.prm.cutoff_f);
       for (int it = 0; it < 64; it++) {
         if (hc > sc + (R)1.e-15) { sc *= 2; e--; }
         else if (hc < sc / 2 - (R)1.e-15) { sc /= 2; e++; }
@@ -659,7 +668,7 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
 template <int D>
 __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__ lhmax, int L,
                                      const SOrigin<D, float>& so, float hi, bool active, int* q, float* fr) {
-  const float cut = (float)c.prm.cutoff;
+  const float cut = c.prm.cutoff_f;
   const float hic = hi * cut;
   const float Rg = (fmaxf(hic, (float)bitsd(c.sc->hmax[L]) * cut) + 1.e-10f) * (1.f + 1.e-5f);
   float hloc = 0.f;
@@ -918,8 +927,8 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   // FP32 Wendland C2: a REAL particle sums (1 - s/2)^4 (1 + 2s), s = r/h,
   // clamped at s = 2, and applies the normalisation C/h^D once at the end
   constexpr bool WEN32 = F32 && KK == K_WEN;
-  const R cos_t = (R)c.prm.cos_thres;
-  const R cut = (R)c.prm.cutoff;
+  const R cos_t = pick<R>(c.prm.cos_thres, c.prm.cos_thres_f);
+  const R cut = pick<R>(c.prm.cutoff, c.prm.cutoff_f);
   R sum = 0;
   int ncount = 0, cnt = 0;
   int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[(q >> 3) * 256 + (q & 7)]
@@ -1075,7 +1084,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
       ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
     }
     const R rho = b.nr[i].w, h = a0.w;
-    const R cos_t = (R)c.prm.cos_thres;
+    const R cos_t = pick<R>(c.prm.cos_thres, c.prm.cos_thres_f);
     const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
     R nu = 0, eta_i = 0;
     R hdt1 = 0;
@@ -1206,7 +1215,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
     if (ti == REAL_P || ti == SURFACE_P) {
       for (int d = 0; d < D; d++) a[d] = F[d];
       if (STAGE == 2)
-        for (int d = 0; d < D; d++) a[d] = a[d] + vi[d] * (R)c.prm.damp_coeff;
+        for (int d = 0; d < D; d++) a[d] = a[d] + vi[d] * pick<R>(c.prm.damp_coeff, c.prm.damp_coeff_f);
       if (ti == SURFACE_P) {  // Map_surface_particle_force, :1122-1126
         R nf = dot3<D, R>(a, ni);
         for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
@@ -1217,7 +1226,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE =
     R ts = (R)0.25 * r_sqrt(h / (A + (R)1.e-15));
     ts = AMIN1(ts, h / (R)40. / (U + (R)1.e-15));
     if (STAGE == 2) {
-      R nu_new = (R)c.prm.nu_coeff * h * U;
+      R nu_new = pick<R>(c.prm.nu_coeff, c.prm.nu_coeff_f) * h * U;
       ts = AMIN1(ts, (R)0.125 * h * h / (nu_new + (R)1.e-15));
       b.nu_next[i] = nu_new;
       b.v1[i] = mk4<R>(vi[0], vi[1], vi[2], U);
@@ -1380,6 +1389,20 @@ class Engine : public EngineBase {
     kc_.n = 0;
     kc_.sc = nullptr;
     st_ = cfg.stream;
+    // FP32 copies of the run parameters, read by the FP32-split kernels
+    kc_.prm.cell_ratio_f = (float)kc_.prm.cell_ratio;
+    kc_.prm.cutoff_f = (float)kc_.prm.cutoff;
+    kc_.prm.cos_thres_f = (float)kc_.prm.cos_thres;
+    kc_.prm.nu_coeff_f = (float)kc_.prm.nu_coeff;
+    kc_.prm.damp_coeff_f = (float)kc_.prm.damp_coeff;
+    kc_.ls.max_phi_f = (float)kc_.ls.max_phi;
+    kc_.ls.dl0_f = (float)kc_.ls.dl0;
+    kc_.ls.min_dl_f = (float)kc_.ls.min_dl;
+    kc_.ls.max_dl_f = (float)kc_.ls.max_dl;
+    kc_.ls.middle_dl_f = (float)kc_.ls.middle_dl;
+    kc_.ls.max_curv_f = (float)kc_.ls.max_curv;
+    kc_.ls.min_curv_f = (float)kc_.ls.min_curv;
+    kc_.geo.max_scale_f = (float)kc_.geo.max_scale;
     if (std::is_same<R, float>::value) init_rc_ = anchor_tables();
   }
   ~Engine() override {

@@ -43,6 +43,7 @@ struct LsSet {
   double max_phi, dl0, min_dl, max_dl;
   int law;                              // 0: tanh law of phi; 1: curvature law
   double middle_dl, max_curv, min_curv; // curvature law (|curv| range over CUT cells)
+  float max_phi_f, dl0_f, min_dl_f, max_dl_f, middle_dl_f, max_curv_f, min_curv_f;  // FP32 copies
   LsLevel lv[MAX_LS];
 };
 
@@ -53,6 +54,7 @@ struct CellGeo {
   int ncl;
   double box_l[3];
   double max_scale, min_scale;
+  float max_scale_f;
   int n[MAX_CL][3];
   double dcell[MAX_CL][3];
   long long off[MAX_CL + 1];
@@ -75,12 +77,15 @@ struct Params {
   double cell_ratio, cutoff, angle_thres, cos_thres, nu_coeff, damp_coeff;
   double box_l[3], box_r[3];
   unsigned long long seed;
+  // FP32 copies (the FP32-split kernels read these, not conversions of the above)
+  float cell_ratio_f, cutoff_f, cos_thres_f, nu_coeff_f, damp_coeff_f;
 };
 
 // Device scalars of a step.  Doubles are kept as their bit patterns so that
 // min/max of non-negative values reduce exactly with integer atomics.
 struct DevScalars {
   unsigned long long dt1, vmax1, dt2, vmax2, dt_adv;
+  float dt_adv_f, hdt_adv_f;  // FP32 dt_adv and dt_adv / 2 (set with dt_adv at the start of a step)
   unsigned long long pairs;
   unsigned long long pairs_total;
   unsigned int remap, nsurf, flags, spill;
@@ -249,6 +254,12 @@ __device__ inline R kernel_dW(int kind, int D, R dist, R h) {
 // hoisted, and reciprocals and square roots come from the hardware
 // approximation units (relative error about 1e-7, well inside the FP32
 // path's tolerance).
+// a run parameter in the path's precision: the double (FP64-plain) or its
+// FP32 copy made once on the host (FP32-split; no conversion per thread)
+template <class R> __host__ __device__ inline R pick(double d, float f);
+template <> __host__ __device__ inline double pick<double>(double d, float) { return d; }
+template <> __host__ __device__ inline float pick<float>(double, float f) { return f; }
+
 __device__ inline double r_rcp(double x) { return 1.0 / x; }
 __device__ inline float r_rcp(float x) { return __fdividef(1.0f, x); }
 __device__ inline double r_div(double a, double b) { return a / b; }
@@ -575,17 +586,20 @@ __device__ inline int ls_tag(const LsSet& ls, const double* x) {
 // by the tanh law from s0 to maximum_dl.
 template <class R>
 __device__ inline R get_scale(const LsSet& ls, R phi, R curv) {
-  if (phi > 0 || r_fabs(phi) < (R)ls.dl0) {
+  const R min_dl = pick<R>(ls.min_dl, ls.min_dl_f);
+  if (phi > 0 || r_fabs(phi) < pick<R>(ls.dl0, ls.dl0_f)) {
     R factor = (R)2.5;
-    R lo = (R)ls.min_dl;
+    R lo = min_dl;
     if (ls.law == 1) {
-      R q = ((R)ls.max_curv - r_fabs(curv)) / ((R)ls.max_curv - (R)ls.min_curv + (R)1.e-20);
+      const R mc = pick<R>(ls.max_curv, ls.max_curv_f);
+      R q = (mc - r_fabs(curv)) / (mc - pick<R>(ls.min_curv, ls.min_curv_f) + (R)1.e-20);
       q = AMAX1((R)0., AMIN1(q, (R)1.));
-      lo = (R)ls.min_dl + q * q * ((R)ls.middle_dl - (R)ls.min_dl);
+      lo = min_dl + q * q * (pick<R>(ls.middle_dl, ls.middle_dl_f) - min_dl);
     }
-    return lo + r_tanh(factor * r_fabs(phi) / (R)ls.max_phi) / r_tanh(factor) * ((R)ls.max_dl - lo);
+    return lo + r_tanh(factor * r_fabs(phi) / pick<R>(ls.max_phi, ls.max_phi_f)) / r_tanh(factor) *
+                    (pick<R>(ls.max_dl, ls.max_dl_f) - lo);
   }
-  return (R)ls.min_dl;
+  return min_dl;
 }
 
 // ---------------------------------------------------------------- reductions
