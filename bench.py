@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cvp-iters", type=int, default=50)
     ap.add_argument("--batch-geoms", type=int, default=64, help="star-shaped geometries of the batched run (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--no-volume-mass", action="store_true", help="skip the cut-cell volume / particle-count leg")
     ap.add_argument("--accuracy-steps", type=int, default=100, help="relaxation steps of the accuracy leg (0: skip)")
     return ap.parse_args()
 
@@ -190,6 +191,17 @@ def cpu_oracle_run(case, steps: int):
     pairs = orc.steps(steps)
     dt = time.perf_counter() - t0
     return {"seconds": dt, "steps": steps, "pairs": pairs, "setup_s": setup, "threads": oracle.num_threads()}
+
+
+def cpu_volume_mass(case):
+    """Time the oracle's cut-cell volume pass (OpenMP, all host threads) on
+    the finest level of the workload."""
+    import oracle
+    oracle.build()
+    orc = oracle.Oracle(case)
+    t0 = time.perf_counter()
+    r = orc.volume_mass(-1)
+    return {"seconds": time.perf_counter() - t0, "threads": oracle.num_threads(), "result": r}
 
 
 def run_reference(args, ws, rank, dist):
@@ -417,6 +429,19 @@ def run_mrsph(args, ws, rank, local, dist):
                "error_edges": int(q["nerror"]), "min_angle": q["min_angle"], "min_angle_avg": q["min_angle_avg"],
                "max_aspect": q["max_aspect"], "G_avg": q["G_avg"], "theta_30": q["theta_30"],
                "total_area": q["total_area"], "angle_hist_4deg": [int(v) for v in q["hist"]]}
+    # cut-cell volume, surface area and particle count of the finest level
+    # (Calculate_total_volume_mass + Get_num_particles), device-timed
+    vm = None
+    if not args.no_volume_mass:
+        gpu.sync()
+        t0 = time.perf_counter()
+        r = gpu.volume_mass(-1)
+        vm_wall = time.perf_counter() - t0
+        vm = {k: r[k] for k in ("total_mass", "total_mass_surface", "total_volume", "total_area",
+                                "num_interface_cell", "num_particle_mesh", "num_particle_surface", "num_particle")}
+        vm.update(device_ms=r["device_ms"], wall_s=vm_wall, level_cells=int(case.levels[-1].phi.size),
+                  timer="CUDA events around the pass on the handle's stream; wall clock incl. scratch "
+                        "allocation and copies")
     gpu.close()
 
     # e2e through the C ABI with host buffers (pinned when torch is available):
@@ -485,13 +510,22 @@ def run_mrsph(args, ws, rank, local, dist):
                "sample": f"{r['steps']} relaxation step(s) of the full workload (N={n}) from step 2 after "
                          f"seeding, FP64 oracle (restatement of the reference, OpenMP {r['threads']} threads)",
                "gpu_same_window": fp64["fp32_same_window"] if fp64 else None}
+    if vm is not None and not args.no_cpu:
+        r = cpu_volume_mass(case)
+        ref = r["result"]
+        vm["cpu"] = {"seconds": r["seconds"], "threads": r["threads"], "kind": "port",
+                     "num_particle": ref["num_particle"],
+                     "counts_equal": all(ref[k] == vm[k] for k in ("num_interface_cell", "num_particle_mesh",
+                                                                   "num_particle_surface")),
+                     "total_mass_rel_diff": abs(ref["total_mass"] - vm["total_mass"]) / abs(ref["total_mass"])}
+        vm["speedup_vs_cpu"] = r["seconds"] / (vm["device_ms"] / 1000.0)
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(case, args.workload),
             "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
             "fp64_plain": fp64,
             "fp32_over_fp64": (fp64["fp32_same_window"]["value"] / fp64["value"]) if fp64 else None,
-            "phase_ms": prof, "cvp": cvp, "triangulation": tri, "batched": batched, "accuracy": accuracy, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "phase_ms": prof, "cvp": cvp, "triangulation": tri, "volume_mass": vm, "batched": batched, "accuracy": accuracy, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": 12 * args.steps, "clocks": clocks, "device_flags": flags}
     print(json.dumps(line), flush=True)
 

@@ -171,6 +171,30 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
 /* Tap: the device-built fields of one level (arrays sized like phi; NULL skips). */
 int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, double* nz, double* curv,
                        unsigned char* tag, double* max_phi);
+/* Cut-cell volume, surface area and particle numbers of one level-set level
+ * (level < 0: the finest): Levelset::Calculate_total_volume_mass
+ * (level_set.cpp:930-972) over Levelset_package::Calculate_volume_mass
+ * (lset_package.cpp:1283-1397) and GeometryCalculator
+ * (geometry_calculator.cpp:12-570), then
+ * SPH_mesh_generation::Get_num_particles (sph_mesh_generation.cpp:900-940)
+ * without segments or singularities.  A cell counts when phi > 0 or
+ * |phi| < dl (the level's smallest cell size); CUT cells take their volume
+ * fraction from adaptive bisection and their area from marching cubes.
+ * cell_vol / cell_area (may be NULL) receive per-cell values sized like phi
+ * (zero outside the counted cells). */
+typedef struct {
+  double total_mass;          /* sum of vol / scale^D (Levelset::total_mass) */
+  double total_mass_surface;  /* sum over CUT cells of area / scale^(D-1) */
+  double total_volume;
+  double total_area;
+  long long num_interface_cell;   /* CUT cells (glbl_num_interface_cell) */
+  long long num_particle_mesh;    /* max(int(total_mass - total_mass_surface / 2), 0) */
+  long long num_particle_surface; /* min(int(total_mass_surface), num_interface_cell) */
+  long long num_particle;         /* mesh + surface (glbl_total_num_particle) */
+  double device_ms;           /* device time of the pass */
+} mrsph_volume_mass_stats;
+int mrsph_volume_mass(mrsph_handle* h, int level, mrsph_volume_mass_stats* out, double* cell_vol,
+                      double* cell_area);
 /* Levelset::Get_phi_at_position / Calculate_particle_infor (level_set.cpp:372-436,
  * particle_mesh_generation.cpp:175-265) at n host points (xyz n x 3). */
 int mrsph_sample_levelset(mrsph_handle* h, long long n, const double* xyz, double* phi, double* norm,

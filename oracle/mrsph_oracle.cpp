@@ -5,13 +5,17 @@
 // baseline and reference arms) may load it.  The product library
 // (sph-mesh-generation_gb300/csrc) never links or calls it.
 //
-// Parity status: UNPINNED against the reference binary.  The reference
-// (Xiangyu-Hu/SPH-mesh-generation) needs TBB, Boost.MPI/Graph/Serialization
-// and voro++ to build, none of which exist here, and it ships no tests, golden
-// vectors or fixtures.  This restatement is pinned instead by analytic
-// known-answer tests (kernel normalisation, zero gradient sum on a lattice,
-// exact bilinear interpolation of linear phi, projection onto phi = 0,
-// spacing-law endpoints) in tests/test_oracle_kat.py.
+// Parity status: UNPINNED against the reference binary for the relaxation
+// step.  The reference (Xiangyu-Hu/SPH-mesh-generation) needs TBB,
+// Boost.MPI/Graph/Serialization and voro++ to build, none of which exist
+// here, and it ships no tests, golden vectors or fixtures.  This restatement
+// is pinned instead by analytic known-answer tests (kernel normalisation,
+// zero gradient sum on a lattice, exact bilinear interpolation of linear phi,
+// projection onto phi = 0, spacing-law endpoints) in tests/test_oracle_kat.py.
+// One piece compiles from the reference's own sources: its marching-cubes
+// polygoniser (geometry_tools/polygonise.cpp, oracle/build_ref.py), which
+// pins the surface-area restatement below (tests/test_volume_mass.py and the
+// golden vectors of tests/golden/make_mc_golden.py).
 //
 // Every function cites the reference file:line it restates (paths relative to
 // the reference's src/).  Arithmetic is FP64 and follows the reference's
@@ -1830,6 +1834,415 @@ int orc_num_threads(void) {
 #else
   return 1;
 #endif
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// F1: cut-cell volume, surface area and the particle count of one level-set
+// level.  Levelset::Calculate_total_volume_mass (level_set_solver/
+// level_set.cpp:930-972) over Levelset_package::Calculate_volume_mass
+// (level_set_solver/lset_package.cpp:1283-1397) with GeometryCalculator
+// (geometry_tools/geometry_calculator.cpp:12-570), and
+// SPH_mesh_generation::Get_num_particles (sph_mesh_generation.cpp:900-940).
+//
+// Surface area: the reference polygonises each half-cell sub-cube with the
+// marching-cubes tables of geometry_tools/polygonise.h.  The polygons follow
+// from the signs alone (a face with two diagonal corners below zero cuts
+// those two corners off, the rule the tables follow on every ambiguous face,
+// checked over all 256 sign cases), so mc_table() below derives them by
+// walking the cut edges; each polygon is then split as a fan from its lowest
+// edge.  The reference's tables split some polygons along other diagonals,
+// so a cell's area may differ in the last digits that a non-planar polygon
+// leaves (about 1e-6 of the total area on smooth surfaces); volumes, masses
+// and counts do not depend on the split.
+// ===========================================================================
+namespace {
+
+// cube vertices of a sub-cube in the order of geometry_calculator.cpp:296-297
+const int MC_V[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {1, 0, 1}};
+// edge endpoints (polygonise.cpp:37-60: the first endpoint is interpolated from)
+const int MC_E[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                         {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+const int MC_F[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+
+struct McTable {
+  signed char t[256][16];  // edge triples, -1 terminated
+};
+
+int mc_edge(int a, int b) {
+  for (int e = 0; e < 12; e++)
+    if ((MC_E[e][0] == a && MC_E[e][1] == b) || (MC_E[e][0] == b && MC_E[e][1] == a)) return e;
+  return -1;
+}
+
+// Bit v of a case is set when vertex v lies below zero (polygonise.cpp:19-27).
+const McTable& mc_table() {
+  static McTable T = [] {
+    McTable M;
+    for (int ci = 0; ci < 256; ci++) {
+      int nb[12][2], nn[12] = {0};
+      for (int f = 0; f < 6; f++) {
+        int in[4], es[4], cut[4], nc = 0;
+        for (int k = 0; k < 4; k++) in[k] = (ci >> MC_F[f][k]) & 1;
+        for (int k = 0; k < 4; k++) es[k] = mc_edge(MC_F[f][k], MC_F[f][(k + 1) & 3]);
+        for (int k = 0; k < 4; k++)
+          if (in[k] != in[(k + 1) & 3]) cut[nc++] = es[k];
+        auto link = [&](int a, int b) {
+          nb[a][nn[a]++] = b;
+          nb[b][nn[b]++] = a;
+        };
+        if (nc == 2) link(cut[0], cut[1]);
+        else if (nc == 4)
+          for (int k = 0; k < 4; k++)
+            if (in[k]) link(es[(k + 3) & 3], es[k]);
+      }
+      int n = 0;
+      bool seen[12] = {false};
+      for (int s = 0; s < 12; s++) {
+        if (!nn[s] || seen[s]) continue;
+        int cyc[12], m = 0, prev = s, cur = nb[s][0] < nb[s][1] ? nb[s][0] : nb[s][1];
+        cyc[m++] = s;
+        seen[s] = true;
+        while (cur != s) {
+          cyc[m++] = cur;
+          seen[cur] = true;
+          int nxt = nb[cur][0] == prev ? nb[cur][1] : nb[cur][0];
+          prev = cur;
+          cur = nxt;
+        }
+        for (int k = 1; k + 1 < m; k++) {
+          M.t[ci][n++] = (signed char)cyc[0];
+          M.t[ci][n++] = (signed char)cyc[k];
+          M.t[ci][n++] = (signed char)cyc[k + 1];
+        }
+      }
+      for (; n < 16; n++) M.t[ci][n] = -1;
+    }
+    return M;
+  }();
+  return T;
+}
+
+struct P3 {
+  double x, y, z;
+};
+
+// Polygonise_MQ::VertexInterp, polygonise.cpp:74-92 (isolevel 0)
+P3 mc_interp(P3 p1, P3 p2, double v1, double v2) {
+  const double iso = 0.0;
+  if (std::fabs(iso - v1) < 1.0e-15) return p1;
+  if (std::fabs(iso - v2) < 1.0e-15) return p2;
+  if (std::fabs(v1 - v2) < 1.0e-15) return p1;
+  double mu = (iso - v1) / (v2 - v1);
+  return P3{p1.x + mu * (p2.x - p1.x), p1.y + mu * (p2.y - p1.y), p1.z + mu * (p2.z - p1.z)};
+}
+
+// GeometryCalculator::get_area_tri, geometry_calculator.cpp:325-350
+double mc_tri_area(P3 p1, P3 p2, P3 p3) {
+  double v1x = p2.x - p1.x, v1y = p2.y - p1.y, v1z = p2.z - p1.z;
+  double v3x = p3.x - p1.x, v3y = p3.y - p1.y, v3z = p3.z - p1.z;
+  double d1 = std::sqrt(v1x * v1x + v1y * v1y + v1z * v1z);
+  double d3 = std::sqrt(v3x * v3x + v3y * v3y + v3z * v3z);
+  double area = 0.5 * (d3 * d1) * std::sin(std::acos((v1x * v3x + v1y * v3y + v1z * v3z) / (d3 * d1 + 1.e-20)));
+  if (std::isnan(area)) area = 0.;
+  return area;
+}
+
+// GeometryCalculator::get_area_MQ, geometry_calculator.cpp:283-321
+double mc_area(const double ph[3][3][3], double dx, double dy, double dz) {
+  const McTable& T = mc_table();
+  double area = 0.0;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < 2; k++) {
+        P3 p[8];
+        double val[8];
+        int ci = 0;
+        for (int v = 0; v < 8; v++) {
+          int vx = i + MC_V[v][0], vy = j + MC_V[v][1], vz = k + MC_V[v][2];
+          p[v] = P3{vx * 0.5 * dx, vy * 0.5 * dy, vz * 0.5 * dz};
+          val[v] = ph[vx][vy][vz];
+          if (val[v] < 0.0) ci |= 1 << v;
+        }
+        const signed char* t = T.t[ci];
+        for (int q = 0; t[q] >= 0; q += 3) {
+          P3 a = mc_interp(p[MC_E[t[q]][0]], p[MC_E[t[q]][1]], val[MC_E[t[q]][0]], val[MC_E[t[q]][1]]);
+          P3 b = mc_interp(p[MC_E[t[q + 1]][0]], p[MC_E[t[q + 1]][1]], val[MC_E[t[q + 1]][0]], val[MC_E[t[q + 1]][1]]);
+          P3 c = mc_interp(p[MC_E[t[q + 2]][0]], p[MC_E[t[q + 2]][1]], val[MC_E[t[q + 2]][0]], val[MC_E[t[q + 2]][1]]);
+          area += mc_tri_area(a, b, c);
+        }
+      }
+  return area;
+}
+
+// GeometryCalculator::check_volume / check_face / mark_volume / mark_face
+// (geometry_calculator.cpp:352-448): 1 all positive, 0 all negative, -1 cut
+int gc_mark(const double* v, int n) {
+  int flag = 0;
+  for (int q = 0; q < n; q++) {
+    if (v[q] > 0.0) flag += 1;
+    else if (v[q] < 0.0) flag -= 1;
+  }
+  return flag == n ? 1 : (flag == -n ? 0 : -1);
+}
+
+// GeometryCalculator::get_subvolume, geometry_calculator.cpp:505-570
+double gc_subvolume(int level_phi, double multi, const double cor[2][2][2]) {
+  int flag = gc_mark(&cor[0][0][0], 8);
+  if (flag == 1) return multi;
+  if (flag == 0) return 0.0;
+  double vof = 0.0;
+  if (level_phi <= 5) {
+    multi *= 0.125;
+    level_phi += 1;
+    double rf[3][3][3];
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++)
+        for (int k = 0; k < 2; k++) rf[2 * i][2 * j][2 * k] = cor[i][j][k];
+    for (int i = 0; i < 3; i += 2)
+      for (int j = 0; j < 3; j += 2) rf[i][j][1] = 0.5 * (rf[i][j][0] + rf[i][j][2]);
+    for (int k = 0; k < 3; k++)
+      for (int i = 0; i < 3; i += 2) rf[i][1][k] = 0.5 * (rf[i][0][k] + rf[i][2][k]);
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++) rf[1][j][k] = 0.5 * (rf[0][j][k] + rf[2][j][k]);
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++)
+        for (int k = 0; k < 2; k++) {
+          double sub[2][2][2];
+          for (int r = 0; r < 2; r++)
+            for (int s = 0; s < 2; s++)
+              for (int t = 0; t < 2; t++) sub[r][s][t] = rf[i + r][j + s][k + t];
+          vof += gc_subvolume(level_phi, multi, sub);
+        }
+  } else {
+    double cv = 0.0;
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++)
+        for (int k = 0; k < 2; k++) cv += cor[i][j][k];
+    vof = cv > 0.0 ? 0.75 * multi : (cv == 0.0 ? 0.5 * multi : 0.25 * multi);
+  }
+  return vof;
+}
+
+// GeometryCalculator::get_face, geometry_calculator.cpp:450-503
+double gc_face(int level_phi, double multi, const double cor[2][2]) {
+  int flag = gc_mark(&cor[0][0], 4);
+  if (flag == 1) return multi;
+  if (flag == 0) return 0.0;
+  double vof = 0.0;
+  if (level_phi <= 5) {
+    multi *= 0.25;
+    level_phi += 1;
+    double rf[3][3];
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++) rf[2 * i][2 * j] = cor[i][j];
+    for (int i = 0; i < 3; i += 2) rf[i][1] = 0.5 * (rf[i][0] + rf[i][2]);
+    for (int j = 0; j < 3; j++) rf[1][j] = 0.5 * (rf[0][j] + rf[2][j]);
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++) {
+        double sub[2][2];
+        for (int r = 0; r < 2; r++)
+          for (int s = 0; s < 2; s++) sub[r][s] = rf[i + r][j + s];
+        vof += gc_face(level_phi, multi, sub);
+      }
+  } else {
+    double cv = 0.0;
+    for (int i = 0; i < 2; i++)
+      for (int j = 0; j < 2; j++) cv += cor[i][j];
+    vof = cv > 0.0 ? 0.75 * multi : (cv == 0.0 ? 0.5 * multi : 0.25 * multi);
+  }
+  return vof;
+}
+
+// GeometryCalculator::Get_corner, geometry_calculator.cpp:12-77: the cell's
+// phi on a half-cell lattice from its 3^D neighbourhood p (p[1][1][1 or 0]
+// the cell itself); 2D uses z index 0 only (DIM_Z = 0).
+void gc_corner(int D, const double p[3][3][3], double c[3][3][3]) {
+  const int DZ = D == 3 ? 1 : 0;
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++)
+      for (int e = 0; e < 3; e++) c[a][b][e] = 0.;
+  c[1][1][DZ] = p[1][1][DZ];
+  for (int r = 0; r < 2; r++)
+    for (int s = 0; s < 2; s++)
+      for (int t = 0; t < 1 + DZ; t++)
+        c[2 * r][2 * s][2 * t] = 0.125 * (p[r][s][t] + p[r + 1][s][t] + p[r][s + 1][t] + p[r + 1][s + 1][t] +
+                                          p[r][s][t + DZ] + p[r + 1][s][t + DZ] + p[r][s + 1][t + DZ] +
+                                          p[r + 1][s + 1][t + DZ]);
+  if (DZ)
+    for (int r = 0; r < 2; r++)
+      for (int s = 0; s < 2; s++)
+        c[2 * r][2 * s][1] = 0.25 * (p[r][s][1] + p[r + 1][s][1] + p[r][s + 1][1] + p[r + 1][s + 1][1]);
+  for (int s = 0; s < 2; s++)
+    for (int t = 0; t < 1 + DZ; t++)
+      c[1][2 * s][2 * t] = 0.25 * (p[1][s][t] + p[1][s][t + DZ] + p[1][s + 1][t] + p[1][s + 1][t + DZ]);
+  for (int r = 0; r < 2; r++)
+    for (int t = 0; t < 1 + DZ; t++)
+      c[2 * r][1][2 * t] = 0.25 * (p[r][1][t] + p[r + 1][1][t] + p[r][1][t + DZ] + p[r + 1][1][t + DZ]);
+  if (DZ)
+    for (int r = 0; r < 2; r++) {
+      c[2 * r][1][1] = 0.5 * (p[r][1][1] + p[r + 1][1][1]);
+      c[1][2 * r][1] = 0.5 * (p[1][r][1] + p[1][r + 1][1]);
+      c[1][1][2 * r] = 0.5 * (p[1][1][r] + p[1][1][r + 1]);
+    }
+}
+
+// Get_cutcell_volume + Get_surface_area (geometry_calculator.cpp:79-262) of
+// one CUT cell from its corner lattice c
+void gc_cut_cell(int D, const double c[3][3][3], double dx, double dy, double dz, double* vol, double* area) {
+  double H = 0., A = 0.;
+  if (D == 3) {
+    int marker = gc_mark(&c[0][0][0], 27);
+    if (marker == -1) {
+      double vof = 0.0;  // get_volume, :262-281
+      for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++)
+          for (int k = 0; k < 2; k++) {
+            double sub[2][2][2];
+            for (int r = 0; r < 2; r++)
+              for (int s = 0; s < 2; s++)
+                for (int t = 0; t < 2; t++) sub[r][s][t] = c[i + r][j + s][k + t];
+            vof += gc_subvolume(0, 0.125, sub);
+          }
+      H = AMIN1(vof, 1.0);
+      A = mc_area(c, dx, dy, dz);
+    } else {
+      H = marker == 1 ? 1.0 : 0.0;
+    }
+    *vol = H * (dx * dy * dz);
+  } else {
+    double face[3][3];
+    for (int r = 0; r < 3; r++)
+      for (int s = 0; s < 3; s++) face[r][s] = c[r][s][0];
+    int marker = gc_mark(&face[0][0], 9);
+    if (marker == -1) {
+      double a = 0.0;  // get_area, :243-260
+      for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) {
+          double sub[2][2];
+          for (int r = 0; r < 2; r++)
+            for (int s = 0; s < 2; s++) sub[r][s] = face[i + r][j + s];
+          a += gc_face(0, 0.25, sub);
+        }
+      H = AMIN1(a, 1.0);
+      double ext[3][3][3];  // the face extruded over a unit depth (:137-148)
+      for (int r = 0; r < 3; r++)
+        for (int s = 0; s < 3; s++)
+          for (int t = 0; t < 3; t++) ext[r][s][t] = face[r][s];
+      A = mc_area(ext, dx, dy, 1.);
+    } else {
+      H = marker == 1 ? 1.0 : 0.0;
+    }
+    *vol = H * (dx * dy * 1.);
+  }
+  *area = A;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Marching-cubes table of mc_table(): 256 x 16 edge indices, -1 padded.
+void orc_mc_table(signed char* out) { std::memcpy(out, mc_table().t, 256 * 16); }
+
+// Area of the surface of one 3x3x3 corner lattice (get_area_MQ).
+double orc_mc_area(const double* c27, double dx, double dy, double dz) {
+  double c[3][3][3];
+  std::memcpy(c, c27, sizeof(c));
+  return mc_area(c, dx, dy, dz);
+}
+
+// Volume and area of one CUT cell from its 3^D neighbourhood (27 values,
+// [x][y][z], z index 0 in 2D): Get_corner, Get_cutcell_volume, Get_surface_area.
+void orc_cut_cell(int D, const double* p27, double dx, double dy, double dz, double* vol, double* area) {
+  double p[3][3][3], c[3][3][3];
+  std::memcpy(p, p27, sizeof(p));
+  gc_corner(D, p, c);
+  gc_cut_cell(D, c, dx, dy, dz, vol, area);
+}
+
+// Calculate_volume_mass over the interior cells of level `level` (after
+// orc_ls_build of that level) and Get_num_particles.  cell_vol / cell_area
+// (may be NULL) receive per-cell values over the full grid incl. margins
+// (zero outside the counted cells).  totals = {total_mass,
+// total_mass_surface, total_volume, total_area}; counts = {interface cells,
+// mesh particles, surface particles, particles}.
+void orc_volume_mass(const orc_ctx* c, int level, double* cell_vol, double* cell_area, double* totals,
+                     long long* counts) {
+  const int D = c->dim;
+  const orc_level& L = c->ls[level];
+  const double dl = ls_dl(L, D);
+  const double dx = ls_dcell(L, 0), dy = ls_dcell(L, 1), dz = D == 3 ? ls_dcell(L, 2) : 1.0;
+  const int n0 = 4 * L.num_pkg[0], n1 = 4 * L.num_pkg[1], n2 = D == 3 ? 4 * L.num_pkg[2] : 1;
+  long long ntot = 1;
+  for (int d = 0; d < D; d++) ntot *= ls_ncell(L, d);
+  std::vector<double> own_v, own_a;
+  if (!cell_vol) {
+    own_v.resize(ntot);
+    cell_vol = own_v.data();
+  }
+  if (!cell_area) {
+    own_a.resize(ntot);
+    cell_area = own_a.data();
+  }
+  std::fill(cell_vol, cell_vol + ntot, 0.0);
+  std::fill(cell_area, cell_area + ntot, 0.0);
+  // per-cell volumes and areas (the packages of the reference's parallel_for)
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int gk = 0; gk < n2; gk++)
+    for (int gj = 0; gj < n1; gj++)
+      for (int gi = 0; gi < n0; gi++) {
+        const long long a = ls_index(L, D, gi, gj, gk);
+        const double phi = L.phi[a];
+        if (!(phi > 0. || std::fabs(phi) < dl)) continue;
+        double vol, area = 0.;
+        if (L.tag[a] == CUT_CELL) {
+          double p[3][3][3] = {}, cr[3][3][3];
+          for (int r = 0; r < 3; r++)
+            for (int s = 0; s < 3; s++)
+              for (int t = 0; t < (D == 3 ? 3 : 1); t++)
+                p[r][s][t] = L.phi[ls_index(L, D, gi + r - 1, gj + s - 1, D == 3 ? gk + t - 1 : 0)];
+          gc_corner(D, p, cr);
+          gc_cut_cell(D, cr, dx, dy, dz, &vol, &area);
+        } else {
+          vol = (dx * dy) * dz;
+        }
+        cell_vol[a] = vol;
+        cell_area[a] = area;
+      }
+  // the sums in cell order
+  double M = 0., Ms = 0., V = 0., A = 0.;
+  long long ncut = 0;
+  for (int gk = 0; gk < n2; gk++)
+    for (int gj = 0; gj < n1; gj++)
+      for (int gi = 0; gi < n0; gi++) {
+        const long long a = ls_index(L, D, gi, gj, gk);
+        if (L.tag[a] == CUT_CELL) ncut++;
+        const double phi = L.phi[a];
+        if (!(phi > 0. || std::fabs(phi) < dl)) continue;
+        const double scale = get_scale(*c, D, phi, L.curv[a]);
+        if (L.tag[a] == CUT_CELL) {
+          A += cell_area[a];
+          Ms += cell_area[a] / powern(scale, D - 1);
+        }
+        M += cell_vol[a] / powern(scale, D);
+        V += cell_vol[a];
+      }
+  totals[0] = M;
+  totals[1] = Ms;
+  totals[2] = V;
+  totals[3] = A;
+  // Get_num_particles, sph_mesh_generation.cpp:909-923 (no segments or singularities)
+  long long n_surface = (long long)(Ms - 0.5 * 0.0);
+  if (n_surface < 0) n_surface = 0;
+  long long n_mesh = (long long)(M - 0.5 * Ms);
+  if (n_mesh < 0) n_mesh = 0;
+  if (ncut < n_surface) n_surface = ncut;
+  counts[0] = ncut;
+  counts[1] = n_mesh;
+  counts[2] = n_surface;
+  counts[3] = n_mesh + n_surface;
 }
 
 }  // extern "C"

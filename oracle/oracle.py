@@ -120,8 +120,36 @@ def lib():
         L.orc_triangulate.restype = C.c_longlong
         L.orc_cvp.argtypes = [C.POINTER(OrcCvpParams), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_void_p, C.c_void_p, C.POINTER(OrcCvpResult)]
+        L.orc_mc_table.argtypes = [C.c_void_p]
+        L.orc_mc_area.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+        L.orc_mc_area.restype = C.c_double
+        L.orc_cut_cell.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_volume_mass.argtypes = [C.POINTER(OrcCtx), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
+
+
+def mc_table() -> np.ndarray:
+    """The oracle's marching-cubes table, 256 x 16 edge indices (-1 padded)."""
+    t = np.zeros((256, 16), dtype=np.int8)
+    lib().orc_mc_table(_p(t))
+    return t
+
+
+def mc_area(corners: np.ndarray, dx: float, dy: float, dz: float) -> float:
+    """Marching-cubes area of a 3x3x3 corner lattice (get_area_MQ)."""
+    c = np.ascontiguousarray(corners, dtype=np.float64).reshape(27)
+    return float(lib().orc_mc_area(_p(c), dx, dy, dz))
+
+
+def cut_cell(dim: int, nbhd: np.ndarray, dx: float, dy: float, dz: float):
+    """(volume, area) of one CUT cell from its 3^D phi neighbourhood, given
+    as 3x3x3 [x][y][z] (z index 0 in 2D)."""
+    p = np.ascontiguousarray(nbhd, dtype=np.float64).reshape(27)
+    v, a = C.c_double(0.0), C.c_double(0.0)
+    lib().orc_cut_cell(dim, _p(p), dx, dy, dz, C.byref(v), C.byref(a))
+    return v.value, a.value
 
 
 def _p(a):
@@ -206,6 +234,24 @@ class Oracle:
         c.middle_dl = middle_dl_of(p, levels)
         self.state = None
         self.arrays = {}
+
+    # ------------------------------------------------------- volume / mass
+    def volume_mass(self, level: int = -1):
+        """Cut-cell volume, area and particle count of one level
+        (Calculate_total_volume_mass + Get_num_particles).  Returns a dict of
+        the totals and counts plus per-cell 'vol' and 'area' arrays over the
+        full grid incl. margins."""
+        if level < 0:
+            level += self.ctx.nls
+        ntot = self.fields[level]["phi"].size
+        vol = np.zeros(ntot)
+        area = np.zeros(ntot)
+        tot = np.zeros(4)
+        cnt = np.zeros(4, dtype=np.int64)
+        lib().orc_volume_mass(C.byref(self.ctx), level, _p(vol), _p(area), _p(tot), _p(cnt))
+        return {"total_mass": tot[0], "total_mass_surface": tot[1], "total_volume": tot[2],
+                "total_area": tot[3], "num_interface_cell": int(cnt[0]), "num_particle_mesh": int(cnt[1]),
+                "num_particle_surface": int(cnt[2]), "num_particle": int(cnt[3]), "vol": vol, "area": area}
 
     # ----------------------------------------------------------------- state
     def alloc(self, n: int):

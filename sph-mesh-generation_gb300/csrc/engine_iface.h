@@ -66,6 +66,13 @@ struct LsBuildDesc {
 };
 cudaError_t ls_build_level(const LsBuildDesc& L, const double* d_phi, double4* g64, double* c64, float4* g32,
                            float* c32, uint8_t* tag, unsigned long long* max_phi_bits, cudaStream_t s);
+// Cut-cell volume / area / mass of one built level (mrsph_levelset.cu);
+// synchronises s (the CUT cells and the cut sub-cubes size the later
+// passes); cnt holds 3 counters.
+// ncut_listed_host = {CUT cells, CUT cells in the mass sums}.
+cudaError_t ls_volume_mass(const LsSet& ls, int level, int D, double* cvol, double* carea, int* list,
+                           double* part, signed char* tab, unsigned long long* cnt, double* tot,
+                           long long* ncut_listed_host, cudaStream_t s);
 
 // sort / scan primitives (mrsph_sort.cu)
 void cell_scan(int* counts, int* cstart, int* blocksums, long long ncells, int ntotal, cudaStream_t s);

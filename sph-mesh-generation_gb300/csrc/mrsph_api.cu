@@ -308,6 +308,82 @@ int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, doubl
   return 0;
 }
 
+int mrsph_volume_mass(mrsph_handle* h, int level, mrsph_volume_mass_stats* out, double* cell_vol,
+                      double* cell_area) {
+  if (!h || !out) return fail(h, MRSPH_ERR_ARG, "null argument");
+  if (h->nls < 1) return fail(h, MRSPH_ERR_STATE, "mrsph_set_levelset must come first");
+  if (level < 0) level += h->nls;
+  if (level < 0 || level >= h->nls) return fail(h, MRSPH_ERR_ARG, "no such level");
+  API_CK(h, cudaSetDevice(h->prm.device));
+  const int D = h->prm.dim;
+  const LsLevel& L = h->ls.lv[level];
+  const long long ntot = h->ls_ntot[level];
+  long long nin = 1;
+  for (int d = 0; d < D; d++) nin *= 4LL * L.num_pkg[d];
+  if (ntot >= (1LL << 31)) return fail(h, MRSPH_ERR_RANGE, "level set grid above 2^31 cells");
+  const long long nb = (nin + 255) / 256;
+  // one scratch allocation: cvol, carea, part, tot (doubles), list, cnt, table
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  const size_t o_vol = take(sizeof(double) * ntot), o_area = take(sizeof(double) * ntot);
+  const size_t o_part = take(sizeof(double) * 4 * nb), o_tot = take(sizeof(double) * 4);
+  const size_t o_list = take(sizeof(int) * nin), o_cnt = take(3 * sizeof(unsigned long long));
+  const size_t o_tab = take(256 * 16);
+  char* buf = nullptr;
+  API_CK(h, cudaMalloc(&buf, off));
+  struct Free {
+    char* p;
+    ~Free() { cudaFree(p); }
+  } guard{buf};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  API_CK(h, cudaEventCreate(&e0));
+  API_CK(h, cudaEventCreate(&e1));
+  struct FreeEv {
+    cudaEvent_t a, b;
+    ~FreeEv() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } gev{e0, e1};
+  double* cvol = reinterpret_cast<double*>(buf + o_vol);
+  double* carea = reinterpret_cast<double*>(buf + o_area);
+  long long ncut[2] = {0, 0};
+  API_CK(h, cudaEventRecord(e0, h->stream));
+  API_CK(h, ls_volume_mass(h->ls, level, D, cvol, carea, reinterpret_cast<int*>(buf + o_list),
+                           reinterpret_cast<double*>(buf + o_part), reinterpret_cast<signed char*>(buf + o_tab),
+                           reinterpret_cast<unsigned long long*>(buf + o_cnt),
+                           reinterpret_cast<double*>(buf + o_tot), ncut, h->stream));
+  API_CK(h, cudaEventRecord(e1, h->stream));
+  double tot[4];
+  API_CK(h, cudaMemcpyAsync(tot, buf + o_tot, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
+  if (cell_vol) API_CK(h, cudaMemcpyAsync(cell_vol, cvol, sizeof(double) * ntot, cudaMemcpyDeviceToHost, h->stream));
+  if (cell_area)
+    API_CK(h, cudaMemcpyAsync(cell_area, carea, sizeof(double) * ntot, cudaMemcpyDeviceToHost, h->stream));
+  API_CK(h, cudaStreamSynchronize(h->stream));
+  float ms = 0.f;
+  API_CK(h, cudaEventElapsedTime(&ms, e0, e1));
+  out->total_mass = tot[0];
+  out->total_mass_surface = tot[1];
+  out->total_volume = tot[2];
+  out->total_area = tot[3];
+  out->num_interface_cell = ncut[0];
+  // Get_num_particles, sph_mesh_generation.cpp:909-923 (no segments or singularities)
+  long long n_surface = (long long)(tot[1] - 0.5 * 0.0);
+  if (n_surface < 0) n_surface = 0;
+  long long n_mesh = (long long)(tot[0] - 0.5 * tot[1]);
+  if (n_mesh < 0) n_mesh = 0;
+  if (ncut[0] < n_surface) n_surface = ncut[0];
+  out->num_particle_mesh = n_mesh;
+  out->num_particle_surface = n_surface;
+  out->num_particle = n_mesh + n_surface;
+  out->device_ms = ms;
+  return 0;
+}
+
 #define NEED_ENG(h)                                                                   \
   do {                                                                                \
     if (!(h)) return fail(nullptr, MRSPH_ERR_ARG, "null handle");                     \

@@ -189,7 +189,677 @@ __global__ void k_ls_to32(long long ntot, const double4* __restrict__ g, const d
   c32[a] = (float)c[a];
 }
 
+// ------------------------------------------------------------------------
+// Cut-cell volume, surface area and mass of one level (row F1):
+// Levelset_package::Calculate_volume_mass (lset_package.cpp:1283-1397) with
+// GeometryCalculator (geometry_calculator.cpp:12-570), FP64 in the
+// reference's operation order.
+//
+// A cut cell's volume fraction comes from adaptive bisection of its eight
+// half-cell sub-cubes (get_subvolume: up to six levels, corner values
+// averaged pairwise, a sign vote at the last level).  Every partial volume is
+// a multiple of 2^-23 of the cell, so the sum is exact in any order.  The
+// surface area polygonises each sub-cube by marching cubes; the polygons of a
+// sign case follow from the signs alone (a face with two diagonal corners
+// below zero cuts those corners off, as the reference's tables do on every
+// ambiguous face) and are split as fans from their lowest edge.
+
+// cube vertices of a sub-cube (geometry_calculator.cpp:296-297) and edges
+// (polygonise.cpp:37-60; the first endpoint is interpolated from)
+__constant__ unsigned char c_mcv[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0},
+                                          {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {1, 0, 1}};
+__constant__ unsigned char c_mce[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                           {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+__constant__ unsigned char c_mcf[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                          {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+
+__device__ int mc_edge_of(int a, int b) {
+  for (int e = 0; e < 12; e++)
+    if ((c_mce[e][0] == a && c_mce[e][1] == b) || (c_mce[e][0] == b && c_mce[e][1] == a)) return e;
+  return 0;
+}
+
+// One thread per sign case (bit v set: vertex v below zero): the polygons
+// of the case as fans of edge triples, -1 padded to 16 entries.
+__global__ void k_mc_table(signed char* __restrict__ tab) {
+  const int ci = threadIdx.x;
+  if (ci >= 256) return;
+  int nb[12][2], nn[12];
+  for (int e = 0; e < 12; e++) nn[e] = 0;
+  for (int f = 0; f < 6; f++) {
+    int in[4], es[4], cut[4], nc = 0;
+    for (int k = 0; k < 4; k++) in[k] = (ci >> c_mcf[f][k]) & 1;
+    for (int k = 0; k < 4; k++) es[k] = mc_edge_of(c_mcf[f][k], c_mcf[f][(k + 1) & 3]);
+    for (int k = 0; k < 4; k++)
+      if (in[k] != in[(k + 1) & 3]) cut[nc++] = es[k];
+    if (nc == 2) {
+      nb[cut[0]][nn[cut[0]]++] = cut[1];
+      nb[cut[1]][nn[cut[1]]++] = cut[0];
+    } else if (nc == 4) {
+      for (int k = 0; k < 4; k++)
+        if (in[k]) {
+          int a = es[(k + 3) & 3], b = es[k];
+          nb[a][nn[a]++] = b;
+          nb[b][nn[b]++] = a;
+        }
+    }
+  }
+  int n = 0;
+  bool seen[12];
+  for (int e = 0; e < 12; e++) seen[e] = false;
+  for (int s = 0; s < 12; s++) {
+    if (nn[s] != 2 || seen[s]) continue;
+    int cyc[12], m = 0, prev = s, cur = min(nb[s][0], nb[s][1]);
+    cyc[m++] = s;
+    seen[s] = true;
+    for (int guard = 0; cur != s && guard < 12; guard++) {  // a cycle has at most 12 edges
+      cyc[m++] = cur;
+      seen[cur] = true;
+      int nxt = nb[cur][0] == prev ? nb[cur][1] : nb[cur][0];
+      prev = cur;
+      cur = nxt;
+    }
+    for (int k = 1; k + 1 < m && n + 3 <= 15; k++) {
+      tab[ci * 16 + n++] = (signed char)cyc[0];
+      tab[ci * 16 + n++] = (signed char)cyc[k];
+      tab[ci * 16 + n++] = (signed char)cyc[k + 1];
+    }
+  }
+  for (; n < 16; n++) tab[ci * 16 + n] = -1;
+}
+
+// check_volume / check_face / mark_volume / mark_face: 1 all positive, 0 all negative, -1 cut
+__host__ __device__ inline int gc_mark(const double* v, int n) {
+  int flag = 0;
+  for (int q = 0; q < n; q++) flag += (v[q] > 0.0) - (v[q] < 0.0);
+  return flag == n ? 1 : (flag == -n ? 0 : -1);
+}
+
+// rf (3x3x3, [x][y][z]) from the 8 corners cor ([x][y][z]) in the order of
+// geometry_calculator.cpp:517-538
+template <class T>
+__host__ __device__ inline void gc_refine3(const T* cor, T* rf) {
+  const T h = (T)0.5;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < 2; k++) rf[(2 * i * 3 + 2 * j) * 3 + 2 * k] = cor[(i * 2 + j) * 2 + k];
+  for (int i = 0; i < 3; i += 2)
+    for (int j = 0; j < 3; j += 2) rf[(i * 3 + j) * 3 + 1] = h * (rf[(i * 3 + j) * 3 + 0] + rf[(i * 3 + j) * 3 + 2]);
+  for (int k = 0; k < 3; k++)
+    for (int i = 0; i < 3; i += 2) rf[(i * 3 + 1) * 3 + k] = h * (rf[(i * 3 + 0) * 3 + k] + rf[(i * 3 + 2) * 3 + k]);
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 3; k++) rf[(1 * 3 + j) * 3 + k] = h * (rf[(0 * 3 + j) * 3 + k] + rf[(2 * 3 + j) * 3 + k]);
+}
+
+// rf (3x3, [x][y]) from 4 corners, geometry_calculator.cpp:462-473
+template <class T>
+__host__ __device__ inline void gc_refine2(const T* cor, T* rf) {
+  const T h = (T)0.5;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) rf[2 * i * 3 + 2 * j] = cor[i * 2 + j];
+  for (int i = 0; i < 3; i += 2) rf[i * 3 + 1] = h * (rf[i * 3 + 0] + rf[i * 3 + 2]);
+  for (int j = 0; j < 3; j++) rf[3 + j] = h * (rf[0 + j] + rf[6 + j]);
+}
+
+template <int D, class T>
+__host__ __device__ inline void gc_refine(const T* cor, T* rf) {
+  if (D == 3) gc_refine3(cor, rf);
+  else gc_refine2(cor, rf);
+}
+
+// corners of child c of a refined lattice rf
+template <int D, class T>
+__host__ __device__ inline void gc_child(const T* rf, int c, T* sub) {
+  if (D == 3) {
+    const int i = c >> 2, j = (c >> 1) & 1, k = c & 1;
+    for (int r = 0; r < 2; r++)
+      for (int s = 0; s < 2; s++)
+        for (int t = 0; t < 2; t++) sub[(r * 2 + s) * 2 + t] = rf[((i + r) * 3 + (j + s)) * 3 + (k + t)];
+  } else {
+    const int i = c >> 1, j = c & 1;
+    for (int r = 0; r < 2; r++)
+      for (int s = 0; s < 2; s++) sub[r * 2 + s] = rf[(i + r) * 3 + (j + s)];
+  }
+}
+
+// FP64 corners of the node reached from the root corners cor by the child
+// indices path[0..n): the reference's refinements along that path.
+template <int D>
+__host__ __device__ __noinline__ void gc_path64(const double* cor, const int* path, int n, double* out) {
+  constexpr int NC = D == 3 ? 8 : 4, NR = D == 3 ? 27 : 9;
+  double cur[NC], rf[NR];
+  for (int q = 0; q < NC; q++) cur[q] = cor[q];
+  for (int l = 0; l < n; l++) {
+    gc_refine<D>(cur, rf);
+    gc_child<D>(rf, path[l], cur);
+  }
+  for (int q = 0; q < NC; q++) out[q] = cur[q];
+}
+
+// The node test of the bisection from FP32 corners s (see gc_walk32):
+// 1 all positive, 0 all negative, -1 cut.  When a corner lies within th of
+// zero the FP64 corners along path[0..n) from `node` decide, and are left
+// in s64 (*have64 = true).
+template <int D>
+__host__ __device__ inline int gc_test32(const float* s, float th, const double* node, const int* path, int n,
+                                         double* s64, bool* have64) {
+  constexpr int NC = D == 3 ? 8 : 4;
+  int pos = 0, neg = 0;
+  for (int q = 0; q < NC; q++) {
+    pos += s[q] > th;
+    neg += s[q] < -th;
+  }
+  if (pos + neg == NC) return pos == NC ? 1 : (neg == NC ? 0 : -1);
+  gc_path64<D>(node, path, n, s64);
+  *have64 = true;
+  return gc_mark(s64, NC);
+}
+
+// The bisection below a cut node at refinement level 2 (FP64 corners
+// `node`), in units of 2^-23 of the cell (geometry_calculator.cpp:450-570):
+// children of a level-l node weigh 8^-(l+2) (4^-(l+2) in 2D); a cut child
+// below level 6 is refined, at level 6 it counts 3/4, 1/2 or 1/4 of its
+// weight by the sign of its corner sum.  Four nested loops, the innermost
+// (the level-6 children, most of the work) unrolled so that its lattice
+// stays in registers.
+//
+// Only signs steer the walk, and they are taken from an FP32 copy of the
+// refinement.  With M the largest |corner| of the node, every FP32 value of
+// the walk lies within (1 + 3 * 4) * 2^-24 * M of the exact refinement of
+// the node's FP64 corners (one rounding for the copy, at most three chained
+// midpoints in each of the four levels) and every FP64 value within
+// 12 * 2^-53 * M, so an FP32 value beyond 2^-20 * M has the sign of the
+// FP64 value, and an FP32 corner sum beyond 2^-16 * M (eight such errors
+// plus seven rounded additions of magnitude <= 8M) the sign of the FP64 sum.
+// A node with a corner (or a corner sum) inside the bound takes its corners
+// from the FP64 refinements along its path from `node`, as the reference
+// computes them.
+template <int D>
+__host__ __device__ unsigned gc_walk32(const double* node) {
+  constexpr int NC = D == 3 ? 8 : 4, NR = D == 3 ? 27 : 9, LB = D == 3 ? 3 : 2;
+  constexpr int SH3 = 23 - 4 * LB, SH4 = 23 - 5 * LB, SH5 = 23 - 6 * LB, SH6 = 23 - 7 * LB;
+  double M = 0.0;
+  for (int q = 0; q < NC; q++) M = fmax(M, fabs(node[q]));
+  const float th = (float)(M * 0x1p-20) + 1.e-37f;
+  const float thc = (float)(M * 0x1p-16) + 1.e-37f;
+  float c32[NC], rf2[NR];
+  for (int q = 0; q < NC; q++) c32[q] = (float)node[q];
+  gc_refine<D>(c32, rf2);
+  unsigned acc = 0;
+  int path[4];
+  double s64[NC];
+  for (int c3 = 0; c3 < NC; c3++) {
+    path[0] = c3;
+    float s3[NC], rf3[NR];
+    gc_child<D>(rf2, c3, s3);
+    bool h64 = false;
+    const int f3 = gc_test32<D>(s3, th, node, path, 1, s64, &h64);
+    if (f3 == 1) acc += 1u << SH3;
+    if (f3 != -1) continue;
+    gc_refine<D>(s3, rf3);
+    for (int c4 = 0; c4 < NC; c4++) {
+      path[1] = c4;
+      float s4[NC], rf4[NR];
+      gc_child<D>(rf3, c4, s4);
+      const int f4 = gc_test32<D>(s4, th, node, path, 2, s64, &h64);
+      if (f4 == 1) acc += 1u << SH4;
+      if (f4 != -1) continue;
+      gc_refine<D>(s4, rf4);
+      for (int c5 = 0; c5 < NC; c5++) {
+        path[2] = c5;
+        float s5[NC], rf5[NR];
+        gc_child<D>(rf4, c5, s5);
+        const int f5 = gc_test32<D>(s5, th, node, path, 3, s64, &h64);
+        if (f5 == 1) acc += 1u << SH5;
+        if (f5 != -1) continue;
+        gc_refine<D>(s5, rf5);
+#pragma unroll
+        for (int c6 = 0; c6 < NC; c6++) {
+          path[3] = c6;
+          float s6[NC];
+          gc_child<D>(rf5, c6, s6);
+          bool have64 = false;
+          const int f6 = gc_test32<D>(s6, th, node, path, 4, s64, &have64);
+          if (f6 == 1) acc += 1u << SH6;
+          if (f6 != -1) continue;
+          float cv = 0.f;
+          for (int q = 0; q < NC; q++) cv += s6[q];
+          int sg;
+          if (fabsf(cv) > thc) {
+            sg = cv > 0.f ? 1 : -1;
+          } else {
+            if (!have64) gc_path64<D>(node, path, 4, s64);
+            double cv64 = 0.0;
+            for (int q = 0; q < NC; q++) cv64 += s64[q];
+            sg = cv64 > 0.0 ? 1 : (cv64 == 0.0 ? 0 : -1);
+          }
+          acc += (unsigned)(sg > 0 ? 3 : (sg == 0 ? 2 : 1)) << (SH6 - 2);
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// get_subvolume(0, 1/8, cor) (3D) or get_face(0, 1/4, cor) (2D),
+// geometry_calculator.cpp:450-570, in units of 2^-23 of the cell.  Every
+// partial volume of the bisection is a multiple of 2^-23 (weights 8^-k or
+// 4^-k, times 1/4, 1/2 or 3/4 at the last level, k <= 7), so the FP64 sum
+// is exact in any order and equals this integer sum.  Levels 0 and 1 are
+// refined in FP64 as the reference does; below, gc_walk32.
+template <int D>
+__host__ __device__ unsigned gc_units(const double* cor) {
+  constexpr int NC = D == 3 ? 8 : 4, NR = D == 3 ? 27 : 9, LB = D == 3 ? 3 : 2;
+  const int f0 = gc_mark(cor, NC);
+  if (f0 == 1) return 1u << (23 - LB);
+  if (f0 == 0) return 0u;
+  double rf0[NR], rf1[NR], s1[NC], s2[NC];
+  gc_refine<D>(cor, rf0);
+  unsigned acc = 0;
+  for (int c1 = 0; c1 < NC; c1++) {
+    gc_child<D>(rf0, c1, s1);
+    const int f1 = gc_mark(s1, NC);
+    if (f1 == 1) acc += 1u << (23 - 2 * LB);
+    if (f1 != -1) continue;
+    gc_refine<D>(s1, rf1);
+    for (int c2 = 0; c2 < NC; c2++) {
+      gc_child<D>(rf1, c2, s2);
+      const int f2 = gc_mark(s2, NC);
+      if (f2 == 1) acc += 1u << (23 - 3 * LB);
+      else if (f2 == -1) acc += gc_walk32<D>(s2);
+    }
+  }
+  return acc;
+}
+
+// Polygonise_MQ::VertexInterp at isolevel 0 (polygonise.cpp:74-92), one axis
+__device__ inline void mc_interp(const double* p1, const double* p2, double v1, double v2, double* o) {
+  if (fabs(0.0 - v1) < 1.0e-15) {
+    o[0] = p1[0]; o[1] = p1[1]; o[2] = p1[2];
+    return;
+  }
+  if (fabs(0.0 - v2) < 1.0e-15) {
+    o[0] = p2[0]; o[1] = p2[1]; o[2] = p2[2];
+    return;
+  }
+  if (fabs(v1 - v2) < 1.0e-15) {
+    o[0] = p1[0]; o[1] = p1[1]; o[2] = p1[2];
+    return;
+  }
+  const double mu = (0.0 - v1) / (v2 - v1);
+  for (int a = 0; a < 3; a++) o[a] = p1[a] + mu * (p2[a] - p1[a]);
+}
+
+// GeometryCalculator::get_area_tri, geometry_calculator.cpp:325-350
+__device__ inline double mc_tri_area(const double* p1, const double* p2, const double* p3) {
+  const double v1x = p2[0] - p1[0], v1y = p2[1] - p1[1], v1z = p2[2] - p1[2];
+  const double v3x = p3[0] - p1[0], v3y = p3[1] - p1[1], v3z = p3[2] - p1[2];
+  const double d1 = sqrt(v1x * v1x + v1y * v1y + v1z * v1z);
+  const double d3 = sqrt(v3x * v3x + v3y * v3y + v3z * v3z);
+  double a = 0.5 * (d3 * d1) * sin(acos((v1x * v3x + v1y * v3y + v1z * v3z) / (d3 * d1 + 1.e-20)));
+  return isnan(a) ? 0.0 : a;
+}
+
+// Marching-cubes area of sub-cube (i, j, k) of a 3x3x3 lattice c ([x][y][z]),
+// one term of get_area_MQ (geometry_calculator.cpp:283-321)
+__device__ double mc_subcube_area(const double* c, int i, int j, int k, double dx, double dy, double dz,
+                                  const signed char* tab) {
+  double p[8][3], val[8];
+  int ci = 0;
+  for (int v = 0; v < 8; v++) {
+    const int vx = i + c_mcv[v][0], vy = j + c_mcv[v][1], vz = k + c_mcv[v][2];
+    p[v][0] = vx * 0.5 * dx;
+    p[v][1] = vy * 0.5 * dy;
+    p[v][2] = vz * 0.5 * dz;
+    val[v] = c[(vx * 3 + vy) * 3 + vz];
+    if (val[v] < 0.0) ci |= 1 << v;
+  }
+  const signed char* t = tab + ci * 16;
+  double area = 0.0;
+  for (int q = 0; q < 15 && t[q] >= 0; q += 3) {
+    double a[3][3];
+    for (int u = 0; u < 3; u++) {
+      const int e = t[q + u], v0 = c_mce[e][0], v1 = c_mce[e][1];
+      mc_interp(p[v0], p[v1], val[v0], val[v1], a[u]);
+    }
+    area += mc_tri_area(a[0], a[1], a[2]);
+  }
+  return area;
+}
+
+__device__ inline long long vm_index(const LsLevel& L, int D, int gi, int gj, int gk) {
+  const long long m4 = 4 * L.margin;
+  return (((D == 3) ? gk + m4 : 0) * L.n[1] + (gj + m4)) * L.n[0] + (gi + m4);
+}
+
+__device__ inline void vm_cell_of(const LsLevel& L, int D, long long q, int* g) {
+  const int n0 = 4 * L.num_pkg[0], n1 = 4 * L.num_pkg[1];
+  g[0] = (int)(q % n0);
+  g[1] = (int)((q / n0) % n1);
+  g[2] = (D == 3) ? (int)(q / ((long long)n0 * n1)) : 0;
+}
+
+__device__ inline bool vm_counted(double phi, double dl) { return phi > 0. || fabs(phi) < dl; }
+
+// Pass 1, one thread per interior cell: CUT cells are counted
+// (glbl_num_interface_cell) and those the mass sums include are listed.
+__global__ void k_vm_list(LsLevel L, int D, long long nin, double dl, int* __restrict__ list,
+                          unsigned long long* __restrict__ cnt) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool cut = false, listed = false;
+  long long a = 0;
+  if (q < nin) {
+    int g[3];
+    vm_cell_of(L, D, q, g);
+    a = vm_index(L, D, g[0], g[1], g[2]);
+    cut = L.tag[a] != 0;
+    listed = cut && vm_counted(L.g64[a].x, dl);
+  }
+  const unsigned mc = __ballot_sync(0xffffffffu, cut), ml = __ballot_sync(0xffffffffu, listed);
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) {
+    if (mc) atomicAdd(cnt + 0, (unsigned long long)__popc(mc));
+    if (ml) base = atomicAdd(cnt + 1, (unsigned long long)__popc(ml));
+  }
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (listed) list[base + __popc(ml & ((1u << lane) - 1u))] = (int)(a);
+}
+
+// Pass 2, eight threads per listed CUT cell (thread s: half-cell sub-cube
+// (s>>2, (s>>1)&1, s&1)): Get_corner and Get_surface_area
+// (geometry_calculator.cpp:12-262) and the first level of
+// Get_cutcell_volume: full sub-cubes add their units to the cell, cut ones
+// become work items (cell, FP64 corners) for pass 2b.  Cells whose corner
+// lattice is not cut get their volume here.
+template <int D>
+__global__ void __launch_bounds__(256) k_vm_cut(LsLevel L, const int* __restrict__ list, long long nlist,
+                                                const signed char* __restrict__ gtab, double* __restrict__ cvol,
+                                                double* __restrict__ carea, unsigned* __restrict__ units,
+                                                signed char* __restrict__ mark, int* __restrict__ item_cell,
+                                                double* __restrict__ item_cor, unsigned long long* __restrict__ nitem) {
+  __shared__ signed char tab[256 * 16];
+  for (int t = threadIdx.x; t < 256 * 16 / 4; t += blockDim.x)
+    reinterpret_cast<int*>(tab)[t] = reinterpret_cast<const int*>(gtab)[t];
+  __syncthreads();
+  constexpr int NC = D == 3 ? 8 : 4;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const int s = threadIdx.x & 7;
+  const bool live = w < nlist;
+  const long long a = live ? list[w] : 0;
+  double area_s = 0.0, sub[8];
+  unsigned u = 0;
+  bool emit = false;
+  int marker = 0;
+  const double dx = L.dcell[0], dy = L.dcell[1], dz = D == 3 ? L.dcell[2] : 1.0;
+  if (live) {
+    // phii0: the 3^D neighbourhood (z index 0 in 2D)
+    double p[27], c[27];
+    const long long sx = 1, sy = L.n[0], sz = (long long)L.n[0] * L.n[1];
+    for (int r = 0; r < 3; r++)
+      for (int q = 0; q < 3; q++)
+        for (int t = 0; t < 3; t++) {
+          if (D == 2 && t > 0) {
+            p[(r * 3 + q) * 3 + t] = 0.0;
+            continue;
+          }
+          const long long off = (r - 1) * sx + (q - 1) * sy + (D == 3 ? (t - 1) * sz : 0);
+          p[(r * 3 + q) * 3 + t] = L.g64[a + off].x;
+        }
+    // Get_corner, geometry_calculator.cpp:12-77
+    constexpr int DZ = D == 3 ? 1 : 0;
+    auto P = [&](int r, int q, int t) { return p[(r * 3 + q) * 3 + t]; };
+    auto Cc = [&](int r, int q, int t) -> double& { return c[(r * 3 + q) * 3 + t]; };
+    for (int v = 0; v < 27; v++) c[v] = 0.0;
+    Cc(1, 1, DZ) = P(1, 1, DZ);
+    for (int r = 0; r < 2; r++)
+      for (int q = 0; q < 2; q++)
+        for (int t = 0; t < 1 + DZ; t++)
+          Cc(2 * r, 2 * q, 2 * t) = 0.125 * (P(r, q, t) + P(r + 1, q, t) + P(r, q + 1, t) + P(r + 1, q + 1, t) +
+                                             P(r, q, t + DZ) + P(r + 1, q, t + DZ) + P(r, q + 1, t + DZ) +
+                                             P(r + 1, q + 1, t + DZ));
+    if (DZ)
+      for (int r = 0; r < 2; r++)
+        for (int q = 0; q < 2; q++)
+          Cc(2 * r, 2 * q, 1) = 0.25 * (P(r, q, 1) + P(r + 1, q, 1) + P(r, q + 1, 1) + P(r + 1, q + 1, 1));
+    for (int q = 0; q < 2; q++)
+      for (int t = 0; t < 1 + DZ; t++)
+        Cc(1, 2 * q, 2 * t) = 0.25 * (P(1, q, t) + P(1, q, t + DZ) + P(1, q + 1, t) + P(1, q + 1, t + DZ));
+    for (int r = 0; r < 2; r++)
+      for (int t = 0; t < 1 + DZ; t++)
+        Cc(2 * r, 1, 2 * t) = 0.25 * (P(r, 1, t) + P(r + 1, 1, t) + P(r, 1, t + DZ) + P(r + 1, 1, t + DZ));
+    if (DZ)
+      for (int r = 0; r < 2; r++) {
+        Cc(2 * r, 1, 1) = 0.5 * (P(r, 1, 1) + P(r + 1, 1, 1));
+        Cc(1, 2 * r, 1) = 0.5 * (P(1, r, 1) + P(1, r + 1, 1));
+        Cc(1, 1, 2 * r) = 0.5 * (P(1, 1, r) + P(1, 1, r + 1));
+      }
+    if (D == 3) {
+      marker = gc_mark(c, 27);
+      if (marker == -1) {
+        const int i = s >> 2, j = (s >> 1) & 1, k = s & 1;
+        for (int r = 0; r < 2; r++)
+          for (int q = 0; q < 2; q++)
+            for (int t = 0; t < 2; t++) sub[(r * 2 + q) * 2 + t] = Cc(i + r, j + q, k + t);
+        area_s = mc_subcube_area(c, i, j, k, dx, dy, dz, tab);
+      }
+    } else {
+      double face[9], ext[27];
+      for (int r = 0; r < 3; r++)
+        for (int q = 0; q < 3; q++) face[r * 3 + q] = Cc(r, q, 0);
+      marker = gc_mark(face, 9);
+      if (marker == -1) {
+        if (s < 4) {
+          const int i = s >> 1, j = s & 1;
+          for (int r = 0; r < 2; r++)
+            for (int q = 0; q < 2; q++) sub[r * 2 + q] = face[(i + r) * 3 + (j + q)];
+        }
+        // the face extruded over a unit depth (geometry_calculator.cpp:137-148)
+        for (int r = 0; r < 3; r++)
+          for (int q = 0; q < 3; q++)
+            for (int t = 0; t < 3; t++) ext[(r * 3 + q) * 3 + t] = face[r * 3 + q];
+        area_s = mc_subcube_area(ext, s >> 2, (s >> 1) & 1, s & 1, dx, dy, 1.0, tab);
+      }
+    }
+    if (marker == -1 && (D == 3 || s < 4)) {
+      const int f = gc_mark(sub, NC);
+      if (f == 1) u = 1u << (23 - (D == 3 ? 3 : 2));
+      else if (f == -1) emit = true;
+    }
+  }
+  // work items, warp-aggregated
+  const unsigned me = __ballot_sync(0xffffffffu, emit);
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0 && me) base = atomicAdd(nitem, (unsigned long long)__popc(me));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (emit) {
+    const unsigned long long it = base + __popc(me & ((1u << lane) - 1u));
+    item_cell[it] = (int)w;
+    for (int q = 0; q < NC; q++) item_cor[it * NC + q] = sub[q];
+  }
+  // the eight sub-cubes of a cell in order (s = 0..7)
+  double asum = 0.0;
+  unsigned usum = 0;
+  const int g0 = threadIdx.x & 24;
+  for (int v = 0; v < 8; v++) {
+    asum += __shfl_sync(0xffffffffu, area_s, g0 + v);
+    usum += __shfl_sync(0xffffffffu, u, g0 + v);
+  }
+  if (live && s == 0) {
+    mark[w] = (signed char)marker;
+    units[w] = usum;
+    if (marker != -1) cvol[a] = (marker == 1 ? 1.0 : 0.0) * (dx * dy * dz);
+    carea[a] = marker == -1 ? asum : 0.0;
+  }
+}
+
+// Pass 2b, one thread per cut sub-cube: the bisection below it (gc_units),
+// added to its cell's units (integer, exact).
+template <int D>
+__global__ void __launch_bounds__(128) k_vm_frac(const int* __restrict__ item_cell, const double* __restrict__ item_cor,
+                                                 long long nitem, unsigned* __restrict__ units) {
+  constexpr int NC = D == 3 ? 8 : 4;
+  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nitem) return;
+  double cor[NC];
+  for (int q = 0; q < NC; q++) cor[q] = item_cor[it * NC + q];
+  const unsigned r = gc_units<D>(cor);
+  if (r) atomicAdd(units + item_cell[it], r);
+}
+
+// Pass 2c, one thread per listed cell with a cut corner lattice: volume =
+// min(fraction, 1) * cell volume (get_volume / get_area, then
+// Get_cutcell_volume).
+__global__ void k_vm_finish(const int* __restrict__ list, long long nlist, const unsigned* __restrict__ units,
+                            const signed char* __restrict__ mark, double dv, double* __restrict__ cvol) {
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nlist || mark[w] != -1) return;
+  const double vof = (double)units[w] * 0x1p-23;
+  const double H = vof <= 1.0 ? vof : 1.0;
+  cvol[list[w]] = H * dv;
+}
+
+// Pass 3, one thread per interior cell: the mass sums of
+// Calculate_volume_mass (lset_package.cpp:1340-1395) with
+// scale = Get_scale(curv, phi), into per-block partials (fixed order).
+template <int D>
+__global__ void __launch_bounds__(256) k_vm_reduce(LsSet ls, int level, long long nin, double dl,
+                                                   double* __restrict__ cvol, double* __restrict__ carea,
+                                                   double* __restrict__ part) {
+  const LsLevel& L = ls.lv[level];
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0., ms = 0., v = 0., ar = 0.;
+  if (q < nin) {
+    int g[3];
+    vm_cell_of(L, D, q, g);
+    const long long a = vm_index(L, D, g[0], g[1], g[2]);
+    const double phi = L.g64[a].x;
+    if (vm_counted(phi, dl)) {
+      const double scale = get_scale<double>(ls, phi, L.c64[a]);
+      double vol, area = 0.;
+      if (L.tag[a] != 0) {
+        vol = cvol[a];
+        area = carea[a];
+        double sp = 1.0;
+        for (int d = 0; d < D - 1; d++) sp *= scale;
+        ar = area;
+        ms = area / sp;
+      } else {
+        vol = (L.dcell[0] * L.dcell[1]) * (D == 3 ? L.dcell[2] : 1.0);
+        cvol[a] = vol;
+      }
+      double sp = 1.0;
+      for (int d = 0; d < D; d++) sp *= scale;
+      m = vol / sp;
+      v = vol;
+    }
+  }
+  __shared__ double sm[4][256];
+  sm[0][threadIdx.x] = m;
+  sm[1][threadIdx.x] = ms;
+  sm[2][threadIdx.x] = v;
+  sm[3][threadIdx.x] = ar;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int u = 0; u < 4; u++) sm[u][threadIdx.x] += sm[u][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) part[(long long)blockIdx.x * 4 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+// Pass 4, one block: the partials summed in a fixed order.
+__global__ void __launch_bounds__(256) k_vm_final(const double* __restrict__ part, long long nb,
+                                                  double* __restrict__ tot) {
+  __shared__ double sm[4][256];
+  double acc[4] = {0., 0., 0., 0.};
+  for (long long b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int u = 0; u < 4; u++) acc[u] += part[b * 4 + u];
+  for (int u = 0; u < 4; u++) sm[u][threadIdx.x] = acc[u];
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int u = 0; u < 4; u++) sm[u][threadIdx.x] += sm[u][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) tot[threadIdx.x] = sm[threadIdx.x][0];
+}
+
 }  // namespace
+
+// Cut-cell volume / area / mass pass of one level (see above).  Device
+// buffers: cvol, carea (full grid incl. margins, zeroed here), list (one int
+// per interior cell), part (4 doubles per 256 interior cells), tab (4 KB),
+// cnt (3 counters), tot (4 doubles); the work items of the cut sub-cubes
+// are allocated here once their number is known.  Enqueued on s, which is
+// synchronised twice.
+cudaError_t ls_volume_mass(const LsSet& ls, int level, int D, double* cvol, double* carea, int* list,
+                           double* part, signed char* tab, unsigned long long* cnt, double* tot,
+                           long long* ncut_listed_host, cudaStream_t s) {
+  const LsLevel& L = ls.lv[level];
+  long long ntot = 1, nin = 1;
+  for (int d = 0; d < D; d++) {
+    ntot *= L.n[d];
+    nin *= 4LL * L.num_pkg[d];
+  }
+  double dl = 1.e20;  // lset_level_infor.cpp:48-52
+  for (int d = 0; d < D; d++) dl = dl <= L.dcell[d] ? dl : L.dcell[d];
+  const double dv = (L.dcell[0] * L.dcell[1]) * (D == 3 ? L.dcell[2] : 1.0);
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(cvol, 0, sizeof(double) * ntot, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(carea, 0, sizeof(double) * ntot, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
+  k_mc_table<<<1, 256, 0, s>>>(tab);
+  const long long nb = (nin + 255) / 256;
+  k_vm_list<<<(unsigned)nb, 256, 0, s>>>(L, D, nin, dl, list, cnt);
+  unsigned long long hc[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  ncut_listed_host[0] = (long long)hc[0];
+  ncut_listed_host[1] = (long long)hc[1];
+  const long long nl = (long long)hc[1];
+  if (nl > 0) {
+    // per listed cell: units, corner-lattice marker; at most 8 (4) work items each
+    const int NC = D == 3 ? 8 : 4;
+    const long long cap = nl * NC;
+    char* buf = nullptr;
+    const size_t o_units = 0, o_mark = (size_t)((sizeof(unsigned) * nl + 255) & ~255LL);
+    const size_t o_cell = o_mark + (size_t)((nl + 255) & ~255LL);
+    const size_t o_cor = o_cell + (size_t)((sizeof(int) * cap + 255) & ~255LL);
+    const size_t bytes = o_cor + sizeof(double) * NC * cap;
+    if ((e = cudaMalloc(&buf, bytes)) != cudaSuccess) return e;
+    unsigned* units = reinterpret_cast<unsigned*>(buf + o_units);
+    signed char* mark = reinterpret_cast<signed char*>(buf + o_mark);
+    int* item_cell = reinterpret_cast<int*>(buf + o_cell);
+    double* item_cor = reinterpret_cast<double*>(buf + o_cor);
+    const long long nbc = (nl * 8 + 255) / 256;
+    if (D == 3)
+      k_vm_cut<3><<<(unsigned)nbc, 256, 0, s>>>(L, list, nl, tab, cvol, carea, units, mark, item_cell, item_cor,
+                                                cnt + 2);
+    else
+      k_vm_cut<2><<<(unsigned)nbc, 256, 0, s>>>(L, list, nl, tab, cvol, carea, units, mark, item_cell, item_cor,
+                                                cnt + 2);
+    unsigned long long ni = 0;
+    if ((e = cudaMemcpyAsync(&ni, cnt + 2, sizeof(ni), cudaMemcpyDeviceToHost, s)) == cudaSuccess &&
+        (e = cudaStreamSynchronize(s)) == cudaSuccess) {
+      if (ni > 0) {
+        const long long nbi = ((long long)ni + 127) / 128;
+        if (D == 3) k_vm_frac<3><<<(unsigned)nbi, 128, 0, s>>>(item_cell, item_cor, (long long)ni, units);
+        else k_vm_frac<2><<<(unsigned)nbi, 128, 0, s>>>(item_cell, item_cor, (long long)ni, units);
+      }
+      k_vm_finish<<<(unsigned)((nl + 255) / 256), 256, 0, s>>>(list, nl, units, mark, dv, cvol);
+      e = cudaStreamSynchronize(s);
+    }
+    cudaError_t e2 = cudaFree(buf);
+    if (e != cudaSuccess) return e;
+    if (e2 != cudaSuccess) return e2;
+  }
+  if (D == 3) k_vm_reduce<3><<<(unsigned)nb, 256, 0, s>>>(ls, level, nin, dl, cvol, carea, part);
+  else k_vm_reduce<2><<<(unsigned)nb, 256, 0, s>>>(ls, level, nin, dl, cvol, carea, part);
+  k_vm_final<<<1, 256, 0, s>>>(part, nb, tot);
+  return cudaGetLastError();
+}
 
 // Builds one level in place: g64 (phi, n), c64, tag, and its float copies.
 // max_phi_bits[0] accumulates the maximum positive interior phi, [1] and [2]

@@ -3,11 +3,13 @@
 // relaxation path: build a workload, seed, relax, write particle restarts.
 //
 //   mrsph_relax --case disc_hole_2d|torus_3d [--precision fp32|fp64] [--steps N]
-//               [--n N] [--output-every K] [--out DIR] [--count-only]
+//               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
 // particle-steps/s, final time step).  --count-only prints the particle count
-// of the workload without touching a GPU.  Exit status 2 on an engine error.
+// of the workload without touching a GPU; --cut-cell-count seeds the count of
+// the reference's cut-cell volume pass on the finest level (Get_num_particles)
+// instead of the workload's.  Exit status 2 on an engine error.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -21,7 +23,7 @@ int main(int argc, char** argv) {
   std::string wl = "disc_hole_2d", out, prec;
   int steps = -1, every = 0;
   long long n = -1;
-  bool count_only = false;
+  bool count_only = false, cut_cell = false;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     auto val = [&]() -> std::string {
@@ -38,9 +40,10 @@ int main(int argc, char** argv) {
     else if (s == "--output-every") every = std::atoi(val().c_str());
     else if (s == "--out") out = val();
     else if (s == "--count-only") count_only = true;
+    else if (s == "--cut-cell-count") cut_cell = true;
     else if (s == "--help" || s == "-h") {
       std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
-                  "                   [--output-every K] [--out DIR] [--count-only]\n");
+                  "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
@@ -63,6 +66,7 @@ int main(int argc, char** argv) {
     }
     if (steps < 0) steps = c.steps;
     SPH_mesh_generation sim(c);
+    if (cut_cell && n < 0) n = sim.Get_num_particles();
     sim.Initialize_case(n);
     Solver solver(sim);
     double ms;

@@ -265,6 +265,12 @@ void SPH_mesh_generation::Initialize_case(long long n) {
   check(mrsph_seed(h_, n_), "mrsph_seed");
 }
 
+mrsph_volume_mass_stats SPH_mesh_generation::Calculate_total_volume_mass(int level) {
+  mrsph_volume_mass_stats st{};
+  check(mrsph_volume_mass(h_, level, &st, nullptr, nullptr), "mrsph_volume_mass");
+  return st;
+}
+
 void SPH_mesh_generation::SPH_run_mesh_generation(int nsteps) { check(mrsph_step(h_, nsteps), "mrsph_step"); }
 
 void SPH_mesh_generation::Run_phase(int phase) { check(mrsph_run_phase(h_, phase), "mrsph_run_phase"); }

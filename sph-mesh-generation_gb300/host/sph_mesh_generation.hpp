@@ -89,6 +89,12 @@ class SPH_mesh_generation {
   // Random_particle_distribution + Pre_run (sph_mesh_generation.cpp:1302-1367,
   // 1010-1050); n < 0 takes the case's particle count.
   void Initialize_case(long long n = -1);
+  // Levelset::Calculate_total_volume_mass (level_set.cpp:930-972) on one
+  // level (< 0: the finest): cut-cell volumes, surface areas, masses and the
+  // particle numbers of Get_num_particles (sph_mesh_generation.cpp:900-940).
+  mrsph_volume_mass_stats Calculate_total_volume_mass(int level = -1);
+  // The reference's particle count (glbl_total_num_particle) of that level.
+  long long Get_num_particles(int level = -1) { return Calculate_total_volume_mass(level).num_particle; }
   // SPH_run_mesh_generation x nsteps (sph_mesh_generation.cpp:1371-1463).
   void SPH_run_mesh_generation(int nsteps = 1);
   // glbl_timestep after the last step (SPH::Get_timestep, sph.cpp:224-227).

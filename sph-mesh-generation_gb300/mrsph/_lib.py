@@ -65,6 +65,13 @@ class TriQuality(C.Structure):
                 [("hist", C.c_longlong * 45)])
 
 
+class VolumeMassStats(C.Structure):
+    _fields_ = ([(k, C.c_double) for k in ("total_mass", "total_mass_surface", "total_volume", "total_area")] +
+                [(k, C.c_longlong) for k in ("num_interface_cell", "num_particle_mesh", "num_particle_surface",
+                                             "num_particle")] +
+                [("device_ms", C.c_double)])
+
+
 class StateIn(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("v", C.c_void_p), ("type", C.c_void_p), ("h", C.c_void_p),
                 ("level", C.c_void_p), ("nu", C.c_void_p), ("dt", C.c_double), ("step", C.c_longlong)]
@@ -77,6 +84,7 @@ EXPORTS = {
     "mrsph_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),
     "mrsph_set_levelset": ([C.c_void_p, C.c_int, C.POINTER(LevelsetLevel)], C.c_int),
     "mrsph_get_levelset": ([C.c_void_p, C.c_int] + [C.c_void_p] * 5 + [C.POINTER(C.c_double)], C.c_int),
+    "mrsph_volume_mass": ([C.c_void_p, C.c_int, C.POINTER(VolumeMassStats), C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_sample_levelset": ([C.c_void_p, C.c_longlong] + [C.c_void_p] * 5, C.c_int),
     "mrsph_sample_levelset_noalloc": ([C.c_void_p, C.c_longlong] + [C.c_void_p] * 5, C.c_int),
     "mrsph_seed": ([C.c_void_p, C.c_longlong], C.c_int),

@@ -208,6 +208,24 @@ class SPHMeshGeneration:
                 self.h, "mrsph_sample_levelset")
         return phi, nrm, curv, tag
 
+    def volume_mass(self, level: int = -1, cells: bool = False) -> dict:
+        """Cut-cell volume, surface area and particle numbers of one level-set
+        level (Levelset::Calculate_total_volume_mass + Get_num_particles).
+        With cells=True the dict also holds per-cell 'vol' and 'area' arrays
+        shaped like the level's phi."""
+        s = L.VolumeMassStats()
+        lv = self.case.levels[level]
+        vol = area = None
+        if cells:
+            vol = np.zeros(lv.phi.shape)
+            area = np.zeros(lv.phi.shape)
+        L.check(self.lib.mrsph_volume_mass(self.h, level, C.byref(s), _ptr(vol) if cells else None,
+                                           _ptr(area) if cells else None), self.h, "mrsph_volume_mass")
+        out = {f: getattr(s, f) for f, _ in L.VolumeMassStats._fields_}
+        if cells:
+            out["vol"], out["area"] = vol, area
+        return out
+
     def sample_levelset_noalloc(self, xyz: np.ndarray):
         """Same as sample_levelset without any device allocation (<= 65536 points)."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)

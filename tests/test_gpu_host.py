@@ -43,3 +43,18 @@ def test_cpp_driver_torus_fp32():
     assert r.returncode == 0, r.stderr
     d = json.loads(r.stdout)
     assert d["n_particles"] == 2410164 and d["step"] == 3 and d["particle_steps_per_s"] > 0
+
+
+def test_cpp_driver_cut_cell_count():
+    """--cut-cell-count seeds the reference's particle count (Get_num_particles
+    over the cut-cell volume pass), the count the Python mirror reports."""
+    binary = build.build_host()
+    r = subprocess.run([binary, "--case", "disc_hole_2d", "--precision", "fp64", "--steps", "2", "--cut-cell-count"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    g = SPHMeshGeneration(case, precision="fp64")
+    n = g.volume_mass(-1)["num_particle"]
+    g.close()
+    assert d["n_particles"] == n and d["step"] == 2 and d["flags"] == 0
