@@ -336,140 +336,228 @@ __host__ __device__ __noinline__ void gc_path64(const double* cor, const int* pa
   for (int q = 0; q < NC; q++) out[q] = cur[q];
 }
 
-// The node test of the bisection from FP32 corners s (see gc_walk32):
-// 1 all positive, 0 all negative, -1 cut.  When a corner lies within th of
-// zero the FP64 corners along path[0..n) from `node` decide, and are left
-// in s64 (*have64 = true).
+// FP32 corners of child c of a node with FP32 corners p: the midpoints of
+// the refinement taken axis by axis (z, then y, then x) with selects, so that
+// no index depends on c; each value takes at most three rounded midpoints
+// (two in 2D) from the node's corners.
 template <int D>
-__host__ __device__ inline int gc_test32(const float* s, float th, const double* node, const int* path, int n,
-                                         double* s64, bool* have64) {
-  constexpr int NC = D == 3 ? 8 : 4;
-  int pos = 0, neg = 0;
-  for (int q = 0; q < NC; q++) {
-    pos += s[q] > th;
-    neg += s[q] < -th;
+__device__ inline void gc_child32(const float* p, int c, float* out) {
+  if (D == 3) {
+    const bool i = (c >> 2) & 1, j = (c >> 1) & 1, k = c & 1;
+    float z[2][2][2], y[2][2][2];
+    for (int x = 0; x < 2; x++)
+      for (int yy = 0; yy < 2; yy++) {
+        const float a = p[(x * 2 + yy) * 2 + 0], b = p[(x * 2 + yy) * 2 + 1], m = 0.5f * (a + b);
+        z[x][yy][0] = k ? m : a;
+        z[x][yy][1] = k ? b : m;
+      }
+    for (int x = 0; x < 2; x++)
+      for (int t = 0; t < 2; t++) {
+        const float a = z[x][0][t], b = z[x][1][t], m = 0.5f * (a + b);
+        y[x][0][t] = j ? m : a;
+        y[x][1][t] = j ? b : m;
+      }
+    for (int s = 0; s < 2; s++)
+      for (int t = 0; t < 2; t++) {
+        const float a = y[0][s][t], b = y[1][s][t], m = 0.5f * (a + b);
+        out[(0 * 2 + s) * 2 + t] = i ? m : a;
+        out[(1 * 2 + s) * 2 + t] = i ? b : m;
+      }
+  } else {
+    const bool i = (c >> 1) & 1, j = c & 1;
+    float y[2][2];
+    for (int x = 0; x < 2; x++) {
+      const float a = p[x * 2 + 0], b = p[x * 2 + 1], m = 0.5f * (a + b);
+      y[x][0] = j ? m : a;
+      y[x][1] = j ? b : m;
+    }
+    for (int s = 0; s < 2; s++) {
+      const float a = y[0][s], b = y[1][s], m = 0.5f * (a + b);
+      out[0 * 2 + s] = i ? m : a;
+      out[1 * 2 + s] = i ? b : m;
+    }
   }
-  if (pos + neg == NC) return pos == NC ? 1 : (neg == NC ? 0 : -1);
-  gc_path64<D>(node, path, n, s64);
-  *have64 = true;
-  return gc_mark(s64, NC);
 }
 
-// The bisection below a cut node at refinement level 2 (FP64 corners
-// `node`), in units of 2^-23 of the cell (geometry_calculator.cpp:450-570):
-// children of a level-l node weigh 8^-(l+2) (4^-(l+2) in 2D); a cut child
-// below level 6 is refined, at level 6 it counts 3/4, 1/2 or 1/4 of its
-// weight by the sign of its corner sum.  Four nested loops, the innermost
-// (the level-6 children, most of the work) unrolled so that its lattice
-// stays in registers.
-//
-// Only signs steer the walk, and they are taken from an FP32 copy of the
-// refinement.  With M the largest |corner| of the node, every FP32 value of
-// the walk lies within (1 + 3 * 4) * 2^-24 * M of the exact refinement of
-// the node's FP64 corners (one rounding for the copy, at most three chained
-// midpoints in each of the four levels) and every FP64 value within
-// 12 * 2^-53 * M, so an FP32 value beyond 2^-20 * M has the sign of the
-// FP64 value, and an FP32 corner sum beyond 2^-16 * M (eight such errors
-// plus seven rounded additions of magnitude <= 8M) the sign of the FP64 sum.
-// A node with a corner (or a corner sum) inside the bound takes its corners
-// from the FP64 refinements along its path from `node`, as the reference
-// computes them.
+// Shared state of one warp of k_vm_walk.
 template <int D>
-__host__ __device__ unsigned gc_walk32(const double* node) {
-  constexpr int NC = D == 3 ? 8 : 4, NR = D == 3 ? 27 : 9, LB = D == 3 ? 3 : 2;
-  constexpr int SH3 = 23 - 4 * LB, SH4 = 23 - 5 * LB, SH5 = 23 - 6 * LB, SH6 = 23 - 7 * LB;
-  double M = 0.0;
-  for (int q = 0; q < NC; q++) M = fmax(M, fabs(node[q]));
-  const float th = (float)(M * 0x1p-20) + 1.e-37f;
-  const float thc = (float)(M * 0x1p-16) + 1.e-37f;
-  float c32[NC], rf2[NR];
-  for (int q = 0; q < NC; q++) c32[q] = (float)node[q];
-  gc_refine<D>(c32, rf2);
+struct VmWarp {
+  static constexpr int NC = D == 3 ? 8 : 4;
+  double s1[NC][NC];        // cut level-1 nodes (FP64 corners)
+  double anc[NC * NC][NC];  // cut level-2 nodes, the anchors (FP64 corners)
+  float th[NC * NC], thc[NC * NC];
+  float q2[NC * NC][NC];    // queue of level-2 nodes (FP32 corners)
+  int c2[NC * NC];          // their codes: anchor << 12 | child path (3 bits per level)
+  float q[3][32][NC];       // queues of levels 3..5
+  int c[3][32];
+};
+
+// Pass 2b, one warp per cut sub-cube: get_subvolume(0, 1/8, cor) (3D) or
+// get_face(0, 1/4, cor) (2D), geometry_calculator.cpp:450-570, in units of
+// 2^-23 of the cell, added to the cell's units.  Every partial volume of the
+// bisection is a multiple of 2^-23 (weights 8^-k or 4^-k, times 1/4, 1/2 or
+// 3/4 at the last level, k <= 7), so the FP64 sum is exact in any order and
+// equals this integer sum.  Children of a level-l node weigh 8^-(l+2)
+// (4^-(l+2)); a cut child below level 6 is refined, at level 6 it counts
+// 3/4, 1/2 or 1/4 of its weight by the sign of its corner sum.
+//
+// Levels 1 and 2 are refined in FP64 as the reference does; the cut level-2
+// nodes (anchors) are then bisected breadth-first by the whole warp, one
+// (node, child) pair per lane, deepest queue first (so no queue below level
+// 2 holds more than 32 nodes).  Only signs steer the bisection, and below
+// the anchors they are taken from FP32 copies: with M the largest |corner|
+// of the anchor, every FP32 value lies within (1 + 3 * 4) * 2^-24 * M of the
+// exact refinement of the anchor's FP64 corners (one rounding for the copy,
+// at most three rounded midpoints in each of four levels) and every FP64
+// value within 12 * 2^-53 * M, so an FP32 value beyond 2^-20 * M has the
+// sign of the FP64 value, and an FP32 corner sum beyond 2^-16 * M (eight
+// such errors plus seven rounded additions of magnitude <= 8M) the sign of
+// the FP64 sum.  A child with a corner (or a corner sum) inside the bound
+// takes its corners from the FP64 refinements along its path from the
+// anchor, as the reference computes them.
+template <int D>
+__global__ void __launch_bounds__(128) k_vm_walk(const int* __restrict__ item_cell, const double* __restrict__ item_cor,
+                                                 long long nitem, unsigned* __restrict__ units) {
+  constexpr int NC = D == 3 ? 8 : 4, NR = D == 3 ? 27 : 9, LB = D == 3 ? 3 : 2, NB = 32 / NC;
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ VmWarp<D> smem[4];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long it = (long long)blockIdx.x * 4 + wid;
+  if (it >= nitem) return;  // whole warps
+  VmWarp<D>& S = smem[wid];
+  const unsigned below = (1u << lane) - 1u;
+  double root[NC];
+  for (int q = 0; q < NC; q++) root[q] = item_cor[it * NC + q];
   unsigned acc = 0;
-  int path[4];
-  double s64[NC];
-  for (int c3 = 0; c3 < NC; c3++) {
-    path[0] = c3;
-    float s3[NC], rf3[NR];
-    gc_child<D>(rf2, c3, s3);
-    bool h64 = false;
-    const int f3 = gc_test32<D>(s3, th, node, path, 1, s64, &h64);
-    if (f3 == 1) acc += 1u << SH3;
-    if (f3 != -1) continue;
-    gc_refine<D>(s3, rf3);
-    for (int c4 = 0; c4 < NC; c4++) {
-      path[1] = c4;
-      float s4[NC], rf4[NR];
-      gc_child<D>(rf3, c4, s4);
-      const int f4 = gc_test32<D>(s4, th, node, path, 2, s64, &h64);
-      if (f4 == 1) acc += 1u << SH4;
-      if (f4 != -1) continue;
-      gc_refine<D>(s4, rf4);
-      for (int c5 = 0; c5 < NC; c5++) {
-        path[2] = c5;
-        float s5[NC], rf5[NR];
-        gc_child<D>(rf4, c5, s5);
-        const int f5 = gc_test32<D>(s5, th, node, path, 3, s64, &h64);
-        if (f5 == 1) acc += 1u << SH5;
-        if (f5 != -1) continue;
-        gc_refine<D>(s5, rf5);
-#pragma unroll
-        for (int c6 = 0; c6 < NC; c6++) {
-          path[3] = c6;
-          float s6[NC];
-          gc_child<D>(rf5, c6, s6);
-          bool have64 = false;
-          const int f6 = gc_test32<D>(s6, th, node, path, 4, s64, &have64);
-          if (f6 == 1) acc += 1u << SH6;
-          if (f6 != -1) continue;
+  // level 1 (FP64), one child per lane
+  bool cut1 = false;
+  if (lane < NC) {
+    double rf[NR], s1[NC];
+    gc_refine<D>(root, rf);
+    gc_child<D>(rf, lane, s1);
+    const int f = gc_mark(s1, NC);
+    if (f == 1) acc += 1u << (23 - 2 * LB);
+    if (f == -1) {
+      cut1 = true;
+      for (int q = 0; q < NC; q++) S.s1[lane][q] = s1[q];
+    }
+  }
+  const unsigned m1 = __ballot_sync(FULL, cut1);
+  __syncwarp();
+  // level 2 (FP64): the anchors
+  int n2 = 0;
+  for (int t0 = 0; t0 < NC * NC; t0 += 32) {
+    const int t = t0 + lane;
+    bool app = false;
+    double s2[NC];
+    if (t < NC * NC && ((m1 >> (t / NC)) & 1)) {
+      double p[NC], rf[NR];
+      for (int q = 0; q < NC; q++) p[q] = S.s1[t / NC][q];
+      gc_refine<D>(p, rf);
+      gc_child<D>(rf, t % NC, s2);
+      const int f = gc_mark(s2, NC);
+      if (f == 1) acc += 1u << (23 - 3 * LB);
+      app = f == -1;
+    }
+    const unsigned ma = __ballot_sync(FULL, app);
+    if (app) {
+      const int pos = n2 + __popc(ma & below);
+      double M = 0.0;
+      for (int q = 0; q < NC; q++) {
+        S.anc[pos][q] = s2[q];
+        S.q2[pos][q] = (float)s2[q];
+        M = fmax(M, fabs(s2[q]));
+      }
+      S.th[pos] = (float)(M * 0x1p-20) + 1.e-37f;
+      S.thc[pos] = (float)(M * 0x1p-16) + 1.e-37f;
+      S.c2[pos] = pos << 12;
+    }
+    n2 += __popc(ma);
+  }
+  __syncwarp();
+  // levels 3..6 (FP32 signs): queue 0 = level 2, queues 1..3 = levels 3..5
+  int n0 = n2, n1 = 0, nq2 = 0, n3 = 0;
+  for (int guard = 0; guard < (1 << 20); guard++) {
+    const int l = n3 ? 3 : (nq2 ? 2 : (n1 ? 1 : (n0 ? 0 : -1)));  // deepest non-empty queue
+    if (l < 0) break;
+    const int have = l == 0 ? n0 : (l == 1 ? n1 : (l == 2 ? nq2 : n3));
+    const int k = have < NB ? have : NB;
+    const int base = have - k;
+    if (l == 0) n0 -= k;
+    else if (l == 1) n1 -= k;
+    else if (l == 2) nq2 -= k;
+    else n3 -= k;
+    const int nd = lane / NC, c = lane % NC;
+    const bool live = nd < k;
+    float pc[NC], ch[NC];
+    int code = 0;
+    if (live) {
+      const float* src = l == 0 ? S.q2[base + nd] : S.q[l - 1][base + nd];
+      for (int q = 0; q < NC; q++) pc[q] = src[q];
+      code = l == 0 ? S.c2[base + nd] : S.c[l - 1][base + nd];
+    }
+    __syncwarp();
+    const int lev = l + 3;                  // the child's refinement level
+    const int sh = 23 - LB * (lev + 1);     // its weight, 2^sh units
+    int f = 2;
+    bool push = false;
+    if (live) {
+      gc_child32<D>(pc, c, ch);
+      const int anc = code >> 12;
+      const float th = S.th[anc];
+      int pos = 0, neg = 0;
+      for (int q = 0; q < NC; q++) {
+        pos += ch[q] > th;
+        neg += ch[q] < -th;
+      }
+      double s64[NC];
+      bool have64 = false;
+      int path[4];
+      for (int m = 0; m < l; m++) path[m] = (code >> (3 * m)) & 7;
+      path[l] = c;
+      if (pos + neg == NC) {
+        f = pos == NC ? 1 : (neg == NC ? 0 : -1);
+      } else {
+        gc_path64<D>(S.anc[anc], path, l + 1, s64);
+        have64 = true;
+        f = gc_mark(s64, NC);
+      }
+      if (f == 1) acc += 1u << sh;
+      if (f == -1) {
+        if (lev <= 5) {
+          push = true;
+        } else {
           float cv = 0.f;
-          for (int q = 0; q < NC; q++) cv += s6[q];
+          for (int q = 0; q < NC; q++) cv += ch[q];
           int sg;
-          if (fabsf(cv) > thc) {
+          if (fabsf(cv) > S.thc[anc]) {
             sg = cv > 0.f ? 1 : -1;
           } else {
-            if (!have64) gc_path64<D>(node, path, 4, s64);
+            if (!have64) gc_path64<D>(S.anc[anc], path, l + 1, s64);
             double cv64 = 0.0;
             for (int q = 0; q < NC; q++) cv64 += s64[q];
             sg = cv64 > 0.0 ? 1 : (cv64 == 0.0 ? 0 : -1);
           }
-          acc += (unsigned)(sg > 0 ? 3 : (sg == 0 ? 2 : 1)) << (SH6 - 2);
+          acc += (unsigned)(sg > 0 ? 3 : (sg == 0 ? 2 : 1)) << (sh - 2);
         }
       }
     }
-  }
-  return acc;
-}
-
-// get_subvolume(0, 1/8, cor) (3D) or get_face(0, 1/4, cor) (2D),
-// geometry_calculator.cpp:450-570, in units of 2^-23 of the cell.  Every
-// partial volume of the bisection is a multiple of 2^-23 (weights 8^-k or
-// 4^-k, times 1/4, 1/2 or 3/4 at the last level, k <= 7), so the FP64 sum
-// is exact in any order and equals this integer sum.  Levels 0 and 1 are
-// refined in FP64 as the reference does; below, gc_walk32.
-template <int D>
-__host__ __device__ unsigned gc_units(const double* cor) {
-  constexpr int NC = D == 3 ? 8 : 4, NR = D == 3 ? 27 : 9, LB = D == 3 ? 3 : 2;
-  const int f0 = gc_mark(cor, NC);
-  if (f0 == 1) return 1u << (23 - LB);
-  if (f0 == 0) return 0u;
-  double rf0[NR], rf1[NR], s1[NC], s2[NC];
-  gc_refine<D>(cor, rf0);
-  unsigned acc = 0;
-  for (int c1 = 0; c1 < NC; c1++) {
-    gc_child<D>(rf0, c1, s1);
-    const int f1 = gc_mark(s1, NC);
-    if (f1 == 1) acc += 1u << (23 - 2 * LB);
-    if (f1 != -1) continue;
-    gc_refine<D>(s1, rf1);
-    for (int c2 = 0; c2 < NC; c2++) {
-      gc_child<D>(rf1, c2, s2);
-      const int f2 = gc_mark(s2, NC);
-      if (f2 == 1) acc += 1u << (23 - 3 * LB);
-      else if (f2 == -1) acc += gc_walk32<D>(s2);
+    const unsigned mp = __ballot_sync(FULL, push);
+    if (mp) {  // l < 3 here; queue l + 1 is empty before this batch
+      const int cnt = l == 0 ? n1 : (l == 1 ? nq2 : n3);
+      if (push) {
+        const int pos = cnt + __popc(mp & below);
+        for (int q = 0; q < NC; q++) S.q[l][pos][q] = ch[q];
+        S.c[l][pos] = code | (c << (3 * l));
+      }
+      if (l == 0) n1 += __popc(mp);
+      else if (l == 1) nq2 += __popc(mp);
+      else n3 += __popc(mp);
     }
+    __syncwarp();
   }
-  return acc;
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+  if (lane == 0 && acc) atomicAdd(units + item_cell[it], acc);
 }
 
 // Polygonise_MQ::VertexInterp at isolevel 0 (polygonise.cpp:74-92), one axis
@@ -694,20 +782,6 @@ __global__ void __launch_bounds__(256) k_vm_cut(LsLevel L, const int* __restrict
   }
 }
 
-// Pass 2b, one thread per cut sub-cube: the bisection below it (gc_units),
-// added to its cell's units (integer, exact).
-template <int D>
-__global__ void __launch_bounds__(128) k_vm_frac(const int* __restrict__ item_cell, const double* __restrict__ item_cor,
-                                                 long long nitem, unsigned* __restrict__ units) {
-  constexpr int NC = D == 3 ? 8 : 4;
-  const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (it >= nitem) return;
-  double cor[NC];
-  for (int q = 0; q < NC; q++) cor[q] = item_cor[it * NC + q];
-  const unsigned r = gc_units<D>(cor);
-  if (r) atomicAdd(units + item_cell[it], r);
-}
-
 // Pass 2c, one thread per listed cell with a cut corner lattice: volume =
 // min(fraction, 1) * cell volume (get_volume / get_area, then
 // Get_cutcell_volume).
@@ -844,9 +918,9 @@ cudaError_t ls_volume_mass(const LsSet& ls, int level, int D, double* cvol, doub
     if ((e = cudaMemcpyAsync(&ni, cnt + 2, sizeof(ni), cudaMemcpyDeviceToHost, s)) == cudaSuccess &&
         (e = cudaStreamSynchronize(s)) == cudaSuccess) {
       if (ni > 0) {
-        const long long nbi = ((long long)ni + 127) / 128;
-        if (D == 3) k_vm_frac<3><<<(unsigned)nbi, 128, 0, s>>>(item_cell, item_cor, (long long)ni, units);
-        else k_vm_frac<2><<<(unsigned)nbi, 128, 0, s>>>(item_cell, item_cor, (long long)ni, units);
+        const long long nbi = ((long long)ni + 3) / 4;  // one warp per cut sub-cube
+        if (D == 3) k_vm_walk<3><<<(unsigned)nbi, 128, 0, s>>>(item_cell, item_cor, (long long)ni, units);
+        else k_vm_walk<2><<<(unsigned)nbi, 128, 0, s>>>(item_cell, item_cor, (long long)ni, units);
       }
       k_vm_finish<<<(unsigned)((nl + 255) / 256), 256, 0, s>>>(list, nl, units, mark, dv, cvol);
       e = cudaStreamSynchronize(s);

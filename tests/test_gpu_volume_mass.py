@@ -14,9 +14,33 @@ from paritylib import make_gpu, small_cases
 
 pytestmark = pytest.mark.gpu
 
+
+
+def dyadic_case(dim: int, kind: str):
+    """Planes at dyadic positions on a dyadic grid (cell 1/64): corner values
+    and bisection midpoints hit exact zeros at many refinement levels, where
+    FP32 cannot decide a sign and the FP64 path must."""
+    p = cases.default_params(dim)
+    p.update(min_dl=1 / 32, max_dl=1 / 32, cell_ratio=2.6, box_l=[0, 0, 0], box_r=[1, 1, 1 if dim == 3 else 0],
+             seed=1)
+    if kind == "box":
+        def sdf(X, Y, Z):
+            f = np.minimum(np.minimum(X - 13 / 64, 51 / 64 + 1 / 512 - X), np.minimum(Y - 0.25 - 3 / 1024, 0.75 - Y))
+            return np.minimum(f, np.minimum(Z - 0.3125, 0.6875 + 1 / 128 - Z)) if dim == 3 else f
+    else:
+        def sdf(X, Y, Z):
+            return 0.25 - np.abs((X - 0.5) + 0.5 * (Y - 0.5) - (0.25 * (Z - 0.5) if dim == 3 else 0.0))
+    lv = cases.make_level(sdf, dim, [0, 0, 0], [1 / 16, 1 / 16, 1 / 16 if dim == 3 else 1.0],
+                          [16, 16, 16 if dim == 3 else 1])
+    return cases.Case(f"{kind}_dyadic_{dim}d", p, [lv], 1000, steps=10)
+
+
 CASES = dict(small_cases())
 CASES["disc2d_fine"] = lambda: cases.disc_hole_2d(spacing=0.01, grid=128)
 CASES["torus3d_single"] = lambda: cases.torus_3d(dx_min=0.01, dx_max=0.04, fine_pkg=24, nlevels=1)
+for _d in (2, 3):
+    for _k in ("box", "tilted"):
+        CASES[f"{_k}_dyadic_{_d}d"] = (lambda d=_d, k=_k: dyadic_case(d, k))
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
