@@ -371,9 +371,10 @@ class LevelSetWriter:
     """Level_set_binary_writer (lset_binary_writer.cpp:12-510) for one level:
     an ImageData piece over the level's interior cells with phi, curv and
     scale at the cell corners and the cut-cell tag ('interface') and
-    characteristic tag ('char', none in these geometries) per cell, its PVTI
-    and the mesh_lset.pvd collection.  The reference's cut-cell 'vol' and
-    'area' fields need its cut-cell geometry (not built) and are left out."""
+    characteristic tag ('char', none in these geometries) per cell, the
+    cut-cell volume 'vol' and surface area 'area' per cell (the GPU's
+    Calculate_volume_mass pass, zero outside the counted cells), its PVTI
+    and the mesh_lset.pvd collection."""
 
     def __init__(self, outdir: str = "outdata"):
         self.outdir = outdir
@@ -392,7 +393,10 @@ class LevelSetWriter:
               ("scale", corner_average(cell_scale(sim, level), m, dim).astype("<f4"))]
         sl = (slice(None),) if dim == 2 else (slice(m, -m),)
         tag = f["tag"][sl + (slice(m, -m), slice(m, -m))].astype("<i4")
-        cd = [("interface", tag), ("char", np.zeros_like(tag))]
+        vm = sim.volume_mass(level, cells=True)
+        inner = sl + (slice(m, -m), slice(m, -m))
+        cd = [("interface", tag), ("char", np.zeros_like(tag)), ("vol", vm["vol"][inner].astype("<f4")),
+              ("area", vm["area"][inner].astype("<f4"))]
         piece = f"mesh_lset_rank_0_step_{n_out}.vti"
         with open(os.path.join(self.outdir, piece), "wb") as fh:
             fh.write(vti_bytes(ncell, origin, spacing, pd, cd))

@@ -33,6 +33,10 @@ def test_writers_and_restart_round_trip(tmp_path):
     mm = 4 * case.levels[0].margin
     assert lf["interface"].sum() == (f0["tag"][0, mm:-mm, mm:-mm] == 1).sum() > 0
     assert np.allclose(lf["curv"], io.corner_average(f0["curv"], mm, 2).ravel().astype(np.float32))
+    vm = g.volume_mass(0, cells=True)
+    assert np.array_equal(lf["vol"], vm["vol"][0, mm:-mm, mm:-mm].ravel().astype(np.float32))
+    assert np.array_equal(lf["area"], vm["area"][0, mm:-mm, mm:-mm].ravel().astype(np.float32))
+    assert abs(float(lf["vol"].astype(np.float64).sum()) - vm["total_volume"]) < 1e-5 * vm["total_volume"]
     pst = io.save_particle_post_file(g, str(tmp_path), first=True)
     assert np.array_equal(io.read_pst(pst), p["xyz"])
     g.close()

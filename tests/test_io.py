@@ -148,6 +148,10 @@ def test_corner_average_and_levelset_writer(tmp_path):
             return {"curv": np.ones(shp), "tag": tag, "max_phi": float(case.levels[level].phi.max()),
                     "nx": np.zeros(shp), "ny": np.zeros(shp), "nz": np.zeros(shp)}
 
+        def volume_mass(self, level, cells=False):
+            phi = case.levels[level].phi
+            return {"vol": np.where(phi > 0, 1e-4, 0.0), "area": np.where(np.abs(phi) < 0.02, 0.01, 0.0)}
+
     sim = LsSim()
     f = io.LevelSetWriter(str(tmp_path)).Output_lset(0, sim, run_time=0)
     r = io.read_vtu(f)
@@ -157,6 +161,8 @@ def test_corner_average_and_levelset_writer(tmp_path):
     assert np.allclose(r["curv"], 1.0)
     assert r["interface"].size == nc * 4 * lv.num_pkg[1]
     assert r["interface"].sum() == sim.levelset_fields(0)["tag"][0, m:-m, m:-m].sum()
+    assert np.array_equal(r["vol"], np.where(lv.phi[0, m:-m, m:-m] > 0, 1e-4, 0.0).ravel().astype(np.float32))
+    assert np.array_equal(r["area"], np.where(np.abs(lv.phi[0, m:-m, m:-m]) < 0.02, 0.01, 0.0).ravel().astype(np.float32))
     sc = r["scale"]
     assert sc.min() >= case.params["min_dl"] - 1e-7 and sc.max() <= case.params["max_dl"] + 1e-7
     head = open(f, "rb").read().split(b"<AppendedData")[0].decode()
