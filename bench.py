@@ -198,10 +198,12 @@ def cpu_volume_mass(case):
     the finest level of the workload."""
     import oracle
     oracle.build()
-    orc = oracle.Oracle(case)
+    t0 = time.perf_counter()
+    orc = oracle.Oracle(case)  # level-set build of every level (normals, tags, curvature, max phi)
+    ls_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     r = orc.volume_mass(-1)
-    return {"seconds": time.perf_counter() - t0, "threads": oracle.num_threads(), "result": r}
+    return {"seconds": time.perf_counter() - t0, "threads": oracle.num_threads(), "result": r, "levelset_s": ls_s}
 
 
 def run_reference(args, ws, rank, dist):
@@ -430,9 +432,15 @@ def run_mrsph(args, ws, rank, local, dist):
                "max_aspect": q["max_aspect"], "G_avg": q["G_avg"], "theta_30": q["theta_30"],
                "total_area": q["total_area"], "angle_hist_4deg": [int(v) for v in q["hist"]]}
     # cut-cell volume, surface area and particle count of the finest level
-    # (Calculate_total_volume_mass + Get_num_particles), device-timed
+    # (Calculate_total_volume_mass + Get_num_particles), device-timed, and
+    # the set-up of a fresh handle (level-set copy and build on the GPU)
     vm = None
     if not args.no_volume_mass:
+        gpu.sync()
+        t0 = time.perf_counter()
+        g_setup = SPHMeshGeneration(case, precision="fp32", device=dev)
+        setup_s = time.perf_counter() - t0
+        g_setup.close()
         gpu.sync()
         t0 = time.perf_counter()
         r = gpu.volume_mass(-1)
@@ -440,8 +448,10 @@ def run_mrsph(args, ws, rank, local, dist):
         vm = {k: r[k] for k in ("total_mass", "total_mass_surface", "total_volume", "total_area",
                                 "num_interface_cell", "num_particle_mesh", "num_particle_surface", "num_particle")}
         vm.update(device_ms=r["device_ms"], wall_s=vm_wall, level_cells=int(case.levels[-1].phi.size),
+                  handle_setup_s=setup_s, levelset_cells=int(sum(lv.phi.size for lv in case.levels)),
                   timer="CUDA events around the pass on the handle's stream; wall clock incl. scratch "
-                        "allocation and copies")
+                        "allocation and copies; handle_setup_s: host wall clock of mrsph_create + "
+                        "mrsph_set_levelset (phi copied in, every level built on the GPU)")
     gpu.close()
 
     # e2e through the C ABI with host buffers (pinned when torch is available):
@@ -517,7 +527,8 @@ def run_mrsph(args, ws, rank, local, dist):
                      "num_particle": ref["num_particle"],
                      "counts_equal": all(ref[k] == vm[k] for k in ("num_interface_cell", "num_particle_mesh",
                                                                    "num_particle_surface")),
-                     "total_mass_rel_diff": abs(ref["total_mass"] - vm["total_mass"]) / abs(ref["total_mass"])}
+                     "total_mass_rel_diff": abs(ref["total_mass"] - vm["total_mass"]) / abs(ref["total_mass"]),
+                     "levelset_build_s": r["levelset_s"]}
         vm["speedup_vs_cpu"] = r["seconds"] / (vm["device_ms"] / 1000.0)
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

@@ -55,3 +55,13 @@ def test_level_plan_rejects_bad_domain():
     h = ctypes.c_void_p()
     rc = lib.mrsph_create(ctypes.byref(p), ctypes.byref(h))
     assert rc == -1  # coarsest cell (1.3) larger than the domain
+
+
+def test_null_arguments_rejected_without_gpu():
+    """Entry points check their handle and output pointers before any device
+    call (mrsph_volume_mass, the stats and step entry points)."""
+    lib = L.load()
+    st = L.VolumeMassStats()
+    assert lib.mrsph_volume_mass(None, -1, ctypes.byref(st), None, None) == -1
+    assert lib.mrsph_step(None, 1) < 0
+    assert lib.mrsph_get_stats(None, None) < 0
