@@ -92,8 +92,13 @@ class SPHMeshGeneration:
             pass
 
     # --------------------------------------------------- reference entry points
-    def Initialize_case(self, n: Optional[int] = None):
-        """Random_particle_distribution + Pre_run (sph_mesh_generation.cpp:594-1050)."""
+    def Initialize_case(self, n: Optional[int] = None, cut_cell_count: bool = False):
+        """Random_particle_distribution + Pre_run (sph_mesh_generation.cpp:594-1050).
+        n defaults to the workload's count, or with cut_cell_count to the
+        reference's own (Get_num_particles over the cut-cell volume pass of the
+        finest level, sph_mesh_generation.cpp:900-940)."""
+        if n is None and cut_cell_count:
+            n = self.Get_num_particles()
         n = int(n if n is not None else self.case.n_particles)
         L.check(self.lib.mrsph_seed(self.h, n), self.h, "mrsph_seed")
         self.n = n
@@ -225,6 +230,11 @@ class SPHMeshGeneration:
         if cells:
             out["vol"], out["area"] = vol, area
         return out
+
+    def Get_num_particles(self, level: int = -1) -> int:
+        """SPH_mesh_generation::Get_num_particles (sph_mesh_generation.cpp:900-940)
+        over the cut-cell volume pass of one level."""
+        return int(self.volume_mass(level)["num_particle"])
 
     def sample_levelset_noalloc(self, xyz: np.ndarray):
         """Same as sample_levelset without any device allocation (<= 65536 points)."""

@@ -95,3 +95,15 @@ def test_volume_mass_full_torus():
     assert r["num_particle_surface"] == min(int(r["total_mass_surface"]), r["num_interface_cell"])
     assert r["num_particle_mesh"] == max(int(r["total_mass"] - 0.5 * r["total_mass_surface"]), 0)
     assert r["num_particle"] == r["num_particle_mesh"] + r["num_particle_surface"]
+
+
+def test_initialize_with_cut_cell_count():
+    """Initialize_case(cut_cell_count=True) seeds Get_num_particles particles."""
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    g = make_gpu(case, "fp64")
+    try:
+        n = g.Get_num_particles()
+        g.Initialize_case(cut_cell_count=True)
+        assert g.n == n and g.stats()["n"] == n
+    finally:
+        g.close()
