@@ -443,7 +443,7 @@ def run_mrsph(args, ws, rank, local, dist):
         g_setup.close()
         gpu.sync()
         t0 = time.perf_counter()
-        r = gpu.volume_mass(-1)
+        r = gpu.volume_mass(-1)  # raises (with the engine's message) on a device error
         vm_wall = time.perf_counter() - t0
         vm = {k: r[k] for k in ("total_mass", "total_mass_surface", "total_volume", "total_area",
                                 "num_interface_cell", "num_particle_mesh", "num_particle_surface", "num_particle")}
@@ -521,7 +521,7 @@ def run_mrsph(args, ws, rank, local, dist):
                          f"seeding, FP64 oracle (restatement of the reference, OpenMP {r['threads']} threads)",
                "gpu_same_window": fp64["fp32_same_window"] if fp64 else None}
     if vm is not None and not args.no_cpu:
-        r = cpu_volume_mass(case)
+        r = cpu_volume_mass(case)  # the oracle (CPU), beside the device pass
         ref = r["result"]
         vm["cpu"] = {"seconds": r["seconds"], "threads": r["threads"], "kind": "port",
                      "num_particle": ref["num_particle"],

@@ -14,8 +14,10 @@ on chip is the kernels' job).  3D FP32-split, per particle:
   stage 2 + reduction    read x 16, h 4, v 16, type 4, n 12; write v 16, nu 4 = 72
                                                                    total 344
 
-plus 8 bytes per cell-list cell for the cell start table.  FP64-plain uses
-24-byte vectors and 8-byte scalars; 2D uses D-component vectors.
+plus 8 bytes per cell-list cell for the cell start table and 20 bytes per
+unique level-set cell the map phase touches (phi, n, curvature: five FP32
+fields; 40 in FP64).  FP64-plain uses 24-byte vectors and 8-byte scalars; 2D
+uses D-component vectors.
 """
 from __future__ import annotations
 
@@ -54,3 +56,12 @@ def step_bytes(dim: int, precision: str, n_particles: int, n_cells: int) -> dict
 
 def total_bytes_per_particle(dim: int, precision: str) -> int:
     return sum(per_particle_bytes(dim, precision).values())
+
+
+def algorithmic_bytes(dim: int, precision: str, n_particles: int, n_lscells_touched: int,
+                      n_cells: int = 0) -> int:
+    """Compulsory bytes of one whole step: the per-particle terms of every
+    phase, 20 bytes (40 in FP64) per unique level-set cell touched by the map
+    phase, and 8 bytes per cell-list cell for the start table."""
+    ls = 20 if precision == "fp32" else 40
+    return total_bytes_per_particle(dim, precision) * n_particles + ls * n_lscells_touched + 8 * n_cells
