@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <fstream>
 
 namespace mrsph_host {
@@ -289,6 +290,25 @@ std::vector<double> SPH_mesh_generation::Positions() {
   return xyz;
 }
 
+void SPH_mesh_generation::Particle_fields(std::vector<int>& type, std::vector<double>& h,
+                                          std::vector<double>& norm, std::vector<int>& nn) {
+  type.assign(n_, 0);
+  h.assign(n_, 0.0);
+  norm.assign(3 * n_, 0.0);
+  mrsph_particle_view v{};
+  v.type = type.data();
+  v.h = h.data();
+  v.norm = norm.data();
+  check(mrsph_get_particles(h_, &v), "mrsph_get_particles");
+  std::vector<long long> off(n_ + 1, 0);
+  long long total = 0;
+  check(mrsph_get_neighbors(h_, nullptr, nullptr, 0, &total), "mrsph_get_neighbors");
+  std::vector<int> nb(total > 0 ? total : 1);
+  check(mrsph_get_neighbors(h_, off.data(), nb.data(), total, &total), "mrsph_get_neighbors");
+  nn.assign(n_, 0);
+  for (long long i = 0; i < n_; i++) nn[i] = (int)(off[i + 1] - off[i]);
+}
+
 std::string SPH_mesh_generation::Save_particle_post_file(const std::string& root, long long run_time, bool first) {
   const std::string dir = root + "/rstfile_particles";
   make_dir(root);
@@ -324,7 +344,9 @@ double Solver::SPH_Mesh_Generation_Solver(int total_steps, int output_interval, 
     ms_total += ms;
     done += k;
     if (!output_root.empty()) {
-      sim_.Save_particle_post_file(output_root, (long long)sim_.Stats().step, first);
+      const long long step = (long long)sim_.Stats().step;
+      sim_.Save_particle_post_file(output_root, step, first);
+      if (write_vtu_) Particle_binary_writer(output_root + "/outdata").Output_particle(n_out_++, sim_, step);
       first = false;
     }
   }
@@ -335,6 +357,133 @@ double Solver::Load_solver(const Initialization& ini, const std::string& output_
   const int every = (int)ini.Get_dt();
   if (every < 1) throw Error(MRSPH_ERR_ARG, "output interval below one step");
   return SPH_Mesh_Generation_Solver(ini.Get_num_timestep() * every, every, output_root);
+}
+
+namespace {
+
+// one appended array: its header line and its raw little-endian bytes
+struct VtuArray {
+  std::string name, type;
+  int comps;  // 0: no NumberOfComponents attribute (the cell arrays)
+  std::string raw;
+};
+
+template <class T>
+std::string raw_of(const T* p, size_t count) {
+  std::string r(sizeof(T) * count, '\0');
+  if (count) std::memcpy(&r[0], p, r.size());  // the library only builds on little-endian hosts
+  return r;
+}
+
+std::string vtu_text(long long n, long long m, const std::vector<VtuArray>& pd, const std::vector<VtuArray>& pts,
+                     const std::vector<VtuArray>& cells) {
+  std::string head, blobs;
+  unsigned long long offset = 0;
+  auto add = [&](const VtuArray& a) {
+    head += "      <DataArray type=\"" + a.type + "\" Name=\"" + a.name + "\"";
+    if (a.comps > 0) head += " NumberOfComponents=\"" + std::to_string(a.comps) + "\"";
+    head += " format=\"appended\" offset=\"" + std::to_string(offset) + "\"/>\n";
+    const uint32_t nb = (uint32_t)a.raw.size();
+    blobs += raw_of(&nb, 1) + a.raw;
+    offset += 4 + a.raw.size();
+  };
+  head += "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+  head += " <UnstructuredGrid>\n";
+  head += "  <Piece NumberOfPoints=\"" + std::to_string(n) + "\" NumberOfCells=\"" + std::to_string(m) + "\">\n";
+  head += "    <PointData Vectors=\"vector\">\n";
+  for (const auto& a : pd) add(a);
+  head += "    </PointData>\n    <Points>\n";
+  for (const auto& a : pts) add(a);
+  head += "    </Points>\n    <Cells>\n";
+  for (const auto& a : cells) add(a);
+  head += "    </Cells>\n  </Piece>\n </UnstructuredGrid>\n <AppendedData encoding=\"raw\">\n _";
+  return head + blobs + "\n </AppendedData>\n</VTKFile>\n";
+}
+
+}  // namespace
+
+std::string particle_vtu(const ParticleFields& f) {
+  const long long n = f.n;
+  std::vector<int> ids(n), zeros(n, 0), offs(n);
+  std::vector<float> h(n), nrm(3 * n), pos(3 * n);
+  std::vector<unsigned char> types(n, 1);  // VTK_VERTEX
+  for (long long i = 0; i < n; i++) {
+    ids[i] = (int)i;
+    offs[i] = (int)(i + 1);
+    h[i] = (float)f.h[i];
+    for (int d = 0; d < 3; d++) {
+      nrm[3 * i + d] = (float)f.norm[3 * i + d];
+      pos[3 * i + d] = (float)f.xyz[3 * i + d];
+    }
+  }
+  std::vector<VtuArray> pd = {
+      {"id", "Int32", 1, raw_of(ids.data(), n)},       {"local_id", "Int32", 1, raw_of(ids.data(), n)},
+      {"type", "Int32", 1, raw_of(f.type, n)},         {"h", "Float32", 1, raw_of(h.data(), n)},
+      {"NN", "Int32", 1, raw_of(f.nn, n)},             {"color", "Int32", 1, raw_of(zeros.data(), n)},
+      {"norm", "Float32", 3, raw_of(nrm.data(), 3 * n)}};
+  std::vector<VtuArray> pts = {{"Position", "Float32", 3, raw_of(pos.data(), 3 * n)}};
+  std::vector<VtuArray> cells = {{"connectivity", "Int32", 0, raw_of(ids.data(), n)},
+                                 {"offsets", "Int32", 0, raw_of(offs.data(), n)},
+                                 {"types", "UInt8", 0, raw_of(types.data(), n)}};
+  return vtu_text(n, n, pd, pts, cells);
+}
+
+std::string particle_pvtu(const std::string& piece) {
+  std::string t = "<VTKFile type=\"PUnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
+                  " <PUnstructuredGrid GhostLevel=\"0\">\n  <PPointData>\n";
+  const char* names[7] = {"id", "local_id", "type", "h", "NN", "color", "norm"};
+  const char* types[7] = {"Int32", "Int32", "Int32", "Float32", "Int32", "Int32", "Float32"};
+  for (int k = 0; k < 7; k++)
+    t += std::string("    <PDataArray type=\"") + types[k] + "\" Name=\"" + names[k] +
+         "\" NumberOfComponents=\"" + (k == 6 ? "3" : "1") + "\"/>\n";
+  t += "  </PPointData>\n  <PPoints>\n    <PDataArray type=\"Float32\" Name=\"Position\" "
+       "NumberOfComponents=\"3\"/>\n  </PPoints>\n  <Piece Source=\"" + piece +
+       "\"/>\n </PUnstructuredGrid>\n</VTKFile>\n";
+  return t;
+}
+
+void update_pvd(const std::string& path, int n_out, const std::string& timestep, const std::string& dataset) {
+  std::vector<std::string> entries;
+  if (n_out != 0) {
+    std::ifstream in(path);
+    std::string ln;
+    while (std::getline(in, ln))
+      if (ln.find("<DataSet") != std::string::npos) entries.push_back(ln);
+  }
+  entries.push_back("    <DataSet timestep=\"" + timestep + "\" group=\"\" part=\"0\" file=\"" + dataset + "\"/>");
+  std::ofstream out(path, std::ios::trunc);
+  out << "<VTKFile type=\"Collection\" version=\"0.1\">\n  <Collection>\n";
+  for (const auto& e : entries) out << e << "\n";
+  out << "  </Collection>\n</VTKFile>\n";
+}
+
+std::string Particle_binary_writer::Output_particle(int n_out, SPH_mesh_generation& sim, long long run_time) {
+  make_dir(outdir_);
+  std::vector<int> type, nn;
+  std::vector<double> h, norm;
+  sim.Particle_fields(type, h, norm, nn);
+  const std::vector<double> xyz = sim.Positions();
+  ParticleFields f;
+  f.n = sim.num_particles();
+  f.xyz = xyz.data();
+  f.type = type.data();
+  f.h = h.data();
+  f.nn = nn.data();
+  f.norm = norm.data();
+  const std::string piece = "particle_rank_0_step_" + std::to_string(n_out) + ".vtu";
+  const std::string pvtu = "particle_step_" + std::to_string(n_out) + ".pvtu";
+  {
+    std::ofstream o(outdir_ + "/" + piece, std::ios::binary | std::ios::trunc);
+    const std::string b = particle_vtu(f);
+    o.write(b.data(), (std::streamsize)b.size());
+  }
+  {
+    std::ofstream o(outdir_ + "/" + pvtu, std::ios::trunc);
+    o << particle_pvtu(piece);
+  }
+  const long long t = run_time < 0 ? sim.Stats().step : run_time;
+  update_pvd(outdir_ + "/particle.pvd", n_out, std::to_string(t), "./" + pvtu);
+  return outdir_ + "/" + piece;
 }
 
 void write_pst(const std::string& path, const std::vector<double>& xyz) {
@@ -359,3 +508,19 @@ std::vector<double> read_pst(const std::string& path) {
 }
 
 }  // namespace mrsph_host
+
+// C entry for the writer tests: the particle VTU bytes of host arrays.
+extern "C" long long mrsph_host_particle_vtu(const char* path, long long n, const double* xyz, const int* type,
+                                             const double* h, const int* nn, const double* norm) {
+  mrsph_host::ParticleFields f;
+  f.n = n;
+  f.xyz = xyz;
+  f.type = type;
+  f.h = h;
+  f.nn = nn;
+  f.norm = norm;
+  const std::string b = mrsph_host::particle_vtu(f);
+  std::ofstream o(path, std::ios::binary | std::ios::trunc);
+  o.write(b.data(), (std::streamsize)b.size());
+  return o ? (long long)b.size() : -1;
+}

@@ -119,6 +119,10 @@ class SPH_mesh_generation {
 
   long long num_particles() const { return n_; }
   mrsph_handle* handle() { return h_; }
+  // Per-particle arrays of the writers in id order: type, h, normal (n x 3)
+  // and neighbour counts of the last density pass (self included).
+  void Particle_fields(std::vector<int>& type, std::vector<double>& h, std::vector<double>& norm,
+                       std::vector<int>& nn);
 
  private:
   void check(int rc, const char* what);
@@ -145,6 +149,9 @@ struct Initialization {
 class Solver {
  public:
   explicit Solver(SPH_mesh_generation& sim) : sim_(sim) {}
+  // With VTU output on, every output also writes the particle VTU series
+  // (Particle_binary_writer) under <output_root>/outdata.
+  void Set_vtu_output(bool on) { write_vtu_ = on; }
   double SPH_Mesh_Generation_Solver(int total_steps, int output_interval = 0, const std::string& output_root = "");
   // Solver::Load_solver (src/solver.cpp:35-101) for the relaxation path:
   // Get_num_timestep() outputs, Get_dt() steps apart, with a particle restart
@@ -153,6 +160,39 @@ class Solver {
 
  private:
   SPH_mesh_generation& sim_;
+  bool write_vtu_ = false;
+  int n_out_ = 0;
+};
+
+// Particle_binary_writer (particle_binary_writer.cpp:12-400) with the
+// reference's default fields (id, local_id, type, h, NN, color, norm): per
+// output n, outdir/particle_rank_0_step_<n>.vtu (VTK XML UnstructuredGrid,
+// raw appended little-endian arrays, each preceded by its UInt32 byte
+// count), particle_step_<n>.pvtu and the particle.pvd collection.
+struct ParticleFields {
+  long long n = 0;
+  const double* xyz = nullptr;   // n x 3
+  const int* type = nullptr;
+  const double* h = nullptr;
+  const int* nn = nullptr;       // neighbour count of the last density pass, self included
+  const double* norm = nullptr;  // n x 3
+};
+std::string particle_vtu(const ParticleFields& f);
+std::string particle_pvtu(const std::string& piece);
+// Rewrites outdir/<name>.pvd with one DataSet entry per output so far
+// (Output_pvd_file, particle_binary_writer.cpp:53-93); n_out = 0 starts it.
+void update_pvd(const std::string& path, int n_out, const std::string& timestep, const std::string& dataset);
+
+class Particle_binary_writer {
+ public:
+  explicit Particle_binary_writer(const std::string& outdir = "outdata") : outdir_(outdir) {}
+  // Output_vtu_file / Output_pvtu_file / Output_pvd_file of output n_out; the
+  // timestep entry is run_time (the completed steps when negative).  Returns
+  // the piece's path.
+  std::string Output_particle(int n_out, SPH_mesh_generation& sim, long long run_time = -1);
+
+ private:
+  std::string outdir_;
 };
 
 // .pst restart files: int32 count, then x, y, z (float64) per particle.

@@ -58,3 +58,20 @@ def test_cpp_driver_cut_cell_count():
     n = g.volume_mass(-1)["num_particle"]
     g.close()
     assert d["n_particles"] == n and d["step"] == 2 and d["flags"] == 0
+
+
+def test_cpp_driver_writes_particle_vtu(tmp_path):
+    """--vtu writes the reference's particle VTU series at every output; the
+    pieces read back with the Python reader and carry the restart's positions."""
+    binary = build.build_host()
+    r = subprocess.run([binary, "--case", "disc_hole_2d", "--precision", "fp64", "--steps", "6",
+                        "--output-every", "3", "--out", str(tmp_path), "--vtu"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "outdata"
+    assert (out / "particle.pvd").read_text().count("<DataSet") == 2
+    v = io.read_vtu(str(out / "particle_rank_0_step_1.vtu"))
+    pst = io.read_pst(str(tmp_path / "rstfile_particles" / "step_6_rank_0.pst"))
+    assert np.array_equal(v["Position"], pst.astype(np.float32))
+    assert np.array_equal(v["id"], np.arange(len(pst))) and v["NN"].min() >= 1
+    assert (out / "particle_step_1.pvtu").exists()

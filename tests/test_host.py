@@ -46,3 +46,31 @@ def test_engine_error_without_gpu(binary):
         pass
     r = run(binary, "--case", "disc_hole_2d", "--steps", "1")
     assert r.returncode == 2 and "mrsph_create" in r.stderr
+
+
+def test_cpp_particle_vtu_matches_python_writer(binary, tmp_path):
+    """The C++ Particle_binary_writer writes the same bytes as the Python
+    writer (mrsph/io.py) for the same particle arrays."""
+    import ctypes
+    import numpy as np
+    from mrsph import io
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    f = lib.mrsph_host_particle_vtu
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p, ctypes.c_longlong] + [ctypes.c_void_p] * 5
+    rng = np.random.default_rng(4)
+    n = 1000
+    xyz = rng.random((n, 3))
+    typ = rng.integers(0, 2, n).astype(np.int32)
+    h = rng.random(n)
+    nn = rng.integers(1, 90, n).astype(np.int32)
+    nrm = rng.normal(size=(n, 3))
+    p = tmp_path / "c.vtu"
+    size = f(str(p).encode(), n, xyz.ctypes.data, typ.ctypes.data, h.ctypes.data, nn.ctypes.data, nrm.ctypes.data)
+    pd = [("id", np.arange(n, dtype="<i4")), ("local_id", np.arange(n, dtype="<i4")), ("type", typ),
+          ("h", h.astype("<f4")), ("NN", nn), ("color", np.zeros(n, dtype="<i4")), ("norm", nrm.astype("<f4"))]
+    ref = io.vtu_bytes(xyz, np.arange(n, dtype="<i4"), 1, pd)
+    got = p.read_bytes()
+    assert size == len(ref) and got == ref
+    back = io.read_vtu(str(p))
+    assert np.array_equal(back["NN"], nn) and np.array_equal(back["Position"], xyz.astype(np.float32))
