@@ -3,15 +3,16 @@
 // relaxation path: build a workload, seed, relax, write particle restarts.
 //
 //   mrsph_relax --case disc_hole_2d|torus_3d [--precision fp32|fp64] [--steps N]
-//               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu]
+//               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
 // particle-steps/s, final time step).  --count-only prints the particle count
 // of the workload without touching a GPU; --cut-cell-count seeds the count of
 // the reference's cut-cell volume pass on the finest level (Get_num_particles)
 // instead of the workload's; --vtu also writes the particle VTU series
-// (outdata/particle_*.vtu, .pvtu, particle.pvd) at every output.  Exit status
-// 2 on an engine error.
+// (outdata/particle_*.vtu, .pvtu, particle.pvd) at every output; --lset
+// writes the level-set image of the finest level (outdata/mesh_lset_*) before
+// seeding.  Exit status 2 on an engine error.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -25,7 +26,7 @@ int main(int argc, char** argv) {
   std::string wl = "disc_hole_2d", out, prec;
   int steps = -1, every = 0;
   long long n = -1;
-  bool count_only = false, cut_cell = false, vtu = false;
+  bool count_only = false, cut_cell = false, vtu = false, lset = false;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     auto val = [&]() -> std::string {
@@ -44,9 +45,10 @@ int main(int argc, char** argv) {
     else if (s == "--count-only") count_only = true;
     else if (s == "--cut-cell-count") cut_cell = true;
     else if (s == "--vtu") vtu = true;
+    else if (s == "--lset") lset = true;
     else if (s == "--help" || s == "-h") {
       std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
-                  "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu]\n");
+                  "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
@@ -69,6 +71,9 @@ int main(int argc, char** argv) {
     }
     if (steps < 0) steps = c.steps;
     SPH_mesh_generation sim(c);
+    if (lset)
+      Level_set_binary_writer((out.empty() ? std::string(".") : out) + "/outdata")
+          .Output_lset(0, sim, (int)c.levels.size() - 1, 0);
     if (cut_cell && n < 0) n = sim.Get_num_particles();
     sim.Initialize_case(n);
     Solver solver(sim);

@@ -4,6 +4,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -21,7 +22,11 @@ std::string last_error(mrsph_handle* h) {
   return std::string(buf);
 }
 
-void make_dir(const std::string& d) { mkdir(d.c_str(), 0755); }
+// creates d and any missing parent directories
+void make_dir(const std::string& d) {
+  for (size_t k = 1; k <= d.size(); k++)
+    if (k == d.size() || d[k] == '/') mkdir(d.substr(0, k).c_str(), 0755);
+}
 }  // namespace
 
 mrsph_params default_params(int dim) {
@@ -486,6 +491,212 @@ std::string Particle_binary_writer::Output_particle(int n_out, SPH_mesh_generati
   return outdir_ + "/" + piece;
 }
 
+std::string repr_double(double v) {
+  if (v == 0.0) return std::signbit(v) ? "-0.0" : "0.0";
+  char buf[64];
+  auto r = std::to_chars(buf, buf + sizeof(buf), v, std::chars_format::scientific);
+  std::string sci(buf, r.ptr);  // [-]d[.ddd]e(+|-)XX
+  const size_t e = sci.find('e');
+  const int exp10 = std::atoi(sci.c_str() + e + 1);
+  std::string mant = sci.substr(0, e), sign;
+  if (mant[0] == '-') {
+    sign = "-";
+    mant = mant.substr(1);
+  }
+  std::string digits;
+  for (char c : mant)
+    if (c != '.') digits += c;
+  if (exp10 >= -4 && exp10 < 16) {  // fixed notation, as repr does
+    std::string out;
+    const int point = exp10 + 1;    // digits before the decimal point
+    if (point <= 0) {
+      out = "0." + std::string(-point, '0') + digits;
+    } else if (point >= (int)digits.size()) {
+      out = digits + std::string(point - digits.size(), '0') + ".0";
+    } else {
+      out = digits.substr(0, point) + "." + digits.substr(point);
+    }
+    return sign + out;
+  }
+  std::string m = digits.substr(0, 1);
+  if (digits.size() > 1) m += "." + digits.substr(1);
+  char eb[16];
+  std::snprintf(eb, sizeof(eb), "e%c%02d", exp10 < 0 ? '-' : '+', exp10 < 0 ? -exp10 : exp10);
+  return sign + m + eb;
+}
+
+std::string vti_bytes(const std::array<int, 3>& ncell, const std::array<double, 3>& origin,
+                      const std::array<double, 3>& spacing, const std::vector<ImageField>& point_data,
+                      const std::vector<ImageField>& cell_data) {
+  std::string ext;
+  for (int d = 0; d < 3; d++) ext += (d ? " 0 " : "0 ") + std::to_string(ncell[d]);
+  std::string head = "<VTKFile type=\"ImageData\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+  head += " <ImageData WholeExtent=\"" + ext + "\" Origin=\"" + repr_double(origin[0]) + " " +
+          repr_double(origin[1]) + " " + repr_double(origin[2]) + "\" Spacing=\"" + repr_double(spacing[0]) + " " +
+          repr_double(spacing[1]) + " " + repr_double(spacing[2]) + "\">\n";
+  head += "  <Piece Extent=\"" + ext + "\">\n";
+  std::string blobs;
+  unsigned long long offset = 0;
+  auto block = [&](const char* tag, const std::vector<ImageField>& fs) {
+    head += std::string("    <") + tag + " Vectors=\"vector\">\n";
+    for (const auto& f : fs) {
+      head += "      <DataArray type=\"" + f.type + "\" Name=\"" + f.name +
+              "\" NumberOfComponents=\"1\" format=\"appended\" offset=\"" + std::to_string(offset) + "\"/>\n";
+      const uint32_t nb = (uint32_t)f.raw.size();
+      blobs += raw_of(&nb, 1) + f.raw;
+      offset += 4 + f.raw.size();
+    }
+    head += std::string("    </") + tag + ">\n";
+  };
+  block("PointData", point_data);
+  block("CellData", cell_data);
+  head += "  </Piece>\n </ImageData>\n <AppendedData encoding=\"raw\">\n _";
+  return head + blobs + "\n </AppendedData>\n</VTKFile>\n";
+}
+
+namespace {
+
+// mean of the 2^D cells around each corner of the interior cells; cells are
+// (nz, ny, nx) incl. m margin cells per side (nz = 1 in 2D)
+std::vector<float> corner_average(const std::vector<double>& c, const std::array<int, 3>& n, int m, int dim) {
+  std::vector<float> out;
+  if (dim == 2) {
+    const int ny = n[1] - 2 * m + 1, nx = n[0] - 2 * m + 1;
+    out.resize((size_t)ny * nx);
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        auto C = [&](int dy, int dx) { return c[(size_t)(y + m - 1 + dy) * n[0] + (x + m - 1 + dx)]; };
+        out[(size_t)y * nx + x] = (float)(0.25 * (C(0, 0) + C(1, 0) + C(0, 1) + C(1, 1)));
+      }
+    return out;
+  }
+  const int nz = n[2] - 2 * m + 1, ny = n[1] - 2 * m + 1, nx = n[0] - 2 * m + 1;
+  out.resize((size_t)nz * ny * nx);
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        double acc = 0.0;
+        for (int dz = 0; dz < 2; dz++)
+          for (int dy = 0; dy < 2; dy++)
+            for (int dx = 0; dx < 2; dx++)
+              acc += c[((size_t)(z + m - 1 + dz) * n[1] + (y + m - 1 + dy)) * n[0] + (x + m - 1 + dx)];
+        out[((size_t)z * ny + y) * nx + x] = (float)(0.125 * acc);
+      }
+  return out;
+}
+
+template <class T, class U>
+std::string interior_raw(const std::vector<U>& c, const std::array<int, 3>& n, int m, int dim) {
+  std::vector<T> v;
+  const int z0 = dim == 3 ? m : 0, z1 = dim == 3 ? n[2] - m : 1;
+  for (int z = z0; z < z1; z++)
+    for (int y = m; y < n[1] - m; y++)
+      for (int x = m; x < n[0] - m; x++) v.push_back((T)c[((size_t)z * n[1] + y) * n[0] + x]);
+  return raw_of(v.data(), v.size());
+}
+
+}  // namespace
+
+std::string Level_set_binary_writer::Output_lset(int n_out, SPH_mesh_generation& sim, int level,
+                                                 long long run_time) {
+  make_dir(outdir_);
+  const Case& cs = sim.Get_case();
+  const mrsph_params& p = cs.params;
+  const int dim = p.dim, nls = (int)cs.levels.size();
+  if (level < 0 || level >= nls) throw Error(MRSPH_ERR_ARG, "no such level-set level");
+  const LevelGrid& lv = cs.levels[level];
+  std::array<int, 3> n{{1, 1, 1}};
+  for (int d = 0; d < dim; d++) n[d] = (lv.num_pkg[d] + 2 * lv.margin) * 4;
+  const size_t ntot = (size_t)n[0] * n[1] * n[2];
+  const int m = 4 * lv.margin;
+  // curvature and tags of every level (the curvature law's range spans all levels)
+  std::vector<std::vector<double>> curv(nls);
+  std::vector<std::vector<unsigned char>> tag(nls);
+  double max_phi = 0.0;
+  for (int l = 0; l < nls; l++) {
+    const size_t nl = cs.levels[l].phi.size();
+    curv[l].assign(nl, 0.0);
+    tag[l].assign(nl, 0);
+    int rc = mrsph_get_levelset(sim.handle(), l, nullptr, nullptr, nullptr, curv[l].data(), tag[l].data(), &max_phi);
+    if (rc) throw Error(rc, "mrsph_get_levelset");
+  }
+  // Levelset::Get_scale (level_set.cpp:311-351) on every cell of the level
+  double dl0 = 1.e20;
+  for (int d = 0; d < dim; d++) dl0 = std::min(dl0, cs.levels[0].dpkg[d] / 4.0);
+  double cmax = 0.0, cmin = 1.e20;
+  bool any_cut = false;
+  for (int l = 0; l < nls; l++)
+    for (size_t a = 0; a < curv[l].size(); a++)
+      if (tag[l][a] == 1) {
+        const double v = std::fabs(curv[l][a]);
+        if (!any_cut) {
+          cmax = cmin = v;
+          any_cut = true;
+        } else {
+          cmax = std::max(cmax, v);
+          cmin = std::min(cmin, v);
+        }
+      }
+  const double mid = p.middle_dl > 0 ? p.middle_dl : 5.0 * dl0;
+  std::vector<double> scale(ntot);
+  for (size_t a = 0; a < ntot; a++) {
+    const double phi = lv.phi[a];
+    double lo = p.min_dl;
+    if (p.scale_law == 1) {
+      double q = (cmax - std::fabs(curv[level][a])) / (cmax - cmin + 1e-20);
+      q = std::min(std::max(q, 0.0), 1.0);
+      lo = p.min_dl + q * q * (mid - p.min_dl);
+    }
+    const double s = lo + std::tanh(2.5 * std::fabs(phi) / max_phi) / std::tanh(2.5) * (p.max_dl - lo);
+    scale[a] = (phi > 0 || std::fabs(phi) < dl0) ? s : p.min_dl;
+  }
+  std::vector<double> vol(ntot), area(ntot);
+  mrsph_volume_mass_stats vm{};
+  int rc = mrsph_volume_mass(sim.handle(), level, &vm, vol.data(), area.data());
+  if (rc) throw Error(rc, "mrsph_volume_mass");
+  auto fl = [](const std::vector<float>& v) { return raw_of(v.data(), v.size()); };
+  std::vector<ImageField> pd = {{"phi", "Float32", fl(corner_average(lv.phi, n, m, dim))},
+                                {"curv", "Float32", fl(corner_average(curv[level], n, m, dim))},
+                                {"scale", "Float32", fl(corner_average(scale, n, m, dim))}};
+  const std::string tags = interior_raw<int>(tag[level], n, m, dim);
+  std::vector<ImageField> cd = {{"interface", "Int32", tags},
+                                {"char", "Int32", std::string(tags.size(), '\0')},
+                                {"vol", "Float32", interior_raw<float>(vol, n, m, dim)},
+                                {"area", "Float32", interior_raw<float>(area, n, m, dim)}};
+  std::array<int, 3> nc{{0, 0, 0}};
+  std::array<double, 3> origin{{0, 0, 0}}, spacing{{1, 1, 1}};
+  for (int d = 0; d < dim; d++) {
+    nc[d] = 4 * lv.num_pkg[d];
+    origin[d] = lv.box_l[d];
+    spacing[d] = lv.dpkg[d] / 4.0;
+  }
+  const std::string piece = "mesh_lset_rank_0_step_" + std::to_string(n_out) + ".vti";
+  {
+    std::ofstream o(outdir_ + "/" + piece, std::ios::binary | std::ios::trunc);
+    const std::string b = vti_bytes(nc, origin, spacing, pd, cd);
+    o.write(b.data(), (std::streamsize)b.size());
+  }
+  const std::string pvti = "mesh_lset_step_" + std::to_string(n_out) + ".pvti";
+  {
+    std::string ext;
+    for (int d = 0; d < 3; d++) ext += (d ? " 0 " : "0 ") + std::to_string(nc[d]);
+    std::ofstream o(outdir_ + "/" + pvti, std::ios::trunc);
+    o << "<VTKFile type=\"PImageData\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
+      << " <PImageData WholeExtent=\"" << ext << "\" GhostLevel=\"0\" Origin=\"" << repr_double(origin[0]) << " "
+      << repr_double(origin[1]) << " " << repr_double(origin[2]) << "\" Spacing=\"" << repr_double(spacing[0]) << " "
+      << repr_double(spacing[1]) << " " << repr_double(spacing[2]) << "\">\n  <PPointData>\n";
+    for (const auto& f : pd)
+      o << "    <PDataArray type=\"" << f.type << "\" Name=\"" << f.name << "\" NumberOfComponents=\"1\"/>\n";
+    o << "  </PPointData>\n  <PCellData>\n";
+    for (const auto& f : cd)
+      o << "    <PDataArray type=\"" << f.type << "\" Name=\"" << f.name << "\" NumberOfComponents=\"1\"/>\n";
+    o << "  </PCellData>\n  <Piece Extent=\"" << ext << "\" Source=\"" << piece << "\"/>\n </PImageData>\n</VTKFile>\n";
+  }
+  const long long t = run_time < 0 ? sim.Stats().step : run_time;
+  update_pvd(outdir_ + "/mesh_lset.pvd", n_out, std::to_string(t), "./" + pvti);
+  return outdir_ + "/" + piece;
+}
+
 void write_pst(const std::string& path, const std::vector<double>& xyz) {
   std::ofstream f(path, std::ios::binary | std::ios::trunc);
   if (!f) throw Error(MRSPH_ERR_ARG, "cannot write " + path);
@@ -520,6 +731,40 @@ extern "C" long long mrsph_host_particle_vtu(const char* path, long long n, cons
   f.nn = nn;
   f.norm = norm;
   const std::string b = mrsph_host::particle_vtu(f);
+  std::ofstream o(path, std::ios::binary | std::ios::trunc);
+  o.write(b.data(), (std::streamsize)b.size());
+  return o ? (long long)b.size() : -1;
+}
+
+// C entry for the writer tests: the level-set VTI bytes of host arrays
+// (point fields at (n0+1) x (n1+1) x (n2+1) corners, cell fields per cell;
+// 2D: n2 = 0, one layer).
+template <class T>
+static std::string host_raw(const T* p, size_t count) {
+  std::string r(sizeof(T) * count, '\0');
+  if (count) std::memcpy(&r[0], p, r.size());
+  return r;
+}
+
+extern "C" long long mrsph_host_lset_vti(const char* path, const int* ncell, const double* origin,
+                                         const double* spacing, const float* phi, const float* curv,
+                                         const float* scale, const int* tag, const float* vol, const float* area) {
+  std::array<int, 3> nc{{ncell[0], ncell[1], ncell[2]}};
+  size_t np = 1, ncl = 1;
+  for (int d = 0; d < 3; d++) {
+    np *= (size_t)(nc[d] + 1);
+    ncl *= (size_t)(nc[d] > 0 ? nc[d] : 1);
+  }
+  std::vector<int> zero(ncl, 0);
+  std::vector<mrsph_host::ImageField> pd = {{"phi", "Float32", host_raw(phi, np)},
+                                            {"curv", "Float32", host_raw(curv, np)},
+                                            {"scale", "Float32", host_raw(scale, np)}};
+  std::vector<mrsph_host::ImageField> cd = {{"interface", "Int32", host_raw(tag, ncl)},
+                                            {"char", "Int32", host_raw(zero.data(), ncl)},
+                                            {"vol", "Float32", host_raw(vol, ncl)},
+                                            {"area", "Float32", host_raw(area, ncl)}};
+  const std::string b = mrsph_host::vti_bytes(nc, {{origin[0], origin[1], origin[2]}},
+                                              {{spacing[0], spacing[1], spacing[2]}}, pd, cd);
   std::ofstream o(path, std::ios::binary | std::ios::trunc);
   o.write(b.data(), (std::streamsize)b.size());
   return o ? (long long)b.size() : -1;

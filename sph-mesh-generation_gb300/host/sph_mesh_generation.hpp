@@ -119,6 +119,7 @@ class SPH_mesh_generation {
 
   long long num_particles() const { return n_; }
   mrsph_handle* handle() { return h_; }
+  const Case& Get_case() const { return case_; }
   // Per-particle arrays of the writers in id order: type, h, normal (n x 3)
   // and neighbour counts of the last density pass (self included).
   void Particle_fields(std::vector<int>& type, std::vector<double>& h, std::vector<double>& norm,
@@ -190,6 +191,32 @@ class Particle_binary_writer {
   // timestep entry is run_time (the completed steps when negative).  Returns
   // the piece's path.
   std::string Output_particle(int n_out, SPH_mesh_generation& sim, long long run_time = -1);
+
+ private:
+  std::string outdir_;
+};
+
+// Level_set_binary_writer (lset_binary_writer.cpp:12-510) for one level:
+// outdir/mesh_lset_rank_0_step_<n>.vti (VTK XML ImageData over the level's
+// interior cells, raw appended arrays) with phi, curv and scale at the cell
+// corners (the mean of the 2^D cells around each corner) and per cell the
+// cut-cell tag 'interface', the characteristic tag 'char' (none here), the
+// cut-cell volume 'vol' and area 'area' (mrsph_volume_mass), its
+// mesh_lset_step_<n>.pvti and the mesh_lset.pvd collection.
+struct ImageField {
+  std::string name, type;  // type "Float32" or "Int32"
+  std::string raw;         // little-endian values, x fastest
+};
+std::string vti_bytes(const std::array<int, 3>& ncell, const std::array<double, 3>& origin,
+                      const std::array<double, 3>& spacing, const std::vector<ImageField>& point_data,
+                      const std::vector<ImageField>& cell_data);
+// Shortest round-trip decimal of a double, written the way Python's repr writes it.
+std::string repr_double(double v);
+
+class Level_set_binary_writer {
+ public:
+  explicit Level_set_binary_writer(const std::string& outdir = "outdata") : outdir_(outdir) {}
+  std::string Output_lset(int n_out, SPH_mesh_generation& sim, int level = 0, long long run_time = -1);
 
  private:
   std::string outdir_;

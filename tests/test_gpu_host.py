@@ -75,3 +75,25 @@ def test_cpp_driver_writes_particle_vtu(tmp_path):
     assert np.array_equal(v["Position"], pst.astype(np.float32))
     assert np.array_equal(v["id"], np.arange(len(pst))) and v["NN"].min() >= 1
     assert (out / "particle_step_1.pvtu").exists()
+
+
+def test_cpp_driver_writes_levelset_image(tmp_path):
+    """--lset writes the level-set image; it equals the Python writer's for the
+    same workload (header bytes and every field; the spacing field within
+    FP32 rounding of the two tanh implementations)."""
+    binary = build.build_host()
+    r = subprocess.run([binary, "--case", "disc_hole_2d", "--precision", "fp64", "--steps", "1", "--out",
+                        str(tmp_path / "c"), "--lset"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    cpp = tmp_path / "c" / "outdata" / "mesh_lset_rank_0_step_0.vti"
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    g = SPHMeshGeneration(case, precision="fp64")
+    py = io.LevelSetWriter(str(tmp_path / "p")).Output_lset(0, g, level=0, run_time=0)
+    g.close()
+    a, b = io.read_vtu(str(cpp)), io.read_vtu(py)
+    head = lambda p: open(p, "rb").read().split(b"<AppendedData")[0]  # noqa: E731
+    assert head(cpp) == head(py)
+    for k in ("interface", "char"):
+        assert np.array_equal(a[k], b[k]), k
+    for k in ("phi", "curv", "vol", "area", "scale"):
+        assert np.allclose(a[k], b[k], rtol=1e-6, atol=1e-30), k

@@ -74,3 +74,59 @@ def test_cpp_particle_vtu_matches_python_writer(binary, tmp_path):
     assert size == len(ref) and got == ref
     back = io.read_vtu(str(p))
     assert np.array_equal(back["NN"], nn) and np.array_equal(back["Position"], xyz.astype(np.float32))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cpp_lset_vti_matches_python_writer(binary, tmp_path, dim):
+    """The C++ Level_set_binary_writer's image bytes equal the Python
+    writer's (vti_bytes) for the same arrays, origin and spacing included."""
+    import ctypes
+    import numpy as np
+    from mrsph import io
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    f = lib.mrsph_host_lset_vti
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 9
+    rng = np.random.default_rng(dim)
+    nc = np.array([12, 8, 6 if dim == 3 else 0], dtype=np.int32)
+    origin = np.array([-1.6, 0.0001, -0.45 if dim == 3 else 0.0])
+    spacing = np.array([0.0125, 1.0 / 3.0, 0.05 if dim == 3 else 1.0])
+    npt = int(np.prod(nc + 1))
+    ncl = int(np.prod(np.maximum(nc, 1)))
+    phi, curv, scale = (rng.normal(size=npt).astype("<f4") for _ in range(3))
+    tag = rng.integers(0, 2, ncl).astype("<i4")
+    vol, area = (rng.random(ncl).astype("<f4") for _ in range(2))
+    p = tmp_path / "c.vti"
+    size = f(str(p).encode(), nc.ctypes.data, origin.ctypes.data, spacing.ctypes.data, phi.ctypes.data,
+             curv.ctypes.data, scale.ctypes.data, tag.ctypes.data, vol.ctypes.data, area.ctypes.data)
+    ref = io.vti_bytes([int(x) for x in nc], list(origin), list(spacing),
+                       [("phi", phi), ("curv", curv), ("scale", scale)],
+                       [("interface", tag), ("char", np.zeros_like(tag)), ("vol", vol), ("area", area)])
+    assert size == len(ref) and p.read_bytes() == ref
+
+
+def test_repr_double_matches_python(binary):
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    assert lib is not None
+    import numpy as np
+    from mrsph import io
+    # through the image header: Origin / Spacing are written with repr
+    vals = [0.0, 1.0, -1.6, 0.0001, 1e-05, 123456789.0, 1e16, 2.5e-7, 0.1 + 0.2, 3.2 / 256]
+    f = lib.mrsph_host_lset_vti
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 9
+    import tempfile
+    nc = np.array([1, 1, 1], dtype=np.int32)
+    z8, z1 = np.zeros(8, dtype="<f4"), np.zeros(1, dtype="<f4")
+    t1 = np.zeros(1, dtype="<i4")
+    with tempfile.TemporaryDirectory() as d:
+        for v in vals:
+            o = np.array([v, -v, v / 3])
+            s = np.array([v + 1.0, 2.0, 0.5])
+            path = os.path.join(d, "r.vti")
+            f(path.encode(), nc.ctypes.data, o.ctypes.data, s.ctypes.data, z8.ctypes.data, z8.ctypes.data,
+              z8.ctypes.data, t1.ctypes.data, z1.ctypes.data, z1.ctypes.data)
+            head = open(path, "rb").read().split(b"<PointData")[0].decode()
+            ref = io.vti_bytes([1, 1, 1], list(o), list(s), [("phi", z8)], []).split(b"<PointData")[0].decode()
+            assert head == ref, (v, head, ref)
