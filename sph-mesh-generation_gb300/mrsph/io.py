@@ -435,6 +435,123 @@ def read_pst(path: str) -> np.ndarray:
     return xyz.reshape(n, 3).copy()
 
 
+# Level-set restart (SPH_mesh_generation::Save_restart_file,
+# sph_mesh_generation.cpp:2671-2736; Levelset::Save_lset_restart_file,
+# level_set.cpp:1022-1094; Levelset_levelinfo::Write_level_set_rstfile,
+# lset_level_infor.cpp:695-929): native-endian binary, written here
+# little-endian.  Header: DIM, domain, box_l, box_r, particle_box,
+# particle_box_l, particle_box_r (float64 x 3 each), resolution (int32 x 3),
+# Lmin, Lmax, ini_num_cell (int32 x 3), num_level; level set: convergence
+# error, 0 singularities, 0 segments, the dl factors, maximum_curv_artificial,
+# the cut-cell totals, maximum phi / psi, maximum / middle / minimum dl,
+# maximum / minimum curvature, interface cells; level: package counts and
+# ranges, dpkg, dcell; then per interior cell (x fastest) phi, n_x, n_y, n_z,
+# curv, psi (float64), tag_interface, tag_characteristic, idx_characteristic
+# (int32) and scale (float64).  One level, as the reference writes.
+_RST_HEAD = "<i" + "d" * 18 + "i" * 3 + "ii" + "i" * 3 + "i"
+_RST_LSET = "<di" + "i" + "d" * 17 + "i"
+_RST_LEVEL = "<idd" + "i" * 21 + "d" * 6
+
+
+def save_lset_restart(sim, path: str = "rstfile/levelset.rst", level: int = -1) -> str:
+    """Writes the level-set restart of one level-set level (the finest by
+    default) from the engine's fields and its cut-cell volume pass."""
+    case = sim.case
+    prm = case.params
+    dim = prm["dim"]
+    nls = len(case.levels)
+    level = level % nls
+    lv = case.levels[level]
+    f = sim.levelset_fields(level)
+    vm = sim.volume_mass(level)
+    m = 4 * lv.margin
+    inner = (slice(None),) if dim == 2 else (slice(m, -m),)
+    inner = inner + (slice(m, -m), slice(m, -m))
+    box_l = [float(prm["box_l"][d]) if d < dim else 0.0 for d in range(3)]
+    box_r = [float(prm["box_r"][d]) if d < dim else 0.0 for d in range(3)]
+    domain = [box_r[d] - box_l[d] for d in range(3)]
+    npkg = [int(lv.num_pkg[d]) if d < dim else 1 for d in range(3)]
+    marg = [int(lv.margin) if d < dim else 0 for d in range(3)]
+    dpkg = [float(lv.dpkg[d]) for d in range(3)]
+    dcell = [x / 4.0 if d < dim else x for d, x in enumerate(dpkg)]
+    dl = min(dcell[d] for d in range(dim))
+    dl0 = min(case.levels[0].dpkg[d] / 4.0 for d in range(dim))
+    # |curvature| range over the CUT cells of all levels
+    cuts = [sim.levelset_fields(l) for l in range(nls)]
+    vals = np.concatenate([np.abs(g["curv"][g["tag"] == 1]) for g in cuts])
+    cmax, cmin = (float(vals.max()), float(vals.min())) if vals.size else (0.0, 1e20)
+    mid = prm.get("middle_dl", 0.0) or 5.0 * dl0
+    phi = lv.phi
+    # the scale Calculate_volume_mass leaves in the counted cells (0 elsewhere)
+    scale = np.where((phi > 0) | (np.abs(phi) < dl), cell_scale(sim, level), 0.0)
+    head = struct.pack(_RST_HEAD, dim, *domain, *box_l, *box_r, *domain, *box_l, *box_r,
+                       *[4 * npkg[d] if d < dim else 1 for d in range(3)], 0, 0, *npkg, 1)
+    lset = struct.pack(_RST_LSET, 1.e-4, 0, 0, prm["max_dl"] / dl0, mid / dl0, prm["min_dl"] / dl0,
+                       min(1.0, cmax), vm["total_mass"], vm["total_mass_surface"], 0.0, vm["total_volume"],
+                       vm["total_area"], 0.0, float(f["max_phi"]), 0.0, float(prm["max_dl"]), float(mid),
+                       float(prm["min_dl"]), cmax, cmin, int(vm["num_interface_cell"]))
+    gnum = [npkg[d] + 2 * marg[d] for d in range(3)]
+    start = [-marg[d] for d in range(3)]
+    end = [npkg[d] + marg[d] for d in range(3)]
+    lev = struct.pack(_RST_LEVEL, int(np.prod(gnum)), dpkg[0], dl, *npkg, *gnum, *start, *end, *start, *end, *marg,
+                      *dpkg, *dcell)
+    cells = [phi, f["nx"], f["ny"], f["nz"], f["curv"], np.zeros_like(phi)]
+    body = b"".join(np.ascontiguousarray(c[inner], dtype="<f8").tobytes() for c in cells)
+    tag = f["tag"][inner].astype("<i4")
+    body += tag.tobytes() + np.zeros_like(tag).tobytes() + np.full_like(tag, -1).tobytes()
+    body += np.ascontiguousarray(scale[inner], dtype="<f8").tobytes()
+    os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+    with open(path, "wb") as fh:
+        fh.write(head + lset + lev + body)
+    return path
+
+
+def load_lset_restart(path: str) -> dict:
+    """Reads a level-set restart written by save_lset_restart (or by the
+    reference on a little-endian host, one level): header values and the
+    per-cell fields shaped (nz, ny, nx) over the interior cells."""
+    data = open(path, "rb").read()
+    o = 0
+    h = struct.unpack_from(_RST_HEAD, data, o)
+    o += struct.calcsize(_RST_HEAD)
+    out = {"dim": h[0], "domain": h[1:4], "box_l": h[4:7], "box_r": h[7:10], "resolution": h[19:22],
+           "Lmin": h[22], "Lmax": h[23], "ini_num_cell": h[24:27], "num_level": h[27]}
+    ls = struct.unpack_from("<di", data, o)
+    o += 12
+    if ls[1] != 0:
+        raise ValueError("restart files with singularities are not supported")
+    nseg = struct.unpack_from("<i", data, o)[0]
+    o += 4
+    if nseg != 0:
+        raise ValueError("restart files with segments are not supported")
+    vals = struct.unpack_from("<" + "d" * 17 + "i", data, o)
+    o += 17 * 8 + 4
+    keys = ["fac_maximum_dl", "fac_middel_dl", "fac_minimum_dl", "maximum_curv_artificial", "total_mass",
+            "total_mass_surface", "total_mass_segment", "total_volume", "total_area", "total_length", "maximum_phi",
+            "maximum_psi", "maximum_dl", "middel_dl", "minimum_dl", "maximum_curv", "minimum_curv"]
+    out.update(dict(zip(keys, vals[:17])))
+    out["convergence_error"] = ls[0]
+    out["glbl_num_interface_cell"] = vals[17]
+    lv = struct.unpack_from(_RST_LEVEL, data, o)
+    o += struct.calcsize(_RST_LEVEL)
+    npkg = lv[3:6]
+    out.update(glbl_total_num_pkg=lv[0], scale=lv[1], dl=lv[2], num_pkg=npkg, glbl_num_pkg=lv[6:9],
+               num_pkg_margin=lv[21:24], dpkg=lv[24:27], dcell=lv[27:30])
+    shape = (npkg[2] * (4 if out["dim"] == 3 else 1), npkg[1] * 4, npkg[0] * 4)
+    nc = int(np.prod(shape))
+    for k in ("phi", "n_x", "n_y", "n_z", "curv", "psi"):
+        out[k] = np.frombuffer(data, dtype="<f8", count=nc, offset=o).reshape(shape).copy()
+        o += 8 * nc
+    for k in ("tag_interface", "tag_characteristic", "idx_characteristic"):
+        out[k] = np.frombuffer(data, dtype="<i4", count=nc, offset=o).reshape(shape).copy()
+        o += 4 * nc
+    out["scale_cells"] = np.frombuffer(data, dtype="<f8", count=nc, offset=o).reshape(shape).copy()
+    o += 8 * nc
+    if o != len(data):
+        raise ValueError("trailing bytes in level-set restart")
+    return out
+
+
 def save_particle_post_file(sim, root: str = ".", run_time: Optional[int] = None, first: bool = False) -> str:
     """Save_particle_post_file (sph_mesh_generation.cpp:2624-2660): positions
     of every particle (in id order) to rstfile_particles/step_<run_time>_rank_0.pst

@@ -8,7 +8,7 @@ import struct
 import numpy as np
 import pytest
 
-from mrsph import io
+from mrsph import cases, io
 
 
 class FakeSim:
@@ -168,3 +168,55 @@ def test_corner_average_and_levelset_writer(tmp_path):
     head = open(f, "rb").read().split(b"<AppendedData")[0].decode()
     assert f'WholeExtent="0 {nc} 0 {4 * lv.num_pkg[1]} 0 0"' in head
     assert (tmp_path / "mesh_lset_step_0.pvti").exists() and (tmp_path / "mesh_lset.pvd").exists()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_lset_restart_round_trip(tmp_path, dim):
+    """save_lset_restart / load_lset_restart: the reference's levelset.rst
+    layout (one level) round-trips the level's fields over the interior
+    cells, the cut-cell totals and the package bookkeeping; the level-set
+    fields come from the FP64 oracle (standing in for the engine)."""
+    import oracle
+    if dim == 2:
+        case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    else:
+        case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    orc = oracle.Oracle(case)
+
+    class RstSim(FakeSim):
+        def __init__(self):
+            super().__init__()
+            self.case = case
+
+        def levelset_fields(self, level):
+            f = orc.fields[level]
+            shp = case.levels[level].phi.shape
+            return {"nx": f["nx"].reshape(shp), "ny": f["ny"].reshape(shp), "nz": f["nz"].reshape(shp),
+                    "curv": f["curv"].reshape(shp), "tag": f["tag"].reshape(shp).astype(np.uint8),
+                    "max_phi": orc.ctx.max_phi}
+
+        def volume_mass(self, level, cells=False):
+            return orc.volume_mass(level)
+
+    sim = RstSim()
+    path = io.save_lset_restart(sim, str(tmp_path / "rstfile" / "levelset.rst"))
+    r = io.load_lset_restart(path)
+    lv = case.levels[-1]
+    m = 4 * lv.margin
+    inner = (slice(None),) if dim == 2 else (slice(m, -m),)
+    inner = inner + (slice(m, -m), slice(m, -m))
+    f = sim.levelset_fields(len(case.levels) - 1)
+    assert r["dim"] == dim and r["num_level"] == 1
+    assert np.array_equal(r["phi"], lv.phi[inner])
+    for k, g in (("n_x", "nx"), ("n_y", "ny"), ("n_z", "nz"), ("curv", "curv")):
+        assert np.array_equal(r[k], f[g][inner]), k
+    assert np.array_equal(r["tag_interface"], f["tag"][inner].astype(np.int32))
+    assert np.all(r["idx_characteristic"] == -1) and np.all(r["tag_characteristic"] == 0)
+    vm = orc.volume_mass(-1)
+    assert r["total_mass"] == vm["total_mass"] and r["glbl_num_interface_cell"] == vm["num_interface_cell"]
+    assert r["maximum_phi"] == orc.ctx.max_phi
+    npkg = [lv.num_pkg[d] if d < dim else 1 for d in range(3)]
+    assert tuple(r["num_pkg"]) == tuple(npkg)
+    assert r["glbl_total_num_pkg"] == int(np.prod([n + (2 if d < dim else 0) for d, n in enumerate(npkg)]))
+    counted = (lv.phi[inner] > 0) | (np.abs(lv.phi[inner]) < r["dl"])
+    assert np.all((r["scale_cells"] > 0) == counted)
