@@ -22,7 +22,8 @@
 // expression order; build with -ffp-contract=off so no multiply-add is fused.
 // Deterministic order: each neighbour list is sorted by particle id before any
 // summation.  Reference build flags restated: _MESH_GENERATION_, _DOUBLE_,
-// _NON_PERI_, _NON_SYM_ (symmetric-mirror ghosts off), one rank.
+// _NON_PERI_, _NON_SYM_ (no symmetric-mirror ghosts: the level set bounds the
+// domain), one rank.
 
 #include <algorithm>
 #include <cmath>
