@@ -380,8 +380,8 @@ std::string raw_of(const T* p, size_t count) {
   return r;
 }
 
-std::string vtu_text(long long n, long long m, const std::vector<VtuArray>& pd, const std::vector<VtuArray>& pts,
-                     const std::vector<VtuArray>& cells) {
+std::string vtu_text(long long n, long long m, const std::vector<VtuArray>& pd, const std::vector<VtuArray>& cd,
+                     const std::vector<VtuArray>& pts, const std::vector<VtuArray>& cells) {
   std::string head, blobs;
   unsigned long long offset = 0;
   auto add = [&](const VtuArray& a) {
@@ -397,7 +397,13 @@ std::string vtu_text(long long n, long long m, const std::vector<VtuArray>& pd, 
   head += "  <Piece NumberOfPoints=\"" + std::to_string(n) + "\" NumberOfCells=\"" + std::to_string(m) + "\">\n";
   head += "    <PointData Vectors=\"vector\">\n";
   for (const auto& a : pd) add(a);
-  head += "    </PointData>\n    <Points>\n";
+  head += "    </PointData>\n";
+  if (!cd.empty()) {
+    head += "    <CellData Vectors=\"vector\">\n";
+    for (const auto& a : cd) add(a);
+    head += "    </CellData>\n";
+  }
+  head += "    <Points>\n";
   for (const auto& a : pts) add(a);
   head += "    </Points>\n    <Cells>\n";
   for (const auto& a : cells) add(a);
@@ -407,30 +413,69 @@ std::string vtu_text(long long n, long long m, const std::vector<VtuArray>& pd, 
 
 }  // namespace
 
-std::string particle_vtu(const ParticleFields& f) {
+// the reference's default particle point fields and the positions
+void particle_arrays(const ParticleFields& f, std::vector<VtuArray>& pd, std::vector<VtuArray>& pts) {
   const long long n = f.n;
-  std::vector<int> ids(n), zeros(n, 0), offs(n);
+  std::vector<int> ids(n), zeros(n, 0);
   std::vector<float> h(n), nrm(3 * n), pos(3 * n);
-  std::vector<unsigned char> types(n, 1);  // VTK_VERTEX
   for (long long i = 0; i < n; i++) {
     ids[i] = (int)i;
-    offs[i] = (int)(i + 1);
     h[i] = (float)f.h[i];
     for (int d = 0; d < 3; d++) {
       nrm[3 * i + d] = (float)f.norm[3 * i + d];
       pos[3 * i + d] = (float)f.xyz[3 * i + d];
     }
   }
-  std::vector<VtuArray> pd = {
-      {"id", "Int32", 1, raw_of(ids.data(), n)},       {"local_id", "Int32", 1, raw_of(ids.data(), n)},
-      {"type", "Int32", 1, raw_of(f.type, n)},         {"h", "Float32", 1, raw_of(h.data(), n)},
-      {"NN", "Int32", 1, raw_of(f.nn, n)},             {"color", "Int32", 1, raw_of(zeros.data(), n)},
-      {"norm", "Float32", 3, raw_of(nrm.data(), 3 * n)}};
-  std::vector<VtuArray> pts = {{"Position", "Float32", 3, raw_of(pos.data(), 3 * n)}};
+  pd = {{"id", "Int32", 1, raw_of(ids.data(), n)},       {"local_id", "Int32", 1, raw_of(ids.data(), n)},
+        {"type", "Int32", 1, raw_of(f.type, n)},         {"h", "Float32", 1, raw_of(h.data(), n)},
+        {"NN", "Int32", 1, raw_of(f.nn, n)},             {"color", "Int32", 1, raw_of(zeros.data(), n)},
+        {"norm", "Float32", 3, raw_of(nrm.data(), 3 * n)}};
+  pts = {{"Position", "Float32", 3, raw_of(pos.data(), 3 * n)}};
+}
+
+std::string particle_vtu(const ParticleFields& f) {
+  const long long n = f.n;
+  std::vector<VtuArray> pd, pts;
+  particle_arrays(f, pd, pts);
+  std::vector<int> ids(n), offs(n);
+  for (long long i = 0; i < n; i++) {
+    ids[i] = (int)i;
+    offs[i] = (int)(i + 1);
+  }
+  std::vector<unsigned char> types(n, 1);  // VTK_VERTEX
   std::vector<VtuArray> cells = {{"connectivity", "Int32", 0, raw_of(ids.data(), n)},
                                  {"offsets", "Int32", 0, raw_of(offs.data(), n)},
                                  {"types", "UInt8", 0, raw_of(types.data(), n)}};
-  return vtu_text(n, n, pd, pts, cells);
+  return vtu_text(n, n, pd, {}, pts, cells);
+}
+
+std::string mesh_vtu(const ParticleFields& f, long long ntri, const int* tris) {
+  std::vector<VtuArray> pd, pts;
+  particle_arrays(f, pd, pts);
+  // per-triangle area and aspect ratio (longest / shortest edge) in the plane
+  // (Tri_quality_statistics, graph_mesh.cpp:411-670)
+  std::vector<float> area(ntri), aspect(ntri);
+  std::vector<int> offs(ntri);
+  for (long long t = 0; t < ntri; t++) {
+    const double* a = f.xyz + 3 * (long long)tris[3 * t];
+    const double* b = f.xyz + 3 * (long long)tris[3 * t + 1];
+    const double* c = f.xyz + 3 * (long long)tris[3 * t + 2];
+    auto len = [](const double* p, const double* q) {
+      const double dx = q[0] - p[0], dy = q[1] - p[1];
+      return std::sqrt(dx * dx + dy * dy);
+    };
+    const double e0 = len(a, b), e1 = len(b, c), e2 = len(c, a);
+    area[t] = (float)(0.5 * std::fabs((b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0])));
+    aspect[t] = (float)(std::max(std::max(e0, e1), e2) / std::min(std::min(e0, e1), e2));
+    offs[t] = (int)(3 * (t + 1));
+  }
+  std::vector<unsigned char> types(ntri, 5);  // VTK_TRIANGLE
+  std::vector<VtuArray> cd = {{"vol", "Float32", 1, raw_of(area.data(), ntri)},
+                              {"aspect", "Float32", 1, raw_of(aspect.data(), ntri)}};
+  std::vector<VtuArray> cells = {{"connectivity", "Int32", 0, raw_of(tris, 3 * ntri)},
+                                 {"offsets", "Int32", 0, raw_of(offs.data(), ntri)},
+                                 {"types", "UInt8", 0, raw_of(types.data(), ntri)}};
+  return vtu_text(f.n, ntri, pd, cd, pts, cells);
 }
 
 std::string particle_pvtu(const std::string& piece) {
@@ -447,6 +492,15 @@ std::string particle_pvtu(const std::string& piece) {
   return t;
 }
 
+std::string mesh_pvtu(const std::string& piece) {
+  std::string t = particle_pvtu(piece);  // the cell fields go between the point fields and the points
+  const std::string cells = "  <PCellData>\n    <PDataArray type=\"Float32\" Name=\"vol\" NumberOfComponents=\"1\"/>\n"
+                            "    <PDataArray type=\"Float32\" Name=\"aspect\" NumberOfComponents=\"1\"/>\n"
+                            "  </PCellData>\n";
+  t.insert(t.find("  <PPoints>"), cells);
+  return t;
+}
+
 void update_pvd(const std::string& path, int n_out, const std::string& timestep, const std::string& dataset) {
   std::vector<std::string> entries;
   if (n_out != 0) {
@@ -460,6 +514,42 @@ void update_pvd(const std::string& path, int n_out, const std::string& timestep,
   out << "<VTKFile type=\"Collection\" version=\"0.1\">\n  <Collection>\n";
   for (const auto& e : entries) out << e << "\n";
   out << "  </Collection>\n</VTKFile>\n";
+}
+
+std::string Mesh_binary_writer::Output_mesh(int n_out, SPH_mesh_generation& sim, long long run_time) {
+  make_dir(outdir_);
+  long long ntri = 0;
+  int rc = mrsph_triangulate(sim.handle(), nullptr, 0, &ntri, nullptr);
+  if (rc) throw Error(rc, "mrsph_triangulate");
+  std::vector<int> tris(3 * (ntri > 0 ? ntri : 1));
+  mrsph_tri_quality q{};
+  rc = mrsph_triangulate(sim.handle(), tris.data(), ntri, &ntri, &q);
+  if (rc) throw Error(rc, "mrsph_triangulate");
+  std::vector<int> type, nn;
+  std::vector<double> h, norm;
+  sim.Particle_fields(type, h, norm, nn);
+  const std::vector<double> xyz = sim.Positions();
+  ParticleFields f;
+  f.n = sim.num_particles();
+  f.xyz = xyz.data();
+  f.type = type.data();
+  f.h = h.data();
+  f.nn = nn.data();
+  f.norm = norm.data();
+  const std::string piece = "mesh_tris_rank_0_step_" + std::to_string(n_out) + ".vtu";
+  const std::string pvtu = "mesh_tris_step_" + std::to_string(n_out) + ".pvtu";
+  {
+    std::ofstream o(outdir_ + "/" + piece, std::ios::binary | std::ios::trunc);
+    const std::string b = mesh_vtu(f, ntri, tris.data());
+    o.write(b.data(), (std::streamsize)b.size());
+  }
+  {
+    std::ofstream o(outdir_ + "/" + pvtu, std::ios::trunc);
+    o << mesh_pvtu(piece);
+  }
+  const long long ts = run_time < 0 ? sim.Stats().step : run_time;
+  update_pvd(outdir_ + "/mesh_tris.pvd", n_out, std::to_string(ts), "./" + pvtu);
+  return outdir_ + "/" + piece;
 }
 
 std::string Particle_binary_writer::Output_particle(int n_out, SPH_mesh_generation& sim, long long run_time) {
@@ -768,4 +858,29 @@ extern "C" long long mrsph_host_lset_vti(const char* path, const int* ncell, con
   std::ofstream o(path, std::ios::binary | std::ios::trunc);
   o.write(b.data(), (std::streamsize)b.size());
   return o ? (long long)b.size() : -1;
+}
+
+// C entry for the writer tests: the triangle-mesh VTU bytes of host arrays.
+extern "C" long long mrsph_host_mesh_vtu(const char* path, long long n, const double* xyz, const int* type,
+                                         const double* h, const int* nn, const double* norm, long long ntri,
+                                         const int* tris) {
+  mrsph_host::ParticleFields f;
+  f.n = n;
+  f.xyz = xyz;
+  f.type = type;
+  f.h = h;
+  f.nn = nn;
+  f.norm = norm;
+  const std::string b = mrsph_host::mesh_vtu(f, ntri, tris);
+  std::ofstream o(path, std::ios::binary | std::ios::trunc);
+  o.write(b.data(), (std::streamsize)b.size());
+  return o ? (long long)b.size() : -1;
+}
+
+// C entry for the writer tests: the particle (mesh = 0) or mesh (mesh = 1)
+// PVTU text for a piece name; returns its length (written when it fits).
+extern "C" long long mrsph_host_pvtu(int mesh, const char* piece, char* buf, long long len) {
+  const std::string t = mesh ? mrsph_host::mesh_pvtu(piece) : mrsph_host::particle_pvtu(piece);
+  if (buf && len > (long long)t.size()) std::memcpy(buf, t.c_str(), t.size() + 1);
+  return (long long)t.size();
 }

@@ -179,10 +179,27 @@ struct ParticleFields {
   const double* norm = nullptr;  // n x 3
 };
 std::string particle_vtu(const ParticleFields& f);
+// Mesh_binary_writer (mesh_binary_writer.cpp:36-390) for the 2D triangle
+// mesh: the particle point fields, one triangle cell per triangle and the
+// cell fields 'vol' (area) and 'aspect' (longest / shortest edge).
+std::string mesh_vtu(const ParticleFields& f, long long ntri, const int* tris);
 std::string particle_pvtu(const std::string& piece);
+std::string mesh_pvtu(const std::string& piece);
 // Rewrites outdir/<name>.pvd with one DataSet entry per output so far
 // (Output_pvd_file, particle_binary_writer.cpp:53-93); n_out = 0 starts it.
 void update_pvd(const std::string& path, int n_out, const std::string& timestep, const std::string& dataset);
+
+class Mesh_binary_writer {
+ public:
+  explicit Mesh_binary_writer(const std::string& outdir = "outdata") : outdir_(outdir) {}
+  // 2D only: triangulates the current particles (mrsph_triangulate) and
+  // writes outdir/mesh_tris_rank_0_step_<n>.vtu, mesh_tris_step_<n>.pvtu and
+  // mesh_tris.pvd.  Returns the piece's path.
+  std::string Output_mesh(int n_out, SPH_mesh_generation& sim, long long run_time = -1);
+
+ private:
+  std::string outdir_;
+};
 
 class Particle_binary_writer {
  public:

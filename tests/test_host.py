@@ -130,3 +130,50 @@ def test_repr_double_matches_python(binary):
             head = open(path, "rb").read().split(b"<PointData")[0].decode()
             ref = io.vti_bytes([1, 1, 1], list(o), list(s), [("phi", z8)], []).split(b"<PointData")[0].decode()
             assert head == ref, (v, head, ref)
+
+
+def test_cpp_mesh_vtu_matches_python_writer(binary, tmp_path):
+    """The C++ triangle-mesh VTU (Mesh_binary_writer) equals the Python
+    writer's bytes for the same particles and triangles."""
+    import ctypes
+    import numpy as np
+    from mrsph import io
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    f = lib.mrsph_host_mesh_vtu
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p, ctypes.c_longlong] + [ctypes.c_void_p] * 5 + [ctypes.c_longlong, ctypes.c_void_p]
+    rng = np.random.default_rng(9)
+    n, m = 400, 700
+    xyz = np.concatenate([rng.random((n, 2)), np.zeros((n, 1))], axis=1)
+    typ = rng.integers(0, 2, n).astype(np.int32)
+    h = rng.random(n)
+    nn = rng.integers(1, 30, n).astype(np.int32)
+    nrm = np.concatenate([rng.normal(size=(n, 2)), np.zeros((n, 1))], axis=1)
+    tris = np.stack([rng.choice(n, 3, replace=False) for _ in range(m)]).astype(np.int32)
+    p = tmp_path / "m.vtu"
+    size = f(str(p).encode(), n, xyz.ctypes.data, typ.ctypes.data, h.ctypes.data, nn.ctypes.data, nrm.ctypes.data,
+             m, tris.ctypes.data)
+    pd = [("id", np.arange(n, dtype="<i4")), ("local_id", np.arange(n, dtype="<i4")), ("type", typ),
+          ("h", h.astype("<f4")), ("NN", nn), ("color", np.zeros(n, dtype="<i4")), ("norm", nrm.astype("<f4"))]
+    vol, aspect = io.triangle_quality(xyz, tris)
+    ref = io.vtu_bytes(xyz, tris, 5, pd, [("vol", vol.astype("<f4")), ("aspect", aspect.astype("<f4"))])
+    assert size == len(ref) and p.read_bytes() == ref
+
+
+@pytest.mark.parametrize("mesh", [0, 1])
+def test_cpp_pvtu_matches_python(binary, mesh):
+    import ctypes
+    import numpy as np
+    from mrsph import io
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    f = lib.mrsph_host_pvtu
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_longlong]
+    buf = ctypes.create_string_buffer(8192)
+    n = f(mesh, b"piece_0.vtu", buf, 8192)
+    pd = [("id", np.zeros(1, "<i4")), ("local_id", np.zeros(1, "<i4")), ("type", np.zeros(1, "<i4")),
+          ("h", np.zeros(1, "<f4")), ("NN", np.zeros(1, "<i4")), ("color", np.zeros(1, "<i4")),
+          ("norm", np.zeros((1, 3), "<f4"))]
+    cd = [("vol", np.zeros(1, "<f4")), ("aspect", np.zeros(1, "<f4"))] if mesh else []
+    ref = io._pvtu_text(["piece_0.vtu"], io._fields_meta(pd), io._fields_meta(cd))
+    assert n == len(ref) and buf.value.decode() == ref
