@@ -516,6 +516,161 @@ void update_pvd(const std::string& path, int n_out, const std::string& timestep,
   out << "  </Collection>\n</VTKFile>\n";
 }
 
+std::string lset_restart_bytes(const LsetRestart& r) {
+  std::string b;
+  auto I = [&](int v) { b += raw_of(&v, 1); };
+  auto D = [&](double v) { b += raw_of(&v, 1); };
+  std::array<double, 3> dom;
+  for (int d = 0; d < 3; d++) dom[d] = r.box_r[d] - r.box_l[d];
+  I(r.dim);
+  for (int k = 0; k < 2; k++) {  // domain, box, then the particle box (the same)
+    for (int d = 0; d < 3; d++) D(dom[d]);
+    for (int d = 0; d < 3; d++) D(r.box_l[d]);
+    for (int d = 0; d < 3; d++) D(r.box_r[d]);
+  }
+  for (int d = 0; d < 3; d++) I(d < r.dim ? 4 * r.num_pkg[d] : 1);  // resolution
+  I(0);  // Lmin
+  I(0);  // Lmax
+  for (int d = 0; d < 3; d++) I(r.num_pkg[d]);  // ini_num_cell
+  I(1);  // num_level
+  D(1.e-4);  // convergence_error
+  I(0);  // singularities
+  I(0);  // segments
+  for (double v : {r.fac_max, r.fac_mid, r.fac_min, r.curv_artificial, r.total_mass, r.total_mass_surface, 0.0,
+                   r.total_volume, r.total_area, 0.0, r.max_phi, 0.0, r.max_dl, r.mid_dl, r.min_dl, r.max_curv,
+                   r.min_curv})
+    D(v);
+  I(r.num_interface_cell);
+  int total = 1;
+  for (int d = 0; d < 3; d++) total *= r.num_pkg[d] + 2 * r.margin[d];
+  I(total);
+  D(r.dpkg[0]);  // scale
+  double dl = 1.e20;
+  for (int d = 0; d < r.dim; d++) dl = std::min(dl, r.dcell[d]);
+  D(dl);
+  for (int d = 0; d < 3; d++) I(r.num_pkg[d]);
+  for (int d = 0; d < 3; d++) I(r.num_pkg[d] + 2 * r.margin[d]);
+  for (int k = 0; k < 2; k++) {  // global and local package ranges (one rank)
+    for (int d = 0; d < 3; d++) I(-r.margin[d]);
+    for (int d = 0; d < 3; d++) I(r.num_pkg[d] + r.margin[d]);
+  }
+  for (int d = 0; d < 3; d++) I(r.margin[d]);
+  for (int d = 0; d < 3; d++) D(r.dpkg[d]);
+  for (int d = 0; d < 3; d++) D(r.dcell[d]);
+  const size_t n = r.phi.size();
+  std::vector<double> zero(n, 0.0);
+  std::vector<int> izero(n, 0), minus(n, -1);
+  const std::vector<double>* fields[6] = {&r.phi, &r.nx, &r.ny, &r.nz, &r.curv, &zero};
+  for (const std::vector<double>* v : fields) b += raw_of(v->data(), n);
+  b += raw_of(r.tag.data(), n) + raw_of(izero.data(), n) + raw_of(minus.data(), n);
+  b += raw_of(r.scale.data(), n);
+  return b;
+}
+
+std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path, int level) {
+  const Case& cs = sim.Get_case();
+  const mrsph_params& p = cs.params;
+  const int dim = p.dim, nls = (int)cs.levels.size();
+  level = ((level % nls) + nls) % nls;
+  const LevelGrid& lv = cs.levels[level];
+  std::array<int, 3> n{{1, 1, 1}};
+  for (int d = 0; d < dim; d++) n[d] = (lv.num_pkg[d] + 2 * lv.margin) * 4;
+  const int m = 4 * lv.margin;
+  std::vector<std::vector<double>> curv(nls);
+  std::vector<std::vector<unsigned char>> tag(nls);
+  std::vector<double> nx, ny, nz;
+  double max_phi = 0.0;
+  for (int l = 0; l < nls; l++) {
+    const size_t nl = cs.levels[l].phi.size();
+    curv[l].assign(nl, 0.0);
+    tag[l].assign(nl, 0);
+    if (l == level) {
+      nx.assign(nl, 0.0);
+      ny.assign(nl, 0.0);
+      nz.assign(nl, 0.0);
+    }
+    int rc = mrsph_get_levelset(sim.handle(), l, l == level ? nx.data() : nullptr, l == level ? ny.data() : nullptr,
+                                l == level ? nz.data() : nullptr, curv[l].data(), tag[l].data(), &max_phi);
+    if (rc) throw Error(rc, "mrsph_get_levelset");
+  }
+  mrsph_volume_mass_stats vm{};
+  int rc = mrsph_volume_mass(sim.handle(), level, &vm, nullptr, nullptr);
+  if (rc) throw Error(rc, "mrsph_volume_mass");
+  double dl0 = 1.e20, dl = 1.e20;
+  for (int d = 0; d < dim; d++) {
+    dl0 = std::min(dl0, cs.levels[0].dpkg[d] / 4.0);
+    dl = std::min(dl, lv.dpkg[d] / 4.0);
+  }
+  double cmax = 0.0, cmin = 1.e20;
+  bool any = false;
+  for (int l = 0; l < nls; l++)
+    for (size_t a = 0; a < curv[l].size(); a++)
+      if (tag[l][a] == 1) {
+        const double v = std::fabs(curv[l][a]);
+        cmax = any ? std::max(cmax, v) : v;
+        cmin = any ? std::min(cmin, v) : v;
+        any = true;
+      }
+  const double mid = p.middle_dl > 0 ? p.middle_dl : 5.0 * dl0;
+  LsetRestart r;
+  r.dim = dim;
+  for (int d = 0; d < 3; d++) {
+    r.box_l[d] = d < dim ? p.box_l[d] : 0.0;
+    r.box_r[d] = d < dim ? p.box_r[d] : 0.0;
+    r.num_pkg[d] = d < dim ? lv.num_pkg[d] : 1;
+    r.margin[d] = d < dim ? lv.margin : 0;
+    r.dpkg[d] = lv.dpkg[d];
+    r.dcell[d] = d < dim ? lv.dpkg[d] / 4.0 : lv.dpkg[d];
+  }
+  r.fac_max = p.max_dl / dl0;
+  r.fac_mid = mid / dl0;
+  r.fac_min = p.min_dl / dl0;
+  r.curv_artificial = std::min(1.0, cmax);
+  r.total_mass = vm.total_mass;
+  r.total_mass_surface = vm.total_mass_surface;
+  r.total_volume = vm.total_volume;
+  r.total_area = vm.total_area;
+  r.max_phi = max_phi;
+  r.max_dl = p.max_dl;
+  r.mid_dl = mid;
+  r.min_dl = p.min_dl;
+  r.max_curv = cmax;
+  r.min_curv = cmin;
+  r.num_interface_cell = (int)vm.num_interface_cell;
+  const int z0 = dim == 3 ? m : 0, z1 = dim == 3 ? n[2] - m : 1;
+  for (int z = z0; z < z1; z++)
+    for (int y = m; y < n[1] - m; y++)
+      for (int x = m; x < n[0] - m; x++) {
+        const size_t a = ((size_t)z * n[1] + y) * n[0] + x;
+        const double phi = lv.phi[a];
+        r.phi.push_back(phi);
+        r.nx.push_back(nx[a]);
+        r.ny.push_back(ny[a]);
+        r.nz.push_back(nz[a]);
+        r.curv.push_back(curv[level][a]);
+        r.tag.push_back(tag[level][a]);
+        double sc = 0.0;  // the scale Calculate_volume_mass leaves in the counted cells
+        if (phi > 0 || std::fabs(phi) < dl) {
+          double lo = p.min_dl;
+          if (p.scale_law == 1) {
+            double q = (cmax - std::fabs(curv[level][a])) / (cmax - cmin + 1e-20);
+            q = std::min(std::max(q, 0.0), 1.0);
+            lo = p.min_dl + q * q * (mid - p.min_dl);
+          }
+          const double s = lo + std::tanh(2.5 * std::fabs(phi) / max_phi) / std::tanh(2.5) * (p.max_dl - lo);
+          sc = (phi > 0 || std::fabs(phi) < dl0) ? s : p.min_dl;
+        }
+        r.scale.push_back(sc);
+      }
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos) make_dir(path.substr(0, slash));
+  std::ofstream o(path, std::ios::binary | std::ios::trunc);
+  const std::string b = lset_restart_bytes(r);
+  o.write(b.data(), (std::streamsize)b.size());
+  if (!o) throw Error(MRSPH_ERR_ARG, "cannot write " + path);
+  return path;
+}
+
 std::string Mesh_binary_writer::Output_mesh(int n_out, SPH_mesh_generation& sim, long long run_time) {
   make_dir(outdir_);
   long long ntri = 0;
@@ -883,4 +1038,42 @@ extern "C" long long mrsph_host_pvtu(int mesh, const char* piece, char* buf, lon
   const std::string t = mesh ? mrsph_host::mesh_pvtu(piece) : mrsph_host::particle_pvtu(piece);
   if (buf && len > (long long)t.size()) std::memcpy(buf, t.c_str(), t.size() + 1);
   return (long long)t.size();
+}
+
+// C entry for the writer tests: level-set restart bytes of host arrays
+// (header values in the order of LsetRestart: box_l[3], box_r[3], dpkg[3],
+// dcell[3], fac_max, fac_mid, fac_min, curv_artificial, total_mass,
+// total_mass_surface, total_volume, total_area, max_phi, max_dl, mid_dl,
+// min_dl, max_curv, min_curv; ints: dim, num_pkg[3], margin[3],
+// num_interface_cell).
+extern "C" long long mrsph_host_lset_restart(const char* path, const double* hd, const int* hi, long long n,
+                                             const double* phi, const double* nx, const double* ny,
+                                             const double* nz, const double* curv, const int* tag,
+                                             const double* scale) {
+  mrsph_host::LsetRestart r;
+  for (int d = 0; d < 3; d++) {
+    r.box_l[d] = hd[d];
+    r.box_r[d] = hd[3 + d];
+    r.dpkg[d] = hd[6 + d];
+    r.dcell[d] = hd[9 + d];
+    r.num_pkg[d] = hi[1 + d];
+    r.margin[d] = hi[4 + d];
+  }
+  double* v[] = {&r.fac_max, &r.fac_mid, &r.fac_min, &r.curv_artificial, &r.total_mass, &r.total_mass_surface,
+                 &r.total_volume, &r.total_area, &r.max_phi, &r.max_dl, &r.mid_dl, &r.min_dl, &r.max_curv,
+                 &r.min_curv};
+  for (int k = 0; k < 14; k++) *v[k] = hd[12 + k];
+  r.dim = hi[0];
+  r.num_interface_cell = hi[7];
+  r.phi.assign(phi, phi + n);
+  r.nx.assign(nx, nx + n);
+  r.ny.assign(ny, ny + n);
+  r.nz.assign(nz, nz + n);
+  r.curv.assign(curv, curv + n);
+  r.tag.assign(tag, tag + n);
+  r.scale.assign(scale, scale + n);
+  const std::string b = mrsph_host::lset_restart_bytes(r);
+  std::ofstream o(path, std::ios::binary | std::ios::trunc);
+  o.write(b.data(), (std::streamsize)b.size());
+  return o ? (long long)b.size() : -1;
 }

@@ -189,6 +189,29 @@ std::string mesh_pvtu(const std::string& piece);
 // (Output_pvd_file, particle_binary_writer.cpp:53-93); n_out = 0 starts it.
 void update_pvd(const std::string& path, int n_out, const std::string& timestep, const std::string& dataset);
 
+// Level-set restart rstfile/levelset.rst of one level (Save_restart_file,
+// sph_mesh_generation.cpp:2671-2736; Save_lset_restart_file,
+// level_set.cpp:1022-1094; Write_level_set_rstfile,
+// lset_level_infor.cpp:695-929), little-endian: the same bytes as the Python
+// writer (mrsph/io.py save_lset_restart).
+struct LsetRestart {
+  int dim = 3;
+  std::array<double, 3> box_l{{0, 0, 0}}, box_r{{0, 0, 0}};
+  std::array<int, 3> num_pkg{{1, 1, 1}}, margin{{0, 0, 0}};
+  std::array<double, 3> dpkg{{1, 1, 1}}, dcell{{1, 1, 1}};
+  double fac_max = 0, fac_mid = 0, fac_min = 0, curv_artificial = 0;
+  double total_mass = 0, total_mass_surface = 0, total_volume = 0, total_area = 0;
+  double max_phi = 0, max_dl = 0, mid_dl = 0, min_dl = 0, max_curv = 0, min_curv = 0;
+  int num_interface_cell = 0;
+  // interior cells, x fastest
+  std::vector<double> phi, nx, ny, nz, curv, scale;
+  std::vector<int> tag;
+};
+std::string lset_restart_bytes(const LsetRestart& r);
+// Gathers the record of one level (< 0: the finest) from the engine and
+// writes it to path.
+std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path, int level = -1);
+
 class Mesh_binary_writer {
  public:
   explicit Mesh_binary_writer(const std::string& outdir = "outdata") : outdir_(outdir) {}

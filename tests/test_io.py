@@ -220,3 +220,52 @@ def test_lset_restart_round_trip(tmp_path, dim):
     assert r["glbl_total_num_pkg"] == int(np.prod([n + (2 if d < dim else 0) for d, n in enumerate(npkg)]))
     counted = (lv.phi[inner] > 0) | (np.abs(lv.phi[inner]) < r["dl"])
     assert np.all((r["scale_cells"] > 0) == counted)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cpp_lset_restart_bytes_match_python(tmp_path, dim):
+    """The C++ host layer's level-set restart serialiser writes the bytes the
+    Python writer wrote, for the values and fields read back from it."""
+    import ctypes
+    from mrsph import build
+    import oracle
+    build.build_host()
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(io.__file__), "..", "libmrsph_host.so"))
+    f = lib.mrsph_host_lset_restart
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong] + [ctypes.c_void_p] * 7
+    case = cases.disc_hole_2d(spacing=0.02, grid=64) if dim == 2 else \
+        cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    orc = oracle.Oracle(case)
+
+    class RstSim(FakeSim):
+        def __init__(self):
+            super().__init__()
+            self.case = case
+
+        def levelset_fields(self, level):
+            g = orc.fields[level]
+            shp = case.levels[level].phi.shape
+            return {"nx": g["nx"].reshape(shp), "ny": g["ny"].reshape(shp), "nz": g["nz"].reshape(shp),
+                    "curv": g["curv"].reshape(shp), "tag": g["tag"].reshape(shp).astype(np.uint8),
+                    "max_phi": orc.ctx.max_phi}
+
+        def volume_mass(self, level, cells=False):
+            return orc.volume_mass(level)
+
+    py = io.save_lset_restart(RstSim(), str(tmp_path / "py.rst"))
+    r = io.load_lset_restart(py)
+    box_r = [r["box_l"][d] + r["domain"][d] for d in range(3)]
+    hd = np.array(list(r["box_l"]) + box_r + list(r["dpkg"]) + list(r["dcell"]) +
+                  [r[k] for k in ("fac_maximum_dl", "fac_middel_dl", "fac_minimum_dl", "maximum_curv_artificial",
+                                  "total_mass", "total_mass_surface", "total_volume", "total_area", "maximum_phi",
+                                  "maximum_dl", "middel_dl", "minimum_dl", "maximum_curv", "minimum_curv")])
+    hi = np.array([r["dim"], *r["num_pkg"], *r["num_pkg_margin"], r["glbl_num_interface_cell"]], dtype=np.int32)
+    arrs = [np.ascontiguousarray(r[k].ravel()) for k in ("phi", "n_x", "n_y", "n_z", "curv")]
+    tag = np.ascontiguousarray(r["tag_interface"].ravel())
+    scale = np.ascontiguousarray(r["scale_cells"].ravel())
+    out = tmp_path / "cpp.rst"
+    size = f(str(out).encode(), hd.ctypes.data, hi.ctypes.data, len(tag), *[a.ctypes.data for a in arrs],
+             tag.ctypes.data, scale.ctypes.data)
+    ref = open(py, "rb").read()
+    assert size == len(ref) and out.read_bytes() == ref
