@@ -341,7 +341,7 @@ __host__ __device__ __noinline__ void gc_path64(const double* cor, const int* pa
 // no index depends on c; each value takes at most three rounded midpoints
 // (two in 2D) from the node's corners.
 template <int D>
-__device__ inline void gc_child32(const float* p, int c, float* out) {
+__host__ __device__ inline void gc_child32(const float* p, int c, float* out) {
   if (D == 3) {
     const bool i = (c >> 2) & 1, j = (c >> 1) & 1, k = c & 1;
     float z[2][2][2], y[2][2][2];
