@@ -94,3 +94,10 @@ def test_fp32_sign_bound(tmp_path):
             assert abs(Fraction(got[q, 1]) - e) <= Fraction(12, 2 ** 53) * Fraction(M)
             if abs(got[q, 0]) > M * 2.0 ** -20:
                 assert np.sign(got[q, 0]) == np.sign(got[q, 1])
+        # the leaf rule's corner sum, in FP32 in the kernel's order, within 2^-16 M
+        cv = np.float32(0.0)
+        for q in range(8):
+            cv = np.float32(cv + np.float32(got[q, 0]))
+        assert abs(Fraction(float(cv)) - sum(ex)) <= Fraction(160, 2 ** 24) * Fraction(M)
+        if abs(float(cv)) > M * 2.0 ** -16:
+            assert np.sign(float(cv)) == np.sign(sum(Fraction(float(v)) for v in got[:, 1]))
