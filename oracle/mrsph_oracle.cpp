@@ -1090,6 +1090,10 @@ void orc_kernel_dW(int kind, int D, long long n, const double* dist, double h, d
   for (long long i = 0; i < n; i++) out[i] = kernel_dW(kind, D, dist[i], h);
 }
 double orc_get_scale(const orc_ctx* c, double phi, double curv) { return get_scale(*c, c->dim, phi, curv); }
+int orc_set_particle_scale(const orc_ctx* c, double h, double scale_in, double* scale_out) {
+  *scale_out = scale_in;
+  return set_particle_scale(*c, h, scale_out);
+}
 
 // max / min |curvature| over the CUT cells of one level (Levelset_package::
 // Get_global_scale, lset_package.cpp:765-785); min stays 1e20 without CUT cells

@@ -99,6 +99,8 @@ def lib():
         L.orc_get_scale.argtypes = [C.POINTER(OrcCtx), C.c_double, C.c_double]
         L.orc_ls_curv_range.argtypes = [C.POINTER(OrcCtx), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_get_scale.restype = C.c_double
+        L.orc_set_particle_scale.argtypes = [C.POINTER(OrcCtx), C.c_double, C.c_double, C.POINTER(C.c_double)]
+        L.orc_set_particle_scale.restype = C.c_int
         L.orc_philox.argtypes = [C.c_uint32] * 4 + [C.c_ulonglong, C.c_void_p]
         L.orc_sample.argtypes = [C.POINTER(OrcCtx), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_void_p]
@@ -378,6 +380,17 @@ def kernel_dW(kind: int, dim: int, dist: np.ndarray, h: float) -> np.ndarray:
     out = np.zeros_like(dist)
     lib().orc_kernel_dW(kind, dim, len(dist), _p(dist), h, _p(out))
     return out
+
+
+def set_particle_scale(h: float, scale: float, cutoff: float, max_scale: float, min_scale: float):
+    """Particle_base::Set_particle_scale of the oracle: (new scale, flag)."""
+    c = OrcCtx()
+    c.cutoff = cutoff
+    c.max_scale = max_scale
+    c.min_scale = min_scale
+    out = C.c_double(0.0)
+    flag = lib().orc_set_particle_scale(C.byref(c), h, scale, C.byref(out))
+    return out.value, int(flag)
 
 
 def philox(c0, c1, c2, c3, seed):
