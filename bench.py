@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--no-volume-mass", action="store_true", help="skip the cut-cell volume / particle-count leg")
     ap.add_argument("--accuracy-steps", type=int, default=100, help="relaxation steps of the accuracy leg (0: skip)")
+    ap.add_argument("--ref-budget", type=float, default=60.0,
+                    help="seconds of timed oracle steps in the reference arm (at least one step)")
     return ap.parse_args()
 
 
@@ -78,7 +80,7 @@ def config_of(case, name):
             "h_over_dx": p["cell_ratio"] / p["cutoff"], "dx_range": [p["min_dl"], p["max_dl"]],
             "levelset_levels": len(case.levels),
             "levelset_cells": [int(lv.phi.size) for lv in case.levels],
-            "precision": "fp32_split", "l2": "working set (state + neighbour lists) larger than the 129 MB L2",
+            "l2": "working set (state + neighbour lists) larger than the 129 MB L2",
             "parallelism": "replicas"}
 
 
@@ -178,9 +180,10 @@ def barrier(dist):
 
 
 def cpu_oracle_run(case, steps: int):
-    """Time the FP64 oracle (OpenMP, all host threads) on the workload."""
+    """Time the FP64 oracle (OpenMP, all host threads, host-CPU tuned build)
+    on the workload."""
+    os.environ["MRSPH_ORACLE_TUNED"] = "1"
     import oracle
-    oracle.build()
     orc = oracle.Oracle(case)
     t0 = time.perf_counter()
     orc.seed(case.n_particles)
@@ -196,8 +199,8 @@ def cpu_oracle_run(case, steps: int):
 def cpu_volume_mass(case):
     """Time the oracle's cut-cell volume pass (OpenMP, all host threads) on
     the finest level of the workload."""
+    os.environ["MRSPH_ORACLE_TUNED"] = "1"
     import oracle
-    oracle.build()
     t0 = time.perf_counter()
     orc = oracle.Oracle(case)  # level-set build of every level (normals, tags, curvature, max phi)
     ls_s = time.perf_counter() - t0
@@ -207,39 +210,44 @@ def cpu_volume_mass(case):
 
 
 def run_reference(args, ws, rank, dist):
+    """The reference arm: the CPU implementation of the path (the FP64 oracle
+    restating the reference; the reference itself does not build here), on
+    the same workload and over the same step window as the GPU arm: seeding
+    and pre-run, the GPU arm's warm-up steps untimed, then the window's steps
+    timed one by one until about --ref-budget seconds are spent (at least
+    one).  The line reports the steps it timed and their window."""
     if rank != 0:
         return
     case = workload(args.workload, "fp32")
     cfg = config_of(case, args.workload)
-    cfg["precision"] = "fp64 (CPU oracle)"
-    warm = min(args.warmup, 1)
+    warm = max(args.warmup, 3)
+    os.environ["MRSPH_ORACLE_TUNED"] = "1"
     import oracle
-    oracle.build()
     orc = oracle.Oracle(case)
     orc.seed(case.n_particles)
     orc.pre_run()
-    if warm:
-        orc.steps(warm)
-    # bounded sample: stop adding steps once ~120 s of CPU time is spent
+    orc.steps(warm)
     t0 = time.perf_counter()
     done, pairs = 0, 0
     while done < args.steps:
         pairs += orc.steps(1)
         done += 1
-        if time.perf_counter() - t0 > 120.0:
+        if time.perf_counter() - t0 > args.ref_budget:
             break
     dt = time.perf_counter() - t0
     v = case.n_particles * done / dt
     threads = oracle.num_threads()
+    window = f"steps {warm + 1}..{warm + done} after seeding"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / done,
+            "steps": done, "warmup": args.warmup, "window": window, "ms_per_step": 1000.0 * dt / done,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": cfg,
             "pair_interactions_per_s": 3.0 * pairs / dt,
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{done} of {args.steps} relaxation steps of the full workload "
+                             "sample": f"{done} relaxation step(s) ({window}; the GPU arm times steps "
+                                       f"{warm + 1}..{warm + args.steps}) of the full workload "
                                        f"(N={case.n_particles}), FP64 oracle restating the reference, "
-                                       f"OpenMP on {threads} threads"},
+                                       f"OpenMP on {threads} threads, -O3 {' '.join(oracle.tuning_flags())}"},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -295,71 +303,112 @@ def run_batched(args, dev, dist):
                         "Wendland C2, h = 1.3 dx, FP32-split"}
 
 
-def spacing_stats(xyz, h, h_over_dx, dim):
-    """Nearest-neighbour distance over the target spacing (h / (h/dx))."""
+def spacing_stats(xyz, h, h_over_dx, dim, type_=None, phi=None):
+    """Nearest-neighbour distance over the target spacing (h / (h/dx)), its
+    percentiles and 40-bin histogram, the minimum pair distance, and the
+    SURFACE particles' count and mean |phi| over their target spacing."""
     import numpy as np
     from scipy.spatial import cKDTree
     pts = xyz[:, :dim]
     d, _ = cKDTree(pts).query(pts, k=2)
     r = d[:, 1] / (h / h_over_dx)
     hist, _ = np.histogram(r, bins=40, range=(0.0, 2.0))
-    return {"median": float(np.median(r)), "p05": float(np.percentile(r, 5)), "p95": float(np.percentile(r, 95)),
-            "min_ratio": float(r.min()), "min_distance": float(d[:, 1].min()), "hist": hist.tolist()}
+    out = {"median": float(np.median(r)), "p05": float(np.percentile(r, 5)), "p95": float(np.percentile(r, 95)),
+           "min_ratio": float(r.min()), "min_distance": float(d[:, 1].min()), "hist": hist.tolist()}
+    if type_ is not None:
+        surf = type_ == 1
+        dev_s = np.abs(phi[surf]) / (h[surf] / h_over_dx) if surf.any() else np.zeros(1)
+        out.update(surface_count=int(surf.sum()), surface_dev_mean=float(dev_s.mean()),
+                   surface_dev_max=float(dev_s.max()))
+    return out
 
 
 def run_accuracy(args, dev):
-    """FP32-split against FP64-plain on the GPU (FP64-plain is held to the FP64
-    oracle at 1e-12 by the parity tests) on torus_3d_small: single-step
-    accelerations from one injected state, and spacing statistics after
-    accuracy_steps steps from the same seed."""
+    """FP32-split against the FP64 oracle (the CPU restatement of the
+    reference) on a 37,658-particle torus (dx 0.02-0.08): the oracle relaxes
+    accuracy_steps steps from its seed; the GPU's FP32 path relaxes the same
+    steps from the same seed state; and, from the oracle's state after 20
+    steps, the GPU makes one step whose binning, neighbour sets, kernel sums
+    and force stages are compared with the oracle's on the GPU's post-map
+    state."""
     import numpy as np
-    from mrsph import SPHMeshGeneration
-    case = workload("torus_3d_small", "fp32")
+    import oracle
+    from mrsph import SPHMeshGeneration, cases
+    case = cases.torus_3d(dx_min=0.02, dx_max=0.08)
     dim = case.params["dim"]
     hdx = case.params["cell_ratio"] / case.params["cutoff"]
-    # one state after 20 FP64 steps, injected into both paths
-    g = SPHMeshGeneration(case, precision="fp64", device=dev)
-    g.Initialize_case()
-    g.SPH_run_mesh_generation(20)
-    st = g.particles(("xyz", "v", "type", "h", "level", "nu"))
-    s0 = g.stats()
+    orc = oracle.Oracle(case)
+    orc.seed(case.n_particles)
+    orc.pre_run()
+    seed_st = orc.get_state()
+
+    def to_gpu(st):
+        return {"xyz": np.stack([st["x"], st["y"], st["z"]], axis=1),
+                "v": np.stack([st["vx"], st["vy"], st["vz"]], axis=1), "type": st["type"], "h": st["h"],
+                "level": st["level"], "nu": st["nu"], "dt": st["dt"], "step": st["step"]}
+
+    t0 = time.perf_counter()
+    orc.steps(20)
+    st20 = orc.get_state()
+    orc.steps(args.accuracy_steps - 20)
+    oracle_s = time.perf_counter() - t0
+    # one step from the oracle's state after 20 steps
+    g = SPHMeshGeneration(case, precision="fp32", device=dev, neighbor_cap=1024)
+    g.set_state(to_gpu(st20))
+    g.run_phase(5)
+    gp = g.particles()
+    lc, _ = g.cells()
+    off, nb = g.neighbors()
     g.close()
-    st["dt"] = s0["dt"]
-    st["step"] = s0["step"]
-    acc = {}
-    for prec in ("fp64", "fp32"):
-        g = SPHMeshGeneration(case, precision=prec, device=dev, neighbor_cap=1024)
-        g.set_state(st)
-        g.run_phase(5)
-        acc[prec] = g.particles(("a1", "a2"))
-        g.close()
+    o2 = oracle.Oracle(case)
+    n = len(gp["xyz"])
+    o2.set_state({"x": gp["xyz"][:, 0], "y": gp["xyz"][:, 1], "z": gp["xyz"][:, 2], "type": gp["type"],
+                  "h": gp["h"], "level": gp["level"], "phi": gp["phi"], "curv": gp["curv"],
+                  "nx": gp["norm"][:, 0], "ny": gp["norm"][:, 1], "nz": gp["norm"][:, 2], "rho": gp["rho"],
+                  "nu": st20["nu"], "id": np.arange(n, dtype=np.int32), "step": st20["step"] + 1,
+                  "vol": 1.0 / gp["rho"],
+                  "scale": o2.ctx.max_scale * np.ldexp(1.0, -np.asarray(gp["level"], dtype=np.int64))})
+    ooff, onb = o2.neighbors()
+
     def rel(a, b):
         return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
-    force = {"stage1_max_rel": rel(acc["fp32"]["a1"], acc["fp64"]["a1"]),
-             "stage2_max_rel": rel(acc["fp32"]["a2"], acc["fp64"]["a2"]),
-             "normalisation": "max |a_fp32 - a_fp64| / max |a_fp64| over particles"}
-    stats = {}
-    for prec in ("fp64", "fp32"):
-        g = SPHMeshGeneration(case, precision=prec, device=dev)
-        g.Initialize_case()
-        g.SPH_run_mesh_generation(args.accuracy_steps)
-        p = g.particles(("xyz", "h", "type", "phi"))
-        g.close()
-        stats[prec] = spacing_stats(p["xyz"], p["h"], hdx, dim)
-        # surface deviation: |phi| of the SURFACE particles over their target spacing
-        surf = p["type"] == 1
-        dev_s = np.abs(p["phi"][surf]) / (p["h"][surf] / hdx) if surf.any() else np.zeros(1)
-        stats[prec].update({"surface_count": int(surf.sum()), "surface_dev_mean": float(dev_s.mean()),
-                            "surface_dev_max": float(dev_s.max())})
-    dif = {k: abs(stats["fp32"][k] - stats["fp64"][k]) / max(abs(stats["fp64"][k]), 1e-300)
+    o2.density(ooff, onb)
+    s0 = o2.get_state()
+    o2.force(ooff, onb, 1)
+    s1 = o2.get_state()
+    o2.force(ooff, onb, 2)
+    s2 = o2.get_state()
+    surf = gp["type"] == 1
+    force = {"cells_equal": bool(np.array_equal(lc, o2.cells())),
+             "neighbour_sets_equal": bool(np.array_equal(off, ooff) and np.array_equal(nb, onb)),
+             "sum_real_max_rel": rel(gp["sum"][~surf], s0["sum"][~surf]),
+             "sum_surface_max_rel": rel(gp["sum"][surf], s0["sum"][surf]) if surf.any() else None,
+             "stage1_max_rel": rel(gp["a1"], np.stack([s1["ax"], s1["ay"], s1["az"]], 1)),
+             "stage2_max_rel": rel(gp["a2"], np.stack([s2["ax"], s2["ay"], s2["az"]], 1)),
+             "surface_particles": int(surf.sum()),
+             "normalisation": "max |gpu - oracle| / max |oracle| over the particles"}
+    # relaxation statistics after accuracy_steps steps from the same seed state
+    g = SPHMeshGeneration(case, precision="fp32", device=dev, neighbor_cap=1024)
+    g.set_state(to_gpu(seed_st))
+    g.SPH_run_mesh_generation(args.accuracy_steps)
+    p = g.particles(("xyz", "h", "type", "phi"))
+    g.close()
+    os_ = orc.get_state()
+    stats = {"fp32": spacing_stats(p["xyz"], p["h"], hdx, dim, p["type"], p["phi"]),
+             "oracle": spacing_stats(np.stack([os_["x"], os_["y"], os_["z"]], 1), os_["h"], hdx, dim,
+                                     os_["type"], os_["phi"])}
+    dif = {k: abs(stats["fp32"][k] - stats["oracle"][k]) / max(abs(stats["oracle"][k]), 1e-300)
            for k in ("median", "p05", "p95", "min_distance", "surface_count", "surface_dev_mean")}
-    return {"workload": f"torus_3d_small (N={case.n_particles})", "reference": "fp64_plain GPU path",
-            "single_step_force": force, "steps": args.accuracy_steps,
+    dif["hist_l1_over_n"] = float(np.abs(np.array(stats["fp32"]["hist"]) -
+                                         np.array(stats["oracle"]["hist"])).sum() / n)
+    return {"workload": f"torus_3d dx 0.02-0.08 (N={case.n_particles})", "reference": "FP64 oracle",
+            "single_step": force, "single_step_state": "the oracle's state after 20 steps",
+            "steps": args.accuracy_steps, "oracle_seconds": oracle_s,
             "spacing_ratio": {"fp32": {k: v for k, v in stats["fp32"].items() if k != "hist"},
-                              "fp64": {k: v for k, v in stats["fp64"].items() if k != "hist"},
+                              "oracle": {k: v for k, v in stats["oracle"].items() if k != "hist"},
                               "hist_bins": "40 bins over [0, 2)", "hist_fp32": stats["fp32"]["hist"],
-                              "hist_fp64": stats["fp64"]["hist"]},
-            "fp32_vs_fp64_rel_diff": dif}
+                              "hist_oracle": stats["oracle"]["hist"]},
+            "fp32_vs_oracle_rel_diff": dif}
 
 
 def run_mrsph(args, ws, rank, local, dist):
@@ -372,11 +421,11 @@ def run_mrsph(args, ws, rank, local, dist):
     case = workload(args.workload, "fp32")
     n = case.n_particles
     dim = case.params["dim"]
+    warm = max(args.warmup, 3)
     gpu = SPHMeshGeneration(case, precision="fp32", device=dev)
     gpu.Initialize_case(n)
-    gpu.SPH_run_mesh_generation(max(args.warmup, 3))
+    gpu.SPH_run_mesh_generation(warm)
     gpu.sync()
-    prof = gpu.profile_steps(3)
     st0 = gpu.stats()
     gpu.sync()
     barrier(dist)
@@ -386,6 +435,8 @@ def run_mrsph(args, ws, rank, local, dist):
     barrier(dist)
     ms = max_over_ranks(ms, dist)
     st1 = gpu.stats()
+    window = f"steps {warm + 1}..{warm + args.steps} after seeding"
+    prof = gpu.profile_steps(3)  # per-phase device times of the three steps after the window
     pairs = st1["pairs_total"] - st0["pairs_total"]
     value = ws * n * args.steps / (ms / 1000.0)
     pair_rate = ws * 3.0 * pairs / (ms / 1000.0)
@@ -470,7 +521,7 @@ def run_mrsph(args, ws, rank, local, dist):
         pinned = False
     g2 = SPHMeshGeneration(case, precision="fp32", device=dev)
     g2.Initialize_case(n)
-    g2.SPH_run_mesh_generation(max(args.warmup, 3) + 3)
+    g2.SPH_run_mesh_generation(warm)
     g2.download_positions(host_in)
     g2.sync()
     barrier(dist)
@@ -531,7 +582,8 @@ def run_mrsph(args, ws, rank, local, dist):
                      "levelset_build_s": r["levelset_s"]}
         vm["speedup_vs_cpu"] = r["seconds"] / (vm["device_ms"] / 1000.0)
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "window": window, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(case, args.workload),
             "pair_interactions_per_s": pair_rate, "pairs_per_particle": pairs / (n * args.steps),
             "fp64_plain": fp64,

@@ -4,9 +4,14 @@ TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py (CPU
 baseline and reference arms) use this module as the checker.  The product
 library never imports it.
 
-Parity status: unpinned against the reference binary (the reference needs TBB,
-Boost.MPI and voro++ and ships no tests or golden vectors); pinned to analytic
-known-answer tests instead.
+Parity status: partly pinned to the reference's own code.  The reference as a
+program does not build here (it needs TBB, Boost.MPI and voro++) and ships no
+tests or golden vectors; its smoothing kernels, their gradients and the level
+law (base_cls_particle/particle.cpp) and its marching-cubes polygoniser
+(geometry_tools/polygonise.cpp) are compiled from its sources into checker
+libraries (build_ref.py) and the oracle's functions are checked against them
+bit for bit (tests/test_ref_pinned.py, tests/golden/).  The rest is pinned by
+known-answer tests derived from the equations (tests/test_oracle_kat.py).
 """
 from __future__ import annotations
 
@@ -19,18 +24,36 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "mrsph_oracle.cpp")
 LIB = os.path.join(HERE, "_build", "libmrsph_oracle.so")
+LIB_TUNED = os.path.join(HERE, "_build", "libmrsph_oracle_native.so")
 
 
-def build(force: bool = False) -> str:
-    """Compile the oracle with g++ (OpenMP, no fused multiply-add)."""
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
-        return LIB
-    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           SRC, "-o", LIB + ".tmp"]
+def tuning_flags() -> list:
+    """Host-CPU tuning of the timed CPU baseline build: -mcpu=native on Arm,
+    -march=native elsewhere.  Results do not change: -ffp-contract=off (no
+    fused multiply-add) and no fast-math hold for both builds."""
+    import platform
+    return ["-mcpu=native"] if platform.machine().lower() in ("aarch64", "arm64") else ["-march=native"]
+
+
+def tuned() -> bool:
+    """The natively tuned library is loaded when MRSPH_ORACLE_TUNED=1 (the
+    benchmark's CPU legs set it before the first use of this module)."""
+    return os.environ.get("MRSPH_ORACLE_TUNED") == "1"
+
+
+def build(force: bool = False, native: bool = None) -> str:
+    """Compile the oracle with g++ (OpenMP, no fused multiply-add); native
+    adds the host-CPU tuning flags (default: tuned())."""
+    native = tuned() if native is None else native
+    out = LIB_TUNED if native else LIB
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
+        return out
+    cmd = ["g++", "-O3", *(tuning_flags() if native else []), "-std=c++17", "-fopenmp", "-ffp-contract=off",
+           "-fPIC", "-shared", SRC, "-o", out + ".tmp"]
     subprocess.check_call(cmd)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(out + ".tmp", out)
+    return out
 
 
 class OrcLevel(C.Structure):
@@ -90,8 +113,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        build()
-        L = C.CDLL(LIB)
+        L = C.CDLL(build())
         L.orc_define_levels.argtypes = [C.POINTER(OrcCtx)]
         L.orc_ls_build.argtypes = [C.POINTER(OrcCtx), C.c_int, C.POINTER(C.c_double)]
         L.orc_kernel_W.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_void_p, C.c_double, C.c_void_p]
