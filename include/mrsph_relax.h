@@ -206,9 +206,12 @@ int mrsph_sample_levelset(mrsph_handle* h, long long n, const double* xyz, doubl
  * latency-critical path): points and results are staged through a fixed
  * scratch array that is part of the library image (held on every GPU that
  * loads the library until exit).  At most 65536 points per call, else
- * MRSPH_ERR_RANGE.  The first call on a device looks up the scratch address;
- * make that first call before any stream capture.  All calls on a device
- * share the scratch: calls that overlap on the GPU race. */
+ * MRSPH_ERR_RANGE.  The first call on a device looks up the scratch address
+ * and keeps it for the life of the process; make that first call before any
+ * stream capture, and do not reset the device (cudaDeviceReset) while the
+ * library is loaded.  Every call is synchronous: it returns with the results
+ * in the caller's arrays.  All calls on a device share the scratch: calls that
+ * overlap on the GPU race. */
 int mrsph_sample_levelset_noalloc(mrsph_handle* h, long long n, const double* xyz, double* phi, double* norm,
                                   double* curv, int* tag);
 

@@ -76,7 +76,46 @@ struct Work {  // per-step arrays in sorted order
   int* perm2;
   int* blocksums;
   int* slot_of_id;
+  int* fixq;    // FP32-split: particles whose density phase is re-decided exactly (count sc->nfix)
+  int* spillq;  // particles whose list spilled (count sc->nspill)
 };
+
+// Neighbour-list entries: the neighbour's storage slot in the low 30 bits;
+// bits 30-31 carry the surface filter |n_i . n_j| > cos(angle_thres) where
+// the FP32-split density fix-up decided it in FP64 (0: decide in FP32).
+constexpr int NB_IDX = 0x3FFFFFFF;
+constexpr unsigned NB_COS_OK = 1u, NB_COS_NO = 2u;
+__host__ __device__ inline int nb_index(int e) { return e & NB_IDX; }
+__host__ __device__ inline unsigned nb_mark(int e) { return (unsigned)e >> 30; }
+
+// FP32-split decisions.  Three decisions of a step must come out as the
+// reference's FP64 arithmetic on the world positions makes them: the cell of
+// a particle (get_cell_id, glbfunc.h:196-208), the neighbour criterion
+// r <= h cutoff + 1e-10 for h_i or h_j (level_infor.cpp:491-500) and the
+// surface filter |n_i . n_j| > cos(angle_thres) (particle_mesh_generation.cpp:
+// 719, 747, 937).  Each is made in FP32 with a band around its threshold that
+// is wider than the FP32 error, and inside the band in FP64 with the
+// reference's operation order on the world coordinates the position taps
+// report.  Bands: the half-cell coordinate of the sort key, 2^-16 of a half
+// cell; the squared distance, 2^-15 of the squared cut-off radius (the
+// +1e-10 moves the radius by at most 2^-18.9 for radii of at least 1e-4,
+// which mrsph_create enforces for FP32-split handles); the cosine, 2^-16.
+constexpr float kBandKey = 1.0f / 65536.0f;
+constexpr float kD2Accept = 1.0f + 1.0f / 32768.0f;  // FP32 d2 above R^2 * this: certainly not a neighbour
+constexpr float kD2Sure = 1.0f - 1.0f / 32768.0f;    // FP32 d2 below R^2 * this: certainly a neighbour
+constexpr float kBandCos = 1.0f / 65536.0f;
+
+// Warp-aggregated append of val to queue q (counter *cnt); every lane of the
+// warp calls it.
+__device__ inline void queue_push(bool pred, unsigned* cnt, int* q, int val) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(cnt, (unsigned)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
 
 struct KCtx {
   Params prm;
@@ -170,12 +209,17 @@ struct PosOps<D, float> {
     if (D == 2) return (int)((unsigned)k[0] | ((unsigned)k[1] << 16));
     return (int)((unsigned)k[0] | ((unsigned)k[1] << 11) | ((unsigned)k[2] << 22));
   }
+  // world coordinate box_l + (k A + o): one fused multiply-add and one add,
+  // both explicit, so every kernel (and the position taps) gets the same bits
+  __device__ static double world1(const KCtx& c, int d, int k, float o) {
+    return __dadd_rn(c.geo.box_l[d], __fma_rn((double)k, c.geo.A[d], (double)o));
+  }
   __device__ static void world(const KCtx& c, const T4& p, int key, double* x) {
     int k[3];
     unpack(key, k);
     float o[3] = {p.x, p.y, p.z};
     x[2] = 0.0;
-    for (int d = 0; d < D; d++) x[d] = c.geo.box_l[d] + ((double)k[d] * c.geo.A[d] + (double)o[d]);
+    for (int d = 0; d < D; d++) x[d] = world1(c, d, k[d], o[d]);
   }
   __device__ static void set_world(const KCtx& c, T4& p, int& key, const double* x) {
     int k[3] = {0, 0, 0};
@@ -286,6 +330,8 @@ static __global__ void k_begin_step(DevScalars* sc, int inc) {
   sc->remap = 0;
   sc->nsurf = 0;
   sc->maxcnt = 0;
+  sc->nfix = 0;
+  sc->nspill = 0;
   for (int l = 0; l < MAX_CL; l++) {
     sc->hmax[l] = 0;
     sc->lcount[l] = 0;
@@ -485,11 +531,26 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
       P::unpack(key, k);
       const float o[3] = {p.x, p.y, p.z};
       const int sh = c.geo.ncl - 1 - L;
+      bool near_edge = false;
       for (int d = 0; d < D; d++) {
         const int cc = k[d] >> sh;
         const float pos = fmaf((float)(k[d] - (cc << sh)), c.geo.Af[d], o[d]);
-        const int hl = (int)floorf(pos * c.geo.ihs_f[L][d]);
-        hq[d] = max(0, min(2 * cc + hl, c.geo.hn[L][d] - 1));
+        const float u = pos * c.geo.ihs_f[L][d];
+        const float fl = floorf(u);
+        const float fr = u - fl;
+        near_edge = near_edge || fr < kBandKey || fr > 1.f - kBandKey;
+        hq[d] = max(0, min(2 * cc + (int)fl, c.geo.hn[L][d] - 1));
+      }
+      if (near_edge) {
+        // within the band of a half-cell face: the reference's FP64 binning,
+        // floor((x - box_l) / dcell), of the world position.  Half cells are
+        // dcell / 2 exactly, so floor((x - box_l) / (dcell / 2)) >> 1 is that
+        // cell.
+        for (int d = 0; d < D; d++) {
+          const double rel = __dsub_rn(P::world1(c, d, k[d], o[d]), c.geo.box_l[d]);
+          const double u = floor(__ddiv_rn(rel, c.geo.hs[L][d]));
+          hq[d] = (int)fmax(0.0, fmin(u, (double)(c.geo.hn[L][d] - 1)));
+        }
       }
       for (int d = D - 1; d >= 0; d--) c0 = c0 * c.geo.n[0][d] + (k[d] >> (c.geo.ncl - 1));
     } else {
@@ -568,6 +629,38 @@ struct RecOps<D, float> {
   }
 };
 
+// The reference's neighbour criterion in FP64 for two FP32-split records
+// (w0 = offset, h; w1 = anchor index): world coordinates as the position taps
+// compute them, dr = x_i - x_j, dist = sqrt(dr.dr) summed in axis order, and
+// dist <= h cutoff + 1e-10 for h_i or h_j (level_infor.cpp:491-500).
+template <int D>
+__device__ __noinline__ bool exact_neighbor(const KCtx& c, const float4& a0, const float4& a1, const float4& b0,
+                                            const float4& b1) {
+  const float ao[3] = {a0.x, a0.y, a0.z}, bo[3] = {b0.x, b0.y, b0.z};
+  const float ak[3] = {a1.x, a1.y, a1.z}, bk[3] = {b1.x, b1.y, b1.z};
+  double d2 = 0.0;
+  for (int d = 0; d < D; d++) {
+    const double xi = PosOps<D, float>::world1(c, d, (int)ak[d], ao[d]);
+    const double xj = PosOps<D, float>::world1(c, d, (int)bk[d], bo[d]);
+    const double dr = __dsub_rn(xi, xj);
+    d2 = (d == 0) ? __dmul_rn(dr, dr) : __dadd_rn(d2, __dmul_rn(dr, dr));
+  }
+  const double dist = __dsqrt_rn(d2);
+  const double ri = __dadd_rn(__dmul_rn((double)a0.w, c.prm.cutoff), 1.e-10);
+  const double rj = __dadd_rn(__dmul_rn((double)b0.w, c.prm.cutoff), 1.e-10);
+  return (dist <= ri) || (dist <= rj);
+}
+
+// The surface filter |n_i . n_j| > cos(angle_thres) in FP64, products summed
+// in axis order (particle_mesh_generation.cpp:719, 747, 937).
+template <int D>
+__device__ __noinline__ bool exact_cos(const KCtx& c, const float* ni, const float* nj) {
+  double ca = __dmul_rn((double)ni[0], (double)nj[0]);
+  ca = __dadd_rn(ca, __dmul_rn((double)ni[1], (double)nj[1]));
+  if (D == 3) ca = __dadd_rn(ca, __dmul_rn((double)ni[2], (double)nj[2]));
+  return fabs(ca) > c.prm.cos_thres;
+}
+
 template <int D, class R>
 __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict__ perm2,
                           int* __restrict__ slot_of_id, long long n, int partial) {
@@ -630,8 +723,8 @@ template <int D> struct SOrigin<D, float> {
 };
 
 // Level L of the candidate search from origin so with smoothing length hi:
-// R_L = cutoff * max(hi, local h maximum of level L) + 1e-10 with a 1e-5
-// relative pad (0 when no level-L particle can pair with the origin), and the
+// R_L = cutoff * max(hi, local h maximum of level L) + 1e-10 with a relative
+// pad (1e-5 FP64, 3e-5 FP32-split; 0 when no level-L particle can pair with the origin), and the
 // origin's half-cell coordinate q + fr on level L.  The local h maximum is
 // the largest lhmax entry over the level-0 cells overlapping the cube of the
 // level-wide bound (every level-L particle that can pair with the origin lies
@@ -670,7 +763,7 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
                                      const SOrigin<D, float>& so, float hi, bool active, int* q, float* fr) {
   const float cut = c.prm.cutoff_f;
   const float hic = hi * cut;
-  const float Rg = (fmaxf(hic, (float)bitsd(c.sc->hmax[L]) * cut) + 1.e-10f) * (1.f + 1.e-5f);
+  const float Rg = (fmaxf(hic, (float)bitsd(c.sc->hmax[L]) * cut) + 1.e-10f) * (1.f + 3.e-5f);
   float hloc = 0.f;
   if (active) {
     const int sh0 = c.geo.ncl - 1;
@@ -695,7 +788,7 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
     q[d] = 2 * cc + (int)fl;
     fr[d] = u - fl;
   }
-  return (fmaxf(hic, hloc * cut) + 1.e-10f) * (1.f + 1.e-5f);
+  return (fmaxf(hic, hloc * cut) + 1.e-10f) * (1.f + 3.e-5f);
 }
 
 // Candidates of particle i over all cell-list levels.  The reference walks
@@ -708,8 +801,10 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
 // (z, y) row of half cells is one contiguous range of the sorted arrays; rows
 // farther than R_L are skipped and the x range of each row is cut to the
 // sphere.  Edge rows extend to infinity (keys are clamped into the table).
-// R_L carries a 1e-5 relative pad for the rounding of the keys and of the
-// FP32 row arithmetic; the candidate test itself decides membership.
+// R_L carries a relative pad for the rounding of the keys and of the row
+// arithmetic (FP64: 1e-5; FP32-split: 3e-5, which also covers the FP32
+// test's acceptance band of 2^-15 on R^2, so the per-lane and the warp-tile
+// scans accept the same candidates); the candidate test decides membership.
 template <int D, class R, class F>
 __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart,
                                        const unsigned* __restrict__ lhmax, const SOrigin<D, R>& so, R hi, F&& f) {
@@ -873,12 +968,10 @@ __device__ inline bool nb_test(double d2, double hi, double hj, double cutoff, d
   dist = sqrt(d2);
   return (dist <= (hi * cutoff + 1.e-10)) || (dist <= (hj * cutoff + 1.e-10));
 }
-__device__ inline bool nb_test(float d2, float hi, float hj, double cutoff, float& dist) {
-  float R = fmaxf(hi, hj) * (float)cutoff;
-  if (d2 > R * R) return false;
-  dist = pair_dist(d2);
-  return true;
-}
+
+// pair distance of the force passes: IEEE square root in FP32 (see wendland_aw)
+__device__ inline double force_dist(double d2) { return sqrt(d2); }
+__device__ inline float force_dist(float d2) { return sqrtf(d2); }
 
 template <class R> __device__ inline R d2_of(const R* dr, int D) {
   R d2 = 0;
@@ -931,6 +1024,8 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   const R cut = pick<R>(c.prm.cutoff, c.prm.cutoff_f);
   R sum = 0;
   int ncount = 0, cnt = 0;
+  bool unc = false;  // FP32-split: a decision of this particle lies in its band (exact re-decision follows)
+  const R R2i = (hi * cut) * (hi * cut);
   int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[(q >> 3) * 256 + (q & 7)]
   int o = 0;  // offset of entry cnt
   // accepted neighbour j at distance vector dr (i - j), |dr| = dist
@@ -953,7 +1048,9 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       R pd = pair_dist(dot3<D, R>(pr, pr));
       const T4 nrj = b.nr[j];
       const R nj[3] = {nrj.x, nrj.y, nrj.z};
-      if (r_fabs(dot3<D, R>(ni, nj)) > cos_t) {
+      const R ca = r_fabs(dot3<D, R>(ni, nj));
+      if (F32 && fabsf((float)ca - (float)cos_t) <= kBandCos) unc = true;
+      if (ca > cos_t) {
         sum += pair_W(kind, D - 1, pd, hi, inv_hi);
         ncount++;
       }
@@ -964,9 +1061,18 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
     ld_rec(b.rec, j, b0, b1);
     R dr[3];
     Q::rel(c, a0, a1, b0, b1, dr);
-    R dist;
-    if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
-    accept(j, dr, dist, b1.w < (R)0);
+    if constexpr (F32) {
+      const float d2 = d2_of(dr, D);
+      const float rj = b0.w * cut;
+      const float Rm = fmaxf(R2i, rj * rj);
+      if (d2 > Rm * kD2Accept) return;
+      if (d2 >= Rm * kD2Sure) unc = true;
+      accept(j, dr, pair_dist(d2), b1.w < 0.f);
+    } else {
+      R dist;
+      if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
+      accept(j, dr, dist, b1.w < (R)0);
+    }
   };
   if constexpr (F32) {
     // warp anchor: lane 0's anchor cell (lane 0 is active whenever any lane is)
@@ -975,8 +1081,6 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
     const float Af[3] = {c.geo.Af[0], c.geo.Af[1], c.geo.Af[2]};
     const float pi[3] = {((float)a1.x - wa[0]) * Af[0] + (float)a0.x, ((float)a1.y - wa[1]) * Af[1] + (float)a0.y,
                          D == 3 ? ((float)a1.z - wa[2]) * Af[2] + (float)a0.z : 0.f};
-    const float ri = (float)hi * (float)cut;
-    const float R2i = ri * ri;
     auto load = [&](int k) {
       float4 b0, b1;
       ld_rec(b.rec, k, b0, b1);
@@ -988,7 +1092,9 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
     auto vtile = [&](int j, const float4& e) {
       float dr[3] = {pi[0] - e.x, pi[1] - e.y, D == 3 ? pi[2] - e.z : 0.f};
       const float d2 = d2_of(dr, D);
-      if (d2 > fmaxf(R2i, fabsf(e.w))) return;
+      const float Rm = fmaxf((float)R2i, fabsf(e.w));
+      if (d2 > Rm * kD2Accept) return;
+      if (d2 >= Rm * kD2Sure) unc = true;
       accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
     };
     warp_scan<D, R>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
@@ -1018,10 +1124,102 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
     if (cnt > w.cap) atomicOr(&c.sc->flags, (unsigned)FLAG_SPILL);
     pairs = (unsigned long long)(cnt - 1);
   }
+  queue_push(active && cnt > w.cap, &c.sc->nspill, w.spillq, (int)i);
+  if (F32) queue_push(active && unc, &c.sc->nfix, w.fixq, (int)i);
   unsigned mc = (unsigned)(pairs + 1);
   for (int o = 16; o > 0; o >>= 1) mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
   if ((threadIdx.x & 31) == 0 && mc > 1) atomicMax(&c.sc->maxcnt, mc);
   block_sum_u64_to_global(pairs, &c.sc->pairs);
+}
+
+// FP32-split density fix-up, one thread per queued particle (grid-stride):
+// every pair of the particle is decided again (FP32 outside the bands, FP64
+// inside), its list is compacted to the accepted pairs in scan order, surface
+// filter decisions made in FP64 are marked on their entries (the force passes
+// read the marks), and its kernel sum, count and share of the step's pair
+// total are redone.  A particle whose list spilled re-scans its cells.
+template <int D, int KK>
+__global__ void __launch_bounds__(256) k_density_fix(KCtx c, Buf<float> b, Work<float> w) {
+  using Q = RecOps<D, float>;
+  constexpr bool WEN = KK == K_WEN;
+  const unsigned nq = c.sc->nfix;
+  const int kind = KK >= 0 ? KK : c.prm.kernel;
+  const float cut = c.prm.cutoff_f, cos_t = c.prm.cos_thres_f;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nq; t += gridDim.x * blockDim.x) {
+    const int i = w.fixq[t];
+    const float4 a0 = b.rec[2 * i], a1 = b.rec[2 * i + 1];
+    const int ti = b.meta[i] & 0xFF;
+    float ni[3] = {0.f, 0.f, 0.f};
+    if (ti == SURFACE_P) {
+      const float4 q = b.nr[i];
+      ni[0] = q.x; ni[1] = q.y; ni[2] = q.z;
+    }
+    const float hi = a0.w, inv_hi = r_rcp(hi);
+    const float R2i = (hi * cut) * (hi * cut);
+    float sum = 0.f;
+    int ncount = 0, cnt = 0;
+    const int old = w.cnt[i];
+    int* row = w.nbl + nb_slot(i, 0, w.cap);
+    auto visit = [&](int j) {
+      float4 b0, b1;
+      ld_rec(b.rec, j, b0, b1);
+      float dr[3];
+      Q::rel(c, a0, a1, b0, b1, dr);
+      const float d2 = d2_of(dr, D);
+      const float rj = b0.w * cut;
+      const float Rm = fmaxf(R2i, rj * rj);
+      if (d2 > Rm * kD2Accept) return;
+      if (d2 >= Rm * kD2Sure && !exact_neighbor<D>(c, a0, a1, b0, b1)) return;
+      int e = j;
+      const float dist = pair_dist(d2);
+      if (ti == REAL_P) {
+        if (WEN) {
+          const float s = dist * inv_hi;
+          const float tt = fmaxf(fmaf(-0.5f, s, 1.f), 0.f), t2 = tt * tt;
+          sum += (t2 * t2) * fmaf(2.f, s, 1.f);
+        } else {
+          sum += pair_W(kind, D, dist, hi, inv_hi);
+          ncount++;
+        }
+      } else if (ti == SURFACE_P && b1.w < 0.f) {
+        const float dn = dot3<D, float>(dr, ni);
+        float pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
+        const float pd = pair_dist(dot3<D, float>(pr, pr));
+        const float4 q = b.nr[j];
+        const float nj[3] = {q.x, q.y, q.z};
+        const float ca = fabsf(dot3<D, float>(ni, nj));
+        bool ok;
+        if (fabsf(ca - cos_t) <= kBandCos) {
+          ok = exact_cos<D>(c, ni, nj);
+          e |= (int)((ok ? NB_COS_OK : NB_COS_NO) << 30);
+        } else {
+          ok = ca > cos_t;
+        }
+        if (ok) {
+          sum += pair_W(kind, D - 1, pd, hi, inv_hi);
+          ncount++;
+        }
+      }
+      if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = e;
+      cnt++;
+    };
+    if (old <= w.cap) {
+      // the list holds every candidate the FP32 test did not certainly
+      // reject; compaction writes entry cnt <= q after reading entry q
+      for (int q = 0; q < old; q++) visit(nb_index(row[((q >> 3) << 8) + (q & 7)]));
+    } else {
+      const SOrigin<D, float> so(c, b.posh[i], b.key[i]);
+      scan_candidates<D, float>(c, w.cstart, w.lhmax, so, hi, visit);
+    }
+    if (WEN && ti == REAL_P) {
+      sum *= (float)kern_norm(K_WEN, D) * (D == 3 ? inv_hi * inv_hi * inv_hi : inv_hi * inv_hi);
+      ncount = cnt;
+    }
+    if (ncount > 1) sum = 1.f / (sum + 1.e-15f);
+    w.sum[i] = sum;
+    w.cnt[i] = cnt;
+    atomicAdd(&c.sc->pairs, (unsigned long long)(long long)(cnt - old));
+  }
 }
 
 static __global__ void k_accum_pairs(DevScalars* sc) { sc->pairs_total += sc->pairs; }
@@ -1055,188 +1253,270 @@ __device__ inline void load4(const double* p, double* v) {
 // reference's quirk), Derivative_kernel_function (particle.cpp:732-750):
 // -5 C (1 - s/2)^3 s / h / (r + 1e-15) with C = norm / h^DK and s = r / h,
 // which is -5 norm (1 - s/2)^3 / h^(DK+2) for r > 0 in FP32, and 0 at r = 0.
+// 1/h is rounded correctly (__frcp_rn): the hardware approximation's error
+// is a smooth function of h, so pairs of similar h_ij share it and a
+// near-balanced sum of hundreds of pair forces does not average it out (it
+// acts as a slightly different kernel); the force passes take the distance
+// from an IEEE square root for the same reason (force_dist).
 template <int DK>
 __device__ inline float wendland_aw(float dist, float h) {
   if (DK == 1) return 0.f;
-  const float ih = r_rcp(h);
+  const float ih = __frcp_rn(h);
   const float t = fmaxf(fmaf(-0.5f * ih, dist, 1.f), 0.f);
   float ihp = (ih * ih) * (ih * ih);
   if (DK == 3) ihp *= ih;
   return dist > 0.f ? (-5.f * (float)kern_norm(K_WEN, DK)) * ihp * (t * t * t) : 0.f;
 }
 
-// KK: the kernel kind fixed at compile time (FP32 Wendland C2), or -1
-template <int D, class R, int STAGE, int KK>
-__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE == 1 ? MRSPH_FORCE_MIN_BLOCKS : MRSPH_FORCE2_MIN_BLOCKS) : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
-  using P = PosOps<D, R>;
+// One particle of a force stage.  SPILL = false: the particle's list is
+// complete (cnt <= cap); SPILL = true: it spilled and re-scans its cells,
+// making the neighbour and surface-filter decisions as the density pass does
+// (FP32-split: exact inside the bands).  my_dt / my_v take the min / max.
+template <int D, class R, int STAGE, int KK, bool SPILL>
+__device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work<R>& w, long long i, double& my_dt,
+                                      double& my_v) {
   using Q = RecOps<D, R>;
-  constexpr bool WEN32 = std::is_same<R, float>::value && KK == K_WEN;
+  constexpr bool F32 = std::is_same<R, float>::value;
+  constexpr bool WEN32 = F32 && KK == K_WEN;
   using T4 = typename V4<R>::T;
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double my_dt = 1.e300, my_v = 0.0;
-  if (i < c.n) {
-    const T4 a0 = b.rec[2 * i], a1r = b.rec[2 * i + 1];
-    const int mi = b.meta[i];
-    const int ti = mi & 0xFF;
-    R ni[3] = {0, 0, 0};
-    if (ti == SURFACE_P) {
-      const T4 nri = b.nr[i];
-      ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
+  const T4 a0 = b.rec[2 * i], a1r = b.rec[2 * i + 1];
+  const int mi = b.meta[i];
+  const int ti = mi & 0xFF;
+  R ni[3] = {0, 0, 0};
+  if (ti == SURFACE_P) {
+    const T4 nri = b.nr[i];
+    ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
+  }
+  const R rho = b.nr[i].w, h = a0.w;
+  const R cos_t = pick<R>(c.prm.cos_thres, c.prm.cos_thres_f);
+  const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
+  R nu = 0, eta_i = 0;
+  R hdt1 = 0;
+  R vi[3] = {0, 0, 0};
+  if (STAGE == 2) {
+    hdt1 = (R)(0.5 * bitsd(c.sc->dt1));
+    T4 an = w.a1[i];
+    vi[0] = an.x * hdt1; vi[1] = an.y * hdt1; vi[2] = an.z * hdt1;
+    eta_i = r_fabs(an.w);
+  } else {
+    nu = b.nu[i];
+  }
+  // FP32-split accumulates a particle's pair forces in groups of four list
+  // entries (a candidate scan groups its accepted neighbours the same way)
+  // and adds each group's sum into F with compensated (Kahan) summation.  The
+  // list is in scan order (levels, then z, y rows), so a plain running sum
+  // first collects every same-signed term of one side and reaches about half
+  // of sum |terms| before the other side cancels it; rounding at that
+  // magnitude, not the terms, dominated the FP32 error.  FP64-plain sums
+  // plainly, in the reference's expression order.
+  R F[3] = {0, 0, 0}, Fb[3] = {0, 0, 0}, Fc[3] = {0, 0, 0};
+  auto accum = [&](int d, R v) {
+    if constexpr (F32) Fb[d] = Fb[d] + v;
+    else F[d] = F[d] + v;
+  };
+  auto flush = [&]() {
+    if constexpr (F32) {
+      for (int d = 0; d < D; d++) {
+        const float y = Fb[d] - Fc[d];
+        const float t = F[d] + y;
+        Fc[d] = (t - F[d]) - y;
+        F[d] = t;
+        Fb[d] = 0.f;
+      }
     }
-    const R rho = b.nr[i].w, h = a0.w;
-    const R cos_t = pick<R>(c.prm.cos_thres, c.prm.cos_thres_f);
-    const R sum = (STAGE == 1) ? w.sum[i] : (R)0;
-    R nu = 0, eta_i = 0;
-    R hdt1 = 0;
-    R vi[3] = {0, 0, 0};
-    if (STAGE == 2) {
-      hdt1 = (R)(0.5 * bitsd(c.sc->dt1));
-      T4 an = w.a1[i];
-      vi[0] = an.x * hdt1; vi[1] = an.y * hdt1; vi[2] = an.z * hdt1;
-      eta_i = r_fabs(an.w);
+  };
+  const R vol_i = (R)1.0 / (rho * rho);
+  // pair (i, j) at relative position vec: the skip rules of :1019-1031 and
+  // :904-920, the direction dr the force acts along and the coefficient.
+  // mark: the surface filter's FP64 decision from the density fix-up (0: none)
+  auto coef = [&](int j, const T4& b0, const T4& b1, const R* vec, R* dr, R& cij, unsigned mark) -> bool {
+    if (j == (int)i) return false;
+    const bool surf_j = b1.w < (R)0;
+    if (ti == SURFACE_P && !surf_j) return false;
+    R aw;
+    const R hij = (R)0.5 * (h + b0.w);
+    if (ti == REAL_P) {
+      dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
+      R dist = force_dist(dot3<D, R>(dr, dr));
+      if constexpr (WEN32) aw = wendland_aw<D>(dist, hij);
+      else aw = pair_dW(c.prm.kernel, D, dist, hij);
     } else {
-      nu = b.nu[i];
+      R dn = dot3<D, R>(vec, ni);
+      dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
+      R dist = force_dist(dot3<D, R>(dr, dr));
+      const T4 nrj = b.nr[j];
+      const R nj[3] = {nrj.x, nrj.y, nrj.z};
+      bool ok;
+      if (mark == NB_COS_OK) {
+        ok = true;
+      } else if (mark == NB_COS_NO) {
+        ok = false;
+      } else {
+        const R ca = r_fabs(dot3<D, R>(ni, nj));
+        ok = ca > cos_t;
+        if constexpr (F32 && SPILL) {
+          if (fabsf(ca - cos_t) <= kBandCos) ok = exact_cos<D>(c, (const float*)ni, (const float*)nj);
+        }
+      }
+      if (!ok) return false;
+      if constexpr (WEN32) aw = wendland_aw<D - 1>(dist, hij);
+      else aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
     }
-    R F[3] = {0, 0, 0};
-    const R vol_i = (R)1.0 / (rho * rho);
-    // pair (i, j) at relative position vec: the skip rules of :1019-1031 and
-    // :904-920, the direction dr the force acts along and the coefficient
-    auto coef = [&](int j, const T4& b0, const T4& b1, const R* vec, R* dr, R& cij) -> bool {
-      if (j == (int)i) return false;
-      const bool surf_j = b1.w < (R)0;
-      if (ti == SURFACE_P && !surf_j) return false;
-      R aw;
-      const R hij = (R)0.5 * (h + b0.w);
-      if (ti == REAL_P) {
-        dr[0] = vec[0]; dr[1] = vec[1]; dr[2] = vec[2];
-        R dist = pair_dist(dot3<D, R>(dr, dr));
-        if constexpr (WEN32) aw = wendland_aw<D>(dist, hij);
-        else aw = pair_dW(c.prm.kernel, D, dist, hij);
-      } else {
-        R dn = dot3<D, R>(vec, ni);
-        dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
-        R dist = pair_dist(dot3<D, R>(dr, dr));
-        const T4 nrj = b.nr[j];
-        const R nj[3] = {nrj.x, nrj.y, nrj.z};
-        if (r_fabs(dot3<D, R>(ni, nj)) <= cos_t) return false;
-        if constexpr (WEN32) aw = wendland_aw<D - 1>(dist, hij);
-        else aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
-      }
-      const R vol_ij = vol_i + r_fabs(b1.w);
-      if (STAGE == 1) {
-        const R P_ij = sum * vol_ij;
-        for (int d = 0; d < D; d++) F[d] = F[d] + (dr[d] * aw) * -P_ij;
-      }
-      cij = aw * vol_ij;
-      return true;
-    };
-    auto visc = [&](int j, R cij) {
-      const T4 anj = w.a1[j];
-      const bool surf_j = signbit(anj.w);
-      R vj[3];
-      if (ti == REAL_P && surf_j) {
-        vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
-      } else {
-        vj[0] = anj.x * hdt1; vj[1] = anj.y * hdt1; vj[2] = anj.z * hdt1;
-      }
-      const R eta_j = r_fabs(anj.w);
-      const R eta_ij = r_div((R)2. * eta_j * eta_i, eta_i + eta_j + (R)1.e-15);
-      const R temp0 = cij * eta_ij;
-      for (int d = 0; d < D; d++) F[d] = F[d] + (vi[d] - vj[d]) * temp0;
-    };
-    if (ti == REAL_P || ti == SURFACE_P) {
+    const R vol_ij = vol_i + r_fabs(b1.w);
+    if (STAGE == 1) {
+      const R P_ij = sum * vol_ij;
+      for (int d = 0; d < D; d++) accum(d, (dr[d] * aw) * -P_ij);
+    }
+    cij = aw * vol_ij;
+    return true;
+  };
+  auto visc = [&](int j, R cij) {
+    const T4 anj = w.a1[j];
+    const bool surf_j = signbit(anj.w);
+    R vj[3];
+    if (ti == REAL_P && surf_j) {
+      vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
+    } else {
+      vj[0] = anj.x * hdt1; vj[1] = anj.y * hdt1; vj[2] = anj.z * hdt1;
+    }
+    const R eta_j = r_fabs(anj.w);
+    const R eta_ij = r_div((R)2. * eta_j * eta_i, eta_i + eta_j + (R)1.e-15);
+    const R temp0 = cij * eta_ij;
+    for (int d = 0; d < D; d++) accum(d, (vi[d] - vj[d]) * temp0);
+  };
+  if (ti == REAL_P || ti == SURFACE_P) {
+    if constexpr (!SPILL) {
       const int cnt = w.cnt[i];
-      if (cnt <= w.cap) {
-        const long long base = nb_slot(i, 0, w.cap);
-        const int* row = w.nbl + base;
-        R* crow = w.pc + base;
-        if (MRSPH_FORCE_VEC == 4) {
-          // four entries per access: q0 is a multiple of 4, so row + o and
-          // crow + o are 16-byte aligned; entries past cnt inside the group
-          // lie within the particle's cap and are ignored (stage 1 stores 0)
-          for (int q0 = 0; q0 < cnt; q0 += 4) {
-            const int o = ((q0 >> 3) << 8) + (q0 & 7);
-            const int4 j4 = __ldg(reinterpret_cast<const int4*>(row + o));
-            const int jj[4] = {j4.x, j4.y, j4.z, j4.w};
-            R cc[4];
-            if (STAGE == 1) {
+      const long long base = nb_slot(i, 0, w.cap);
+      const int* row = w.nbl + base;
+      R* crow = w.pc + base;
+      if (MRSPH_FORCE_VEC == 4) {
+        // four entries per access: q0 is a multiple of 4, so row + o and
+        // crow + o are 16-byte aligned; entries past cnt inside the group
+        // lie within the particle's cap and are ignored (stage 1 stores 0)
+        for (int q0 = 0; q0 < cnt; q0 += 4) {
+          const int o = ((q0 >> 3) << 8) + (q0 & 7);
+          const int4 j4 = __ldg(reinterpret_cast<const int4*>(row + o));
+          const int jj[4] = {j4.x, j4.y, j4.z, j4.w};
+          R cc[4];
+          if (STAGE == 1) {
 #pragma unroll
-              for (int k = 0; k < 4; k++) {
-                cc[k] = 0;
-                if (q0 + k < cnt) {
-                  const int j = jj[k];
-                  T4 b0, b1;
-                  ld_rec(b.rec, j, b0, b1);
-                  R vec[3], dr[3];
-                  Q::rel(c, a0, a1r, b0, b1, vec);
-                  coef(j, b0, b1, vec, dr, cc[k]);
-                }
+            for (int k = 0; k < 4; k++) {
+              cc[k] = 0;
+              if (q0 + k < cnt) {
+                const int j = nb_index(jj[k]);
+                T4 b0, b1;
+                ld_rec(b.rec, j, b0, b1);
+                R vec[3], dr[3];
+                Q::rel(c, a0, a1r, b0, b1, vec);
+                coef(j, b0, b1, vec, dr, cc[k], nb_mark(jj[k]));
               }
-              store4(crow + o, cc);
-            } else {
-              load4(crow + o, cc);
+            }
+            store4(crow + o, cc);
+          } else {
+            load4(crow + o, cc);
 #pragma unroll
-              for (int k = 0; k < 4; k++)
-                if (q0 + k < cnt && cc[k] != (R)0) visc(jj[k], cc[k]);
-            }
+            for (int k = 0; k < 4; k++)
+              if (q0 + k < cnt && cc[k] != (R)0) visc(nb_index(jj[k]), cc[k]);
           }
-        } else {
-          for (int q = 0; q < cnt; q++) {
-            const int o = ((q >> 3) << 8) + (q & 7);
-            if (STAGE == 1) {
-              const int j = __ldg(&row[o]);
-              T4 b0, b1;
-              ld_rec(b.rec, j, b0, b1);
-              R vec[3], dr[3], cij = 0;
-              Q::rel(c, a0, a1r, b0, b1, vec);
-              coef(j, b0, b1, vec, dr, cij);
-              crow[o] = cij;
-            } else {
-              const R cij = __ldg(&crow[o]);
-              if (cij == (R)0) continue;
-              visc(__ldg(&row[o]), cij);
-            }
-          }
+          flush();
         }
       } else {
-        const SOrigin<D, R> so(c, b.posh[i], b.key ? b.key[i] : 0);
-        scan_candidates<D, R>(c, w.cstart, w.lhmax, so, h, [&](int j) {
-          T4 b0, b1;
-          ld_rec(b.rec, j, b0, b1);
-          R vec[3], dr[3], cij = 0;
-          Q::rel(c, a0, a1r, b0, b1, vec);
+        for (int q = 0; q < cnt; q++) {
+          const int o = ((q >> 3) << 8) + (q & 7);
+          if (STAGE == 1) {
+            const int e = __ldg(&row[o]);
+            const int j = nb_index(e);
+            T4 b0, b1;
+            ld_rec(b.rec, j, b0, b1);
+            R vec[3], dr[3], cij = 0;
+            Q::rel(c, a0, a1r, b0, b1, vec);
+            coef(j, b0, b1, vec, dr, cij, nb_mark(e));
+            crow[o] = cij;
+          } else {
+            const R cij = __ldg(&crow[o]);
+            if (cij != (R)0) visc(nb_index(__ldg(&row[o])), cij);
+          }
+          if ((q & 3) == 3 || q == cnt - 1) flush();
+        }
+      }
+    } else {
+      const R cut = pick<R>(c.prm.cutoff, c.prm.cutoff_f);
+      const R R2i = (h * cut) * (h * cut);
+      const SOrigin<D, R> so(c, b.posh[i], b.key ? b.key[i] : 0);
+      int q = 0;  // accepted neighbours so far (the list entries this scan replaces)
+      scan_candidates<D, R>(c, w.cstart, w.lhmax, so, h, [&](int j) {
+        T4 b0, b1;
+        ld_rec(b.rec, j, b0, b1);
+        R vec[3], dr[3], cij = 0;
+        Q::rel(c, a0, a1r, b0, b1, vec);
+        if constexpr (F32) {
+          const float d2 = d2_of(vec, D);
+          const float rj = b0.w * cut;
+          const float Rm = fmaxf(R2i, rj * rj);
+          if (d2 > Rm * kD2Accept) return;
+          if (d2 >= Rm * kD2Sure && !exact_neighbor<D>(c, a0, a1r, b0, b1)) return;
+        } else {
           R dist;
           if (!nb_test(d2_of(vec, D), h, b0.w, c.prm.cutoff, dist)) return;
-          if (coef(j, b0, b1, vec, dr, cij) && STAGE == 2 && cij != (R)0) visc(j, cij);
-        });
-      }
+        }
+        if (coef(j, b0, b1, vec, dr, cij, 0u) && STAGE == 2 && cij != (R)0) visc(j, cij);
+        if ((q & 3) == 3) flush();
+        q++;
+      });
+      if (q & 3) flush();
     }
-    R a[3] = {0, 0, 0};
-    if (ti == REAL_P || ti == SURFACE_P) {
-      for (int d = 0; d < D; d++) a[d] = F[d];
-      if (STAGE == 2)
-        for (int d = 0; d < D; d++) a[d] = a[d] + vi[d] * pick<R>(c.prm.damp_coeff, c.prm.damp_coeff_f);
-      if (ti == SURFACE_P) {  // Map_surface_particle_force, :1122-1126
-        R nf = dot3<D, R>(a, ni);
-        for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
-      }
+  }
+  R a[3] = {0, 0, 0};
+  if (ti == REAL_P || ti == SURFACE_P) {
+    if constexpr (F32)
+      for (int d = 0; d < D; d++) F[d] = F[d] - Fc[d];
+    for (int d = 0; d < D; d++) a[d] = F[d];
+    if (STAGE == 2)
+      for (int d = 0; d < D; d++) a[d] = a[d] + vi[d] * pick<R>(c.prm.damp_coeff, c.prm.damp_coeff_f);
+    if (ti == SURFACE_P) {  // Map_surface_particle_force, :1122-1126
+      R nf = dot3<D, R>(a, ni);
+      for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
     }
-    R U = r_sqrt(dot3<D, R>(vi, vi));
-    R A = r_sqrt(dot3<D, R>(a, a));
-    R ts = (R)0.25 * r_sqrt(h / (A + (R)1.e-15));
-    ts = AMIN1(ts, h / (R)40. / (U + (R)1.e-15));
-    if (STAGE == 2) {
-      R nu_new = pick<R>(c.prm.nu_coeff, c.prm.nu_coeff_f) * h * U;
-      ts = AMIN1(ts, (R)0.125 * h * h / (nu_new + (R)1.e-15));
-      b.nu_next[i] = nu_new;
-      b.v1[i] = mk4<R>(vi[0], vi[1], vi[2], U);
-      b.a2[i] = mk4<R>(a[0], a[1], a[2], 0);
-    } else {
-      const R eta = nu * rho;
-      w.a1[i] = mk4<R>(a[0], a[1], a[2], ti == SURFACE_P ? -eta : eta);
-    }
-    my_dt = (double)ts;
-    my_v = (double)U;
+  }
+  R U = r_sqrt(dot3<D, R>(vi, vi));
+  R A = r_sqrt(dot3<D, R>(a, a));
+  R ts = (R)0.25 * r_sqrt(h / (A + (R)1.e-15));
+  ts = AMIN1(ts, h / (R)40. / (U + (R)1.e-15));
+  if (STAGE == 2) {
+    R nu_new = pick<R>(c.prm.nu_coeff, c.prm.nu_coeff_f) * h * U;
+    ts = AMIN1(ts, (R)0.125 * h * h / (nu_new + (R)1.e-15));
+    b.nu_next[i] = nu_new;
+    b.v1[i] = mk4<R>(vi[0], vi[1], vi[2], U);
+    b.a2[i] = mk4<R>(a[0], a[1], a[2], 0);
+  } else {
+    const R eta = nu * rho;
+    w.a1[i] = mk4<R>(a[0], a[1], a[2], ti == SURFACE_P ? -eta : eta);
+  }
+  my_dt = fmin(my_dt, (double)ts);
+  my_v = fmax(my_v, (double)U);
+}
+
+// KK: the kernel kind fixed at compile time (FP32 Wendland C2), or -1.
+// Particles whose list spilled are left to k_force_spill.
+template <int D, class R, int STAGE, int KK>
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE == 1 ? MRSPH_FORCE_MIN_BLOCKS : MRSPH_FORCE2_MIN_BLOCKS) : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double my_dt = 1.e300, my_v = 0.0;
+  if (i < c.n && w.cnt[i] <= w.cap) force_particle<D, R, STAGE, KK, false>(c, b, w, i, my_dt, my_v);
+  if (STAGE == 1) block_minmax_to_global(my_dt, my_v, &c.sc->dt1, &c.sc->vmax1);
+  else block_minmax_to_global(my_dt, my_v, &c.sc->dt2, &c.sc->vmax2);
+}
+
+// The force stage of the particles whose list spilled (queued by the density
+// pass; grid-stride), re-scanning their cells.
+template <int D, class R, int STAGE, int KK>
+__global__ void __launch_bounds__(256) k_force_spill(KCtx c, Buf<R> b, Work<R> w) {
+  double my_dt = 1.e300, my_v = 0.0;
+  const unsigned nq = c.sc->nspill;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nq; t += gridDim.x * blockDim.x) {
+    const int i = w.spillq[t];
+    if (w.cnt[i] > w.cap) force_particle<D, R, STAGE, KK, true>(c, b, w, i, my_dt, my_v);
   }
   if (STAGE == 1) block_minmax_to_global(my_dt, my_v, &c.sc->dt1, &c.sc->vmax1);
   else block_minmax_to_global(my_dt, my_v, &c.sc->dt2, &c.sc->vmax2);
@@ -1295,7 +1575,7 @@ __global__ void k_export_tri(KCtx c, Buf<R> b, Work<R> w, double* __restrict__ x
   const int* src = w.nbl + nb_slot(s, 0, w.cap);
   int* dst = rows + k * rowcap;
   for (int q = 0; q < m; q++) {  // insertion sort by id
-    int v = b.id[src[((q >> 3) << 8) + (q & 7)]];
+    int v = b.id[nb_index(src[((q >> 3) << 8) + (q & 7)])];
     int p = q;
     while (p > 0 && dst[p - 1] > v) { dst[p] = dst[p - 1]; p--; }
     dst[p] = v;
@@ -1404,6 +1684,10 @@ class Engine : public EngineBase {
     kc_.ls.min_curv_f = (float)kc_.ls.min_curv;
     kc_.geo.max_scale_f = (float)kc_.geo.max_scale;
     if (std::is_same<R, float>::value) init_rc_ = anchor_tables();
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    if (sms_ < 1) sms_ = 1;
   }
   ~Engine() override {
     release();
@@ -1653,7 +1937,7 @@ class Engine : public EngineBase {
     for (long long k = 0; k < n_; k++) off[k + 1] = off[k] + byid_cnt[k];
     for (long long s = 0; s < n_; s++) {
       long long base = off[ids[s]];
-      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nbl[nb_slot(s, q, w_.cap)]];
+      for (int q = 0; q < cnt[s]; q++) nb[base + q] = ids[nb_index(nbl[nb_slot(s, q, w_.cap)])];
       std::sort(nb + base, nb + base + cnt[s]);
     }
     return 0;
@@ -1729,6 +2013,9 @@ class Engine : public EngineBase {
   static unsigned long long dbits_host(double x) { unsigned long long u; std::memcpy(&u, &x, 8); return u; }
   static double bitsd_host(unsigned long long u) { double x; std::memcpy(&x, &u, 8); return x; }
   static int grid(long long n) { return (int)((n + 255) / 256); }
+  // grid of the queue kernels (density fix-up, spilled force stages): the
+  // queues' lengths are known on the device only; two blocks per SM at most
+  int qgrid() const { return std::max(1, std::min(grid(n_), 2 * sms_)); }
 
   int pre_run() {
     k_begin_step<<<1, 1, 0, st_>>>(kc_.sc, 0);
@@ -1793,24 +2080,35 @@ class Engine : public EngineBase {
     cur_ ^= 1;
     mark(4);
     if (phase < MRSPH_PHASE_DENSITY) return 0;
-    if (sizeof(R) == 4 && kc_.prm.kernel == K_WEN)
+    const bool wen32 = sizeof(R) == 4 && kc_.prm.kernel == K_WEN;
+    if (wen32)
       k_density<D, R, (sizeof(R) == 4 ? K_WEN : -1)><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
     else
       k_density<D, R, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    if constexpr (std::is_same<R, float>::value) {
+      if (wen32) k_density_fix<D, K_WEN><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+      else k_density_fix<D, -1><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    }
     k_accum_pairs<<<1, 1, 0, st_>>>(kc_.sc);
     have_work_ = true;
     mark(5);
     if (phase < MRSPH_PHASE_FORCE1) return 0;
-    if (sizeof(R) == 4 && kc_.prm.kernel == K_WEN)
+    if (wen32) {
       k_force<D, R, 1, (sizeof(R) == 4 ? K_WEN : -1)><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
-    else
+      k_force_spill<D, R, 1, (sizeof(R) == 4 ? K_WEN : -1)><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    } else {
       k_force<D, R, 1, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+      k_force_spill<D, R, 1, -1><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    }
     mark(6);
     if (phase < MRSPH_PHASE_FORCE2) return 0;
-    if (sizeof(R) == 4 && kc_.prm.kernel == K_WEN)
+    if (wen32) {
       k_force<D, R, 2, (sizeof(R) == 4 ? K_WEN : -1)><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
-    else
+      k_force_spill<D, R, 2, (sizeof(R) == 4 ? K_WEN : -1)><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    } else {
       k_force<D, R, 2, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+      k_force_spill<D, R, 2, -1><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+    }
     mark(7);
     MR_CK(cudaGetLastError());
     return 0;
@@ -1948,6 +2246,8 @@ class Engine : public EngineBase {
       rc |= A((void**)&w_.perm2, sizeof(int) * n);
       rc |= A((void**)&w_.blocksums, sizeof(int) * scan_blocksums_size(ncells_));
       rc |= A((void**)&w_.slot_of_id, sizeof(int) * n);
+      rc |= A((void**)&w_.fixq, sizeof(int) * n);
+      rc |= A((void**)&w_.spillq, sizeof(int) * n);
       rc |= A((void**)&stage_, sizeof(double) * 3 * n);
       rc |= A((void**)&kc_.sc, sizeof(DevScalars));
     }
@@ -1984,6 +2284,7 @@ class Engine : public EngineBase {
   std::vector<void*> allocs_;
   std::vector<void*> anc_allocs_;  // anchor tables, kept across re-allocations
   int init_rc_ = 0;
+  int sms_ = 1;  // multiprocessors of the engine's device
 };
 
 }  // namespace mrsph

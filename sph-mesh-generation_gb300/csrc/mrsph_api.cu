@@ -109,6 +109,10 @@ static int plan_levels(mrsph_handle* h) {
     g.Af[d] = (float)g.A[d];
   }
   if (p.precision == MRSPH_FP32_SPLIT) {
+    // the FP32 neighbour test's band covers the reference's +1e-10 on the
+    // cut-off radius (h cutoff = scale cell_ratio) only for radii >= 1e-4
+    if (p.min_dl * p.cell_ratio < 1.e-4)
+      return fail(h, MRSPH_ERR_RANGE, "FP32-split needs a smallest cut-off radius (min_dl * cell_ratio) of 1e-4");
     int lim[3] = {D == 2 ? 65536 : 2048, D == 2 ? 65536 : 2048, D == 2 ? 1 : 1024};
     for (int d = 0; d < D; d++)
       if (g.n[lm][d] > lim[d]) return fail(h, MRSPH_ERR_RANGE, "finest cell grid too large for the FP32-split key");

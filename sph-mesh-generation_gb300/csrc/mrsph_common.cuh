@@ -91,6 +91,8 @@ struct DevScalars {
   unsigned int remap, nsurf, flags, spill;
   unsigned int step;
   unsigned int maxcnt;  // largest neighbour count of the last density phase
+  unsigned int nfix;    // FP32-split: particles queued for the exact re-decision of the density phase
+  unsigned int nspill;  // particles whose neighbour list spilled (re-scanned by the force fix-up launches)
   unsigned long long hmax[MAX_CL];  // FP64 bits of the largest h per level (this step)
   unsigned int lcount[MAX_CL];      // particles per level (this step)
 };
@@ -323,9 +325,13 @@ __device__ inline float kernel_W_fast(int kind, int D, float dist, float inv_h) 
   return 0.f;
 }
 
-// FP32 dW/dr / dist (Derivative_kernel_function, particle.cpp:405-807)
+// FP32 dW/dr / dist (Derivative_kernel_function, particle.cpp:405-807).
+// Reciprocals and the exponential are the correctly rounded / accurate
+// forms: the hardware approximations' errors vary smoothly with their input,
+// so they would act as a slightly different kernel on every pair of similar
+// h and not average out of a near-balanced force sum.
 __device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
-  const float ih = r_rcp(h);
+  const float ih = __frcp_rn(h);
   const float s = dist * ih;
   float hD = ih;
   if (D >= 2) hD *= ih;
@@ -334,7 +340,7 @@ __device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
     if (D == 1 || !(s < 2.f)) return 0.f;
     const float C = (float)(D == 2 ? kern_norm(K_WEN, 2) : kern_norm(K_WEN, 3)) * hD;
     const float t = 1.f - 0.5f * s;
-    return -5.f * C * (t * t * t) * s * ih * r_rcp(dist + 1.e-15f);
+    return -5.f * C * (t * t * t) * s * ih * __frcp_rn(dist + 1.e-15f);
   }
   if (kind == K_HYP) {
     const float C = (float)(D == 1 ? kern_norm(K_HYP, 1) : D == 2 ? kern_norm(K_HYP, 2) : kern_norm(K_HYP, 3)) *
@@ -342,7 +348,7 @@ __device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
     float v = 0.f;
     if (s < 1.f) v = C * (-6.f + 3.f * s * s);
     else if (s < 2.f) { const float t = 2.f - s; v = C * -3.f * t * t; }
-    return v * r_rcp(dist + 1.e-20f);
+    return v * __frcp_rn(dist + 1.e-20f);
   }
   if (kind == K_CUB) {
     const float C = (float)(D == 1 ? kern_norm(K_CUB, 1) : D == 2 ? kern_norm(K_CUB, 2) : kern_norm(K_CUB, 3)) *
@@ -350,7 +356,7 @@ __device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
     float v = 0.f;
     if (s < 1.f) v = 3.f * C * (-s + 0.75f * s * s);
     else if (s < 2.f) { const float t = 2.f - s; v = -0.75f * C * t * t; }
-    return v * r_rcp(dist + 1.e-20f);
+    return v * __frcp_rn(dist + 1.e-20f);
   }
   if (kind == K_GAU) {
     const float fac = 0.5f * 2.f / sqrtf((float)PI_REF);
@@ -358,7 +364,7 @@ __device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
     if (D > 1) f *= fac;
     if (D > 2) f *= fac;
     if (!(s < 3.f)) return 0.f;
-    return -2.f * s * __expf(-s * s) * f * hD * ih * r_rcp(dist + 1.e-15f);
+    return -2.f * s * expf(-s * s) * f * hD * ih * __frcp_rn(dist + 1.e-15f);
   }
   const float C = (float)(D == 1 ? kern_norm(K_QUI, 1) : D == 2 ? kern_norm(K_QUI, 2) : kern_norm(K_QUI, 3)) * hD;
   const float a = 3.f - s, b = 2.f - s, c = 1.f - s;
@@ -368,7 +374,7 @@ __device__ inline float kernel_dW_fast(int kind, int D, float dist, float h) {
   else if (s < 2.f) v = C * (-5.f * a4 + 30.f * b4);
   else if (s < 3.f) v = C * (-5.f * a4);
   else return 0.f;
-  return v * ih * r_rcp(dist + 1.e-15f);
+  return v * ih * __frcp_rn(dist + 1.e-15f);
 }
 
 // path dispatch: FP64 keeps the reference arithmetic

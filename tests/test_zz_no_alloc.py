@@ -38,6 +38,30 @@ def test_noalloc_sampling_matches_allocating_entry_point(prec):
     gpu.close()
 
 
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """After the first call on the device (its set-up: the scratch address
+    looked up), further calls at the largest size take no device memory: free
+    memory before and after three calls is the same (cudaMemGetInfo, seen
+    through torch on the same primary context)."""
+    torch = pytest.importorskip("torch")
+    case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    gpu = SPHMeshGeneration(case, precision="fp32")
+    lo = np.array(case.params["box_l"])
+    hi = np.array(case.params["box_r"])
+    pts = lo + np.random.default_rng(3).random((MAX_POINTS, 3)) * (hi - lo)
+    first = gpu.sample_levelset_noalloc(pts)
+    torch.cuda.synchronize(0)
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(3):
+        again = gpu.sample_levelset_noalloc(pts)
+    torch.cuda.synchronize(0)
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
+    for a, b in zip(first, again):
+        assert np.array_equal(a, b)
+    gpu.close()
+
+
 def test_noalloc_rejects_oversized_requests():
     case = cases.disc_hole_2d(spacing=0.02, grid=64)
     gpu = SPHMeshGeneration(case, precision="fp64")
