@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cvp-vps", type=int, default=256)
     ap.add_argument("--cvp-iters", type=int, default=50)
-    ap.add_argument("--batch-geoms", type=int, default=64, help="star-shaped geometries of the batched run (0: skip)")
+    ap.add_argument("--batch-geoms", type=int, default=512, help="star-shaped geometries of the batched run (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--no-volume-mass", action="store_true", help="skip the cut-cell volume / particle-count leg")
     ap.add_argument("--accuracy-steps", type=int, default=100, help="relaxation steps of the accuracy leg (0: skip)")
@@ -252,31 +252,44 @@ def run_reference(args, ws, rank, dist):
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args, dev, dist):
-    """Many independent star-shaped 2D/3D geometries relaxed together (one
-    graph launch per step), against stepping them one at a time in FP32 and
-    in FP64.  All three are timed on steps 2-4 after seeding; the batch also
-    on the batch_steps steps that follow."""
+def run_batched(args, dev, dist, geoms=None):
+    """Many independent star-shaped 2D/3D geometries relaxed together, in the
+    three batch modes: the persistent batch kernel (one cooperative launch
+    runs up to 32 whole steps of every geometry; the default), the per-phase
+    batch kernels (one launch per phase over every geometry's blocks) and each
+    handle's own step graph on its own stream; against stepping the
+    geometries one at a time in FP32 and in FP64.  All are timed on steps 2-4
+    after seeding; the persistent batch also on the batch_steps steps that
+    follow."""
     from mrsph import BatchRelaxation, SPHMeshGeneration, cases
-    t0 = time.perf_counter()
-    geoms = cases.star_batch(args.batch_geoms)
-    gen_s = time.perf_counter() - t0
+    gen_s = 0.0
+    if geoms is None:
+        t0 = time.perf_counter()
+        geoms = cases.star_batch(args.batch_geoms)
+        gen_s = time.perf_counter() - t0
     ntot = sum(c.n_particles for c in geoms)
-    hs = [SPHMeshGeneration(c, precision="fp32", device=dev) for c in geoms]
-    for h in hs:
-        h.Initialize_case()
-    b = BatchRelaxation(hs)
-    b.SPH_run_mesh_generation(1)
-    b.sync()
-    barrier(dist)
-    ms_win = max_over_ranks(b.step_timed(3), dist)
-    ms_long = max_over_ranks(b.step_timed(args.batch_steps), dist)
+    rate = lambda steps, ms: ntot * steps / (ms / 1000.0)
+    modes = {}
     flags = 0
-    for h in hs:
-        flags |= h.stats()["flags"]
-    b.close()
-    for h in hs:
-        h.close()
+    graph = None
+    ms_long = None
+    for mode in ("persistent", "phases", "streams"):
+        hs = [SPHMeshGeneration(c, precision="fp32", device=dev) for c in geoms]
+        for h in hs:
+            h.Initialize_case()
+        b = BatchRelaxation(hs, mode=mode)
+        b.SPH_run_mesh_generation(1)
+        b.sync()
+        barrier(dist)
+        modes[mode] = max_over_ranks(b.step_timed(3), dist)
+        if mode == "persistent":
+            ms_long = max_over_ranks(b.step_timed(args.batch_steps), dist)
+            graph = b.graph_captured
+        for h in hs:
+            flags |= h.stats()["flags"]
+        b.close()
+        for h in hs:
+            h.close()
     seq = {}
     for prec in ("fp32", "fp64"):
         tot = 0.0
@@ -288,15 +301,23 @@ def run_batched(args, dev, dist):
             tot += g.step_timed(3)
             g.close()
         seq[prec] = max_over_ranks(tot, dist)
-    rate = lambda steps, ms: ntot * steps / (ms / 1000.0)
+    ms_win = modes["persistent"]
     return {"geometries": len(geoms), "particles": ntot,
             "n_range": [min(c.n_particles for c in geoms), max(c.n_particles for c in geoms)],
             "value": rate(args.batch_steps, ms_long), "unit": "particle-steps/s",
+            "ms_per_step": ms_long / args.batch_steps, "mode": "persistent",
+            "launch": "one cooperative launch of the persistent batch kernel per 32 steps"
+                      + (", replayed from a CUDA graph" if graph else ""),
             "steps": args.batch_steps, "window": "steps 5..%d after seeding" % (4 + args.batch_steps),
-            "steps_2_4": {"batched_fp32": rate(3, ms_win), "one_at_a_time_fp32": rate(3, seq["fp32"]),
-                          "one_at_a_time_fp64": rate(3, seq["fp64"])},
+            "steps_2_4": {"persistent_fp32": rate(3, ms_win), "phases_fp32": rate(3, modes["phases"]),
+                          "streams_fp32": rate(3, modes["streams"]),
+                          "one_at_a_time_fp32": rate(3, seq["fp32"]), "one_at_a_time_fp64": rate(3, seq["fp64"]),
+                          "ms_per_step": {"persistent": ms_win / 3, "phases": modes["phases"] / 3,
+                                          "streams": modes["streams"] / 3, "one_at_a_time_fp32": seq["fp32"] / 3,
+                                          "one_at_a_time_fp64": seq["fp64"] / 3}},
             "batched_fp32_over_fp64_plain": seq["fp64"] / ms_win,
             "batched_over_one_at_a_time_fp32": seq["fp32"] / ms_win,
+            "persistent_over_streams": modes["streams"] / ms_win,
             "generation_s": gen_s, "device_flags": flags,
             "workload": "star-shaped bodies, 8-32 radial harmonics, sum of amplitudes <= 0.3, even ids 2D "
                         "(128^2 level set) and odd 3D (64^3), counts log-uniform 2k-200k, constant spacing, "
@@ -415,8 +436,15 @@ def run_mrsph(args, ws, rank, local, dist):
     import numpy as np
     from mrsph import SPHMeshGeneration
     from mrsph import build as mbuild
+    from mrsph import cases as mcases
     from mrsph import roofline
     mbuild.build()
+    # the batched leg's geometries, built in spawned processes before this
+    # process touches the GPU
+    t0 = time.perf_counter()
+    batch_geoms = mcases.star_batch(args.batch_geoms, workers=min(16, os.cpu_count() or 1)) \
+        if args.batch_geoms > 0 else None
+    batch_gen_s = time.perf_counter() - t0
     dev = local
     case = workload(args.workload, "fp32")
     n = case.n_particles
@@ -558,7 +586,9 @@ def run_mrsph(args, ws, rank, local, dist):
                 "ms_per_step": win["fp64"]["ms_per_step"], "window": f"steps 2..{1 + args.fp64_steps} after seeding",
                 "fp32_same_window": win["fp32"]}
 
-    batched = run_batched(args, dev, dist) if args.batch_geoms > 0 else None
+    batched = run_batched(args, dev, dist, batch_geoms) if args.batch_geoms > 0 else None
+    if batched is not None:
+        batched["generation_s"] = batch_gen_s
     accuracy = run_accuracy(args, dev) if (args.accuracy_steps > 0 and rank == 0) else None
 
     if rank != 0:

@@ -318,23 +318,43 @@ int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri
 
 /* Batched relaxation of independent geometries (no counterpart in the
  * reference, which relaxes one geometry per run, SPH_run_mesh_generation,
- * sph_mesh_generation.cpp:1371-1463).  A batch steps seeded handles of one
- * device together: each step launches every handle's own step graph on the
- * handle's own stream, so the geometries run concurrently and each handle's
- * results equal those of stepping it alone.  Work queued on a handle before
- * mrsph_batch_step runs first; work queued on it afterwards runs after the
- * batch's steps.  A handle may be stepped
- * alone between batch calls; it must not be destroyed while in a batch. */
+ * sph_mesh_generation.cpp:1371-1463, from Solver::SPH_Mesh_Generation_Solver,
+ * solver.cpp:257-321).  A batch steps seeded handles of one device together;
+ * each handle's results equal those of stepping it alone.  Modes:
+ *   MRSPH_BATCH_PERSISTENT (default when every handle is FP32-split): one
+ *     cooperative launch of a persistent kernel runs up to 32 whole steps of
+ *     every geometry over (geometry, block) work lists with grid-wide
+ *     barriers between the phases; a barrier that waits longer than one
+ *     second gives up and the batch reports MRSPH_ERR_DEVICE.
+ *   MRSPH_BATCH_PHASES: the same work lists, one launch per phase.
+ *   MRSPH_BATCH_STREAMS (FP64-plain batches): each handle's own step graph on
+ *     the handle's own stream.
+ * Work queued on a handle before mrsph_batch_step runs first; work queued on
+ * it afterwards runs after the batch's steps.  A handle may be stepped alone
+ * between batch calls; it must not be destroyed while in a batch. */
 typedef struct mrsph_batch mrsph_batch;
+#define MRSPH_BATCH_STREAMS 0
+#define MRSPH_BATCH_PERSISTENT 1
+#define MRSPH_BATCH_PHASES 2
 int mrsph_batch_create(mrsph_handle* const* handles, int count, mrsph_batch** out);
 int mrsph_batch_destroy(mrsph_batch* b);
 int mrsph_batch_last_error(mrsph_batch* b, char* buf, size_t len);
+/* MRSPH_BATCH_PERSISTENT and MRSPH_BATCH_PHASES need FP32-split handles. */
+int mrsph_batch_set_mode(mrsph_batch* b, int mode);
+/* the mode; graph_captured (may be NULL): 1 when the persistent launches are
+ * replayed from CUDA graphs. */
+int mrsph_batch_get_mode(mrsph_batch* b, int* mode, int* graph_captured);
 /* nsteps steps of every handle (asynchronous; capacity checks every 32 steps). */
 int mrsph_batch_step(mrsph_batch* b, int nsteps);
 /* Same, device-timed with CUDA events (ms from before the first handle's first
  * step to after every handle's last step). */
 int mrsph_batch_step_timed(mrsph_batch* b, int nsteps, double* ms);
 int mrsph_batch_sync(mrsph_batch* b);
+/* Self-test of the persistent kernel's bounded barrier wait (no counterpart in
+ * the reference): a two-block cooperative launch in which one block never
+ * arrives; the other must give up after limit_ms (0 < limit_ms <= 10000) and
+ * raise the error bit.  *raised = 1 when it did. */
+int mrsph_batch_barrier_selftest(int device, double limit_ms, int* raised);
 
 /* e2e helpers: positions in id order (n x 3), host memory (pinned or not). */
 int mrsph_upload_positions(mrsph_handle* h, const double* xyz);

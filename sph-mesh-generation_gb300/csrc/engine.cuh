@@ -125,6 +125,19 @@ struct KCtx {
   DevScalars* sc;
 };
 
+// One FP32-split geometry of a batch as the batch kernels (mrsph_persist.cu)
+// see it: the handle's context, both state buffers, its per-step arrays, the
+// size of its cell table and the buffer that holds its state when the batch
+// launch starts.
+struct BatchSlot {
+  KCtx c;
+  Buf<float> buf[2];
+  Work<float> w;
+  long long ncells;
+  int dim;
+  int cur;
+};
+
 enum { MAP_STEP = 0, MAP_PRE = 1 };
 
 // Tuning of the FP32 map and neighbour passes: resident 256-thread blocks per SM the
@@ -291,6 +304,31 @@ __device__ __forceinline__ void ld_rec(const double4* rec, long long j, double4&
       : "=d"(b1.x), "=d"(b1.y), "=d"(b1.z), "=d"(b1.w) : "l"(rec + 2 * j + 1));
 }
 
+// Load policies of the step's device functions.  LdNC: the read-only data
+// path (ld.global.nc, __ldg) for the per-handle kernels, which never write
+// what they read this way.  LdPlain: ordinary global loads for the persistent
+// batch kernel, where a buffer read in one phase was written by other blocks
+// in an earlier phase of the same launch (after a grid barrier whose fences
+// make those writes visible).  The pointers reach the batch kernel through a
+// shared-memory copy of the geometry's slot, never as const __restrict__
+// kernel parameters, so these loads are not turned into read-only ones.
+struct LdNC {
+  __device__ static void rec(const float4* r, long long j, float4& b0, float4& b1) { ld_rec(r, j, b0, b1); }
+  __device__ static void rec(const double4* r, long long j, double4& b0, double4& b1) { ld_rec(r, j, b0, b1); }
+  template <class T> __device__ static T ld(const T* p) { return __ldg(p); }
+};
+struct LdPlain {
+  __device__ static void rec(const float4* r, long long j, float4& b0, float4& b1) {
+    b0 = r[2 * j];
+    b1 = r[2 * j + 1];
+  }
+  __device__ static void rec(const double4* r, long long j, double4& b0, double4& b1) {
+    b0 = r[2 * j];
+    b1 = r[2 * j + 1];
+  }
+  template <class T> __device__ static T ld(const T* p) { return *p; }
+};
+
 template <class R> __device__ inline typename V4<R>::T mk4(R a, R b, R c, R d);
 template <> __device__ inline double4 mk4<double>(double a, double b, double c, double d) { return make_double4(a, b, c, d); }
 template <> __device__ inline float4 mk4<float>(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
@@ -318,7 +356,7 @@ __device__ inline void set_info(const KCtx& c, R phi, R curv, R& h, R& rho) {
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-static __global__ void k_begin_step(DevScalars* sc, int inc) {
+__device__ inline void begin_step_body(DevScalars* sc, int inc) {
   sc->dt_adv = sc->dt2;
   sc->dt_adv_f = (float)bitsd(sc->dt2);
   sc->hdt_adv_f = (float)(0.5 * bitsd(sc->dt2));
@@ -337,6 +375,13 @@ static __global__ void k_begin_step(DevScalars* sc, int inc) {
     sc->lcount[l] = 0;
   }
   sc->step += inc;
+}
+static __global__ void k_begin_step(DevScalars* sc, int inc) { begin_step_body(sc, inc); }
+
+// clears n words (a step's per-level h maxima) as block blk of 256 threads
+__device__ inline void fill_block(unsigned* p, long long n, long long blk) {
+  const long long i = blk * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0u;
 }
 
 // Random_particle_distribution, sph_mesh_generation.cpp:1302-1367 (one rank)
@@ -386,8 +431,8 @@ __global__ void k_seed(KCtx c, Buf<R> b, unsigned max_att) {
 // map part of Pre_run (sph_mesh_generation.cpp:1010-1050): no advection,
 // Set_particle_info before Find_and_map.
 template <int D, class R>
-__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_MAP_MIN_BLOCKS : 1))
-k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att) {
+__device__ inline void map_block(const KCtx& c, const Buf<R>& b, int* counts, unsigned* lhmax, int mode,
+                                 unsigned max_att, long long blk) {
   using P = PosOps<D, R>;
   constexpr bool F32 = std::is_same<R, float>::value;
   __shared__ unsigned long long s_hmax[MAX_CL];
@@ -397,7 +442,7 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
     s_lcount[threadIdx.x] = 0;
   }
   __syncthreads();
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long i = blk * blockDim.x + threadIdx.x;
   unsigned surf = 0;
   if (i < c.n) {
     int meta = b.meta[i];
@@ -590,6 +635,12 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
   }
 }
 
+template <int D, class R>
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_MAP_MIN_BLOCKS : 1))
+k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att) {
+  map_block<D, R>(c, b, counts, lhmax, mode, max_att, blockIdx.x);
+}
+
 // Packed record read by the neighbour passes, two V4 words per particle so
 // that one candidate costs one 32-byte sector (FP32):
 //   FP32: w0 = (offset x, y, z, h), w1 = (anchor x, y, z as exact floats, +-1/rho^2)
@@ -662,9 +713,9 @@ __device__ __noinline__ bool exact_cos(const KCtx& c, const float* ni, const flo
 }
 
 template <int D, class R>
-__global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict__ perm2,
-                          int* __restrict__ slot_of_id, long long n, int partial) {
-  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ inline void reorder_block(const Buf<R>& src, const Buf<R>& dst, const KCtx& c, const int* perm2,
+                                     int* slot_of_id, long long n, int partial, long long blk) {
+  long long s = blk * blockDim.x + threadIdx.x;
   if (s >= n) return;
   int o = perm2[s];
   const auto p = src.posh[o];
@@ -693,8 +744,15 @@ __global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict_
   slot_of_id[id] = (int)s;
 }
 
+template <int D, class R>
+__global__ void k_reorder(Buf<R> src, Buf<R> dst, KCtx c, const int* __restrict__ perm2,
+                          int* __restrict__ slot_of_id, long long n, int partial) {
+  reorder_block<D, R>(src, dst, c, perm2, slot_of_id, n, partial, blockIdx.x);
+}
+
 // Largest h of level-L particles (lhmax entries) over the level-0 cells
 // lo..hi (0: none).
+template <class LD = LdNC>
 __device__ inline float lhmax_over(const KCtx& c, const unsigned* __restrict__ lhmax, int L, const int* lo,
                                    const int* hi) {
   const unsigned* o = lhmax + (long long)L * c.geo.nc0;
@@ -702,7 +760,7 @@ __device__ inline float lhmax_over(const KCtx& c, const unsigned* __restrict__ l
   for (int z = lo[2]; z <= hi[2]; z++)
     for (int y = lo[1]; y <= hi[1]; y++)
       for (int x = lo[0]; x <= hi[0]; x++)
-        m = max(m, __ldg(&o[((long long)z * c.geo.n[0][1] + y) * c.geo.n[0][0] + x]));
+        m = max(m, LD::ld(&o[((long long)z * c.geo.n[0][1] + y) * c.geo.n[0][0] + x]));
   return __uint_as_float(m);
 }
 
@@ -732,7 +790,7 @@ template <int D> struct SOrigin<D, float> {
 // FP32-split works in FP32 relative to the anchor: a level-L cell is
 // 2^(finest - L) anchor cells, so the position inside the origin's level-L
 // (or level-0) cell is (anchor index - cell's first anchor) * A + offset.
-template <int D>
+template <int D, class LD = LdNC>
 __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__ lhmax, int L,
                                      const SOrigin<D, double>& so, double hi, bool active, int* q, float* fr) {
   const double hic = hi * c.prm.cutoff;
@@ -745,7 +803,7 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
       lo[d] = (int)fmax(0.0, fmin(floor((so.xr[d] - Rg) * c.geo.idc0[d]), top));
       up[d] = (int)fmax(0.0, fmin(floor((so.xr[d] + Rg) * c.geo.idc0[d]), top));
     }
-    hloc = lhmax_over(c, lhmax, L, lo, up);
+    hloc = lhmax_over<LD>(c, lhmax, L, lo, up);
   }
   if (!(hloc > 0.f)) return 0.f;
   const double Rw = fmax(hic, (double)hloc * c.prm.cutoff) + 1.e-10;
@@ -758,7 +816,7 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
   }
   return (float)(Rw * (1.0 + 1.e-5));
 }
-template <int D>
+template <int D, class LD = LdNC>
 __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__ lhmax, int L,
                                      const SOrigin<D, float>& so, float hi, bool active, int* q, float* fr) {
   const float cut = c.prm.cutoff_f;
@@ -776,7 +834,7 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
       lo[d] = max(0, min(c0 + (int)floorf(fmaxf(u0 - r0, -1.0e6f)), top));
       up[d] = max(0, min(c0 + (int)floorf(fminf(u0 + r0, 1.0e6f)), top));
     }
-    hloc = lhmax_over(c, lhmax, L, lo, up);
+    hloc = lhmax_over<LD>(c, lhmax, L, lo, up);
   }
   if (!(hloc > 0.f)) return 0.f;
   const int sh = c.geo.ncl - 1 - L;
@@ -805,14 +863,14 @@ __device__ inline float level_origin(const KCtx& c, const unsigned* __restrict__
 // arithmetic (FP64: 1e-5; FP32-split: 3e-5, which also covers the FP32
 // test's acceptance band of 2^-15 on R^2, so the per-lane and the warp-tile
 // scans accept the same candidates); the candidate test decides membership.
-template <int D, class R, class F>
+template <int D, class R, class LD = LdNC, class F>
 __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cstart,
                                        const unsigned* __restrict__ lhmax, const SOrigin<D, R>& so, R hi, F&& f) {
   for (int L = 0; L < c.geo.ncl; L++) {
     if (c.sc->lcount[L] == 0) continue;
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {0, 0, 0}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
-    const float R = level_origin<D>(c, lhmax, L, so, hi, true, q, fr);
+    const float R = level_origin<D, LD>(c, lhmax, L, so, hi, true, q, fr);
     if (!(R > 0.f)) continue;
     for (int d = 0; d < 3; d++) hn[d] = c.geo.hn[L][d];
     for (int d = 0; d < D; d++) {
@@ -844,7 +902,7 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
         const int xh = min(q[0] + (int)floorf(fr[0] + w), hn[0] - 1);
         if (xl > xh) continue;
         const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
-        const int s0 = __ldg(&cstart[rb + xl]), e0 = __ldg(&cstart[rb + xh + 1]);
+        const int s0 = LD::ld(&cstart[rb + xl]), e0 = LD::ld(&cstart[rb + xh + 1]);
         for (int j = s0; j < e0; j++) f(j);
       }
     }
@@ -864,7 +922,7 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
 // load(k) builds the tile entry of candidate k (uniform mode), vtile(j, e)
 // visits it, vglob(j) visits candidate j straight from global memory
 // (per-lane mode).
-template <int D, class R, class E, class FL, class FT, class FG>
+template <int D, class R, class LD = LdNC, class E, class FL, class FT, class FG>
 __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, const unsigned* __restrict__ lhmax,
                                  bool active, const SOrigin<D, R>& so, R hi, E* tile, FL&& load, FT&& vtile,
                                  FG&& vglob) {
@@ -874,7 +932,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
     if (c.sc->lcount[L] == 0) continue;
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {-1, -1, -1}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
-    const float R = level_origin<D>(c, lhmax, L, so, hi, active, q, fr);
+    const float R = level_origin<D, LD>(c, lhmax, L, so, hi, active, q, fr);
     const bool need = R > 0.f;
     if (!__any_sync(FULL, need)) continue;
     const float R2 = R * R;
@@ -930,7 +988,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
           const int ul = __reduce_min_sync(FULL, xl), uh = __reduce_max_sync(FULL, xh);
           if (ul > uh) continue;
           const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
-          const int s0 = __ldg(&cstart[rb + ul]), e0 = __ldg(&cstart[rb + uh + 1]);
+          const int s0 = LD::ld(&cstart[rb + ul]), e0 = LD::ld(&cstart[rb + uh + 1]);
           for (int t0 = s0; t0 < e0; t0 += 32) {
             const int k = t0 + lane;
             if (k < e0) tile[lane] = load(k);
@@ -954,7 +1012,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
           row_range(z, y, xl, xh);
           if (xl > xh) continue;
           const long long rb = base + ((long long)z * hn[1] + y) * hn[0];
-          const int s0 = __ldg(&cstart[rb + xl]), e0 = __ldg(&cstart[rb + xh + 1]);
+          const int s0 = LD::ld(&cstart[rb + xl]), e0 = LD::ld(&cstart[rb + xh + 1]);
           for (int j = s0; j < e0; j++) vglob(j);
         }
     }
@@ -988,8 +1046,8 @@ template <class R> struct RecPair { typename V4<R>::T a, b; };
 
 
 // KK: the kernel kind fixed at compile time (FP32 Wendland C2), or -1
-template <int D, class R, int KK>
-__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DENSITY_MIN_BLOCKS : 1)) k_density(KCtx c, Buf<R> b, Work<R> w) {
+template <int D, class R, int KK, class LD = LdNC>
+__device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<R>& w, long long blk) {
   using P = PosOps<D, R>;
   using Q = RecOps<D, R>;
   using T4 = typename V4<R>::T;
@@ -998,7 +1056,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   // (cutoff*h)^2, negative for a SURFACE particle; FP64: the packed record
   using E = typename std::conditional<F32, float4, RecPair<R>>::type;
   __shared__ E s_tile[8][32];
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long i = blk * blockDim.x + threadIdx.x;
   const bool active = i < c.n;
   unsigned long long pairs = 0;
   T4 a0 = mk4<R>(0, 0, 0, 0), a1 = mk4<R>(0, 0, 0, 0);
@@ -1058,7 +1116,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   };
   auto vglob = [&](int j) {
     T4 b0, b1;
-    ld_rec(b.rec, j, b0, b1);
+    LD::rec(b.rec, j, b0, b1);
     R dr[3];
     Q::rel(c, a0, a1, b0, b1, dr);
     if constexpr (F32) {
@@ -1083,7 +1141,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
                          D == 3 ? ((float)a1.z - wa[2]) * Af[2] + (float)a0.z : 0.f};
     auto load = [&](int k) {
       float4 b0, b1;
-      ld_rec(b.rec, k, b0, b1);
+      LD::rec(b.rec, k, b0, b1);
       const float rj = b0.w * (float)cut;
       const float r2 = rj * rj;
       return make_float4((b1.x - wa[0]) * Af[0] + b0.x, (b1.y - wa[1]) * Af[1] + b0.y,
@@ -1097,11 +1155,11 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (d2 >= Rm * kD2Sure) unc = true;
       accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
     };
-    warp_scan<D, R>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R, LD>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   } else {
     auto load = [&](int k) {
       RecPair<R> e;
-      ld_rec(b.rec, k, e.a, e.b);
+      LD::rec(b.rec, k, e.a, e.b);
       return e;
     };
     auto vtile = [&](int j, const RecPair<R>& e) {
@@ -1111,7 +1169,7 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
       if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) return;
       accept(j, dr, dist, e.b.w < (R)0);
     };
-    warp_scan<D, R>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R, LD>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
   }
   if (active) {
     if (WEN32 && ti == REAL_P) {
@@ -1132,20 +1190,37 @@ __global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DE
   block_sum_u64_to_global(pairs, &c.sc->pairs);
 }
 
-// FP32-split density fix-up, one thread per queued particle (grid-stride):
-// every pair of the particle is decided again (FP32 outside the bands, FP64
-// inside), its list is compacted to the accepted pairs in scan order, surface
-// filter decisions made in FP64 are marked on their entries (the force passes
-// read the marks), and its kernel sum, count and share of the step's pair
-// total are redone.  A particle whose list spilled re-scans its cells.
-template <int D, int KK>
-__global__ void __launch_bounds__(256) k_density_fix(KCtx c, Buf<float> b, Work<float> w) {
+template <int D, class R, int KK>
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? MRSPH_DENSITY_MIN_BLOCKS : 1)) k_density(KCtx c, Buf<R> b, Work<R> w) {
+  density_block<D, R, KK>(c, b, w, blockIdx.x);
+}
+
+// FP32-split density fix-up, one warp per queued particle (grid-stride over
+// warps): every pair of the particle is decided again (FP32 outside the
+// bands, FP64 inside), its list is compacted to the accepted pairs in scan
+// order (the lanes take 32 entries at a time; a ballot gives each accepted
+// entry its new position), surface-filter decisions made in FP64 are marked
+// on their entries (the force passes read the marks), and its kernel sum,
+// count and share of the step's pair total are redone.  The sum has one
+// fixed order whatever the path: the accepted pairs' terms in list order,
+// term p into lane p mod 32's partial sum, the partials folded by a butterfly
+// (xor 16, 8, 4, 2, 1).  The list path stores the terms in the pair
+// coefficient array (which stage 1 overwrites) and sums them strided; a
+// particle whose list spilled re-scans its cells on lane 0, which keeps the
+// 32 partial sums itself and folds them the same way.
+template <int D, int KK, class LD = LdNC>
+__device__ inline void density_fix_items(const KCtx& c, const Buf<float>& b, const Work<float>& w, long long blk,
+                                         long long nblk) {
   using Q = RecOps<D, float>;
   constexpr bool WEN = KK == K_WEN;
+  const unsigned FULL = 0xffffffffu;
   const unsigned nq = c.sc->nfix;
+  const long long wpb = blockDim.x >> 5;
+  if (blk * wpb >= (long long)nq) return;  // block-uniform: nothing queued for this block
+  const int lane = threadIdx.x & 31;
   const int kind = KK >= 0 ? KK : c.prm.kernel;
   const float cut = c.prm.cutoff_f, cos_t = c.prm.cos_thres_f;
-  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nq; t += gridDim.x * blockDim.x) {
+  for (long long t = blk * wpb + (threadIdx.x >> 5); t < nq; t += nblk * wpb) {  // warp-uniform
     const int i = w.fixq[t];
     const float4 a0 = b.rec[2 * i], a1 = b.rec[2 * i + 1];
     const int ti = b.meta[i] & 0xFF;
@@ -1156,30 +1231,35 @@ __global__ void __launch_bounds__(256) k_density_fix(KCtx c, Buf<float> b, Work<
     }
     const float hi = a0.w, inv_hi = r_rcp(hi);
     const float R2i = (hi * cut) * (hi * cut);
-    float sum = 0.f;
-    int ncount = 0, cnt = 0;
     const int old = w.cnt[i];
-    int* row = w.nbl + nb_slot(i, 0, w.cap);
-    auto visit = [&](int j) {
+    const long long base = nb_slot(i, 0, w.cap);
+    int* row = w.nbl + base;
+    float* prow = w.pc + base;
+    // decision of pair (i, j): false if j is no neighbour; else e = j with
+    // the surface-filter mark, term its kernel-sum term and counted whether
+    // it counts towards ncount (generic kernels)
+    auto visit = [&](int j, int& e, float& term, bool& counted) -> bool {
       float4 b0, b1;
-      ld_rec(b.rec, j, b0, b1);
+      LD::rec(b.rec, j, b0, b1);
       float dr[3];
       Q::rel(c, a0, a1, b0, b1, dr);
       const float d2 = d2_of(dr, D);
       const float rj = b0.w * cut;
       const float Rm = fmaxf(R2i, rj * rj);
-      if (d2 > Rm * kD2Accept) return;
-      if (d2 >= Rm * kD2Sure && !exact_neighbor<D>(c, a0, a1, b0, b1)) return;
-      int e = j;
+      if (d2 > Rm * kD2Accept) return false;
+      if (d2 >= Rm * kD2Sure && !exact_neighbor<D>(c, a0, a1, b0, b1)) return false;
+      e = j;
+      term = 0.f;
+      counted = false;
       const float dist = pair_dist(d2);
       if (ti == REAL_P) {
         if (WEN) {
           const float s = dist * inv_hi;
           const float tt = fmaxf(fmaf(-0.5f, s, 1.f), 0.f), t2 = tt * tt;
-          sum += (t2 * t2) * fmaf(2.f, s, 1.f);
+          term = (t2 * t2) * fmaf(2.f, s, 1.f);
         } else {
-          sum += pair_W(kind, D, dist, hi, inv_hi);
-          ncount++;
+          term = pair_W(kind, D, dist, hi, inv_hi);
+          counted = true;
         }
       } else if (ti == SURFACE_P && b1.w < 0.f) {
         const float dn = dot3<D, float>(dr, ni);
@@ -1196,33 +1276,83 @@ __global__ void __launch_bounds__(256) k_density_fix(KCtx c, Buf<float> b, Work<
           ok = ca > cos_t;
         }
         if (ok) {
-          sum += pair_W(kind, D - 1, pd, hi, inv_hi);
-          ncount++;
+          term = pair_W(kind, D - 1, pd, hi, inv_hi);
+          counted = true;
         }
       }
-      if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = e;
-      cnt++;
+      return true;
     };
+    int cnt = 0, ncount = 0;
+    float sum = 0.f;
     if (old <= w.cap) {
       // the list holds every candidate the FP32 test did not certainly
-      // reject; compaction writes entry cnt <= q after reading entry q
-      for (int q = 0; q < old; q++) visit(nb_index(row[((q >> 3) << 8) + (q & 7)]));
+      // reject; each chunk of 32 entries is read before any of it is written,
+      // and an accepted entry moves to a position <= its own
+      for (int q0 = 0; q0 < old; q0 += 32) {
+        const int q = q0 + lane;
+        int e = 0;
+        float term = 0.f;
+        bool acc = false, counted = false;
+        if (q < old) acc = visit(nb_index(LD::ld(&row[((q >> 3) << 8) + (q & 7)])), e, term, counted);
+        const unsigned m = __ballot_sync(FULL, acc);
+        ncount += __popc(__ballot_sync(FULL, acc && counted));
+        if (acc) {
+          const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+          const int o = ((pos >> 3) << 8) + (pos & 7);
+          row[o] = e;
+          prow[o] = term;
+        }
+        cnt += __popc(m);
+        __syncwarp();
+      }
+      for (int p = lane; p < cnt; p += 32) sum += LD::ld(&prow[((p >> 3) << 8) + (p & 7)]);
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
     } else {
-      const SOrigin<D, float> so(c, b.posh[i], b.key[i]);
-      scan_candidates<D, float>(c, w.cstart, w.lhmax, so, hi, visit);
+      if (lane == 0) {
+        float part[32];
+        for (int l = 0; l < 32; l++) part[l] = 0.f;
+        const SOrigin<D, float> so(c, b.posh[i], b.key[i]);
+        scan_candidates<D, float, LD>(c, w.cstart, w.lhmax, so, hi, [&](int j) {
+          int e = 0;
+          float term = 0.f;
+          bool counted = false;
+          if (!visit(j, e, term, counted)) return;
+          if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = e;
+          part[cnt & 31] += term;
+          ncount += counted ? 1 : 0;
+          cnt++;
+        });
+        for (int o = 16; o > 0; o >>= 1) {
+          float nxt[32];
+          for (int l = 0; l < 32; l++) nxt[l] = part[l] + part[l ^ o];
+          for (int l = 0; l < 32; l++) part[l] = nxt[l];
+        }
+        sum = part[0];
+      }
+      cnt = __shfl_sync(FULL, cnt, 0);
+      ncount = __shfl_sync(FULL, ncount, 0);
     }
-    if (WEN && ti == REAL_P) {
-      sum *= (float)kern_norm(K_WEN, D) * (D == 3 ? inv_hi * inv_hi * inv_hi : inv_hi * inv_hi);
-      ncount = cnt;
+    if (lane == 0) {
+      if (WEN && ti == REAL_P) {
+        sum *= (float)kern_norm(K_WEN, D) * (D == 3 ? inv_hi * inv_hi * inv_hi : inv_hi * inv_hi);
+        ncount = cnt;
+      }
+      if (ncount > 1) sum = 1.f / (sum + 1.e-15f);
+      w.sum[i] = sum;
+      w.cnt[i] = cnt;
+      atomicAdd(&c.sc->pairs, (unsigned long long)(long long)(cnt - old));
     }
-    if (ncount > 1) sum = 1.f / (sum + 1.e-15f);
-    w.sum[i] = sum;
-    w.cnt[i] = cnt;
-    atomicAdd(&c.sc->pairs, (unsigned long long)(long long)(cnt - old));
+    __syncwarp();
   }
 }
 
-static __global__ void k_accum_pairs(DevScalars* sc) { sc->pairs_total += sc->pairs; }
+template <int D, int KK>
+__global__ void __launch_bounds__(256) k_density_fix(KCtx c, Buf<float> b, Work<float> w) {
+  density_fix_items<D, KK>(c, b, w, blockIdx.x, gridDim.x);
+}
+
+__device__ inline void accum_pairs_body(DevScalars* sc) { sc->pairs_total += sc->pairs; }
+static __global__ void k_accum_pairs(DevScalars* sc) { accum_pairs_body(sc); }
 
 // four consecutive pair coefficients (16-byte aligned)
 __device__ inline void store4(float* p, const float* v) {
@@ -1232,12 +1362,14 @@ __device__ inline void store4(double* p, const double* v) {
   reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
+template <class LD>
 __device__ inline void load4(const float* p, float* v) {
-  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  const float4 t = LD::ld(reinterpret_cast<const float4*>(p));
   v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
 }
+template <class LD>
 __device__ inline void load4(const double* p, double* v) {
-  const double2 t0 = __ldg(reinterpret_cast<const double2*>(p)), t1 = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  const double2 t0 = LD::ld(reinterpret_cast<const double2*>(p)), t1 = LD::ld(reinterpret_cast<const double2*>(p) + 1);
   v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
 }
 
@@ -1272,7 +1404,7 @@ __device__ inline float wendland_aw(float dist, float h) {
 // complete (cnt <= cap); SPILL = true: it spilled and re-scans its cells,
 // making the neighbour and surface-filter decisions as the density pass does
 // (FP32-split: exact inside the bands).  my_dt / my_v take the min / max.
-template <int D, class R, int STAGE, int KK, bool SPILL>
+template <int D, class R, int STAGE, int KK, bool SPILL, class LD = LdNC>
 __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work<R>& w, long long i, double& my_dt,
                                       double& my_v) {
   using Q = RecOps<D, R>;
@@ -1396,7 +1528,7 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
         // lie within the particle's cap and are ignored (stage 1 stores 0)
         for (int q0 = 0; q0 < cnt; q0 += 4) {
           const int o = ((q0 >> 3) << 8) + (q0 & 7);
-          const int4 j4 = __ldg(reinterpret_cast<const int4*>(row + o));
+          const int4 j4 = LD::ld(reinterpret_cast<const int4*>(row + o));
           const int jj[4] = {j4.x, j4.y, j4.z, j4.w};
           R cc[4];
           if (STAGE == 1) {
@@ -1406,7 +1538,7 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
               if (q0 + k < cnt) {
                 const int j = nb_index(jj[k]);
                 T4 b0, b1;
-                ld_rec(b.rec, j, b0, b1);
+                LD::rec(b.rec, j, b0, b1);
                 R vec[3], dr[3];
                 Q::rel(c, a0, a1r, b0, b1, vec);
                 coef(j, b0, b1, vec, dr, cc[k], nb_mark(jj[k]));
@@ -1414,7 +1546,7 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
             }
             store4(crow + o, cc);
           } else {
-            load4(crow + o, cc);
+            load4<LD>(crow + o, cc);
 #pragma unroll
             for (int k = 0; k < 4; k++)
               if (q0 + k < cnt && cc[k] != (R)0) visc(nb_index(jj[k]), cc[k]);
@@ -1425,17 +1557,17 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
         for (int q = 0; q < cnt; q++) {
           const int o = ((q >> 3) << 8) + (q & 7);
           if (STAGE == 1) {
-            const int e = __ldg(&row[o]);
+            const int e = LD::ld(&row[o]);
             const int j = nb_index(e);
             T4 b0, b1;
-            ld_rec(b.rec, j, b0, b1);
+            LD::rec(b.rec, j, b0, b1);
             R vec[3], dr[3], cij = 0;
             Q::rel(c, a0, a1r, b0, b1, vec);
             coef(j, b0, b1, vec, dr, cij, nb_mark(e));
             crow[o] = cij;
           } else {
-            const R cij = __ldg(&crow[o]);
-            if (cij != (R)0) visc(nb_index(__ldg(&row[o])), cij);
+            const R cij = LD::ld(&crow[o]);
+            if (cij != (R)0) visc(nb_index(LD::ld(&row[o])), cij);
           }
           if ((q & 3) == 3 || q == cnt - 1) flush();
         }
@@ -1445,9 +1577,9 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
       const R R2i = (h * cut) * (h * cut);
       const SOrigin<D, R> so(c, b.posh[i], b.key ? b.key[i] : 0);
       int q = 0;  // accepted neighbours so far (the list entries this scan replaces)
-      scan_candidates<D, R>(c, w.cstart, w.lhmax, so, h, [&](int j) {
+      scan_candidates<D, R, LD>(c, w.cstart, w.lhmax, so, h, [&](int j) {
         T4 b0, b1;
-        ld_rec(b.rec, j, b0, b1);
+        LD::rec(b.rec, j, b0, b1);
         R vec[3], dr[3], cij = 0;
         Q::rel(c, a0, a1r, b0, b1, vec);
         if constexpr (F32) {
@@ -1499,27 +1631,39 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
 
 // KK: the kernel kind fixed at compile time (FP32 Wendland C2), or -1.
 // Particles whose list spilled are left to k_force_spill.
-template <int D, class R, int STAGE, int KK>
-__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE == 1 ? MRSPH_FORCE_MIN_BLOCKS : MRSPH_FORCE2_MIN_BLOCKS) : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <int D, class R, int STAGE, int KK, class LD = LdNC>
+__device__ inline void force_block(const KCtx& c, const Buf<R>& b, const Work<R>& w, long long blk) {
+  long long i = blk * blockDim.x + threadIdx.x;
   double my_dt = 1.e300, my_v = 0.0;
-  if (i < c.n && w.cnt[i] <= w.cap) force_particle<D, R, STAGE, KK, false>(c, b, w, i, my_dt, my_v);
+  if (i < c.n && w.cnt[i] <= w.cap) force_particle<D, R, STAGE, KK, false, LD>(c, b, w, i, my_dt, my_v);
   if (STAGE == 1) block_minmax_to_global(my_dt, my_v, &c.sc->dt1, &c.sc->vmax1);
   else block_minmax_to_global(my_dt, my_v, &c.sc->dt2, &c.sc->vmax2);
 }
 
+template <int D, class R, int STAGE, int KK>
+__global__ void __launch_bounds__(256, (std::is_same<R, float>::value ? (STAGE == 1 ? MRSPH_FORCE_MIN_BLOCKS : MRSPH_FORCE2_MIN_BLOCKS) : 1)) k_force(KCtx c, Buf<R> b, Work<R> w) {
+  force_block<D, R, STAGE, KK>(c, b, w, blockIdx.x);
+}
+
 // The force stage of the particles whose list spilled (queued by the density
 // pass; grid-stride), re-scanning their cells.
-template <int D, class R, int STAGE, int KK>
-__global__ void __launch_bounds__(256) k_force_spill(KCtx c, Buf<R> b, Work<R> w) {
+template <int D, class R, int STAGE, int KK, class LD = LdNC>
+__device__ inline void force_spill_items(const KCtx& c, const Buf<R>& b, const Work<R>& w, long long blk,
+                                         long long nblk) {
   double my_dt = 1.e300, my_v = 0.0;
   const unsigned nq = c.sc->nspill;
-  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nq; t += gridDim.x * blockDim.x) {
+  if (blk * blockDim.x >= (long long)nq) return;  // block-uniform: nothing queued for this block
+  for (long long t = blk * blockDim.x + threadIdx.x; t < nq; t += nblk * blockDim.x) {
     const int i = w.spillq[t];
-    if (w.cnt[i] > w.cap) force_particle<D, R, STAGE, KK, true>(c, b, w, i, my_dt, my_v);
+    if (w.cnt[i] > w.cap) force_particle<D, R, STAGE, KK, true, LD>(c, b, w, i, my_dt, my_v);
   }
   if (STAGE == 1) block_minmax_to_global(my_dt, my_v, &c.sc->dt1, &c.sc->vmax1);
   else block_minmax_to_global(my_dt, my_v, &c.sc->dt2, &c.sc->vmax2);
+}
+
+template <int D, class R, int STAGE, int KK>
+__global__ void __launch_bounds__(256) k_force_spill(KCtx c, Buf<R> b, Work<R> w) {
+  force_spill_items<D, R, STAGE, KK>(c, b, w, blockIdx.x, gridDim.x);
 }
 
 // ----------------------------------------------------------------- taps
@@ -2009,6 +2153,27 @@ class Engine : public EngineBase {
 
   int neighbor_capacity() const override { return w_.cap; }
 
+  // The batch kernels' view of this handle (FP32-split only).
+  int batch_slot(BatchSlot* out) override {
+    if (!std::is_same<R, float>::value) { err = "batched kernels take FP32-split handles"; return MRSPH_ERR_ARG; }
+    if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
+    BatchSlot s{};
+    s.c = kc_;
+    std::memcpy((void*)&s.buf[0], (const void*)&buf_[0], sizeof(Buf<float>));
+    std::memcpy((void*)&s.buf[1], (const void*)&buf_[1], sizeof(Buf<float>));
+    std::memcpy((void*)&s.w, (const void*)&w_, sizeof(Work<float>));
+    s.ncells = ncells_;
+    s.dim = D;
+    s.cur = cur_;
+    *out = s;
+    return 0;
+  }
+  // nsteps whole steps ran on this handle's state in a batch launch
+  void batch_advance(int nsteps) override {
+    cur_ ^= (nsteps & 1);
+    have_work_ = true;
+  }
+
  private:
   static unsigned long long dbits_host(double x) { unsigned long long u; std::memcpy(&u, &x, 8); return u; }
   static double bitsd_host(unsigned long long u) { double x; std::memcpy(&x, &u, 8); return x; }
@@ -2086,8 +2251,9 @@ class Engine : public EngineBase {
     else
       k_density<D, R, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
     if constexpr (std::is_same<R, float>::value) {
-      if (wen32) k_density_fix<D, K_WEN><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
-      else k_density_fix<D, -1><<<qgrid(), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+      // one warp per queued particle: as many warps as particles / 32
+      if (wen32) k_density_fix<D, K_WEN><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
+      else k_density_fix<D, -1><<<grid(n), 256, 0, st_>>>(kc_, buf_[cur_], w_);
     }
     k_accum_pairs<<<1, 1, 0, st_>>>(kc_.sc);
     have_work_ = true;

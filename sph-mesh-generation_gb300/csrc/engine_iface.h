@@ -8,6 +8,8 @@
 
 namespace mrsph {
 
+struct BatchSlot;  // engine.cuh
+
 struct EngineConfig {
   Params prm;
   CellGeo geo;
@@ -52,6 +54,10 @@ class EngineBase {
   virtual int step_batched() = 0;
   virtual int prepare_steps() = 0;
   virtual int check_capacity() = 0;
+  // The batch kernels' view of the handle (FP32-split engines; see BatchSlot)
+  // and the bookkeeping after nsteps steps of a batch launch.
+  virtual int batch_slot(BatchSlot* out) = 0;
+  virtual void batch_advance(int nsteps) = 0;
   std::string err;
 };
 

@@ -110,6 +110,9 @@ EXPORTS = {
     "mrsph_batch_step": ([C.c_void_p, C.c_int], C.c_int),
     "mrsph_batch_step_timed": ([C.c_void_p, C.c_int, C.POINTER(C.c_double)], C.c_int),
     "mrsph_batch_sync": ([C.c_void_p], C.c_int),
+    "mrsph_batch_set_mode": ([C.c_void_p, C.c_int], C.c_int),
+    "mrsph_batch_get_mode": ([C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+    "mrsph_batch_barrier_selftest": ([C.c_int, C.c_double, C.POINTER(C.c_int)], C.c_int),
     "mrsph_upload_positions": ([C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_download_positions": ([C.c_void_p, C.c_void_p], C.c_int),
 }

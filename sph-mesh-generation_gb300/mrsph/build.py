@@ -28,6 +28,7 @@ SOURCES = {
     "mrsph_cvp.cu": ["-fmad=false"],
     "mrsph_tri.cu": ["-fmad=false"],
     "mrsph_batch.cu": [],
+    "mrsph_persist.cu": [],
 }
 
 

@@ -410,15 +410,25 @@ def star_shape(dim: int, seed: int, n_target: int, kernel: str = "wendland", h_o
     return Case(f"star_{dim}d_{seed}", p, [lv], n, steps=300)
 
 
+def _star_job(job):
+    dim, seed, n, precision = job
+    return star_shape(dim, seed, n, precision=precision)
+
+
 def star_batch(count: int = 512, seed: int = 11, n_min: int = 2000, n_max: int = 200000,
-               precision: str = "fp32") -> List[Case]:
+               precision: str = "fp32", workers: int = 1) -> List[Case]:
     """count independent star-shaped geometries, even indices 2D and odd 3D,
     particle counts log-uniform in [n_min, n_max] (about 20M in total for
-    512 geometries)."""
+    512 geometries).  workers > 1 builds them in that many spawned processes
+    (spawned, so a caller that already uses the GPU is not forked)."""
     rng = np.random.default_rng(seed)
     targets = np.exp(rng.uniform(np.log(n_min), np.log(n_max), count))
-    return [star_shape(2 if g % 2 == 0 else 3, seed * 100003 + g, int(targets[g]), precision=precision)
-            for g in range(count)]
+    jobs = [(2 if g % 2 == 0 else 3, seed * 100003 + g, int(targets[g]), precision) for g in range(count)]
+    if workers > 1 and count > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(workers, count)) as pool:
+            return pool.map(_star_job, jobs, chunksize=4)
+    return [_star_job(j) for j in jobs]
 
 
 def _ellipse_root(r0, z0, z1, g, iters=160):

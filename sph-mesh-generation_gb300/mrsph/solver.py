@@ -313,12 +313,18 @@ class SPHMeshGeneration:
         return out
 
 
-class BatchRelaxation:
-    """Many independent geometries relaxed together (one CUDA graph launch per
-    step over all handles; mrsph_batch_*).  Each handle's results equal those
-    of stepping it alone."""
+BATCH_MODES = {"streams": 0, "persistent": 1, "phases": 2}
 
-    def __init__(self, solvers):
+
+class BatchRelaxation:
+    """Many independent geometries relaxed together (mrsph_batch_*).  Modes:
+    "persistent" (default for FP32-split handles: one cooperative launch of
+    the persistent batch kernel runs up to 32 steps of every geometry),
+    "phases" (the same work lists, one launch per phase) and "streams" (each
+    handle's own step graph on its own stream; FP64-plain batches).  Each
+    handle's results equal those of stepping it alone."""
+
+    def __init__(self, solvers, mode: str = None):
         self.solvers = list(solvers)
         self.lib = L.load()
         arr = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
@@ -327,6 +333,23 @@ class BatchRelaxation:
         if rc != 0:
             raise L.MrsphError(f"mrsph_batch_create failed ({rc})")
         self.b = b
+        if mode is not None:
+            self.set_mode(mode)
+
+    def set_mode(self, mode: str):
+        self._check(self.lib.mrsph_batch_set_mode(self.b, BATCH_MODES[mode]), "mrsph_batch_set_mode")
+
+    @property
+    def mode(self) -> str:
+        m, g = C.c_int(0), C.c_int(0)
+        self._check(self.lib.mrsph_batch_get_mode(self.b, C.byref(m), C.byref(g)), "mrsph_batch_get_mode")
+        return {v: k for k, v in BATCH_MODES.items()}[m.value]
+
+    @property
+    def graph_captured(self) -> bool:
+        m, g = C.c_int(0), C.c_int(0)
+        self._check(self.lib.mrsph_batch_get_mode(self.b, C.byref(m), C.byref(g)), "mrsph_batch_get_mode")
+        return bool(g.value)
 
     def _check(self, rc, what):
         if rc != 0:
@@ -355,3 +378,15 @@ class BatchRelaxation:
             self.close()
         except Exception:
             pass
+
+
+def barrier_selftest(device: int = 0, limit_ms: float = 200.0) -> bool:
+    """The persistent batch kernel's bounded barrier wait: a two-block
+    cooperative launch in which one block never arrives; True when the other
+    gave up after limit_ms and raised the error bit."""
+    lib = L.load()
+    raised = C.c_int(0)
+    rc = lib.mrsph_batch_barrier_selftest(int(device), float(limit_ms), C.byref(raised))
+    if rc != 0:
+        raise L.MrsphError(f"mrsph_batch_barrier_selftest failed ({rc})")
+    return bool(raised.value)

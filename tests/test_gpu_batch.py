@@ -1,11 +1,14 @@
 """Batched relaxation (mrsph_batch_*): a batch of independent 2D and 3D
 geometries of uneven size, stepped together, gives every handle exactly the
-state that stepping it alone gives (both precisions), across a neighbour-list
-capacity check."""
+state that stepping it alone gives (both precisions; FP32-split in the
+persistent, the per-phase and the per-handle-stream modes), across a
+neighbour-list capacity check; the persistent kernel's grid barrier gives up
+after its time limit."""
 import numpy as np
 import pytest
 
 from mrsph import BatchRelaxation, SPHMeshGeneration, cases
+from mrsph.solver import barrier_selftest
 
 pytestmark = pytest.mark.gpu
 
@@ -15,8 +18,9 @@ def _geoms():
             cases.star_shape(3, 8, 2500), cases.disc_hole_2d(spacing=0.02, grid=64)]
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp64"])
-def test_batch_equals_solo(prec):
+@pytest.mark.parametrize("prec,mode", [("fp32", "persistent"), ("fp32", "phases"), ("fp32", "streams"),
+                                       ("fp64", "streams")])
+def test_batch_equals_solo(prec, mode):
     geoms = _geoms()
     steps = 40
     solo = []
@@ -32,6 +36,9 @@ def test_batch_equals_solo(prec):
         g.Initialize_case()
         hs.append(g)
     b = BatchRelaxation(hs)
+    assert b.mode == ("persistent" if prec == "fp32" else "streams")
+    b.set_mode(mode)
+    assert b.mode == mode
     b.SPH_run_mesh_generation(25)
     b.SPH_run_mesh_generation(steps - 25)
     for g, ref in zip(hs, solo):
@@ -72,6 +79,42 @@ def test_batch_then_solo_steps():
     b.SPH_run_mesh_generation(6)
     for g, r in zip(hs, ref):
         assert np.array_equal(g.particles(("xyz",))["xyz"], r)
+    b.close()
+    for g in hs:
+        g.close()
+
+
+def test_batch_kernels_need_fp32_split():
+    hs = []
+    for c in _geoms()[:2]:
+        g = SPHMeshGeneration(c, precision="fp64")
+        g.Initialize_case()
+        hs.append(g)
+    b = BatchRelaxation(hs)
+    assert b.mode == "streams"
+    for mode in ("persistent", "phases"):
+        with pytest.raises(Exception):
+            b.set_mode(mode)
+    b.close()
+    for g in hs:
+        g.close()
+
+
+def test_persistent_barrier_wait_is_bounded():
+    """A barrier that one block of the launch never reaches: the wait gives
+    up after its limit, the kernel returns with its error bit raised, and the
+    device still runs a persistent batch afterwards."""
+    assert barrier_selftest(0, 200.0)
+    hs = []
+    for c in _geoms()[:2]:
+        g = SPHMeshGeneration(c, precision="fp32")
+        g.Initialize_case()
+        hs.append(g)
+    b = BatchRelaxation(hs)
+    assert b.mode == "persistent"
+    b.SPH_run_mesh_generation(3)
+    b.sync()
+    assert all(g.stats()["step"] == 3 for g in hs)
     b.close()
     for g in hs:
         g.close()
