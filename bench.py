@@ -143,14 +143,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str, precision: str, dim: int):
-    """DRAM bytes per particle of a kernel from a committed ncu summary, or None."""
+def ncu_summary(kernel: str, precision: str, dim: int) -> dict:
+    """A kernel's entry of the committed ncu summary (DRAM bytes per particle,
+    issue and FP32-pipe fractions), or {}."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
             d = json.load(f)
-        return d[f"{precision}_{dim}d"][kernel]["dram_bytes_per_particle"]
+        return d[f"{precision}_{dim}d"][kernel]
     except Exception:
-        return None
+        return {}
 
 
 def dist_init():
@@ -476,10 +477,16 @@ def run_mrsph(args, ws, rank, local, dist):
     peak, peak_kind = peaks()
     ach = bytes_[top] / (prof[top] / 1000.0) / 1e9
     step_ach = sum(bytes_.values()) / (ms_step / 1000.0) / 1e9
-    tr = ncu_traffic(top, "fp32", dim)
+    ns = ncu_summary(top, "fp32", dim)
+    tr = ns.get("dram_bytes_per_particle")
     roof = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": ach / peak, "peak_kind": peak_kind,
             "traffic": (tr * n if tr is not None else None),
+            "issue": {"issue_active_frac": ns.get("issue_active_pct", 0.0) / 100.0 or None,
+                      "fp32_fma_pipe_frac": ns.get("fma_pipe_pct", 0.0) / 100.0 or None,
+                      "source": "ncu --set full of the same kernel on the 301,270-particle torus "
+                                "(profiles/density_torus_3d_small.md): the kernel is issue-bound, so its "
+                                "instruction-issue and FP32-pipe fractions bound it, not HBM"},
             "algorithmic_bytes_per_launch": bytes_[top],
             "step_achieved": step_ach, "step_frac": step_ach / peak,
             "step_bytes_per_particle": roofline.total_bytes_per_particle(dim, "fp32")}

@@ -919,12 +919,15 @@ __device__ inline void scan_candidates(const KCtx& c, const int* __restrict__ cs
 // (levels, rows, storage order), so its accepted neighbours and their order
 // do not depend on the mode; lanes also see extra candidates of the union,
 // which the candidate test rejects.
-// load(k) builds the tile entry of candidate k (uniform mode), vtile(j, e)
-// visits it, vglob(j) visits candidate j straight from global memory
-// (per-lane mode).
-template <int D, class R, class LD = LdNC, class E, class FL, class FT, class FG>
+// load(k) builds the tile entry of candidate k (uniform mode),
+// vchunk(t0, m, tile) visits the m candidates t0 .. t0 + m - 1 held in the
+// tile, in that order, vglob(j) visits candidate j straight from global
+// memory (per-lane mode).
+// origin() gives the search origin (built per level from memory rather than
+// held in registers across the scan).
+template <int D, class R, class LD = LdNC, class E, class SO, class FL, class FT, class FG>
 __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, const unsigned* __restrict__ lhmax,
-                                 bool active, const SOrigin<D, R>& so, R hi, E* tile, FL&& load, FT&& vtile,
+                                 bool active, SO&& origin, R hi, E* tile, FL&& load, FT&& vchunk,
                                  FG&& vglob) {
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
@@ -932,7 +935,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
     if (c.sc->lcount[L] == 0) continue;
     int q[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, up[3] = {-1, -1, -1}, hn[3];
     float fr[3] = {0.f, 0.f, 0.f}, hs[3] = {1.f, 1.f, 1.f};
-    const float R = level_origin<D, LD>(c, lhmax, L, so, hi, active, q, fr);
+    const float R = level_origin<D, LD>(c, lhmax, L, origin(), hi, active, q, fr);
     const bool need = R > 0.f;
     if (!__any_sync(FULL, need)) continue;
     const float R2 = R * R;
@@ -994,14 +997,7 @@ __device__ inline void warp_scan(const KCtx& c, const int* __restrict__ cstart, 
             if (k < e0) tile[lane] = load(k);
             __syncwarp();
             const int m = min(32, e0 - t0);
-            if (need) {
-              if (m == 32) {
-#pragma unroll kTileUnroll
-                for (int t = 0; t < 32; t++) vtile(t0 + t, tile[t]);
-              } else {
-                for (int t = 0; t < m; t++) vtile(t0 + t, tile[t]);
-              }
-            }
+            if (need) vchunk(t0, m, (const E*)tile);
             __syncwarp();
           }
         }
@@ -1066,12 +1062,14 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
     a0 = b.rec[2 * i];
     a1 = b.rec[2 * i + 1];
     ti = b.meta[i] & 0xFF;
-    if (ti == SURFACE_P) {
+    if (!F32 && ti == SURFACE_P) {
       const T4 nri = b.nr[i];
       ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
     }
   }
-  const SOrigin<D, R> so(c, active ? b.posh[i] : mk4<R>(0, 0, 0, 0), (active && b.key) ? b.key[i] : 0);
+  auto origin = [&]() {
+    return SOrigin<D, R>(c, active ? b.posh[i] : mk4<R>(0, 0, 0, 0), (active && b.key) ? b.key[i] : 0);
+  };
   const R hi = a0.w;
   const R inv_hi = active ? r_rcp(hi) : (R)0;
   const int kind = KK >= 0 ? KK : c.prm.kernel;
@@ -1085,11 +1083,9 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
   bool unc = false;  // FP32-split: a decision of this particle lies in its band (exact re-decision follows)
   const R R2i = (hi * cut) * (hi * cut);
   int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[(q >> 3) * 256 + (q & 7)]
-  int o = 0;  // offset of entry cnt
   // accepted neighbour j at distance vector dr (i - j), |dr| = dist
   auto accept = [&](int j, const R* dr, R dist, bool surf_j) {
-    if (cnt < w.cap) row[o] = j;
-    o += ((o & 7) == 7) ? 249 : 1;
+    if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = j;
     cnt++;
     if (ti == REAL_P) {
       if constexpr (WEN32) {
@@ -1101,6 +1097,10 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
         ncount++;
       }
     } else if (ti == SURFACE_P && surf_j) {  // surface neighbour of a surface particle
+      if constexpr (F32) {  // the normal is not kept in registers across the scan
+        const T4 nri = b.nr[i];
+        ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
+      }
       R dn = dot3<D, R>(dr, ni);
       R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
       R pd = pair_dist(dot3<D, R>(pr, pr));
@@ -1114,40 +1114,25 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
       }
     }
   };
-  auto vglob = [&](int j) {
-    T4 b0, b1;
-    LD::rec(b.rec, j, b0, b1);
-    R dr[3];
-    Q::rel(c, a0, a1, b0, b1, dr);
-    if constexpr (F32) {
-      const float d2 = d2_of(dr, D);
-      const float rj = b0.w * cut;
-      const float Rm = fmaxf(R2i, rj * rj);
-      if (d2 > Rm * kD2Accept) return;
-      if (d2 >= Rm * kD2Sure) unc = true;
-      accept(j, dr, pair_dist(d2), b1.w < 0.f);
-    } else {
-      R dist;
-      if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
-      accept(j, dr, dist, b1.w < (R)0);
-    }
-  };
   if constexpr (F32) {
-    // warp anchor: lane 0's anchor cell (lane 0 is active whenever any lane is)
+    // Positions relative to the warp's anchor (lane 0's anchor cell; lane 0
+    // is active whenever any lane is), in the tile and in the per-lane path
+    // alike, so the particle's own record is not kept across the scan.
     const float wa[3] = {__shfl_sync(0xffffffffu, (float)a1.x, 0), __shfl_sync(0xffffffffu, (float)a1.y, 0),
                          __shfl_sync(0xffffffffu, (float)a1.z, 0)};
-    const float Af[3] = {c.geo.Af[0], c.geo.Af[1], c.geo.Af[2]};
-    const float pi[3] = {((float)a1.x - wa[0]) * Af[0] + (float)a0.x, ((float)a1.y - wa[1]) * Af[1] + (float)a0.y,
-                         D == 3 ? ((float)a1.z - wa[2]) * Af[2] + (float)a0.z : 0.f};
+    const float pi[3] = {((float)a1.x - wa[0]) * c.geo.Af[0] + (float)a0.x,
+                         ((float)a1.y - wa[1]) * c.geo.Af[1] + (float)a0.y,
+                         D == 3 ? ((float)a1.z - wa[2]) * c.geo.Af[2] + (float)a0.z : 0.f};
     auto load = [&](int k) {
       float4 b0, b1;
       LD::rec(b.rec, k, b0, b1);
       const float rj = b0.w * (float)cut;
       const float r2 = rj * rj;
-      return make_float4((b1.x - wa[0]) * Af[0] + b0.x, (b1.y - wa[1]) * Af[1] + b0.y,
-                         D == 3 ? (b1.z - wa[2]) * Af[2] + b0.z : 0.f, b1.w < 0.f ? -r2 : r2);
+      return make_float4((b1.x - wa[0]) * c.geo.Af[0] + b0.x, (b1.y - wa[1]) * c.geo.Af[1] + b0.y,
+                         D == 3 ? (b1.z - wa[2]) * c.geo.Af[2] + b0.z : 0.f, b1.w < 0.f ? -r2 : r2);
     };
-    auto vtile = [&](int j, const float4& e) {
+    auto vglob = [&](int j) {
+      const float4 e = load(j);
       float dr[3] = {pi[0] - e.x, pi[1] - e.y, D == 3 ? pi[2] - e.z : 0.f};
       const float d2 = d2_of(dr, D);
       const float Rm = fmaxf((float)R2i, fabsf(e.w));
@@ -1155,21 +1140,62 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
       if (d2 >= Rm * kD2Sure) unc = true;
       accept(j, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
     };
-    warp_scan<D, R, LD>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    // A chunk of 32 tile entries in two parts: every entry is tested without
+    // branches into a bit mask, then the lane walks only its own set bits in
+    // ascending order (the candidates' order) to accept them.  Accepting in
+    // the test loop made the whole warp run the accept path for almost every
+    // entry (some lane accepts nearly every candidate), with a third of the
+    // lanes idle.
+    auto test = [&](const float4& e) -> bool {
+      const float dr[3] = {pi[0] - e.x, pi[1] - e.y, D == 3 ? pi[2] - e.z : 0.f};
+      return d2_of(dr, D) <= fmaxf((float)R2i, fabsf(e.w)) * kD2Accept;
+    };
+    auto vchunk = [&](int t0, int m, const float4* tile) {
+      unsigned mask = 0u;
+      if (m == 32) {
+#pragma unroll
+        for (int t = 0; t < 32; t++) mask |= test(tile[t]) ? (1u << t) : 0u;
+      } else {
+        for (int t = 0; t < m; t++) mask |= test(tile[t]) ? (1u << t) : 0u;
+      }
+      while (mask) {
+        const int t = __ffs(mask) - 1;
+        mask &= mask - 1u;
+        const float4 e = tile[t];
+        float dr[3] = {pi[0] - e.x, pi[1] - e.y, D == 3 ? pi[2] - e.z : 0.f};
+        const float d2 = d2_of(dr, D);
+        const float Rm = fmaxf((float)R2i, fabsf(e.w));
+        if (d2 >= Rm * kD2Sure) unc = true;
+        accept(t0 + t, (R*)dr, (R)pair_dist(d2), e.w < 0.f);
+      }
+    };
+    warp_scan<D, R, LD>(c, w.cstart, w.lhmax, active, origin, hi, s_tile[threadIdx.x >> 5], load, vchunk, vglob);
   } else {
+    auto vglob = [&](int j) {
+      T4 b0, b1;
+      LD::rec(b.rec, j, b0, b1);
+      R dr[3];
+      Q::rel(c, a0, a1, b0, b1, dr);
+      R dist;
+      if (!nb_test(d2_of(dr, D), hi, b0.w, c.prm.cutoff, dist)) return;
+      accept(j, dr, dist, b1.w < (R)0);
+    };
     auto load = [&](int k) {
       RecPair<R> e;
       LD::rec(b.rec, k, e.a, e.b);
       return e;
     };
-    auto vtile = [&](int j, const RecPair<R>& e) {
-      R dr[3];
-      Q::rel(c, a0, a1, e.a, e.b, dr);
-      R dist;
-      if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) return;
-      accept(j, dr, dist, e.b.w < (R)0);
+    auto vchunk = [&](int t0, int m, const RecPair<R>* tile) {
+      for (int t = 0; t < m; t++) {
+        const RecPair<R>& e = tile[t];
+        R dr[3];
+        Q::rel(c, a0, a1, e.a, e.b, dr);
+        R dist;
+        if (!nb_test(d2_of(dr, D), hi, e.a.w, c.prm.cutoff, dist)) continue;
+        accept(t0 + t, dr, dist, e.b.w < (R)0);
+      }
     };
-    warp_scan<D, R, LD>(c, w.cstart, w.lhmax, active, so, hi, s_tile[threadIdx.x >> 5], load, vtile, vglob);
+    warp_scan<D, R, LD>(c, w.cstart, w.lhmax, active, origin, hi, s_tile[threadIdx.x >> 5], load, vchunk, vglob);
   }
   if (active) {
     if (WEN32 && ti == REAL_P) {
