@@ -70,6 +70,9 @@ def workload(name: str, precision: str):
         return cases.ellipses_2d(precision=precision)
     if name == "spheres_3d":
         return cases.spheres_3d(precision=precision)
+    if name == "spheres_3d_full":  # four nested level-set levels down to 512^3, about 6.2 M particles
+        return cases.spheres_3d(fine_pkg=128, nlevels=4, dx_min=0.0015, middle_dl=0.0025, dx_max=0.012,
+                                precision=precision)
     raise SystemExit(f"unknown workload {name}")
 
 

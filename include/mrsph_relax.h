@@ -58,6 +58,8 @@ extern "C" {
 #define MRSPH_FLAG_SEED_EXHAUSTED 2  /* a seeding loop hit its attempt limit */
 #define MRSPH_FLAG_LEVEL_CLAMPED 4   /* a particle scale left the planned cell-list levels */
 #define MRSPH_FLAG_NEIGHBOR_SPILL 8  /* a neighbour list exceeded its capacity (handled by re-scan) */
+#define MRSPH_FLAG_CAPACITY_CLAMPED 16 /* host side: the list capacity could not grow to the largest
+                                          list (memory budget or allocation), so lists keep spilling */
 
 /* run_phase selectors (a step is MAP -> BIN -> DENSITY -> FORCE1 -> FORCE2) */
 #define MRSPH_PHASE_MAP 1

@@ -1939,17 +1939,32 @@ class Engine : public EngineBase {
 
   // Reads the largest neighbour count of the last step and grows the list
   // capacity (graphs are rebuilt).  Stays with the re-scan fallback when the
-  // allocation fails or exceeds the budget, or when the caller fixed the cap.
+  // allocation fails or exceeds the budget (half of the device memory free
+  // beside the current lists, at least 48 GB), or when the caller fixed the
+  // cap; a growth that falls short raises MRSPH_FLAG_CAPACITY_CLAMPED in the
+  // next stats.
   int maybe_grow_cap() {
     unsigned mc = 0;
     MR_CK(cudaMemcpyAsync(&mc, &kc_.sc->maxcnt, sizeof(unsigned), cudaMemcpyDeviceToHost, st_));
     MR_CK(cudaStreamSynchronize(st_));
     if ((int)mc <= w_.cap || cfg_.neighbor_cap > 0) return 0;
     long long want = ((long long)mc * 5 / 4 + 31) / 32 * 32;
-    const long long budget = 48ll << 30;  // bytes for the lists and their pair coefficients
     const long long n32 = (n_ + 31) / 32 * 32;  // nb_slot blocks of 32 particles
-    long long maxcap = budget / ((long long)(sizeof(int) + sizeof(R)) * n32) / 8 * 8;
-    if (want > maxcap) want = maxcap;
+    const long long per_entry = (long long)(sizeof(int) + sizeof(R)) * n32;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      free_b = 0;
+    }
+    // the current lists are freed only once the new ones are in place, so the
+    // new ones must fit beside them
+    const long long avail = (long long)free_b + per_entry * w_.cap;
+    const long long budget = std::max(48ll << 30, std::min(avail / 2, (long long)free_b));  // lists + pair coefficients
+    long long maxcap = budget / per_entry / 8 * 8;
+    if (want > maxcap) {
+      want = maxcap;
+      cap_clamped_ = true;
+    }
     if (want <= w_.cap) return 0;
     int* nb = nullptr;
     R* pc = nullptr;
@@ -1958,7 +1973,11 @@ class Engine : public EngineBase {
       e = cudaMalloc(&pc, sizeof(R) * (size_t)want * n32);
       if (e != cudaSuccess) cudaFree(nb);
     }
-    if (e != cudaSuccess) { cudaGetLastError(); return 0; }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      cap_clamped_ = true;
+      return 0;
+    }
     for (auto& p : allocs_) {
       if (p == w_.nbl) { cudaFree(p); p = nb; }
       else if (p == w_.pc) { cudaFree(p); p = pc; }
@@ -2028,7 +2047,8 @@ class Engine : public EngineBase {
     o->pairs = (long long)h.pairs;
     o->pairs_total = (long long)h.pairs_total;
     o->remapped = h.remap;
-    o->flags = (int)h.flags;
+    o->flags = (int)h.flags | (cap_clamped_ ? MRSPH_FLAG_CAPACITY_CLAMPED : 0);
+    cap_clamped_ = false;
     o->num_cell_levels = kc_.geo.ncl;
     o->num_cells = kc_.geo.hoff[kc_.geo.ncl];
     o->max_phi = kc_.ls.max_phi;
@@ -2477,6 +2497,7 @@ class Engine : public EngineBase {
   std::vector<void*> anc_allocs_;  // anchor tables, kept across re-allocations
   int init_rc_ = 0;
   int sms_ = 1;  // multiprocessors of the engine's device
+  bool cap_clamped_ = false;  // a list-capacity growth fell short since the last stats
 };
 
 }  // namespace mrsph

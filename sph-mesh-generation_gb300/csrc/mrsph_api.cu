@@ -100,7 +100,9 @@ static int plan_levels(mrsph_handle* h) {
   g.off[num_level] = off;
   g.hoff[num_level] = hoff;
   g.nc0 = (long long)g.n[0][0] * g.n[0][1] * g.n[0][2];
-  if (hoff > (1ll << 28)) return fail(h, MRSPH_ERR_RANGE, "more than 2^25 (3D) / 2^26 (2D) cell-list cells");
+  // cell keys are 32-bit: the half-cell table (counts + starts, 8 bytes per
+  // entry; 1.06 G entries for four levels down to 480^3 cells) must index in int
+  if (hoff > 2147483000ll) return fail(h, MRSPH_ERR_RANGE, "more than 2^31 half cells over the cell-list levels");
   const int lm = num_level - 1;
   for (int d = 0; d < 3; d++) {
     g.A[d] = g.dcell[lm][d];

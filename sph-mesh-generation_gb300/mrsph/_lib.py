@@ -20,6 +20,7 @@ REAL, SURFACE, SINGULARITY, SEGMENT = 0, 1, 2, 3
 PHASE_MAP, PHASE_BIN, PHASE_DENSITY, PHASE_FORCE1, PHASE_FORCE2 = 1, 2, 3, 4, 5
 TIMERS = ("map", "scan", "sort", "reorder", "density", "force1", "force2")
 FLAG_REMAP_EXHAUSTED, FLAG_SEED_EXHAUSTED, FLAG_LEVEL_CLAMPED, FLAG_NEIGHBOR_SPILL = 1, 2, 4, 8
+FLAG_CAPACITY_CLAMPED = 16
 
 
 class Params(C.Structure):

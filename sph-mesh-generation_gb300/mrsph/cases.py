@@ -87,9 +87,15 @@ def cell_centres(box_l, dpkg, num_pkg, margin, dim):
     return axes
 
 
-def make_level(sdf: Callable, dim: int, box_l, dpkg, num_pkg, margin: int = 1) -> LevelGrid:
+def make_level(sdf: Callable, dim: int, box_l, dpkg, num_pkg, margin: int = 1, broadcast: bool = False) -> LevelGrid:
+    """phi of one level at the cell centres; broadcast=True hands sdf the
+    axes as broadcastable (1, 1, nx), (1, ny, 1), (nz, 1, 1) arrays instead
+    of full meshgrids."""
     ax = cell_centres(box_l, dpkg, num_pkg, margin, dim)
-    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    if broadcast:
+        X, Y, Z = ax[0][None, None, :], ax[1][None, :, None], ax[2][:, None, None]
+    else:
+        Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
     phi = np.ascontiguousarray(sdf(X, Y, Z), dtype=np.float64)
     return LevelGrid(list(box_l), list(dpkg), list(num_pkg), margin, phi, None)
 
@@ -119,17 +125,50 @@ def curvature_estimate(lv: LevelGrid, dim: int) -> np.ndarray:
     """|curvature| of phi on the cells next to the interface (0 elsewhere) by
     the level-set build's difference formulas, clamped to 2 / |cell|; the
     interface test is a sign change over the 3^D neighbourhood.  Used only to
-    count particles under the curvature law."""
+    count particles under the curvature law.  The interface cells are found
+    first and the differences evaluated there only (the grid's outermost two
+    cells are never interface cells: they are margin cells far from phi = 0)."""
     ph = lv.phi if dim == 3 else lv.phi[0]
     dc = [lv.dpkg[d] / 4.0 for d in range(dim)]
     ax = list(range(dim))[::-1]  # array axis of coordinate d
-    def sh(a, d, k):
-        return np.roll(a, -k, axis=ax[d])
-    g1 = [(8.0 * (sh(ph, d, 1) - sh(ph, d, -1)) - (sh(ph, d, 2) - sh(ph, d, -2))) / dc[d] / 12.0 for d in range(dim)]
-    g2 = [(sh(ph, d, 1) - 2 * ph + sh(ph, d, -1)) / dc[d] / dc[d] for d in range(dim)]
+    shape = ph.shape
+    # sign change over the axis neighbours: min / max of the cell and its 2D
+    # neighbours along the axes (array edges compare with themselves)
+    lo = ph.copy()
+    hi = ph.copy()
+    for d in range(dim):
+        a = ax[d]
+        for k in (-1, 1):
+            sl_dst = [slice(None)] * ph.ndim
+            sl_src = [slice(None)] * ph.ndim
+            if k == 1:
+                sl_dst[a], sl_src[a] = slice(0, -1), slice(1, None)
+            else:
+                sl_dst[a], sl_src[a] = slice(1, None), slice(0, -1)
+            np.minimum(lo[tuple(sl_dst)], ph[tuple(sl_src)], out=lo[tuple(sl_dst)])
+            np.maximum(hi[tuple(sl_dst)], ph[tuple(sl_src)], out=hi[tuple(sl_dst)])
+    cut = (lo < 0) & (hi > 0)
+    del lo, hi
+    idx = np.flatnonzero(cut)
+    coords = np.unravel_index(idx, shape)
+    inner = np.ones(idx.shape, dtype=bool)
+    for a in range(ph.ndim):
+        inner &= (coords[a] >= 2) & (coords[a] < shape[a] - 2)
+    idx = idx[inner]
+    flat = ph.ravel()
+    stride = [int(np.prod(shape[a + 1:])) for a in range(ph.ndim)]
+
+    def sh(d, k):  # phi at offset k along coordinate d of the interface cells
+        return flat[idx + k * stride[ax[d]]]
+
+    def sh2(a_, ka, b_, kb):
+        return flat[idx + ka * stride[ax[a_]] + kb * stride[ax[b_]]]
+    p0 = flat[idx]
+    g1 = [(8.0 * (sh(d, 1) - sh(d, -1)) - (sh(d, 2) - sh(d, -2))) / dc[d] / 12.0 for d in range(dim)]
+    g2 = [(sh(d, 1) - 2 * p0 + sh(d, -1)) / dc[d] / dc[d] for d in range(dim)]
+
     def mixed(a, b):
-        return 0.25 * (sh(sh(ph, a, 1), b, 1) - sh(sh(ph, a, -1), b, 1) - sh(sh(ph, a, 1), b, -1)
-                       + sh(sh(ph, a, -1), b, -1)) / dc[a] / dc[b]
+        return 0.25 * (sh2(a, 1, b, 1) - sh2(a, -1, b, 1) - sh2(a, 1, b, -1) + sh2(a, -1, b, -1)) / dc[a] / dc[b]
     if dim == 2:
         px, py = g1
         pxx, pyy = g2
@@ -147,14 +186,8 @@ def curvature_estimate(lv: LevelGrid, dim: int) -> np.ndarray:
         c = np.where(den > 0, num / den, 0.0)
     cd = np.sqrt(sum(v * v for v in dc))
     c = np.abs(np.clip(c, -2.0 / cd, 2.0 / cd))
-    lo = ph.copy()
-    hi = ph.copy()
-    for d in range(dim):
-        for k in (-1, 1):
-            lo = np.minimum(lo, sh(ph, d, k))
-            hi = np.maximum(hi, sh(ph, d, k))
-    cut = (lo < 0) & (hi > 0)
-    out = np.where(cut, c, 0.0)
+    out = np.zeros(ph.size)
+    out[idx] = c
     return out.reshape(lv.phi.shape)
 
 
@@ -317,9 +350,28 @@ def spheres_3d(n_spheres: int = 32, seed: int = 7, dx_min: float = 0.0025, dx_ma
     c = rng.random((n_spheres, 3))
 
     def sdf(X, Y, Z):
-        out = np.full(X.shape, -1.0e9)
+        # X, Y, Z broadcastable axes; each sphere adds ((x-cx)^2 + (y-cy)^2) +
+        # (z-cz)^2 in that order, square root, r - d, running maximum
+        # slabs of z planes small enough to stay in cache, operations in place
+        shape = np.broadcast_shapes(np.shape(X), np.shape(Y), np.shape(Z))
+        out = np.full(shape, -1.0e9)
+        nz = shape[0]
+        plane = int(np.prod(shape[1:]))
+        step = max(1, (1 << 21) // max(plane, 1))
+        zs = np.broadcast_to(Z, (nz, 1, 1))
+        ys = np.broadcast_to(Y, (1,) + (shape[1], 1))
         for (cx, cy, cz), rk in zip(c, r):
-            np.maximum(out, rk - np.sqrt((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2), out=out)
+            dx = X - cx
+            dy = ys - cy
+            dxy = dx * dx + dy * dy  # (1, ny, nx)
+            dz = zs - cz
+            dz2 = dz * dz
+            for z0 in range(0, nz, step):
+                z1 = min(nz, z0 + step)
+                tmp = dxy + dz2[z0:z1]
+                np.sqrt(tmp, out=tmp)
+                np.subtract(rk, tmp, out=tmp)
+                np.maximum(out[z0:z1], tmp, out=out[z0:z1])
         return out
 
     p = default_params(3)
@@ -335,7 +387,7 @@ def spheres_3d(n_spheres: int = 32, seed: int = 7, dx_min: float = 0.0025, dx_ma
     for l in range(nlevels):
         f = 1 << l
         dp = dpkg0 / f
-        lv = make_level(sdf, 3, box_l, [dp, dp, dp], [npx0 * f] * 3)
+        lv = make_level(sdf, 3, box_l, [dp, dp, dp], [npx0 * f] * 3, broadcast=True)
         if l > 0:
             lv.active = nested_active(lv, 4.0 * (dp * 2 / 4.0), 3)
         levels.append(lv)
