@@ -170,6 +170,26 @@ int mrsph_last_error(mrsph_handle* h, char* buf, size_t len);
  * copies phi to the device and builds normals, cut-cell tags, curvature and
  * maximum phi there.  nlevels <= 4, finest last. */
 int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level* levels);
+/* The geometry's characteristic points and segments (Levelset::singularity,
+ * ::segment, level_set.h:37-41; the counts and coordinates that Levelset's
+ * restart file carries, level_set.cpp:1053-1070).  sing holds nsing points
+ * as (x, y, z) and seg holds nseg segments as (x1, y1, z1, x2, y2, z2); z is
+ * ignored in 2D.  Must come before mrsph_set_levelset.  That call then tags
+ * each level's characteristic cells on the device: Get_singularity_tag
+ * (lset_package.cpp:515-555), where the interface cell (tag not NORMAL)
+ * whose centre is nearest each point, among the cells of the point's
+ * package, becomes a SINGULARITY cell, and Get_segment_tag
+ * (lset_package.cpp:559-585), where every other interface cell whose box a
+ * segment meets becomes a SEGMENT cell (the first such segment).  Particles in those cells are mapped onto the
+ * point (MRSPH_SINGULARITY) or the segment's line (MRSPH_SEGMENT), as in
+ * particle_mesh_generation.cpp:439-465.  Counts up to 2^20 each; both zero
+ * clears them. */
+int mrsph_set_characteristics(mrsph_handle* h, int nsing, const double* sing, int nseg, const double* seg);
+/* Tap: the characteristic tag of every cell of one level (sized like phi):
+ * 0 for a NORMAL cell, k + 1 for a SEGMENT cell of segment k, -(k + 1) for
+ * the SINGULARITY cell of point k (tag_characteristic and
+ * idx_characteristic of Levelset_cell, in one int). */
+int mrsph_get_characteristics(mrsph_handle* h, int level, int* chr);
 /* Tap: the device-built fields of one level (arrays sized like phi; NULL skips). */
 int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, double* nz, double* curv,
                        unsigned char* tag, double* max_phi);

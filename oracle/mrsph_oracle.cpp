@@ -202,6 +202,8 @@ struct orc_level {
   double* curv;
   int* tag;         // tag_interface: NORMAL_CELL / CUT_CELL
   const uint8_t* active;  // per package incl. margins (NULL = all active)
+  int* chr;         // [ntot] tag_characteristic (NORMAL / SINGULARITY_CELL / SEGMENT_CELL), or NULL
+  int* chr_idx;     // [ntot] idx_characteristic (-1 without), or NULL
 };
 
 struct orc_ctx {
@@ -228,6 +230,13 @@ struct orc_ctx {
   // orc_ls_build results by the caller)
   int scale_law;
   double middle_dl, max_curv, min_curv;
+  // characteristic points and segments of the geometry (Levelset::singularity,
+  // Levelset::segment, read with the level set, level_set.cpp:1100-1125):
+  // sing[3 * nsing], seg[6 * nseg] (first point, second point)
+  int nsing;
+  const double* sing;
+  int nseg;
+  const double* seg;
 };
 
 struct orc_state {
@@ -401,6 +410,111 @@ void ls_build(orc_level& L, double* max_phi) {
 }
 
 // ---------------------------------------------------------------------------
+// Characteristic cells of one level (Levelset_package::Get_singularity_tag,
+// lset_package.cpp:515-556; Get_segment_tag, :560-590;
+// is_Segment_intersec_AABB, :594-619), after the interface tags.  A
+// singularity tags, in every interior package whose half-open box holds it
+// (is_in_current_pkg: 0 < x - corner < dpkg + 1e-10 per axis), the interface
+// cell (tag_interface != NORMAL) nearest to it, cell centres at
+// pkg dpkg + (cell + 0.5) dcell + box_l; equal distances go to the first cell
+// in (i, j, k) loop order (the reference sorts with std::sort, whose order
+// of equal keys is unspecified).  A segment tags every other interface cell
+// whose box it meets, the first segment in order winning.  Points and
+// segments are 3-vectors (z = 0 in 2D, where the AABB test reduces to its
+// 2D separating axes).
+// ---------------------------------------------------------------------------
+enum { CHAR_NORMAL = 0, CHAR_SINGULARITY = 1, CHAR_SEGMENT = 2 };  // glbparam.h:48-51
+
+inline bool segment_meets_box(const double* p1, const double* p2, const double* mn, const double* mx) {
+  const double EPSILON = 1.e-20;
+  double d[3], e[3], cc[3], ad[3];
+  for (int k = 0; k < 3; k++) {
+    d[k] = (p2[k] - p1[k]) * 0.5;
+    e[k] = (mx[k] - mn[k]) * 0.5;
+    cc[k] = (p1[k] + d[k]) - (mx[k] + mn[k]) * 0.5;
+    ad[k] = std::fabs(d[k]);
+  }
+  for (int k = 0; k < 3; k++)
+    if (std::fabs(cc[k]) > e[k] + ad[k]) return false;
+  if (std::fabs(d[1] * cc[2] - d[2] * cc[1]) > e[1] * ad[2] + e[2] * ad[1] + EPSILON) return false;
+  if (std::fabs(d[2] * cc[0] - d[0] * cc[2]) > e[2] * ad[0] + e[0] * ad[2] + EPSILON) return false;
+  if (std::fabs(d[0] * cc[1] - d[1] * cc[0]) > e[0] * ad[1] + e[1] * ad[0] + EPSILON) return false;
+  return true;
+}
+
+template <int D>
+void ls_characteristics(const orc_ctx& c, orc_level& L) {
+  if (!L.chr || !L.chr_idx) return;
+  const int n0 = ls_ncell(L, 0), n1 = ls_ncell(L, 1), n2 = (D == 3) ? ls_ncell(L, 2) : 1;
+  const long long ntot = (long long)n0 * n1 * n2;
+  for (long long a = 0; a < ntot; a++) { L.chr[a] = CHAR_NORMAL; L.chr_idx[a] = -1; }
+  double dc[3] = {ls_dcell(L, 0), ls_dcell(L, 1), (D == 3) ? ls_dcell(L, 2) : 0.0};
+  auto cell_of_pkg = [&](const int* pk, const int* ce) {
+    return ls_index(L, D, 4 * pk[0] + ce[0], 4 * pk[1] + ce[1], (D == 3) ? 4 * pk[2] + ce[2] : 0);
+  };
+  for (int ic = 0; ic < c.nsing; ic++) {
+    const double* p = c.sing + 3 * ic;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      int q = (int)std::floor((p[d] - L.box_l[d]) / L.dpkg[d]);
+      lo[d] = IMAX1(0, q - 1);
+      hi[d] = IMIN1(L.num_pkg[d] - 1, q + 1);
+    }
+    for (int pi = lo[0]; pi <= hi[0]; pi++)
+      for (int pj = lo[1]; pj <= hi[1]; pj++)
+        for (int pk_ = lo[2]; pk_ <= hi[2]; pk_++) {
+          const int pk[3] = {pi, pj, pk_};
+          bool inside = true;
+          for (int d = 0; d < D; d++) {
+            const double corner = pk[d] * L.dpkg[d] + L.box_l[d];
+            const double dr = p[d] - corner;
+            inside = inside && dr < L.dpkg[d] + 1.e-10 && dr > 0.;
+          }
+          if (!inside) continue;
+          double best = 0.0;
+          long long besta = -1;
+          for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+              for (int k = 0; k < ((D == 3) ? 4 : 1); k++) {
+                const int ce[3] = {i, j, k};
+                const long long a = cell_of_pkg(pk, ce);
+                if (L.tag[a] == NORMAL_CELL) continue;
+                double dist = 0.0;
+                for (int d = 0; d < D; d++) {
+                  const double cp = (pk[d] * L.dpkg[d] + (ce[d] + 0.5) * dc[d]) + L.box_l[d];
+                  dist += (cp - p[d]) * (cp - p[d]);
+                }
+                dist = std::sqrt(dist);
+                if (besta < 0 || dist < best) { best = dist; besta = a; }
+              }
+          if (besta >= 0) { L.chr[besta] = CHAR_SINGULARITY; L.chr_idx[besta] = ic; }
+        }
+  }
+  if (c.nseg <= 0) return;
+  for (int pk2 = 0; pk2 < ((D == 3) ? L.num_pkg[2] : 1); pk2++)
+    for (int pk1 = 0; pk1 < L.num_pkg[1]; pk1++)
+      for (int pk0 = 0; pk0 < L.num_pkg[0]; pk0++)
+        for (int i = 0; i < 4; i++)
+          for (int j = 0; j < 4; j++)
+            for (int k = 0; k < ((D == 3) ? 4 : 1); k++) {
+              const int pk[3] = {pk0, pk1, pk2}, ce[3] = {i, j, k};
+              const long long a = cell_of_pkg(pk, ce);
+              if (L.tag[a] == NORMAL_CELL || L.chr[a] == CHAR_SINGULARITY) continue;
+              double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+              for (int d = 0; d < D; d++) {
+                mn[d] = (pk[d] * L.dpkg[d] + ce[d] * dc[d]) + L.box_l[d];
+                mx[d] = mn[d] + dc[d];
+              }
+              for (int is = 0; is < c.nseg; is++)
+                if (segment_meets_box(c.seg + 6 * is, c.seg + 6 * is + 3, mn, mx)) {
+                  L.chr[a] = CHAR_SEGMENT;
+                  L.chr_idx[a] = is;
+                  break;
+                }
+            }
+}
+
+// ---------------------------------------------------------------------------
 // Nested level choice (build extension for reference quirk Q9: the reference
 // has one level-set level).  The finest level whose interior box contains the
 // point and whose package there is active is used; level 0 otherwise.
@@ -478,7 +592,7 @@ void sample(const orc_ctx& c, const double* x, double* phi, double* n, double* c
 // Get_level_set_char_cell_tag_and_idx, particle_mesh_generation.cpp:552-573,
 // via Levelset_levelinfo::Get_id_pkg_cell, lset_level_infor.cpp:350-366.
 template <int D>
-int cell_tag(const orc_ctx& c, const double* x) {
+int cell_tag(const orc_ctx& c, const double* x, int* chr = nullptr, int* chr_idx = nullptr) {
   const orc_level& L = c.ls[ls_pick<D>(c, x)];
   int g[3] = {0, 0, 0};
   for (int d = 0; d < D; d++) {
@@ -491,7 +605,10 @@ int cell_tag(const orc_ctx& c, const double* x) {
     ci = IMAX1(0, IMIN1(ci, 3));
     g[d] = p * 4 + ci;
   }
-  return L.tag[ls_index(L, D, g[0], g[1], g[2])];
+  const long long a = ls_index(L, D, g[0], g[1], g[2]);
+  if (chr) *chr = L.chr ? L.chr[a] : CHAR_NORMAL;
+  if (chr_idx) *chr_idx = L.chr_idx ? L.chr_idx[a] : -1;
+  return L.tag[a];
 }
 
 // Levelset::Get_scale, level_set.cpp:311-351.  Law 0: the active tanh law.
@@ -571,15 +688,16 @@ bool remap(const orc_ctx& c, orc_state& s, long long i) {
 // ---------------------------------------------------------------------------
 // A3: Particle_mesh_generation::Find_and_map_particle :408-467 plus the
 // driver loop sph_mesh_generation.cpp:1506-1545 (dispersal, re-sample,
-// re-seed of REAL particles with phi < 0).  No characteristic
-// (segment/singularity) cells exist in any configured level set, so
-// tag_characteristic is always NORMAL_CELL.
+// re-seed of REAL particles with phi < 0).  A particle in a characteristic
+// cell (ls_characteristics) goes onto the segment's line or the point; with
+// no characteristic points or segments every cell is NORMAL.
 // ---------------------------------------------------------------------------
 template <int D>
 void map_particle(const orc_ctx& c, orc_state& s, long long i, long long* nremap) {
   double x[3];
   get_xyz<D>(s, i, x);
-  int tag = cell_tag<D>(c, x);
+  int chr = CHAR_NORMAL, cidx = -1;
+  int tag = cell_tag<D>(c, x, &chr, &cidx);
   int t = s.type[i];
   double nrm[3] = {s.nx[i], s.ny[i], s.nz[i]};
   double phi = s.phi[i];
@@ -590,7 +708,7 @@ void map_particle(const orc_ctx& c, orc_state& s, long long i, long long* nremap
     if (D == 3) d += nrm[2] * nrm[2];
     return std::sqrt(d);
   };
-  if (tag == CUT_CELL && (t == REAL_PARTICLE || t == SURFACE_PARTICLE)) {
+  if (tag == CUT_CELL && (t == REAL_PARTICLE || t == SURFACE_PARTICLE) && chr == CHAR_NORMAL) {
     t = SURFACE_PARTICLE;
     double dist = std::fabs(phi);
     double div = 1.0 / (nlen() + 1.0e-15);
@@ -599,11 +717,30 @@ void map_particle(const orc_ctx& c, orc_state& s, long long i, long long* nremap
       double n_d = phi < 0.0 ? nn : -nn;
       x[d] = x[d] + n_d * dist;
     }
+  } else if (chr == CHAR_SEGMENT && cidx >= 0) {
+    // projection onto the segment's line, particle_mesh_generation.cpp:439-455
+    t = SEGMENT_PARTICLE;
+    const double* p1 = c.seg + 6 * cidx;
+    const double* p2 = p1 + 3;
+    double P[3] = {0, 0, 0}, N[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) { P[d] = p2[d] - p1[d]; N[d] = x[d] - p1[d]; }
+    double len = 0.0;
+    len += P[0] * P[0]; len += P[1] * P[1]; if (D == 3) len += P[2] * P[2];
+    len = std::sqrt(len);
+    const double inv = 1. / AMAX1(len, 1.e-15);
+    double e[3] = {P[0] * inv, P[1] * inv, (D == 3) ? P[2] * inv : 0.0};
+    double dist = 0.0;
+    dist += N[0] * e[0]; dist += N[1] * e[1]; if (D == 3) dist += N[2] * e[2];
+    for (int d = 0; d < D; d++) x[d] = p1[d] + e[d] * dist;
+  } else if (chr == CHAR_SINGULARITY && cidx >= 0) {
+    // particle_mesh_generation.cpp:456-465
+    t = SINGULARITY_PARTICLE;
+    for (int d = 0; d < D; d++) x[d] = c.sing[3 * cidx + d];
   } else {
     t = REAL_PARTICLE;
   }
   s.type[i] = t;
-  if (t == SURFACE_PARTICLE) {
+  if (t == SURFACE_PARTICLE || t == SEGMENT_PARTICLE) {
     // Get_dispersed_position(0.00001*h), particle_mesh_generation.cpp:385-404
     double dx = 0.00001 * s.h[i];
     double div = 1.0 / (nlen() + 1.0e-15);
@@ -808,6 +945,28 @@ void density(const orc_ctx& c, orc_state& s, const Neighbors& nb) {
           sum += kernel_W(c.kernel, D - 1, dist, s.h[i]);
           ncount++;
         }
+      } else if (ti == SEGMENT_PARTICLE && D == 3) {
+        // :740-759: segment and singularity neighbours with the 1D kernel
+        double dn = 0.0;
+        dn += vec[0] * ni[0]; dn += vec[1] * ni[1]; if (D == 3) dn += vec[2] * ni[2];
+        double dr[3];
+        for (int d = 0; d < 3; d++) dr[d] = vec[d] - ni[d] * dn;
+        double dist = 0.0;
+        dist += dr[0] * dr[0]; dist += dr[1] * dr[1]; if (D == 3) dist += dr[2] * dr[2];
+        dist = std::sqrt(dist);
+        int tj = s.type[j];
+        if (tj == SEGMENT_PARTICLE) {
+          double nj[3] = {s.nx[j], s.ny[j], s.nz[j]};
+          double ca = 0.0;
+          ca += ni[0] * nj[0]; ca += ni[1] * nj[1]; if (D == 3) ca += ni[2] * nj[2];
+          if (std::fabs(ca) > cos_t) {
+            sum += kernel_W(c.kernel, 1, dist, s.h[i]);
+            ncount++;
+          }
+        } else if (tj == SINGULARITY_PARTICLE) {
+          sum += kernel_W(c.kernel, 1, dist, s.h[i]);
+          ncount++;
+        }
       }
     }
     if (ncount > 1) sum = 1. / (sum + 1.e-15);
@@ -834,11 +993,14 @@ void force_stage(const orc_ctx& c, orc_state& s, const Neighbors& nb, int stage)
     double v[3] = {s.vx[i], s.vy[i], (D == 3) ? s.vz[i] : 0.0};
     double rho = s.rho[i], h = s.h[i], sum = s.sum[i], nu = s.nu[i];
     double P = 1.0, mass_j = 1.0, P_j = 1.0, sigma = 1.;
-    if (ti == REAL_PARTICLE || ti == SURFACE_PARTICLE) {
+    if (ti == REAL_PARTICLE || ti == SURFACE_PARTICLE || ti == SEGMENT_PARTICLE) {
       for (long long q = nb.off[i]; q < nb.off[i + 1]; q++) {
         int j = nb.nb[q];
         int tj = s.type[j];
         if (ti == SURFACE_PARTICLE && tj == REAL_PARTICLE) continue;
+        // Accumulate_particle_force_seg, :769-879: segment and singularity
+        // neighbours only, the 1D kernel gradient in 3D (none in 2D)
+        if (ti == SEGMENT_PARTICLE && (tj == REAL_PARTICLE || tj == SURFACE_PARTICLE)) continue;
         if (s.id[i] == s.id[j]) continue;
         double h_j = s.h[j], rho_j = s.rho[j], nu_j = s.nu[j];
         double vj[3] = {s.vx[j], s.vy[j], (D == 3) ? s.vz[j] : 0.0};
@@ -857,13 +1019,15 @@ void force_stage(const orc_ctx& c, orc_state& s, const Neighbors& nb, int stage)
           for (int d = 0; d < 3; d++) dr[d] = vec[d] - ni[d] * dn;
           dist += dr[0] * dr[0]; dist += dr[1] * dr[1]; if (D == 3) dist += dr[2] * dr[2];
           dist = std::sqrt(dist);
-          if (tj == SURFACE_PARTICLE) {
+          if ((ti == SURFACE_PARTICLE && tj == SURFACE_PARTICLE) ||
+              (ti == SEGMENT_PARTICLE && tj == SEGMENT_PARTICLE)) {
             double nj[3] = {s.nx[j], s.ny[j], s.nz[j]};
             double ca = 0.0;
             ca += ni[0] * nj[0]; ca += ni[1] * nj[1]; if (D == 3) ca += ni[2] * nj[2];
             if (std::fabs(ca) <= cos_t) continue;
           }
-          aw = kernel_dW(c.kernel, D - 1, dist, 0.5 * (h + h_j));
+          if (ti == SEGMENT_PARTICLE) aw = (D == 3) ? kernel_dW(c.kernel, 1, dist, 0.5 * (h + h_j)) : 0.0;
+          else aw = kernel_dW(c.kernel, D - 1, dist, 0.5 * (h + h_j));
         }
         double awax[3] = {dr[0] * aw, dr[1] * aw, dr[2] * aw};
         if (stage == 1) {
@@ -878,11 +1042,11 @@ void force_stage(const orc_ctx& c, orc_state& s, const Neighbors& nb, int stage)
       }
     }
     double a[3] = {0, 0, 0};
-    if (ti == REAL_PARTICLE || ti == SURFACE_PARTICLE) {
+    if (ti == REAL_PARTICLE || ti == SURFACE_PARTICLE || ti == SEGMENT_PARTICLE) {
       for (int d = 0; d < D; d++) a[d] = F1[d] + F2[d];
       if (stage == 2)
         for (int d = 0; d < D; d++) a[d] = a[d] + v[d] * c.damp_coeff;
-      if (ti == SURFACE_PARTICLE) {
+      if (ti == SURFACE_PARTICLE || ti == SEGMENT_PARTICLE) {  // Map_surface_particle_force
         double nf = 0.0;
         nf += a[0] * ni[0]; nf += a[1] * ni[1]; if (D == 3) nf += a[2] * ni[2];
         for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
@@ -1080,6 +1244,13 @@ int orc_define_levels(orc_ctx* c) {
 int orc_ls_build(orc_ctx* c, int level, double* max_phi) {
   if (c->dim == 2) ls_build<2>(c->ls[level], max_phi);
   else ls_build<3>(c->ls[level], max_phi);
+  return 0;
+}
+
+// characteristic cells of a built level (needs chr / chr_idx buffers)
+int orc_ls_characteristics(orc_ctx* c, int level) {
+  if (c->dim == 2) ls_characteristics<2>(*c, c->ls[level]);
+  else ls_characteristics<3>(*c, c->ls[level]);
   return 0;
 }
 

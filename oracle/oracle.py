@@ -59,7 +59,8 @@ def build(force: bool = False, native: bool = None) -> str:
 class OrcLevel(C.Structure):
     _fields_ = [("box_l", C.c_double * 3), ("dpkg", C.c_double * 3), ("num_pkg", C.c_int * 3),
                 ("margin", C.c_int), ("phi", C.c_void_p), ("nx", C.c_void_p), ("ny", C.c_void_p),
-                ("nz", C.c_void_p), ("curv", C.c_void_p), ("tag", C.c_void_p), ("active", C.c_void_p)]
+                ("nz", C.c_void_p), ("curv", C.c_void_p), ("tag", C.c_void_p), ("active", C.c_void_p),
+                ("chr", C.c_void_p), ("chr_idx", C.c_void_p)]
 
 
 class OrcCtx(C.Structure):
@@ -71,7 +72,8 @@ class OrcCtx(C.Structure):
                 ("max_scale", C.c_double), ("min_scale", C.c_double), ("ini_num_cell", C.c_int * 3),
                 ("cl_dcell", (C.c_double * 3) * 16), ("cl_ncell", (C.c_int * 3) * 16),
                 ("cl_scale", C.c_double * 16), ("scale_law", C.c_int), ("middle_dl", C.c_double),
-                ("max_curv", C.c_double), ("min_curv", C.c_double)]
+                ("max_curv", C.c_double), ("min_curv", C.c_double),
+                ("nsing", C.c_int), ("sing", C.c_void_p), ("nseg", C.c_int), ("seg", C.c_void_p)]
 
 
 _DBL_FIELDS = ["x", "y", "z", "vx", "vy", "vz"]
@@ -116,6 +118,7 @@ def lib():
         L = C.CDLL(build())
         L.orc_define_levels.argtypes = [C.POINTER(OrcCtx)]
         L.orc_ls_build.argtypes = [C.POINTER(OrcCtx), C.c_int, C.POINTER(C.c_double)]
+        L.orc_ls_characteristics.argtypes = [C.POINTER(OrcCtx), C.c_int]
         L.orc_kernel_W.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_void_p, C.c_double, C.c_void_p]
         L.orc_kernel_dW.argtypes = L.orc_kernel_W.argtypes
         L.orc_get_scale.argtypes = [C.POINTER(OrcCtx), C.c_double, C.c_double]
@@ -211,6 +214,13 @@ class Oracle:
             c.box_l[d] = p["box_l"][d]
             c.box_r[d] = p["box_r"][d]
         c.seed = p["seed"]
+        # characteristic points and segments (3-vectors; z = 0 in 2D)
+        sing = np.ascontiguousarray(case.extra.get("singularities", np.zeros((0, 3))), dtype=np.float64).reshape(-1, 3)
+        seg = np.ascontiguousarray(case.extra.get("segments", np.zeros((0, 6))), dtype=np.float64).reshape(-1, 6)
+        self.characteristics = {"singularities": sing, "segments": seg}
+        c.nsing, c.sing = len(sing), (_p(sing) if len(sing) else None)
+        c.nseg, c.seg = len(seg), (_p(seg) if len(seg) else None)
+        has_chr = len(sing) > 0 or len(seg) > 0
         # level-set levels
         self._keep = []
         levels = case.levels
@@ -230,6 +240,12 @@ class Oracle:
             f["tag"] = np.zeros(phi.shape, dtype=np.int32)
             for k in ("phi", "nx", "ny", "nz", "curv", "tag"):
                 setattr(L, k, _p(f[k]))
+            if has_chr:
+                f["chr"] = np.zeros(phi.shape, dtype=np.int32)
+                f["chr_idx"] = np.full(phi.shape, -1, dtype=np.int32)
+                L.chr, L.chr_idx = _p(f["chr"]), _p(f["chr_idx"])
+            else:
+                L.chr, L.chr_idx = None, None
             if lv.active is not None:
                 act = np.ascontiguousarray(lv.active, dtype=np.uint8).ravel()
                 f["active"] = act
@@ -248,6 +264,8 @@ class Oracle:
         for i in range(len(levels)):
             m = C.c_double(0.0)
             lib().orc_ls_build(C.byref(c), i, C.byref(m))
+            if has_chr:
+                lib().orc_ls_characteristics(C.byref(c), i)
             mp = max(mp, m.value)
             a_, b_ = C.c_double(0.0), C.c_double(0.0)
             lib().orc_ls_curv_range(C.byref(c), i, C.byref(a_), C.byref(b_))

@@ -483,25 +483,33 @@ __device__ inline void map_block(const KCtx& c, const Buf<R>& b, int* counts, un
         ls_sample<D, R>(c.ls, xw, ph, nn, cv);
       }
     };
-    auto tag_here = [&]() -> int {
+    auto tag_here = [&](int* chr) -> int {
       if constexpr (F32) {
+        // the cell in FP32 unless a cell face lies within the band, then
+        // the reference's FP64 lookup of the world position
         int k[3];
         P::unpack(key, k);
         const float o[3] = {p.x, p.y, p.z};
-        return ls_tag_anchor<D>(c.ls, k, o);
+        bool near = false;
+        const int t = ls_tag_anchor<D>(c.ls, k, o, chr, &near);
+        if (!near) return t;
+        double xw[3];
+        P::world(c, p, key, xw);
+        return ls_tag<D, double>(c.ls, xw, chr);
       } else {
         double xw[3];
         P::world(c, p, key, xw);
-        return ls_tag<D, R>(c.ls, xw);
+        return ls_tag<D, R>(c.ls, xw, chr);
       }
     };
     R phi, n[3], curv, rho = 0;
     sample_here(phi, n, curv);  // A2 Get_particle_info
     if (mode == MAP_PRE) set_info<D, R>(c, phi, curv, h, rho);
     // A3 Find_and_map_particle (:408-467) + driver loop (sph_mesh_generation.cpp:1506-1545)
-    int tag = tag_here();
+    int chr = 0;  // characteristic cell: k + 1 on segment k, -(k + 1) at singularity k
+    int tag = tag_here(&chr);
     R nl = r_sqrt(dot3<D, R>(n, n));
-    if (tag == CUT_CELL && (type == REAL_P || type == SURFACE_P)) {
+    if (tag == CUT_CELL && (type == REAL_P || type == SURFACE_P) && chr == 0) {
       type = SURFACE_P;
       R dist = r_fabs(phi);
       R div = (R)1.0 / (nl + (R)1.0e-15);
@@ -512,10 +520,40 @@ __device__ inline void map_block(const KCtx& c, const Buf<R>& b, int* counts, un
         dl[d] = nd * dist;
       }
       P::add(c, p, key, dl);
+    } else if (chr > 0) {
+      // SEGMENT: onto the segment's line (:439-455), in FP64 on the world
+      // position: e = (p2 - p1) / max(|p2 - p1|, 1e-15), x = p1 + e ((x - p1) . e)
+      type = SEGMENT_P;
+      const double* p1 = c.ls.seg + 6 * (chr - 1);
+      const double* p2 = p1 + 3;
+      double xw[3];
+      P::world(c, p, key, xw);
+      double Pv[3] = {0.0, 0.0, 0.0}, Nv[3] = {0.0, 0.0, 0.0};
+      for (int d = 0; d < D; d++) {
+        Pv[d] = __dsub_rn(p2[d], p1[d]);
+        Nv[d] = __dsub_rn(xw[d], p1[d]);
+      }
+      double len = __dmul_rn(Pv[0], Pv[0]);
+      len = __dadd_rn(len, __dmul_rn(Pv[1], Pv[1]));
+      if (D == 3) len = __dadd_rn(len, __dmul_rn(Pv[2], Pv[2]));
+      const double inv = __ddiv_rn(1.0, fmax(__dsqrt_rn(len), 1.e-15));
+      double e[3] = {0.0, 0.0, 0.0};
+      for (int d = 0; d < D; d++) e[d] = __dmul_rn(Pv[d], inv);
+      double dist = __dmul_rn(Nv[0], e[0]);
+      dist = __dadd_rn(dist, __dmul_rn(Nv[1], e[1]));
+      if (D == 3) dist = __dadd_rn(dist, __dmul_rn(Nv[2], e[2]));
+      for (int d = 0; d < D; d++) xw[d] = __dadd_rn(p1[d], __dmul_rn(e[d], dist));
+      P::set_world(c, p, key, xw);
+    } else if (chr < 0) {
+      // SINGULARITY: at the point (:456-465)
+      type = SINGULARITY_P;
+      const double* ps = c.ls.sing + 3 * (-chr - 1);
+      double xw[3] = {ps[0], ps[1], D == 3 ? ps[2] : 0.0};
+      P::set_world(c, p, key, xw);
     } else {
       type = REAL_P;
     }
-    if (type == SURFACE_P) {  // Get_dispersed_position(0.00001*h), :385-404
+    if (type == SURFACE_P || type == SEGMENT_P) {  // Get_dispersed_position(0.00001*h), :385-404
       R dx = (R)0.00001 * h;
       R div = (R)1.0 / (nl + (R)1.0e-15);
       R dl[3] = {0, 0, 0};
@@ -645,7 +683,7 @@ k_map(KCtx c, Buf<R> b, int* counts, unsigned* lhmax, int mode, unsigned max_att
 // that one candidate costs one 32-byte sector (FP32):
 //   FP32: w0 = (offset x, y, z, h), w1 = (anchor x, y, z as exact floats, +-1/rho^2)
 //   FP64: w0 = (x, y, z, h),        w1 = (0, 0, 0, +-1/rho^2)
-// The sign carries the type: negative for a SURFACE particle.  1/rho^2 is the
+// The sign carries the type: negative for a particle that is not REAL.  1/rho^2 is the
 // neighbour's share of the pair coefficient of the force stages, computed once
 // per particle (as 1 / (rho * rho), the forces' own expression).
 template <int D, class R> struct RecOps;
@@ -654,7 +692,7 @@ struct RecOps<D, double> {
   __device__ static void pack(const KCtx&, const double4& p, int, int type, double rho, double4& w0, double4& w1) {
     w0 = p;
     const double vol = r_rcp(rho * rho);
-    w1 = make_double4(0.0, 0.0, 0.0, type == SURFACE_P ? -vol : vol);
+    w1 = make_double4(0.0, 0.0, 0.0, type != REAL_P ? -vol : vol);
   }
   __device__ static void rel(const KCtx&, const double4& a0, const double4&, const double4& b0, const double4&,
                              double* dr) {
@@ -670,7 +708,7 @@ struct RecOps<D, float> {
     PosOps<D, float>::unpack(key, k);
     w0 = p;
     const float vol = r_rcp(rho * rho);
-    w1 = make_float4((float)k[0], (float)k[1], (float)k[2], type == SURFACE_P ? -vol : vol);
+    w1 = make_float4((float)k[0], (float)k[1], (float)k[2], type != REAL_P ? -vol : vol);
   }
   __device__ static void rel(const KCtx& c, const float4& a0, const float4& a1, const float4& b0, const float4& b1,
                              float* dr) {
@@ -1035,6 +1073,17 @@ template <class R> __device__ inline R d2_of(const R* dr, int D) {
   return d2;
 }
 
+// How a SURFACE or SEGMENT particle i pairs with a neighbour j that is not
+// REAL, in the kernel sum (particle_mesh_generation.cpp:717-759) and the
+// forces (:769-991): 1 = through the normal-angle filter (j of i's own type),
+// 2 = without the filter, 0 = not at all.  A SURFACE particle takes SURFACE,
+// SEGMENT and SINGULARITY neighbours; a SEGMENT particle SEGMENT and
+// SINGULARITY neighbours.  Both skip REAL neighbours.
+__device__ inline int char_pair(int ti, int tj) {
+  if (ti == SURFACE_P) return tj == SURFACE_P ? 1 : 2;
+  return tj == SEGMENT_P ? 1 : (tj == SINGULARITY_P ? 2 : 0);
+}
+
 // A6 + A7: Refresh_neighbor_info (level_infor.cpp:469-506) and
 // Get_kernel_summation (particle_mesh_generation.cpp:690-765).  The
 // neighbour list is written in the fixed scan order.
@@ -1049,7 +1098,7 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
   using T4 = typename V4<R>::T;
   constexpr bool F32 = std::is_same<R, float>::value;
   // FP32 tile entry: position relative to the warp's anchor cell and
-  // (cutoff*h)^2, negative for a SURFACE particle; FP64: the packed record
+  // (cutoff*h)^2, negative for a particle that is not REAL; FP64: the packed record
   using E = typename std::conditional<F32, float4, RecPair<R>>::type;
   __shared__ E s_tile[8][32];
   long long i = blk * blockDim.x + threadIdx.x;
@@ -1062,7 +1111,7 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
     a0 = b.rec[2 * i];
     a1 = b.rec[2 * i + 1];
     ti = b.meta[i] & 0xFF;
-    if (!F32 && ti == SURFACE_P) {
+    if (!F32 && ti != REAL_P) {
       const T4 nri = b.nr[i];
       ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
     }
@@ -1083,8 +1132,10 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
   bool unc = false;  // FP32-split: a decision of this particle lies in its band (exact re-decision follows)
   const R R2i = (hi * cut) * (hi * cut);
   int* row = w.nbl + nb_slot(active ? i : 0, 0, w.cap);  // entry q at row[(q >> 3) * 256 + (q & 7)]
-  // accepted neighbour j at distance vector dr (i - j), |dr| = dist
-  auto accept = [&](int j, const R* dr, R dist, bool surf_j) {
+  // accepted neighbour j at distance vector dr (i - j), |dr| = dist; char_j:
+  // j is not REAL.  A SEGMENT particle sums in 3D only (:740-759).
+  const bool char_i = ti == SURFACE_P || (D == 3 && ti == SEGMENT_P);
+  auto accept = [&](int j, const R* dr, R dist, bool char_j) {
     if (cnt < w.cap) row[((cnt >> 3) << 8) + (cnt & 7)] = j;
     cnt++;
     if (ti == REAL_P) {
@@ -1096,7 +1147,9 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
         sum += pair_W(kind, D, dist, hi, inv_hi);
         ncount++;
       }
-    } else if (ti == SURFACE_P && surf_j) {  // surface neighbour of a surface particle
+    } else if (char_i && char_j) {  // the tangential kernel sum of a surface or segment particle
+      const int rule = char_pair(ti, b.meta[j] & 0xFF);
+      if (rule == 0) return;
       if constexpr (F32) {  // the normal is not kept in registers across the scan
         const T4 nri = b.nr[i];
         ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
@@ -1104,12 +1157,16 @@ __device__ inline void density_block(const KCtx& c, const Buf<R>& b, const Work<
       R dn = dot3<D, R>(dr, ni);
       R pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
       R pd = pair_dist(dot3<D, R>(pr, pr));
-      const T4 nrj = b.nr[j];
-      const R nj[3] = {nrj.x, nrj.y, nrj.z};
-      const R ca = r_fabs(dot3<D, R>(ni, nj));
-      if (F32 && fabsf((float)ca - (float)cos_t) <= kBandCos) unc = true;
-      if (ca > cos_t) {
-        sum += pair_W(kind, D - 1, pd, hi, inv_hi);
+      bool ok = true;
+      if (rule == 1) {
+        const T4 nrj = b.nr[j];
+        const R nj[3] = {nrj.x, nrj.y, nrj.z};
+        const R ca = r_fabs(dot3<D, R>(ni, nj));
+        if (F32 && fabsf((float)ca - (float)cos_t) <= kBandCos) unc = true;
+        ok = ca > cos_t;
+      }
+      if (ok) {
+        sum += pair_W(kind, ti == SEGMENT_P ? 1 : D - 1, pd, hi, inv_hi);
         ncount++;
       }
     }
@@ -1251,10 +1308,11 @@ __device__ inline void density_fix_items(const KCtx& c, const Buf<float>& b, con
     const float4 a0 = b.rec[2 * i], a1 = b.rec[2 * i + 1];
     const int ti = b.meta[i] & 0xFF;
     float ni[3] = {0.f, 0.f, 0.f};
-    if (ti == SURFACE_P) {
+    if (ti != REAL_P) {
       const float4 q = b.nr[i];
       ni[0] = q.x; ni[1] = q.y; ni[2] = q.z;
     }
+    const bool char_i = ti == SURFACE_P || (D == 3 && ti == SEGMENT_P);
     const float hi = a0.w, inv_hi = r_rcp(hi);
     const float R2i = (hi * cut) * (hi * cut);
     const int old = w.cnt[i];
@@ -1287,22 +1345,26 @@ __device__ inline void density_fix_items(const KCtx& c, const Buf<float>& b, con
           term = pair_W(kind, D, dist, hi, inv_hi);
           counted = true;
         }
-      } else if (ti == SURFACE_P && b1.w < 0.f) {
+      } else if (char_i && b1.w < 0.f) {
+        const int rule = char_pair(ti, b.meta[j] & 0xFF);
+        if (rule == 0) return true;
         const float dn = dot3<D, float>(dr, ni);
         float pr[3] = {dr[0] - ni[0] * dn, dr[1] - ni[1] * dn, dr[2] - ni[2] * dn};
         const float pd = pair_dist(dot3<D, float>(pr, pr));
-        const float4 q = b.nr[j];
-        const float nj[3] = {q.x, q.y, q.z};
-        const float ca = fabsf(dot3<D, float>(ni, nj));
-        bool ok;
-        if (fabsf(ca - cos_t) <= kBandCos) {
-          ok = exact_cos<D>(c, ni, nj);
-          e |= (int)((ok ? NB_COS_OK : NB_COS_NO) << 30);
-        } else {
-          ok = ca > cos_t;
+        bool ok = true;
+        if (rule == 1) {
+          const float4 q = b.nr[j];
+          const float nj[3] = {q.x, q.y, q.z};
+          const float ca = fabsf(dot3<D, float>(ni, nj));
+          if (fabsf(ca - cos_t) <= kBandCos) {
+            ok = exact_cos<D>(c, ni, nj);
+            e |= (int)((ok ? NB_COS_OK : NB_COS_NO) << 30);
+          } else {
+            ok = ca > cos_t;
+          }
         }
         if (ok) {
-          term = pair_W(kind, D - 1, pd, hi, inv_hi);
+          term = pair_W(kind, ti == SEGMENT_P ? 1 : D - 1, pd, hi, inv_hi);
           counted = true;
         }
       }
@@ -1403,7 +1465,7 @@ __device__ inline void load4(const double* p, double* v) {
 // Stage 1 evaluates each pair's kernel gradient aw and stores, in the
 // neighbour list's layout, the pair coefficient c_ij = aw * (1/rho_i^2 +
 // 1/rho_j^2) (0 for a pair the forces skip), and per particle (a1, eta),
-// eta = nu * rho, negated for a SURFACE particle.  The stage-2 viscous term
+// eta = nu * rho, negated for a particle that is not REAL.  The stage-2 viscous term
 // of a pair is c_ij * eta_ij * (v_i - v_j) (:1021-1049), so stage 2 reads the
 // coefficient and one vector per neighbour; a particle whose list spilled
 // re-scans its cells and recomputes c_ij in both stages.
@@ -1441,7 +1503,7 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
   const int mi = b.meta[i];
   const int ti = mi & 0xFF;
   R ni[3] = {0, 0, 0};
-  if (ti == SURFACE_P) {
+  if (ti != REAL_P) {
     const T4 nri = b.nr[i];
     ni[0] = nri.x; ni[1] = nri.y; ni[2] = nri.z;
   }
@@ -1489,8 +1551,12 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
   // mark: the surface filter's FP64 decision from the density fix-up (0: none)
   auto coef = [&](int j, const T4& b0, const T4& b1, const R* vec, R* dr, R& cij, unsigned mark) -> bool {
     if (j == (int)i) return false;
-    const bool surf_j = b1.w < (R)0;
-    if (ti == SURFACE_P && !surf_j) return false;
+    int rule = 0;
+    if (ti != REAL_P) {  // SURFACE or SEGMENT: j must not be REAL
+      if (!(b1.w < (R)0)) return false;
+      rule = char_pair(ti, b.meta[j] & 0xFF);
+      if (rule == 0) return false;
+    }
     R aw;
     const R hij = (R)0.5 * (h + b0.w);
     if (ti == REAL_P) {
@@ -1502,23 +1568,30 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
       R dn = dot3<D, R>(vec, ni);
       dr[0] = vec[0] - ni[0] * dn; dr[1] = vec[1] - ni[1] * dn; dr[2] = vec[2] - ni[2] * dn;
       R dist = force_dist(dot3<D, R>(dr, dr));
-      const T4 nrj = b.nr[j];
-      const R nj[3] = {nrj.x, nrj.y, nrj.z};
-      bool ok;
-      if (mark == NB_COS_OK) {
-        ok = true;
-      } else if (mark == NB_COS_NO) {
-        ok = false;
-      } else {
-        const R ca = r_fabs(dot3<D, R>(ni, nj));
-        ok = ca > cos_t;
-        if constexpr (F32 && SPILL) {
-          if (fabsf(ca - cos_t) <= kBandCos) ok = exact_cos<D>(c, (const float*)ni, (const float*)nj);
+      bool ok = true;
+      if (rule == 1) {
+        if (mark == NB_COS_OK) {
+          ok = true;
+        } else if (mark == NB_COS_NO) {
+          ok = false;
+        } else {
+          const T4 nrj = b.nr[j];
+          const R nj[3] = {nrj.x, nrj.y, nrj.z};
+          const R ca = r_fabs(dot3<D, R>(ni, nj));
+          ok = ca > cos_t;
+          if constexpr (F32 && SPILL) {
+            if (fabsf(ca - cos_t) <= kBandCos) ok = exact_cos<D>(c, (const float*)ni, (const float*)nj);
+          }
         }
       }
       if (!ok) return false;
-      if constexpr (WEN32) aw = wendland_aw<D - 1>(dist, hij);
-      else aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
+      if (ti == SEGMENT_P) {  // the 1D kernel gradient in 3D, none in 2D (:769-879)
+        if constexpr (WEN32) aw = wendland_aw<1>(dist, hij);
+        else aw = (D == 3) ? pair_dW(c.prm.kernel, 1, dist, hij) : (R)0;
+      } else {
+        if constexpr (WEN32) aw = wendland_aw<D - 1>(dist, hij);
+        else aw = pair_dW(c.prm.kernel, D - 1, dist, hij);
+      }
     }
     const R vol_ij = vol_i + r_fabs(b1.w);
     if (STAGE == 1) {
@@ -1530,9 +1603,9 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
   };
   auto visc = [&](int j, R cij) {
     const T4 anj = w.a1[j];
-    const bool surf_j = signbit(anj.w);
+    const bool char_j = signbit(anj.w);  // j is not REAL
     R vj[3];
-    if (ti == REAL_P && surf_j) {
+    if (ti == REAL_P && char_j) {
       vj[0] = vi[0] * (R)-1.0; vj[1] = vi[1] * (R)-1.0; vj[2] = vi[2] * (R)-1.0;
     } else {
       vj[0] = anj.x * hdt1; vj[1] = anj.y * hdt1; vj[2] = anj.z * hdt1;
@@ -1542,7 +1615,7 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
     const R temp0 = cij * eta_ij;
     for (int d = 0; d < D; d++) accum(d, (vi[d] - vj[d]) * temp0);
   };
-  if (ti == REAL_P || ti == SURFACE_P) {
+  if (ti != SINGULARITY_P) {  // a SINGULARITY particle has no force
     if constexpr (!SPILL) {
       const int cnt = w.cnt[i];
       const long long base = nb_slot(i, 0, w.cap);
@@ -1626,13 +1699,13 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
     }
   }
   R a[3] = {0, 0, 0};
-  if (ti == REAL_P || ti == SURFACE_P) {
+  if (ti != SINGULARITY_P) {
     if constexpr (F32)
       for (int d = 0; d < D; d++) F[d] = F[d] - Fc[d];
     for (int d = 0; d < D; d++) a[d] = F[d];
     if (STAGE == 2)
       for (int d = 0; d < D; d++) a[d] = a[d] + vi[d] * pick<R>(c.prm.damp_coeff, c.prm.damp_coeff_f);
-    if (ti == SURFACE_P) {  // Map_surface_particle_force, :1122-1126
+    if (ti == SURFACE_P || ti == SEGMENT_P) {  // Map_surface_particle_force, :1122-1126
       R nf = dot3<D, R>(a, ni);
       for (int d = 0; d < D; d++) a[d] = a[d] - ni[d] * nf;
     }
@@ -1649,7 +1722,7 @@ __device__ inline void force_particle(const KCtx& c, const Buf<R>& b, const Work
     b.a2[i] = mk4<R>(a[0], a[1], a[2], 0);
   } else {
     const R eta = nu * rho;
-    w.a1[i] = mk4<R>(a[0], a[1], a[2], ti == SURFACE_P ? -eta : eta);
+    w.a1[i] = mk4<R>(a[0], a[1], a[2], ti != REAL_P ? -eta : eta);
   }
   my_dt = fmin(my_dt, (double)ts);
   my_v = fmax(my_v, (double)U);

@@ -72,6 +72,10 @@ struct LsBuildDesc {
 };
 cudaError_t ls_build_level(const LsBuildDesc& L, const double* d_phi, double4* g64, double* c64, float4* g32,
                            float* c32, uint8_t* tag, unsigned long long* max_phi_bits, cudaStream_t s);
+// Characteristic cells of one built level (L.tag set): chr per cell (0 none,
+// k + 1 segment k, -(k + 1) singularity k), mrsph_levelset.cu.
+cudaError_t ls_build_characteristics(const LsLevel& L, int D, long long ntot, int* chr, const double* d_sing,
+                                     int nsing, const double* d_seg, int nseg, cudaStream_t s);
 // Cut-cell volume / area / mass of one built level (mrsph_levelset.cu);
 // synchronises s (the CUT cells and the cut sub-cubes size the later
 // passes); cnt holds 3 counters.

@@ -15,4 +15,6 @@ struct mrsph_handle {
   long long ls_ntot[mrsph::MAX_LS] = {0, 0, 0, 0};
   std::vector<void*> ls_allocs;
   mrsph::EngineBase* eng = nullptr;
+  // the geometry's singularity points and segments (mrsph_set_characteristics)
+  std::vector<double> sing, seg;
 };

@@ -255,6 +255,33 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
     L.c32 = c32;
     L.tag = tag;
     L.active = act;
+    L.chr = nullptr;
+  }
+  // characteristic points and segments (mrsph_set_characteristics) and the
+  // characteristic cells of every level
+  ls.nsing = (int)(h->sing.size() / 3);
+  ls.nseg = (int)(h->seg.size() / 6);
+  if (ls.nsing > 0 || ls.nseg > 0) {
+    double* d_pts = nullptr;
+    const size_t npts = h->sing.size() + h->seg.size();
+    API_CK(h, cudaMalloc(&d_pts, sizeof(double) * npts));
+    h->ls_allocs.push_back(d_pts);
+    if (!h->sing.empty())
+      API_CK(h, cudaMemcpyAsync(d_pts, h->sing.data(), sizeof(double) * h->sing.size(), cudaMemcpyHostToDevice,
+                                h->stream));
+    if (!h->seg.empty())
+      API_CK(h, cudaMemcpyAsync(d_pts + h->sing.size(), h->seg.data(), sizeof(double) * h->seg.size(),
+                                cudaMemcpyHostToDevice, h->stream));
+    ls.sing = d_pts;
+    ls.seg = d_pts + h->sing.size();
+    for (int l = 0; l < nlevels; l++) {
+      int* chr = nullptr;
+      API_CK(h, cudaMalloc(&chr, sizeof(int) * h->ls_ntot[l]));
+      h->ls_allocs.push_back(chr);
+      API_CK(h, ls_build_characteristics(ls.lv[l], D, h->ls_ntot[l], chr, ls.sing, ls.nsing, ls.seg, ls.nseg,
+                                         h->stream));
+      ls.lv[l].chr = chr;
+    }
   }
   unsigned long long mb[3] = {0, 0, 0};
   API_CK(h, cudaMemcpyAsync(mb, d_max, sizeof(mb), cudaMemcpyDeviceToHost, h->stream));
@@ -294,6 +321,17 @@ int mrsph_set_levelset(mrsph_handle* h, int nlevels, const mrsph_levelset_level*
   return 0;
 }
 
+int mrsph_set_characteristics(mrsph_handle* h, int nsing, const double* sing, int nseg, const double* seg) {
+  if (!h) return fail(h, MRSPH_ERR_ARG, "null handle");
+  if (h->eng) return fail(h, MRSPH_ERR_STATE, "mrsph_set_characteristics must come before mrsph_set_levelset");
+  if (nsing < 0 || nseg < 0 || (nsing > 0 && !sing) || (nseg > 0 && !seg))
+    return fail(h, MRSPH_ERR_ARG, "bad characteristic point or segment arrays");
+  if (nsing > (1 << 20) || nseg > (1 << 20)) return fail(h, MRSPH_ERR_RANGE, "at most 2^20 points and segments");
+  h->sing.assign(sing ? sing : nullptr, sing ? sing + 3 * (size_t)nsing : nullptr);
+  h->seg.assign(seg ? seg : nullptr, seg ? seg + 6 * (size_t)nseg : nullptr);
+  return 0;
+}
+
 int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, double* nz, double* curv,
                        unsigned char* tag, double* max_phi) {
   if (!h) return fail(h, MRSPH_ERR_ARG, "null handle");
@@ -311,6 +349,20 @@ int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, doubl
   if (curv) API_CK(h, cudaMemcpy(curv, L.c64, sizeof(double) * ntot, cudaMemcpyDeviceToHost));
   if (tag) API_CK(h, cudaMemcpy(tag, L.tag, ntot, cudaMemcpyDeviceToHost));
   if (max_phi) *max_phi = h->ls.max_phi;
+  return 0;
+}
+
+int mrsph_get_characteristics(mrsph_handle* h, int level, int* chr) {
+  if (!h || !chr) return fail(h, MRSPH_ERR_ARG, "null argument");
+  if (level < 0 || level >= h->nls) return fail(h, MRSPH_ERR_ARG, "no such level");
+  API_CK(h, cudaSetDevice(h->prm.device));
+  const LsLevel& L = h->ls.lv[level];
+  const long long ntot = h->ls_ntot[level];
+  if (!L.chr) {
+    std::memset(chr, 0, sizeof(int) * ntot);
+    return 0;
+  }
+  API_CK(h, cudaMemcpy(chr, L.chr, sizeof(int) * ntot, cudaMemcpyDeviceToHost));
   return 0;
 }
 
@@ -419,8 +471,8 @@ int mrsph_set_state(mrsph_handle* h, long long n, const mrsph_state_in* st, int 
   if (!st || !st->xyz || n <= 0) return fail(h, MRSPH_ERR_ARG, "state needs positions");
   if (st->type)
     for (long long i = 0; i < n; i++)
-      if (st->type[i] != MRSPH_REAL && st->type[i] != MRSPH_SURFACE)
-        return fail(h, MRSPH_ERR_ARG, "only REAL and SURFACE particles are supported");
+      if (st->type[i] < MRSPH_REAL || st->type[i] > MRSPH_SEGMENT)
+        return fail(h, MRSPH_ERR_ARG, "particle type must be REAL, SURFACE, SINGULARITY or SEGMENT");
   if (st->level)
     for (long long i = 0; i < n; i++)
       if (st->level[i] < 0 || st->level[i] >= h->geo.ncl) return fail(h, MRSPH_ERR_ARG, "level out of range");

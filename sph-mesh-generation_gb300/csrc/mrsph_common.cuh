@@ -30,6 +30,9 @@ struct LsLevel {
   const float* c32;
   const uint8_t* tag;
   const uint8_t* active;  // per package incl. margins, or nullptr
+  // characteristic cell (tag_characteristic + idx_characteristic): 0 none,
+  // k + 1 on segment k, -(k + 1) at singularity k; nullptr without any
+  const int* chr;
   // FP32-split location (set by the FP32 engine): per axis, for every anchor
   // cell k of the cell list, the package of the anchor's lower corner (.x)
   // and the corner's offset inside that package as FP32 bits (.y); FP32
@@ -45,6 +48,11 @@ struct LsSet {
   double middle_dl, max_curv, min_curv; // curvature law (|curv| range over CUT cells)
   float max_phi_f, dl0_f, min_dl_f, max_dl_f, middle_dl_f, max_curv_f, min_curv_f;  // FP32 copies
   LsLevel lv[MAX_LS];
+  // the geometry's singularity points (3 each) and segments (6 each: first
+  // point, second point; z = 0 in 2D), device copies
+  int nsing, nseg;
+  const double* sing;
+  const double* seg;
 };
 
 // Cell-list levels (Level_info, level_infor.cpp:35-110): level 0 is the
@@ -502,13 +510,30 @@ __device__ inline void ls_loc_anchor(const LsLevel& L, const int* k, const float
   }
 }
 
-// ls_pick on the anchor representation: the finest level containing the
-// point with an active package, and the point's location on it.
+// near (optional): the location lies within 2^-16 of a cell face of L,
+// measured in cells (package faces are cell faces).  The FP32 location is
+// within about 2^-22 cells of the exact one, so outside that band its cell is
+// the cell of the FP64 location.
 template <int D>
-__device__ inline int ls_pick_anchor(const LsSet& ls, const int* k, const float* o, int* P, float* csp) {
+__device__ inline void ls_near_face(const LsLevel& L, const float* csp, bool* near) {
+  if (!near) return;
+  for (int d = 0; d < D; d++) {
+    const float u = csp[d] * L.inv_dcell_f[d];
+    const float fr = u - floorf(u);
+    if (fr < 1.0f / 65536.0f || fr > 1.0f - 1.0f / 65536.0f) *near = true;
+  }
+}
+
+// ls_pick on the anchor representation: the finest level containing the
+// point with an active package, and the point's location on it.  near: see
+// ls_near_face, over every level the choice examines.
+template <int D>
+__device__ inline int ls_pick_anchor(const LsSet& ls, const int* k, const float* o, int* P, float* csp,
+                                     bool* near = nullptr) {
   for (int l = ls.nls - 1; l >= 1; l--) {
     const LsLevel& L = ls.lv[l];
     ls_loc_anchor<D>(L, k, o, P, csp);
+    ls_near_face<D>(L, csp, near);
     bool inside = true;
     for (int d = 0; d < D; d++) inside = inside && P[d] >= 0 && P[d] < L.num_pkg[d];
     if (!inside) continue;
@@ -520,6 +545,7 @@ __device__ inline int ls_pick_anchor(const LsSet& ls, const int* k, const float*
     return l;
   }
   ls_loc_anchor<D>(ls.lv[0], k, o, P, csp);
+  ls_near_face<D>(ls.lv[0], csp, near);
   return 0;
 }
 
@@ -547,12 +573,16 @@ __device__ inline void ls_sample_anchor(const LsSet& ls, const int* k, const flo
   ls_interp<D, float>(L, pos, im, w, phi, n, curv);
 }
 
-// ls_tag for the FP32-split particle representation.
+// ls_tag for the FP32-split particle representation.  near (optional) is
+// set when a cell face of a level the lookup examined lies within the FP32
+// location's band; the caller then decides in FP64 (ls_tag on the world
+// position), as the reference locates the cell.
 template <int D>
-__device__ inline int ls_tag_anchor(const LsSet& ls, const int* k, const float* o) {
+__device__ inline int ls_tag_anchor(const LsSet& ls, const int* k, const float* o, int* chr = nullptr,
+                                    bool* near = nullptr) {
   int P[3] = {0, 0, 0};
   float csp[3] = {0.f, 0.f, 0.f};
-  const LsLevel& L = ls.lv[ls_pick_anchor<D>(ls, k, o, P, csp)];
+  const LsLevel& L = ls.lv[ls_pick_anchor<D>(ls, k, o, P, csp, near)];
   int g[3] = {0, 0, 0};
   for (int d = 0; d < D; d++) {
     int p = P[d], ci;
@@ -561,13 +591,15 @@ __device__ inline int ls_tag_anchor(const LsSet& ls, const int* k, const float* 
     else ci = max(0, min((int)floorf(csp[d] * L.inv_dcell_f[d]), 3));
     g[d] = p * 4 + ci;
   }
-  return L.tag[ls_index(L, D, g[0], g[1], g[2])];
+  const long long a = ls_index(L, D, g[0], g[1], g[2]);
+  if (chr) *chr = L.chr ? L.chr[a] : 0;
+  return L.tag[a];
 }
 
 // Get_level_set_char_cell_tag_and_idx (particle_mesh_generation.cpp:552-573)
 // via Get_id_pkg_cell (lset_level_infor.cpp:350-366).
 template <int D, class R>
-__device__ inline int ls_tag(const LsSet& ls, const double* x) {
+__device__ inline int ls_tag(const LsSet& ls, const double* x, int* chr = nullptr) {
   constexpr bool F32 = std::is_same<R, float>::value;
   const LsLevel& L = ls.lv[ls_pick<D, R>(ls, x)];
   int g[3] = {0, 0, 0};
@@ -581,7 +613,9 @@ __device__ inline int ls_tag(const LsSet& ls, const double* x) {
     ci = max(0, min(ci, 3));
     g[d] = p * 4 + ci;
   }
-  return L.tag[ls_index(L, D, g[0], g[1], g[2])];
+  const long long a = ls_index(L, D, g[0], g[1], g[2]);
+  if (chr) *chr = L.chr ? L.chr[a] : 0;
+  return L.tag[a];
 }
 
 // Levelset::Get_scale, level_set.cpp:311-351.  Law 0: the active tanh law.

@@ -938,6 +938,108 @@ cudaError_t ls_volume_mass(const LsSet& ls, int level, int D, double* cvol, doub
 // Builds one level in place: g64 (phi, n), c64, tag, and its float copies.
 // max_phi_bits[0] accumulates the maximum positive interior phi, [1] and [2]
 // the maximum and minimum |curvature| of CUT cells (FP64 bit patterns).
+// ---------------------------------------------------------------- characteristic cells
+// Levelset_package::Get_singularity_tag (lset_package.cpp:515-556) and
+// Get_segment_tag (:560-590) with is_Segment_intersec_AABB (:594-619), after
+// the interface tags, in FP64 without contraction (this file is compiled with
+// -fmad=false), in the reference's operation order.  A singularity tags, in
+// every interior package whose half-open box holds it (0 < x - corner <
+// dpkg + 1e-10 per axis), the interface cell (tag != NORMAL) nearest to it by
+// cell centre, equal distances going to the first cell in (x, y, z) loop
+// order; the singularities run in order on one thread, so a later one
+// overwrites an earlier one's cell.  A segment tags every other interface
+// cell whose box it meets, the first segment in order winning.
+__device__ inline bool segment_meets_box(const double* p1, const double* p2, const double* mn, const double* mx) {
+  const double EPSILON = 1.e-20;
+  double d[3], e[3], cc[3], ad[3];
+  for (int k = 0; k < 3; k++) {
+    d[k] = (p2[k] - p1[k]) * 0.5;
+    e[k] = (mx[k] - mn[k]) * 0.5;
+    cc[k] = (p1[k] + d[k]) - (mx[k] + mn[k]) * 0.5;
+    ad[k] = fabs(d[k]);
+  }
+  for (int k = 0; k < 3; k++)
+    if (fabs(cc[k]) > e[k] + ad[k]) return false;
+  if (fabs(d[1] * cc[2] - d[2] * cc[1]) > e[1] * ad[2] + e[2] * ad[1] + EPSILON) return false;
+  if (fabs(d[2] * cc[0] - d[0] * cc[2]) > e[2] * ad[0] + e[0] * ad[2] + EPSILON) return false;
+  if (fabs(d[0] * cc[1] - d[1] * cc[0]) > e[0] * ad[1] + e[1] * ad[0] + EPSILON) return false;
+  return true;
+}
+
+__global__ void k_ls_singularities(LsLevel L, int D, const uint8_t* __restrict__ tag, int* __restrict__ chr,
+                                   const double* __restrict__ sing, int nsing) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int ic = 0; ic < nsing; ic++) {
+    const double* p = sing + 3 * ic;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < D; d++) {
+      const int q = (int)floor((p[d] - L.box_l[d]) / L.dpkg[d]);
+      lo[d] = max(0, q - 1);
+      hi[d] = min(L.num_pkg[d] - 1, q + 1);
+    }
+    for (int pi = lo[0]; pi <= hi[0]; pi++)
+      for (int pj = lo[1]; pj <= hi[1]; pj++)
+        for (int pk_ = lo[2]; pk_ <= hi[2]; pk_++) {
+          const int pk[3] = {pi, pj, pk_};
+          bool inside = true;
+          for (int d = 0; d < D; d++) {
+            const double corner = pk[d] * L.dpkg[d] + L.box_l[d];
+            const double dr = p[d] - corner;
+            inside = inside && dr < L.dpkg[d] + 1.e-10 && dr > 0.;
+          }
+          if (!inside) continue;
+          double best = 0.0;
+          long long besta = -1;
+          for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+              for (int k = 0; k < (D == 3 ? 4 : 1); k++) {
+                const int ce[3] = {i, j, k};
+                const long long a = ls_index(L, D, 4 * pk[0] + i, 4 * pk[1] + j, D == 3 ? 4 * pk[2] + k : 0);
+                if (tag[a] == 0) continue;
+                double dist = 0.0;
+                for (int d = 0; d < D; d++) {
+                  const double cp = (pk[d] * L.dpkg[d] + (ce[d] + 0.5) * L.dcell[d]) + L.box_l[d];
+                  dist += (cp - p[d]) * (cp - p[d]);
+                }
+                dist = sqrt(dist);
+                if (besta < 0 || dist < best) { best = dist; besta = a; }
+              }
+          if (besta >= 0) chr[besta] = -(ic + 1);
+        }
+  }
+}
+
+__global__ void k_ls_segments(LsLevel L, int D, const uint8_t* __restrict__ tag, int* __restrict__ chr,
+                              const double* __restrict__ seg, int nseg) {
+  const long long ni[3] = {4ll * L.num_pkg[0], 4ll * L.num_pkg[1], D == 3 ? 4ll * L.num_pkg[2] : 1};
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ni[0] * ni[1] * ni[2]) return;
+  const int g[3] = {(int)(t % ni[0]), (int)((t / ni[0]) % ni[1]), (int)(t / (ni[0] * ni[1]))};
+  const long long a = ls_index(L, D, g[0], g[1], g[2]);
+  if (tag[a] == 0 || chr[a] < 0) return;
+  double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+  for (int d = 0; d < D; d++) {
+    const int pk = g[d] >> 2, ce = g[d] & 3;
+    mn[d] = (pk * L.dpkg[d] + ce * L.dcell[d]) + L.box_l[d];
+    mx[d] = mn[d] + L.dcell[d];
+  }
+  for (int is = 0; is < nseg; is++)
+    if (segment_meets_box(seg + 6 * is, seg + 6 * is + 3, mn, mx)) {
+      chr[a] = is + 1;
+      return;
+    }
+}
+
+cudaError_t ls_build_characteristics(const LsLevel& L, int D, long long ntot, int* chr, const double* d_sing,
+                                     int nsing, const double* d_seg, int nseg, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(chr, 0, sizeof(int) * ntot, s);
+  if (e != cudaSuccess) return e;
+  if (nsing > 0) k_ls_singularities<<<1, 1, 0, s>>>(L, D, L.tag, chr, d_sing, nsing);
+  const long long ncell = 4ll * L.num_pkg[0] * 4ll * L.num_pkg[1] * (D == 3 ? 4ll * L.num_pkg[2] : 1);
+  if (nseg > 0) k_ls_segments<<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(L, D, L.tag, chr, d_seg, nseg);
+  return cudaGetLastError();
+}
+
 cudaError_t ls_build_level(const LsBuildDesc& L, const double* d_phi, double4* g64, double* c64, float4* g32,
                            float* c32, uint8_t* tag, unsigned long long* max_phi_bits, cudaStream_t s) {
   long long ntot = (long long)L.n[0] * L.n[1] * L.n[2];

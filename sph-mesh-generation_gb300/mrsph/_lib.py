@@ -84,6 +84,8 @@ EXPORTS = {
     "mrsph_destroy": ([C.c_void_p], C.c_int),
     "mrsph_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),
     "mrsph_set_levelset": ([C.c_void_p, C.c_int, C.POINTER(LevelsetLevel)], C.c_int),
+    "mrsph_set_characteristics": ([C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "mrsph_get_characteristics": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "mrsph_get_levelset": ([C.c_void_p, C.c_int] + [C.c_void_p] * 5 + [C.POINTER(C.c_double)], C.c_int),
     "mrsph_volume_mass": ([C.c_void_p, C.c_int, C.POINTER(VolumeMassStats), C.c_void_p, C.c_void_p], C.c_int),
     "mrsph_sample_levelset": ([C.c_void_p, C.c_longlong] + [C.c_void_p] * 5, C.c_int),

@@ -298,6 +298,59 @@ def disc_hole_2d(spacing: float = 0.01, grid: int = 256, kernel: str = "wendland
     return Case("disc_hole_2d", p, [lv], n, steps=steps)
 
 
+def box_with_corners(dim: int = 2, spacing: float = 0.02, grid: int = 64, kernel: str = "wendland",
+                     h_over_dx: float = 1.3, precision: str = "fp64", seed: int = 0, lo_b: float = 0.1,
+                     hi_b: float = 0.9, edges: bool = True, steps: int = 200) -> Case:
+    """A box [lo_b, hi_b]^dim (phi = the distance to the nearest face inside,
+    min over the faces), whose corners are the geometry's singularity points
+    and, in 3D with edges=True, whose 12 edges are its segments
+    (Levelset::singularity / Levelset::segment): the characteristic cells
+    of the reference's level set, where particles become SINGULARITY and
+    SEGMENT particles.  Constant spacing; the same unit-cube domain with
+    margins as disc_hole_2d (grid cells per unit length)."""
+    p = default_params(dim)
+    npkg_unit = grid // 4
+    dpkg = 1.0 / npkg_unit
+    cell_ratio = 2.0 * h_over_dx
+    margin_pkg = max(npkg_unit // 16, 1)
+    while not cell_levels_consistent([-margin_pkg * dpkg] * dim, [1.0 + margin_pkg * dpkg] * dim, dim,
+                                     spacing * cell_ratio, spacing * cell_ratio):
+        margin_pkg += 1
+    lo = -margin_pkg * dpkg
+    hi = 1.0 + margin_pkg * dpkg
+    npkg = npkg_unit + 2 * margin_pkg
+    box_l = [lo, lo, lo if dim == 3 else 0.0]
+    box_r = [hi, hi, hi if dim == 3 else 0.0]
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=spacing, max_dl=spacing,
+             cell_ratio=cell_ratio, box_l=box_l, box_r=box_r, seed=seed)
+
+    def sdf(X, Y, Z):
+        out = np.minimum(np.minimum(X - lo_b, hi_b - X), np.minimum(Y - lo_b, hi_b - Y))
+        if dim == 3:
+            out = np.minimum(out, np.minimum(Z - lo_b, hi_b - Z))
+        return out
+
+    lv = make_level(sdf, dim, box_l, [dpkg, dpkg, dpkg if dim == 3 else 1.0],
+                    [npkg, npkg, npkg if dim == 3 else 1])
+    n = particle_count([lv], p)
+    cs = Case(f"box_{dim}d", p, [lv], n, steps=steps)
+    v = (lo_b, hi_b)
+    if dim == 2:
+        corners = np.array([[x, y, 0.0] for y in v for x in v])
+    else:
+        corners = np.array([[x, y, z] for z in v for y in v for x in v])
+    cs.extra["singularities"] = corners
+    if dim == 3 and edges:
+        segs = []
+        for a in v:
+            for b_ in v:
+                segs.append([lo_b, a, b_, hi_b, a, b_])   # along x
+                segs.append([a, lo_b, b_, a, hi_b, b_])   # along y
+                segs.append([a, b_, lo_b, a, b_, hi_b])   # along z
+        cs.extra["segments"] = np.array(segs)
+    return cs
+
+
 def torus_3d(dx_min: float = 0.005, dx_max: float = 0.02, kernel: str = "wendland",
              h_over_dx: float = 1.3, precision: str = "fp32", seed: int = 0, steps: int = 500,
              fine_pkg: int = 64, nlevels: int = 3) -> Case:

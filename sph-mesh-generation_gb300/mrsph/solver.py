@@ -60,6 +60,18 @@ class SPHMeshGeneration:
     # ------------------------------------------------------------------ setup
     def _set_levelset(self):
         levels = self.case.levels
+        extra = getattr(self.case, "extra", None) or {}
+        sing = np.ascontiguousarray(np.asarray(extra.get("singularities", np.zeros((0, 3))),
+                                               dtype=np.float64).reshape(-1, 3))
+        seg = np.ascontiguousarray(np.asarray(extra.get("segments", np.zeros((0, 6))),
+                                              dtype=np.float64).reshape(-1, 6))
+        if len(sing) or len(seg):
+            # Levelset::singularity / ::segment, tagged by Get_singularity_tag
+            # and Get_segment_tag when the level set is built
+            L.check(self.lib.mrsph_set_characteristics(
+                self.h, len(sing), sing.ctypes.data_as(C.c_void_p) if len(sing) else None,
+                len(seg), seg.ctypes.data_as(C.c_void_p) if len(seg) else None),
+                self.h, "mrsph_set_characteristics")
         arr = (L.LevelsetLevel * len(levels))()
         self._ls_keep = []
         for i, lv in enumerate(levels):
@@ -200,6 +212,13 @@ class SPHMeshGeneration:
                                             _ptr(out["curv"]), _ptr(out["tag"]), C.byref(mp)), self.h,
                 "mrsph_get_levelset")
         out["max_phi"] = mp.value
+        return out
+
+    def characteristic_tags(self, level: int) -> np.ndarray:
+        """Per cell of one level: 0 (NORMAL), k + 1 (on segment k) or -(k + 1)
+        (at singularity point k)."""
+        out = np.zeros(self.case.levels[level].phi.shape, dtype=np.int32)
+        L.check(self.lib.mrsph_get_characteristics(self.h, level, _ptr(out)), self.h, "mrsph_get_characteristics")
         return out
 
     def sample_levelset(self, xyz: np.ndarray):
