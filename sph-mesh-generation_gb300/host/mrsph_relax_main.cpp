@@ -2,8 +2,9 @@
 // counterpart of the reference's main (src/main.cpp) + Solver for the
 // relaxation path: build a workload, seed, relax, write particle restarts.
 //
-//   mrsph_relax --case disc_hole_2d|torus_3d [--precision fp32|fp64] [--steps N]
+//   mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N]
 //               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]
+//               [--lset-restart]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
 // particle-steps/s, final time step).  --count-only prints the particle count
@@ -12,7 +13,11 @@
 // instead of the workload's; --vtu also writes the particle VTU series
 // (outdata/particle_*.vtu, .pvtu, particle.pvd) at every output; --lset
 // writes the level-set image of the finest level (outdata/mesh_lset_*) before
-// seeding.  Exit status 2 on an engine error.
+// seeding; --lset-restart writes the level-set restart of the finest level
+// (rstfile/levelset.rst, Save_restart_file's level-set part) before seeding.
+// box_2d / box_3d are boxes whose corners (and, in 3D, edges) are the
+// geometry's singularity points and segments.  Exit status 2 on an engine
+// error.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -26,7 +31,7 @@ int main(int argc, char** argv) {
   std::string wl = "disc_hole_2d", out, prec;
   int steps = -1, every = 0;
   long long n = -1;
-  bool count_only = false, cut_cell = false, vtu = false, lset = false;
+  bool count_only = false, cut_cell = false, vtu = false, lset = false, lset_rst = false;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     auto val = [&]() -> std::string {
@@ -46,9 +51,11 @@ int main(int argc, char** argv) {
     else if (s == "--cut-cell-count") cut_cell = true;
     else if (s == "--vtu") vtu = true;
     else if (s == "--lset") lset = true;
+    else if (s == "--lset-restart") lset_rst = true;
     else if (s == "--help" || s == "-h") {
-      std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
-                  "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n");
+      std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
+                  "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n"
+                  "                   [--lset-restart]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
@@ -61,6 +68,9 @@ int main(int argc, char** argv) {
                                                prec == "fp32" ? MRSPH_FP32_SPLIT : MRSPH_FP64_PLAIN);
     else if (wl == "torus_3d") c = torus_3d(0.005, 0.02, MRSPH_KERNEL_WENDLAND, 1.3,
                                            prec == "fp64" ? MRSPH_FP64_PLAIN : MRSPH_FP32_SPLIT);
+    else if (wl == "box_3d" || wl == "box_2d")
+      c = box_with_corners(wl == "box_3d" ? 3 : 2, wl == "box_3d" ? 0.04 : 0.02, wl == "box_3d" ? 32 : 64,
+                           MRSPH_KERNEL_HYPERBOLIC, 1.0, prec == "fp32" ? MRSPH_FP32_SPLIT : MRSPH_FP64_PLAIN);
     else {
       std::fprintf(stderr, "unknown case %s\n", wl.c_str());
       return 1;
@@ -74,6 +84,7 @@ int main(int argc, char** argv) {
     if (lset)
       Level_set_binary_writer((out.empty() ? std::string(".") : out) + "/outdata")
           .Output_lset(0, sim, (int)c.levels.size() - 1, 0);
+    if (lset_rst) Save_lset_restart(sim, (out.empty() ? std::string(".") : out) + "/rstfile/levelset.rst", -1);
     if (cut_cell && n < 0) n = sim.Get_num_particles();
     sim.Initialize_case(n);
     Solver solver(sim);

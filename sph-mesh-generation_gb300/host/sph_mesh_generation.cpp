@@ -239,6 +239,68 @@ Case torus_3d(double dx_min, double dx_max, int kernel, double h_over_dx, int pr
   return c;
 }
 
+Case box_with_corners(int dim, double spacing, int grid, int kernel, double h_over_dx, int precision,
+                      unsigned long long seed, double lo_b, double hi_b, bool edges) {
+  if (dim != 2 && dim != 3) throw Error(MRSPH_ERR_ARG, "box_with_corners: dim must be 2 or 3");
+  Case c;
+  c.name = dim == 3 ? "box_3d" : "box_2d";
+  mrsph_params p = default_params(dim);
+  const int npkg_unit = grid / 4;
+  const double dpkg = 1.0 / npkg_unit;
+  const double cell_ratio = 2.0 * h_over_dx;
+  int margin_pkg = std::max(npkg_unit / 16, 1);
+  for (;;) {
+    double bl[3], br[3];
+    for (int d = 0; d < 3; d++) {
+      bl[d] = -margin_pkg * dpkg;
+      br[d] = 1.0 + margin_pkg * dpkg;
+    }
+    if (cell_levels_consistent(bl, br, dim, spacing * cell_ratio, spacing * cell_ratio)) break;
+    margin_pkg++;
+  }
+  const double lo = -margin_pkg * dpkg, hi = 1.0 + margin_pkg * dpkg;
+  const int npkg = npkg_unit + 2 * margin_pkg;
+  p.kernel = kernel;
+  p.precision = precision;
+  p.min_dl = spacing;
+  p.max_dl = spacing;
+  p.cell_ratio = cell_ratio;
+  for (int d = 0; d < 3; d++) {
+    p.box_l[d] = d < dim ? lo : 0.0;
+    p.box_r[d] = d < dim ? hi : 0.0;
+  }
+  p.seed = seed;
+  auto sdf = [=](double X, double Y, double Z) {
+    double out = std::min(std::min(X - lo_b, hi_b - X), std::min(Y - lo_b, hi_b - Y));
+    if (dim == 3) out = std::min(out, std::min(Z - lo_b, hi_b - Z));
+    return out;
+  };
+  c.params = p;
+  c.levels.push_back(make_level(sdf, dim, {lo, lo, dim == 3 ? lo : 0.0}, {dpkg, dpkg, dim == 3 ? dpkg : 1.0},
+                                {npkg, npkg, dim == 3 ? npkg : 1}));
+  c.n_particles = particle_count(c.levels, p);
+  c.steps = 200;
+  const double v[2] = {lo_b, hi_b};
+  for (int z = 0; z < (dim == 3 ? 2 : 1); z++)
+    for (int y = 0; y < 2; y++)
+      for (int x = 0; x < 2; x++) {
+        c.singularities.push_back(v[x]);
+        c.singularities.push_back(v[y]);
+        c.singularities.push_back(dim == 3 ? v[z] : 0.0);
+      }
+  if (dim == 3 && edges)
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++) {
+        const double along_x[6] = {lo_b, v[a], v[b], hi_b, v[a], v[b]};
+        const double along_y[6] = {v[a], lo_b, v[b], v[a], hi_b, v[b]};
+        const double along_z[6] = {v[a], v[b], lo_b, v[a], v[b], hi_b};
+        c.segments.insert(c.segments.end(), along_x, along_x + 6);
+        c.segments.insert(c.segments.end(), along_y, along_y + 6);
+        c.segments.insert(c.segments.end(), along_z, along_z + 6);
+      }
+  return c;
+}
+
 // ------------------------------------------------------------------ solver
 SPH_mesh_generation::SPH_mesh_generation(const Case& c, int device) : case_(c) {
   case_.params.device = device;
@@ -255,6 +317,12 @@ SPH_mesh_generation::SPH_mesh_generation(const Case& c, int device) : case_(c) {
     lv[l].phi = L.phi.data();
     lv[l].active = L.active.empty() ? nullptr : L.active.data();
   }
+  if (!case_.singularities.empty() || !case_.segments.empty())
+    check(mrsph_set_characteristics(h_, (int)(case_.singularities.size() / 3),
+                                    case_.singularities.empty() ? nullptr : case_.singularities.data(),
+                                    (int)(case_.segments.size() / 6),
+                                    case_.segments.empty() ? nullptr : case_.segments.data()),
+          "mrsph_set_characteristics");
   check(mrsph_set_levelset(h_, (int)lv.size(), lv.data()), "mrsph_set_levelset");
 }
 
@@ -534,8 +602,10 @@ std::string lset_restart_bytes(const LsetRestart& r) {
   for (int d = 0; d < 3; d++) I(r.num_pkg[d]);  // ini_num_cell
   I(1);  // num_level
   D(1.e-4);  // convergence_error
-  I(0);  // singularities
-  I(0);  // segments
+  I((int)(r.sing.size() / 3));
+  for (double v : r.sing) D(v);
+  I((int)(r.seg.size() / 6));
+  for (double v : r.seg) D(v);
   for (double v : {r.fac_max, r.fac_mid, r.fac_min, r.curv_artificial, r.total_mass, r.total_mass_surface, 0.0,
                    r.total_volume, r.total_area, 0.0, r.max_phi, 0.0, r.max_dl, r.mid_dl, r.min_dl, r.max_curv,
                    r.min_curv})
@@ -562,7 +632,9 @@ std::string lset_restart_bytes(const LsetRestart& r) {
   std::vector<int> izero(n, 0), minus(n, -1);
   const std::vector<double>* fields[6] = {&r.phi, &r.nx, &r.ny, &r.nz, &r.curv, &zero};
   for (const std::vector<double>* v : fields) b += raw_of(v->data(), n);
-  b += raw_of(r.tag.data(), n) + raw_of(izero.data(), n) + raw_of(minus.data(), n);
+  b += raw_of(r.tag.data(), n);
+  b += r.chr_tag.size() == n ? raw_of(r.chr_tag.data(), n) : raw_of(izero.data(), n);
+  b += r.chr_idx.size() == n ? raw_of(r.chr_idx.data(), n) : raw_of(minus.data(), n);
   b += raw_of(r.scale.data(), n);
   return b;
 }
@@ -596,6 +668,13 @@ std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path,
   mrsph_volume_mass_stats vm{};
   int rc = mrsph_volume_mass(sim.handle(), level, &vm, nullptr, nullptr);
   if (rc) throw Error(rc, "mrsph_volume_mass");
+  const bool has_chr = !cs.singularities.empty() || !cs.segments.empty();
+  std::vector<int> chr;
+  if (has_chr) {
+    chr.assign(lv.phi.size(), 0);
+    rc = mrsph_get_characteristics(sim.handle(), level, chr.data());
+    if (rc) throw Error(rc, "mrsph_get_characteristics");
+  }
   double dl0 = 1.e20, dl = 1.e20;
   for (int d = 0; d < dim; d++) {
     dl0 = std::min(dl0, cs.levels[0].dpkg[d] / 4.0);
@@ -614,6 +693,8 @@ std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path,
   const double mid = p.middle_dl > 0 ? p.middle_dl : 5.0 * dl0;
   LsetRestart r;
   r.dim = dim;
+  r.sing = cs.singularities;
+  r.seg = cs.segments;
   for (int d = 0; d < 3; d++) {
     r.box_l[d] = d < dim ? p.box_l[d] : 0.0;
     r.box_r[d] = d < dim ? p.box_r[d] : 0.0;
@@ -649,6 +730,11 @@ std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path,
         r.nz.push_back(nz[a]);
         r.curv.push_back(curv[level][a]);
         r.tag.push_back(tag[level][a]);
+        if (has_chr) {  // k + 1: segment k (SEGMENT_CELL 2); -(k + 1): point k (SINGULARITY_CELL 1)
+          const int e = chr[a];
+          r.chr_tag.push_back(e > 0 ? 2 : (e < 0 ? 1 : 0));
+          r.chr_idx.push_back(e > 0 ? e - 1 : (e < 0 ? -e - 1 : -1));
+        }
         double sc = 0.0;  // the scale Calculate_volume_mass leaves in the counted cells
         if (phi > 0 || std::fabs(phi) < dl) {
           double lo = p.min_dl;
@@ -904,8 +990,15 @@ std::string Level_set_binary_writer::Output_lset(int n_out, SPH_mesh_generation&
                                 {"curv", "Float32", fl(corner_average(curv[level], n, m, dim))},
                                 {"scale", "Float32", fl(corner_average(scale, n, m, dim))}};
   const std::string tags = interior_raw<int>(tag[level], n, m, dim);
+  // tag_characteristic: 1 SINGULARITY_CELL, 2 SEGMENT_CELL (glbparam.h:48-51)
+  std::vector<int> ctag(ntot, 0);
+  if (!cs.singularities.empty() || !cs.segments.empty()) {
+    rc = mrsph_get_characteristics(sim.handle(), level, ctag.data());
+    if (rc) throw Error(rc, "mrsph_get_characteristics");
+    for (int& e : ctag) e = e > 0 ? 2 : (e < 0 ? 1 : 0);
+  }
   std::vector<ImageField> cd = {{"interface", "Int32", tags},
-                                {"char", "Int32", std::string(tags.size(), '\0')},
+                                {"char", "Int32", interior_raw<int>(ctag, n, m, dim)},
                                 {"vol", "Float32", interior_raw<float>(vol, n, m, dim)},
                                 {"area", "Float32", interior_raw<float>(area, n, m, dim)}};
   std::array<int, 3> nc{{0, 0, 0}};
@@ -993,7 +1086,8 @@ static std::string host_raw(const T* p, size_t count) {
 
 extern "C" long long mrsph_host_lset_vti(const char* path, const int* ncell, const double* origin,
                                          const double* spacing, const float* phi, const float* curv,
-                                         const float* scale, const int* tag, const float* vol, const float* area) {
+                                         const float* scale, const int* tag, const float* vol, const float* area,
+                                         const int* chr) {
   std::array<int, 3> nc{{ncell[0], ncell[1], ncell[2]}};
   size_t np = 1, ncl = 1;
   for (int d = 0; d < 3; d++) {
@@ -1005,7 +1099,7 @@ extern "C" long long mrsph_host_lset_vti(const char* path, const int* ncell, con
                                             {"curv", "Float32", host_raw(curv, np)},
                                             {"scale", "Float32", host_raw(scale, np)}};
   std::vector<mrsph_host::ImageField> cd = {{"interface", "Int32", host_raw(tag, ncl)},
-                                            {"char", "Int32", host_raw(zero.data(), ncl)},
+                                            {"char", "Int32", host_raw(chr ? chr : zero.data(), ncl)},
                                             {"vol", "Float32", host_raw(vol, ncl)},
                                             {"area", "Float32", host_raw(area, ncl)}};
   const std::string b = mrsph_host::vti_bytes(nc, {{origin[0], origin[1], origin[2]}},
@@ -1045,12 +1139,18 @@ extern "C" long long mrsph_host_pvtu(int mesh, const char* piece, char* buf, lon
 // dcell[3], fac_max, fac_mid, fac_min, curv_artificial, total_mass,
 // total_mass_surface, total_volume, total_area, max_phi, max_dl, mid_dl,
 // min_dl, max_curv, min_curv; ints: dim, num_pkg[3], margin[3],
-// num_interface_cell).
+// num_interface_cell); nsing points and nseg segments; chr_tag / chr_idx
+// may be NULL (NORMAL / -1).
 extern "C" long long mrsph_host_lset_restart(const char* path, const double* hd, const int* hi, long long n,
                                              const double* phi, const double* nx, const double* ny,
                                              const double* nz, const double* curv, const int* tag,
-                                             const double* scale) {
+                                             const double* scale, int nsing, const double* sing, int nseg,
+                                             const double* seg, const int* chr_tag, const int* chr_idx) {
   mrsph_host::LsetRestart r;
+  if (nsing > 0) r.sing.assign(sing, sing + 3 * (size_t)nsing);
+  if (nseg > 0) r.seg.assign(seg, seg + 6 * (size_t)nseg);
+  if (chr_tag) r.chr_tag.assign(chr_tag, chr_tag + n);
+  if (chr_idx) r.chr_idx.assign(chr_idx, chr_idx + n);
   for (int d = 0; d < 3; d++) {
     r.box_l[d] = hd[d];
     r.box_r[d] = hd[3 + d];

@@ -43,6 +43,9 @@ struct Case {
   std::vector<LevelGrid> levels;
   long long n_particles = 0;
   int steps = 0;
+  // characteristic points (x, y, z each) and segments (x1, y1, z1, x2, y2,
+  // z2 each): Levelset::singularity and ::segment (level_set.h:37-41)
+  std::vector<double> singularities, segments;
 };
 
 // Reference defaults (sph_mesh_generation.cpp:688-703, glbparam.h:171-183).
@@ -70,6 +73,13 @@ Case disc_hole_2d(double spacing = 0.01, int grid = 256, int kernel = MRSPH_KERN
 Case torus_3d(double dx_min = 0.005, double dx_max = 0.02, int kernel = MRSPH_KERNEL_WENDLAND,
               double h_over_dx = 1.3, int precision = MRSPH_FP32_SPLIT, unsigned long long seed = 0,
               int fine_pkg = 64, int nlevels = 3);
+
+// The box [lo_b, hi_b]^dim of a unit domain with margins: phi is the
+// distance to the nearest face inside, its corners are singularity points
+// and, in 3D with edges, its 12 edges are segments.  Constant spacing.
+Case box_with_corners(int dim = 3, double spacing = 0.04, int grid = 32, int kernel = MRSPH_KERNEL_HYPERBOLIC,
+                      double h_over_dx = 1.0, int precision = MRSPH_FP64_PLAIN, unsigned long long seed = 0,
+                      double lo_b = 0.1, double hi_b = 0.9, bool edges = true);
 
 class Error : public std::runtime_error {
  public:
@@ -203,9 +213,11 @@ struct LsetRestart {
   double total_mass = 0, total_mass_surface = 0, total_volume = 0, total_area = 0;
   double max_phi = 0, max_dl = 0, mid_dl = 0, min_dl = 0, max_curv = 0, min_curv = 0;
   int num_interface_cell = 0;
-  // interior cells, x fastest
+  // characteristic points (3 doubles each) and segments (6 doubles each)
+  std::vector<double> sing, seg;
+  // interior cells, x fastest; chr_tag / chr_idx empty = NORMAL / -1
   std::vector<double> phi, nx, ny, nz, curv, scale;
-  std::vector<int> tag;
+  std::vector<int> tag, chr_tag, chr_idx;
 };
 std::string lset_restart_bytes(const LsetRestart& r);
 // Gathers the record of one level (< 0: the finest) from the engine and

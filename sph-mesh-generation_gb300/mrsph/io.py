@@ -371,7 +371,8 @@ class LevelSetWriter:
     """Level_set_binary_writer (lset_binary_writer.cpp:12-510) for one level:
     an ImageData piece over the level's interior cells with phi, curv and
     scale at the cell corners and the cut-cell tag ('interface') and
-    characteristic tag ('char', none in these geometries) per cell, the
+    characteristic tag ('char': tag_characteristic, 1 SINGULARITY, 2 SEGMENT)
+    per cell, the
     cut-cell volume 'vol' and surface area 'area' per cell (the GPU's
     Calculate_volume_mass pass, zero outside the counted cells), its PVTI
     and the mesh_lset.pvd collection."""
@@ -395,7 +396,12 @@ class LevelSetWriter:
         tag = f["tag"][sl + (slice(m, -m), slice(m, -m))].astype("<i4")
         vm = sim.volume_mass(level, cells=True)
         inner = sl + (slice(m, -m), slice(m, -m))
-        cd = [("interface", tag), ("char", np.zeros_like(tag)), ("vol", vm["vol"][inner].astype("<f4")),
+        extra = getattr(sim.case, "extra", None) or {}
+        if len(extra.get("singularities", ())) or len(extra.get("segments", ())):
+            ctag = characteristic_fields(sim.characteristic_tags(level)[inner])[0].astype("<i4")
+        else:
+            ctag = np.zeros_like(tag)
+        cd = [("interface", tag), ("char", ctag), ("vol", vm["vol"][inner].astype("<f4")),
               ("area", vm["area"][inner].astype("<f4"))]
         piece = f"mesh_lset_rank_0_step_{n_out}.vti"
         with open(os.path.join(self.outdir, piece), "wb") as fh:
@@ -442,15 +448,27 @@ def read_pst(path: str) -> np.ndarray:
 # little-endian.  Header: DIM, domain, box_l, box_r, particle_box,
 # particle_box_l, particle_box_r (float64 x 3 each), resolution (int32 x 3),
 # Lmin, Lmax, ini_num_cell (int32 x 3), num_level; level set: convergence
-# error, 0 singularities, 0 segments, the dl factors, maximum_curv_artificial,
+# error, the singularity count (int32) and points (float64 x 3 each), the
+# segment count (int32) and segments (float64 x 6 each, start then end),
+# the dl factors, maximum_curv_artificial,
 # the cut-cell totals, maximum phi / psi, maximum / middle / minimum dl,
 # maximum / minimum curvature, interface cells; level: package counts and
 # ranges, dpkg, dcell; then per interior cell (x fastest) phi, n_x, n_y, n_z,
-# curv, psi (float64), tag_interface, tag_characteristic, idx_characteristic
-# (int32) and scale (float64).  One level, as the reference writes.
+# curv, psi (float64), tag_interface, tag_characteristic (0 NORMAL, 1
+# SINGULARITY, 2 SEGMENT), idx_characteristic (-1 without) (int32) and
+# scale (float64).  One level, as the reference writes.
 _RST_HEAD = "<i" + "d" * 18 + "i" * 3 + "ii" + "i" * 3 + "i"
-_RST_LSET = "<di" + "i" + "d" * 17 + "i"
+_RST_LSET = "<" + "d" * 17 + "i"
 _RST_LEVEL = "<idd" + "i" * 21 + "d" * 6
+
+
+def characteristic_fields(chr_encoded: np.ndarray):
+    """(tag_characteristic, idx_characteristic) of Levelset_cell from the
+    engine's encoding (k + 1 on segment k, -(k + 1) at singularity k)."""
+    c = np.asarray(chr_encoded).astype(np.int32)
+    tag = np.where(c > 0, 2, np.where(c < 0, 1, 0)).astype(np.int32)
+    idx = np.where(c > 0, c - 1, np.where(c < 0, -c - 1, -1)).astype(np.int32)
+    return tag, idx
 
 
 def save_lset_restart(sim, path: str = "rstfile/levelset.rst", level: int = -1) -> str:
@@ -486,7 +504,11 @@ def save_lset_restart(sim, path: str = "rstfile/levelset.rst", level: int = -1) 
     scale = np.where((phi > 0) | (np.abs(phi) < dl), cell_scale(sim, level), 0.0)
     head = struct.pack(_RST_HEAD, dim, *domain, *box_l, *box_r, *domain, *box_l, *box_r,
                        *[4 * npkg[d] if d < dim else 1 for d in range(3)], 0, 0, *npkg, 1)
-    lset = struct.pack(_RST_LSET, 1.e-4, 0, 0, prm["max_dl"] / dl0, mid / dl0, prm["min_dl"] / dl0,
+    extra = getattr(case, "extra", None) or {}
+    sing = np.asarray(extra.get("singularities", np.zeros((0, 3))), dtype="<f8").reshape(-1, 3)
+    seg = np.asarray(extra.get("segments", np.zeros((0, 6))), dtype="<f8").reshape(-1, 6)
+    lset = struct.pack("<di", 1.e-4, len(sing)) + sing.tobytes() + struct.pack("<i", len(seg)) + seg.tobytes()
+    lset += struct.pack(_RST_LSET, prm["max_dl"] / dl0, mid / dl0, prm["min_dl"] / dl0,
                        min(1.0, cmax), vm["total_mass"], vm["total_mass_surface"], 0.0, vm["total_volume"],
                        vm["total_area"], 0.0, float(f["max_phi"]), 0.0, float(prm["max_dl"]), float(mid),
                        float(prm["min_dl"]), cmax, cmin, int(vm["num_interface_cell"]))
@@ -498,7 +520,11 @@ def save_lset_restart(sim, path: str = "rstfile/levelset.rst", level: int = -1) 
     cells = [phi, f["nx"], f["ny"], f["nz"], f["curv"], np.zeros_like(phi)]
     body = b"".join(np.ascontiguousarray(c[inner], dtype="<f8").tobytes() for c in cells)
     tag = f["tag"][inner].astype("<i4")
-    body += tag.tobytes() + np.zeros_like(tag).tobytes() + np.full_like(tag, -1).tobytes()
+    if len(sing) or len(seg):
+        ctag, cidx = characteristic_fields(sim.characteristic_tags(level)[inner])
+    else:
+        ctag, cidx = np.zeros_like(tag), np.full_like(tag, -1)
+    body += tag.tobytes() + ctag.astype("<i4").tobytes() + cidx.astype("<i4").tobytes()
     body += np.ascontiguousarray(scale[inner], dtype="<f8").tobytes()
     os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
     with open(path, "wb") as fh:
@@ -518,12 +544,12 @@ def load_lset_restart(path: str) -> dict:
            "Lmin": h[22], "Lmax": h[23], "ini_num_cell": h[24:27], "num_level": h[27]}
     ls = struct.unpack_from("<di", data, o)
     o += 12
-    if ls[1] != 0:
-        raise ValueError("restart files with singularities are not supported")
+    out["singularities"] = np.frombuffer(data, dtype="<f8", count=3 * ls[1], offset=o).reshape(-1, 3).copy()
+    o += 24 * ls[1]
     nseg = struct.unpack_from("<i", data, o)[0]
     o += 4
-    if nseg != 0:
-        raise ValueError("restart files with segments are not supported")
+    out["segments"] = np.frombuffer(data, dtype="<f8", count=6 * nseg, offset=o).reshape(-1, 6).copy()
+    o += 48 * nseg
     vals = struct.unpack_from("<" + "d" * 17 + "i", data, o)
     o += 17 * 8 + 4
     keys = ["fac_maximum_dl", "fac_middel_dl", "fac_minimum_dl", "maximum_curv_artificial", "total_mass",

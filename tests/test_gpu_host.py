@@ -97,3 +97,44 @@ def test_cpp_driver_writes_levelset_image(tmp_path):
         assert np.array_equal(a[k], b[k]), k
     for k in ("phi", "curv", "vol", "area", "scale"):
         assert np.allclose(a[k], b[k], rtol=1e-6, atol=1e-30), k
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cpp_driver_box_characteristics(tmp_path, dim):
+    """A box with corners (and edges in 3D): the C++ driver passes the
+    singularity points and segments to the engine; its level-set image
+    ('char' = tag_characteristic) and level-set restart equal the Python
+    writers' for the same workload, and its particles after relaxation match
+    the Python mirror's (SINGULARITY and SEGMENT particles included)."""
+    binary = build.build_host()
+    r = subprocess.run([binary, "--case", f"box_{dim}d", "--precision", "fp64", "--steps", "300",
+                        "--output-every", "300", "--out", str(tmp_path / "c"), "--lset", "--lset-restart"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    kw = dict(spacing=0.04, grid=32) if dim == 3 else dict(spacing=0.02, grid=64)
+    case = cases.box_with_corners(dim=dim, kernel="hyperbolic", h_over_dx=1.0, **kw)
+    g = SPHMeshGeneration(case, precision="fp64")
+    py_vti = io.LevelSetWriter(str(tmp_path / "p")).Output_lset(0, g, level=0, run_time=0)
+    py_rst = io.save_lset_restart(g, str(tmp_path / "p" / "levelset.rst"))
+    ctag = io.characteristic_fields(g.characteristic_tags(0))[0]
+    assert np.count_nonzero(ctag == 1) == len(case.extra["singularities"])
+    cpp_vti = tmp_path / "c" / "outdata" / "mesh_lset_rank_0_step_0.vti"
+    a, b = io.read_vtu(str(cpp_vti)), io.read_vtu(py_vti)
+    assert np.array_equal(a["char"], b["char"]) and np.count_nonzero(a["char"] == 1) == len(ctag[ctag == 1])
+    if dim == 3:
+        assert np.count_nonzero(a["char"] == 2) > 0
+    cpp_rst = (tmp_path / "c" / "rstfile" / "levelset.rst").read_bytes()
+    rc, rp = io.load_lset_restart(str(tmp_path / "c" / "rstfile" / "levelset.rst")), io.load_lset_restart(py_rst)
+    for k in ("singularities", "segments", "tag_characteristic", "idx_characteristic", "tag_interface", "phi"):
+        assert np.array_equal(rc[k], rp[k]), k
+    # the spacing fields differ by the two tanh implementations only
+    assert len(cpp_rst) == len(open(py_rst, "rb").read())
+    g.Initialize_case()
+    g.SPH_run_mesh_generation(300)
+    gp = g.particles(("xyz", "type"))
+    g.close()
+    cpp = io.read_pst(str(tmp_path / "c" / "rstfile_particles" / "step_300_rank_0.pst"))
+    assert d["step"] == 300 and d["flags"] & ~8 == 0
+    assert np.max(np.abs(cpp - gp["xyz"])) < 1e-12
+    assert (gp["type"] == 2).any()

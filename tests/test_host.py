@@ -35,6 +35,10 @@ def test_counts_match_python_workloads(binary):
     assert d["n_particles"] == cases.disc_hole_2d(spacing=0.02, grid=64).n_particles
     t = json.loads(run(binary, "--case", "torus_3d", "--count-only").stdout)
     assert t["n_particles"] == cases.torus_3d().n_particles
+    for dim, kw in ((2, dict(spacing=0.02, grid=64)), (3, dict(spacing=0.04, grid=32))):
+        b = json.loads(run(binary, "--case", f"box_{dim}d", "--count-only").stdout)
+        assert b["n_particles"] == cases.box_with_corners(dim=dim, kernel="hyperbolic", h_over_dx=1.0,
+                                                          **kw).n_particles
 
 
 def test_engine_error_without_gpu(binary):
@@ -86,7 +90,7 @@ def test_cpp_lset_vti_matches_python_writer(binary, tmp_path, dim):
     lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
     f = lib.mrsph_host_lset_vti
     f.restype = ctypes.c_longlong
-    f.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 9
+    f.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 10
     rng = np.random.default_rng(dim)
     nc = np.array([12, 8, 6 if dim == 3 else 0], dtype=np.int32)
     origin = np.array([-1.6, 0.0001, -0.45 if dim == 3 else 0.0])
@@ -96,12 +100,14 @@ def test_cpp_lset_vti_matches_python_writer(binary, tmp_path, dim):
     phi, curv, scale = (rng.normal(size=npt).astype("<f4") for _ in range(3))
     tag = rng.integers(0, 2, ncl).astype("<i4")
     vol, area = (rng.random(ncl).astype("<f4") for _ in range(2))
+    chr_ = rng.integers(0, 3, ncl).astype("<i4")
     p = tmp_path / "c.vti"
     size = f(str(p).encode(), nc.ctypes.data, origin.ctypes.data, spacing.ctypes.data, phi.ctypes.data,
-             curv.ctypes.data, scale.ctypes.data, tag.ctypes.data, vol.ctypes.data, area.ctypes.data)
+             curv.ctypes.data, scale.ctypes.data, tag.ctypes.data, vol.ctypes.data, area.ctypes.data,
+             chr_.ctypes.data)
     ref = io.vti_bytes([int(x) for x in nc], list(origin), list(spacing),
                        [("phi", phi), ("curv", curv), ("scale", scale)],
-                       [("interface", tag), ("char", np.zeros_like(tag)), ("vol", vol), ("area", area)])
+                       [("interface", tag), ("char", chr_), ("vol", vol), ("area", area)])
     assert size == len(ref) and p.read_bytes() == ref
 
 
@@ -115,7 +121,7 @@ def test_repr_double_matches_python(binary):
     vals = [0.0, 1.0, -1.6, 0.0001, 1e-05, 123456789.0, 1e16, 2.5e-7, 0.1 + 0.2, 3.2 / 256]
     f = lib.mrsph_host_lset_vti
     f.restype = ctypes.c_longlong
-    f.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 9
+    f.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 10
     import tempfile
     nc = np.array([1, 1, 1], dtype=np.int32)
     z8, z1 = np.zeros(8, dtype="<f4"), np.zeros(1, dtype="<f4")
@@ -126,7 +132,7 @@ def test_repr_double_matches_python(binary):
             s = np.array([v + 1.0, 2.0, 0.5])
             path = os.path.join(d, "r.vti")
             f(path.encode(), nc.ctypes.data, o.ctypes.data, s.ctypes.data, z8.ctypes.data, z8.ctypes.data,
-              z8.ctypes.data, t1.ctypes.data, z1.ctypes.data, z1.ctypes.data)
+              z8.ctypes.data, t1.ctypes.data, z1.ctypes.data, z1.ctypes.data, None)
             head = open(path, "rb").read().split(b"<PointData")[0].decode()
             ref = io.vti_bytes([1, 1, 1], list(o), list(s), [("phi", z8)], []).split(b"<PointData")[0].decode()
             assert head == ref, (v, head, ref)

@@ -212,6 +212,7 @@ def test_lset_restart_round_trip(tmp_path, dim):
         assert np.array_equal(r[k], f[g][inner]), k
     assert np.array_equal(r["tag_interface"], f["tag"][inner].astype(np.int32))
     assert np.all(r["idx_characteristic"] == -1) and np.all(r["tag_characteristic"] == 0)
+    assert r["singularities"].shape == (0, 3) and r["segments"].shape == (0, 6)
     vm = orc.volume_mass(-1)
     assert r["total_mass"] == vm["total_mass"] and r["glbl_num_interface_cell"] == vm["num_interface_cell"]
     assert r["maximum_phi"] == orc.ctx.max_phi
@@ -222,22 +223,40 @@ def test_lset_restart_round_trip(tmp_path, dim):
     assert np.all((r["scale_cells"] > 0) == counted)
 
 
+def _oracle_chr(orc, level):
+    f = orc.fields[level]
+    shp = orc.case.levels[level].phi.shape
+    enc = np.where(f["chr"] == 2, f["chr_idx"] + 1, np.where(f["chr"] == 1, -(f["chr_idx"] + 1), 0))
+    return enc.reshape(shp).astype(np.int32)
+
+
 @pytest.mark.parametrize("dim", [2, 3])
-def test_cpp_lset_restart_bytes_match_python(tmp_path, dim):
-    """The C++ host layer's level-set restart serialiser writes the bytes the
-    Python writer wrote, for the values and fields read back from it."""
-    import ctypes
-    from mrsph import build
+def test_lset_restart_characteristics(tmp_path, dim):
+    """A geometry with corners (and edges in 3D): the restart carries the
+    singularity points, the segments and each cell's tag_characteristic /
+    idx_characteristic (level_set.cpp:1053-1070)."""
     import oracle
-    build.build_host()
-    lib = ctypes.CDLL(os.path.join(os.path.dirname(io.__file__), "..", "libmrsph_host.so"))
-    f = lib.mrsph_host_lset_restart
-    f.restype = ctypes.c_longlong
-    f.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong] + [ctypes.c_void_p] * 7
-    case = cases.disc_hole_2d(spacing=0.02, grid=64) if dim == 2 else \
-        cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2)
+    case = cases.box_with_corners(dim=dim, spacing=0.04 if dim == 3 else 0.02, grid=32 if dim == 3 else 64,
+                                  kernel="hyperbolic", h_over_dx=1.0)
     orc = oracle.Oracle(case)
 
+    r = io.load_lset_restart(io.save_lset_restart(_restart_sim(case, orc), str(tmp_path / "levelset.rst")))
+    assert np.array_equal(r["singularities"], case.extra["singularities"])
+    segs = case.extra.get("segments", np.zeros((0, 6)))
+    assert np.array_equal(r["segments"], np.asarray(segs).reshape(-1, 6))
+    lv = case.levels[-1]
+    m = 4 * lv.margin
+    inner = ((slice(None),) if dim == 2 else (slice(m, -m),)) + (slice(m, -m), slice(m, -m))
+    f = orc.fields[-1]
+    shp = lv.phi.shape
+    assert np.array_equal(r["tag_characteristic"], f["chr"].reshape(shp)[inner])
+    assert np.array_equal(r["idx_characteristic"], f["chr_idx"].reshape(shp)[inner])
+    assert np.count_nonzero(r["tag_characteristic"] == 1) == len(case.extra["singularities"])
+    if dim == 3:
+        assert np.count_nonzero(r["tag_characteristic"] == 2) > 0
+
+
+def _restart_sim(case, orc):
     class RstSim(FakeSim):
         def __init__(self):
             super().__init__()
@@ -250,10 +269,37 @@ def test_cpp_lset_restart_bytes_match_python(tmp_path, dim):
                     "curv": g["curv"].reshape(shp), "tag": g["tag"].reshape(shp).astype(np.uint8),
                     "max_phi": orc.ctx.max_phi}
 
+        def characteristic_tags(self, level):
+            return _oracle_chr(orc, level)
+
         def volume_mass(self, level, cells=False):
             return orc.volume_mass(level)
+    return RstSim()
 
-    py = io.save_lset_restart(RstSim(), str(tmp_path / "py.rst"))
+
+@pytest.mark.parametrize("name", ["disc2d", "torus3d", "box2d", "box3d"])
+def test_cpp_lset_restart_bytes_match_python(tmp_path, name):
+    """The C++ host layer's level-set restart serialiser writes the bytes the
+    Python writer wrote, for the values and fields read back from it (with
+    and without characteristic points and segments)."""
+    import ctypes
+    from mrsph import build
+    import oracle
+    build.build_host()
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(io.__file__), "..", "libmrsph_host.so"))
+    f = lib.mrsph_host_lset_restart
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong] + [ctypes.c_void_p] * 7 + \
+        [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    case = {"disc2d": lambda: cases.disc_hole_2d(spacing=0.02, grid=64),
+            "torus3d": lambda: cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=2),
+            "box2d": lambda: cases.box_with_corners(dim=2, spacing=0.02, grid=64, kernel="hyperbolic",
+                                                    h_over_dx=1.0),
+            "box3d": lambda: cases.box_with_corners(dim=3, spacing=0.04, grid=32, kernel="hyperbolic",
+                                                    h_over_dx=1.0)}[name]()
+    orc = oracle.Oracle(case)
+
+    py = io.save_lset_restart(_restart_sim(case, orc), str(tmp_path / "py.rst"))
     r = io.load_lset_restart(py)
     box_r = [r["box_l"][d] + r["domain"][d] for d in range(3)]
     hd = np.array(list(r["box_l"]) + box_r + list(r["dpkg"]) + list(r["dcell"]) +
@@ -265,7 +311,12 @@ def test_cpp_lset_restart_bytes_match_python(tmp_path, dim):
     tag = np.ascontiguousarray(r["tag_interface"].ravel())
     scale = np.ascontiguousarray(r["scale_cells"].ravel())
     out = tmp_path / "cpp.rst"
+    sing = np.ascontiguousarray(r["singularities"])
+    seg = np.ascontiguousarray(r["segments"])
+    ctag = np.ascontiguousarray(r["tag_characteristic"].ravel())
+    cidx = np.ascontiguousarray(r["idx_characteristic"].ravel())
     size = f(str(out).encode(), hd.ctypes.data, hi.ctypes.data, len(tag), *[a.ctypes.data for a in arrs],
-             tag.ctypes.data, scale.ctypes.data)
+             tag.ctypes.data, scale.ctypes.data, len(sing), sing.ctypes.data if len(sing) else None,
+             len(seg), seg.ctypes.data if len(seg) else None, ctag.ctypes.data, cidx.ctypes.data)
     ref = open(py, "rb").read()
     assert size == len(ref) and out.read_bytes() == ref
