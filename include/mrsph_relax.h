@@ -308,6 +308,23 @@ int mrsph_cvp(mrsph_handle* h, const mrsph_cvp_params* p, double* vp_xyz, int* l
 int mrsph_cvp_points(mrsph_handle* h, long long n, const double* xyz, const double* mass,
                      const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass,
                      mrsph_cvp_result* res);
+/* Level-set partition with ghost VPs: Voronoi_lset::
+ * Partitioning_for_initial_VP_distribution (src/CVP/voronoi_lset.cpp:824-889)
+ * on weighted points (the level set's package centres with their total mass
+ * and surface mass, lset_package.cpp:1283-1397).  The points start coloured
+ * by their nearest VP (Voronoi_lset::Initialize, :147-169).  Each iteration
+ * first mirrors, in VP order, every VP k > 0 whose points include one with
+ * surface mass across the surface: x - 2 phi n, with phi and the
+ * interpolated normal at the VP on the handle's level set, when phi >= 1e-6
+ * (Ghost_VP_generation, :250-308; the reference's colour > 0 test leaves VP 0
+ * out).  The ghosts then take part in the assignment: a point nearest a
+ * ghost belongs to no VP (label -1).  They also bound the VPs' cells like
+ * walls: a face with a ghost takes the VP's own pressure (:555-594).  The
+ * rest is mrsph_cvp_points.  num_vp <= 512.  ghost_xyz (num_vp x 3) and
+ * num_ghost (may be NULL) receive the last iteration's ghosts. */
+int mrsph_cvp_lset(mrsph_handle* h, long long n, const double* xyz, const double* mass, const double* mass_surface,
+                   const mrsph_cvp_params* p, double* vp_xyz, int* labels, double* vp_mass, double* ghost_xyz,
+                   int* num_ghost, mrsph_cvp_result* res);
 
 /* 2D triangulation of the relaxed particles (row A14): the neighbour-graph
  * mesh of Voronoi_construction::Local_VD_generation

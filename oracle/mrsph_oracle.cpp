@@ -1407,9 +1407,10 @@ static int cvp_clip(double (*v)[3], int nv, const double* n, double d, double (*
   return no < CVP_MAXV ? no : CVP_MAXV;
 }
 
-// plane p of VP k: unit normal n (outward of k) and offset d (n.x <= d inside)
-static void cvp_plane(const orc_cvp_params& P, const double* vp, int k, int p, double* n, double* d) {
-  const int K = P.num_vp;
+// plane p of VP k: unit normal n (outward of k) and offset d (n.x <= d inside).
+// p < K: the bisector with point p of vp (VPs, then ghost VPs); p >= K: box
+// wall p - K.  K here is the number of points (VPs and ghosts).
+static void cvp_plane(const orc_cvp_params& P, const double* vp, int k, int p, double* n, double* d, int K) {
   if (p < K) {
     const double* ck = vp + 3 * k;
     const double* cm = vp + 3 * p;
@@ -1426,11 +1427,12 @@ static void cvp_plane(const orc_cvp_params& P, const double* vp, int k, int p, d
   }
 }
 
-// face of VP k on plane p: returns 1 and area, normal, dist if non-empty
-static int cvp_face(const orc_cvp_params& P, const double* vp, int k, int p, double* area, double* nrm, double* dist) {
-  const int K = P.num_vp;
+// face of VP k on plane p: returns 1 and area, normal, dist if non-empty.
+// vp holds K points (VPs, then ghost VPs); p < K a point, p >= K wall p - K.
+static int cvp_face(const orc_cvp_params& P, const double* vp, int k, int p, double* area, double* nrm, double* dist,
+                    int K) {
   double n[3], d;
-  cvp_plane(P, vp, k, p, n, &d);
+  cvp_plane(P, vp, k, p, n, &d, K);
   double lo[3], hi[3];
   for (int q = 0; q < 3; q++) {
     lo[q] = q < P.dim ? P.box_l[q] : -0.5;
@@ -1471,7 +1473,7 @@ static int cvp_face(const orc_cvp_params& P, const double* vp, int k, int p, dou
   for (int m = 0; m < K && nv > 0; m++) {
     if (m == k || m == p) continue;
     double bn[3], bd;
-    cvp_plane(P, vp, k, m, bn, &bd);
+    cvp_plane(P, vp, k, m, bn, &bd, K);
     nv = cvp_clip(A, nv, bn, bd, B);
     for (int a = 0; a < nv; a++) for (int q = 0; q < 3; q++) A[a][q] = B[a][q];
   }
@@ -1502,10 +1504,58 @@ static inline double cvp_dist(int D, const double* a, const double* b) {  // get
   return std::sqrt(s);
 }
 
-int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const double* pmass, double* vp, int* label,
-            double* vp_mass, orc_cvp_result* res) {
-  const orc_cvp_params& P = *Pp;
-  const int K = P.num_vp, D = P.dim, NP = K + 2 * D;
+// Ghost VPs of the level-set partition, Voronoi_lset::Ghost_VP_generation
+// (voronoi_lset.cpp:250-308): every VP k > 0 (the reference's colour > 0
+// test leaves VP 0 out) whose packages include one with surface mass, in VP
+// order, mirrored across the surface, x - 2 phi n with phi and the
+// interpolated normal n at the VP, when phi >= 1e-6 there.
+static int cvp_ghosts(const orc_ctx& c, int D, int K, const double* vp, const std::vector<unsigned char>& flag,
+                      double* ghost) {
+  int G = 0;
+  for (int k = 0; k < K; k++) {
+    if (!flag[k]) continue;
+    double phi, nn[3], cv;
+    if (D == 3) sample<3>(c, vp + 3 * k, &phi, nn, &cv);
+    else sample<2>(c, vp + 3 * k, &phi, nn, &cv);
+    if (phi >= 1.e-6) {
+      for (int q = 0; q < 3; q++) ghost[3 * G + q] = q < D ? vp[3 * k + q] - 2. * phi * nn[q] : vp[3 * k + q];
+      G++;
+    }
+  }
+  return G;
+}
+
+// The partition loop; with a level set (c != NULL) the level-set partition
+// Voronoi_lset::Partitioning_for_initial_VP_distribution
+// (voronoi_lset.cpp:824-889): each iteration first makes the ghost VPs from
+// the previous assignment (the first from the nearest-VP assignment of the
+// initial VPs, as Voronoi_lset::Initialize colours the packages), then
+// assigns every point to its nearest VP or ghost (label -1 for a ghost: the
+// point belongs to no VP), and the ghosts bound the VPs' cells like walls
+// (a face with a ghost takes the VP's own pressure).
+static int cvp_core(const orc_cvp_params& P, const orc_ctx* c, long long n, const double* xyz, const double* pmass,
+                    const double* psurf, double* vp, int* label, double* vp_mass, double* ghost_out, int* nghost_out,
+                    orc_cvp_result* res) {
+  const int K = P.num_vp, D = P.dim;
+  const int GM = c ? K : 0;           // ghost slots
+  const int NP = K + GM + 2 * D;      // planes per VP: VPs, ghost slots, walls
+  std::vector<double> src(3 * (size_t)(K + GM));
+  std::vector<unsigned char> flag(K, 0);
+  int G = 0;
+  auto nearest = [&](const double* x, int ns) {
+    double best = 1.e20;
+    int idx = 0;
+    for (int k = 0; k < ns; k++) {
+      double dd = cvp_dist(D, x, src.data() + 3 * k);
+      if (dd < best) { best = dd; idx = k; }
+    }
+    return idx;
+  };
+  if (c) {  // Voronoi_lset::Initialize: packages coloured by their nearest VP
+    for (int q = 0; q < 3 * K; q++) src[q] = vp[q];
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; i++) label[i] = nearest(xyz + 3 * i, K);
+  }
   const long long nchunk = (n + CVP_CHUNK - 1) / CVP_CHUNK;
   std::vector<double> part((size_t)nchunk * K * 5), tmass(nchunk);
   // Set_target_mass (voronoi.cpp:495-510), chunked order
@@ -1525,16 +1575,20 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
   double error_max = 0.0, total_energy = 0.0;
   for (iter = 0; iter <= P.max_iter && converged == 0; iter++) {
     double scale_coeff = 0.25 + 1.75 * (1. - AMIN1((iter - 1) / 500., 1.));
-    // assignment: Get_CPU_id (voronoi.cpp:480-493), strict <
+    for (int q = 0; q < 3 * K; q++) src[q] = vp[q];
+    G = 0;
+    if (c) {
+      std::fill(flag.begin(), flag.end(), (unsigned char)0);
+      for (long long i = 0; i < n; i++)
+        if (psurf[i] > 0. && label[i] > 0) flag[label[i]] = 1;
+      G = cvp_ghosts(*c, D, K, vp, flag, src.data() + 3 * K);
+    }
+    // assignment: Get_CPU_id (voronoi.cpp:480-493) / find_voronoi_cell over
+    // VPs and ghosts (voronoi_lset.cpp:435-445), strict <
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < n; i++) {
-      double best = 1.e20;
-      int idx = 0;
-      for (int k = 0; k < K; k++) {
-        double dd = cvp_dist(D, xyz + 3 * i, vp + 3 * k);
-        if (dd < best) { best = dd; idx = k; }
-      }
-      label[i] = idx;
+      const int idx = nearest(xyz + 3 * i, K + G);
+      label[i] = idx < K ? idx : -1;
     }
     // mass, mass centre, energy (voronoi.cpp:617-631)
 #pragma omp parallel for schedule(static)
@@ -1585,11 +1639,13 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
 #pragma omp parallel for schedule(dynamic, 4)
     for (long long t = 0; t < (long long)K * NP; t++) {
       int k = (int)(t / NP), p = (int)(t % NP);
-      int pp = (p < K) ? p : K + (p - K);  // walls: x-, x+, y-, y+, (z-, z+)
       fex[t] = 0;
       if (p < K && p == k) continue;
+      if (p >= K && p < K + GM && p - K >= G) continue;  // unused ghost slot
+      // point index among the K + G points, or wall K + G + w (x-, x+, y-, y+, z-, z+)
+      int pp = p < K + GM ? p : K + G + (p - K - GM);
       double ar, nn[3], ds;
-      if (cvp_face(P, vp, k, pp, &ar, nn, &ds)) {
+      if (cvp_face(P, src.data(), k, pp, &ar, nn, &ds, K + G)) {
         fex[t] = 1;
         farea[t] = ar;
         fnrm[3 * t] = nn[0]; fnrm[3 * t + 1] = nn[1]; fnrm[3 * t + 2] = nn[2];
@@ -1663,8 +1719,24 @@ int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const doub
     relax = AMIN1(relax, 0.90);
   }
   if (vp_mass) for (int k = 0; k < K; k++) vp_mass[k] = mass[k];
+  if (ghost_out) for (int q = 0; q < 3 * G; q++) ghost_out[q] = src[3 * K + q];
+  if (nghost_out) *nghost_out = G;
   if (res) { res->iterations = iter; res->converged = converged; res->error_max = error_max; res->total_energy = total_energy; }
   return 0;
+}
+
+int orc_cvp(const orc_cvp_params* Pp, long long n, const double* xyz, const double* pmass, double* vp, int* label,
+            double* vp_mass, orc_cvp_result* res) {
+  return cvp_core(*Pp, nullptr, n, xyz, pmass, nullptr, vp, label, vp_mass, nullptr, nullptr, res);
+}
+
+// level-set partition of weighted points (package centres) with ghost VPs;
+// psurf: the points' surface mass; ghost (K x 3, may be NULL) and nghost
+// receive the last iteration's ghosts
+int orc_cvp_lset(const orc_ctx* c, const orc_cvp_params* Pp, long long n, const double* xyz, const double* pmass,
+                 const double* psurf, double* vp, int* label, double* vp_mass, double* ghost, int* nghost,
+                 orc_cvp_result* res) {
+  return cvp_core(*Pp, c, n, xyz, pmass, psurf, vp, label, vp_mass, ghost, nghost, res);
 }
 
 // ===========================================================================

@@ -147,6 +147,9 @@ def lib():
         L.orc_triangulate.restype = C.c_longlong
         L.orc_cvp.argtypes = [C.POINTER(OrcCvpParams), C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_void_p, C.c_void_p, C.POINTER(OrcCvpResult)]
+        L.orc_cvp_lset.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcCvpParams), C.c_longlong, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.POINTER(C.c_int), C.POINTER(OrcCvpResult)]
         L.orc_mc_table.argtypes = [C.c_void_p]
         L.orc_mc_area.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
         L.orc_mc_area.restype = C.c_double
@@ -379,6 +382,33 @@ class Oracle:
         tag = np.zeros(n, dtype=np.int32)
         lib().orc_sample(C.byref(self.ctx), n, _p(xyz), _p(phi), _p(nrm), _p(curv), _p(tag))
         return phi, nrm, curv, tag
+
+    def cvp_lset(self, xyz, mass, mass_surface, vp_xyz, max_iter=800, error_tolerance=0.05, relax_ratio=0.8,
+                 pressure_step=True):
+        """Voronoi_lset::Partitioning_for_initial_VP_distribution restated
+        (CVP/voronoi_lset.cpp:824-889) on weighted points with ghost VPs on
+        this oracle's level set."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        vp = np.ascontiguousarray(vp_xyz, dtype=np.float64).reshape(-1, 3).copy()
+        n, K = len(xyz), len(vp)
+        pm = np.ascontiguousarray(mass, dtype=np.float64)
+        ps = np.ascontiguousarray(mass_surface, dtype=np.float64)
+        p = OrcCvpParams()
+        p.dim, p.num_vp, p.max_iter, p.pressure_step = self.ctx.dim, K, max_iter, 1 if pressure_step else 0
+        p.error_tolerance, p.relax_ratio = error_tolerance, relax_ratio
+        for d in range(3):
+            p.box_l[d] = self.case.params["box_l"][d]
+            p.box_r[d] = self.case.params["box_r"][d]
+        labels = np.zeros(n, dtype=np.int32)
+        vmass = np.zeros(K)
+        ghost = np.zeros((K, 3))
+        ng = C.c_int(0)
+        res = OrcCvpResult()
+        lib().orc_cvp_lset(C.byref(self.ctx), C.byref(p), n, _p(xyz), _p(pm), _p(ps), _p(vp), _p(labels),
+                           _p(vmass), _p(ghost), C.byref(ng), C.byref(res))
+        out = {f: getattr(res, f) for f, _ in OrcCvpResult._fields_}
+        out["ghosts"] = ghost[: ng.value].copy()
+        return vp, labels, vmass, out
 
     def triangulate(self, xyz, type_, phi, off, nbr):
         """2D neighbour-graph triangulation + quality (graph_mesh.cpp:37-670), id space."""

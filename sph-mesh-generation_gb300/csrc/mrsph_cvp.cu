@@ -13,6 +13,11 @@
 //                   (replaces voro++, voronoi.cpp:724-790)
 //   k_cvp_update    face pressure force, h, Update_position (voronoi.cpp:830-897),
 //                   Update_position_CVT (:901-992), Check_partition_error (:1228-1262)
+// The level-set partition (Voronoi_lset::Partitioning_for_initial_VP_distribution,
+// voronoi_lset.cpp:824-889) adds, before the assignment, k_cvp_flags and
+// k_cvp_ghosts: the ghost VPs (Ghost_VP_generation, :250-308), which take
+// part in the assignment (a point nearest a ghost belongs to no VP, label -1)
+// and bound the VPs' cells like walls.
 // Compiled with -fmad=false: every operation rounds as written, in the same
 // order as the oracle, so labels and VP positions match it bit for bit.
 #include <cuda_runtime.h>
@@ -29,14 +34,18 @@ constexpr int CVP_CHUNK = 2048;
 constexpr int CVP_MAXV = 64;
 constexpr int CVP_MAX_K = 1024;
 
+// K VPs; the points that bound their cells are the K VPs, then GM ghost
+// slots (0 without a level set, else K), then the 2 D box walls: NP planes
+// per VP.  Bisector planes are stored per VP for the K + GM points.
 struct CvpGeo {
-  int dim, K, NP;
+  int dim, K, GM, NP;
   double box_l[3], box_r[3];
 };
 
 struct CvpState {  // device-resident iteration state
   double relax, error_record, error_max, total_energy, target;
   int converged, iter;
+  int nghost;  // ghosts of the current iteration (in slots K .. K + nghost - 1)
 };
 
 __device__ inline double cdot(const double* a, const double* b) {
@@ -77,8 +86,10 @@ __device__ int cclip(double (*v)[3], int nv, const double* n, double d, double (
   return no < CVP_MAXV ? no : CVP_MAXV;
 }
 
+// plane p of VP k: a bisector with point p (p < K + GM; vp holds the VPs and
+// the ghost slots) or wall p - K - GM
 __device__ void cplane(const CvpGeo& G, const double* vp, int k, int p, double* n, double* d) {
-  if (p < G.K) {
+  if (p < G.K + G.GM) {
     const double* ck = vp + 3 * k;
     const double* cm = vp + 3 * p;
     double e[3] = {cm[0] - ck[0], cm[1] - ck[1], cm[2] - ck[2]};
@@ -87,7 +98,7 @@ __device__ void cplane(const CvpGeo& G, const double* vp, int k, int p, double* 
     for (int q = 0; q < 3; q++) n[q] = e[q] / len;
     *d = cdot(n, mid);
   } else {
-    int w = p - G.K, ax = w / 2, hi = w % 2;
+    int w = p - G.K - G.GM, ax = w / 2, hi = w % 2;
     n[0] = n[1] = n[2] = 0.0;
     n[ax] = hi ? 1.0 : -1.0;
     *d = hi ? G.box_r[ax] : -G.box_l[ax];
@@ -99,12 +110,14 @@ __device__ void cplane(const CvpGeo& G, const double* vp, int k, int p, double* 
 // FP32 error bound of it (1e-6 x (coordinate magnitude + distance), several
 // times the bound) are then compared in FP64, in index order.  Every VP whose
 // FP64 distance ties the minimum is among them, so the label is the one the
-// full FP64 scan gives.
-__global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int K, const double* __restrict__ vp,
-                             int D, int* __restrict__ label) {
+// full FP64 scan gives.  vp holds the K VPs and then st->nghost ghost VPs
+// (st NULL: none); a point nearest a ghost gets label -1.
+__global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int KV, const double* __restrict__ vp,
+                             int D, int* __restrict__ label, const CvpState* st) {
   __shared__ double s_vp[3 * CVP_MAX_K];
   __shared__ float4 s_vf[CVP_MAX_K];
   __shared__ float s_lvp;
+  const int K = KV + (st ? st->nghost : 0);
   for (int t = threadIdx.x; t < 3 * K; t += blockDim.x) s_vp[t] = vp[t];
   __syncthreads();
   for (int t = threadIdx.x; t < K; t += blockDim.x)
@@ -133,7 +146,7 @@ __global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int K,
   const float thr = df + 2.e-6f * (L + df) + 1.e-30f;
   const float T = thr * thr * 1.0001f;
   if (b2 > T) {  // no other VP within the bound: the FP64 scan would pick bk
-    label[i] = bk;
+    label[i] = bk < KV ? bk : -1;
     return;
   }
   double best = 1.e20;
@@ -145,7 +158,42 @@ __global__ void k_cvp_assign(long long n, const double* __restrict__ xyz, int K,
     double dd = cdist(D, x, s_vp + 3 * k);
     if (dd < best) { best = dd; idx = k; }
   }
-  label[i] = idx;
+  label[i] = idx < KV ? idx : -1;
+}
+
+// VPs k > 0 that hold a point with surface mass (the reference's
+// contains_cutcell, colour > 0, voronoi_lset.cpp:256-266)
+__global__ void k_cvp_flags(long long n, const double* __restrict__ psurf, const int* __restrict__ label,
+                            unsigned char* flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int l = label[i];
+  if (l > 0 && psurf[i] > 0.) flag[l] = 1;
+}
+
+// One block: the VPs copied to the point array, then thread 0 makes the ghost
+// VPs in VP order (Ghost_VP_generation, voronoi_lset.cpp:276-301): x - 2 phi n
+// with phi and the interpolated normal at the VP, when phi >= 1e-6 there;
+// the flags are cleared for the next iteration.
+template <int D>
+__global__ void k_cvp_ghosts(LsSet ls, int K, const double* __restrict__ vp, unsigned char* flag, double* src,
+                             CvpState* st) {
+  for (int t = threadIdx.x; t < 3 * K; t += blockDim.x) src[t] = vp[t];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  int G = 0;
+  for (int k = 0; k < K; k++) {
+    if (!flag[k]) continue;
+    flag[k] = 0;
+    double phi, nn[3], cv;
+    ls_sample<D, double>(ls, vp + 3 * k, phi, nn, cv);
+    if (phi >= 1.e-6) {
+      double* g = src + 3 * (K + G);
+      for (int q = 0; q < 3; q++) g[q] = q < D ? vp[3 * k + q] - 2. * phi * nn[q] : vp[3 * k + q];
+      G++;
+    }
+  }
+  st->nghost = G;
 }
 
 // total point mass in chunked order (Set_target_mass, voronoi.cpp:495-510)
@@ -187,7 +235,7 @@ __global__ void __launch_bounds__(256) k_cvp_partials(long long n, const double*
   for (int t = tid; t < m; t += blockDim.x) {
     const int l = __ldg(&label[b + t]);
     s_lab[t] = l;
-    atomicAdd(&s_cur[l], 1);
+    if (l >= 0) atomicAdd(&s_cur[l], 1);  // -1: nearest a ghost, no VP
   }
   __syncthreads();
   if (tid < 32) {  // exclusive scan of the counts; s_cur becomes each VP's fill cursor
@@ -212,7 +260,7 @@ __global__ void __launch_bounds__(256) k_cvp_partials(long long n, const double*
     // take consecutive slots in lane order
     for (int t0 = 0; t0 < m; t0 += 32) {
       const int t = t0 + lane;
-      const bool ok = t < m;
+      const bool ok = t < m && s_lab[t] >= 0;
       const unsigned act = __ballot_sync(0xffffffffu, ok);
       if (ok) {
         const int l = s_lab[t];
@@ -272,13 +320,15 @@ __global__ void k_cvp_reduce(long long nchunk, int K, int D, const double* __res
   err[k] = fabs(m - target) / target;
 }
 
-// bisector planes of every VP pair, computed once per iteration
+// bisector planes of every (VP, point) pair, computed once per iteration
+// (row stride K + GM; slots of absent ghosts are left alone)
 __global__ void k_cvp_planes(CvpGeo G, const double* __restrict__ vp, double* __restrict__ planes,
-                             float4* __restrict__ planes_f) {
+                             float4* __restrict__ planes_f, const CvpState* st) {
+  const int PS = G.K + G.GM;
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)G.K * G.K) return;
-  int k = (int)(t / G.K), m = (int)(t % G.K);
-  if (k == m) return;
+  if (t >= (long long)G.K * PS) return;
+  int k = (int)(t / PS), m = (int)(t % PS);
+  if (k == m || m >= G.K + st->nghost) return;
   double n[3], d;
   cplane(G, vp, k, m, n, &d);
   double* o = planes + 4 * t;
@@ -308,16 +358,19 @@ __device__ inline void cbound(double (*v)[3], int nv, double* C, double* r) {
 // an FP32 skip is always an FP64 skip; the others take the FP64 test.
 __global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __restrict__ vp,
                                                    const double* __restrict__ planes,
-                                                   const float4* __restrict__ planes_f, double* __restrict__ face) {
+                                                   const float4* __restrict__ planes_f, double* __restrict__ face,
+                                                   const CvpState* st) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)G.K * G.NP) return;
   int k = (int)(t / G.NP), p = (int)(t % G.NP);
   double* out = face + 6 * t;
   out[0] = 0.0;
   if (p < G.K && p == k) return;
+  const int PS = G.K + G.GM, NPT = G.K + st->nghost;  // plane row stride, points present
+  if (p >= NPT && p < PS) return;  // an unused ghost slot
   double n[3], d;
-  if (p < G.K) {
-    const double* pl = planes + 4 * ((long long)k * G.K + p);
+  if (p < PS) {
+    const double* pl = planes + 4 * ((long long)k * PS + p);
     n[0] = pl[0]; n[1] = pl[1]; n[2] = pl[2]; d = pl[3];
   } else {
     cplane(G, vp, k, p, n, &d);
@@ -364,16 +417,16 @@ __global__ void __launch_bounds__(128) k_cvp_faces(CvpGeo G, const double* __res
     rf = (float)r;
   };
   for (int wq = 0; wq < 6 && nv > 0; wq++) {
-    if (p >= G.K && wq == p - G.K) continue;
+    if (p >= PS && wq == p - PS) continue;
     int axw = wq / 2, hw = wq % 2;
     double wn[3] = {0, 0, 0};
     wn[axw] = hw ? 1.0 : -1.0;
     double wd = hw ? hi[axw] : -lo[axw];
     clip(wn, wd);
   }
-  const double* pk = planes + 4 * (long long)k * G.K;
-  const float4* pkf = planes_f + (long long)k * G.K;
-  for (int m = 0; m < G.K && nv > 0; m++) {
+  const double* pk = planes + 4 * (long long)k * PS;
+  const float4* pkf = planes_f + (long long)k * PS;
+  for (int m = 0; m < NPT && nv > 0; m++) {
     if (m == k || m == p) continue;
     const float4 pf = __ldg(&pkf[m]);
     const float scf = (pf.x * Cf[0] + pf.y * Cf[1] + pf.z * Cf[2]) - pf.w;
@@ -527,14 +580,20 @@ int cfail(mrsph_handle* h, int code, const std::string& msg) {
     if (e_ != cudaSuccess) { rc = cfail(h, MRSPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); goto done; } \
   } while (0)
 
-// Core loop on device points (xyz n x 3, pm n), id order.
+// Core loop on device points (xyz n x 3, pm n), id order.  d_ps (surface
+// mass per point) not NULL: the level-set partition with ghost VPs on the
+// handle's level set; ghost_xyz (K x 3) / nghost (may be NULL) receive the
+// last iteration's ghosts.
 int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrsph_cvp_params* p, double* vp_xyz,
-            int* labels, double* vp_mass, mrsph_cvp_result* res) {
+            int* labels, double* vp_mass, mrsph_cvp_result* res, const double* d_ps = nullptr,
+            double* ghost_xyz = nullptr, int* nghost = nullptr) {
   const int K = p->num_vp, D = h->prm.dim;
+  const bool ghosts = d_ps != nullptr;
   CvpGeo G;
   G.dim = D;
   G.K = K;
-  G.NP = K + 2 * D;
+  G.GM = ghosts ? K : 0;
+  G.NP = K + G.GM + 2 * D;
   for (int q = 0; q < 3; q++) {
     G.box_l[q] = h->prm.box_l[q];
     G.box_r[q] = h->prm.box_r[q];
@@ -544,8 +603,11 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
   int rc = 0;
   std::vector<void*> mem;
   double *d_vp = nullptr, *d_part = nullptr, *d_face = nullptr, *d_k = nullptr, *d_tm = nullptr, *d_planes = nullptr;
+  double* d_src = nullptr;  // VPs then ghost VPs (level-set partition)
+  unsigned char* d_flag = nullptr;
   float4* d_planes_f = nullptr;
   int* d_label = nullptr;
+  const size_t PS = (size_t)K + G.GM;
   CvpState* d_st = nullptr;
   CvpState hs;
   std::memset(&hs, 0, sizeof(hs));
@@ -558,8 +620,13 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
   CV_CK(A((void**)&d_vp, sizeof(double) * 3 * K));
   CV_CK(A((void**)&d_part, sizeof(double) * 5 * K * nchunk));
   CV_CK(A((void**)&d_face, sizeof(double) * 6 * (size_t)K * G.NP));
-  CV_CK(A((void**)&d_planes, sizeof(double) * 4 * (size_t)K * K));
-  CV_CK(A((void**)&d_planes_f, sizeof(float4) * (size_t)K * K));
+  CV_CK(A((void**)&d_planes, sizeof(double) * 4 * (size_t)K * PS));
+  CV_CK(A((void**)&d_planes_f, sizeof(float4) * (size_t)K * PS));
+  if (ghosts) {
+    CV_CK(A((void**)&d_src, sizeof(double) * 3 * PS));
+    CV_CK(A((void**)&d_flag, (size_t)K));
+    CV_CK(cudaMemsetAsync(d_flag, 0, (size_t)K, h->stream));
+  }
   CV_CK(A((void**)&d_k, sizeof(double) * 12 * K));  // mass, mc(3), energy, P, err, f(3), hk, pad
   CV_CK(A((void**)&d_tm, sizeof(double) * nchunk));
   CV_CK(A((void**)&d_label, sizeof(int) * n));
@@ -575,13 +642,21 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
     k_cvp_target<<<1, 1, 0, s>>>(nchunk, d_tm, K, d_st);
     const int nb = (int)((n + 255) / 256);
     const int ftot = K * G.NP;
+    const double* pts = ghosts ? d_src : d_vp;  // the points that bound the cells
+    // Voronoi_lset::Initialize: points coloured by their nearest VP
+    if (ghosts) k_cvp_assign<<<nb, 256, 0, s>>>(n, d_xyz, K, d_vp, D, d_label, nullptr);
     int it = 0;
     for (; it <= p->max_iter; it++) {
-      k_cvp_assign<<<nb, 256, 0, s>>>(n, d_xyz, K, d_vp, D, d_label);
+      if (ghosts) {
+        k_cvp_flags<<<nb, 256, 0, s>>>(n, d_ps, d_label, d_flag);
+        if (D == 3) k_cvp_ghosts<3><<<1, 256, 0, s>>>(h->ls, K, d_vp, d_flag, d_src, d_st);
+        else k_cvp_ghosts<2><<<1, 256, 0, s>>>(h->ls, K, d_vp, d_flag, d_src, d_st);
+      }
+      k_cvp_assign<<<nb, 256, 0, s>>>(n, d_xyz, K, pts, D, d_label, d_st);
       k_cvp_partials<<<(unsigned)nchunk, 256, 0, s>>>(n, d_xyz, d_pm, d_label, K, d_vp, D, d_part);
       k_cvp_reduce<<<(K + 127) / 128, 128, 0, s>>>(nchunk, K, D, d_part, d_st, d_vp, mass, mc, energy, P, err);
-      k_cvp_planes<<<(K * K + 255) / 256, 256, 0, s>>>(G, d_vp, d_planes, d_planes_f);
-      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, d_vp, d_planes, d_planes_f, d_face);
+      k_cvp_planes<<<(int)((K * PS + 255) / 256), 256, 0, s>>>(G, pts, d_planes, d_planes_f, d_st);
+      k_cvp_faces<<<(ftot + 127) / 128, 128, 0, s>>>(G, pts, d_planes, d_planes_f, d_face, d_st);
       k_cvp_update<<<1, (K + 31) / 32 * 32, 0, s>>>(G, d_vp, d_face, mass, mc, energy, P, err, f, hk, vp3, d_st,
                                                    p->error_tolerance, p->pressure_step);
       CV_CK(cudaGetLastError());
@@ -592,7 +667,10 @@ int cvp_run(mrsph_handle* h, long long n, double* d_xyz, double* d_pm, const mrs
     CV_CK(cudaMemcpyAsync(vp_xyz, d_vp, sizeof(double) * 3 * K, cudaMemcpyDeviceToHost, s));
     if (labels) CV_CK(cudaMemcpyAsync(labels, d_label, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
     if (vp_mass) CV_CK(cudaMemcpyAsync(vp_mass, mass, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+    if (ghosts && ghost_xyz)
+      CV_CK(cudaMemcpyAsync(ghost_xyz, d_src + 3 * (size_t)K, sizeof(double) * 3 * K, cudaMemcpyDeviceToHost, s));
     CV_CK(cudaStreamSynchronize(s));
+    if (nghost) *nghost = ghosts ? hs.nghost : 0;
     if (res) {
       res->iterations = it;
       res->converged = hs.converged;
@@ -639,6 +717,32 @@ extern "C" int mrsph_cvp_points(mrsph_handle* h, long long n, const double* xyz,
   rc = cvp_run(h, n, d_xyz, d_pm, p, vp_xyz, labels, vp_mass, res);
   cudaFree(d_xyz);
   cudaFree(d_pm);
+  return rc;
+}
+
+extern "C" int mrsph_cvp_lset(mrsph_handle* h, long long n, const double* xyz, const double* mass,
+                              const double* mass_surface, const mrsph_cvp_params* p, double* vp_xyz, int* labels,
+                              double* vp_mass, double* ghost_xyz, int* num_ghost, mrsph_cvp_result* res) {
+  int rc = cvp_check(h, p, vp_xyz);
+  if (rc) return rc;
+  if (n <= 0 || !xyz || !mass || !mass_surface) return cfail(h, MRSPH_ERR_ARG, "no points or masses");
+  if (2 * p->num_vp > CVP_MAX_K) return cfail(h, MRSPH_ERR_RANGE, "num_vp must be 1..512 with ghost VPs");
+  if (h->nls < 1) return cfail(h, MRSPH_ERR_STATE, "mrsph_set_levelset must come first");
+  if (cudaSetDevice(h->prm.device) != cudaSuccess) return cfail(h, MRSPH_ERR_CUDA, "cudaSetDevice failed");
+  double *d_xyz = nullptr, *d_pm = nullptr, *d_ps = nullptr;
+  if (cudaMalloc(&d_xyz, sizeof(double) * 3 * n) != cudaSuccess || cudaMalloc(&d_pm, sizeof(double) * n) != cudaSuccess ||
+      cudaMalloc(&d_ps, sizeof(double) * n) != cudaSuccess) {
+    cudaFree(d_xyz);
+    cudaFree(d_pm);
+    return cfail(h, MRSPH_ERR_OOM, "cudaMalloc failed");
+  }
+  cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(d_pm, mass, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(d_ps, mass_surface, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream);
+  rc = cvp_run(h, n, d_xyz, d_pm, p, vp_xyz, labels, vp_mass, res, d_ps, ghost_xyz, num_ghost);
+  cudaFree(d_xyz);
+  cudaFree(d_pm);
+  cudaFree(d_ps);
   return rc;
 }
 

@@ -105,6 +105,9 @@ EXPORTS = {
                   C.c_int),
     "mrsph_cvp_points": ([C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p, C.POINTER(CvpParams), C.c_void_p,
                           C.c_void_p, C.c_void_p, C.POINTER(CvpResult)], C.c_int),
+    "mrsph_cvp_lset": ([C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(CvpParams),
+                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.POINTER(CvpResult)],
+                       C.c_int),
     "mrsph_triangulate": ([C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(TriQuality)],
                           C.c_int),
     "mrsph_batch_create": ([C.c_void_p, C.c_int, C.POINTER(C.c_void_p)], C.c_int),

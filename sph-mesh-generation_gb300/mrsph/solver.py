@@ -307,6 +307,61 @@ class SPHMeshGeneration:
                                           _ptr(labels), _ptr(vmass), C.byref(res)), self.h, "mrsph_cvp_points")
         return vp, labels, vmass, {f: getattr(res, f) for f, _ in L.CvpResult._fields_}
 
+    def lset_packages(self, level: int = 0):
+        """The interior packages of one level-set level with mass: centres and
+        total / surface mass, Levelset_package::Calculate_volume_mass
+        (lset_package.cpp:1283-1397): sum of vol / scale^D and of area /
+        scale^(D-1) over the package's cells, scale the cell's target spacing.
+        Returns (xyz, mass, mass_surface) in package order (x fastest)."""
+        from .io import cell_scale
+        lv = self.case.levels[level]
+        dim = self.case.params["dim"]
+        vm = self.volume_mass(level, cells=True)
+        sc = cell_scale(self, level)
+        m = lv.margin
+        with np.errstate(divide="ignore", invalid="ignore"):
+            cm = np.where(vm["vol"] > 0, vm["vol"] / sc ** dim, 0.0)
+            cs = np.where(vm["area"] > 0, vm["area"] / sc ** (dim - 1), 0.0)
+        npk = [lv.num_pkg[d] + 2 * m if d < dim else 1 for d in range(3)]
+        cz = 4 if dim == 3 else 1
+        def per_pkg(a):
+            a = a.reshape(npk[2], cz, npk[1], 4, npk[0], 4)
+            return a.sum(axis=(1, 3, 5))
+        pm, ps = per_pkg(cm), per_pkg(cs)
+        sl = (slice(m, -m) if dim == 3 else slice(None), slice(m, -m), slice(m, -m))
+        pm, ps = pm[sl], ps[sl]
+        idx = np.stack(np.meshgrid(*[np.arange(pm.shape[a]) for a in range(3)], indexing="ij"), -1).reshape(-1, 3)
+        centre = np.zeros((len(idx), 3))
+        for d in range(dim):
+            centre[:, d] = lv.box_l[d] + (idx[:, 2 - d] + 0.5) * lv.dpkg[d]
+        keep = pm.ravel() > 0
+        return centre[keep], pm.ravel()[keep], ps.ravel()[keep]
+
+    def partition_lset(self, xyz: np.ndarray, mass: np.ndarray, mass_surface: np.ndarray, vp_xyz: np.ndarray,
+                       max_iter: int = 800, error_tolerance: float = 0.05, relax_ratio: float = 0.8,
+                       pressure_step: bool = True):
+        """Voronoi_lset::Partitioning_for_initial_VP_distribution
+        (CVP/voronoi_lset.cpp:824-889): the level-set partition of weighted
+        package centres with ghost VPs.  Returns (vp, labels (-1: nearest a
+        ghost), vp mass, result dict incl. 'ghosts')."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        pm = np.ascontiguousarray(mass, dtype=np.float64)
+        ps = np.ascontiguousarray(mass_surface, dtype=np.float64)
+        vp = np.ascontiguousarray(vp_xyz, dtype=np.float64).reshape(-1, 3).copy()
+        K = len(vp)
+        labels = np.zeros(len(xyz), dtype=np.int32)
+        vmass = np.zeros(K)
+        ghost = np.zeros((K, 3))
+        ng = C.c_int(0)
+        res = L.CvpResult()
+        prm = self._cvp_params(K, max_iter, error_tolerance, relax_ratio, pressure_step)
+        L.check(self.lib.mrsph_cvp_lset(self.h, len(xyz), _ptr(xyz), _ptr(pm), _ptr(ps), C.byref(prm), _ptr(vp),
+                                        _ptr(labels), _ptr(vmass), _ptr(ghost), C.byref(ng), C.byref(res)),
+                self.h, "mrsph_cvp_lset")
+        out = {f: getattr(res, f) for f, _ in L.CvpResult._fields_}
+        out["ghosts"] = ghost[: ng.value].copy()
+        return vp, labels, vmass, out
+
     # -------------------------------------------------------- triangulation
     def Reconstruct_tris(self):
         """2D triangle mesh of the current particles and its quality statistics
