@@ -27,6 +27,7 @@
 //     each phase its own kernel (own register allocation, read-only loads).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -65,9 +66,19 @@ __host__ __device__ constexpr int phase_min_blocks(int ph) {
          : ph == BP_FORCE2 ? MRSPH_FORCE2_MIN_BLOCKS : 1;
 }
 
-// item lists: 0 one item per geometry, 1 particle blocks, 2 scan blocks
+// item lists: 0 one item per geometry, 1 particle blocks, 2 scan blocks,
+// 3 queue blocks (the density fix-up and the spilled force stages, whose
+// queues hold a few per cent of a geometry's particles at most: one item per
+// MRSPH_BATCH_QUEUE_DIV particle blocks, at least one per geometry, each
+// striding over the geometry's queue)
+constexpr int kBatchLists = 4;
+#ifndef MRSPH_BATCH_QUEUE_DIV
+#define MRSPH_BATCH_QUEUE_DIV 16
+#endif
 __host__ __device__ inline int phase_list(int ph) {
-  return (ph == BP_BEGIN || ph == BP_SCAN_TOP) ? 0 : (ph == BP_SCAN_REDUCE || ph == BP_SCAN_DOWN) ? 2 : 1;
+  return (ph == BP_BEGIN || ph == BP_SCAN_TOP) ? 0
+         : (ph == BP_SCAN_REDUCE || ph == BP_SCAN_DOWN) ? 2
+         : (ph == BP_FIX || ph == BP_SPILL1 || ph == BP_SPILL2) ? 3 : 1;
 }
 
 // items a block claims at a time from a phase's work queue
@@ -77,8 +88,8 @@ __host__ __device__ inline int phase_list(int ph) {
 
 struct BatchPlan {
   const BatchSlot* slots;  // [ng]
-  const long long* off;    // 3 prefix tables of [ng + 1] items (lists 0, 1, 2)
-  long long nitems[3];
+  const long long* off;    // kBatchLists prefix tables of [ng + 1] items
+  long long nitems[kBatchLists];
   int ng;
   int nsteps;
   int step0;                // steps of this launch sequence already run (buffer parity)
@@ -245,7 +256,7 @@ struct Persist {
   unsigned long long* d_queue = nullptr;  // work-queue counters, 32 steps x BP_COUNT phases
   std::vector<BatchSlot> h_slots;
   std::vector<long long> h_off;
-  long long nitems[3] = {0, 0, 0};
+  long long nitems[kBatchLists] = {0, 0, 0, 0};
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // persistent launch per step count
   bool capture_ok = true;
   std::string err;
@@ -290,7 +301,7 @@ BatchPlan plan_of(const Persist& S, int nsteps, int step0) {
   BatchPlan P{};
   P.slots = S.d_slots;
   P.off = S.d_off;
-  for (int k = 0; k < 3; k++) P.nitems[k] = S.nitems[k];
+  for (int k = 0; k < kBatchLists; k++) P.nitems[k] = S.nitems[k];
   P.ng = S.ng;
   P.nsteps = nsteps;
   P.step0 = step0;
@@ -326,7 +337,7 @@ Persist* persist_create(int device, int kk, int ng) {
   S->ng = ng;
   S->grid = persist_grid(kk, device);
   if (cudaMalloc(&S->d_slots, sizeof(BatchSlot) * ng) != cudaSuccess ||
-      cudaMalloc(&S->d_off, sizeof(long long) * 3 * (ng + 1)) != cudaSuccess ||
+      cudaMalloc(&S->d_off, sizeof(long long) * kBatchLists * (ng + 1)) != cudaSuccess ||
       cudaMalloc(&S->d_flags, sizeof(unsigned) * 2) != cudaSuccess ||
       cudaMalloc(&S->d_queue, sizeof(unsigned long long) * 32 * BP_COUNT) != cudaSuccess ||
       cudaMemset(S->d_flags, 0, sizeof(unsigned) * 2) != cudaSuccess) {
@@ -358,7 +369,7 @@ bool persist_resident(const Persist* S) { return S && S->grid > 0; }
 int persist_refresh(Persist* S, EngineBase* const* engines, cudaStream_t s) {
   const int ng = S->ng;
   S->h_slots.assign(ng, BatchSlot{});
-  S->h_off.assign(3 * (ng + 1), 0);
+  S->h_off.assign(kBatchLists * (ng + 1), 0);
   for (int g = 0; g < ng; g++) {
     int rc = engines[g]->batch_slot(&S->h_slots[g]);
     if (rc) {
@@ -371,12 +382,16 @@ int persist_refresh(Persist* S, EngineBase* const* engines, cudaStream_t s) {
     S->h_off[0 * (ng + 1) + g + 1] = g + 1;
     S->h_off[1 * (ng + 1) + g + 1] = S->h_off[1 * (ng + 1) + g] + (b.c.n + kBatchThreads - 1) / kBatchThreads;
     S->h_off[2 * (ng + 1) + g + 1] = S->h_off[2 * (ng + 1) + g] + (b.ncells + kBatchScanCells - 1) / kBatchScanCells;
+    const long long pb = (b.c.n + kBatchThreads - 1) / kBatchThreads;
+    S->h_off[3 * (ng + 1) + g + 1] =
+        S->h_off[3 * (ng + 1) + g] + std::max(1LL, (pb + MRSPH_BATCH_QUEUE_DIV - 1) / MRSPH_BATCH_QUEUE_DIV);
   }
-  for (int k = 0; k < 3; k++) S->nitems[k] = S->h_off[k * (ng + 1) + ng];
+  for (int k = 0; k < kBatchLists; k++) S->nitems[k] = S->h_off[k * (ng + 1) + ng];
   // the host vectors are pageable: the copies return once staged
   if (cudaMemcpyAsync(S->d_slots, S->h_slots.data(), sizeof(BatchSlot) * ng, cudaMemcpyHostToDevice, s) !=
           cudaSuccess ||
-      cudaMemcpyAsync(S->d_off, S->h_off.data(), sizeof(long long) * 3 * (ng + 1), cudaMemcpyHostToDevice, s) !=
+      cudaMemcpyAsync(S->d_off, S->h_off.data(), sizeof(long long) * kBatchLists * (ng + 1), cudaMemcpyHostToDevice,
+                      s) !=
           cudaSuccess) {
     S->err = "batch slot upload failed";
     return MRSPH_ERR_CUDA;
