@@ -4,7 +4,7 @@
 //
 //   mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N]
 //               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]
-//               [--lset-restart]
+//               [--lset-restart] [--cvp K] [--cvp-iter M]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
 // particle-steps/s, final time step).  --count-only prints the particle count
@@ -16,7 +16,10 @@
 // seeding; --lset-restart writes the level-set restart of the finest level
 // (rstfile/levelset.rst, Save_restart_file's level-set part) before seeding.
 // box_2d / box_3d are boxes whose corners (and, in 3D, edges) are the
-// geometry's singularity points and segments.  Exit status 2 on an engine
+// geometry's singularity points and segments.  --cvp K partitions the
+// relaxed particles into K cells (Voronoi::Partitioning, M iterations at
+// most, default 4000), the initial VPs at particles 0, n/K, 2n/K, ...; the
+// JSON line then carries the result and the final VPs.  Exit status 2 on an engine
 // error.
 #include <cstdio>
 #include <cstdlib>
@@ -29,7 +32,7 @@ using namespace mrsph_host;
 
 int main(int argc, char** argv) {
   std::string wl = "disc_hole_2d", out, prec;
-  int steps = -1, every = 0;
+  int steps = -1, every = 0, cvp_k = 0, cvp_iter = 4000;
   long long n = -1;
   bool count_only = false, cut_cell = false, vtu = false, lset = false, lset_rst = false;
   for (int a = 1; a < argc; a++) {
@@ -52,10 +55,12 @@ int main(int argc, char** argv) {
     else if (s == "--vtu") vtu = true;
     else if (s == "--lset") lset = true;
     else if (s == "--lset-restart") lset_rst = true;
+    else if (s == "--cvp") cvp_k = std::atoi(val().c_str());
+    else if (s == "--cvp-iter") cvp_iter = std::atoi(val().c_str());
     else if (s == "--help" || s == "-h") {
       std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
                   "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n"
-                  "                   [--lset-restart]\n");
+                  "                   [--lset-restart] [--cvp K] [--cvp-iter M]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
@@ -99,10 +104,35 @@ int main(int argc, char** argv) {
       ms = solver.SPH_Mesh_Generation_Solver(steps, every, out);
     }
     const mrsph_stats st = sim.Stats();
+    std::string cvp;
+    if (cvp_k > 0) {
+      const std::vector<double> x = sim.Positions();
+      const long long np = sim.num_particles();
+      std::vector<double> vp(3 * (size_t)cvp_k);
+      for (int k = 0; k < cvp_k; k++)
+        for (int q = 0; q < 3; q++) vp[3 * k + q] = x[3 * (size_t)((long long)k * np / cvp_k) + q];
+      mrsph_cvp_params p{};
+      p.num_vp = cvp_k;
+      p.max_iter = cvp_iter;
+      p.pressure_step = 1;
+      p.error_tolerance = 0.05;
+      p.relax_ratio = 0.8;
+      const mrsph_cvp_result r = sim.Partitioning(vp, p);
+      char buf[160];
+      std::snprintf(buf, sizeof(buf), ", \"cvp\": {\"iterations\": %d, \"converged\": %d, \"error_max\": %.17g, \"vp\": [",
+                    r.iterations, r.converged, r.error_max);
+      cvp = buf;
+      for (size_t q = 0; q < vp.size(); q++) {
+        std::snprintf(buf, sizeof(buf), "%s%.17g", q ? ", " : "", vp[q]);
+        cvp += buf;
+      }
+      cvp += "]}";
+    }
     std::printf("{\"workload\": \"%s\", \"n_particles\": %lld, \"steps\": %d, \"device_ms\": %.6f, "
-                "\"particle_steps_per_s\": %.6e, \"dt\": %.17g, \"step\": %lld, \"flags\": %d}\n",
+                "\"particle_steps_per_s\": %.6e, \"dt\": %.17g, \"step\": %lld, \"flags\": %d%s}\n",
                 c.name.c_str(), sim.num_particles(), steps, ms,
-                ms > 0 ? (double)sim.num_particles() * steps / (ms / 1000.0) : 0.0, st.dt, st.step, st.flags);
+                ms > 0 ? (double)sim.num_particles() * steps / (ms / 1000.0) : 0.0, st.dt, st.step, st.flags,
+                cvp.c_str());
   } catch (const Error& e) {
     std::fprintf(stderr, "mrsph_relax: %s (status %d)\n", e.what(), e.code);
     return 2;

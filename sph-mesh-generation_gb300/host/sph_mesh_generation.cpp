@@ -326,6 +326,37 @@ SPH_mesh_generation::SPH_mesh_generation(const Case& c, int device) : case_(c) {
   check(mrsph_set_levelset(h_, (int)lv.size(), lv.data()), "mrsph_set_levelset");
 }
 
+mrsph_cvp_result SPH_mesh_generation::Partitioning(std::vector<double>& vp, const mrsph_cvp_params& p,
+                                                   std::vector<int>* labels, std::vector<double>* vp_mass) {
+  if ((int)vp.size() != 3 * p.num_vp) throw Error(MRSPH_ERR_ARG, "Partitioning: vp must hold num_vp x 3 values");
+  if (labels) labels->assign(n_, 0);
+  if (vp_mass) vp_mass->assign(p.num_vp, 0.0);
+  mrsph_cvp_result r{};
+  check(mrsph_cvp(h_, &p, vp.data(), labels ? labels->data() : nullptr, vp_mass ? vp_mass->data() : nullptr, &r),
+        "mrsph_cvp");
+  return r;
+}
+
+mrsph_cvp_result SPH_mesh_generation::Partitioning_for_initial_VP_distribution(
+    const std::vector<double>& xyz, const std::vector<double>& mass, const std::vector<double>& mass_surface,
+    std::vector<double>& vp, const mrsph_cvp_params& p, std::vector<int>* labels, std::vector<double>* vp_mass,
+    std::vector<double>* ghosts) {
+  const long long n = (long long)mass.size();
+  if ((long long)xyz.size() != 3 * n || (long long)mass_surface.size() != n)
+    throw Error(MRSPH_ERR_ARG, "Partitioning_for_initial_VP_distribution: xyz, mass and mass_surface disagree");
+  if ((int)vp.size() != 3 * p.num_vp) throw Error(MRSPH_ERR_ARG, "vp must hold num_vp x 3 values");
+  if (labels) labels->assign(n, 0);
+  if (vp_mass) vp_mass->assign(p.num_vp, 0.0);
+  std::vector<double> g(3 * (size_t)p.num_vp, 0.0);
+  int ng = 0;
+  mrsph_cvp_result r{};
+  check(mrsph_cvp_lset(h_, n, xyz.data(), mass.data(), mass_surface.data(), &p, vp.data(),
+                       labels ? labels->data() : nullptr, vp_mass ? vp_mass->data() : nullptr, g.data(), &ng, &r),
+        "mrsph_cvp_lset");
+  if (ghosts) ghosts->assign(g.begin(), g.begin() + 3 * (size_t)ng);
+  return r;
+}
+
 SPH_mesh_generation::~SPH_mesh_generation() {
   if (h_) mrsph_destroy(h_);
 }

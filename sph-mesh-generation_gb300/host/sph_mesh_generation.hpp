@@ -127,6 +127,23 @@ class SPH_mesh_generation {
   // with Set_timestep and the half-step kicks (sph_mesh_generation.cpp:1371-1463).
   void Run_phase(int phase);
 
+  // Centroidal Voronoi partition of the particles (mass 1), Voronoi::
+  // Partitioning (CVP/voronoi.cpp:1376-1446): vp (K x 3) holds the initial
+  // VPs and receives the final ones; labels (n, id order) and vp_mass (K).
+  mrsph_cvp_result Partitioning(std::vector<double>& vp, const mrsph_cvp_params& p, std::vector<int>* labels = nullptr,
+                                std::vector<double>* vp_mass = nullptr);
+  // The level-set partition of weighted points with ghost VPs, Voronoi_lset::
+  // Partitioning_for_initial_VP_distribution (CVP/voronoi_lset.cpp:824-889);
+  // labels -1 for points nearest a ghost; ghosts receive the last
+  // iteration's ghost VPs (x, y, z each).
+  mrsph_cvp_result Partitioning_for_initial_VP_distribution(const std::vector<double>& xyz,
+                                                            const std::vector<double>& mass,
+                                                            const std::vector<double>& mass_surface,
+                                                            std::vector<double>& vp, const mrsph_cvp_params& p,
+                                                            std::vector<int>* labels = nullptr,
+                                                            std::vector<double>* vp_mass = nullptr,
+                                                            std::vector<double>* ghosts = nullptr);
+
   long long num_particles() const { return n_; }
   mrsph_handle* handle() { return h_; }
   const Case& Get_case() const { return case_; }
