@@ -138,3 +138,26 @@ def test_cpp_driver_box_characteristics(tmp_path, dim):
     assert d["step"] == 300 and d["flags"] & ~8 == 0
     assert np.max(np.abs(cpp - gp["xyz"])) < 1e-12
     assert (gp["type"] == 2).any()
+
+
+def test_cpp_driver_partitioning_matches_python():
+    """--cvp K: SPH_mesh_generation::Partitioning (Voronoi::Partitioning over
+    the C ABI) of the relaxed particles gives the VPs the Python API gives
+    for the same particles and initial VPs, bit for bit."""
+    binary = build.build_host()
+    K, iters = 8, 100
+    r = subprocess.run([binary, "--case", "disc_hole_2d", "--precision", "fp64", "--steps", "20", "--cvp", str(K),
+                        "--cvp-iter", str(iters)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    g = SPHMeshGeneration(case, precision="fp64")
+    g.Initialize_case()
+    g.SPH_run_mesh_generation(20)
+    x = g.particles(("xyz",))["xyz"]
+    n = len(x)
+    vp0 = np.array([x[k * n // K] for k in range(K)])
+    vp, labels, mass, res = g.Partitioning(vp0, max_iter=iters)
+    g.close()
+    assert d["cvp"]["iterations"] == res["iterations"]
+    assert np.array_equal(np.array(d["cvp"]["vp"]).reshape(K, 3), vp)
