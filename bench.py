@@ -352,10 +352,10 @@ def run_accuracy(args, dev):
     """FP32-split against the FP64 oracle (the CPU restatement of the
     reference) on a 37,658-particle torus (dx 0.02-0.08): the oracle relaxes
     accuracy_steps steps from its seed; the GPU's FP32 path relaxes the same
-    steps from the same seed state; and, from the oracle's state after 20
-    steps, the GPU makes one step whose binning, neighbour sets, kernel sums
-    and force stages are compared with the oracle's on the GPU's post-map
-    state."""
+    steps from the same seed state; and, from the oracle's state after those
+    steps (with SURFACE particles), the GPU makes one step whose binning,
+    neighbour sets, kernel sums (REAL and SURFACE) and force stages are
+    compared with the oracle's on the GPU's post-map state."""
     import numpy as np
     import oracle
     from mrsph import SPHMeshGeneration, cases
@@ -373,13 +373,12 @@ def run_accuracy(args, dev):
                 "level": st["level"], "nu": st["nu"], "dt": st["dt"], "step": st["step"]}
 
     t0 = time.perf_counter()
-    orc.steps(20)
-    st20 = orc.get_state()
-    orc.steps(args.accuracy_steps - 20)
+    orc.steps(args.accuracy_steps)
+    st_acc = orc.get_state()
     oracle_s = time.perf_counter() - t0
-    # one step from the oracle's state after 20 steps
+    # one step from the oracle's state after accuracy_steps steps
     g = SPHMeshGeneration(case, precision="fp32", device=dev, neighbor_cap=1024)
-    g.set_state(to_gpu(st20))
+    g.set_state(to_gpu(st_acc))
     g.run_phase(5)
     gp = g.particles()
     lc, _ = g.cells()
@@ -390,7 +389,7 @@ def run_accuracy(args, dev):
     o2.set_state({"x": gp["xyz"][:, 0], "y": gp["xyz"][:, 1], "z": gp["xyz"][:, 2], "type": gp["type"],
                   "h": gp["h"], "level": gp["level"], "phi": gp["phi"], "curv": gp["curv"],
                   "nx": gp["norm"][:, 0], "ny": gp["norm"][:, 1], "nz": gp["norm"][:, 2], "rho": gp["rho"],
-                  "nu": st20["nu"], "id": np.arange(n, dtype=np.int32), "step": st20["step"] + 1,
+                  "nu": st_acc["nu"], "id": np.arange(n, dtype=np.int32), "step": st_acc["step"] + 1,
                   "vol": 1.0 / gp["rho"],
                   "scale": o2.ctx.max_scale * np.ldexp(1.0, -np.asarray(gp["level"], dtype=np.int64))})
     ooff, onb = o2.neighbors()
@@ -427,7 +426,7 @@ def run_accuracy(args, dev):
     dif["hist_l1_over_n"] = float(np.abs(np.array(stats["fp32"]["hist"]) -
                                          np.array(stats["oracle"]["hist"])).sum() / n)
     return {"workload": f"torus_3d dx 0.02-0.08 (N={case.n_particles})", "reference": "FP64 oracle",
-            "single_step": force, "single_step_state": "the oracle's state after 20 steps",
+            "single_step": force, "single_step_state": f"the oracle's state after {args.accuracy_steps} steps",
             "steps": args.accuracy_steps, "oracle_seconds": oracle_s,
             "spacing_ratio": {"fp32": {k: v for k, v in stats["fp32"].items() if k != "hist"},
                               "oracle": {k: v for k, v in stats["oracle"].items() if k != "hist"},
