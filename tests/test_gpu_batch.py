@@ -118,3 +118,38 @@ def test_persistent_barrier_wait_is_bounded():
     b.close()
     for g in hs:
         g.close()
+
+
+@pytest.mark.parametrize("prec,mode", [("fp32", "persistent"), ("fp32", "phases"), ("fp64", "streams")])
+def test_batch_with_characteristic_particles(prec, mode):
+    """Geometries with corners and edges (SINGULARITY and SEGMENT particles,
+    the hyperbolic kernel) batched with a star: every handle ends where
+    stepping it alone ends, bit for bit."""
+    geoms = [cases.box_with_corners(dim=3, spacing=0.04, grid=32, kernel="hyperbolic", h_over_dx=1.0),
+             cases.box_with_corners(dim=2, spacing=0.02, grid=64, kernel="hyperbolic", h_over_dx=1.0),
+             cases.star_shape(3, 8, 2500)]
+    steps = 160
+    solo = []
+    for c in geoms:
+        g = SPHMeshGeneration(c, precision=prec)
+        g.Initialize_case()
+        g.SPH_run_mesh_generation(steps)
+        solo.append(g.particles(("xyz", "type", "h")))
+        g.close()
+    hs = []
+    for c in geoms:
+        g = SPHMeshGeneration(c, precision=prec)
+        g.Initialize_case()
+        hs.append(g)
+    b = BatchRelaxation(hs, mode=mode)
+    b.SPH_run_mesh_generation(steps)
+    for g, ref in zip(hs, solo):
+        got = g.particles(("xyz", "type", "h"))
+        assert np.array_equal(got["xyz"], ref["xyz"])
+        assert np.array_equal(got["type"], ref["type"])
+        assert np.array_equal(got["h"], ref["h"])
+    t = solo[0]["type"]
+    assert (t == 2).any() and (t == 3).any()
+    b.close()
+    for g in hs:
+        g.close()
