@@ -370,7 +370,12 @@ int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri
  *     the handle's own stream.
  * Work queued on a handle before mrsph_batch_step runs first; work queued on
  * it afterwards runs after the batch's steps.  A handle may be stepped alone
- * between batch calls; it must not be destroyed while in a batch. */
+ * between batch calls.  Handles and batches may be destroyed in any order:
+ * destroying a handle that a batch holds waits for the batch's queued work
+ * and takes the handle out of it, after which the batch's step and sync
+ * calls return MRSPH_ERR_STATE (only mrsph_batch_destroy remains).
+ * FP32-split results of a batch whose geometries use different smoothing
+ * kernels equal those of stepping each alone as well. */
 typedef struct mrsph_batch mrsph_batch;
 #define MRSPH_BATCH_STREAMS 0
 #define MRSPH_BATCH_PERSISTENT 1

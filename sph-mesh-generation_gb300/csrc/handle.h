@@ -5,6 +5,8 @@
 
 #include "engine_iface.h"
 
+struct mrsph_batch;
+
 struct mrsph_handle {
   mrsph_params prm{};
   std::string err;
@@ -17,4 +19,11 @@ struct mrsph_handle {
   mrsph::EngineBase* eng = nullptr;
   // the geometry's singularity points and segments (mrsph_set_characteristics)
   std::vector<double> sing, seg;
+  // the batches that hold this handle (mrsph_batch_create); mrsph_destroy
+  // detaches the handle from them first
+  std::vector<mrsph_batch*> batches;
 };
+
+// Waits for the batch's queued work and takes handle h out of it; the batch
+// then refuses to step (mrsph_batch.cu).
+void mrsph_batch_detach(mrsph_batch* b, mrsph_handle* h);

@@ -158,6 +158,10 @@ int mrsph_create(const mrsph_params* p, mrsph_handle** out) {
 int mrsph_destroy(mrsph_handle* h) {
   if (!h) return 0;
   cudaSetDevice(h->prm.device);
+  // a batch still holding the handle: its queued work finishes first and it
+  // forgets the handle (whichever of the two is destroyed first)
+  const std::vector<mrsph_batch*> bs = h->batches;
+  for (mrsph_batch* b : bs) mrsph_batch_detach(b, h);
   delete h->eng;
   for (void* p : h->ls_allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);

@@ -22,6 +22,7 @@
 // MRSPH_ERR_DEVICE and makes each handle's neighbour-list capacity check.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -53,7 +54,21 @@ struct mrsph_batch {
   bool fp32 = true;
   mrsph::Persist* P = nullptr;
   std::string err;
+  bool detached = false;  // a handle was destroyed while the batch held it
 };
+
+void mrsph_batch_detach(mrsph_batch* b, mrsph_handle* h) {
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  for (size_t k = 0; k < b->hs.size(); k++)
+    if (b->hs[k] == h) {
+      b->hs[k] = nullptr;
+      b->engines[k] = nullptr;
+      b->detached = true;
+    }
+  auto& v = h->batches;
+  v.erase(std::remove(v.begin(), v.end(), b), v.end());
+}
 
 namespace {
 
@@ -189,6 +204,7 @@ extern "C" int mrsph_batch_create(mrsph_handle* const* handles, int count, mrsph
     b->P = mrsph::persist_create(b->device, wen ? mrsph::K_WEN : -1, count);
     if (b->P) b->mode = mrsph::persist_resident(b->P) ? MRSPH_BATCH_PERSISTENT : MRSPH_BATCH_PHASES;
   }
+  for (auto* h : b->hs) h->batches.push_back(b);
   *out = b;
   return 0;
 }
@@ -197,7 +213,12 @@ extern "C" int mrsph_batch_destroy(mrsph_batch* b) {
   if (!b) return 0;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
-  for (auto* h : b->hs) cudaStreamSynchronize(h->stream);
+  for (auto* h : b->hs) {
+    if (!h) continue;  // destroyed before the batch
+    cudaStreamSynchronize(h->stream);
+    auto& v = h->batches;
+    v.erase(std::remove(v.begin(), v.end(), b), v.end());
+  }
   mrsph::persist_destroy(b->P);
   for (auto e : b->ev) cudaEventDestroy(e);
   if (b->done) cudaEventDestroy(b->done);
@@ -234,8 +255,14 @@ extern "C" int mrsph_batch_get_mode(mrsph_batch* b, int* mode, int* graph_captur
   return 0;
 }
 
+// a batch whose handle was destroyed steps no more
+static int batch_usable(mrsph_batch* b) {
+  return b->detached ? bfail(b, MRSPH_ERR_STATE, "a handle of the batch was destroyed") : 0;
+}
+
 extern "C" int mrsph_batch_step(mrsph_batch* b, int nsteps) {
   if (!b) return MRSPH_ERR_ARG;
+  if (int rc = batch_usable(b)) return rc;
   if (nsteps <= 0) return 0;
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, MRSPH_ERR_CUDA, "cudaSetDevice failed");
   return run_steps(b, nsteps, true);
@@ -243,6 +270,7 @@ extern "C" int mrsph_batch_step(mrsph_batch* b, int nsteps) {
 
 extern "C" int mrsph_batch_step_timed(mrsph_batch* b, int nsteps, double* ms) {
   if (!b || !ms) return MRSPH_ERR_ARG;
+  if (int rc = batch_usable(b)) return rc;
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, MRSPH_ERR_CUDA, "cudaSetDevice failed");
   // settle capacities and build every graph outside the timed region
   int rc = check_caps(b);
@@ -294,6 +322,7 @@ extern "C" int mrsph_batch_step_timed(mrsph_batch* b, int nsteps, double* ms) {
 
 extern "C" int mrsph_batch_sync(mrsph_batch* b) {
   if (!b) return MRSPH_ERR_ARG;
+  if (int rc = batch_usable(b)) return rc;
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, MRSPH_ERR_CUDA, "cudaSetDevice failed");
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, MRSPH_ERR_CUDA, "batch stream failed");
   for (auto* h : b->hs)

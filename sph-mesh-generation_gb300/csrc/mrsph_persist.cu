@@ -197,8 +197,17 @@ __device__ inline void run_item(const BatchPlan& P, int ph, long long it, int st
   const long long blk = it - off[g];
   const long long nblk = off[g + 1] - off[g];
   const int cur = (s_slot.cur + step) & 1;
-  if (s_slot.dim == 2) run_item_d<2, KK, LD>(s_slot, ph, blk, nblk, cur);
-  else run_item_d<3, KK, LD>(s_slot, ph, blk, nblk, cur);
+  // in a batch of mixed smoothing kernels (KK = -1) a Wendland geometry takes
+  // the Wendland-specialised block functions, as its own handle's kernels do,
+  // so its results stay those of stepping it alone
+  const bool wen = KK < 0 && s_slot.c.prm.kernel == K_WEN;
+  if (s_slot.dim == 2) {
+    if (wen) run_item_d<2, K_WEN, LD>(s_slot, ph, blk, nblk, cur);
+    else run_item_d<2, KK, LD>(s_slot, ph, blk, nblk, cur);
+  } else {
+    if (wen) run_item_d<3, K_WEN, LD>(s_slot, ph, blk, nblk, cur);
+    else run_item_d<3, KK, LD>(s_slot, ph, blk, nblk, cur);
+  }
 }
 
 template <int KK>

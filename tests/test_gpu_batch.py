@@ -153,3 +153,26 @@ def test_batch_with_characteristic_particles(prec, mode):
     b.close()
     for g in hs:
         g.close()
+
+
+def test_destroy_handle_before_batch():
+    """A handle destroyed while a batch holds it leaves the batch (after its
+    queued work): the batch then refuses to step, and both destructions in
+    either order are safe."""
+    from mrsph import _lib as L
+    geoms = _geoms()[:2]
+    hs = []
+    for c in geoms:
+        g = SPHMeshGeneration(c, precision="fp32")
+        g.Initialize_case()
+        hs.append(g)
+    b = BatchRelaxation(hs)
+    b.SPH_run_mesh_generation(2)
+    hs[0].close()
+    with pytest.raises(L.MrsphError):
+        b.SPH_run_mesh_generation(1)
+    b.close()
+    hs[1].SPH_run_mesh_generation(1)
+    hs[1].sync()
+    assert hs[1].stats()["step"] == 3
+    hs[1].close()
