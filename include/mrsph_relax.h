@@ -198,8 +198,12 @@ int mrsph_get_levelset(mrsph_handle* h, int level, double* nx, double* ny, doubl
  * (level_set.cpp:930-972) over Levelset_package::Calculate_volume_mass
  * (lset_package.cpp:1283-1397) and GeometryCalculator
  * (geometry_calculator.cpp:12-570), then
- * SPH_mesh_generation::Get_num_particles (sph_mesh_generation.cpp:900-940)
- * without segments or singularities.  A cell counts when phi > 0 or
+ * SPH_mesh_generation::Get_num_particles (sph_mesh_generation.cpp:900-940),
+ * with the segment and singularity terms of a geometry given by
+ * mrsph_set_characteristics: in 3D a SEGMENT cell adds the length of its
+ * segment inside the cell box (GeometryCalculator::Get_segment_length,
+ * geometry_calculator.cpp:571-589, over AABB_calculator.cpp:6-55) over its
+ * scale to total_mass_segment.  A cell counts when phi > 0 or
  * |phi| < dl (the level's smallest cell size); CUT cells take their volume
  * fraction from adaptive bisection and their area from marching cubes.
  * cell_vol / cell_area (may be NULL) receive per-cell values sized like phi
@@ -212,8 +216,12 @@ typedef struct {
   long long num_interface_cell;   /* CUT cells (glbl_num_interface_cell) */
   long long num_particle_mesh;    /* max(int(total_mass - total_mass_surface / 2), 0) */
   long long num_particle_surface; /* min(int(total_mass_surface), num_interface_cell) */
-  long long num_particle;         /* mesh + surface (glbl_total_num_particle) */
+  long long num_particle;         /* mesh + surface + segment + singularity (glbl_total_num_particle) */
   double device_ms;           /* device time of the pass */
+  double total_mass_segment;  /* 3D: sum over SEGMENT cells of length / scale (Levelset::total_mass_segment) */
+  double total_length;        /* 3D: sum of those lengths (Levelset::total_length) */
+  long long num_particle_segment;     /* max(int(total_mass_segment - 0.5 x singularity points), 0) */
+  long long num_particle_singularity; /* the geometry's singularity points */
 } mrsph_volume_mass_stats;
 int mrsph_volume_mass(mrsph_handle* h, int level, mrsph_volume_mass_stats* out, double* cell_vol,
                       double* cell_area);

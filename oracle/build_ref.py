@@ -1,10 +1,13 @@
 """Compile parts of the reference's own code into oracle/_ref/ (checker only).
 
-TEST INFRASTRUCTURE ONLY.  Two pieces of the reference's relaxation path are
+TEST INFRASTRUCTURE ONLY.  Three pieces of the reference's relaxation path are
 compiled from its sources, where they lie, with C-ABI shims of this project:
 
 * geometry_tools/polygonise.cpp (+ polygonise.h): needs nothing but the C++
   standard library; pins the oracle's marching-cubes surface area.
+* geometry_tools/AABB_calculator.cpp (+ its header): needs nothing but the
+  C++ standard library; pins the oracle's segment-in-cell length (the
+  SEGMENT cells' term of the cut-cell pass).
 * base_cls_particle/particle.cpp: the smoothing kernels and their gradients
   (Kernel_function*, Derivative_kernel_function*) and Set_particle_scale.  Its
   global headers include TBB, Boost (MPI, serialization, graph) and the
@@ -28,6 +31,8 @@ OUT_DIR = os.path.join(HERE, "_ref")
 OUT = os.path.join(OUT_DIR, "libref_polygonise.so")
 SHIM = os.path.join(HERE, "ref_polygonise_shim.cpp")
 KSHIM = os.path.join(HERE, "ref_kernels_shim.cpp")
+ASHIM = os.path.join(HERE, "ref_aabb_shim.cpp")
+AABB_OUT = os.path.join(OUT_DIR, "libref_aabb.so")
 STUBS = os.path.join(HERE, "ref_stubs")
 # kernel ids of the C ABI (hyperbolic, cubic, Wendland, Gaussian, quintic) ->
 # the reference's compile-time kernel macros (Makefile.in:36-40)
@@ -38,6 +43,21 @@ KERNEL_NAMES = {0: "hyperbolic", 1: "cubic", 2: "wendland", 3: "gaussian", 4: "q
 
 def available() -> bool:
     return os.path.exists(os.path.join(REF_SRC, "geometry_tools", "polygonise.cpp"))
+
+
+def aabb_available() -> bool:
+    return os.path.exists(os.path.join(REF_SRC, "geometry_tools", "AABB_calculator.cpp"))
+
+
+def build_aabb(force: bool = False):
+    srcs = [ASHIM, os.path.join(REF_SRC, "geometry_tools", "AABB_calculator.cpp")]
+    if not force and _fresh(AABB_OUT, srcs):
+        return AABB_OUT
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+           os.path.join(REF_SRC, "geometry_tools")] + srcs + ["-o", AABB_OUT + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(AABB_OUT + ".tmp", AABB_OUT)
+    return AABB_OUT
 
 
 def kernels_available() -> bool:
@@ -95,6 +115,8 @@ def build(force: bool = False):
         return OUT if os.path.exists(OUT) else None
     os.makedirs(OUT_DIR, exist_ok=True)
     build_polygonise(force)
+    if aabb_available():
+        build_aabb(force)
     if kernels_available():
         build_kernels(force)
     return OUT

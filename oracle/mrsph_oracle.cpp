@@ -2410,12 +2410,37 @@ void orc_cut_cell(int D, const double* p27, double dx, double dy, double dz, dou
   gc_cut_cell(D, c, dx, dy, dz, vol, area);
 }
 
+// Length of segment v0-v1 inside the box [mn, mx]: Segment_AABB_Intersection
+// (AABB_calculator.cpp:6-55) clips the segment's parameter range [0, 1] by
+// the three slabs in turn (IEEE infinities and NaNs for a segment parallel to
+// a slab, which the comparisons then pass or reject) and
+// GeometryCalculator::Get_segment_length (geometry_calculator.cpp:571-589)
+// returns the clipped piece's length, 0 when it is empty.
+double orc_segment_length(const double* mn, const double* mx, const double* v0, const double* v1) {
+  double f0 = 0., f1 = 1.;
+  for (int d = 0; d < 3; d++) {
+    double a = (mn[d] - v0[d]) / (v1[d] - v0[d]);
+    double b = (mx[d] - v0[d]) / (v1[d] - v0[d]);
+    if (b < a) std::swap(a, b);
+    if (b < f0 || a > f1) return 0.;
+    f0 = a >= f0 ? a : f0;
+    f1 = b <= f1 ? b : f1;
+    if (f0 > f1) return 0.;
+  }
+  double pp[3];
+  for (int d = 0; d < 3; d++) pp[d] = ((v1[d] - v0[d]) * f1 + v0[d]) - ((v1[d] - v0[d]) * f0 + v0[d]);
+  return std::sqrt(pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]);
+}
+
 // Calculate_volume_mass over the interior cells of level `level` (after
 // orc_ls_build of that level) and Get_num_particles.  cell_vol / cell_area
 // (may be NULL) receive per-cell values over the full grid incl. margins
 // (zero outside the counted cells).  totals = {total_mass,
-// total_mass_surface, total_volume, total_area}; counts = {interface cells,
-// mesh particles, surface particles, particles}.
+// total_mass_surface, total_volume, total_area, total_mass_segment,
+// total_length}; counts = {interface cells, mesh particles, surface
+// particles, particles, segment particles, singularity particles}.  In 3D a
+// SEGMENT cell adds its segment's length inside the cell over its scale
+// (lset_package.cpp:1371-1383).
 void orc_volume_mass(const orc_ctx* c, int level, double* cell_vol, double* cell_area, double* totals,
                      long long* counts) {
   const int D = c->dim;
@@ -2460,7 +2485,7 @@ void orc_volume_mass(const orc_ctx* c, int level, double* cell_vol, double* cell
         cell_area[a] = area;
       }
   // the sums in cell order
-  double M = 0., Ms = 0., V = 0., A = 0.;
+  double M = 0., Ms = 0., V = 0., A = 0., Mg = 0., Lg = 0.;
   long long ncut = 0;
   for (int gk = 0; gk < n2; gk++)
     for (int gj = 0; gj < n1; gj++)
@@ -2474,6 +2499,19 @@ void orc_volume_mass(const orc_ctx* c, int level, double* cell_vol, double* cell
           A += cell_area[a];
           Ms += cell_area[a] / powern(scale, D - 1);
         }
+        if (D == 3 && L.chr && L.chr[a] == CHAR_SEGMENT) {
+          const int g[3] = {gi, gj, gk};
+          double mn[3], mx[3];
+          for (int d = 0; d < 3; d++) {
+            const int pk = g[d] / 4, ce = g[d] % 4;
+            mn[d] = (pk * L.dpkg[d] + ce * ls_dcell(L, d)) + L.box_l[d];
+            mx[d] = mn[d] + ls_dcell(L, d);
+          }
+          const double* sg = c->seg + 6 * L.chr_idx[a];
+          const double len = orc_segment_length(mn, mx, sg, sg + 3);
+          Lg += len;
+          Mg += len / scale;
+        }
         M += cell_vol[a] / powern(scale, D);
         V += cell_vol[a];
       }
@@ -2481,16 +2519,20 @@ void orc_volume_mass(const orc_ctx* c, int level, double* cell_vol, double* cell
   totals[1] = Ms;
   totals[2] = V;
   totals[3] = A;
-  // Get_num_particles, sph_mesh_generation.cpp:909-923 (no segments or singularities)
-  long long n_surface = (long long)(Ms - 0.5 * 0.0);
-  if (n_surface < 0) n_surface = 0;
-  long long n_mesh = (long long)(M - 0.5 * Ms);
-  if (n_mesh < 0) n_mesh = 0;
+  totals[4] = Mg;
+  totals[5] = Lg;
+  // Get_num_particles, sph_mesh_generation.cpp:909-923
+  const int nsing = c->nsing;
+  const long long n_segment = AMAX1(int(Mg * 1. - 0.5 * nsing), 0);
+  long long n_surface = AMAX1(int(Ms * 1. - 0.5 * Mg * 1.), 0);
+  const long long n_mesh = AMAX1(int(M * 1. - 0.5 * Ms * 1.), 0);
   if (ncut < n_surface) n_surface = ncut;
   counts[0] = ncut;
   counts[1] = n_mesh;
   counts[2] = n_surface;
-  counts[3] = n_mesh + n_surface;
+  counts[3] = n_mesh + n_surface + nsing + n_segment;
+  counts[4] = n_segment;
+  counts[5] = nsing;
 }
 
 }  // extern "C"

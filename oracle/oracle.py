@@ -150,6 +150,8 @@ def lib():
         L.orc_cvp_lset.argtypes = [C.POINTER(OrcCtx), C.POINTER(OrcCvpParams), C.c_longlong, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.POINTER(C.c_int), C.POINTER(OrcCvpResult)]
+        L.orc_segment_length.argtypes = [C.c_void_p] * 4
+        L.orc_segment_length.restype = C.c_double
         L.orc_mc_table.argtypes = [C.c_void_p]
         L.orc_mc_area.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
         L.orc_mc_area.restype = C.c_double
@@ -291,12 +293,22 @@ class Oracle:
         ntot = self.fields[level]["phi"].size
         vol = np.zeros(ntot)
         area = np.zeros(ntot)
-        tot = np.zeros(4)
-        cnt = np.zeros(4, dtype=np.int64)
+        tot = np.zeros(6)
+        cnt = np.zeros(6, dtype=np.int64)
         lib().orc_volume_mass(C.byref(self.ctx), level, _p(vol), _p(area), _p(tot), _p(cnt))
         return {"total_mass": tot[0], "total_mass_surface": tot[1], "total_volume": tot[2],
-                "total_area": tot[3], "num_interface_cell": int(cnt[0]), "num_particle_mesh": int(cnt[1]),
-                "num_particle_surface": int(cnt[2]), "num_particle": int(cnt[3]), "vol": vol, "area": area}
+                "total_area": tot[3], "total_mass_segment": tot[4], "total_length": tot[5],
+                "num_interface_cell": int(cnt[0]), "num_particle_mesh": int(cnt[1]),
+                "num_particle_surface": int(cnt[2]), "num_particle": int(cnt[3]),
+                "num_particle_segment": int(cnt[4]), "num_particle_singularity": int(cnt[5]),
+                "vol": vol, "area": area}
+
+    @staticmethod
+    def segment_length(mn, mx, v0, v1) -> float:
+        """GeometryCalculator::Get_segment_length restated: the length of
+        segment v0-v1 inside the box [mn, mx]."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (mn, mx, v0, v1)]
+        return lib().orc_segment_length(*[_p(x) for x in a])
 
     # ----------------------------------------------------------------- state
     def alloc(self, n: int):

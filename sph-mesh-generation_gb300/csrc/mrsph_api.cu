@@ -2,6 +2,7 @@
 // cell-list level plan, level-set upload/build and the engine dispatch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -392,7 +393,7 @@ int mrsph_volume_mass(mrsph_handle* h, int level, mrsph_volume_mass_stats* out, 
     return o;
   };
   const size_t o_vol = take(sizeof(double) * ntot), o_area = take(sizeof(double) * ntot);
-  const size_t o_part = take(sizeof(double) * 4 * nb), o_tot = take(sizeof(double) * 4);
+  const size_t o_part = take(sizeof(double) * 6 * nb), o_tot = take(sizeof(double) * 6);
   const size_t o_list = take(sizeof(int) * nin), o_cnt = take(3 * sizeof(unsigned long long));
   const size_t o_tab = take(256 * 16);
   char* buf = nullptr;
@@ -420,7 +421,7 @@ int mrsph_volume_mass(mrsph_handle* h, int level, mrsph_volume_mass_stats* out, 
                            reinterpret_cast<unsigned long long*>(buf + o_cnt),
                            reinterpret_cast<double*>(buf + o_tot), ncut, h->stream));
   API_CK(h, cudaEventRecord(e1, h->stream));
-  double tot[4];
+  double tot[6];
   API_CK(h, cudaMemcpyAsync(tot, buf + o_tot, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
   if (cell_vol) API_CK(h, cudaMemcpyAsync(cell_vol, cvol, sizeof(double) * ntot, cudaMemcpyDeviceToHost, h->stream));
   if (cell_area)
@@ -433,15 +434,19 @@ int mrsph_volume_mass(mrsph_handle* h, int level, mrsph_volume_mass_stats* out, 
   out->total_volume = tot[2];
   out->total_area = tot[3];
   out->num_interface_cell = ncut[0];
-  // Get_num_particles, sph_mesh_generation.cpp:909-923 (no segments or singularities)
-  long long n_surface = (long long)(tot[1] - 0.5 * 0.0);
-  if (n_surface < 0) n_surface = 0;
-  long long n_mesh = (long long)(tot[0] - 0.5 * tot[1]);
-  if (n_mesh < 0) n_mesh = 0;
+  out->total_mass_segment = tot[4];
+  out->total_length = tot[5];
+  // Get_num_particles, sph_mesh_generation.cpp:909-923
+  const int nsing = (int)(h->sing.size() / 3);
+  const long long n_segment = std::max((long long)(int)(tot[4] * 1. - 0.5 * nsing), 0LL);
+  long long n_surface = std::max((long long)(int)(tot[1] * 1. - 0.5 * tot[4] * 1.), 0LL);
+  const long long n_mesh = std::max((long long)(int)(tot[0] * 1. - 0.5 * tot[1] * 1.), 0LL);
   if (ncut[0] < n_surface) n_surface = ncut[0];
   out->num_particle_mesh = n_mesh;
   out->num_particle_surface = n_surface;
-  out->num_particle = n_mesh + n_surface;
+  out->num_particle_segment = n_segment;
+  out->num_particle_singularity = nsing;
+  out->num_particle = n_mesh + n_surface + nsing + n_segment;
   out->device_ms = ms;
   return 0;
 }

@@ -794,16 +794,46 @@ __global__ void k_vm_finish(const int* __restrict__ list, long long nlist, const
   cvol[list[w]] = H * dv;
 }
 
+// Length of segment v0-v1 inside the box [mn, mx]: the segment is clipped
+// to the parameter range [0, 1] by the box's three slabs in turn, each slab
+// giving the parameters where the segment crosses its two planes (IEEE
+// infinities and NaNs for a segment parallel to it, which the comparisons
+// then pass or reject), and the clipped piece's length is returned (0 when
+// it is empty).  Segment_AABB_Intersection (AABB_calculator.cpp:6-55) and
+// GeometryCalculator::Get_segment_length (geometry_calculator.cpp:571-589),
+// in their operation order (this file is compiled with -fmad=false).
+__device__ inline double seg_box_length(const double* mn, const double* mx, const double* v0, const double* v1) {
+  double f0 = 0., f1 = 1.;
+  for (int d = 0; d < 3; d++) {
+    double a = (mn[d] - v0[d]) / (v1[d] - v0[d]);
+    double b = (mx[d] - v0[d]) / (v1[d] - v0[d]);
+    if (b < a) {
+      const double t = a;
+      a = b;
+      b = t;
+    }
+    if (b < f0 || a > f1) return 0.;
+    f0 = a >= f0 ? a : f0;
+    f1 = b <= f1 ? b : f1;
+    if (f0 > f1) return 0.;
+  }
+  double pp[3];
+  for (int d = 0; d < 3; d++) pp[d] = ((v1[d] - v0[d]) * f1 + v0[d]) - ((v1[d] - v0[d]) * f0 + v0[d]);
+  return sqrt(pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]);
+}
+
 // Pass 3, one thread per interior cell: the mass sums of
 // Calculate_volume_mass (lset_package.cpp:1340-1395) with
-// scale = Get_scale(curv, phi), into per-block partials (fixed order).
+// scale = Get_scale(curv, phi), into per-block partials (fixed order): mass,
+// surface mass, volume, area, and in 3D the segment mass and length of the
+// SEGMENT cells (:1371-1383).
 template <int D>
 __global__ void __launch_bounds__(256) k_vm_reduce(LsSet ls, int level, long long nin, double dl,
                                                    double* __restrict__ cvol, double* __restrict__ carea,
                                                    double* __restrict__ part) {
   const LsLevel& L = ls.lv[level];
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double m = 0., ms = 0., v = 0., ar = 0.;
+  double m = 0., ms = 0., v = 0., ar = 0., mg = 0., lg = 0.;
   if (q < nin) {
     int g[3];
     vm_cell_of(L, D, q, g);
@@ -823,49 +853,62 @@ __global__ void __launch_bounds__(256) k_vm_reduce(LsSet ls, int level, long lon
         vol = (L.dcell[0] * L.dcell[1]) * (D == 3 ? L.dcell[2] : 1.0);
         cvol[a] = vol;
       }
+      if (D == 3 && L.chr && L.chr[a] > 0) {  // a SEGMENT cell of segment chr - 1
+        double mn[3], mx[3];
+        for (int d = 0; d < 3; d++) {
+          const int pk = g[d] >> 2, ce = g[d] & 3;
+          mn[d] = (pk * L.dpkg[d] + ce * L.dcell[d]) + L.box_l[d];
+          mx[d] = mn[d] + L.dcell[d];
+        }
+        const double* sg = ls.seg + 6 * (L.chr[a] - 1);
+        lg = seg_box_length(mn, mx, sg, sg + 3);
+        mg = lg / scale;
+      }
       double sp = 1.0;
       for (int d = 0; d < D; d++) sp *= scale;
       m = vol / sp;
       v = vol;
     }
   }
-  __shared__ double sm[4][256];
+  __shared__ double sm[6][256];
   sm[0][threadIdx.x] = m;
   sm[1][threadIdx.x] = ms;
   sm[2][threadIdx.x] = v;
   sm[3][threadIdx.x] = ar;
+  sm[4][threadIdx.x] = mg;
+  sm[5][threadIdx.x] = lg;
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
     if (threadIdx.x < st)
-      for (int u = 0; u < 4; u++) sm[u][threadIdx.x] += sm[u][threadIdx.x + st];
+      for (int u = 0; u < 6; u++) sm[u][threadIdx.x] += sm[u][threadIdx.x + st];
     __syncthreads();
   }
-  if (threadIdx.x < 4) part[(long long)blockIdx.x * 4 + threadIdx.x] = sm[threadIdx.x][0];
+  if (threadIdx.x < 6) part[(long long)blockIdx.x * 6 + threadIdx.x] = sm[threadIdx.x][0];
 }
 
 // Pass 4, one block: the partials summed in a fixed order.
 __global__ void __launch_bounds__(256) k_vm_final(const double* __restrict__ part, long long nb,
                                                   double* __restrict__ tot) {
-  __shared__ double sm[4][256];
-  double acc[4] = {0., 0., 0., 0.};
+  __shared__ double sm[6][256];
+  double acc[6] = {0., 0., 0., 0., 0., 0.};
   for (long long b = threadIdx.x; b < nb; b += blockDim.x)
-    for (int u = 0; u < 4; u++) acc[u] += part[b * 4 + u];
-  for (int u = 0; u < 4; u++) sm[u][threadIdx.x] = acc[u];
+    for (int u = 0; u < 6; u++) acc[u] += part[b * 6 + u];
+  for (int u = 0; u < 6; u++) sm[u][threadIdx.x] = acc[u];
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
     if (threadIdx.x < st)
-      for (int u = 0; u < 4; u++) sm[u][threadIdx.x] += sm[u][threadIdx.x + st];
+      for (int u = 0; u < 6; u++) sm[u][threadIdx.x] += sm[u][threadIdx.x + st];
     __syncthreads();
   }
-  if (threadIdx.x < 4) tot[threadIdx.x] = sm[threadIdx.x][0];
+  if (threadIdx.x < 6) tot[threadIdx.x] = sm[threadIdx.x][0];
 }
 
 }  // namespace
 
 // Cut-cell volume / area / mass pass of one level (see above).  Device
 // buffers: cvol, carea (full grid incl. margins, zeroed here), list (one int
-// per interior cell), part (4 doubles per 256 interior cells), tab (4 KB),
-// cnt (3 counters), tot (4 doubles); the work items of the cut sub-cubes
+// per interior cell), part (6 doubles per 256 interior cells), tab (4 KB),
+// cnt (3 counters), tot (6 doubles); the work items of the cut sub-cubes
 // are allocated here once their number is known.  Enqueued on s, which is
 // synchronised twice.
 cudaError_t ls_volume_mass(const LsSet& ls, int level, int D, double* cvol, double* carea, int* list,

@@ -637,8 +637,9 @@ std::string lset_restart_bytes(const LsetRestart& r) {
   for (double v : r.sing) D(v);
   I((int)(r.seg.size() / 6));
   for (double v : r.seg) D(v);
-  for (double v : {r.fac_max, r.fac_mid, r.fac_min, r.curv_artificial, r.total_mass, r.total_mass_surface, 0.0,
-                   r.total_volume, r.total_area, 0.0, r.max_phi, 0.0, r.max_dl, r.mid_dl, r.min_dl, r.max_curv,
+  for (double v : {r.fac_max, r.fac_mid, r.fac_min, r.curv_artificial, r.total_mass, r.total_mass_surface,
+                   r.total_mass_segment, r.total_volume, r.total_area, r.total_length, r.max_phi, 0.0, r.max_dl,
+                   r.mid_dl, r.min_dl, r.max_curv,
                    r.min_curv})
     D(v);
   I(r.num_interface_cell);
@@ -742,6 +743,8 @@ std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path,
   r.total_mass_surface = vm.total_mass_surface;
   r.total_volume = vm.total_volume;
   r.total_area = vm.total_area;
+  r.total_mass_segment = vm.total_mass_segment;
+  r.total_length = vm.total_length;
   r.max_phi = max_phi;
   r.max_dl = p.max_dl;
   r.mid_dl = mid;
@@ -1169,7 +1172,8 @@ extern "C" long long mrsph_host_pvtu(int mesh, const char* piece, char* buf, lon
 // (header values in the order of LsetRestart: box_l[3], box_r[3], dpkg[3],
 // dcell[3], fac_max, fac_mid, fac_min, curv_artificial, total_mass,
 // total_mass_surface, total_volume, total_area, max_phi, max_dl, mid_dl,
-// min_dl, max_curv, min_curv; ints: dim, num_pkg[3], margin[3],
+// min_dl, max_curv, min_curv, total_mass_segment, total_length; ints: dim,
+// num_pkg[3], margin[3],
 // num_interface_cell); nsing points and nseg segments; chr_tag / chr_idx
 // may be NULL (NORMAL / -1).
 extern "C" long long mrsph_host_lset_restart(const char* path, const double* hd, const int* hi, long long n,
@@ -1192,8 +1196,8 @@ extern "C" long long mrsph_host_lset_restart(const char* path, const double* hd,
   }
   double* v[] = {&r.fac_max, &r.fac_mid, &r.fac_min, &r.curv_artificial, &r.total_mass, &r.total_mass_surface,
                  &r.total_volume, &r.total_area, &r.max_phi, &r.max_dl, &r.mid_dl, &r.min_dl, &r.max_curv,
-                 &r.min_curv};
-  for (int k = 0; k < 14; k++) *v[k] = hd[12 + k];
+                 &r.min_curv, &r.total_mass_segment, &r.total_length};
+  for (int k = 0; k < 16; k++) *v[k] = hd[12 + k];
   r.dim = hi[0];
   r.num_interface_cell = hi[7];
   r.phi.assign(phi, phi + n);

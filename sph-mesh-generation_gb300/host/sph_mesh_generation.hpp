@@ -228,6 +228,7 @@ struct LsetRestart {
   std::array<double, 3> dpkg{{1, 1, 1}}, dcell{{1, 1, 1}};
   double fac_max = 0, fac_mid = 0, fac_min = 0, curv_artificial = 0;
   double total_mass = 0, total_mass_surface = 0, total_volume = 0, total_area = 0;
+  double total_mass_segment = 0, total_length = 0;
   double max_phi = 0, max_dl = 0, mid_dl = 0, min_dl = 0, max_curv = 0, min_curv = 0;
   int num_interface_cell = 0;
   // characteristic points (3 doubles each) and segments (6 doubles each)

@@ -70,7 +70,8 @@ class VolumeMassStats(C.Structure):
     _fields_ = ([(k, C.c_double) for k in ("total_mass", "total_mass_surface", "total_volume", "total_area")] +
                 [(k, C.c_longlong) for k in ("num_interface_cell", "num_particle_mesh", "num_particle_surface",
                                              "num_particle")] +
-                [("device_ms", C.c_double)])
+                [("device_ms", C.c_double), ("total_mass_segment", C.c_double), ("total_length", C.c_double),
+                 ("num_particle_segment", C.c_longlong), ("num_particle_singularity", C.c_longlong)])
 
 
 class StateIn(C.Structure):

@@ -509,8 +509,9 @@ def save_lset_restart(sim, path: str = "rstfile/levelset.rst", level: int = -1) 
     seg = np.asarray(extra.get("segments", np.zeros((0, 6))), dtype="<f8").reshape(-1, 6)
     lset = struct.pack("<di", 1.e-4, len(sing)) + sing.tobytes() + struct.pack("<i", len(seg)) + seg.tobytes()
     lset += struct.pack(_RST_LSET, prm["max_dl"] / dl0, mid / dl0, prm["min_dl"] / dl0,
-                       min(1.0, cmax), vm["total_mass"], vm["total_mass_surface"], 0.0, vm["total_volume"],
-                       vm["total_area"], 0.0, float(f["max_phi"]), 0.0, float(prm["max_dl"]), float(mid),
+                       min(1.0, cmax), vm["total_mass"], vm["total_mass_surface"], vm.get("total_mass_segment", 0.0),
+                       vm["total_volume"], vm["total_area"], vm.get("total_length", 0.0), float(f["max_phi"]), 0.0,
+                       float(prm["max_dl"]), float(mid),
                        float(prm["min_dl"]), cmax, cmin, int(vm["num_interface_cell"]))
     gnum = [npkg[d] + 2 * marg[d] for d in range(3)]
     start = [-marg[d] for d in range(3)]

@@ -38,6 +38,11 @@ def dyadic_case(dim: int, kind: str):
 CASES = dict(small_cases())
 CASES["disc2d_fine"] = lambda: cases.disc_hole_2d(spacing=0.01, grid=128)
 CASES["torus3d_single"] = lambda: cases.torus_3d(dx_min=0.01, dx_max=0.04, fine_pkg=24, nlevels=1)
+# corners and edges: the segment mass and the singularity / segment particle numbers
+CASES["box3d_corners"] = lambda: cases.box_with_corners(dim=3, spacing=0.04, grid=32, kernel="hyperbolic",
+                                                        h_over_dx=1.0)
+CASES["box2d_corners"] = lambda: cases.box_with_corners(dim=2, spacing=0.02, grid=64, kernel="hyperbolic",
+                                                        h_over_dx=1.0)
 for _d in (2, 3):
     for _k in ("box", "tilted"):
         CASES[f"{_k}_dyadic_{_d}d"] = (lambda d=_d, k=_k: dyadic_case(d, k))
@@ -57,9 +62,11 @@ def test_volume_mass_matches_oracle(name):
             assert np.array_equal(vol, ref["vol"]), f"cell volumes, level {level}"
             scale = max(np.abs(ref["area"]).max(), 1e-300)
             assert np.max(np.abs(area - ref["area"])) <= 1e-12 * scale, f"cell areas, level {level}"
-            for k in ("total_mass", "total_mass_surface", "total_volume", "total_area"):
+            for k in ("total_mass", "total_mass_surface", "total_volume", "total_area", "total_mass_segment",
+                      "total_length"):
                 assert abs(got[k] - ref[k]) <= 1e-10 * abs(ref[k]) + 1e-300, (k, level)
-            for k in ("num_interface_cell", "num_particle_mesh", "num_particle_surface", "num_particle"):
+            for k in ("num_interface_cell", "num_particle_mesh", "num_particle_surface", "num_particle",
+                      "num_particle_segment", "num_particle_singularity"):
                 assert got[k] == ref[k], (k, level)
             assert got["device_ms"] > 0
     finally:

@@ -252,8 +252,11 @@ def test_lset_restart_characteristics(tmp_path, dim):
     assert np.array_equal(r["tag_characteristic"], f["chr"].reshape(shp)[inner])
     assert np.array_equal(r["idx_characteristic"], f["chr_idx"].reshape(shp)[inner])
     assert np.count_nonzero(r["tag_characteristic"] == 1) == len(case.extra["singularities"])
+    vm = orc.volume_mass(len(case.levels) - 1)
+    assert r["total_mass_segment"] == vm["total_mass_segment"] and r["total_length"] == vm["total_length"]
     if dim == 3:
         assert np.count_nonzero(r["tag_characteristic"] == 2) > 0
+        assert r["total_mass_segment"] > 0
 
 
 def _restart_sim(case, orc):
@@ -305,7 +308,8 @@ def test_cpp_lset_restart_bytes_match_python(tmp_path, name):
     hd = np.array(list(r["box_l"]) + box_r + list(r["dpkg"]) + list(r["dcell"]) +
                   [r[k] for k in ("fac_maximum_dl", "fac_middel_dl", "fac_minimum_dl", "maximum_curv_artificial",
                                   "total_mass", "total_mass_surface", "total_volume", "total_area", "maximum_phi",
-                                  "maximum_dl", "middel_dl", "minimum_dl", "maximum_curv", "minimum_curv")])
+                                  "maximum_dl", "middel_dl", "minimum_dl", "maximum_curv", "minimum_curv",
+                                  "total_mass_segment", "total_length")])
     hi = np.array([r["dim"], *r["num_pkg"], *r["num_pkg_margin"], r["glbl_num_interface_cell"]], dtype=np.int32)
     arrs = [np.ascontiguousarray(r[k].ravel()) for k in ("phi", "n_x", "n_y", "n_z", "curv")]
     tag = np.ascontiguousarray(r["tag_interface"].ravel())

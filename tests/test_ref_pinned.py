@@ -56,3 +56,29 @@ def test_golden_vectors_are_the_reference_output():
                 W, dW = mk.evaluate(L, which, dists)
                 assert np.array_equal(W, GOLD[f"W_{dim}d_{name}_{which}"])
                 assert np.array_equal(dW, GOLD[f"dW_{dim}d_{name}_{which}"])
+
+
+AABB = np.load(os.path.join(HERE, "golden", "aabb_reference.npz"))
+
+
+def test_segment_length_bit_exact_vs_reference():
+    """The length of a segment inside a cell (Segment_AABB_Intersection,
+    AABB_calculator.cpp:6-55, through Get_segment_length,
+    geometry_calculator.cpp:571-589), incl. axis-parallel segments whose slab
+    tests see infinities and NaNs: the oracle's restatement bit for bit."""
+    for mn, mx, v0, v1, L in zip(AABB["mn"], AABB["mx"], AABB["v0"], AABB["v1"], AABB["length"]):
+        got = oracle.Oracle.segment_length(mn, mx, v0, v1)
+        assert np.array_equal(got, L), (mn, mx, v0, v1, got, L)
+    assert (AABB["length"] > 0).sum() > 100 and (AABB["length"] == 0).sum() > 50
+
+
+def test_aabb_golden_is_the_reference_output():
+    import build_ref
+    if not build_ref.aabb_available():
+        pytest.skip("reference sources absent")
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import make_aabb_golden as mk
+    mn, mx, v0, v1 = mk.cases()
+    assert np.array_equal(mk.reference_lengths(mn, mx, v0, v1), AABB["length"])
+    for k, v in (("mn", mn), ("mx", mx), ("v0", v0), ("v1", v1)):
+        assert np.array_equal(v, AABB[k])

@@ -162,3 +162,29 @@ def test_count_close_to_spacing_integral():
     r = oracle.Oracle(case).volume_mass(-1)
     n_int = cases.particle_count(case.levels, case.params)
     assert abs(r["num_particle"] - n_int) / n_int < 0.1
+
+
+def test_oracle_segment_and_singularity_terms():
+    """A box [0.1, 0.9]^3 whose 8 corners are singularities and 12 edges
+    segments: the SEGMENT cells' lengths add up to the edges' length outside
+    the corner (SINGULARITY) cells, and Get_num_particles
+    (sph_mesh_generation.cpp:909-923) counts 8 singularity particles and
+    int(total_mass_segment - 4) segment particles; in 2D neither term exists
+    beyond the 4 singularities."""
+    import oracle
+    from mrsph import cases
+    case = cases.box_with_corners(dim=3, spacing=0.04, grid=32, kernel="hyperbolic", h_over_dx=1.0)
+    orc = oracle.Oracle(case)
+    r = orc.volume_mass(0)
+    dc = case.levels[0].dpkg[0] / 4
+    assert 12 * 0.8 - 24 * dc * 1.5 < r["total_length"] <= 12 * 0.8 + 1e-12
+    assert r["num_particle_singularity"] == 8
+    assert r["num_particle_segment"] == max(int(r["total_mass_segment"] - 4.0), 0) > 0
+    surf = max(int(r["total_mass_surface"] - 0.5 * r["total_mass_segment"]), 0)
+    assert r["num_particle_surface"] == min(surf, r["num_interface_cell"])
+    assert r["num_particle"] == (r["num_particle_mesh"] + r["num_particle_surface"] + r["num_particle_segment"] +
+                                 r["num_particle_singularity"])
+    case2 = cases.box_with_corners(dim=2, spacing=0.02, grid=64, kernel="hyperbolic", h_over_dx=1.0)
+    r2 = oracle.Oracle(case2).volume_mass(0)
+    assert r2["total_mass_segment"] == 0.0 and r2["num_particle_segment"] == 0
+    assert r2["num_particle_singularity"] == 4
