@@ -646,3 +646,58 @@ def case_by_name(name: str, **kw) -> Case:
     if name == "torus_3d":
         return torus_3d(**kw)
     raise KeyError(name)
+
+
+def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.3, precision: str = "fp32",
+                      seed: int = 0, scale_law: int = 0) -> Case:
+    """A case from a level-set restart (rstfile/levelset.rst, the layout of
+    Levelset::Save_lset_restart_file, level_set.cpp:1022-1094, read by
+    Load_lset_restart_file, :1098-1175, and Load_level_set_rstfile,
+    lset_level_infor.cpp:932-1080): the domain, the level's packages and the
+    interior cells' phi, the spacing bounds and middle spacing, and the
+    singularity points and segments.
+
+    The file holds the interior cells only.  The reference fills the margin
+    packages from its analytic geometry before reading the file
+    (Levelset::Initialize); here a margin cell takes the phi of the nearest
+    interior cell minus its distance to that cell, i.e. a distance field
+    continued outward."""
+    from .io import load_lset_restart
+    r = load_lset_restart(path)
+    dim = int(r["dim"])
+    m = int(r["num_pkg_margin"][0])
+    npkg = [int(r["num_pkg"][d]) if d < dim else 1 for d in range(3)]
+    dpkg = [float(r["dpkg"][d]) for d in range(3)]
+    dcell = [float(r["dcell"][d]) for d in range(3)]
+    box_l = [float(r["box_l"][d]) if d < dim else 0.0 for d in range(3)]
+    box_r = [float(r["box_r"][d]) if d < dim else 0.0 for d in range(3)]
+    inner = np.asarray(r["phi"], dtype=np.float64)
+    pad = [4 * m if d < dim else 0 for d in range(3)]
+    shape = tuple(inner.shape[a] + 2 * pad[2 - a] for a in range(3))
+    # nearest interior index and the offset to it, per axis (arrays are z, y, x)
+    idx, off = [], []
+    for a in range(3):
+        d = 2 - a
+        g = np.arange(shape[a]) - pad[d]
+        c = np.clip(g, 0, inner.shape[a] - 1)
+        idx.append(c)
+        off.append((g - c) * (dcell[d] if d < dim else 0.0))
+    Z, Y, X = np.meshgrid(*idx, indexing="ij")
+    dz, dy, dx = np.meshgrid(*off, indexing="ij")
+    phi = inner[Z, Y, X] - np.sqrt(dx * dx + dy * dy + dz * dz)
+    lv = LevelGrid(box_l, dpkg, npkg, m, np.ascontiguousarray(phi), None)
+    p = default_params(dim)
+    cell_ratio = 2.0 * h_over_dx
+    min_dl, max_dl = float(r["minimum_dl"]), float(r["maximum_dl"])
+    if not cell_levels_consistent(box_l, box_r, dim, max_dl * cell_ratio, min_dl * cell_ratio):
+        raise ValueError("the restart's domain and spacing give an inconsistent cell-list level plan "
+                         "(sph.cpp:144-180); choose another h_over_dx")
+    p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=min_dl, max_dl=max_dl,
+             cell_ratio=cell_ratio, box_l=box_l, box_r=box_r, seed=seed, scale_law=scale_law,
+             middle_dl=float(r["middel_dl"]))
+    cs = Case("lset_restart", p, [lv], particle_count([lv], p))
+    if len(r["singularities"]):
+        cs.extra["singularities"] = np.asarray(r["singularities"])
+    if len(r["segments"]):
+        cs.extra["segments"] = np.asarray(r["segments"])
+    return cs

@@ -44,3 +44,23 @@ def test_writers_and_restart_round_trip(tmp_path):
     assert io.load_data_for_post(g2, pst, pre_run=False) == len(p["xyz"])
     assert np.array_equal(g2.particles(("xyz",))["xyz"], p["xyz"])
     g2.close()
+
+
+def test_case_from_lset_restart_relaxes_like_its_writer(tmp_path):
+    """A level-set restart written from a live handle and loaded back as a
+    case (cases.from_lset_restart) relaxes the same particles, bit for bit,
+    as the case that wrote it."""
+    case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=1)
+    g = SPHMeshGeneration(case, precision="fp32")
+    path = io.save_lset_restart(g, str(tmp_path / "levelset.rst"))
+    c2 = cases.from_lset_restart(path, kernel="wendland", h_over_dx=case.params["cell_ratio"] / 2,
+                                 precision="fp32", scale_law=case.params.get("scale_law", 0))
+    g2 = SPHMeshGeneration(c2, precision="fp32")
+    out = []
+    for s in (g, g2):
+        s.Initialize_case()
+        s.SPH_run_mesh_generation(20)
+        out.append(s.particles(("xyz", "type", "h")))
+        s.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k

@@ -324,3 +324,53 @@ def test_cpp_lset_restart_bytes_match_python(tmp_path, name):
              len(seg), seg.ctypes.data if len(seg) else None, ctag.ctypes.data, cidx.ctypes.data)
     ref = open(py, "rb").read()
     assert size == len(ref) and out.read_bytes() == ref
+
+
+@pytest.mark.parametrize("name", ["disc2d", "box2d", "torus3d"])
+def test_case_from_lset_restart(tmp_path, name):
+    """A case read back from a level-set restart (Load_lset_restart_file,
+    level_set.cpp:1098-1175): the interior cells' phi, the domain, the
+    spacing bounds and the characteristic points and segments are the
+    written ones; a margin cell holds the nearest interior cell's phi minus
+    its distance to it; and the oracle relaxes the same particles from it as
+    from the case that wrote the file (the margins are never sampled)."""
+    import oracle
+    case = {"disc2d": lambda: cases.disc_hole_2d(spacing=0.02, grid=64),
+            "box2d": lambda: cases.box_with_corners(dim=2, spacing=0.02, grid=64),
+            "torus3d": lambda: cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=1)}[name]()
+    orc = oracle.Oracle(case)
+    path = io.save_lset_restart(_restart_sim(case, orc), str(tmp_path / "levelset.rst"))
+    kern = {v: k for k, v in cases.KERNELS.items()}[case.params["kernel"]]
+    c2 = cases.from_lset_restart(path, kernel=kern, h_over_dx=case.params["cell_ratio"] / 2,
+                                 precision="fp64", scale_law=case.params.get("scale_law", 0))
+    dim = case.params["dim"]
+    lv, lv2 = case.levels[0], c2.levels[0]
+    m = 4 * lv.margin
+    inner = (slice(m, -m) if dim == 3 else slice(None), slice(m, -m), slice(m, -m))
+    assert lv2.phi.shape == lv.phi.shape and lv2.margin == lv.margin
+    assert np.array_equal(lv2.phi[inner], lv.phi[inner])
+    assert lv2.num_pkg[:dim] == lv.num_pkg[:dim] and lv2.dpkg[:dim] == lv.dpkg[:dim]
+    for k in ("min_dl", "max_dl", "cell_ratio", "box_l", "box_r", "kernel", "dim"):
+        assert np.array_equal(np.asarray(c2.params[k])[:dim] if k.startswith("box") else c2.params[k],
+                              np.asarray(case.params[k])[:dim] if k.startswith("box") else case.params[k]), k
+    for k in ("singularities", "segments"):
+        assert (k in c2.extra) == (k in case.extra)
+        if k in case.extra:
+            assert np.array_equal(np.asarray(c2.extra[k]), np.asarray(case.extra[k]))
+    # corner of the margin: (m, m[, m]) cells outward along each axis
+    dc = [lv.dpkg[d] / 4.0 for d in range(dim)]
+    corner = (0 if dim == 2 else 0, 0, 0)
+    near = (0 if dim == 2 else m, m, m)
+    want = lv.phi[near] - np.sqrt(sum((m * dc[d]) ** 2 for d in range(dim)))
+    assert lv2.phi[corner] == want
+    assert c2.n_particles == case.n_particles
+    o2 = oracle.Oracle(c2)
+    n = case.n_particles
+    for o in (orc, o2):
+        o.alloc(n)
+        o.seed(n)
+        o.pre_run()
+        o.steps(3)
+    s1, s2 = orc.get_state(), o2.get_state()
+    for k in s1:
+        assert np.array_equal(s1[k], s2[k]), k
