@@ -5,6 +5,7 @@
 //   mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N]
 //               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]
 //               [--lset-restart] [--cvp K] [--cvp-iter M]
+//   mrsph_relax --load-lset-restart PATH [--kernel NAME] [--h-over-dx X] [...]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
 // particle-steps/s, final time step).  --count-only prints the particle count
@@ -19,8 +20,13 @@
 // geometry's singularity points and segments.  --cvp K partitions the
 // relaxed particles into K cells (Voronoi::Partitioning, M iterations at
 // most, default 4000), the initial VPs at particles 0, n/K, 2n/K, ...; the
-// JSON line then carries the result and the final VPs.  Exit status 2 on an engine
-// error.
+// JSON line then carries the result and the final VPs.  --load-lset-restart
+// is the reference's restart run (Load_rst_case): the workload is the level
+// set of a rstfile/levelset.rst (one level, its characteristic points and
+// segments), seeded with Get_num_particles over the file's totals; --kernel
+// (hyperbolic, cubic, wendland, gaussian, quintic; default wendland) and
+// --h-over-dx (default 1.3) set the smoothing kernel and h / dx.  Exit status
+// 2 on an engine or file error.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -31,7 +37,8 @@
 using namespace mrsph_host;
 
 int main(int argc, char** argv) {
-  std::string wl = "disc_hole_2d", out, prec;
+  std::string wl = "disc_hole_2d", out, prec, rst, kern = "wendland";
+  double hdx = 1.3;
   int steps = -1, every = 0, cvp_k = 0, cvp_iter = 4000;
   long long n = -1;
   bool count_only = false, cut_cell = false, vtu = false, lset = false, lset_rst = false;
@@ -57,10 +64,14 @@ int main(int argc, char** argv) {
     else if (s == "--lset-restart") lset_rst = true;
     else if (s == "--cvp") cvp_k = std::atoi(val().c_str());
     else if (s == "--cvp-iter") cvp_iter = std::atoi(val().c_str());
+    else if (s == "--load-lset-restart") rst = val();
+    else if (s == "--kernel") kern = val();
+    else if (s == "--h-over-dx") hdx = std::atof(val().c_str());
     else if (s == "--help" || s == "-h") {
       std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
                   "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n"
-                  "                   [--lset-restart] [--cvp K] [--cvp-iter M]\n");
+                  "                   [--lset-restart] [--cvp K] [--cvp-iter M]\n"
+                  "       mrsph_relax --load-lset-restart PATH [--kernel NAME] [--h-over-dx X] [...]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
@@ -69,7 +80,18 @@ int main(int argc, char** argv) {
   }
   try {
     Case c;
-    if (wl == "disc_hole_2d") c = disc_hole_2d(0.02, 64, MRSPH_KERNEL_WENDLAND, 1.3,
+    if (!rst.empty()) {
+      static const char* names[] = {"hyperbolic", "cubic", "wendland", "gaussian", "quintic"};
+      int k = -1;
+      for (int q = 0; q < 5; q++)
+        if (kern == names[q]) k = q;
+      if (k < 0) {
+        std::fprintf(stderr, "unknown kernel %s\n", kern.c_str());
+        return 1;
+      }
+      c = case_from_lset_restart(Load_lset_restart(rst), k, hdx,
+                                 prec == "fp64" ? MRSPH_FP64_PLAIN : MRSPH_FP32_SPLIT);
+    } else if (wl == "disc_hole_2d") c = disc_hole_2d(0.02, 64, MRSPH_KERNEL_WENDLAND, 1.3,
                                                prec == "fp32" ? MRSPH_FP32_SPLIT : MRSPH_FP64_PLAIN);
     else if (wl == "torus_3d") c = torus_3d(0.005, 0.02, MRSPH_KERNEL_WENDLAND, 1.3,
                                            prec == "fp64" ? MRSPH_FP64_PLAIN : MRSPH_FP32_SPLIT);

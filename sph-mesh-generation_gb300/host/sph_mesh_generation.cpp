@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 
 namespace mrsph_host {
 
@@ -671,6 +672,153 @@ std::string lset_restart_bytes(const LsetRestart& r) {
   return b;
 }
 
+namespace {
+// Sequential little-endian reader over a file's bytes.
+struct ByteReader {
+  std::string b;
+  size_t o = 0;
+  template <class T>
+  T get() {
+    T v;
+    need(sizeof(T));
+    std::memcpy(&v, b.data() + o, sizeof(T));
+    o += sizeof(T);
+    return v;
+  }
+  template <class T>
+  void get_n(std::vector<T>& v, size_t n) {
+    need(sizeof(T) * n);
+    v.resize(n);
+    if (n) std::memcpy(v.data(), b.data() + o, sizeof(T) * n);
+    o += sizeof(T) * n;
+  }
+  void need(size_t k) const {
+    if (b.size() - o < k) throw Error(MRSPH_ERR_ARG, "level-set restart: file too short");
+  }
+};
+}  // namespace
+
+LsetRestart Load_lset_restart(const std::string& path) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) throw Error(MRSPH_ERR_ARG, "level-set restart: cannot open " + path);
+  ByteReader rd;
+  rd.b.assign(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
+  LsetRestart r;
+  r.dim = rd.get<int>();
+  if (r.dim != 2 && r.dim != 3) throw Error(MRSPH_ERR_ARG, "level-set restart: dimension must be 2 or 3");
+  for (int d = 0; d < 3; d++) rd.get<double>();  // domain
+  for (int d = 0; d < 3; d++) r.box_l[d] = rd.get<double>();
+  for (int d = 0; d < 3; d++) r.box_r[d] = rd.get<double>();
+  for (int k = 0; k < 9; k++) rd.get<double>();  // particle box: domain, left, right
+  for (int k = 0; k < 8; k++) rd.get<int>();     // resolution, Lmin, Lmax, ini_num_cell
+  if (rd.get<int>() != 1) throw Error(MRSPH_ERR_ARG, "level-set restart: only one level is read");
+  rd.get<double>();  // convergence_error
+  const int nsing = rd.get<int>();
+  if (nsing < 0) throw Error(MRSPH_ERR_ARG, "level-set restart: negative singularity count");
+  rd.get_n(r.sing, 3 * (size_t)nsing);
+  const int nseg = rd.get<int>();
+  if (nseg < 0) throw Error(MRSPH_ERR_ARG, "level-set restart: negative segment count");
+  rd.get_n(r.seg, 6 * (size_t)nseg);
+  double* v[] = {&r.fac_max, &r.fac_mid, &r.fac_min, &r.curv_artificial, &r.total_mass, &r.total_mass_surface,
+                 &r.total_mass_segment, &r.total_volume, &r.total_area, &r.total_length, &r.max_phi, nullptr,
+                 &r.max_dl, &r.mid_dl, &r.min_dl, &r.max_curv, &r.min_curv};
+  for (double* p : v) {
+    const double x = rd.get<double>();
+    if (p) *p = x;  // maximum_psi is not kept
+  }
+  r.num_interface_cell = rd.get<int>();
+  rd.get<int>();     // packages incl. margins
+  rd.get<double>();  // scale
+  rd.get<double>();  // dl
+  for (int d = 0; d < 3; d++) r.num_pkg[d] = rd.get<int>();
+  for (int k = 0; k < 15; k++) rd.get<int>();  // package counts incl. margins, global and local ranges
+  for (int d = 0; d < 3; d++) r.margin[d] = rd.get<int>();
+  for (int d = 0; d < 3; d++) r.dpkg[d] = rd.get<double>();
+  for (int d = 0; d < 3; d++) r.dcell[d] = rd.get<double>();
+  size_t n = 1;
+  for (int d = 0; d < 3; d++) {
+    if (r.num_pkg[d] < 1 || (d >= r.dim && r.num_pkg[d] != 1) || r.margin[d] < 0)
+      throw Error(MRSPH_ERR_ARG, "level-set restart: bad package counts");
+    n *= (size_t)r.num_pkg[d] * (d < r.dim ? 4 : 1);
+  }
+  std::vector<double> psi;
+  std::vector<double>* dbl[] = {&r.phi, &r.nx, &r.ny, &r.nz, &r.curv, &psi};
+  for (std::vector<double>* a : dbl) rd.get_n(*a, n);
+  rd.get_n(r.tag, n);
+  rd.get_n(r.chr_tag, n);
+  rd.get_n(r.chr_idx, n);
+  rd.get_n(r.scale, n);
+  if (rd.o != rd.b.size()) throw Error(MRSPH_ERR_ARG, "level-set restart: trailing bytes");
+  return r;
+}
+
+long long restart_num_particles(double total_mass, double total_mass_surface, double total_mass_segment,
+                                int num_singularity, int num_interface_cell) {
+  const long long seg = std::max((long long)(total_mass_segment - 0.5 * num_singularity), 0LL);
+  long long surf = std::max((long long)(total_mass_surface - 0.5 * total_mass_segment), 0LL);
+  surf = std::min(surf, (long long)num_interface_cell);
+  const long long mesh = std::max((long long)(total_mass - 0.5 * total_mass_surface), 0LL);
+  return mesh + surf + num_singularity + seg;
+}
+
+Case case_from_lset_restart(const LsetRestart& r, int kernel, double h_over_dx, int precision,
+                            unsigned long long seed, int scale_law) {
+  const int dim = r.dim;
+  Case c;
+  c.name = "lset_restart";
+  mrsph_params p = default_params(dim);
+  p.kernel = kernel;
+  p.precision = precision;
+  p.min_dl = r.min_dl;
+  p.max_dl = r.max_dl;
+  p.cell_ratio = 2.0 * h_over_dx;
+  for (int d = 0; d < 3; d++) {
+    p.box_l[d] = d < dim ? r.box_l[d] : 0.0;
+    p.box_r[d] = d < dim ? r.box_r[d] : 0.0;
+  }
+  p.seed = seed;
+  p.scale_law = scale_law;
+  p.middle_dl = r.mid_dl;
+  if (!cell_levels_consistent(p.box_l, p.box_r, dim, r.max_dl * p.cell_ratio, r.min_dl * p.cell_ratio))
+    throw Error(MRSPH_ERR_ARG, "the restart's domain and spacing give an inconsistent cell-list level plan "
+                               "(sph.cpp:144-180); choose another h_over_dx");
+  LevelGrid L;
+  const int m = r.margin[0];
+  int in[3], pad[3], full[3];
+  for (int d = 0; d < 3; d++) {
+    L.box_l[d] = p.box_l[d];
+    L.dpkg[d] = r.dpkg[d];
+    L.num_pkg[d] = d < dim ? r.num_pkg[d] : 1;
+    in[d] = r.num_pkg[d] * (d < dim ? 4 : 1);
+    pad[d] = d < dim ? 4 * m : 0;
+    full[d] = in[d] + 2 * pad[d];
+  }
+  L.margin = m;
+  L.phi.resize((size_t)full[0] * full[1] * full[2]);
+  for (int z = 0; z < full[2]; z++)
+    for (int y = 0; y < full[1]; y++)
+      for (int x = 0; x < full[0]; x++) {
+        const int g[3] = {x - pad[0], y - pad[1], z - pad[2]};
+        int q[3];
+        double off[3];
+        for (int d = 0; d < 3; d++) {
+          q[d] = std::min(std::max(g[d], 0), in[d] - 1);
+          off[d] = (double)(g[d] - q[d]) * (d < dim ? r.dcell[d] : 0.0);
+        }
+        const double near = r.phi[((size_t)q[2] * in[1] + q[1]) * in[0] + q[0]];
+        L.phi[((size_t)z * full[1] + y) * full[0] + x] =
+            near - std::sqrt(off[0] * off[0] + off[1] * off[1] + off[2] * off[2]);
+      }
+  c.levels.push_back(std::move(L));
+  c.params = p;
+  c.singularities = r.sing;
+  c.segments = r.seg;
+  c.n_particles = restart_num_particles(r.total_mass, r.total_mass_surface, r.total_mass_segment,
+                                        (int)(r.sing.size() / 3), r.num_interface_cell);
+  c.steps = 200;
+  return c;
+}
+
 std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path, int level) {
   const Case& cs = sim.Get_case();
   const mrsph_params& p = cs.params;
@@ -1211,4 +1359,34 @@ extern "C" long long mrsph_host_lset_restart(const char* path, const double* hd,
   std::ofstream o(path, std::ios::binary | std::ios::trunc);
   o.write(b.data(), (std::streamsize)b.size());
   return o ? (long long)b.size() : -1;
+}
+
+// C entry for the loader tests: the case a level-set restart gives
+// (case_from_lset_restart), its phi incl. margins copied to phi (cap
+// values at most); prm receives min_dl, max_dl, middle_dl, cell_ratio,
+// box_l[3], box_r[3]; cnt receives the particle count, the number of phi
+// values, the singularity and segment counts.  Returns 0, or -1 with the
+// message in err.
+extern "C" int mrsph_host_lset_case(const char* path, int kernel, double h_over_dx, int precision, int scale_law,
+                                    double* phi, long long cap, double* prm, long long* cnt, char* err,
+                                    long long err_len) {
+  try {
+    const mrsph_host::Case c =
+        mrsph_host::case_from_lset_restart(mrsph_host::Load_lset_restart(path), kernel, h_over_dx, precision, 0,
+                                           scale_law);
+    const std::vector<double>& f = c.levels[0].phi;
+    if ((long long)f.size() <= cap) std::memcpy(phi, f.data(), f.size() * sizeof(double));
+    const double v[] = {c.params.min_dl, c.params.max_dl, c.params.middle_dl, c.params.cell_ratio,
+                        c.params.box_l[0], c.params.box_l[1], c.params.box_l[2],
+                        c.params.box_r[0], c.params.box_r[1], c.params.box_r[2]};
+    std::memcpy(prm, v, sizeof(v));
+    cnt[0] = c.n_particles;
+    cnt[1] = (long long)f.size();
+    cnt[2] = (long long)(c.singularities.size() / 3);
+    cnt[3] = (long long)(c.segments.size() / 6);
+    return 0;
+  } catch (const std::exception& e) {
+    if (err && err_len > 0) std::snprintf(err, (size_t)err_len, "%s", e.what());
+    return -1;
+  }
 }

@@ -241,6 +241,28 @@ std::string lset_restart_bytes(const LsetRestart& r);
 // Gathers the record of one level (< 0: the finest) from the engine and
 // writes it to path.
 std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path, int level = -1);
+// Reads a level-set restart of one level, the bytes lset_restart_bytes
+// writes (Load_rst_case, sph_mesh_generation.cpp:323-414, with
+// Load_lset_restart_file, level_set.cpp:1098-1175, and
+// Load_level_set_rstfile, lset_level_infor.cpp:932-1080); throws Error on a
+// short, oversized or inconsistent file.
+LsetRestart Load_lset_restart(const std::string& path);
+// Get_num_particles (sph_mesh_generation.cpp:900-930) over a level set's
+// totals: one particle per singularity point; segment, surface and interior
+// counts each less half the next-lower-dimensional mass, truncated and at
+// least 0; the surface count at most the number of interface cells.
+long long restart_num_particles(double total_mass, double total_mass_surface, double total_mass_segment,
+                                int num_singularity, int num_interface_cell);
+// A runnable case from a level-set restart (the reference's restart run):
+// the file's domain, spacing bounds, middle spacing, characteristic points
+// and segments, and one level-set level whose interior cells hold the file's
+// phi.  The reference fills the margin packages from its analytic geometry;
+// here a margin cell holds the nearest interior cell's phi minus its
+// distance to that cell.  The count is restart_num_particles of the file's
+// totals.  Throws Error when the domain and spacing give an inconsistent
+// cell-list level plan.
+Case case_from_lset_restart(const LsetRestart& r, int kernel = MRSPH_KERNEL_WENDLAND, double h_over_dx = 1.3,
+                            int precision = MRSPH_FP32_SPLIT, unsigned long long seed = 0, int scale_law = 0);
 
 class Mesh_binary_writer {
  public:

@@ -648,6 +648,20 @@ def case_by_name(name: str, **kw) -> Case:
     raise KeyError(name)
 
 
+def restart_num_particles(total_mass: float, total_mass_surface: float, total_mass_segment: float,
+                          num_singularity: int, num_interface_cell: int) -> int:
+    """SPH_mesh_generation::Get_num_particles (sph_mesh_generation.cpp:900-930)
+    over a level set's totals: one particle per singularity point; segment,
+    surface and interior counts each less half the next-lower-dimensional
+    mass, truncated and at least 0; the surface count at most the number of
+    interface cells."""
+    seg = max(int(total_mass_segment - 0.5 * num_singularity), 0)
+    surf = max(int(total_mass_surface - 0.5 * total_mass_segment), 0)
+    surf = min(surf, int(num_interface_cell))
+    mesh = max(int(total_mass - 0.5 * total_mass_surface), 0)
+    return mesh + surf + int(num_singularity) + seg
+
+
 def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.3, precision: str = "fp32",
                       seed: int = 0, scale_law: int = 0) -> Case:
     """A case from a level-set restart (rstfile/levelset.rst, the layout of
@@ -661,7 +675,8 @@ def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.
     packages from its analytic geometry before reading the file
     (Levelset::Initialize); here a margin cell takes the phi of the nearest
     interior cell minus its distance to that cell, i.e. a distance field
-    continued outward."""
+    continued outward.  The particle count is the reference's restart count,
+    Get_num_particles over the file's totals (restart_num_particles)."""
     from .io import load_lset_restart
     r = load_lset_restart(path)
     dim = int(r["dim"])
@@ -695,7 +710,9 @@ def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.
     p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=min_dl, max_dl=max_dl,
              cell_ratio=cell_ratio, box_l=box_l, box_r=box_r, seed=seed, scale_law=scale_law,
              middle_dl=float(r["middel_dl"]))
-    cs = Case("lset_restart", p, [lv], particle_count([lv], p))
+    n = restart_num_particles(r["total_mass"], r["total_mass_surface"], r["total_mass_segment"],
+                              len(r["singularities"]), r["glbl_num_interface_cell"])
+    cs = Case("lset_restart", p, [lv], n)
     if len(r["singularities"]):
         cs.extra["singularities"] = np.asarray(r["singularities"])
     if len(r["segments"]):

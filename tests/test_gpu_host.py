@@ -161,3 +161,32 @@ def test_cpp_driver_partitioning_matches_python():
     g.close()
     assert d["cvp"]["iterations"] == res["iterations"]
     assert np.array_equal(np.array(d["cvp"]["vp"]).reshape(K, 3), vp)
+
+
+def test_cpp_driver_restart_run_matches_python(tmp_path):
+    """The reference's two-run workflow: a level-set restart written by the
+    C++ driver (--lset-restart) is relaxed by the C++ restart run
+    (--load-lset-restart, Load_rst_case) and by the Python mirror
+    (cases.from_lset_restart) to the same particles, SINGULARITY particles
+    included (the first appear after about 250 steps); the driver seeds the
+    reference's restart count."""
+    binary = build.build_host()
+    r = subprocess.run([binary, "--case", "box_2d", "--precision", "fp64", "--steps", "1", "--out",
+                        str(tmp_path / "a"), "--lset-restart"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    rst = str(tmp_path / "a" / "rstfile" / "levelset.rst")
+    r = subprocess.run([binary, "--load-lset-restart", rst, "--kernel", "hyperbolic", "--h-over-dx", "1.0",
+                        "--precision", "fp64", "--steps", "300", "--output-every", "300", "--out",
+                        str(tmp_path / "b")], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    case = cases.from_lset_restart(rst, kernel="hyperbolic", h_over_dx=1.0, precision="fp64")
+    assert d["n_particles"] == case.n_particles and d["step"] == 300 and d["flags"] & ~8 == 0
+    g = SPHMeshGeneration(case, precision="fp64")
+    g.Initialize_case()
+    g.SPH_run_mesh_generation(300)
+    gp = g.particles(("xyz", "type"))
+    g.close()
+    cpp = io.read_pst(str(tmp_path / "b" / "rstfile_particles" / "step_300_rank_0.pst"))
+    assert np.max(np.abs(cpp - gp["xyz"])) < 1e-12
+    assert (gp["type"] == 2).any()

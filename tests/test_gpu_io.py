@@ -53,12 +53,14 @@ def test_case_from_lset_restart_relaxes_like_its_writer(tmp_path):
     case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=1)
     g = SPHMeshGeneration(case, precision="fp32")
     path = io.save_lset_restart(g, str(tmp_path / "levelset.rst"))
-    c2 = cases.from_lset_restart(path, kernel="wendland", h_over_dx=case.params["cell_ratio"] / 2,
+    kern = {v: k for k, v in cases.KERNELS.items()}[case.params["kernel"]]
+    c2 = cases.from_lset_restart(path, kernel=kern, h_over_dx=case.params["cell_ratio"] / 2,
                                  precision="fp32", scale_law=case.params.get("scale_law", 0))
     g2 = SPHMeshGeneration(c2, precision="fp32")
     out = []
+    assert c2.n_particles == g.volume_mass(0)["num_particle"]
     for s in (g, g2):
-        s.Initialize_case()
+        s.Initialize_case(case.n_particles)
         s.SPH_run_mesh_generation(20)
         out.append(s.particles(("xyz", "type", "h")))
         s.close()

@@ -183,3 +183,53 @@ def test_cpp_pvtu_matches_python(binary, mesh):
     cd = [("vol", np.zeros(1, "<f4")), ("aspect", np.zeros(1, "<f4"))] if mesh else []
     ref = io._pvtu_text(["piece_0.vtu"], io._fields_meta(pd), io._fields_meta(cd))
     assert n == len(ref) and buf.value.decode() == ref
+
+
+@pytest.mark.parametrize("name", ["disc2d", "box3d"])
+def test_cpp_case_from_lset_restart_matches_python(binary, tmp_path, name):
+    """The C++ restart run (Load_lset_restart + case_from_lset_restart, the
+    reference's Load_rst_case) builds the case the Python loader builds from
+    the same rstfile/levelset.rst: phi incl. margins bit-equal, the same
+    spacing bounds, domain, characteristic points and segments, and the
+    reference's restart count (Get_num_particles over the file's totals);
+    the driver seeds that count.  A truncated file is an error (status 2)."""
+    import ctypes
+    import oracle
+    from mrsph import io
+    from test_io import _restart_sim
+    case = {"disc2d": lambda: cases.disc_hole_2d(spacing=0.02, grid=64),
+            "box3d": lambda: cases.box_with_corners(dim=3, spacing=0.04, grid=32, kernel="hyperbolic",
+                                                    h_over_dx=1.0)}[name]()
+    orc = oracle.Oracle(case)
+    path = io.save_lset_restart(_restart_sim(case, orc), str(tmp_path / "levelset.rst"))
+    kern = {v: k for k, v in cases.KERNELS.items()}[case.params["kernel"]]
+    hdx = case.params["cell_ratio"] / 2
+    py = cases.from_lset_restart(path, kernel=kern, h_over_dx=hdx)
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    f = lib.mrsph_host_lset_case
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong]
+    import numpy as np
+    phi = np.empty(py.levels[0].phi.size)
+    prm = np.empty(10)
+    cnt = np.empty(4, dtype=np.int64)
+    err = ctypes.create_string_buffer(256)
+    assert f(path.encode(), py.params["kernel"], hdx, 0, 0, phi.ctypes.data, len(phi), prm.ctypes.data,
+             cnt.ctypes.data, err, 256) == 0, err.value
+    assert cnt[1] == py.levels[0].phi.size
+    assert np.array_equal(phi, py.levels[0].phi.ravel())
+    p = py.params
+    assert list(prm[:4]) == [p["min_dl"], p["max_dl"], p["middle_dl"], p["cell_ratio"]]
+    assert list(prm[4:7]) == list(p["box_l"]) and list(prm[7:10]) == list(p["box_r"])
+    assert cnt[0] == py.n_particles == orc.volume_mass(0)["num_particle"]
+    assert cnt[2] == len(py.extra.get("singularities", [])) and cnt[3] == len(py.extra.get("segments", []))
+    d = json.loads(run(binary, "--load-lset-restart", path, "--kernel", kern, "--h-over-dx", str(hdx),
+                       "--count-only").stdout)
+    assert d["n_particles"] == py.n_particles and d["workload"] == "lset_restart"
+    short = tmp_path / "short.rst"
+    short.write_bytes(open(path, "rb").read()[:-8])
+    assert f(str(short).encode(), 2, 1.3, 0, 0, phi.ctypes.data, len(phi), prm.ctypes.data, cnt.ctypes.data,
+             err, 256) == -1 and b"too short" in err.value
+    r = run(binary, "--load-lset-restart", str(short), "--count-only")
+    assert r.returncode == 2 and "too short" in r.stderr

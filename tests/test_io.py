@@ -363,7 +363,7 @@ def test_case_from_lset_restart(tmp_path, name):
     near = (0 if dim == 2 else m, m, m)
     want = lv.phi[near] - np.sqrt(sum((m * dc[d]) ** 2 for d in range(dim)))
     assert lv2.phi[corner] == want
-    assert c2.n_particles == case.n_particles
+    assert c2.n_particles == orc.volume_mass(0)["num_particle"]
     o2 = oracle.Oracle(c2)
     n = case.n_particles
     for o in (orc, o2):
