@@ -363,6 +363,40 @@ typedef struct {
  * cap >= *ntri.  quality may be NULL.  2D handles only. */
 int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri, mrsph_tri_quality* quality);
 
+/* 3D tetrahedralisation and tet quality: replaces Graphmeshcls::Reconstruct_tets
+ * (graph_mesh.cpp:981-1100, TetGen's Delaunay tetrahedralisation of all
+ * particles followed by Check_whether_this_tet_should_be_delete, :675-979)
+ * and Tet_quality_statistics (:1967-2400).  The tets are the Delaunay tets
+ * of the particles (positions snapped to the grid `grid`, about one ulp of
+ * the domain's largest coordinate) whose circumsphere lies inside the
+ * neighbour ball (radius cutoff * h) of one of their four particles; tets
+ * whose four particles are all not REAL and whose aspect ratio (longest
+ * edge / smallest height) exceeds 10 are dropped, as in the reference.
+ * Large tets across concavities of the body and on the convex hull, which
+ * TetGen keeps, are not produced.  Uses the neighbour rows of the last
+ * density phase (spilled rows: MRSPH_ERR_RANGE). */
+typedef struct {
+  long long ntet;
+  long long nopen;     /* particles whose ring of certified tets does not close */
+  long long ndeleted;  /* tets dropped by the aspect-ratio rule */
+  long long ntie;      /* particles that met five co-spherical particles */
+  double grid;         /* the snapping grid */
+  double total_volume, min_volume, max_volume;
+  double min_edge, max_edge;
+  double min_aspect, max_aspect, avg_aspect;
+  double min_radius_ratio, max_radius_ratio, avg_radius_ratio; /* 3 r_in / r_circ */
+  double min_dihedral, max_dihedral, avg_min_dihedral;         /* degrees */
+  long long nsmall_dihedral[4]; /* tets whose smallest dihedral is below 10, 20, 30, 40 degrees */
+  long long aspect_hist[12];    /* bins up to 1.5, 2, 2.5, 3, 4, 6, 10, 15, 25, 50, 100, above */
+  long long radius_hist[56];    /* radius ratio in bins of 0.02 (the last takes 1.1 and above) */
+  long long dihedral_hist[45];  /* all six dihedral angles, 4-degree bins */
+} mrsph_tet_quality;
+
+/* tets (cap x 4 ints, ascending vertex ids per tet) may be NULL or too
+ * small: *ntet is always set and tets is filled only when cap >= *ntet.
+ * quality may be NULL.  3D handles only. */
+int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, long long* ntet, mrsph_tet_quality* quality);
+
 /* Batched relaxation of independent geometries (no counterpart in the
  * reference, which relaxes one geometry per run, SPH_run_mesh_generation,
  * sph_mesh_generation.cpp:1371-1463, from Solver::SPH_Mesh_Generation_Solver,

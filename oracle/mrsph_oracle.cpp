@@ -2536,3 +2536,404 @@ void orc_volume_mass(const orc_ctx* c, int level, double* cell_vol, double* cell
 }
 
 }  // extern "C"
+
+// ====================================================================== tets
+// 3D tetrahedralisation (row F3; the reference: Graphmeshcls::Reconstruct_tets,
+// graph_mesh.cpp:981-1100, TetGen's Delaunay tetrahedralisation of all
+// particles, Check_whether_this_tet_should_be_delete, :675-979, and
+// Tet_quality_statistics, :1967-2400).  TetGen is not available, so this
+// oracle restates the local certified-star construction of the library (per
+// particle: gift wrapping over its neighbour row; a tet counts when its
+// circumsphere lies in the row's ball of radius cutoff * h and no row
+// particle lies inside or on it) on the CPU with its own exact arithmetic;
+// the tests pin it against qhull's Delaunay tetrahedralisation (scipy) of
+// the same snapped points.
+namespace tetorc {
+struct Big {  // two's complement, 5 x 64 bits
+  unsigned long long w[5];
+};
+static Big big(long long v) {
+  Big r;
+  r.w[0] = (unsigned long long)v;
+  for (int k = 1; k < 5; k++) r.w[k] = v < 0 ? ~0ull : 0ull;
+  return r;
+}
+static Big add(const Big& a, const Big& b) {
+  Big r;
+  unsigned __int128 c = 0;
+  for (int k = 0; k < 5; k++) {
+    c += (unsigned __int128)a.w[k] + b.w[k];
+    r.w[k] = (unsigned long long)c;
+    c >>= 64;
+  }
+  return r;
+}
+static Big neg(const Big& a) {
+  Big r;
+  for (int k = 0; k < 5; k++) r.w[k] = ~a.w[k];
+  return add(r, big(1));
+}
+static Big sub(const Big& a, const Big& b) { return add(a, neg(b)); }
+static bool isneg(const Big& a) { return (long long)a.w[4] < 0; }
+static Big mul(const Big& a, const Big& b) {
+  const bool na = isneg(a), nb = isneg(b);
+  const Big x = na ? neg(a) : a, y = nb ? neg(b) : b;
+  unsigned long long r[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < 5; i++) {
+    unsigned __int128 c = 0;
+    for (int j = 0; i + j < 5; j++) {
+      c += (unsigned __int128)x.w[i] * y.w[j] + r[i + j];
+      r[i + j] = (unsigned long long)c;
+      c >>= 64;
+    }
+  }
+  Big o;
+  for (int k = 0; k < 5; k++) o.w[k] = r[k];
+  return na != nb ? neg(o) : o;
+}
+static int sign(const Big& a) {
+  if (isneg(a)) return -1;
+  for (int k = 0; k < 5; k++)
+    if (a.w[k]) return 1;
+  return 0;
+}
+static Big M2(long long p, long long q) { return mul(big(p), big(q)); }
+
+struct Ctx {
+  const double* x;
+  double ig;
+  long long I(int j, int q) const { return (long long)std::nearbyint(x[3 * (size_t)j + q] * ig); }
+};
+// exact signs over the integer coordinates (no floating-point filter)
+static int orient(const Ctx& C, int a, int b, int c, int d) {
+  long long v[3][3];
+  const int p[3] = {a, b, c};
+  for (int k = 0; k < 3; k++)
+    for (int q = 0; q < 3; q++) v[k][q] = C.I(p[k], q) - C.I(d, q);
+  const Big m1 = sub(M2(v[1][1], v[2][2]), M2(v[1][2], v[2][1]));
+  const Big m2 = sub(M2(v[2][1], v[0][2]), M2(v[2][2], v[0][1]));
+  const Big m3 = sub(M2(v[0][1], v[1][2]), M2(v[0][2], v[1][1]));
+  return sign(add(add(mul(big(v[0][0]), m1), mul(big(v[1][0]), m2)), mul(big(v[2][0]), m3)));
+}
+static int insph(const Ctx& C, int a, int b, int c, int d, int e) {
+  long long v[4][3];
+  const int p[4] = {a, b, c, d};
+  for (int k = 0; k < 4; k++)
+    for (int q = 0; q < 3; q++) v[k][q] = C.I(p[k], q) - C.I(e, q);
+  Big lift[4], mz[4];
+  for (int k = 0; k < 4; k++) {
+    lift[k] = add(add(M2(v[k][0], v[k][0]), M2(v[k][1], v[k][1])), M2(v[k][2], v[k][2]));
+    mz[k] = big(v[k][2]);
+  }
+  auto xy = [&](int s, int t) { return sub(M2(v[s][0], v[t][1]), M2(v[t][0], v[s][1])); };
+  const Big ab = xy(0, 1), bc = xy(1, 2), cd = xy(2, 3), da = xy(3, 0), ac = xy(0, 2), bd = xy(1, 3);
+  const Big abc = add(sub(mul(mz[0], bc), mul(mz[1], ac)), mul(mz[2], ab));
+  const Big bcd = add(sub(mul(mz[1], cd), mul(mz[2], bd)), mul(mz[3], bc));
+  const Big cda = add(add(mul(mz[2], da), mul(mz[3], ac)), mul(mz[0], cd));
+  const Big dab = add(add(mul(mz[3], ab), mul(mz[0], bd)), mul(mz[1], da));
+  return sign(add(sub(mul(lift[3], abc), mul(lift[2], dab)), sub(mul(lift[1], cda), mul(lift[0], bcd))));
+}
+
+static void cross(const double* u, const double* v, double* w) {
+  w[0] = u[1] * v[2] - u[2] * v[1];
+  w[1] = u[2] * v[0] - u[0] * v[2];
+  w[2] = u[0] * v[1] - u[1] * v[0];
+}
+static double dot(const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; }
+
+// the canonical geometry of a tet over its ascending ids (same terms and
+// order as the library's)
+struct Geo {
+  double A[3][3], det, c[3], rc, vs, P[4][3];
+};
+static Geo geo(const Ctx& C, const int* v) {
+  Geo g;
+  for (int k = 0; k < 4; k++)
+    for (int q = 0; q < 3; q++) g.P[k][q] = C.x[3 * (size_t)v[k] + q];
+  for (int k = 0; k < 3; k++)
+    for (int q = 0; q < 3; q++) g.A[k][q] = g.P[k][q] - g.P[3][q];
+  double x12[3], x20[3], x01[3];
+  cross(g.A[1], g.A[2], x12);
+  cross(g.A[2], g.A[0], x20);
+  cross(g.A[0], g.A[1], x01);
+  g.det = dot(g.A[0], x12);
+  const double r0 = 0.5 * dot(g.A[0], g.A[0]), r1 = 0.5 * dot(g.A[1], g.A[1]), r2 = 0.5 * dot(g.A[2], g.A[2]);
+  for (int q = 0; q < 3; q++) g.c[q] = (r0 * x12[q] + r1 * x20[q] + r2 * x01[q]) / g.det;
+  g.rc = std::sqrt(dot(g.c, g.c));
+  g.vs = std::sqrt(dot(g.A[0], g.A[0])) * std::sqrt(dot(g.A[1], g.A[1])) * std::sqrt(dot(g.A[2], g.A[2]));
+  return g;
+}
+static bool in_ball(const Geo& g, const double* x, double h, double cutoff) {
+  if (!(std::fabs(g.det) >= 1.e-6 * g.vs)) return false;
+  double v[3];
+  for (int q = 0; q < 3; q++) v[q] = g.P[3][q] + g.c[q] - x[q];
+  return std::sqrt(dot(v, v)) + g.rc <= cutoff * h * (1.0 - 1.e-6);
+}
+// aspect, inverse heights and unit inward normals
+static double heights(const Geo& g, double n[4][3], double H[4], double* hmax, double* hsum) {
+  cross(g.A[1], g.A[2], n[0]);
+  cross(g.A[2], g.A[0], n[1]);
+  cross(g.A[0], g.A[1], n[2]);
+  for (int k = 0; k < 3; k++)
+    for (int q = 0; q < 3; q++) n[k][q] /= g.det;
+  for (int q = 0; q < 3; q++) n[3][q] = -n[0][q] - n[1][q] - n[2][q];
+  *hmax = 0.0;
+  *hsum = 0.0;
+  for (int k = 0; k < 4; k++) {
+    H[k] = std::sqrt(dot(n[k], n[k]));
+    *hsum += H[k];
+    *hmax = std::fmax(*hmax, H[k]);
+  }
+  double longlen = 0.0, e[3];
+  for (int k = 0; k < 3; k++) longlen = std::fmax(longlen, dot(g.A[k], g.A[k]));
+  const int ea[3] = {1, 2, 0}, eb[3] = {0, 1, 2};
+  for (int k = 0; k < 3; k++) {
+    for (int q = 0; q < 3; q++) e[q] = g.P[ea[k]][q] - g.P[eb[k]][q];
+    longlen = std::fmax(longlen, dot(e, e));
+  }
+  return longlen;
+}
+static void sort4(int* v) { std::sort(v, v + 4); }
+}  // namespace tetorc
+
+extern "C" {
+struct orc_tet_quality {
+  long long ntet, nopen, ndeleted, ntie;
+  double grid, total_volume, min_volume, max_volume, min_edge, max_edge, min_aspect, max_aspect, avg_aspect;
+  double min_radius_ratio, max_radius_ratio, avg_radius_ratio, min_dihedral, max_dihedral, avg_min_dihedral;
+  long long nsmall_dihedral[4], aspect_hist[12], radius_hist[56], dihedral_hist[45];
+};
+
+// xyz (n x 3, FP64), type, h, neighbour rows (CSR off / nbr in id space,
+// self may be listed); box_l / box_r bound the coordinates.  Returns the tet
+// count (tets filled when cap allows; ascending ids per tet, in the order of
+// the emitting particle and its star), -1 when a star exceeds the library's
+// per-particle limits (96 tets, 160 link edges).
+long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type, const double* h,
+                             const long long* off, const int* nbr, double cutoff, const double* box_l,
+                             const double* box_r, int* tets, long long cap, orc_tet_quality* Q) {
+  using namespace tetorc;
+  double Mx = 1.0;
+  for (int d = 0; d < 3; d++) Mx = std::fmax(Mx, std::fmax(std::fabs(box_l[d]), std::fabs(box_r[d])));
+  int e = 0;
+  std::frexp(Mx, &e);
+  e += 1;
+  const double g = std::ldexp(1.0, e - 52), ig = std::ldexp(1.0, 52 - e);
+  std::vector<double> X(3 * (size_t)n);
+  for (size_t k = 0; k < X.size(); k++) X[k] = std::nearbyint(xyz_in[k] * ig) * g;
+  const Ctx C{X.data(), ig};
+  std::vector<std::vector<int>> out(n);
+  std::vector<int> open(n, 0), tie(n, 0);
+  std::vector<long long> ndel(n, 0);
+  bool overflow = false;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long long i64 = 0; i64 < n; i64++) {
+    const int i = (int)i64;
+    std::vector<int> S;
+    for (long long q = off[i]; q < off[i + 1]; q++)
+      if (nbr[q] != i) S.push_back(nbr[q]);
+    const double* xi = &X[3 * (size_t)i];
+    auto d2 = [&](int j) {
+      const double* p = &X[3 * (size_t)j];
+      const double dx = p[0] - xi[0], dy = p[1] - xi[1], dz = p[2] - xi[2];
+      return dx * dx + dy * dy + dz * dz;
+    };
+    bool degen = false;
+    auto wrap = [&](int a, int b, int s) {
+      int best = -1;
+      for (int d : S) {
+        if (d == a || d == b) continue;
+        if (s * orient(C, i, a, b, d) <= 0) continue;
+        if (best < 0 || s * insph(C, i, a, b, best, d) > 0) best = d;
+      }
+      return best;
+    };
+    auto certify = [&](int a, int b, int d) {
+      int v[4] = {i, a, b, d};
+      sort4(v);
+      const Geo G = geo(C, v);
+      if (!in_ball(G, xi, h[i], cutoff)) return false;
+      const int o = orient(C, v[0], v[1], v[2], v[3]);
+      if (o == 0) return false;
+      // fails on a row particle inside or on the sphere; a tie when some lie
+      // on it and none inside
+      bool inside = false, on = false;
+      for (int q : S) {
+        if (q == v[0] || q == v[1] || q == v[2] || q == v[3]) continue;
+        const int s = o * insph(C, v[0], v[1], v[2], v[3], q);
+        if (s > 0) { inside = true; break; }
+        if (s == 0) on = true;
+      }
+      if (inside || on) {
+        if (!inside) degen = true;
+        return false;
+      }
+      return true;
+    };
+    // nearest particle, then the smallest circumcircle through i and it
+    int a = -1, c = -1;
+    double best = 0.0, bestr = 0.0;
+    for (int j : S) {
+      const double v = d2(j);
+      if (a < 0 || v < best || (v == best && j < a)) { a = j; best = v; }
+    }
+    if (a >= 0) {
+      const double* pa = &X[3 * (size_t)a];
+      const double u[3] = {pa[0] - xi[0], pa[1] - xi[1], pa[2] - xi[2]};
+      const double uu = dot(u, u);
+      for (int j : S) {
+        if (j == a) continue;
+        const double* pj = &X[3 * (size_t)j];
+        const double v[3] = {pj[0] - xi[0], pj[1] - xi[1], pj[2] - xi[2]};
+        const double w[3] = {v[0] - u[0], v[1] - u[1], v[2] - u[2]};
+        double x[3];
+        cross(u, v, x);
+        const double xx = dot(x, x);
+        if (!(xx > 0.0)) continue;
+        const double r2 = uu * dot(v, v) * dot(w, w) / (4.0 * xx);
+        if (c < 0 || r2 < bestr || (r2 == bestr && j < c)) { c = j; bestr = r2; }
+      }
+    }
+    std::vector<std::array<int, 3>> star;
+    if (c >= 0) {
+      for (int s = 1; s >= -1 && star.empty(); s -= 2) {
+        const int d = wrap(a, c, s);
+        if (d >= 0 && certify(a, c, d)) star.push_back(s > 0 ? std::array<int, 3>{a, c, d} : std::array<int, 3>{c, a, d});
+      }
+    }
+    bool op = star.empty(), ovf = false;
+    // link edges (u, v) in the orientation of the tet that registered them
+    std::vector<std::array<int, 2>> le;
+    std::vector<char> done;
+    size_t head = 0;
+    while (!ovf) {
+      for (; head < star.size(); head++) {
+        const auto t = star[head];
+        for (int k = 0; k < 3; k++) {
+          const int u = t[k], v = t[(k + 1) % 3];
+          int f = -1;
+          for (size_t q = 0; q < le.size(); q++)
+            if ((le[q][0] == u && le[q][1] == v) || (le[q][0] == v && le[q][1] == u)) { f = (int)q; break; }
+          if (f >= 0) done[f] = 1;
+          else if (le.size() < 160) { le.push_back({u, v}); done.push_back(0); }
+          else { ovf = true; op = true; }
+        }
+      }
+      int f = -1;
+      for (size_t q = 0; q < le.size(); q++)
+        if (!done[q]) { f = (int)q; break; }
+      if (f < 0) break;
+      done[f] = 1;
+      const int u = le[f][0], v = le[f][1];
+      const int d = wrap(u, v, -1);
+      if (d < 0 || !certify(u, v, d)) { op = true; continue; }
+      bool dup = false;
+      for (const auto& t : star) {
+        auto has = [&](int z) { return t[0] == z || t[1] == z || t[2] == z; };
+        if (has(u) && has(v) && has(d)) { dup = true; break; }
+      }
+      if (dup) continue;
+      if (star.size() == 96) { ovf = true; op = true; break; }
+      star.push_back({v, u, d});
+    }
+    if (ovf) {
+#pragma omp atomic write
+      overflow = true;
+    }
+    for (const auto& t : star) {
+      int v[4] = {i, t[0], t[1], t[2]};
+      sort4(v);
+      const Geo G = geo(C, v);
+      int owner = -1;
+      for (int k = 0; k < 4 && owner < 0; k++)
+        if (in_ball(G, G.P[k], h[v[k]], cutoff)) owner = v[k];
+      if (owner != i) continue;
+      const bool allb = type[v[0]] != 0 && type[v[1]] != 0 && type[v[2]] != 0 && type[v[3]] != 0;
+      if (allb) {
+        double n4[4][3], H[4], hmax, hsum;
+        const double ll = heights(G, n4, H, &hmax, &hsum);
+        if (std::sqrt(ll) * hmax > 10.0) { ndel[i]++; continue; }
+      }
+      if (out[i].size() == 4 * 96) {
+#pragma omp atomic write
+        overflow = true;
+        break;
+      }
+      out[i].insert(out[i].end(), v, v + 4);
+    }
+    open[i] = op;
+    tie[i] = degen;
+  }
+  if (overflow) return -1;
+  long long ntet = 0;
+  for (long long i = 0; i < n; i++) ntet += (long long)out[i].size() / 4;
+  if (tets && cap >= ntet) {
+    long long o = 0;
+    for (long long i = 0; i < n; i++)
+      for (int v : out[i]) tets[o++] = v;
+  }
+  if (Q) {
+    std::memset(Q, 0, sizeof(*Q));
+    Q->ntet = ntet;
+    Q->grid = g;
+    for (long long i = 0; i < n; i++) {
+      Q->nopen += open[i];
+      Q->ntie += tie[i];
+      Q->ndeleted += ndel[i];
+    }
+    double cosd[46], coss[4];
+    for (int k = 0; k <= 45; k++) cosd[k] = std::cos(4.0 * k * M_PI / 180.0);
+    for (int k = 0; k < 4; k++) coss[k] = std::cos(10.0 * (k + 1) * M_PI / 180.0);
+    double vmin = 1.e300, vmax = 0, emin = 1.e300, emax = 0, amin = 1.e300, amax = 0, rmin = 1.e300, rmax = 0;
+    double dmin = 1.e300, dmax = 0, vsum = 0, asum = 0, rsum = 0, dsum = 0;
+    const double tab[11] = {1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 10.0, 15.0, 25.0, 50.0, 100.0};
+    for (long long i = 0; i < n; i++)
+      for (size_t t = 0; t < out[i].size(); t += 4) {
+        const Geo G = geo(C, &out[i][t]);
+        double nn[4][3], H[4], hmax, hsum;
+        const double hi = heights(G, nn, H, &hmax, &hsum);
+        for (int k = 0; k < 4; k++)
+          for (int q = 0; q < 3; q++) nn[k][q] /= H[k];
+        double lo = 1.e300, e2[3];
+        for (int k = 0; k < 3; k++) lo = std::fmin(lo, dot(G.A[k], G.A[k]));
+        const int ea[3] = {1, 2, 0}, eb[3] = {0, 1, 2};
+        for (int k = 0; k < 3; k++) {
+          for (int q = 0; q < 3; q++) e2[q] = G.P[ea[k]][q] - G.P[eb[k]][q];
+          lo = std::fmin(lo, dot(e2, e2));
+        }
+        const double vol = std::fabs(G.det) / 6.0, aspect = std::sqrt(hi) * hmax, ratio = 3.0 * (1.0 / hsum) / G.rc;
+        vsum += vol; vmin = std::fmin(vmin, vol); vmax = std::fmax(vmax, vol);
+        emin = std::fmin(emin, lo); emax = std::fmax(emax, hi);
+        asum += aspect; amin = std::fmin(amin, aspect); amax = std::fmax(amax, aspect);
+        rsum += ratio; rmin = std::fmin(rmin, ratio); rmax = std::fmax(rmax, ratio);
+        int ai = 0;
+        while (ai < 11 && aspect > tab[ai]) ai++;
+        Q->aspect_hist[ai]++;
+        const double rq = std::floor(ratio / 0.02);
+        Q->radius_hist[rq >= 0.0 ? (rq < 55 ? (int)rq : 55) : 0]++;
+        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+        double cmax = -2.0, cmin = 2.0;
+        for (int k = 0; k < 6; k++) {
+          const double cs = std::fmin(1.0, std::fmax(-1.0, -dot(nn[pa[k]], nn[pb[k]])));
+          cmax = std::fmax(cmax, cs);
+          cmin = std::fmin(cmin, cs);
+          int b = 0;
+          while (b < 44 && cs <= cosd[b + 1]) b++;
+          Q->dihedral_hist[b]++;
+        }
+        for (int k = 0; k < 4; k++)
+          if (cmax > coss[k]) Q->nsmall_dihedral[k]++;
+        const double ds = std::acos(cmax) / M_PI * 180.0, db = std::acos(cmin) / M_PI * 180.0;
+        dmin = std::fmin(dmin, ds); dmax = std::fmax(dmax, db); dsum += ds;
+      }
+    if (ntet > 0) {
+      Q->total_volume = vsum; Q->min_volume = vmin; Q->max_volume = vmax;
+      Q->min_edge = std::sqrt(emin); Q->max_edge = std::sqrt(emax);
+      Q->min_aspect = amin; Q->max_aspect = amax; Q->avg_aspect = asum / ntet;
+      Q->min_radius_ratio = rmin; Q->max_radius_ratio = rmax; Q->avg_radius_ratio = rsum / ntet;
+      Q->min_dihedral = dmin; Q->max_dihedral = dmax; Q->avg_min_dihedral = dsum / ntet;
+    }
+  }
+  return ntet;
+}
+}

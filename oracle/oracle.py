@@ -109,6 +109,16 @@ class OrcTriQuality(C.Structure):
                 + [("hist", C.c_longlong * 45)])
 
 
+class OrcTetQuality(C.Structure):
+    _fields_ = ([(f, C.c_longlong) for f in ("ntet", "nopen", "ndeleted", "ntie")]
+                + [(f, C.c_double) for f in ("grid", "total_volume", "min_volume", "max_volume", "min_edge",
+                                             "max_edge", "min_aspect", "max_aspect", "avg_aspect",
+                                             "min_radius_ratio", "max_radius_ratio", "avg_radius_ratio",
+                                             "min_dihedral", "max_dihedral", "avg_min_dihedral")]
+                + [("nsmall_dihedral", C.c_longlong * 4), ("aspect_hist", C.c_longlong * 12),
+                   ("radius_hist", C.c_longlong * 56), ("dihedral_hist", C.c_longlong * 45)])
+
+
 _lib = None
 
 
@@ -158,6 +168,10 @@ def lib():
         L.orc_cut_cell.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_volume_mass.argtypes = [C.POINTER(OrcCtx), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_tetrahedralize.argtypes = [C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
+                                         C.POINTER(OrcTetQuality)]
+        L.orc_tetrahedralize.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -439,6 +453,11 @@ class Oracle:
         qd["hist"] = list(q.hist)
         return tris[:ntri], qd
 
+    def tetrahedralize(self, xyz, type_, h, off, nbr):
+        """3D tetrahedralisation + tet quality (row F3), id space; see tetrahedralize()."""
+        p = self.case.params
+        return tetrahedralize(xyz, type_, h, off, nbr, p["cutoff"], p["box_l"], p["box_r"])
+
     def get_scale(self, phi: float, curv: float = 0.0) -> float:
         return lib().orc_get_scale(C.byref(self.ctx), phi, curv)
 
@@ -503,3 +522,39 @@ def cvp(dim, box_l, box_r, xyz, vp_xyz, mass=None, max_iter=4000, error_toleranc
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+def tetrahedralize(xyz, type_, h, off, nbr, cutoff, box_l, box_r):
+    """Certified local Delaunay tets of the particles (the library's
+    construction for Graphmeshcls::Reconstruct_tets, graph_mesh.cpp:981-1100,
+    restated on the CPU) and their quality statistics
+    (Tet_quality_statistics, :1967-2400): (tets (m x 4, ascending ids),
+    quality dict).  Raises when a star exceeds the per-particle limits."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(type_, dtype=np.int32)
+    hh = np.ascontiguousarray(h, dtype=np.float64)
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    bl = np.ascontiguousarray([float(box_l[d]) if d < len(box_l) else 0.0 for d in range(3)])
+    br = np.ascontiguousarray([float(box_r[d]) if d < len(box_r) else 0.0 for d in range(3)])
+    n = len(xyz)
+    q = OrcTetQuality()
+    args = (n, _p(xyz), _p(t), _p(hh), _p(off), _p(nbr), float(cutoff), _p(bl), _p(br))
+    m = lib().orc_tetrahedralize(*args, None, 0, None)
+    if m < 0:
+        raise RuntimeError("a particle's star exceeds the per-particle limits")
+    tets = np.zeros((max(m, 1), 4), dtype=np.int32)
+    lib().orc_tetrahedralize(*args, _p(tets), m, C.byref(q))
+    qd = {f: getattr(q, f) for f, _ in OrcTetQuality._fields_}
+    for f in ("nsmall_dihedral", "aspect_hist", "radius_hist", "dihedral_hist"):
+        qd[f] = list(getattr(q, f))
+    return tets[:m], qd
+
+
+def snap(xyz, box_l, box_r):
+    """The tetrahedralisation's snapped positions: rint(x / g) g with g =
+    2^(e - 52), 2^(e - 1) above every |coordinate| of the domain (and 1)."""
+    m = max([1.0] + [abs(float(v)) for v in list(box_l) + list(box_r)])
+    e = int(np.frexp(m)[1]) + 1
+    g = np.ldexp(1.0, e - 52)
+    return np.rint(np.asarray(xyz, dtype=np.float64) / g) * g

@@ -1802,7 +1802,7 @@ __global__ void k_tap(KCtx c, Buf<R> b, Work<R> w, const int* __restrict__ slot_
 template <int D, class R>
 __global__ void k_export_tri(KCtx c, Buf<R> b, Work<R> w, double* __restrict__ xyz, int* __restrict__ type,
                              double* __restrict__ phi, int* __restrict__ rows, int* __restrict__ cnt, int rowcap,
-                             unsigned* flags) {
+                             unsigned* flags, double* __restrict__ hout, bool sort_rows) {
   using P = PosOps<D, R>;
   long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= c.n) return;
@@ -1812,11 +1812,16 @@ __global__ void k_export_tri(KCtx c, Buf<R> b, Work<R> w, double* __restrict__ x
   xyz[3 * k] = x[0]; xyz[3 * k + 1] = x[1]; xyz[3 * k + 2] = x[2];
   type[k] = b.meta[s] & 0xFF;
   phi[k] = (double)b.phi[s];
+  if (hout) hout[k] = (double)b.posh[s].w;
   int m = w.cnt[s];
   if (m > w.cap || m > rowcap) { atomicOr(flags, 4u); m = min(w.cap, rowcap); }
   cnt[k] = m;
   const int* src = w.nbl + nb_slot(s, 0, w.cap);
   int* dst = rows + k * rowcap;
+  if (!sort_rows) {
+    for (int q = 0; q < m; q++) dst[q] = b.id[nb_index(src[((q >> 3) << 8) + (q & 7)])];
+    return;
+  }
   for (int q = 0; q < m; q++) {  // insertion sort by id
     int v = b.id[nb_index(src[((q >> 3) << 8) + (q & 7)])];
     int p = q;
@@ -2261,11 +2266,11 @@ class Engine : public EngineBase {
   }
 
   int export_tri(double* d_xyz, int* d_type, double* d_phi, int* d_rows, int* d_cnt, int rowcap,
-                 unsigned* d_flags) override {
+                 unsigned* d_flags, double* d_h = nullptr, bool sort_rows = true) override {
     if (!n_) { err = "no particles"; return MRSPH_ERR_STATE; }
     if (!have_work_) { err = "no density phase has run"; return MRSPH_ERR_STATE; }
     k_export_tri<D, R><<<grid(n_), 256, 0, st_>>>(kc_, buf_[cur_], w_, d_xyz, d_type, d_phi, d_rows, d_cnt, rowcap,
-                                                   d_flags);
+                                                   d_flags, d_h, sort_rows);
     MR_CK(cudaGetLastError());
     return 0;
   }

@@ -43,9 +43,11 @@ class EngineBase {
   virtual int world_positions(double* d_out) = 0;
   // Triangulation inputs in particle-id order: FP64 positions (n x 3), type,
   // phi, neighbour rows of the last density phase (n x rowcap ids, ascending,
-  // spilled rows clamped with bit 4 set in *d_flags) and their counts.
+  // spilled rows clamped with bit 4 set in *d_flags) and their counts;
+  // d_h (optional) receives the smoothing lengths; sort_rows = false leaves
+  // each row in list order (for consumers whose result is order-independent).
   virtual int export_tri(double* d_xyz, int* d_type, double* d_phi, int* d_rows, int* d_cnt, int rowcap,
-                         unsigned* d_flags) = 0;
+                         unsigned* d_flags, double* d_h = nullptr, bool sort_rows = true) = 0;
   virtual int neighbor_capacity() const = 0;
   // Batched stepping: one step launched on the handle's stream without the
   // periodic capacity check; the step graphs built ahead of a timed region;

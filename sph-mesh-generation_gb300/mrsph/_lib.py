@@ -66,6 +66,16 @@ class TriQuality(C.Structure):
                 [("hist", C.c_longlong * 45)])
 
 
+class TetQuality(C.Structure):
+    _fields_ = ([(k, C.c_longlong) for k in ("ntet", "nopen", "ndeleted", "ntie")] +
+                [(k, C.c_double) for k in ("grid", "total_volume", "min_volume", "max_volume", "min_edge", "max_edge",
+                                           "min_aspect", "max_aspect", "avg_aspect", "min_radius_ratio",
+                                           "max_radius_ratio", "avg_radius_ratio", "min_dihedral", "max_dihedral",
+                                           "avg_min_dihedral")] +
+                [("nsmall_dihedral", C.c_longlong * 4), ("aspect_hist", C.c_longlong * 12),
+                 ("radius_hist", C.c_longlong * 56), ("dihedral_hist", C.c_longlong * 45)])
+
+
 class VolumeMassStats(C.Structure):
     _fields_ = ([(k, C.c_double) for k in ("total_mass", "total_mass_surface", "total_volume", "total_area")] +
                 [(k, C.c_longlong) for k in ("num_interface_cell", "num_particle_mesh", "num_particle_surface",
@@ -111,6 +121,8 @@ EXPORTS = {
                        C.c_int),
     "mrsph_triangulate": ([C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(TriQuality)],
                           C.c_int),
+    "mrsph_tetrahedralize": ([C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
+                              C.POINTER(TetQuality)], C.c_int),
     "mrsph_batch_create": ([C.c_void_p, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
     "mrsph_batch_destroy": ([C.c_void_p], C.c_int),
     "mrsph_batch_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_int),

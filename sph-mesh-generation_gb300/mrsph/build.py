@@ -27,6 +27,7 @@ SOURCES = {
     "mrsph_noalloc.cu": [],
     "mrsph_cvp.cu": ["-fmad=false"],
     "mrsph_tri.cu": ["-fmad=false"],
+    "mrsph_tet.cu": ["-fmad=false"],
     "mrsph_batch.cu": [],
     "mrsph_persist.cu": [],
 }

@@ -379,6 +379,27 @@ class SPHMeshGeneration:
         out["hist"] = np.array(q.hist[:], dtype=np.int64)
         return tris[: nt.value], out
 
+    def Reconstruct_tets(self):
+        """3D tet mesh of the current particles and its quality statistics
+        (Graphmeshcls::Reconstruct_tets, geometry_tools/graph_mesh.cpp:981-1100,
+        with the deletion rule of Check_whether_this_tet_should_be_delete,
+        :675-979; Tet_quality_statistics, :1967-2400): the Delaunay tets whose
+        circumsphere lies in the neighbour ball of one of their particles.
+        Returns (tets (ntet x 4 ascending ids), quality dict)."""
+        q = L.TetQuality()
+        nt = C.c_longlong(0)
+        tets = np.zeros((8 * max(self.n, 1), 4), dtype=np.int32)
+        L.check(self.lib.mrsph_tetrahedralize(self.h, _ptr(tets), len(tets), C.byref(nt), C.byref(q)), self.h,
+                "mrsph_tetrahedralize")
+        if nt.value > len(tets):
+            tets = np.zeros((nt.value, 4), dtype=np.int32)
+            L.check(self.lib.mrsph_tetrahedralize(self.h, _ptr(tets), len(tets), C.byref(nt), C.byref(q)), self.h,
+                    "mrsph_tetrahedralize")
+        out = {f: getattr(q, f) for f, _ in L.TetQuality._fields_}
+        for f in ("nsmall_dihedral", "aspect_hist", "radius_hist", "dihedral_hist"):
+            out[f] = np.array(getattr(q, f)[:], dtype=np.int64)
+        return tets[: nt.value], out
+
     def upload_positions(self, xyz: np.ndarray):
         L.check(self.lib.mrsph_upload_positions(self.h, _ptr(xyz)), self.h, "mrsph_upload_positions")
 
