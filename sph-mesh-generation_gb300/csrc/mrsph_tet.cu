@@ -374,13 +374,25 @@ __device__ int wrap(const TetIn& T, const int* S, int m, const Pt& pi, const Pt&
       hc = sphere_rel(pi, pa, pb, pd, c, &cn);
     }
   }
+  // shuffle reduction; a lane whose partner lies past the warp gets its own
+  // candidate back, which is never compared with itself
   for (int off = 16; off > 0; off >>= 1) {
     const int ob = __shfl_down_sync(kFull, best, off);
     const Pt po{__shfl_down_sync(kFull, pbest.x, off), __shfl_down_sync(kFull, pbest.y, off),
                 __shfl_down_sync(kFull, pbest.z, off)};
-    if (ob >= 0 && (best < 0 || s * insphere(pi, pa, pb, pbest, po, T.inv_g) > 0)) {
+    const float oc0 = __shfl_down_sync(kFull, c[0], off), oc1 = __shfl_down_sync(kFull, c[1], off);
+    const float oc2 = __shfl_down_sync(kFull, c[2], off), ocn = __shfl_down_sync(kFull, cn, off);
+    const bool ohc = __shfl_down_sync(kFull, (int)hc, off) != 0;
+    if (ob < 0 || ob == best) continue;
+    bool take = best < 0;
+    if (!take) {
+      const int pt = hc ? power_test(rel(po, pi), c, cn) : 0;
+      take = pt != 0 ? pt > 0 : s * insphere(pi, pa, pb, pbest, po, T.inv_g) > 0;
+    }
+    if (take) {
       best = ob;
       pbest = po;
+      c[0] = oc0; c[1] = oc1; c[2] = oc2; cn = ocn; hc = ohc;
     }
   }
   return __shfl_sync(kFull, best, 0);
