@@ -2882,8 +2882,10 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       Q->ndeleted += ndel[i];
     }
     double cosd[46], coss[4];
-    for (int k = 0; k <= 45; k++) cosd[k] = std::cos(4.0 * k * M_PI / 180.0);
-    for (int k = 0; k < 4; k++) coss[k] = std::cos(10.0 * (k + 1) * M_PI / 180.0);
+    // degrees as the reference converts them, with its PI (glbparam.h:186)
+    const double pi_ref = 3.1415926;
+    for (int k = 0; k <= 45; k++) cosd[k] = std::cos(4.0 * k * pi_ref / 180.0);
+    for (int k = 0; k < 4; k++) coss[k] = std::cos(10.0 * (k + 1) * pi_ref / 180.0);
     double vmin = 1.e300, vmax = 0, emin = 1.e300, emax = 0, amin = 1.e300, amax = 0, rmin = 1.e300, rmax = 0;
     double dmin = 1.e300, dmax = 0, vsum = 0, asum = 0, rsum = 0, dsum = 0;
     const double tab[11] = {1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 10.0, 15.0, 25.0, 50.0, 100.0};
@@ -2923,7 +2925,7 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
         }
         for (int k = 0; k < 4; k++)
           if (cmax > coss[k]) Q->nsmall_dihedral[k]++;
-        const double ds = std::acos(cmax) / M_PI * 180.0, db = std::acos(cmin) / M_PI * 180.0;
+        const double ds = std::acos(cmax) / pi_ref * 180.0, db = std::acos(cmin) / pi_ref * 180.0;
         dmin = std::fmin(dmin, ds); dmax = std::fmax(dmax, db); dsum += ds;
       }
     if (ntet > 0) {

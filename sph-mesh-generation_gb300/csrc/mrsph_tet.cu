@@ -655,6 +655,8 @@ struct TetQIn {
   unsigned long long* hist;  // aspect 12, radius 56, dihedral 45, small-dihedral 4
 };
 constexpr int kAspectBins = 12, kRadiusBins = 56, kDihedBins = 45;
+// degrees as the reference converts them: acos(x) / PI * 180 with its PI (glbparam.h:186)
+constexpr double kPiRef = 3.1415926;
 
 __device__ void tet_quality_one(const TetQIn& Q, long long t, TetStat& s) {
   Pt P[4];
@@ -727,7 +729,7 @@ __device__ void tet_quality_one(const TetQIn& Q, long long t, TetStat& s) {
   }
   for (int k = 0; k < 4; k++)
     if (cmax > Q.cos_small[k]) atomicAdd(&Q.hist[kAspectBins + kRadiusBins + kDihedBins + k], 1ull);
-  const double dsmall = acos(cmax) / M_PI * 180.0, dbig = acos(cmin) / M_PI * 180.0;
+  const double dsmall = acos(cmax) / kPiRef * 180.0, dbig = acos(cmin) / kPiRef * 180.0;
   s.dmin = fmin(s.dmin, dsmall);
   s.dmax = fmax(s.dmax, dbig);
   s.dsum += dsmall;
@@ -818,8 +820,8 @@ extern "C" int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, l
   long long ntet = 0;
   unsigned flags = 0;
   double cosv[50];
-  for (int k = 0; k <= kDihedBins; k++) cosv[k] = std::cos(4.0 * k * M_PI / 180.0);
-  for (int k = 0; k < 4; k++) cosv[46 + k] = std::cos(10.0 * (k + 1) * M_PI / 180.0);
+  for (int k = 0; k <= kDihedBins; k++) cosv[k] = std::cos(4.0 * k * kPiRef / 180.0);
+  for (int k = 0; k < 4; k++) cosv[46 + k] = std::cos(10.0 * (k + 1) * kPiRef / 180.0);
   if (!A((void**)&d_x, sizeof(double) * 3 * n) || !A((void**)&d_phi, sizeof(double) * n) ||
       !A((void**)&d_h, sizeof(double) * n) || !A((void**)&d_type, sizeof(int) * n) ||
       !A((void**)&d_rows, sizeof(int) * NC) || !A((void**)&d_cnt, sizeof(int) * n) ||

@@ -4,7 +4,7 @@
 //
 //   mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N]
 //               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]
-//               [--lset-restart] [--cvp K] [--cvp-iter M]
+//               [--lset-restart] [--cvp K] [--cvp-iter M] [--mesh]
 //   mrsph_relax --load-lset-restart PATH [--kernel NAME] [--h-over-dx X] [...]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
@@ -25,8 +25,10 @@
 // set of a rstfile/levelset.rst (one level, its characteristic points and
 // segments), seeded with Get_num_particles over the file's totals; --kernel
 // (hyperbolic, cubic, wendland, gaussian, quintic; default wendland) and
-// --h-over-dx (default 1.3) set the smoothing kernel and h / dx.  Exit status
-// 2 on an engine or file error.
+// --h-over-dx (default 1.3) set the smoothing kernel and h / dx.  --mesh
+// writes the mesh of the relaxed particles (Mesh_binary_writer: triangles in
+// 2D, tets in 3D, outdata/mesh_*) and, in 3D, adds the tet count and
+// quality to the JSON line.  Exit status 2 on an engine or file error.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -41,7 +43,7 @@ int main(int argc, char** argv) {
   double hdx = 1.3;
   int steps = -1, every = 0, cvp_k = 0, cvp_iter = 4000;
   long long n = -1;
-  bool count_only = false, cut_cell = false, vtu = false, lset = false, lset_rst = false;
+  bool count_only = false, cut_cell = false, vtu = false, lset = false, lset_rst = false, mesh = false;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     auto val = [&]() -> std::string {
@@ -65,12 +67,13 @@ int main(int argc, char** argv) {
     else if (s == "--cvp") cvp_k = std::atoi(val().c_str());
     else if (s == "--cvp-iter") cvp_iter = std::atoi(val().c_str());
     else if (s == "--load-lset-restart") rst = val();
+    else if (s == "--mesh") mesh = true;
     else if (s == "--kernel") kern = val();
     else if (s == "--h-over-dx") hdx = std::atof(val().c_str());
     else if (s == "--help" || s == "-h") {
       std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
                   "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n"
-                  "                   [--lset-restart] [--cvp K] [--cvp-iter M]\n"
+                  "                   [--lset-restart] [--cvp K] [--cvp-iter M] [--mesh]\n"
                   "       mrsph_relax --load-lset-restart PATH [--kernel NAME] [--h-over-dx X] [...]\n");
       return 0;
     } else {
@@ -149,6 +152,21 @@ int main(int argc, char** argv) {
         cvp += buf;
       }
       cvp += "]}";
+    }
+    if (mesh) {
+      const std::string od = (out.empty() ? std::string(".") : out) + "/outdata";
+      Mesh_binary_writer(od).Output_mesh(0, sim);
+      if (c.params.dim == 3) {
+        std::vector<int> tets;
+        const mrsph_tet_quality tq = sim.Reconstruct_tets(tets);
+        char buf[320];
+        std::snprintf(buf, sizeof(buf),
+                      ", \"tets\": {\"ntet\": %lld, \"nopen\": %lld, \"ndeleted\": %lld, \"total_volume\": %.17g, "
+                      "\"max_aspect\": %.17g, \"avg_aspect\": %.17g, \"min_dihedral\": %.17g}",
+                      tq.ntet, tq.nopen, tq.ndeleted, tq.total_volume, tq.max_aspect, tq.avg_aspect,
+                      tq.min_dihedral);
+        cvp += buf;
+      }
     }
     std::printf("{\"workload\": \"%s\", \"n_particles\": %lld, \"steps\": %d, \"device_ms\": %.6f, "
                 "\"particle_steps_per_s\": %.6e, \"dt\": %.17g, \"step\": %lld, \"flags\": %d%s}\n",

@@ -327,6 +327,19 @@ SPH_mesh_generation::SPH_mesh_generation(const Case& c, int device) : case_(c) {
   check(mrsph_set_levelset(h_, (int)lv.size(), lv.data()), "mrsph_set_levelset");
 }
 
+mrsph_tet_quality SPH_mesh_generation::Reconstruct_tets(std::vector<int>& tets) {
+  mrsph_tet_quality q{};
+  long long nt = 0;
+  tets.assign(4 * (size_t)std::max<long long>(8 * n_, 1), 0);
+  check(mrsph_tetrahedralize(h_, tets.data(), (long long)(tets.size() / 4), &nt, &q), "mrsph_tetrahedralize");
+  if (4 * nt > (long long)tets.size()) {
+    tets.assign(4 * (size_t)nt, 0);
+    check(mrsph_tetrahedralize(h_, tets.data(), nt, &nt, &q), "mrsph_tetrahedralize");
+  }
+  tets.resize(4 * (size_t)nt);
+  return q;
+}
+
 mrsph_cvp_result SPH_mesh_generation::Partitioning(std::vector<double>& vp, const mrsph_cvp_params& p,
                                                    std::vector<int>* labels, std::vector<double>* vp_mass) {
   if ((int)vp.size() != 3 * p.num_vp) throw Error(MRSPH_ERR_ARG, "Partitioning: vp must hold num_vp x 3 values");
@@ -578,6 +591,66 @@ std::string mesh_vtu(const ParticleFields& f, long long ntri, const int* tris) {
   return vtu_text(f.n, ntri, pd, cd, pts, cells);
 }
 
+std::string tet_mesh_vtu(const ParticleFields& f, long long ntet, const int* tets) {
+  std::vector<VtuArray> pd, pts;
+  particle_arrays(f, pd, pts);
+  // per-tet volume, aspect ratio (longest edge / smallest height), radius
+  // ratio (3 r_in / r_circ) and smallest dihedral angle (Tet_quality_statistics,
+  // graph_mesh.cpp:1967-2400)
+  std::vector<float> vol(ntet), aspect(ntet), ratio(ntet), mind(ntet);
+  std::vector<int> offs(ntet);
+  auto cross = [](const double* u, const double* v, double* w) {
+    w[0] = u[1] * v[2] - u[2] * v[1];
+    w[1] = u[2] * v[0] - u[0] * v[2];
+    w[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  auto dot = [](const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+  for (long long t = 0; t < ntet; t++) {
+    const double* P[4];
+    for (int k = 0; k < 4; k++) P[k] = f.xyz + 3 * (long long)tets[4 * t + k];
+    double A[3][3], N[4][3], H[4], c[3];
+    for (int k = 0; k < 3; k++)
+      for (int q = 0; q < 3; q++) A[k][q] = P[k][q] - P[3][q];
+    cross(A[1], A[2], N[0]);
+    cross(A[2], A[0], N[1]);
+    cross(A[0], A[1], N[2]);
+    const double det = dot(A[0], N[0]);
+    const double r[3] = {0.5 * dot(A[0], A[0]), 0.5 * dot(A[1], A[1]), 0.5 * dot(A[2], A[2])};
+    for (int q = 0; q < 3; q++) c[q] = (r[0] * N[0][q] + r[1] * N[1][q] + r[2] * N[2][q]) / det;
+    for (int k = 0; k < 3; k++)
+      for (int q = 0; q < 3; q++) N[k][q] /= det;
+    for (int q = 0; q < 3; q++) N[3][q] = -(N[0][q] + N[1][q] + N[2][q]);
+    double hsum = 0.0, hmax = 0.0, longest = 0.0, cmax = -2.0;
+    for (int k = 0; k < 4; k++) {
+      H[k] = std::sqrt(dot(N[k], N[k]));
+      hsum += H[k];
+      hmax = std::max(hmax, H[k]);
+    }
+    for (int a = 0; a < 4; a++)
+      for (int b = a + 1; b < 4; b++) {
+        const double e[3] = {P[a][0] - P[b][0], P[a][1] - P[b][1], P[a][2] - P[b][2]};
+        longest = std::max(longest, dot(e, e));
+        double ua[3], ub[3];
+        for (int q = 0; q < 3; q++) { ua[q] = N[a][q] / H[a]; ub[q] = N[b][q] / H[b]; }
+        cmax = std::max(cmax, -dot(ua, ub));
+      }
+    vol[t] = (float)(std::fabs(det) / 6.0);
+    aspect[t] = (float)(std::sqrt(longest) * hmax);
+    ratio[t] = (float)(3.0 / hsum / std::sqrt(dot(c, c)));
+    mind[t] = (float)(std::acos(std::min(std::max(cmax, -1.0), 1.0)) / PI_REF * 180.0);
+    offs[t] = (int)(4 * (t + 1));
+  }
+  std::vector<unsigned char> types(ntet, 10);  // VTK_TETRA
+  std::vector<VtuArray> cd = {{"vol", "Float32", 1, raw_of(vol.data(), ntet)},
+                              {"aspect", "Float32", 1, raw_of(aspect.data(), ntet)},
+                              {"radius_ratio", "Float32", 1, raw_of(ratio.data(), ntet)},
+                              {"mindihedangle", "Float32", 1, raw_of(mind.data(), ntet)}};
+  std::vector<VtuArray> cells = {{"connectivity", "Int32", 0, raw_of(tets, 4 * ntet)},
+                                 {"offsets", "Int32", 0, raw_of(offs.data(), ntet)},
+                                 {"types", "UInt8", 0, raw_of(types.data(), ntet)}};
+  return vtu_text(f.n, ntet, pd, cd, pts, cells);
+}
+
 std::string particle_pvtu(const std::string& piece) {
   std::string t = "<VTKFile type=\"PUnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
                   " <PUnstructuredGrid GhostLevel=\"0\">\n  <PPointData>\n";
@@ -592,11 +665,14 @@ std::string particle_pvtu(const std::string& piece) {
   return t;
 }
 
-std::string mesh_pvtu(const std::string& piece) {
+std::string mesh_pvtu(const std::string& piece, bool tets) {
   std::string t = particle_pvtu(piece);  // the cell fields go between the point fields and the points
-  const std::string cells = "  <PCellData>\n    <PDataArray type=\"Float32\" Name=\"vol\" NumberOfComponents=\"1\"/>\n"
-                            "    <PDataArray type=\"Float32\" Name=\"aspect\" NumberOfComponents=\"1\"/>\n"
-                            "  </PCellData>\n";
+  std::string cells = "  <PCellData>\n    <PDataArray type=\"Float32\" Name=\"vol\" NumberOfComponents=\"1\"/>\n"
+                      "    <PDataArray type=\"Float32\" Name=\"aspect\" NumberOfComponents=\"1\"/>\n";
+  if (tets)
+    cells += "    <PDataArray type=\"Float32\" Name=\"radius_ratio\" NumberOfComponents=\"1\"/>\n"
+             "    <PDataArray type=\"Float32\" Name=\"mindihedangle\" NumberOfComponents=\"1\"/>\n";
+  cells += "  </PCellData>\n";
   t.insert(t.find("  <PPoints>"), cells);
   return t;
 }
@@ -941,6 +1017,35 @@ std::string Save_lset_restart(SPH_mesh_generation& sim, const std::string& path,
 
 std::string Mesh_binary_writer::Output_mesh(int n_out, SPH_mesh_generation& sim, long long run_time) {
   make_dir(outdir_);
+  if (sim.Get_case().params.dim == 3) {
+    std::vector<int> tets;
+    sim.Reconstruct_tets(tets);
+    std::vector<int> type, nn;
+    std::vector<double> h, norm;
+    sim.Particle_fields(type, h, norm, nn);
+    const std::vector<double> xyz = sim.Positions();
+    ParticleFields f;
+    f.n = sim.num_particles();
+    f.xyz = xyz.data();
+    f.type = type.data();
+    f.h = h.data();
+    f.nn = nn.data();
+    f.norm = norm.data();
+    const std::string piece = "mesh_tets_rank_0_step_" + std::to_string(n_out) + ".vtu";
+    const std::string pvtu = "mesh_tets_step_" + std::to_string(n_out) + ".pvtu";
+    {
+      std::ofstream o(outdir_ + "/" + piece, std::ios::binary | std::ios::trunc);
+      const std::string b = tet_mesh_vtu(f, (long long)(tets.size() / 4), tets.data());
+      o.write(b.data(), (std::streamsize)b.size());
+    }
+    {
+      std::ofstream o(outdir_ + "/" + pvtu, std::ios::trunc);
+      o << mesh_pvtu(piece, true);
+    }
+    const long long ts = run_time < 0 ? sim.Stats().step : run_time;
+    update_pvd(outdir_ + "/mesh_tets.pvd", n_out, std::to_string(ts), "./" + pvtu);
+    return outdir_ + "/" + piece;
+  }
   long long ntri = 0;
   int rc = mrsph_triangulate(sim.handle(), nullptr, 0, &ntri, nullptr);
   if (rc) throw Error(rc, "mrsph_triangulate");
@@ -968,7 +1073,7 @@ std::string Mesh_binary_writer::Output_mesh(int n_out, SPH_mesh_generation& sim,
   }
   {
     std::ofstream o(outdir_ + "/" + pvtu, std::ios::trunc);
-    o << mesh_pvtu(piece);
+    o << mesh_pvtu(piece, false);
   }
   const long long ts = run_time < 0 ? sim.Stats().step : run_time;
   update_pvd(outdir_ + "/mesh_tris.pvd", n_out, std::to_string(ts), "./" + pvtu);
@@ -1291,6 +1396,23 @@ extern "C" long long mrsph_host_lset_vti(const char* path, const int* ncell, con
   return o ? (long long)b.size() : -1;
 }
 
+// C entry for the writer tests: the tet-mesh VTU bytes of host arrays.
+extern "C" long long mrsph_host_tet_vtu(const char* path, long long n, const double* xyz, const int* type,
+                                        const double* h, const int* nn, const double* norm, long long ntet,
+                                        const int* tets) {
+  mrsph_host::ParticleFields f;
+  f.n = n;
+  f.xyz = xyz;
+  f.type = type;
+  f.h = h;
+  f.nn = nn;
+  f.norm = norm;
+  const std::string b = mrsph_host::tet_mesh_vtu(f, ntet, tets);
+  std::ofstream o(path, std::ios::binary | std::ios::trunc);
+  o.write(b.data(), (std::streamsize)b.size());
+  return o ? (long long)b.size() : -1;
+}
+
 // C entry for the writer tests: the triangle-mesh VTU bytes of host arrays.
 extern "C" long long mrsph_host_mesh_vtu(const char* path, long long n, const double* xyz, const int* type,
                                          const double* h, const int* nn, const double* norm, long long ntri,
@@ -1308,10 +1430,11 @@ extern "C" long long mrsph_host_mesh_vtu(const char* path, long long n, const do
   return o ? (long long)b.size() : -1;
 }
 
-// C entry for the writer tests: the particle (mesh = 0) or mesh (mesh = 1)
-// PVTU text for a piece name; returns its length (written when it fits).
+// C entry for the writer tests: the particle (mesh = 0), triangle-mesh
+// (mesh = 1) or tet-mesh (mesh = 2) PVTU text for a piece name; returns its
+// length (written when it fits).
 extern "C" long long mrsph_host_pvtu(int mesh, const char* piece, char* buf, long long len) {
-  const std::string t = mesh ? mrsph_host::mesh_pvtu(piece) : mrsph_host::particle_pvtu(piece);
+  const std::string t = mesh ? mrsph_host::mesh_pvtu(piece, mesh == 2) : mrsph_host::particle_pvtu(piece);
   if (buf && len > (long long)t.size()) std::memcpy(buf, t.c_str(), t.size() + 1);
   return (long long)t.size();
 }

@@ -144,6 +144,11 @@ class SPH_mesh_generation {
                                                             std::vector<double>* vp_mass = nullptr,
                                                             std::vector<double>* ghosts = nullptr);
 
+  // The tet mesh of the current particles (3D): Graphmeshcls::Reconstruct_tets
+  // (geometry_tools/graph_mesh.cpp:981-1100) with Tet_quality_statistics
+  // (:1967-2400) over mrsph_tetrahedralize; tets receives 4 ascending ids per tet.
+  mrsph_tet_quality Reconstruct_tets(std::vector<int>& tets);
+
   long long num_particles() const { return n_; }
   mrsph_handle* handle() { return h_; }
   const Case& Get_case() const { return case_; }
@@ -210,8 +215,12 @@ std::string particle_vtu(const ParticleFields& f);
 // mesh: the particle point fields, one triangle cell per triangle and the
 // cell fields 'vol' (area) and 'aspect' (longest / shortest edge).
 std::string mesh_vtu(const ParticleFields& f, long long ntri, const int* tris);
+// Its 3D branch (mesh_binary_writer.cpp:392-640): one VTK_TETRA cell per tet
+// and the cell fields 'vol', 'aspect' (longest edge / smallest height),
+// 'radius_ratio' (3 r_in / r_circ) and 'mindihedangle' (degrees).
+std::string tet_mesh_vtu(const ParticleFields& f, long long ntet, const int* tets);
 std::string particle_pvtu(const std::string& piece);
-std::string mesh_pvtu(const std::string& piece);
+std::string mesh_pvtu(const std::string& piece, bool tets = false);
 // Rewrites outdir/<name>.pvd with one DataSet entry per output so far
 // (Output_pvd_file, particle_binary_writer.cpp:53-93); n_out = 0 starts it.
 void update_pvd(const std::string& path, int n_out, const std::string& timestep, const std::string& dataset);
@@ -267,9 +276,11 @@ Case case_from_lset_restart(const LsetRestart& r, int kernel = MRSPH_KERNEL_WEND
 class Mesh_binary_writer {
  public:
   explicit Mesh_binary_writer(const std::string& outdir = "outdata") : outdir_(outdir) {}
-  // 2D only: triangulates the current particles (mrsph_triangulate) and
-  // writes outdir/mesh_tris_rank_0_step_<n>.vtu, mesh_tris_step_<n>.pvtu and
-  // mesh_tris.pvd.  Returns the piece's path.
+  // 2D: triangulates the current particles (mrsph_triangulate) and writes
+  // outdir/mesh_tris_rank_0_step_<n>.vtu, mesh_tris_step_<n>.pvtu and
+  // mesh_tris.pvd; 3D: tetrahedralises them (mrsph_tetrahedralize) and
+  // writes mesh_tets_rank_0_step_<n>.vtu, mesh_tets_step_<n>.pvtu and
+  // mesh_tets.pvd.  Returns the piece's path.
   std::string Output_mesh(int n_out, SPH_mesh_generation& sim, long long run_time = -1);
 
  private:

@@ -31,6 +31,8 @@ _VTK_TYPE = {np.dtype("<i4"): "Int32", np.dtype("<f4"): "Float32", np.dtype("<f8
 # Fields written per particle by default (Particle_binary_writer::Particle_binary_writer,
 # particle_binary_writer.cpp:12-30): id, local_id, type, h, NN, color, norm.
 PARTICLE_FIELDS_DEFAULT = ("id", "local_id", "type", "h", "NN", "color", "norm")
+# the reference's PI (glbparam.h:186), which its angle statistics divide by
+PI_REF = 3.1415926
 PARTICLE_FIELDS_ALL = ("id", "local_id", "type", "phi", "h", "scale", "curv", "NN", "color", "norm", "accel",
                        "vel", "timestep")
 
@@ -262,17 +264,47 @@ def triangle_quality(xyz: np.ndarray, tris: np.ndarray) -> Tuple[np.ndarray, np.
     return area, e.max(1) / e.min(1)
 
 
+def tet_quality(xyz: np.ndarray, tets: np.ndarray) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+    """Per-tet volume, aspect ratio (longest edge / smallest height), radius
+    ratio (3 r_in / r_circ) and smallest dihedral angle in degrees (with the
+    reference's PI, glbparam.h:186, as Tet_quality_statistics converts): the
+    'vol', 'aspect', 'radius_ratio' and 'mindihedangle' of
+    Tet_quality_statistics (geometry_tools/graph_mesh.cpp:1967-2400)."""
+    P = np.asarray(xyz, dtype=np.float64)[np.asarray(tets, dtype=np.int64)]  # (m, 4, 3)
+    A = P[:, :3] - P[:, 3:4]
+    n0, n1, n2 = np.cross(A[:, 1], A[:, 2]), np.cross(A[:, 2], A[:, 0]), np.cross(A[:, 0], A[:, 1])
+    det = np.einsum("ij,ij->i", A[:, 0], n0)
+    N = np.stack([n0, n1, n2], 1) / det[:, None, None]
+    N = np.concatenate([N, -N.sum(1, keepdims=True)], 1)
+    H = np.linalg.norm(N, axis=2)
+    r2 = 0.5 * np.einsum("ijk,ijk->ij", A, A)
+    c = (r2[:, 0:1] * n0 + r2[:, 1:2] * n1 + r2[:, 2:3] * n2) / det[:, None]
+    e = [P[:, a] - P[:, b] for a in range(4) for b in range(a + 1, 4)]
+    longest = np.sqrt(np.max([np.einsum("ij,ij->i", v, v) for v in e], axis=0))
+    u = N / H[:, :, None]
+    cosd = np.stack([-np.einsum("ij,ij->i", u[:, a], u[:, b]) for a in range(4) for b in range(a + 1, 4)], 1)
+    mind = np.arccos(np.clip(cosd.max(1), -1.0, 1.0)) / PI_REF * 180.0
+    return np.abs(det) / 6.0, longest * H.max(1), 3.0 / H.sum(1) / np.linalg.norm(c, axis=1), mind
+
+
 class MeshWriter:
-    """Mesh_binary_writer for the 2D triangle mesh: a VTU piece with one
-    triangle cell per triangle (point fields as for particles, cell fields
-    'vol' and 'aspect'), its PVTU and the mesh_tris.pvd collection."""
+    """Mesh_binary_writer (mesh_binary_writer.cpp:36-640): in 2D the
+    triangle mesh, a VTU piece with one triangle cell per triangle (point
+    fields as for particles, cell fields 'vol' and 'aspect'), its PVTU and
+    the mesh_tris.pvd collection; in 3D the tet mesh (VTK cell type 10, cell
+    fields 'vol', 'aspect', 'radius_ratio', 'mindihedangle'),
+    outdata/mesh_tets_rank_0_step_<n>.vtu, mesh_tets_step_<n>.pvtu and
+    mesh_tets.pvd."""
 
     def __init__(self, outdir: str = "outdata", fields: Sequence[str] = PARTICLE_FIELDS_DEFAULT):
         self.outdir = outdir
         self.fields = tuple(fields)
 
-    def Output_mesh(self, n_out: int, sim, tris: Optional[np.ndarray] = None, run_time: Optional[float] = None) -> str:
+    def Output_mesh(self, n_out: int, sim, tris: Optional[np.ndarray] = None, run_time: Optional[float] = None,
+                    tets: Optional[np.ndarray] = None) -> str:
         os.makedirs(self.outdir, exist_ok=True)
+        if sim.case.params.get("dim", 2) == 3:
+            return self._tets(n_out, sim, tets, run_time)
         if tris is None:
             tris, _ = sim.Reconstruct_tris()
         tris = np.asarray(tris, dtype="<i4").reshape(-1, 3)
@@ -288,6 +320,25 @@ class MeshWriter:
             f.write(_pvtu_text([piece], _fields_meta(pd), _fields_meta(cd)))
         t = sim.stats()["step"] if run_time is None else run_time
         update_pvd(os.path.join(self.outdir, "mesh_tris.pvd"), n_out, t, f"./{pvtu}")
+        return os.path.join(self.outdir, piece)
+
+    def _tets(self, n_out: int, sim, tets: Optional[np.ndarray], run_time: Optional[float]) -> str:
+        if tets is None:
+            tets, _ = sim.Reconstruct_tets()
+        tets = np.asarray(tets, dtype="<i4").reshape(-1, 4)
+        xyz = sim.particles(("xyz",))["xyz"]
+        pd = particle_point_data(sim, self.fields)
+        vol, aspect, ratio, mind = tet_quality(xyz, tets)
+        cd = [("vol", vol.astype("<f4")), ("aspect", aspect.astype("<f4")), ("radius_ratio", ratio.astype("<f4")),
+              ("mindihedangle", mind.astype("<f4"))]
+        piece = f"mesh_tets_rank_0_step_{n_out}.vtu"
+        with open(os.path.join(self.outdir, piece), "wb") as f:
+            f.write(vtu_bytes(xyz, tets, 10, pd, cd))
+        pvtu = f"mesh_tets_step_{n_out}.pvtu"
+        with open(os.path.join(self.outdir, pvtu), "w") as f:
+            f.write(_pvtu_text([piece], _fields_meta(pd), _fields_meta(cd)))
+        t = sim.stats()["step"] if run_time is None else run_time
+        update_pvd(os.path.join(self.outdir, "mesh_tets.pvd"), n_out, t, f"./{pvtu}")
         return os.path.join(self.outdir, piece)
 
 

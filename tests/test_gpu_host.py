@@ -190,3 +190,24 @@ def test_cpp_driver_restart_run_matches_python(tmp_path):
     cpp = io.read_pst(str(tmp_path / "b" / "rstfile_particles" / "step_300_rank_0.pst"))
     assert np.max(np.abs(cpp - gp["xyz"])) < 1e-12
     assert (gp["type"] == 2).any()
+
+
+def test_cpp_driver_writes_tet_mesh(tmp_path):
+    """--mesh in 3D: Mesh_binary_writer's tet branch writes
+    outdata/mesh_tets_rank_0_step_0.vtu (VTK_TETRA cells with 'vol',
+    'aspect', 'radius_ratio', 'mindihedangle') and the JSON line carries the
+    tet count and quality of SPH_mesh_generation::Reconstruct_tets."""
+    binary = build.build_host()
+    r = subprocess.run([binary, "--case", "box_3d", "--precision", "fp64", "--steps", "50", "--out", str(tmp_path),
+                        "--mesh"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout)
+    t = d["tets"]
+    assert t["ntet"] > 3 * d["n_particles"] and t["total_volume"] > 0 and t["max_aspect"] >= t["avg_aspect"] > 1
+    v = io.read_vtu(str(tmp_path / "outdata" / "mesh_tets_rank_0_step_0.vtu"))
+    assert len(v["types"]) == t["ntet"] and set(np.unique(v["types"])) == {10}
+    assert len(v["connectivity"]) == 4 * t["ntet"] and v["connectivity"].max() < d["n_particles"]
+    for k in ("vol", "aspect", "radius_ratio", "mindihedangle"):
+        assert np.all(np.isfinite(v[k])) and len(v[k]) == t["ntet"], k
+    assert abs(float(v["vol"].astype(np.float64).sum()) - t["total_volume"]) < 1e-5 * t["total_volume"]
+    assert (tmp_path / "outdata" / "mesh_tets.pvd").exists()

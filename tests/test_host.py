@@ -166,7 +166,43 @@ def test_cpp_mesh_vtu_matches_python_writer(binary, tmp_path):
     assert size == len(ref) and p.read_bytes() == ref
 
 
-@pytest.mark.parametrize("mesh", [0, 1])
+def test_cpp_tet_vtu_matches_python_writer(binary, tmp_path):
+    """The C++ tet-mesh VTU (the 3D branch of Mesh_binary_writer) equals the
+    Python writer's bytes for the same particles and tets (cell fields from
+    each side's own tet quality evaluation)."""
+    import ctypes
+    import numpy as np
+    from mrsph import io
+    lib = ctypes.CDLL(os.path.join(ROOT, "sph-mesh-generation_gb300", "libmrsph_host.so"))
+    f = lib.mrsph_host_tet_vtu
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p, ctypes.c_longlong] + [ctypes.c_void_p] * 5 + [ctypes.c_longlong, ctypes.c_void_p]
+    rng = np.random.default_rng(10)
+    n, m = 300, 600
+    xyz = rng.random((n, 3))
+    typ = rng.integers(0, 3, n).astype(np.int32)
+    h = rng.random(n)
+    nn = rng.integers(1, 60, n).astype(np.int32)
+    nrm = rng.normal(size=(n, 3))
+    tets = np.stack([rng.choice(n, 4, replace=False) for _ in range(m)]).astype(np.int32)
+    p = tmp_path / "t.vtu"
+    size = f(str(p).encode(), n, xyz.ctypes.data, typ.ctypes.data, h.ctypes.data, nn.ctypes.data, nrm.ctypes.data,
+             m, tets.ctypes.data)
+    pd = [("id", np.arange(n, dtype="<i4")), ("local_id", np.arange(n, dtype="<i4")), ("type", typ),
+          ("h", h.astype("<f4")), ("NN", nn), ("color", np.zeros(n, dtype="<i4")), ("norm", nrm.astype("<f4"))]
+    vol, aspect, ratio, mind = io.tet_quality(xyz, tets)
+    cd = [("vol", vol.astype("<f4")), ("aspect", aspect.astype("<f4")), ("radius_ratio", ratio.astype("<f4")),
+          ("mindihedangle", mind.astype("<f4"))]
+    ref = io.vtu_bytes(xyz, tets, 10, pd, cd)
+    got = p.read_bytes()
+    assert size == len(ref)
+    if got != ref:  # report which cell field differs
+        r, q = io.read_vtu(str(p)), io.read_vtu_bytes(ref) if hasattr(io, "read_vtu_bytes") else None
+        bad = [k for k, v in cd if not np.array_equal(r[k], v)]
+        raise AssertionError(f"tet VTU bytes differ; fields {bad}")
+
+
+@pytest.mark.parametrize("mesh", [0, 1, 2])
 def test_cpp_pvtu_matches_python(binary, mesh):
     import ctypes
     import numpy as np
@@ -181,6 +217,8 @@ def test_cpp_pvtu_matches_python(binary, mesh):
           ("h", np.zeros(1, "<f4")), ("NN", np.zeros(1, "<i4")), ("color", np.zeros(1, "<i4")),
           ("norm", np.zeros((1, 3), "<f4"))]
     cd = [("vol", np.zeros(1, "<f4")), ("aspect", np.zeros(1, "<f4"))] if mesh else []
+    if mesh == 2:
+        cd += [("radius_ratio", np.zeros(1, "<f4")), ("mindihedangle", np.zeros(1, "<f4"))]
     ref = io._pvtu_text(["piece_0.vtu"], io._fields_meta(pd), io._fields_meta(cd))
     assert n == len(ref) and buf.value.decode() == ref
 

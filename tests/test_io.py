@@ -124,6 +124,32 @@ def test_mesh_writer_and_quality(tmp_path):
     assert 'timestep="3"' in (tmp_path / "mesh_tris.pvd").read_text()
 
 
+def test_tet_mesh_writer_and_quality(tmp_path):
+    """The 3D branch of Mesh_binary_writer (mesh_binary_writer.cpp:392-640):
+    tet cells (VTK type 10) with 'vol', 'aspect', 'radius_ratio' and
+    'mindihedangle'; a regular tetrahedron has radius ratio 1, aspect
+    ratio sqrt(3/2) and dihedral angles arccos(1/3)."""
+    sim = FakeSim(n=5)
+    sim.case.params["dim"] = 3
+    s = 1.0 / np.sqrt(2.0)
+    sim.xyz = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1], [0, 0, -3]], dtype=np.float64) * s
+    tets = np.array([[0, 1, 2, 3], [1, 2, 3, 4]])
+    vol, aspect, ratio, mind = io.tet_quality(sim.xyz, tets)
+    edge = 2.0
+    assert np.isclose(vol[0], edge ** 3 / (6 * np.sqrt(2))) and np.isclose(ratio[0], 1.0)
+    assert np.isclose(aspect[0], np.sqrt(1.5)) and np.isclose(mind[0], np.arccos(1 / 3) / 3.1415926 * 180.0)
+    assert ratio[1] < 1.0 and aspect[1] > aspect[0]
+    f = io.MeshWriter(str(tmp_path)).Output_mesh(0, sim, tets=tets, run_time=4)
+    assert os.path.basename(f) == "mesh_tets_rank_0_step_0.vtu"
+    r = io.read_vtu(f)
+    assert np.array_equal(r["connectivity"], tets.reshape(-1)) and np.array_equal(r["types"], [10, 10])
+    assert np.array_equal(r["offsets"], [4, 8])
+    for k, v in (("vol", vol), ("aspect", aspect), ("radius_ratio", ratio), ("mindihedangle", mind)):
+        assert np.array_equal(r[k], v.astype(np.float32)), k
+    assert 'timestep="4"' in (tmp_path / "mesh_tets.pvd").read_text()
+    assert (tmp_path / "mesh_tets_step_0.pvtu").exists()
+
+
 def test_corner_average_and_levelset_writer(tmp_path):
     from mrsph import cases
     case = cases.disc_hole_2d(spacing=0.02, grid=64)

@@ -109,7 +109,8 @@ def test_oracle_tets_pinned_against_qhull(kind):
         a, n, det = _aspect(P)
         H = [np.linalg.norm(v) for v in n]
         u = [v / np.linalg.norm(v) for v in n]
-        ang = [np.degrees(np.arccos(np.clip(-np.dot(u[i], u[j]), -1, 1))) for i in range(4) for j in range(i + 1, 4)]
+        ang = [np.arccos(np.clip(-np.dot(u[i], u[j]), -1, 1)) / 3.1415926 * 180.0 for i in range(4)
+               for j in range(i + 1, 4)]
         vols.append(abs(det) / 6)
         asp.append(a)
         rr.append(3.0 / sum(H) / _circ(P)[1])
