@@ -2748,15 +2748,15 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       }
       return best;
     };
-    auto certify = [&](int a, int b, int d) {
+    // 0: a row particle inside or on the sphere (or coplanar); 1: none (a
+    // tet of the row's Delaunay tetrahedralisation); 2: also inside i's ball
+    // and not flat (certified)
+    auto status = [&](int a, int b, int d) {
       int v[4] = {i, a, b, d};
       sort4(v);
       const Geo G = geo(C, v);
-      if (!in_ball(G, xi, h[i], cutoff)) return false;
       const int o = orient(C, v[0], v[1], v[2], v[3]);
-      if (o == 0) return false;
-      // fails on a row particle inside or on the sphere; a tie when some lie
-      // on it and none inside
+      if (o == 0) return 0;
       bool inside = false, on = false;
       for (int q : S) {
         if (q == v[0] || q == v[1] || q == v[2] || q == v[3]) continue;
@@ -2766,9 +2766,9 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       }
       if (inside || on) {
         if (!inside) degen = true;
-        return false;
+        return 0;
       }
-      return true;
+      return in_ball(G, xi, h[i], cutoff) ? 2 : 1;
     };
     // nearest particle, then the smallest circumcircle through i and it
     int a = -1, c = -1;
@@ -2795,10 +2795,15 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       }
     }
     std::vector<std::array<int, 3>> star;
+    std::vector<char> cert;
     if (c >= 0) {
       for (int s = 1; s >= -1 && star.empty(); s -= 2) {
         const int d = wrap(a, c, s);
-        if (d >= 0 && certify(a, c, d)) star.push_back(s > 0 ? std::array<int, 3>{a, c, d} : std::array<int, 3>{c, a, d});
+        const int st = d >= 0 ? status(a, c, d) : 0;
+        if (st > 0) {
+          star.push_back(s > 0 ? std::array<int, 3>{a, c, d} : std::array<int, 3>{c, a, d});
+          cert.push_back(st == 2);
+        }
       }
     }
     bool op = star.empty(), ovf = false;
@@ -2826,7 +2831,8 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       done[f] = 1;
       const int u = le[f][0], v = le[f][1];
       const int d = wrap(u, v, -1);
-      if (d < 0 || !certify(u, v, d)) { op = true; continue; }
+      const int st = d >= 0 ? status(u, v, d) : 0;
+      if (st == 0) { op = true; continue; }
       bool dup = false;
       for (const auto& t : star) {
         auto has = [&](int z) { return t[0] == z || t[1] == z || t[2] == z; };
@@ -2835,12 +2841,15 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       if (dup) continue;
       if (star.size() == 96) { ovf = true; op = true; break; }
       star.push_back({v, u, d});
+      cert.push_back(st == 2);
     }
     if (ovf) {
 #pragma omp atomic write
       overflow = true;
     }
-    for (const auto& t : star) {
+    for (size_t k0 = 0; k0 < star.size(); k0++) {
+      if (!cert[k0]) continue;
+      const auto& t = star[k0];
       int v[4] = {i, t[0], t[1], t[2]};
       sort4(v);
       const Geo G = geo(C, v);

@@ -398,20 +398,22 @@ __device__ int wrap(const TetIn& T, const int* S, int m, const Pt& pi, const Pt&
   return __shfl_sync(kFull, best, 0);
 }
 
-// Certificate of tet (i, a, b, d) for particle i: inside i's ball, and no
-// row particle inside or on its sphere.  *degen is set when row particles
-// lie on the sphere and none inside it.  Warp-uniform result.
-__device__ bool certify(const TetIn& T, const int* S, int m, int i, int a, int b, int d, const double* xi,
-                        double hi, bool* degen, int lane) {
+// Status of tet (i, a, b, d) for particle i: 0 when a row particle lies
+// inside or on its sphere (or the four are coplanar), 1 when none does (a
+// tet of the row's Delaunay tetrahedralisation), 2 when moreover the sphere
+// lies inside i's ball and the tet is not flat (certified: a Delaunay tet
+// of all particles).  *degen is set when row particles lie on the sphere
+// and none inside it.  Warp-uniform result.
+__device__ int tet_status(const TetIn& T, const int* S, int m, int i, int a, int b, int d, const double* xi,
+                          double hi, bool* degen, int lane) {
   int v[4] = {i, a, b, d};
   sort4(v);
   Pt P[4];
   for (int k = 0; k < 4; k++) P[k] = load_pt(T, v[k]);
   TetGeo g;
   tet_geo(P, g);
-  if (!tet_in_ball(g, P, xi, hi, T.cutoff)) return false;
   const int o = orient3d(P[0], P[1], P[2], P[3], T.inv_g);
-  if (o == 0) return false;
+  if (o == 0) return 0;
   // the sphere's centre relative to i (the pre-test needs |det| >= 1e-3 of the edge product)
   const bool hc = fabs(g.det) >= 1.e-3 * g.vol_scale;
   float c[3];
@@ -437,9 +439,9 @@ __device__ bool certify(const TetIn& T, const int* S, int m, int i, int a, int b
   const bool any_in = __any_sync(kFull, inside), any_on = __any_sync(kFull, on);
   if (any_in || any_on) {
     if (!any_in) *degen = true;
-    return false;
+    return 0;
   }
-  return true;
+  return tet_in_ball(g, P, xi, hi, T.cutoff) ? 2 : 1;
 }
 
 constexpr int kStarWarps = 4;  // warps (particles) per block of k_tet_star
@@ -453,8 +455,10 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
   __shared__ int s_star[kStarWarps][kMaxStar][3];
   __shared__ int s_le[kStarWarps][kMaxLink][2];
   __shared__ unsigned char s_done[kStarWarps][kMaxLink];
+  __shared__ unsigned char s_cert[kStarWarps][kMaxStar];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int(*star)[3] = s_star[wib];
+  unsigned char* cert = s_cert[wib];
   int(*le)[2] = s_le[wib];
   unsigned char* ldone = s_done[wib];
   const long long nwarps = (long long)gridDim.x * kStarWarps;
@@ -515,11 +519,13 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
       const Pt pa = load_pt(T, a), pc = load_pt(T, c);
       for (int s = 1; s >= -1 && ns == 0; s -= 2) {
         const int d = wrap(T, S, m, pi, pa, pc, i, a, c, s, lane);
-        if (d >= 0 && certify(T, S, m, i, a, c, d, xi, hi, &degen, lane)) {
+        const int st = d >= 0 ? tet_status(T, S, m, i, a, c, d, xi, hi, &degen, lane) : 0;
+        if (st > 0) {
           if (lane == 0) {
             star[0][0] = s > 0 ? a : c;
             star[0][1] = s > 0 ? c : a;
             star[0][2] = d;
+            cert[0] = st == 2;
           }
           ns = 1;
         }
@@ -527,7 +533,9 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
     }
     __syncwarp();
     if (ns == 0) open = true;
-    // 3. breadth-first over the link: every tet (x, y, z) is stored with
+    // 3. breadth-first over the link, through every tet of the row's
+    // Delaunay tetrahedralisation around i (certified or not, so that the
+    // whole star is reached): every tet (x, y, z) is stored with
     // orient3d(i, x, y, z) > 0; its link edges (x, y), (y, z), (z, x) lead
     // to the tets across the faces (i, x, y) ...  (warp-uniform; lane 0 writes)
     int head = 0;
@@ -561,7 +569,8 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
       const Pt pu = load_pt(T, u), pv = load_pt(T, v);
       // the stored tet (u, v, w) has orient3d(i, u, v, w) > 0: wrap to the other side
       const int d = wrap(T, S, m, pi, pu, pv, i, u, v, -1, lane);
-      if (d < 0 || !certify(T, S, m, i, u, v, d, xi, hi, &degen, lane)) {
+      const int st = d >= 0 ? tet_status(T, S, m, i, u, v, d, xi, hi, &degen, lane) : 0;
+      if (st == 0) {
         open = true;
         continue;
       }
@@ -578,7 +587,7 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
         open = true;
         break;
       }
-      if (lane == 0) { star[ns][0] = v; star[ns][1] = u; star[ns][2] = d; }  // orient3d(i, v, u, d) > 0
+      if (lane == 0) { star[ns][0] = v; star[ns][1] = u; star[ns][2] = d; cert[ns] = st == 2; }  // orient3d(i, v, u, d) > 0
       ns++;
       __syncwarp();
     }
@@ -590,7 +599,7 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
       const int q = base + lane;
       bool emit = false, del = false;
       int v[4] = {0, 0, 0, 0};
-      if (q < ns) {
+      if (q < ns && cert[q]) {
         v[0] = i; v[1] = star[q][0]; v[2] = star[q][1]; v[3] = star[q][2];
         sort4(v);
         Pt P[4];

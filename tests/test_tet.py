@@ -128,3 +128,41 @@ def test_oracle_tets_pinned_against_qhull(kind):
     want = np.bincount(np.minimum(np.floor(np.array(dih) / 4.0).astype(int), 44), minlength=45)
     assert np.abs(np.array(q["dihedral_hist"]) - want).max() <= 1  # bin edges by cosine vs by angle
     assert q["nsmall_dihedral"] == [int(np.sum(np.array(dmin) < a)) for a in (10, 20, 30, 40)]
+
+
+def test_oracle_tets_on_relaxed_particles_pinned_against_qhull():
+    """The same pins on particles the oracle relaxed (a box whose corners
+    and edges are singularity points and segments, 30 steps, the oracle's
+    own neighbour rows): every tet is a qhull tet, none twice, and every
+    qhull tet whose circumsphere lies in one of its particles' balls is
+    found or dropped by the deletion rule."""
+    from mrsph import cases
+    case = cases.box_with_corners(dim=3, spacing=0.04, grid=32, kernel="hyperbolic", h_over_dx=1.0)
+    o = oracle.Oracle(case)
+    n = case.n_particles
+    o.alloc(n)
+    o.seed(n)
+    o.pre_run()
+    o.steps(30)
+    st = o.get_state()
+    xyz = np.stack([st["x"], st["y"], st["z"]], 1)
+    typ, h = st["type"].astype(np.int32), st["h"]
+    assert (typ == 1).any() and (typ == 3).any()
+    off, nb = o.neighbors()
+    p = case.params
+    tets, q = oracle.tetrahedralize(xyz, typ, h, off, nb, p["cutoff"], p["box_l"], p["box_r"])
+    xs = oracle.snap(xyz, p["box_l"], p["box_r"])
+    simp = np.sort(Delaunay(xs).simplices, axis=1)
+    qh = set(map(tuple, simp))
+    mine = set(map(tuple, tets))
+    assert len(mine) == len(tets) > 5 * n and mine <= qh
+    P = xs[simp]
+    A = P[:, :3] - P[:, 3:4]
+    c = P[:, 3] + np.linalg.solve(A, 0.5 * (A * A).sum(2)[..., None])[..., 0]
+    r = np.linalg.norm(c - P[:, 3], axis=1)
+    held = np.zeros(len(simp), bool)
+    for k in range(4):
+        held |= np.linalg.norm(c - P[:, k], axis=1) + r <= p["cutoff"] * h[simp[:, k]] * (1 - 1e-5)
+    missing = [tuple(t) for t in simp[held] if tuple(t) not in mine]
+    dropped = [t for t in missing if all(typ[v] != 0 for v in t) and _aspect(xs[list(t)])[0] > 10.0]
+    assert len(missing) == len(dropped) == q["ndeleted"] and q["ntie"] == 0
