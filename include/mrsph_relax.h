@@ -377,7 +377,7 @@ int mrsph_triangulate(mrsph_handle* h, int* tris, long long cap, long long* ntri
  * density phase (spilled rows: MRSPH_ERR_RANGE). */
 typedef struct {
   long long ntet;
-  long long nopen;     /* particles whose ring of certified tets does not close */
+  long long nopen;     /* particles on the hull of their neighbour row (their star does not close) */
   long long ndeleted;  /* tets dropped by the aspect-ratio rule */
   long long ntie;      /* particles that met five co-spherical particles */
   double grid;         /* the snapping grid */
