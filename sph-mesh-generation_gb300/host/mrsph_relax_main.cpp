@@ -5,7 +5,7 @@
 //   mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N]
 //               [--n N] [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]
 //               [--lset-restart] [--cvp K] [--cvp-iter M] [--mesh]
-//   mrsph_relax --load-lset-restart PATH [--kernel NAME] [--h-over-dx X] [...]
+//   mrsph_relax --load-lset-restart PATH [--retarget] [--kernel NAME] [--h-over-dx X] [...]
 //
 // Prints one line of JSON (workload, particles, steps, device milliseconds,
 // particle-steps/s, final time step).  --count-only prints the particle count
@@ -23,7 +23,10 @@
 // JSON line then carries the result and the final VPs.  --load-lset-restart
 // is the reference's restart run (Load_rst_case): the workload is the level
 // set of a rstfile/levelset.rst (one level, its characteristic points and
-// segments), seeded with Get_num_particles over the file's totals; --kernel
+// segments), seeded with Get_num_particles over the file's totals
+// (--retarget: the run that re-targets the spacing to 2, 5 and 16 level-set
+// cells, _READ_TARGET_FIELD_; seed with --cut-cell-count for the reference's
+// count of the recomputed totals); --kernel
 // (hyperbolic, cubic, wendland, gaussian, quintic; default wendland) and
 // --h-over-dx (default 1.3) set the smoothing kernel and h / dx.  --mesh
 // writes the mesh of the relaxed particles (Mesh_binary_writer: triangles in
@@ -44,6 +47,7 @@ int main(int argc, char** argv) {
   int steps = -1, every = 0, cvp_k = 0, cvp_iter = 4000;
   long long n = -1;
   bool count_only = false, cut_cell = false, vtu = false, lset = false, lset_rst = false, mesh = false;
+  bool retarget = false;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     auto val = [&]() -> std::string {
@@ -68,13 +72,14 @@ int main(int argc, char** argv) {
     else if (s == "--cvp-iter") cvp_iter = std::atoi(val().c_str());
     else if (s == "--load-lset-restart") rst = val();
     else if (s == "--mesh") mesh = true;
+    else if (s == "--retarget") retarget = true;
     else if (s == "--kernel") kern = val();
     else if (s == "--h-over-dx") hdx = std::atof(val().c_str());
     else if (s == "--help" || s == "-h") {
       std::printf("usage: mrsph_relax --case disc_hole_2d|torus_3d|box_2d|box_3d [--precision fp32|fp64] [--steps N] [--n N]\n"
                   "                   [--output-every K] [--out DIR] [--count-only] [--cut-cell-count] [--vtu] [--lset]\n"
                   "                   [--lset-restart] [--cvp K] [--cvp-iter M] [--mesh]\n"
-                  "       mrsph_relax --load-lset-restart PATH [--kernel NAME] [--h-over-dx X] [...]\n");
+                  "       mrsph_relax --load-lset-restart PATH [--retarget] [--kernel NAME] [--h-over-dx X] [...]\n");
       return 0;
     } else {
       std::fprintf(stderr, "unknown argument %s\n", s.c_str());
@@ -93,7 +98,8 @@ int main(int argc, char** argv) {
         return 1;
       }
       c = case_from_lset_restart(Load_lset_restart(rst), k, hdx,
-                                 prec == "fp64" ? MRSPH_FP64_PLAIN : MRSPH_FP32_SPLIT);
+                                 prec == "fp64" ? MRSPH_FP64_PLAIN : MRSPH_FP32_SPLIT, 0, 0,
+                                 retarget ? kRetargetFactors : nullptr);
     } else if (wl == "disc_hole_2d") c = disc_hole_2d(0.02, 64, MRSPH_KERNEL_WENDLAND, 1.3,
                                                prec == "fp32" ? MRSPH_FP32_SPLIT : MRSPH_FP64_PLAIN);
     else if (wl == "torus_3d") c = torus_3d(0.005, 0.02, MRSPH_KERNEL_WENDLAND, 1.3,

@@ -838,7 +838,7 @@ long long restart_num_particles(double total_mass, double total_mass_surface, do
 }
 
 Case case_from_lset_restart(const LsetRestart& r, int kernel, double h_over_dx, int precision,
-                            unsigned long long seed, int scale_law) {
+                            unsigned long long seed, int scale_law, const double* retarget) {
   const int dim = r.dim;
   Case c;
   c.name = "lset_restart";
@@ -847,6 +847,14 @@ Case case_from_lset_restart(const LsetRestart& r, int kernel, double h_over_dx, 
   p.precision = precision;
   p.min_dl = r.min_dl;
   p.max_dl = r.max_dl;
+  p.middle_dl = r.mid_dl;
+  if (retarget) {
+    double dl = 1.e300;
+    for (int d = 0; d < dim; d++) dl = std::min(dl, r.dcell[d]);
+    p.min_dl = retarget[0] * dl;
+    p.middle_dl = retarget[1] * dl;
+    p.max_dl = retarget[2] * dl;
+  }
   p.cell_ratio = 2.0 * h_over_dx;
   for (int d = 0; d < 3; d++) {
     p.box_l[d] = d < dim ? r.box_l[d] : 0.0;
@@ -854,8 +862,7 @@ Case case_from_lset_restart(const LsetRestart& r, int kernel, double h_over_dx, 
   }
   p.seed = seed;
   p.scale_law = scale_law;
-  p.middle_dl = r.mid_dl;
-  if (!cell_levels_consistent(p.box_l, p.box_r, dim, r.max_dl * p.cell_ratio, r.min_dl * p.cell_ratio))
+  if (!cell_levels_consistent(p.box_l, p.box_r, dim, p.max_dl * p.cell_ratio, p.min_dl * p.cell_ratio))
     throw Error(MRSPH_ERR_ARG, "the restart's domain and spacing give an inconsistent cell-list level plan "
                                "(sph.cpp:144-180); choose another h_over_dx");
   LevelGrid L;
@@ -889,8 +896,9 @@ Case case_from_lset_restart(const LsetRestart& r, int kernel, double h_over_dx, 
   c.params = p;
   c.singularities = r.sing;
   c.segments = r.seg;
-  c.n_particles = restart_num_particles(r.total_mass, r.total_mass_surface, r.total_mass_segment,
-                                        (int)(r.sing.size() / 3), r.num_interface_cell);
+  c.n_particles = retarget ? particle_count(c.levels, p)
+                           : restart_num_particles(r.total_mass, r.total_mass_surface, r.total_mass_segment,
+                                                   (int)(r.sing.size() / 3), r.num_interface_cell);
   c.steps = 200;
   return c;
 }
@@ -1486,17 +1494,18 @@ extern "C" long long mrsph_host_lset_restart(const char* path, const double* hd,
 
 // C entry for the loader tests: the case a level-set restart gives
 // (case_from_lset_restart), its phi incl. margins copied to phi (cap
-// values at most); prm receives min_dl, max_dl, middle_dl, cell_ratio,
+// values at most; retarget: the reference's re-targeting factors); prm
+// receives min_dl, max_dl, middle_dl, cell_ratio,
 // box_l[3], box_r[3]; cnt receives the particle count, the number of phi
 // values, the singularity and segment counts.  Returns 0, or -1 with the
 // message in err.
 extern "C" int mrsph_host_lset_case(const char* path, int kernel, double h_over_dx, int precision, int scale_law,
                                     double* phi, long long cap, double* prm, long long* cnt, char* err,
-                                    long long err_len) {
+                                    long long err_len, int retarget) {
   try {
     const mrsph_host::Case c =
         mrsph_host::case_from_lset_restart(mrsph_host::Load_lset_restart(path), kernel, h_over_dx, precision, 0,
-                                           scale_law);
+                                           scale_law, retarget ? mrsph_host::kRetargetFactors : nullptr);
     const std::vector<double>& f = c.levels[0].phi;
     if ((long long)f.size() <= cap) std::memcpy(phi, f.data(), f.size() * sizeof(double));
     const double v[] = {c.params.min_dl, c.params.max_dl, c.params.middle_dl, c.params.cell_ratio,

@@ -268,10 +268,17 @@ long long restart_num_particles(double total_mass, double total_mass_surface, do
 // phi.  The reference fills the margin packages from its analytic geometry;
 // here a margin cell holds the nearest interior cell's phi minus its
 // distance to that cell.  The count is restart_num_particles of the file's
-// totals.  Throws Error when the domain and spacing give an inconsistent
-// cell-list level plan.
+// totals.  retarget (3 factors, may be NULL; kRetargetFactors are the
+// reference's) is the restart run that re-targets the spacing
+// (_READ_TARGET_FIELD_, sph_mesh_generation.cpp:658-666): minimum, middle and
+// maximum spacing become the factors times the level's cell size
+// (level_set.cpp:939-941) and the count the spacing integral of the new law.
+// Throws Error when the domain and spacing give an inconsistent cell-list
+// level plan.
+constexpr double kRetargetFactors[3] = {2.0, 5.0, 16.0};
 Case case_from_lset_restart(const LsetRestart& r, int kernel = MRSPH_KERNEL_WENDLAND, double h_over_dx = 1.3,
-                            int precision = MRSPH_FP32_SPLIT, unsigned long long seed = 0, int scale_law = 0);
+                            int precision = MRSPH_FP32_SPLIT, unsigned long long seed = 0, int scale_law = 0,
+                            const double* retarget = nullptr);
 
 class Mesh_binary_writer {
  public:

@@ -18,7 +18,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
-from typing import Callable, List, Optional
+from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 
@@ -662,8 +662,14 @@ def restart_num_particles(total_mass: float, total_mass_surface: float, total_ma
     return mesh + surf + int(num_singularity) + seg
 
 
+# The factors of the reference's restart run that re-targets the spacing
+# (_READ_TARGET_FIELD_, sph_mesh_generation.cpp:658-666): minimum, middle and
+# maximum spacing in cells of the level set (level_set.cpp:939-941).
+RETARGET_FACTORS = (2.0, 5.0, 16.0)
+
+
 def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.3, precision: str = "fp32",
-                      seed: int = 0, scale_law: int = 0) -> Case:
+                      seed: int = 0, scale_law: int = 0, retarget: Optional[Sequence[float]] = None) -> Case:
     """A case from a level-set restart (rstfile/levelset.rst, the layout of
     Levelset::Save_lset_restart_file, level_set.cpp:1022-1094, read by
     Load_lset_restart_file, :1098-1175, and Load_level_set_rstfile,
@@ -676,7 +682,14 @@ def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.
     (Levelset::Initialize); here a margin cell takes the phi of the nearest
     interior cell minus its distance to that cell, i.e. a distance field
     continued outward.  The particle count is the reference's restart count,
-    Get_num_particles over the file's totals (restart_num_particles)."""
+    Get_num_particles over the file's totals (restart_num_particles).
+
+    retarget = (fac_min, fac_mid, fac_max) (RETARGET_FACTORS are the
+    reference's) is the restart run that re-targets the spacing: minimum,
+    middle and maximum spacing become the factors times the level's cell
+    size, and the count is the spacing integral of the new law;
+    Initialize_case(cut_cell_count=True) seeds Get_num_particles over the
+    recomputed cut-cell totals, as that run does."""
     from .io import load_lset_restart
     r = load_lset_restart(path)
     dim = int(r["dim"])
@@ -703,15 +716,21 @@ def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.
     lv = LevelGrid(box_l, dpkg, npkg, m, np.ascontiguousarray(phi), None)
     p = default_params(dim)
     cell_ratio = 2.0 * h_over_dx
-    min_dl, max_dl = float(r["minimum_dl"]), float(r["maximum_dl"])
+    min_dl, max_dl, mid_dl = float(r["minimum_dl"]), float(r["maximum_dl"]), float(r["middel_dl"])
+    if retarget is not None:
+        dl = min(dcell[d] for d in range(dim))
+        min_dl, mid_dl, max_dl = (float(f) * dl for f in retarget)
     if not cell_levels_consistent(box_l, box_r, dim, max_dl * cell_ratio, min_dl * cell_ratio):
         raise ValueError("the restart's domain and spacing give an inconsistent cell-list level plan "
                          "(sph.cpp:144-180); choose another h_over_dx")
     p.update(kernel=KERNELS[kernel], precision=PRECISIONS[precision], min_dl=min_dl, max_dl=max_dl,
              cell_ratio=cell_ratio, box_l=box_l, box_r=box_r, seed=seed, scale_law=scale_law,
-             middle_dl=float(r["middel_dl"]))
-    n = restart_num_particles(r["total_mass"], r["total_mass_surface"], r["total_mass_segment"],
-                              len(r["singularities"]), r["glbl_num_interface_cell"])
+             middle_dl=mid_dl)
+    if retarget is not None:
+        n = particle_count([lv], p)
+    else:
+        n = restart_num_particles(r["total_mass"], r["total_mass_surface"], r["total_mass_segment"],
+                                  len(r["singularities"]), r["glbl_num_interface_cell"])
     cs = Case("lset_restart", p, [lv], n)
     if len(r["singularities"]):
         cs.extra["singularities"] = np.asarray(r["singularities"])

@@ -247,14 +247,15 @@ def test_cpp_case_from_lset_restart_matches_python(binary, tmp_path, name):
     f = lib.mrsph_host_lset_case
     f.restype = ctypes.c_int
     f.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
-                  ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong]
+                  ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong,
+                  ctypes.c_int]
     import numpy as np
     phi = np.empty(py.levels[0].phi.size)
     prm = np.empty(10)
     cnt = np.empty(4, dtype=np.int64)
     err = ctypes.create_string_buffer(256)
     assert f(path.encode(), py.params["kernel"], hdx, 0, 0, phi.ctypes.data, len(phi), prm.ctypes.data,
-             cnt.ctypes.data, err, 256) == 0, err.value
+             cnt.ctypes.data, err, 256, 0) == 0, err.value
     assert cnt[1] == py.levels[0].phi.size
     assert np.array_equal(phi, py.levels[0].phi.ravel())
     p = py.params
@@ -268,6 +269,17 @@ def test_cpp_case_from_lset_restart_matches_python(binary, tmp_path, name):
     short = tmp_path / "short.rst"
     short.write_bytes(open(path, "rb").read()[:-8])
     assert f(str(short).encode(), 2, 1.3, 0, 0, phi.ctypes.data, len(phi), prm.ctypes.data, cnt.ctypes.data,
-             err, 256) == -1 and b"too short" in err.value
+             err, 256, 0) == -1 and b"too short" in err.value
+    # the re-targeting restart run: spacing 2, 5, 16 cells; count = spacing integral
+    rt = cases.from_lset_restart(path, kernel=kern, h_over_dx=hdx, retarget=cases.RETARGET_FACTORS)
+    assert f(path.encode(), py.params["kernel"], hdx, 0, 0, phi.ctypes.data, len(phi), prm.ctypes.data,
+             cnt.ctypes.data, err, 256, 1) == 0, err.value
+    dl = min(rt.levels[0].dpkg[d] / 4.0 for d in range(rt.params["dim"]))
+    assert list(prm[:3]) == [rt.params["min_dl"], rt.params["max_dl"], rt.params["middle_dl"]]
+    assert rt.params["min_dl"] == 2.0 * dl and rt.params["max_dl"] == 16.0 * dl
+    assert cnt[0] == rt.n_particles == cases.particle_count(rt.levels, rt.params)
+    d2 = json.loads(run(binary, "--load-lset-restart", path, "--retarget", "--kernel", kern, "--h-over-dx",
+                        str(hdx), "--count-only").stdout)
+    assert d2["n_particles"] == rt.n_particles
     r = run(binary, "--load-lset-restart", str(short), "--count-only")
     assert r.returncode == 2 and "too short" in r.stderr
