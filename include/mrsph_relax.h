@@ -394,7 +394,11 @@ typedef struct {
 
 /* tets (cap x 4 ints, ascending vertex ids per tet) may be NULL or too
  * small: *ntet is always set and tets is filled only when cap >= *ntet.
- * quality may be NULL.  3D handles only. */
+ * quality may be NULL.  3D handles only.  MRSPH_ERR_RANGE when a particle's
+ * star holds more than 96 tets or 160 link edges (about 27 and 40 on
+ * average), or when its neighbour row spilled.  The device work is
+ * synchronous; scratch (about 400 bytes per particle plus the neighbour
+ * rows) is allocated and freed by the call. */
 int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, long long* ntet, mrsph_tet_quality* quality);
 
 /* Batched relaxation of independent geometries (no counterpart in the
