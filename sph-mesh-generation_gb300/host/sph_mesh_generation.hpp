@@ -272,7 +272,8 @@ long long restart_num_particles(double total_mass, double total_mass_surface, do
 // reference's) is the restart run that re-targets the spacing
 // (_READ_TARGET_FIELD_, sph_mesh_generation.cpp:658-666): minimum, middle and
 // maximum spacing become the factors times the level's cell size
-// (level_set.cpp:939-941) and the count the spacing integral of the new law.
+// (level_set.cpp:939-941) and the count the spacing integral of the new law
+// (particle_count: the tanh law; with scale_law 1 seed the cut-cell count).
 // Throws Error when the domain and spacing give an inconsistent cell-list
 // level plan.
 constexpr double kRetargetFactors[3] = {2.0, 5.0, 16.0};

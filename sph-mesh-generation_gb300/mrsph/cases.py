@@ -710,9 +710,9 @@ def from_lset_restart(path: str, kernel: str = "wendland", h_over_dx: float = 1.
         c = np.clip(g, 0, inner.shape[a] - 1)
         idx.append(c)
         off.append((g - c) * (dcell[d] if d < dim else 0.0))
-    Z, Y, X = np.meshgrid(*idx, indexing="ij")
-    dz, dy, dx = np.meshgrid(*off, indexing="ij")
-    phi = inner[Z, Y, X] - np.sqrt(dx * dx + dy * dy + dz * dz)
+    # open-mesh gather and offsets (no full-size index arrays), summed in x, y, z order
+    dz, dy, dx = off[0][:, None, None], off[1][None, :, None], off[2][None, None, :]
+    phi = inner[np.ix_(*idx)] - np.sqrt(dx * dx + dy * dy + dz * dz)
     lv = LevelGrid(box_l, dpkg, npkg, m, np.ascontiguousarray(phi), None)
     p = default_params(dim)
     cell_ratio = 2.0 * h_over_dx
