@@ -390,13 +390,15 @@ typedef struct {
   long long aspect_hist[12];    /* bins up to 1.5, 2, 2.5, 3, 4, 6, 10, 15, 25, 50, 100, above */
   long long radius_hist[56];    /* radius ratio in bins of 0.02 (the last takes 1.1 and above) */
   long long dihedral_hist[45];  /* all six dihedral angles, 4-degree bins */
+  long long ntrunc;             /* particles whose star outgrew 128 tets or 224 link edges: their walk
+                                   stopped there, and tets they alone would have emitted are missing */
 } mrsph_tet_quality;
 
 /* tets (cap x 4 ints, ascending vertex ids per tet) may be NULL or too
  * small: *ntet is always set and tets is filled only when cap >= *ntet.
- * quality may be NULL.  3D handles only.  MRSPH_ERR_RANGE when a particle's
- * star holds more than 96 tets or 160 link edges (about 27 and 40 on
- * average), or when its neighbour row spilled.  The device work is
+ * quality may be NULL.  3D handles only.  MRSPH_ERR_RANGE when a neighbour
+ * row spilled.  A star is walked up to 128 tets and 224 link edges (about
+ * 27 and 40 on average; ntrunc counts stars cut there).  The device work is
  * synchronous; scratch (about 400 bytes per particle plus the neighbour
  * rows) is allocated and freed by the call. */
 int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, long long* ntet, mrsph_tet_quality* quality);

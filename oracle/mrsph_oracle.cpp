@@ -2702,13 +2702,14 @@ struct orc_tet_quality {
   double grid, total_volume, min_volume, max_volume, min_edge, max_edge, min_aspect, max_aspect, avg_aspect;
   double min_radius_ratio, max_radius_ratio, avg_radius_ratio, min_dihedral, max_dihedral, avg_min_dihedral;
   long long nsmall_dihedral[4], aspect_hist[12], radius_hist[56], dihedral_hist[45];
+  long long ntrunc;
 };
 
 // xyz (n x 3, FP64), type, h, neighbour rows (CSR off / nbr in id space,
 // self may be listed); box_l / box_r bound the coordinates.  Returns the tet
 // count (tets filled when cap allows; ascending ids per tet, in the order of
-// the emitting particle and its star), -1 when a star exceeds the library's
-// per-particle limits (96 tets, 160 link edges).
+// the emitting particle and its star).  A star stops its walk at the
+// library's per-particle limits (128 tets, 224 link edges; counted).
 long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type, const double* h,
                              const long long* off, const int* nbr, double cutoff, const double* box_l,
                              const double* box_r, int* tets, long long cap, orc_tet_quality* Q) {
@@ -2723,9 +2724,8 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
   for (size_t k = 0; k < X.size(); k++) X[k] = std::nearbyint(xyz_in[k] * ig) * g;
   const Ctx C{X.data(), ig};
   std::vector<std::vector<int>> out(n);
-  std::vector<int> open(n, 0), tie(n, 0);
+  std::vector<int> open(n, 0), tie(n, 0), trunc(n, 0);
   std::vector<long long> ndel(n, 0);
-  bool overflow = false;
 #pragma omp parallel for schedule(dynamic, 64)
   for (long long i64 = 0; i64 < n; i64++) {
     const int i = (int)i64;
@@ -2820,10 +2820,11 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
           for (size_t q = 0; q < le.size(); q++)
             if ((le[q][0] == u && le[q][1] == v) || (le[q][0] == v && le[q][1] == u)) { f = (int)q; break; }
           if (f >= 0) done[f] = 1;
-          else if (le.size() < 160) { le.push_back({u, v}); done.push_back(0); }
-          else { ovf = true; op = true; }
+          else if (le.size() < 224) { le.push_back({u, v}); done.push_back(0); }
+          else ovf = true;
         }
       }
+      if (ovf) break;
       int f = -1;
       for (size_t q = 0; q < le.size(); q++)
         if (!done[q]) { f = (int)q; break; }
@@ -2839,14 +2840,11 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
         if (has(u) && has(v) && has(d)) { dup = true; break; }
       }
       if (dup) continue;
-      if (star.size() == 96) { ovf = true; op = true; break; }
+      if (star.size() == 128) { ovf = true; break; }
       star.push_back({v, u, d});
       cert.push_back(st == 2);
     }
-    if (ovf) {
-#pragma omp atomic write
-      overflow = true;
-    }
+    trunc[i] = ovf;
     for (size_t k0 = 0; k0 < star.size(); k0++) {
       if (!cert[k0]) continue;
       const auto& t = star[k0];
@@ -2863,17 +2861,11 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
         const double ll = heights(G, n4, H, &hmax, &hsum);
         if (std::sqrt(ll) * hmax > 10.0) { ndel[i]++; continue; }
       }
-      if (out[i].size() == 4 * 96) {
-#pragma omp atomic write
-        overflow = true;
-        break;
-      }
       out[i].insert(out[i].end(), v, v + 4);
     }
     open[i] = op;
     tie[i] = degen;
   }
-  if (overflow) return -1;
   long long ntet = 0;
   for (long long i = 0; i < n; i++) ntet += (long long)out[i].size() / 4;
   if (tets && cap >= ntet) {
@@ -2889,6 +2881,7 @@ long long orc_tetrahedralize(long long n, const double* xyz_in, const int* type,
       Q->nopen += open[i];
       Q->ntie += tie[i];
       Q->ndeleted += ndel[i];
+      Q->ntrunc += trunc[i];
     }
     double cosd[46], coss[4];
     // degrees as the reference converts them, with its PI (glbparam.h:186)

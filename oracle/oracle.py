@@ -116,7 +116,8 @@ class OrcTetQuality(C.Structure):
                                              "min_radius_ratio", "max_radius_ratio", "avg_radius_ratio",
                                              "min_dihedral", "max_dihedral", "avg_min_dihedral")]
                 + [("nsmall_dihedral", C.c_longlong * 4), ("aspect_hist", C.c_longlong * 12),
-                   ("radius_hist", C.c_longlong * 56), ("dihedral_hist", C.c_longlong * 45)])
+                   ("radius_hist", C.c_longlong * 56), ("dihedral_hist", C.c_longlong * 45),
+                   ("ntrunc", C.c_longlong)])
 
 
 _lib = None
@@ -529,7 +530,7 @@ def tetrahedralize(xyz, type_, h, off, nbr, cutoff, box_l, box_r):
     construction for Graphmeshcls::Reconstruct_tets, graph_mesh.cpp:981-1100,
     restated on the CPU) and their quality statistics
     (Tet_quality_statistics, :1967-2400): (tets (m x 4, ascending ids),
-    quality dict).  Raises when a star exceeds the per-particle limits."""
+    quality dict)."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
     t = np.ascontiguousarray(type_, dtype=np.int32)
     hh = np.ascontiguousarray(h, dtype=np.float64)
@@ -541,8 +542,6 @@ def tetrahedralize(xyz, type_, h, off, nbr, cutoff, box_l, box_r):
     q = OrcTetQuality()
     args = (n, _p(xyz), _p(t), _p(hh), _p(off), _p(nbr), float(cutoff), _p(bl), _p(br))
     m = lib().orc_tetrahedralize(*args, None, 0, None)
-    if m < 0:
-        raise RuntimeError("a particle's star exceeds the per-particle limits")
     tets = np.zeros((max(m, 1), 4), dtype=np.int32)
     lib().orc_tetrahedralize(*args, _p(tets), m, C.byref(q))
     qd = {f: getattr(q, f) for f, _ in OrcTetQuality._fields_}

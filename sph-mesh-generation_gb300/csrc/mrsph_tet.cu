@@ -287,10 +287,11 @@ __device__ double tet_aspect(const TetGeo& g, const Pt* P) {
   return sqrt(longlen) * hmax;
 }
 
-constexpr int kMaxStar = 96;   // tets around one particle
-constexpr int kMaxLink = 160;  // link edges around one particle
+constexpr int kMaxStar = 128;  // tets around one particle
+constexpr int kMaxLink = 224;  // link edges around one particle
 constexpr int kMaxOut = kMaxStar;  // tets emitted by one particle (at most its star)
-// flags: 1 star overflow, 2 emit overflow, 4 spilled neighbour row
+// flags: 2 emit overflow, 4 spilled neighbour row (a star that outgrows
+// kMaxStar / kMaxLink stops its walk and is counted in stats[3])
 
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -448,7 +449,8 @@ constexpr int kStarWarps = 4;  // warps (particles) per block of k_tet_star
 
 // One warp per particle (grid-stride): its certified star, the tets it
 // emits (ascending ids, in star order) into out[i * kMaxOut ...], their
-// number into count[i].  stats: [0] open stars, [1] deleted tets, [2] ties.
+// number into count[i].  stats: [0] open stars, [1] deleted tets, [2] ties,
+// [3] stars cut at the per-particle limits.
 __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __restrict__ out,
                                                               int* __restrict__ count, unsigned long long* stats,
                                                               unsigned* flags) {
@@ -469,7 +471,7 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
     const Pt pi = load_pt(T, i);
     const double xi[3] = {pi.x, pi.y, pi.z};
     const double hi = T.h[i];
-    bool degen = false, open = false;
+    bool degen = false, open = false, trunc = false;
     int ns = 0, nl = 0;
     // 1. nearest neighbour a (ties: lower id) and the third point c of the
     // smallest circumcircle through i and a (ties: lower id)
@@ -552,12 +554,12 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
             if (lane == 0) { le[nl][0] = u; le[nl][1] = v; ldone[nl] = 0; }
             nl++;
           } else {
-            if (lane == 0) atomicOr(flags, 1u);
-            open = true;
+            trunc = true;
           }
           __syncwarp();
         }
       }
+      if (trunc) break;
       int f = -1;
       for (int q = 0; q < nl; q++)
         if (!ldone[q]) { f = q; break; }
@@ -583,8 +585,7 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
       }
       if (dup) continue;
       if (ns == kMaxStar) {
-        if (lane == 0) atomicOr(flags, 1u);
-        open = true;
+        trunc = true;
         break;
       }
       if (lane == 0) { star[ns][0] = v; star[ns][1] = u; star[ns][2] = d; cert[ns] = st == 2; }  // orient3d(i, v, u, d) > 0
@@ -631,6 +632,7 @@ __global__ void __launch_bounds__(32 * kStarWarps) k_tet_star(TetIn T, int* __re
       if (open) atomicAdd(&stats[0], 1ull);
       if (ndel) atomicAdd(&stats[1], ndel);
       if (degen) atomicAdd(&stats[2], 1ull);
+      if (trunc) atomicAdd(&stats[3], 1ull);
     }
     __syncwarp();
   }
@@ -822,7 +824,7 @@ extern "C" int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, l
   TetStat *d_part = nullptr, *d_tq = nullptr;
   const size_t NC = (size_t)n * rowcap;
   constexpr int kHist = kAspectBins + kRadiusBins + kDihedBins + 4;
-  unsigned long long st[3] = {0, 0, 0}, hist[kHist];
+  unsigned long long st[4] = {0, 0, 0, 0}, hist[kHist];
   std::memset(hist, 0, sizeof(hist));
   TetStat tq;
   std::memset(&tq, 0, sizeof(tq));
@@ -863,7 +865,6 @@ extern "C" int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, l
     if (cudaStreamSynchronize(s) != cudaSuccess) { rc = tfail(h, MRSPH_ERR_CUDA, "tetrahedralisation failed"); goto done; }
     ntet = (long long)tot + last;
     if (flags & 4u) { rc = tfail(h, MRSPH_ERR_RANGE, "neighbour list spilled; raise neighbor_cap"); goto done; }
-    if (flags & 1u) { rc = tfail(h, MRSPH_ERR_RANGE, "a particle's star holds more tets than the kernel keeps"); goto done; }
     if (flags & 2u) { rc = tfail(h, MRSPH_ERR_RANGE, "a particle emits more tets than the kernel keeps"); goto done; }
     if (ntet > 0) {
       if (!A((void**)&d_tets, sizeof(int) * 4 * ntet)) { rc = tfail(h, MRSPH_ERR_OOM, "cudaMalloc failed"); goto done; }
@@ -892,6 +893,7 @@ extern "C" int mrsph_tetrahedralize(mrsph_handle* h, int* tets, long long cap, l
     q->nopen = (long long)st[0];
     q->ndeleted = (long long)st[1];
     q->ntie = (long long)st[2];
+    q->ntrunc = (long long)st[3];
     q->grid = g;
     if (ntet > 0) {
       q->total_volume = tq.vol; q->min_volume = tq.vmin; q->max_volume = tq.vmax;

@@ -73,7 +73,7 @@ class TetQuality(C.Structure):
                                            "max_radius_ratio", "avg_radius_ratio", "min_dihedral", "max_dihedral",
                                            "avg_min_dihedral")] +
                 [("nsmall_dihedral", C.c_longlong * 4), ("aspect_hist", C.c_longlong * 12),
-                 ("radius_hist", C.c_longlong * 56), ("dihedral_hist", C.c_longlong * 45)])
+                 ("radius_hist", C.c_longlong * 56), ("dihedral_hist", C.c_longlong * 45), ("ntrunc", C.c_longlong)])
 
 
 class VolumeMassStats(C.Structure):

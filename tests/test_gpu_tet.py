@@ -36,7 +36,7 @@ def test_gpu_tets_match_oracle(name):
                                    case.params["box_l"], case.params["box_r"])
     assert len(tets) == q["ntet"] == len(ot) > 3 * len(p["xyz"])
     assert np.array_equal(tets, ot)
-    for k in ("ntet", "nopen", "ndeleted", "ntie"):
+    for k in ("ntet", "nopen", "ndeleted", "ntie", "ntrunc"):
         assert q[k] == oq[k], k
     for k in ("nsmall_dihedral", "aspect_hist", "radius_hist", "dihedral_hist"):
         assert list(q[k]) == list(oq[k]), k

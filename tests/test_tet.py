@@ -99,7 +99,7 @@ def test_oracle_tets_pinned_against_qhull(kind):
             if all(typ[v] != 0 for v in t) and _aspect(P)[0] > 10.0:
                 dropped += 1
     assert len(held - set(mine)) == dropped == q["ndeleted"]
-    assert q["ntie"] == 0 and q["ntet"] == len(mine) > 4 * len(x) // 2
+    assert q["ntie"] == 0 and q["ntrunc"] == 0 and q["ntet"] == len(mine) > 4 * len(x) // 2
     if kind == "ball":
         assert dropped > 0
     # quality statistics against numpy
@@ -165,4 +165,4 @@ def test_oracle_tets_on_relaxed_particles_pinned_against_qhull():
         held |= np.linalg.norm(c - P[:, k], axis=1) + r <= p["cutoff"] * h[simp[:, k]] * (1 - 1e-5)
     missing = [tuple(t) for t in simp[held] if tuple(t) not in mine]
     dropped = [t for t in missing if all(typ[v] != 0 for v in t) and _aspect(xs[list(t)])[0] > 10.0]
-    assert len(missing) == len(dropped) == q["ndeleted"] and q["ntie"] == 0
+    assert len(missing) == len(dropped) == q["ndeleted"] and q["ntie"] == 0 and q["ntrunc"] == 0
