@@ -27,6 +27,8 @@ def run(binary, *args):
 def test_help(binary):
     r = run(binary, "--help")
     assert r.returncode == 0 and "--case" in r.stdout
+    for flag in ("--load-lset-restart", "--retarget", "--mesh", "--lset-restart", "--cvp"):
+        assert flag in r.stdout, flag
     assert run(binary, "--bogus").returncode == 1
 
 
@@ -283,3 +285,25 @@ def test_cpp_case_from_lset_restart_matches_python(binary, tmp_path, name):
     assert d2["n_particles"] == rt.n_particles
     r = run(binary, "--load-lset-restart", str(short), "--count-only")
     assert r.returncode == 2 and "too short" in r.stderr
+
+
+def test_cpp_lset_restart_rejects_bad_headers(binary, tmp_path):
+    """Load_lset_restart refuses a file whose dimension is not 2 or 3 or that
+    holds more than one level (status 2 from the driver, with the reason)."""
+    import struct
+    import oracle
+    from mrsph import io
+    from test_io import _restart_sim
+    case = cases.disc_hole_2d(spacing=0.02, grid=64)
+    path = io.save_lset_restart(_restart_sim(case, oracle.Oracle(case)), str(tmp_path / "levelset.rst"))
+    raw = bytearray(open(path, "rb").read())
+    bad_dim = tmp_path / "dim.rst"
+    bad_dim.write_bytes(struct.pack("<i", 4) + bytes(raw[4:]))
+    r = run(binary, "--load-lset-restart", str(bad_dim), "--count-only")
+    assert r.returncode == 2 and "dimension" in r.stderr
+    lv = 4 + 18 * 8 + 8 * 4  # dim, domain/box/particle box, resolution, Lmin, Lmax, ini_num_cell
+    assert struct.unpack_from("<i", raw, lv)[0] == 1
+    two = tmp_path / "two.rst"
+    two.write_bytes(bytes(raw[:lv]) + struct.pack("<i", 2) + bytes(raw[lv + 4:]))
+    r = run(binary, "--load-lset-restart", str(two), "--count-only")
+    assert r.returncode == 2 and "one level" in r.stderr
