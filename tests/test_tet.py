@@ -166,3 +166,12 @@ def test_oracle_tets_on_relaxed_particles_pinned_against_qhull():
     missing = [tuple(t) for t in simp[held] if tuple(t) not in mine]
     dropped = [t for t in missing if all(typ[v] != 0 for v in t) and _aspect(xs[list(t)])[0] > 10.0]
     assert len(missing) == len(dropped) == q["ndeleted"] and q["ntie"] == 0 and q["ntrunc"] == 0
+    # the mesh writer's per-tet fields (io.tet_quality) against the quality pass
+    from mrsph import io
+    vol, asp, rr, mind = io.tet_quality(xs, tets)
+    assert np.isclose(vol.sum(), q["total_volume"], rtol=1e-12)
+    assert np.isclose(asp.max(), q["max_aspect"], rtol=1e-12) and np.isclose(asp.mean(), q["avg_aspect"], rtol=1e-12)
+    assert np.isclose(rr.min(), q["min_radius_ratio"], rtol=1e-12)
+    assert np.isclose(rr.mean(), q["avg_radius_ratio"], rtol=1e-12)
+    assert np.isclose(mind.min(), q["min_dihedral"], rtol=1e-12)
+    assert np.isclose(mind.mean(), q["avg_min_dihedral"], rtol=1e-12)
