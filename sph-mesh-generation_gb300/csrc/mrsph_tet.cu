@@ -5,15 +5,17 @@
 //   drops the tets Check_whether_this_tet_should_be_delete (:675-979) names:
 //   all four particles not REAL and aspect ratio above tet_delete_thres = 10
 //   (its phi tests are commented out).
-//     -> k_tet_star: local Delaunay stars.  Particle i gift-wraps the tets
-//        around itself over its neighbour row, which holds every particle
-//        within cutoff * h_i.  A tet is certified when its circumsphere lies
-//        inside that ball and no row particle lies inside or on it; then no
-//        particle at all does, so it is a Delaunay tet of the whole set and
-//        the unique one through its four particles.  Each certified tet is
-//        emitted once, by the lowest-id particle whose ball holds it.  Tets
-//        that no ball holds (across concavities of the body and on the
-//        convex hull, where TetGen keeps large tets) are not produced.
+//     -> k_tet_star: local Delaunay stars, one warp per particle.  Particle
+//        i gift-wraps the tets around itself over its neighbour row, which
+//        holds every particle within cutoff * h_i, walking its whole star in
+//        the row's Delaunay tetrahedralisation.  A tet is certified when its
+//        circumsphere lies inside that ball and no row particle lies inside
+//        or on it; then no particle at all does, so it is a Delaunay tet of
+//        the whole set and the unique one through its four particles.  Each
+//        certified tet is emitted once, by the lowest-id particle whose ball
+//        holds it.  Tets that no ball holds (across concavities of the body
+//        and on the convex hull, where TetGen keeps large tets) are not
+//        produced.
 //   Graphmeshcls::Tet_quality_statistics (:1967-2400) -> k_tet_quality: the
 //   volume, edge, aspect-ratio, radius-ratio and dihedral-angle statistics
 //   and histograms of the kept tets.
