@@ -400,3 +400,23 @@ def test_case_from_lset_restart(tmp_path, name):
     s1, s2 = orc.get_state(), o2.get_state()
     for k in s1:
         assert np.array_equal(s1[k], s2[k]), k
+
+
+def test_case_from_lset_restart_retarget_curvature_law(tmp_path):
+    """The re-targeting restart run under the curvature law: minimum, middle
+    and maximum spacing are 2, 5 and 16 level-set cells, and the count is the
+    spacing integral of that law (between the counts at the two bounds)."""
+    import oracle
+    case = cases.torus_3d(dx_min=0.03, dx_max=0.09, fine_pkg=32, nlevels=1)
+    orc = oracle.Oracle(case)
+    path = io.save_lset_restart(_restart_sim(case, orc), str(tmp_path / "levelset.rst"))
+    kern = {v: k for k, v in cases.KERNELS.items()}[case.params["kernel"]]
+    hdx = case.params["cell_ratio"] / 2
+    rt = cases.from_lset_restart(path, kernel=kern, h_over_dx=hdx, scale_law=1, retarget=cases.RETARGET_FACTORS)
+    dl = min(case.levels[0].dpkg[d] / 4.0 for d in range(3))
+    p = rt.params
+    assert (p["min_dl"], p["middle_dl"], p["max_dl"]) == (2.0 * dl, 5.0 * dl, 16.0 * dl) and p["scale_law"] == 1
+    assert rt.n_particles == cases.particle_count(rt.levels, p) > 0
+    lo = cases.particle_count(rt.levels, dict(p, scale_law=0, max_dl=p["min_dl"]))
+    hi = cases.particle_count(rt.levels, dict(p, scale_law=0, min_dl=p["max_dl"]))
+    assert hi < rt.n_particles < lo
